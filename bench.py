@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark of the formal-solve hot path: point.ray.freq solves per second.
+
+Workload (default): the 64^3 Cartesian grid cut to a sphere of radius half the box
+(rays of uneven length), 48 HEALPix rays (24 ray pairs), a 5-level linear rotor
+(4 lines) with nquads 31 (124 frequencies), temperature ~ r^-0.5 from 300 K, radial
+outflow 5-15 km/s plus 0.5 km/s noise; the split-precision solver.  A step is one
+second-order Feautrier formal solve over all points, ray pairs and frequencies
+(Model::compute_radiation_field_feautrier_order_2).
+
+Arms:
+  default           : this library on the GPU.  `value` = solves/s with the model
+                      resident in HBM (CUDA events on the solver's stream, L2 flushed
+                      between steps); `e2e` = the same through the public API
+                      core.Model.compute_radiation_field_feautrier_order_2 with a fresh
+                      host->device upload and the J/ALO read-back every step.
+  --impl reference  : the reference algorithm on the host cores (the CPU oracle port,
+                      all threads), on a bounded sample of the same workload.
+Under torchrun with N>1 every rank runs an independent replica (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "point.ray.freq solves/s"
+UNIT = "solves/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=64, help="grid points per side")
+    p.add_argument("--nside", type=int, default=2)
+    p.add_argument("--nquads", type=int, default=31)
+    p.add_argument("--precision", default="split", choices=["split", "fp64"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def workload(args):
+    from magritte_gb300 import synthetic
+    raw = synthetic.grid_sphere(n=args.n, nside=args.nside, nquads=args.nquads)
+    desc = (f"grid_sphere {args.n}^3 cutout r=box/2 ({raw.npoints} points), {raw.nrays} rays, "
+            f"5-level rotor (4 lines) x nquads {args.nquads}")
+    return raw, desc
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        dev = os.environ.get("LOCAL_RANK", "0")
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(raw, nthreads, rr_count=2, n_origins=40000):
+    """The oracle port of the reference CPU algorithm on a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    arrays = oracle.reference_setup(raw)
+    orc = oracle.Oracle(arrays)
+    n_o = min(n_origins, arrays["npoints"])
+    t0 = time.perf_counter()
+    orc.formal_solve_fo2_range(0, rr_count, 0, n_o, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    solves = n_o * rr_count * arrays["nfreqs"]
+    return {"value": solves / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"ray pairs 0-{rr_count - 1} x origins 0-{n_o - 1} ({solves} solves, {dt:.2f} s)"}
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    raw, desc = workload(args)
+    nthreads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    arrays = oracle.reference_setup(raw)
+    orc = oracle.Oracle(arrays)
+    rr_count, n_o = 1, min(40000, arrays["npoints"])
+    solves = n_o * rr_count * arrays["nfreqs"]
+    for _ in range(args.warmup):
+        orc.formal_solve_fo2_range(0, rr_count, 0, n_o, nthreads=nthreads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.formal_solve_fo2_range(0, rr_count, 0, n_o, nthreads=nthreads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = solves * args.steps / total
+    sample = f"ray pair 0 x origins 0-{n_o - 1} per step ({solves} solves)"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": desc, "precision": "reference FP64 (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, ws):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from magritte_gb300 import _abi, loader
+
+    raw, desc = workload(args)
+    model = loader.to_core(raw, precision=args.precision)
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    lib = _abi.load()
+    handle = C.c_void_p(model.upload())
+    prm = model.parameters
+    P, F, R, L = prm.npoints(), prm.nfreqs(), prm.hnrays(), prm.nlines()
+    prec = _abi.PRECISION[args.precision]
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.ExternalStream(lib.mgr_model_stream(handle), device=dev)
+    J = torch.empty((P, F), dtype=torch.float64, device=dev)
+    lam = torch.empty((P, L), dtype=torch.float64, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+
+    def step():
+        rc = lib.mgr_formal_solve_fo2_device(handle, prec, C.c_void_p(J.data_ptr()), None,
+                                             C.c_void_p(lam.data_ptr()))
+        if rc != 0:
+            raise RuntimeError(lib.mgr_last_error().decode())
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        stream.synchronize()
+        _abi._check(lib.mgr_sync(handle))
+
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        launches0 = _abi.launch_count()
+        clocks = Clocks()
+        barrier(ws)
+        torch.cuda.synchronize()
+        clocks.start()
+        t_wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        barrier(ws)
+        wall = time.perf_counter() - t_wall0
+        clk = clocks.stop()
+        launches = _abi.launch_count() - launches0
+        _abi._check(lib.mgr_sync(handle))
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    kernel_s = sum(step_ms) / 1000.0
+    kernel_s = max_over_ranks(kernel_s, ws)
+    solves = float(P) * R * F
+    value = ws * solves * args.steps / kernel_s
+
+    # work statistics for the algorithmic-bytes roofline
+    st_steps, st_nbr, st_elem = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    _abi._check(lib.mgr_ray_statistics(handle, C.byref(st_steps), C.byref(st_nbr), C.byref(st_elem)))
+    alg_bytes = 28.0 * (st_steps.value + st_nbr.value) + 52.0 * st_elem.value + 32.0 * solves
+    mean_launch_s = kernel_s / args.steps
+    achieved = alg_bytes / mean_launch_s / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = json.load(open(peaks_path))["hbm_gbs"]
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+
+    # accuracy of this precision against the FP64 path on the full workload
+    J_ref = torch.empty_like(J)
+    with torch.cuda.stream(stream):
+        rc = lib.mgr_formal_solve_fo2_device(handle, _abi.PRECISION["fp64"], C.c_void_p(J_ref.data_ptr()), None, None)
+        if rc != 0:
+            raise RuntimeError(lib.mgr_last_error().decode())
+        step()
+        stream.synchronize()
+    max_rel = float(((J - J_ref).abs() / J_ref.abs()).max().item())
+    # plain FP64 GPU throughput on the same workload (the comparison path)
+    fp64_ms = None
+    if args.precision != "fp64":
+        with torch.cuda.stream(stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            e0.record(stream)
+            rc = lib.mgr_formal_solve_fo2_device(handle, _abi.PRECISION["fp64"], C.c_void_p(J_ref.data_ptr()),
+                                                 None, None)
+            e1.record(stream)
+            stream.synchronize()
+        fp64_ms = e0.elapsed_time(e1)
+
+    # end to end through the public API: fresh upload, solve, read-back of J and the ALO
+    e2e = None
+    if not args.no_e2e:
+        prm.store_u = False
+        model.release_device()
+        model.compute_radiation_field_feautrier_order_2()  # warm the host paths
+        e2e_times = []
+        for _ in range(max(1, min(args.steps, 3))):
+            model.release_device()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            model.compute_radiation_field_feautrier_order_2()
+            e2e_times.append(time.perf_counter() - t0)
+        h2d = (P * 3 * 8 * 2 + len(raw.neighbors) * 4 + P * 4 * 3 + P * F * 8 + 4 * P * L * 8 + P * 8 * 3
+               + F * 4 * 4 + F)
+        d2h = P * F * 8 + P * L * 8
+        e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times), ws)
+        e2e = {"value": ws * solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s,
+               "path": "core.Model.compute_radiation_field_feautrier_order_2 (upload + solve + J/ALO read-back)"}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(raw, os.cpu_count() or 1)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * kernel_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if args.precision == "split" else "f64", "data": "synthetic",
+        "config": {"workload": desc, "npoints": P, "ray_pairs": R, "nfreqs": F, "precision": args.precision,
+                   "approx": "CloseLines", "solves_per_step": solves, "l2": "flushed between steps (512 MB write)",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "note": "FP64-pipe bound kernel; bytes per SURVEY 8(d) formula"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "wall_s_timed": wall,
+        "step_ms": step_ms,
+        "max_rel_err_J_vs_fp64_gpu": max_rel,
+        "fp64_gpu_solves_per_s": (solves / (fp64_ms / 1000.0)) if fp64_ms else None,
+        "speedup_vs_fp64_gpu": (fp64_ms / (1000.0 * kernel_s / args.steps)) if fp64_ms else None,
+        "work": {"trace_steps": st_steps.value, "neighbour_reads": st_nbr.value, "elements": st_elem.value},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, ws = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+    else:
+        run_ours(args, rank, ws)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

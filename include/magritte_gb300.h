@@ -1,0 +1,166 @@
+/*
+ * magritte_gb300 -- C ABI of the GB300 (sm_103a) formal-solve library libmgr_gpu.so.
+ *
+ * The entry points replace the bodies of Magritte's Model::compute_* methods on the
+ * formal-solve hot path (Magritte 0.9.3, src/model/model.hpp:58-80,
+ * src/model/model.cpp).  Everything is plain C: pointers, sizes, int status codes.
+ * Host arrays follow the reference's row-major layouts (index conventions noted per
+ * field).  All functions return MGR_OK (0) or a negative MgrStatus; the message of
+ * the last failure on the calling thread is available from mgr_last_error().
+ *
+ * Threading: one MgrModel is used by one host thread at a time.  Each MgrModel owns
+ * its CUDA stream and its device copies; host buffers stay with the caller.
+ */
+#ifndef MAGRITTE_GB300_H
+#define MAGRITTE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MGR_OK              = 0,
+    MGR_ERR_ARGUMENT    = -1, /* invalid argument or size                                 */
+    MGR_ERR_CUDA        = -2, /* CUDA runtime error (message has the CUDA error string)    */
+    MGR_ERR_NO_DEVICE   = -3, /* no CUDA device visible                                    */
+    MGR_ERR_TRACE       = -4, /* ray left the grid without meeting a boundary point        */
+    MGR_ERR_CAPACITY    = -5, /* ray longer than the configured capacity                   */
+    MGR_ERR_NONFINITE   = -6, /* non-finite optical depth or pivot detected in a solve     */
+    MGR_ERR_UNSUPPORTED = -7  /* option not implemented on this path                       */
+} MgrStatus;
+
+/* Line-sum approximation, Solver ApproximationType (src/solver/solver.hpp:9). */
+typedef enum { MGR_APPROX_NONE = 0, MGR_APPROX_ONELINE = 1, MGR_APPROX_CLOSELINES = 2 } MgrApprox;
+
+/* Arithmetic of the formal solve.
+ *  MGR_PRECISION_FP64  : the reference's arithmetic: FP64 storage with its
+ *                        single-precision libm calls (expf, erff, logf, powf).
+ *  MGR_PRECISION_SPLIT : profile, opacity, source and optical-depth arithmetic in
+ *                        FP32; the Feautrier elimination and back substitution in
+ *                        FP64.  Ray traces are identical in both modes.            */
+typedef enum { MGR_PRECISION_FP64 = 0, MGR_PRECISION_SPLIT = 1 } MgrPrecision;
+
+/* Boundary conditions (src/model/geometry/boundary/boundary.hpp:7). */
+typedef enum { MGR_BC_ZERO = 0, MGR_BC_THERMAL = 1, MGR_BC_CMB = 2 } MgrBoundaryCondition;
+
+/* Flat description of a Magritte Model after its set-up calls
+ * (compute_spectral_discretisation, compute_inverse_line_widths, level populations,
+ * set_dshift_max).  P = npoints, L = nlines, F = nfreqs, Q = nquads.
+ * Layouts: position/velocity [P][3] (velocity as v/c, points.hpp); CSR neighbour
+ * lists (points.hpp:15-17); emissivity/opacity/inverse_width/interp_criterion [P][L]
+ * (index l + p*L, lines.tpp:8-10); nu [P][F] (index f + p*F, radiation.tpp:3-5);
+ * ray_direction [nrays][3]; quad_* [nlspecs][Q]. */
+typedef struct {
+    uint32_t npoints, nrays, hnrays, nlines, nquads, nfreqs, nlspecs, nboundary;
+    const double*   position;
+    const double*   velocity;
+    const uint32_t* n_neighbors;
+    const uint32_t* cum_n_neighbors;
+    const uint32_t* neighbors;
+    const uint32_t* point2boundary;       /* npoints marks an interior point */
+    const int32_t*  boundary_condition;   /* [nboundary] MgrBoundaryCondition */
+    const double*   boundary_temperature; /* [nboundary] */
+    const double*   ray_direction;
+    const double*   ray_weight;           /* [nrays] */
+    const uint32_t* antipod;              /* [nrays] */
+    const double*   line;                 /* [L] line centre frequencies */
+    const double*   sorted_line;          /* [L] ascending */
+    const uint32_t* sorted_line_map;      /* [L] */
+    double          max_inverse_mass;
+    const double*   emissivity;
+    const double*   opacity;
+    const double*   inverse_width;
+    const double*   interp_criterion;     /* opacity / population_tot */
+    const double*   temperature;          /* [P] */
+    const double*   vturb2;               /* [P] */
+    const double*   dshift_max;           /* [P] */
+    const double*   nu;                   /* [P][F] */
+    const uint32_t* corr_line;            /* [F] global line of each frequency */
+    const uint32_t* corr_lspec;           /* [F] */
+    const uint32_t* corr_k;               /* [F] */
+    const uint32_t* corr_z;               /* [F] */
+    const uint8_t*  in_line_integral;     /* [F] */
+    const uint32_t* nrad;                 /* [nlspecs] */
+    const uint32_t* nrad_cum;             /* [nlspecs] */
+    const double*   line_A;               /* [L] */
+    const double*   lspec_inverse_mass;   /* [nlspecs] */
+    const double*   quad_weights;         /* [nlspecs][Q] */
+    const double*   quad_roots;           /* [nlspecs][Q] */
+    double min_opacity;
+    double min_dtau;
+    double max_interpolation_diff;
+    double max_distance_opacity_contribution;
+    int32_t approx;                       /* MgrApprox */
+} MgrModelDesc;
+
+typedef struct MgrModel MgrModel;
+
+/* Library / device state. */
+const char* mgr_last_error(void);
+int mgr_version(void);
+int mgr_device_count(int* count);
+
+/* Upload a model to the current CUDA device (host -> device copies, derived
+ * per-edge and per-point tables).  Replaces the Paracabs host->device mirroring
+ * (copy_vec_to_ptr) the reference's accelerated_for loops rely on. */
+int mgr_model_create(const MgrModelDesc* desc, MgrModel** out);
+void mgr_model_free(MgrModel* model);
+
+/* Replace the per-(point, line) line data after new level populations
+ * (Lines::set_emissivity_and_opacity, lines.tpp:29-40) or line widths
+ * (Lines::set_inverse_width, lines.tpp:45-59).  Any pointer may be NULL to keep
+ * the resident copy. */
+int mgr_model_set_line_data(MgrModel* model, const double* emissivity, const double* opacity,
+                            const double* inverse_width, const double* interp_criterion);
+
+/* Longest ray pair in elements, including interpolation points
+ * (Solver::get_ray_lengths_max, src/solver/solver.tpp:105-126). */
+int mgr_ray_lengths_max(MgrModel* model, uint32_t* length);
+
+/* Trace one ray pair (o, rr) for global line l, exactly as Solver::trace_ray_for_line
+ * lays it out (solver.tpp:773-800): elements first..last with the origin at index
+ * `centre` of the returned arrays (so centre = number of backward elements).
+ * Arrays have room for `capacity` elements; *n_tot receives the element count.
+ * dZ[i] is the distance between elements i and i+1. */
+int mgr_trace_ray_pair(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
+                       uint32_t* n_tot, uint32_t* centre, uint32_t* nr, uint32_t* nr_interp,
+                       double* interp_factor, double* shift, double* dZ);
+
+/* Model::compute_radiation_field_feautrier_order_2 (src/model/model.cpp:353-390 ->
+ * Solver::solve_feautrier_order_2, src/solver/solver.tpp:458-540), n_off_diag = 0.
+ * Host buffers (any may be NULL except J):
+ *   J            [P][F]           mean intensity  (radiation.J)
+ *   u            [hnrays][P][F]   Feautrier mean intensity per ray pair (radiation.u)
+ *   lambda_diag  [P][L]           summed diagonal ALO element (Lambda::Ls, lambda.tpp:79-89)
+ * The call blocks until the results are in host memory. */
+int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, double* lambda_diag);
+
+/* Device-resident variant: output pointers are device pointers; enqueued on the
+ * model's stream and not synchronised.  Any of u / lambda_diag may be NULL. */
+int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, double* u_dev,
+                                double* lambda_diag_dev);
+
+/* Work counted over one formal solve (all origins, all ray pairs): trace steps,
+ * neighbour records scanned by the trace (Geometry::get_next, geometry.tpp:22-38),
+ * and ray-pair elements including interpolation points summed over lines
+ * (the n_tot of solver.tpp:492-496 per line).  Used for algorithmic-byte counts. */
+int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_reads, uint64_t* elements);
+
+/* Block until all work on the model's stream has finished; returns the first
+ * kernel-side status recorded since the last call (trace / capacity / non-finite). */
+int mgr_sync(MgrModel* model);
+
+/* The model's CUDA stream (a cudaStream_t), for callers that time or order work. */
+void* mgr_model_stream(MgrModel* model);
+
+/* Number of this library's kernel launches so far (all models, all streams). */
+uint64_t mgr_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAGRITTE_GB300_H */

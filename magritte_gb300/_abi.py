@@ -1,0 +1,202 @@
+"""ctypes binding of libmgr_gpu.so (the C ABI declared in include/magritte_gb300.h).
+
+This is the thin Python view of the drop-in boundary: ``DeviceModel`` owns one
+``MgrModel`` and calls the formal-solve entry points with host numpy buffers.
+It fails loudly when the library is missing or no CUDA device is present; there
+is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libmgr_gpu.so")
+
+MGR_OK = 0
+PRECISION = {"fp64": 0, "split": 1}
+APPROX = {"None": 0, "OneLine": 1, "CloseLines": 2}
+
+_u32p = C.POINTER(C.c_uint32)
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+
+DESC_FIELDS = [
+    ("npoints", C.c_uint32), ("nrays", C.c_uint32), ("hnrays", C.c_uint32), ("nlines", C.c_uint32),
+    ("nquads", C.c_uint32), ("nfreqs", C.c_uint32), ("nlspecs", C.c_uint32), ("nboundary", C.c_uint32),
+    ("position", _f64p), ("velocity", _f64p), ("n_neighbors", _u32p), ("cum_n_neighbors", _u32p),
+    ("neighbors", _u32p), ("point2boundary", _u32p), ("boundary_condition", _i32p),
+    ("boundary_temperature", _f64p), ("ray_direction", _f64p), ("ray_weight", _f64p), ("antipod", _u32p),
+    ("line", _f64p), ("sorted_line", _f64p), ("sorted_line_map", _u32p), ("max_inverse_mass", C.c_double),
+    ("emissivity", _f64p), ("opacity", _f64p), ("inverse_width", _f64p), ("interp_criterion", _f64p),
+    ("temperature", _f64p), ("vturb2", _f64p), ("dshift_max", _f64p), ("nu", _f64p),
+    ("corr_line", _u32p), ("corr_lspec", _u32p), ("corr_k", _u32p), ("corr_z", _u32p),
+    ("in_line_integral", _u8p), ("nrad", _u32p), ("nrad_cum", _u32p), ("line_A", _f64p),
+    ("lspec_inverse_mass", _f64p), ("quad_weights", _f64p), ("quad_roots", _f64p),
+    ("min_opacity", C.c_double), ("min_dtau", C.c_double), ("max_interpolation_diff", C.c_double),
+    ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int32),
+]
+
+_PTR_TYPES = {_u32p: np.uint32, _i32p: np.int32, _f64p: np.float64, _u8p: np.uint8}
+
+
+class MgrModelDesc(C.Structure):
+    _fields_ = DESC_FIELDS
+
+
+# Every exported symbol of include/magritte_gb300.h with its ctypes signature.
+SIGNATURES = {
+    "mgr_last_error": (C.c_char_p, []),
+    "mgr_version": (C.c_int, []),
+    "mgr_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "mgr_model_create": (C.c_int, [C.POINTER(MgrModelDesc), C.POINTER(C.c_void_p)]),
+    "mgr_model_free": (None, [C.c_void_p]),
+    "mgr_model_set_line_data": (C.c_int, [C.c_void_p, _f64p, _f64p, _f64p, _f64p]),
+    "mgr_ray_lengths_max": (C.c_int, [C.c_void_p, _u32p]),
+    "mgr_trace_ray_pair": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _u32p, _u32p,
+                                     _u32p, _u32p, _f64p, _f64p, _f64p]),
+    "mgr_formal_solve_fo2": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p]),
+    "mgr_formal_solve_fo2_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                     C.POINTER(C.c_uint64)]),
+    "mgr_sync": (C.c_int, [C.c_void_p]),
+    "mgr_model_stream": (C.c_void_p, [C.c_void_p]),
+    "mgr_launch_count": (C.c_uint64, []),
+}
+
+_lib = None
+
+
+class MgrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"magritte_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def load():
+    """Load libmgr_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m magritte_gb300.build` first")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(rc):
+    if rc != MGR_OK:
+        raise MgrError(rc, load().mgr_last_error().decode())
+
+
+def _ptr(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def make_desc(arrays):
+    """MgrModelDesc over a dict of numpy arrays/scalars (keys = field names).
+    Returns (desc, keepalive list)."""
+    desc = MgrModelDesc()
+    keep = []
+    for name, typ in DESC_FIELDS:
+        v = arrays[name]
+        if typ in _PTR_TYPES:
+            a = np.ascontiguousarray(v, dtype=_PTR_TYPES[typ])
+            keep.append(a)
+            setattr(desc, name, _ptr(a, typ))
+        else:
+            setattr(desc, name, v)
+    return desc, keep
+
+
+class DeviceModel:
+    """A model resident on the GPU (mgr_model_create / mgr_model_free)."""
+
+    def __init__(self, arrays):
+        lib = load()
+        self.a = arrays
+        self.P = int(arrays["npoints"])
+        self.F = int(arrays["nfreqs"])
+        self.L = int(arrays["nlines"])
+        self.R = int(arrays["hnrays"])
+        desc, keep = make_desc(arrays)
+        h = C.c_void_p()
+        _check(lib.mgr_model_create(C.byref(desc), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mgr_model_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_line_data(self, emissivity=None, opacity=None, inverse_width=None, interp_criterion=None):
+        conv = lambda x: None if x is None else np.ascontiguousarray(x, np.float64)
+        e, o, i, c = conv(emissivity), conv(opacity), conv(inverse_width), conv(interp_criterion)
+        _check(load().mgr_model_set_line_data(self.h, _ptr(e, _f64p), _ptr(o, _f64p), _ptr(i, _f64p),
+                                              _ptr(c, _f64p)))
+
+    def ray_lengths_max(self):
+        n = C.c_uint32()
+        _check(load().mgr_ray_lengths_max(self.h, C.byref(n)))
+        return n.value
+
+    def trace(self, o, rr, l, capacity=4096):
+        nr = np.zeros(capacity, np.uint32)
+        ni = np.zeros(capacity, np.uint32)
+        fac = np.zeros(capacity)
+        sh = np.zeros(capacity)
+        dz = np.zeros(capacity)
+        n_tot = C.c_uint32()
+        centre = C.c_uint32()
+        _check(load().mgr_trace_ray_pair(self.h, o, rr, l, capacity, C.byref(n_tot), C.byref(centre),
+                                         _ptr(nr, _u32p), _ptr(ni, _u32p), _ptr(fac, _f64p), _ptr(sh, _f64p),
+                                         _ptr(dz, _f64p)))
+        n = n_tot.value
+        return dict(centre=centre.value, nr=nr[:n].copy(), nr_interp=ni[:n].copy(), interp_factor=fac[:n].copy(),
+                    shift=sh[:n].copy(), dZ=dz[:n - 1].copy())
+
+    def formal_solve_fo2(self, precision="fp64", want_u=False, want_lambda=True):
+        J = np.empty((self.P, self.F))
+        u = np.empty((self.R, self.P, self.F)) if want_u else None
+        lam = np.empty((self.P, self.L)) if want_lambda else None
+        _check(load().mgr_formal_solve_fo2(self.h, PRECISION[precision], _ptr(J, _f64p), _ptr(u, _f64p),
+                                           _ptr(lam, _f64p)))
+        return dict(J=J, u=u, lambda_diag=lam)
+
+    def formal_solve_fo2_device(self, precision, J_dev, u_dev=None, lam_dev=None):
+        """Enqueue on the model stream with device pointers (ints); no synchronisation."""
+        _check(load().mgr_formal_solve_fo2_device(self.h, PRECISION[precision], C.c_void_p(J_dev),
+                                                  C.c_void_p(u_dev) if u_dev else None,
+                                                  C.c_void_p(lam_dev) if lam_dev else None))
+
+    def ray_statistics(self):
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(load().mgr_ray_statistics(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return dict(steps=a.value, neighbor_reads=b.value, elements=c.value)
+
+    def sync(self):
+        _check(load().mgr_sync(self.h))
+
+    def stream(self):
+        return load().mgr_model_stream(self.h)
+
+
+def launch_count():
+    return int(load().mgr_launch_count())
+
+
+def device_count():
+    n = C.c_int()
+    rc = load().mgr_device_count(C.byref(n))
+    return n.value if rc == MGR_OK else 0

@@ -1,0 +1,549 @@
+// Host-side Model: set-up arithmetic and the C-ABI calls of the formal solve.
+// Compiled with -ffp-contract=off so every a*b+c rounds twice, as in the
+// reference's x86-64 build.
+#include "model.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+
+namespace mgrhost {
+
+static void check(int rc) {
+    if (rc != MGR_OK) throw std::runtime_error(std::string("magritte_gb300: ") + mgr_last_error());
+}
+
+Model::~Model() { release_device(); }
+
+void Model::release_device() {
+    if (dev_) {
+        mgr_model_free(dev_);
+        dev_ = nullptr;
+    }
+}
+
+uint64_t Model::launches() const { return mgr_launch_count(); }
+
+// ---------------------------------------------------------------------------------
+// prepare(): derived data that the reference computes in its read() methods.
+// ---------------------------------------------------------------------------------
+void Model::prepare() {
+    Parameters& prm = parameters;
+    const Size P = (Size)(geometry.points.position.shape.empty() ? 0 : geometry.points.position.shape[0]);
+    if (P == 0) throw std::runtime_error("Model::prepare: geometry.points.position is not set");
+    prm.npoints_.set(P, "npoints");
+
+    // Points::read (points.cpp:7-65): cumulative neighbour counts.
+    Points& pts = geometry.points;
+    if (pts.n_neighbors.size() != P) throw std::runtime_error("n_neighbors must have npoints entries");
+    if (pts.velocity.size() != 3 * (size_t)P) throw std::runtime_error("velocity must be [npoints][3]");
+    pts.cum_n_neighbors.resize({P});
+    size_t E = 0;
+    for (Size p = 0; p < P; p++) {
+        pts.cum_n_neighbors[p] = (Size)E;
+        E += pts.n_neighbors[p];
+    }
+    if (E != pts.neighbors.size()) throw std::runtime_error("neighbors length differs from sum(n_neighbors)");
+
+    // Rays::read (rays.cpp:5-66): hnrays and antipodes (tolerance 1e-9, last match wins).
+    Rays& rays = geometry.rays;
+    const Size nrays = (Size)(rays.direction.shape.empty() ? 0 : rays.direction.shape[0]);
+    if (nrays == 0 || rays.weight.size() != nrays) throw std::runtime_error("ray directions/weights not set");
+    prm.nrays_.set(nrays, "nrays");
+    prm.hnrays_.set(nrays / 2, "hnrays");
+    rays.antipod.resize({nrays});
+    for (Size r1 = 0; r1 < nrays; r1++) {
+        bool found = false;
+        for (Size r2 = 0; r2 < nrays; r2++) {
+            const double x = rays.direction[3 * r1] + rays.direction[3 * r2];
+            const double y = rays.direction[3 * r1 + 1] + rays.direction[3 * r2 + 1];
+            const double z = rays.direction[3 * r1 + 2] + rays.direction[3 * r2 + 2];
+            if (x * x + y * y + z * z < 1.0e-9) {
+                rays.antipod[r1] = r2;
+                found = true;
+            }
+        }
+        if (!found) throw std::runtime_error("ray without antipode: directions must come in opposite pairs");
+    }
+
+    // Boundary::read (boundary.cpp:5-48).
+    Boundary& bd = geometry.boundary;
+    const Size B = (Size)bd.boundary2point.size();
+    prm.nboundary_.set(B, "nboundary");
+    bd.point2boundary.resize({P});
+    for (Size p = 0; p < P; p++) bd.point2boundary[p] = P;
+    for (Size b = 0; b < B; b++) {
+        if (bd.boundary2point[b] >= P) throw std::runtime_error("boundary2point index out of range");
+        bd.point2boundary[bd.boundary2point[b]] = b;
+    }
+    if (bd.boundary_condition.size() != B) {
+        std::vector<int32_t> cmb(B, CMB);
+        bd.boundary_condition.assign({B}, cmb.data());
+    }
+    if (bd.boundary_temperature.size() != B) {
+        std::vector<double> t(B, T_CMB);
+        bd.boundary_temperature.assign({B}, t.data());
+    }
+
+    // Lines::read (lines.cpp:11-69) and the LAMDA-derived quantities
+    // (magritte/setup.py:766-770) when the user did not set them.
+    const Size nlspecs = (Size)lines.lineProducingSpecies.size();
+    if (nlspecs == 0) throw std::runtime_error("no line producing species");
+    prm.nlspecs_.set(nlspecs, "nlspecs");
+    lines.nrad_cum.resize({nlspecs});
+    Size L = 0;
+    lines.max_inverse_mass = 0.0;
+    for (Size l = 0; l < nlspecs; l++) {
+        LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        Linedata& ld = ls.linedata;
+        ld.nlev = (Size)ld.energy.size();
+        ld.nrad = (Size)ld.irad.size();
+        if (ld.weight.size() != ld.nlev || ld.jrad.size() != ld.nrad || ld.A.size() != ld.nrad)
+            throw std::runtime_error("inconsistent line data");
+        if (ld.frequency.size() != ld.nrad) {
+            ld.frequency.resize(ld.nrad);
+            for (Size k = 0; k < ld.nrad; k++) ld.frequency[k] = (ld.energy[ld.irad[k]] - ld.energy[ld.jrad[k]]) / HH;
+        }
+        if (ld.Bs.size() != ld.nrad || ld.Ba.size() != ld.nrad) {
+            ld.Bs.resize(ld.nrad);
+            ld.Ba.resize(ld.nrad);
+            for (Size k = 0; k < ld.nrad; k++) {
+                ld.Bs[k] = ld.A[k] * CC * CC / (2.0 * HH * std::pow(ld.frequency[k], 3));
+                ld.Ba[k] = ld.weight[ld.irad[k]] / ld.weight[ld.jrad[k]] * ld.Bs[k];
+            }
+        }
+        lines.nrad_cum[l] = L;
+        L += ld.nrad;
+        lines.max_inverse_mass = std::max(ld.inverse_mass, lines.max_inverse_mass);
+    }
+    prm.nlines_.set(L, "nlines");
+    if (lines.line.size() != L) {
+        lines.line.resize({L});
+        lines.sorted_line.resize({L});
+        lines.sorted_line_map.resize({L});
+    }
+    Size idx = 0;
+    for (auto& ls : lines.lineProducingSpecies)
+        for (Size k = 0; k < ls.linedata.nrad; k++) lines.line[idx++] = ls.linedata.frequency[k];
+    // heapsort in the reference (lines.cpp:59); a stable sort agrees for distinct lines
+    std::vector<Size> order(L);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](Size a, Size b) { return lines.line[a] < lines.line[b]; });
+    for (Size s = 0; s < L; s++) {
+        lines.sorted_line_map[s] = order[s];
+        lines.sorted_line[s] = lines.line[order[s]];
+    }
+    if (lines.emissivity.size() != (size_t)P * L) {
+        lines.emissivity.resize({P, L});
+        lines.opacity.resize({P, L});
+        lines.inverse_width.resize({P, L});
+    }
+
+    // chemistry: population_tot = abundance[p][num] (lineProducingSpecies.tpp:55)
+    const Array<double>& ab = chemistry.species.abundance;
+    if (ab.shape.size() != 2 || ab.shape[0] != P) throw std::runtime_error("abundance must be [npoints][nspecs]");
+    const Size nspecs = (Size)ab.shape[1];
+    prm.nspecs_.set(nspecs, "nspecs");
+    for (auto& ls : lines.lineProducingSpecies) {
+        if (ls.linedata.num >= nspecs) throw std::runtime_error("line species index outside the abundance table");
+        ls.population_tot.resize({P});
+        for (Size p = 0; p < P; p++) ls.population_tot[p] = ab[(size_t)p * nspecs + ls.linedata.num];
+        if (ls.population.size() != (size_t)P * ls.linedata.nlev) ls.population.resize({(size_t)P * ls.linedata.nlev});
+        if (ls.quadrature.roots.size() == 0) throw std::runtime_error("quadrature roots/weights not set");
+    }
+    const Size Q = (Size)lines.lineProducingSpecies[0].quadrature.roots.size();
+    prm.nquads_.set(Q, "nquads");
+    for (auto& ls : lines.lineProducingSpecies)
+        if (ls.quadrature.roots.size() != Q || ls.quadrature.weights.size() != Q)
+            throw std::runtime_error("every species needs nquads roots and weights");
+    if (thermodynamics.temperature.gas.size() != P || thermodynamics.turbulence.vturb2.size() != P)
+        throw std::runtime_error("temperature and turbulence must have npoints entries");
+}
+
+// ---------------------------------------------------------------------------------
+// Model::compute_inverse_line_widths -> Lines::set_inverse_width (lines.tpp:45-59)
+// ---------------------------------------------------------------------------------
+int Model::compute_inverse_line_widths() {
+    prepare();
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v;
+    const auto& T = thermodynamics.temperature.gas;
+    const auto& vt2 = thermodynamics.turbulence.vturb2;
+    for (Size p = 0; p < P; p++) {
+        for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+            const Linedata& ld = lines.lineProducingSpecies[l].linedata;
+            for (Size k = 0; k < ld.nrad; k++) {
+                const Size lid = lines.nrad_cum[l] + k;
+                const double width =
+                    ld.frequency[k] * std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * ld.inverse_mass * T[p] + vt2[p]);
+                lines.inverse_width[(size_t)p * L + lid] = (Real)1.0 / width;
+            }
+        }
+    }
+    lines.inverse_width.touch();
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Model::compute_spectral_discretisation (model.cpp:70-298)
+// ---------------------------------------------------------------------------------
+int Model::compute_spectral_discretisation() {
+    prepare();
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v, Q = parameters.nquads_.v;
+    const Size F = L * Q;
+    parameters.nfreqs_ = F;
+    Frequencies& fr = radiation.frequencies;
+    fr.nu.resize({P, F});
+    fr.corresponding_line.resize({F});
+    fr.corresponding_l_for_spec.resize({F});
+    fr.corresponding_k_for_tran.resize({F});
+    fr.corresponding_z_for_line.resize({F});
+    fr.appears_in_line_integral.resize({F});
+    const auto& T = thermodynamics.temperature.gas;
+    const auto& vt2 = thermodynamics.turbulence.vturb2;
+    for (Size p = 0; p < P; p++) {
+        Size index0 = 0, index1 = 0;
+        for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+            const LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+            const double inverse_mass = ls.linedata.inverse_mass;
+            for (Size k = 0; k < ls.linedata.nrad; k++) {
+                const double freqs_line = lines.line[index0];
+                const double width =
+                    freqs_line * std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * inverse_mass * T[p] + vt2[p]);
+                for (Size z = 0; z < Q; z++) {
+                    fr.nu[(size_t)p * F + index1] = freqs_line + width * ls.quadrature.roots[z];
+                    index1++;
+                }
+                index0++;
+            }
+        }
+    }
+    Size index2 = 0;
+    for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+        for (Size k = 0; k < lines.lineProducingSpecies[l].linedata.nrad; k++) {
+            for (Size z = 0; z < Q; z++) {
+                fr.appears_in_line_integral[index2] = 1;
+                fr.corresponding_l_for_spec[index2] = l;
+                fr.corresponding_k_for_tran[index2] = k;
+                fr.corresponding_z_for_line[index2] = z;
+                fr.corresponding_line[index2] = lines.nrad_cum[l] + k;
+                index2++;
+            }
+        }
+    }
+    spectralDiscretisation = SD_Lines;
+    return 0;
+}
+
+int Model::compute_spectral_discretisation(Real width) {
+    prepare();
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v, Q = parameters.nquads_.v;
+    const Size F = L * Q;
+    parameters.nfreqs_ = F;
+    Frequencies& fr = radiation.frequencies;
+    fr.nu.resize({P, F});
+    fr.corresponding_line.resize({F});
+    fr.corresponding_l_for_spec.resize({F});
+    fr.corresponding_k_for_tran.resize({F});
+    fr.corresponding_z_for_line.resize({F});
+    fr.appears_in_line_integral.resize({F});
+    for (Size p = 0; p < P; p++) {
+        Size index0 = 0, index1 = 0;
+        for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+            const LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+            for (Size k = 0; k < ls.linedata.nrad; k++) {
+                const double freqs_line = lines.line[index0];
+                for (Size z = 0; z < Q; z++) {
+                    fr.nu[(size_t)p * F + index1] = freqs_line + freqs_line * width * ls.quadrature.roots[z];
+                    index1++;
+                }
+                index0++;
+            }
+        }
+    }
+    Size index2 = 0;
+    for (Size l = 0; l < parameters.nlspecs_.v; l++)
+        for (Size k = 0; k < lines.lineProducingSpecies[l].linedata.nrad; k++)
+            for (Size z = 0; z < Q; z++) {
+                fr.appears_in_line_integral[index2] = 1;
+                fr.corresponding_l_for_spec[index2] = l;
+                fr.corresponding_k_for_tran[index2] = k;
+                fr.corresponding_z_for_line[index2] = z;
+                fr.corresponding_line[index2] = lines.nrad_cum[l] + k;
+                index2++;
+            }
+    spectralDiscretisation = SD_Image;
+    return 0;
+}
+
+int Model::compute_spectral_discretisation(Real nu_min, Real nu_max) {
+    prepare();
+    return compute_spectral_discretisation(nu_min, nu_max, parameters.nlines_.v * parameters.nquads_.v);
+}
+
+int Model::compute_spectral_discretisation(Real nu_min, Real nu_max, Size n_image_freqs) {
+    if (n_image_freqs < 1)
+        throw std::runtime_error("At least a single frequency is needed to compute a spectral discretization.");
+    prepare();
+    const Size P = parameters.npoints_.v;
+    parameters.nfreqs_ = n_image_freqs;
+    Frequencies& fr = radiation.frequencies;
+    fr.nu.resize({P, n_image_freqs});
+    fr.corresponding_line.resize({n_image_freqs});
+    fr.corresponding_l_for_spec.resize({n_image_freqs});
+    fr.corresponding_k_for_tran.resize({n_image_freqs});
+    fr.corresponding_z_for_line.resize({n_image_freqs});
+    fr.appears_in_line_integral.resize({n_image_freqs});
+    for (Size f = 0; f < n_image_freqs; f++) {
+        fr.appears_in_line_integral[f] = 0;
+        fr.corresponding_l_for_spec[f] = n_image_freqs;
+        fr.corresponding_k_for_tran[f] = n_image_freqs;
+        fr.corresponding_z_for_line[f] = n_image_freqs;
+        fr.corresponding_line[f] = 0;
+    }
+    if (n_image_freqs == 1) {
+        for (Size p = 0; p < P; p++) fr.nu[p] = (Real)(nu_min + nu_max) / 2.0;
+    } else {
+        const long double dnu = (nu_max - nu_min) / (n_image_freqs - 1);
+        for (Size p = 0; p < P; p++)
+            for (Size f = 0; f < n_image_freqs; f++)
+                fr.nu[(size_t)p * n_image_freqs + f] = (Real)(nu_min + f * dnu);
+    }
+    spectralDiscretisation = SD_Image;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------
+// LTE populations (lineProducingSpecies.tpp:52-75) and line emissivity/opacity
+// (lineProducingSpecies.tpp:23-44, lines.tpp:29-40).  Populations are double here
+// where the reference keeps long double.
+// ---------------------------------------------------------------------------------
+void Model::set_emissivity_and_opacity() {
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v;
+    for (Size p = 0; p < P; p++) {
+        for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+            const LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+            const Linedata& ld = ls.linedata;
+            for (Size k = 0; k < ld.nrad; k++) {
+                const Size lid = lines.nrad_cum[l] + k;
+                const Size i = ls.index(p, ld.irad[k]);
+                const Size j = ls.index(p, ld.jrad[k]);
+                const double freq = ld.frequency[k];
+                const double em = freq * HH_OVER_FOUR_PI * ld.A[k] * ls.population[i];
+                const double op = freq * HH_OVER_FOUR_PI * (ls.population[j] * ld.Ba[k] - ls.population[i] * ld.Bs[k]);
+                lines.emissivity[(size_t)p * L + lid] = std::max(em, parameters.min_line_emissivity);
+                lines.opacity[(size_t)p * L + lid] = std::max(op, parameters.min_line_opacity);
+            }
+        }
+    }
+    lines.emissivity.touch();
+    lines.opacity.touch();
+}
+
+int Model::compute_LTE_level_populations() {
+    prepare();
+    const Size P = parameters.npoints_.v;
+    const auto& T = thermodynamics.temperature.gas;
+    for (auto& ls : lines.lineProducingSpecies) {
+        const Linedata& ld = ls.linedata;
+        for (Size p = 0; p < P; p++) {
+            double partition_function = 0.0;
+            for (Size i = 0; i < ld.nlev; i++) {
+                const Size ind = ls.index(p, i);
+                ls.population[ind] = ld.weight[i] * std::exp(-ld.energy[i] / (KB * T[p]));
+                partition_function += ls.population[ind];
+            }
+            for (Size i = 0; i < ld.nlev; i++) ls.population[ls.index(p, i)] *= ls.population_tot[p] / partition_function;
+        }
+        ls.population.touch();
+    }
+    set_emissivity_and_opacity();
+    return 0;
+}
+
+// Model::set_dshift_max (model.cpp:1158-1178)
+int Model::set_dshift_max() {
+    const Size P = parameters.npoints_.v;
+    dshift_max.resize({P});
+    const auto& T = thermodynamics.temperature.gas;
+    const auto& vt2 = thermodynamics.turbulence.vturb2;
+    for (Size o = 0; o < P; o++) {
+        dshift_max[o] = std::numeric_limits<Real>::max();
+        for (const auto& ls : lines.lineProducingSpecies) {
+            const double nd = parameters.max_width_fraction *
+                              std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * ls.linedata.inverse_mass * T[o] + vt2[o]);
+            if (dshift_max[o] > nd) dshift_max[o] = nd;
+        }
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Device model
+// ---------------------------------------------------------------------------------
+uint64_t Model::signature() const {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t x) {
+        h ^= x;
+        h *= 1099511628211ull;
+    };
+    mix(geometry.points.position.version);
+    mix(geometry.points.velocity.version);
+    mix(geometry.points.neighbors.version);
+    mix(geometry.points.n_neighbors.version);
+    mix(geometry.rays.direction.version);
+    mix(geometry.rays.weight.version);
+    mix(geometry.boundary.boundary2point.version);
+    mix(geometry.boundary.boundary_condition.version);
+    mix(geometry.boundary.boundary_temperature.version);
+    mix(thermodynamics.temperature.gas.version);
+    mix(thermodynamics.turbulence.vturb2.version);
+    mix(radiation.frequencies.nu.version);
+    mix(dshift_max.version);
+    mix((uint64_t)parameters.approx());
+    double knobs[4] = {parameters.min_opacity, parameters.min_dtau, parameters.max_interpolation_diff,
+                       parameters.max_distance_opacity_contribution};
+    for (double k : knobs) {
+        uint64_t b;
+        std::memcpy(&b, &k, 8);
+        mix(b);
+    }
+    return h;
+}
+
+namespace {
+struct DescStorage {
+    std::vector<Size> nrad;
+    std::vector<double> line_A, inv_mass, quad_w, quad_r;
+};
+}  // namespace
+
+void Model::fill_desc(MgrModelDesc& d) {
+    std::memset(&d, 0, sizeof(d));
+    d.npoints = parameters.npoints_.v;
+    d.nrays = parameters.nrays_.v;
+    d.hnrays = parameters.hnrays_.v;
+    d.nlines = parameters.nlines_.v;
+    d.nquads = parameters.nquads_.v;
+    d.nfreqs = parameters.nfreqs_;
+    d.nlspecs = parameters.nlspecs_.v;
+    d.nboundary = parameters.nboundary_.v;
+    d.position = geometry.points.position.data();
+    d.velocity = geometry.points.velocity.data();
+    d.n_neighbors = geometry.points.n_neighbors.data();
+    d.cum_n_neighbors = geometry.points.cum_n_neighbors.data();
+    d.neighbors = geometry.points.neighbors.data();
+    d.point2boundary = geometry.boundary.point2boundary.data();
+    d.boundary_condition = geometry.boundary.boundary_condition.data();
+    d.boundary_temperature = geometry.boundary.boundary_temperature.data();
+    d.ray_direction = geometry.rays.direction.data();
+    d.ray_weight = geometry.rays.weight.data();
+    d.antipod = geometry.rays.antipod.data();
+    d.line = lines.line.data();
+    d.sorted_line = lines.sorted_line.data();
+    d.sorted_line_map = lines.sorted_line_map.data();
+    d.max_inverse_mass = lines.max_inverse_mass;
+    d.emissivity = lines.emissivity.data();
+    d.opacity = lines.opacity.data();
+    d.inverse_width = lines.inverse_width.data();
+    d.interp_criterion = crit_.data();
+    d.temperature = thermodynamics.temperature.gas.data();
+    d.vturb2 = thermodynamics.turbulence.vturb2.data();
+    d.dshift_max = dshift_max.data();
+    d.nu = radiation.frequencies.nu.data();
+    d.corr_line = radiation.frequencies.corresponding_line.data();
+    d.corr_lspec = radiation.frequencies.corresponding_l_for_spec.data();
+    d.corr_k = radiation.frequencies.corresponding_k_for_tran.data();
+    d.corr_z = radiation.frequencies.corresponding_z_for_line.data();
+    d.in_line_integral = radiation.frequencies.appears_in_line_integral.data();
+    d.min_opacity = parameters.min_opacity;
+    d.min_dtau = parameters.min_dtau;
+    d.max_interpolation_diff = parameters.max_interpolation_diff;
+    d.max_distance_opacity_contribution = parameters.max_distance_opacity_contribution;
+    d.approx = parameters.approx();
+}
+
+MgrModel* Model::device_model() {
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v;
+    // InterpHelper criterion: opacity / population_tot (solver_interp_helper.hpp:15-24)
+    crit_.resize((size_t)P * L);
+    for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+        const LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        for (Size k = 0; k < ls.linedata.nrad; k++) {
+            const Size lid = lines.nrad_cum[l] + k;
+            for (Size p = 0; p < P; p++)
+                crit_[(size_t)p * L + lid] = lines.opacity[(size_t)p * L + lid] / ls.population_tot[p];
+        }
+    }
+    const uint64_t sig = signature();
+    if (dev_ && sig == dev_signature_) {
+        check(mgr_model_set_line_data(dev_, lines.emissivity.data(), lines.opacity.data(), lines.inverse_width.data(),
+                                      crit_.data()));
+        return dev_;
+    }
+    release_device();
+    DescStorage st;
+    const Size nls = parameters.nlspecs_.v, Q = parameters.nquads_.v;
+    for (Size l = 0; l < nls; l++) {
+        const LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        st.nrad.push_back(ls.linedata.nrad);
+        st.inv_mass.push_back(ls.linedata.inverse_mass);
+        for (Size k = 0; k < ls.linedata.nrad; k++) st.line_A.push_back(ls.linedata.A[k]);
+        for (Size z = 0; z < Q; z++) {
+            st.quad_w.push_back(ls.quadrature.weights[z]);
+            st.quad_r.push_back(ls.quadrature.roots[z]);
+        }
+    }
+    MgrModelDesc d;
+    fill_desc(d);
+    d.nrad = st.nrad.data();
+    d.nrad_cum = lines.nrad_cum.data();
+    d.line_A = st.line_A.data();
+    d.lspec_inverse_mass = st.inv_mass.data();
+    d.quad_weights = st.quad_w.data();
+    d.quad_roots = st.quad_r.data();
+    check(mgr_model_create(&d, &dev_));
+    dev_signature_ = sig;
+    return dev_;
+}
+
+// ---------------------------------------------------------------------------------
+// Model::compute_radiation_field_feautrier_order_2 (model.cpp:353-390)
+// ---------------------------------------------------------------------------------
+MgrModel* Model::upload() {
+    prepare();
+    if (radiation.frequencies.nu.size() == 0)
+        throw std::runtime_error("compute_spectral_discretisation must be called before the formal solve");
+    if (parameters.n_off_diag != 0)
+        throw std::runtime_error("n_off_diag > 0 (non-local ALO) is not supported by the GPU formal solve");
+    set_dshift_max();
+    return device_model();
+}
+
+int Model::compute_radiation_field_feautrier_order_2() {
+    MgrModel* dev = upload();
+    const Size P = parameters.npoints_.v, F = parameters.nfreqs_, L = parameters.nlines_.v;
+    const Size R = parameters.hnrays_.v;
+    radiation.J.resize({P, F});
+    if (parameters.store_u) radiation.u.resize({R, P, F});
+    std::vector<double> lam((size_t)P * L);
+    check(mgr_formal_solve_fo2(dev, parameters.precision, radiation.J.data(),
+                               parameters.store_u ? radiation.u.data() : nullptr, lam.data()));
+    // Lambda::Ls diagonal per species (lambda.tpp:79-89)
+    for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+        LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        const Size nrad = ls.linedata.nrad;
+        ls.lambda_diag.resize({P, nrad});
+        ls.lambda_has.resize({P, nrad});
+        for (Size p = 0; p < P; p++)
+            for (Size k = 0; k < nrad; k++) {
+                const double v = lam[(size_t)p * L + lines.nrad_cum[l] + k];
+                ls.lambda_diag[(size_t)p * nrad + k] = v;
+                ls.lambda_has[(size_t)p * nrad + k] = v != 0.0;
+            }
+    }
+    return 0;
+}
+
+}  // namespace mgrhost

@@ -1,0 +1,489 @@
+// C ABI of libmgr_gpu.so: model upload, formal-solve entry points, status handling.
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mgr_internal.h"
+
+namespace mgr {
+
+static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char* what) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return MGR_ERR_CUDA;
+}
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+template <typename T>
+static cudaError_t dalloc(MgrModel* m, T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    if (e != cudaSuccess) return e;
+    m->allocations.push_back(q);
+    *p = static_cast<T*>(q);
+    return cudaSuccess;
+}
+
+template <typename T>
+static cudaError_t upload(MgrModel* m, const T** dst, const T* src, size_t count) {
+    T* p = nullptr;
+    cudaError_t e = dalloc(m, &p, count);
+    if (e != cudaSuccess) return e;
+    if (count) e = cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, m->stream);
+    *dst = p;
+    return e;
+}
+
+static int decode_status(int st) {
+    if (st & ST_TRACE) {
+        set_error("ray left the point cloud on an interior point (neighbour lists or boundary incomplete)");
+        return MGR_ERR_TRACE;
+    }
+    if (st & ST_CAPACITY) {
+        set_error("ray longer than the sized ray buffer");
+        return MGR_ERR_CAPACITY;
+    }
+    if (st & ST_NONFINITE) {
+        set_error("non-finite intensity in a ray-pair solve");
+        return MGR_ERR_NONFINITE;
+    }
+    return MGR_OK;
+}
+
+static int read_status(MgrModel* model) {
+    int st = 0;
+    cudaError_t e = cudaMemcpyAsync(&st, model->status, sizeof(int), cudaMemcpyDeviceToHost, model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "status read");
+    e = cudaStreamSynchronize(model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
+    e = cudaMemsetAsync(model->status, 0, sizeof(int), model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "status reset");
+    return decode_status(st);
+}
+
+static int ensure_scratch(MgrModel* m, double** p, size_t* have, size_t bytes) {
+    if (*have >= bytes) return MGR_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "scratch allocation");
+    *p = static_cast<double*>(q);
+    *have = bytes;
+    return MGR_OK;
+}
+
+static int size_model(MgrModel* model) {
+    uint32_t* d_max = nullptr;
+    cudaError_t e = cudaMalloc(&d_max, sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_fail(e, "sizing allocation");
+    cudaMemsetAsync(d_max, 0, sizeof(uint32_t), model->stream);
+    e = launch_size_rays(model, d_max);
+    uint32_t mx = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    cudaFree(d_max);
+    if (e != cudaSuccess) return cuda_fail(e, "ray sizing");
+    int st = read_status(model);
+    if (st != MGR_OK) return st;
+    model->half_cap = mx > 0 ? mx : 1;
+    return MGR_OK;
+}
+
+}  // namespace mgr
+
+using namespace mgr;
+
+extern "C" {
+
+const char* mgr_last_error(void) { return g_last_error.c_str(); }
+
+int mgr_version(void) { return 1; }
+
+uint64_t mgr_launch_count(void) { return g_launches.load(); }
+
+int mgr_device_count(int* count) {
+    if (!count) return MGR_ERR_ARGUMENT;
+    cudaError_t e = cudaGetDeviceCount(count);
+    if (e != cudaSuccess) {
+        *count = 0;
+        set_error(std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+        return MGR_ERR_NO_DEVICE;
+    }
+    return MGR_OK;
+}
+
+void mgr_model_free(MgrModel* model) {
+    if (!model) return;
+    if (model->stream) cudaStreamSynchronize(model->stream);
+    for (void* p : model->allocations) cudaFree(p);
+    if (model->J_scratch) cudaFree(model->J_scratch);
+    if (model->u_scratch) cudaFree(model->u_scratch);
+    if (model->lam_scratch) cudaFree(model->lam_scratch);
+    if (model->stream) cudaStreamDestroy(model->stream);
+    delete model;
+}
+
+int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
+    if (!d || !out) {
+        set_error("mgr_model_create: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    *out = nullptr;
+    if (d->npoints == 0 || d->nrays < 2 || d->hnrays * 2 != d->nrays || d->nlines == 0 || d->nquads == 0 ||
+        d->nfreqs == 0 || d->nlspecs == 0) {
+        set_error("mgr_model_create: inconsistent sizes (npoints, nrays = 2*hnrays, nlines, nquads, nfreqs, nlspecs)");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!d->position || !d->velocity || !d->n_neighbors || !d->cum_n_neighbors || !d->neighbors ||
+        !d->point2boundary || !d->ray_direction || !d->ray_weight || !d->antipod || !d->line || !d->sorted_line ||
+        !d->sorted_line_map || !d->emissivity || !d->opacity || !d->inverse_width || !d->interp_criterion ||
+        !d->temperature || !d->vturb2 || !d->dshift_max || !d->nu || !d->corr_line || !d->corr_lspec || !d->corr_k ||
+        !d->corr_z || !d->in_line_integral || !d->nrad_cum || !d->line_A || !d->lspec_inverse_mass ||
+        !d->quad_weights) {
+        set_error("mgr_model_create: a required array is null");
+        return MGR_ERR_ARGUMENT;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        set_error("mgr_model_create: no CUDA device");
+        return MGR_ERR_NO_DEVICE;
+    }
+    const uint32_t P = d->npoints, L = d->nlines, F = d->nfreqs;
+    // neighbour count and index checks (host side, before anything reaches the GPU)
+    size_t E = 0;
+    for (uint32_t p = 0; p < P; p++) {
+        if ((size_t)d->cum_n_neighbors[p] != E) {
+            set_error("mgr_model_create: cum_n_neighbors is not the prefix sum of n_neighbors");
+            return MGR_ERR_ARGUMENT;
+        }
+        E += d->n_neighbors[p];
+    }
+    for (size_t i = 0; i < E; i++) {
+        if (d->neighbors[i] >= P) {
+            set_error("mgr_model_create: neighbour index out of range");
+            return MGR_ERR_ARGUMENT;
+        }
+    }
+    for (uint32_t p = 0; p < P; p++) {
+        if (d->point2boundary[p] != P && d->point2boundary[p] >= d->nboundary) {
+            set_error("mgr_model_create: point2boundary out of range");
+            return MGR_ERR_ARGUMENT;
+        }
+    }
+    for (uint32_t r = 0; r < d->nrays; r++) {
+        if (d->antipod[r] >= d->nrays) {
+            set_error("mgr_model_create: antipod index out of range");
+            return MGR_ERR_ARGUMENT;
+        }
+    }
+    for (uint32_t f = 0; f < F; f++) {
+        if (d->corr_line[f] >= L || d->corr_lspec[f] >= d->nlspecs || d->corr_z[f] >= d->nquads) {
+            set_error("mgr_model_create: frequency maps out of range");
+            return MGR_ERR_ARGUMENT;
+        }
+    }
+    if (F != L * d->nquads) {
+        set_error("mgr_model_create: the formal solve needs a line spectral discretisation (nfreqs = nlines*nquads)");
+        return MGR_ERR_UNSUPPORTED;
+    }
+
+    MgrModel* m = new MgrModel();
+    cudaGetDevice(&m->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete m;
+        return cuda_fail(e, "stream creation");
+    }
+    DevModel& dm = m->dm;
+    dm.P = P;
+    dm.nrays = d->nrays;
+    dm.hnrays = d->hnrays;
+    dm.L = L;
+    dm.Q = d->nquads;
+    dm.F = F;
+    dm.nlspecs = d->nlspecs;
+    dm.B = d->nboundary;
+    dm.max_inv_mass = d->max_inverse_mass;
+    dm.min_opacity = d->min_opacity;
+    dm.min_dtau = d->min_dtau;
+    dm.max_interp_diff = d->max_interpolation_diff;
+    dm.max_dist = d->max_distance_opacity_contribution;
+    dm.log_max_interp_diff = logf((float)d->max_interpolation_diff);
+    dm.approx = d->approx;
+    m->n_edges = E;
+
+    // host-side derived tables
+    std::vector<double4_32a> pos4(P), vel4(P), edge(E ? E : 1);
+    for (uint32_t p = 0; p < P; p++) {
+        pos4[p] = make_double4_32a(d->position[3 * p], d->position[3 * p + 1], d->position[3 * p + 2], 0.0);
+        vel4[p] = make_double4_32a(d->velocity[3 * p], d->velocity[3 * p + 1], d->velocity[3 * p + 2], 0.0);
+    }
+    for (size_t i = 0; i < E; i++) {
+        const uint32_t n = d->neighbors[i];
+        long long bits = (long long)n;
+        double w;
+        std::memcpy(&w, &bits, sizeof(w));
+        edge[i] = make_double4_32a(d->position[3 * n], d->position[3 * n + 1], d->position[3 * n + 2], w);
+    }
+    std::vector<double> ub(P);
+    for (uint32_t p = 0; p < P; p++)
+        ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
+    std::vector<float> dsm_f(P);
+    for (uint32_t p = 0; p < P; p++) dsm_f[p] = (float)d->dshift_max[p];
+
+    const size_t PL = (size_t)P * L;
+    do {
+        if ((e = upload(m, &dm.pos, pos4.data(), P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.vel, vel4.data(), P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.n_nb, d->n_neighbors, P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.cum_nb, d->cum_n_neighbors, P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.edge, edge.data(), E ? E : 1)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.p2b, d->point2boundary, P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.bc, d->boundary_condition, d->nboundary)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.bt, d->boundary_temperature, d->nboundary)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.raydir, d->ray_direction, 3 * (size_t)d->nrays)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.rayw, d->ray_weight, d->nrays)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.antipod, d->antipod, d->nrays)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.line, d->line, L)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.sorted_line, d->sorted_line, L)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.sorted_map, d->sorted_line_map, L)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->em, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->op, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->iw, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->Sp, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->crit, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->em_f, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->op_f, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->iw_f, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->Sp_f, PL)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(m->em, d->emissivity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(m->op, d->opacity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(m->iw, d->inverse_width, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(m->crit, d->interp_criterion, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.ub, ub.data(), P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.T, d->temperature, P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.vt2, d->vturb2, P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.dshift_max, d->dshift_max, P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.dshift_max_f, dsm_f.data(), P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.nu, d->nu, (size_t)P * F)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.corr_line, d->corr_line, F)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.corr_lspec, d->corr_lspec, F)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.corr_k, d->corr_k, F)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.corr_z, d->corr_z, F)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.in_line, d->in_line_integral, F)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.nrad_cum, d->nrad_cum, d->nlspecs)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.line_A, d->line_A, L)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.lspec_inv_mass, d->lspec_inverse_mass, d->nlspecs)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.quad_w, d->quad_weights, (size_t)d->nlspecs * d->nquads)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->status, 1)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(m->status, 0, sizeof(int), m->stream)) != cudaSuccess) break;
+    } while (false);
+    if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "model upload");
+        mgr_model_free(m);
+        return rc;
+    }
+    dm.em = m->em;
+    dm.op = m->op;
+    dm.iw = m->iw;
+    dm.Sp = m->Sp;
+    dm.crit = m->crit;
+    dm.em_f = m->em_f;
+    dm.op_f = m->op_f;
+    dm.iw_f = m->iw_f;
+    dm.Sp_f = m->Sp_f;
+    if ((e = launch_line_tables(m)) != cudaSuccess) {
+        int rc = cuda_fail(e, "line tables");
+        mgr_model_free(m);
+        return rc;
+    }
+    int rc = size_model(m);
+    if (rc != MGR_OK) {
+        mgr_model_free(m);
+        return rc;
+    }
+    *out = m;
+    return MGR_OK;
+}
+
+int mgr_model_set_line_data(MgrModel* model, const double* emissivity, const double* opacity,
+                            const double* inverse_width, const double* interp_criterion) {
+    if (!model) {
+        set_error("mgr_model_set_line_data: null model");
+        return MGR_ERR_ARGUMENT;
+    }
+    const size_t bytes = (size_t)model->dm.P * model->dm.L * 8;
+    cudaError_t e = cudaSuccess;
+    if (emissivity && e == cudaSuccess) e = cudaMemcpyAsync(model->em, emissivity, bytes, cudaMemcpyHostToDevice, model->stream);
+    if (opacity && e == cudaSuccess) e = cudaMemcpyAsync(model->op, opacity, bytes, cudaMemcpyHostToDevice, model->stream);
+    if (inverse_width && e == cudaSuccess) e = cudaMemcpyAsync(model->iw, inverse_width, bytes, cudaMemcpyHostToDevice, model->stream);
+    if (interp_criterion && e == cudaSuccess) e = cudaMemcpyAsync(model->crit, interp_criterion, bytes, cudaMemcpyHostToDevice, model->stream);
+    if (e == cudaSuccess) e = launch_line_tables(model);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "line data update");
+    return MGR_OK;
+}
+
+int mgr_ray_lengths_max(MgrModel* model, uint32_t* length) {
+    if (!model || !length) {
+        set_error("mgr_ray_lengths_max: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    uint32_t* d_max = nullptr;
+    cudaError_t e = cudaMalloc(&d_max, sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_fail(e, "allocation");
+    cudaMemsetAsync(d_max, 0, sizeof(uint32_t), model->stream);
+    e = launch_ray_lengths(model, d_max);
+    uint32_t mx = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    cudaFree(d_max);
+    if (e != cudaSuccess) return cuda_fail(e, "ray lengths");
+    int st = read_status(model);
+    if (st != MGR_OK) return st;
+    *length = mx;
+    return MGR_OK;
+}
+
+int mgr_trace_ray_pair(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity, uint32_t* n_tot,
+                       uint32_t* centre, uint32_t* nr, uint32_t* nr_interp, double* interp_factor, double* shift,
+                       double* dZ) {
+    if (!model || !n_tot || !centre || !nr || !nr_interp || !interp_factor || !shift || !dZ || capacity == 0) {
+        set_error("mgr_trace_ray_pair: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (o >= model->dm.P || rr >= model->dm.hnrays || l >= model->dm.L) {
+        set_error("mgr_trace_ray_pair: index out of range");
+        return MGR_ERR_ARGUMENT;
+    }
+    uint32_t* d_meta = nullptr;
+    uint32_t *d_nr = nullptr, *d_ni = nullptr;
+    double *d_fac = nullptr, *d_shift = nullptr, *d_dZ = nullptr;
+    cudaError_t e = cudaMalloc(&d_meta, 3 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_nr, capacity * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_ni, capacity * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_fac, capacity * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_shift, capacity * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_dZ, capacity * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_dZ, 0, capacity * sizeof(double), model->stream);
+    if (e == cudaSuccess) e = launch_trace_export(model, o, rr, l, capacity, d_meta, d_nr, d_ni, d_fac, d_shift, d_dZ);
+    uint32_t meta[3] = {0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(meta, d_meta, sizeof(meta), cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    int rc = MGR_OK;
+    if (e != cudaSuccess) rc = cuda_fail(e, "trace export");
+    if (rc == MGR_OK && meta[2] == 2) {
+        set_error("mgr_trace_ray_pair: capacity too small");
+        rc = MGR_ERR_CAPACITY;
+    }
+    if (rc == MGR_OK) {
+        int st = read_status(model);
+        if (st != MGR_OK) rc = st;
+    }
+    if (rc == MGR_OK) {
+        const size_t n = meta[0];
+        *n_tot = meta[0];
+        *centre = meta[1];
+        e = cudaMemcpy(nr, d_nr, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(nr_interp, d_ni, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(interp_factor, d_fac, n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(shift, d_shift, n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(dZ, d_dZ, n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = cuda_fail(e, "trace export copy");
+    }
+    cudaFree(d_meta);
+    cudaFree(d_nr);
+    cudaFree(d_ni);
+    cudaFree(d_fac);
+    cudaFree(d_shift);
+    cudaFree(d_dZ);
+    return rc;
+}
+
+int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, double* u_dev,
+                                double* lambda_diag_dev) {
+    if (!model || !J_dev) {
+        set_error("mgr_formal_solve_fo2_device: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
+        set_error("mgr_formal_solve_fo2_device: unknown precision mode");
+        return MGR_ERR_ARGUMENT;
+    }
+    cudaError_t e = launch_fo2(model, precision, J_dev, u_dev, lambda_diag_dev);
+    if (e != cudaSuccess) return cuda_fail(e, "formal solve launch");
+    return MGR_OK;
+}
+
+int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, double* lambda_diag) {
+    if (!model || !J) {
+        set_error("mgr_formal_solve_fo2: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    const DevModel& dm = model->dm;
+    const size_t PF = (size_t)dm.P * dm.F;
+    int rc = ensure_scratch(model, &model->J_scratch, &model->J_scratch_bytes, PF * 8);
+    if (rc != MGR_OK) return rc;
+    if (u && (rc = ensure_scratch(model, &model->u_scratch, &model->u_scratch_bytes, PF * dm.hnrays * 8)) != MGR_OK)
+        return rc;
+    if (lambda_diag &&
+        (rc = ensure_scratch(model, &model->lam_scratch, &model->lam_scratch_bytes, (size_t)dm.P * dm.L * 8)) != MGR_OK)
+        return rc;
+    rc = mgr_formal_solve_fo2_device(model, precision, model->J_scratch, u ? model->u_scratch : nullptr,
+                                     lambda_diag ? model->lam_scratch : nullptr);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(J, model->J_scratch, PF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && u)
+        e = cudaMemcpyAsync(u, model->u_scratch, PF * dm.hnrays * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && lambda_diag)
+        e = cudaMemcpyAsync(lambda_diag, model->lam_scratch, (size_t)dm.P * dm.L * 8, cudaMemcpyDeviceToHost,
+                            model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "result copy");
+    return read_status(model);
+}
+
+int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_reads, uint64_t* elements) {
+    if (!model || !steps || !neighbor_reads || !elements) {
+        set_error("mgr_ray_statistics: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 3 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(e, "allocation");
+    unsigned long long h[3] = {0, 0, 0};
+    e = cudaMemsetAsync(d, 0, sizeof(h), model->stream);
+    if (e == cudaSuccess) e = launch_ray_stats(model, d);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "ray statistics");
+    int st = read_status(model);
+    if (st != MGR_OK) return st;
+    *steps = h[0];
+    *neighbor_reads = h[1];
+    *elements = h[2];
+    return MGR_OK;
+}
+
+int mgr_sync(MgrModel* model) {
+    if (!model) {
+        set_error("mgr_sync: null model");
+        return MGR_ERR_ARGUMENT;
+    }
+    return read_status(model);
+}
+
+void* mgr_model_stream(MgrModel* model) { return model ? (void*)model->stream : nullptr; }
+
+}  // extern "C"

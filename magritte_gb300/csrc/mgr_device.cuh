@@ -1,0 +1,243 @@
+// Device-side model, physics and ray tracing for the Magritte formal-solve path.
+//
+// Every function restates one reference statement (Magritte 0.9.3 paths given per
+// function).  Precision policy:
+//   * Ray tracing (neighbour choice, Z, dZ, Doppler shift, interpolation split) uses
+//     explicitly rounded FP64 operations (__dmul_rn/__dadd_rn) so that no multiply-add
+//     is contracted: point sequences are bit-identical to the reference's FP64 CPU code.
+//   * MGR_PRECISION_FP64 follows the reference's arithmetic: FP64 with the reference's
+//     single-precision libm calls (expf, erff, logf, powf, expm1f).
+//   * MGR_PRECISION_SPLIT evaluates profiles, opacities, sources and optical depths in
+//     FP32 (frequencies as FP32 offsets from the line centre, so no catastrophic
+//     cancellation), and keeps the Feautrier elimination in FP64.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mgr {
+
+// src/tools/constants.hpp:15-40
+constexpr double INVERSE_SQRT_PI = 0.5 * 1.12837916709551257390;
+constexpr double CC = 2.99792458E+8;
+constexpr double HH = 6.62607004E-34;
+constexpr double KB = 1.38064852E-23;
+constexpr double AMU = 1.66053904E-27;
+constexpr double T_CMB = 2.7254800;
+constexpr double CC_SQUARED = 8.98755179E+16;
+constexpr double TWO_KB_OVER_AMU_CC_SQUARED = 2.0 * KB / (AMU * CC_SQUARED);
+constexpr double TWO_HH_OVER_CC_SQUARED = 2.0 * HH / CC_SQUARED;
+constexpr double HH_OVER_KB = HH / KB;
+
+enum { APPROX_NONE = 0, APPROX_ONELINE = 1, APPROX_CLOSELINES = 2 };
+enum { BC_ZERO = 0, BC_THERMAL = 1, BC_CMB = 2 };
+enum { MODE_FP64 = 0, MODE_SPLIT = 1 };
+
+// Kernel-side status bits (combined with atomicOr; decoded by the host).
+enum : int { ST_TRACE = 1, ST_CAPACITY = 2, ST_NONFINITE = 4 };
+
+// Device-resident model.  Per-(point, line) tables are [P][L] (index l + p*L).
+struct DevModel {
+    uint32_t P, nrays, hnrays, L, Q, F, nlspecs, B;
+    const double4_32a* pos;      // [P] x, y, z
+    const double4_32a* vel;      // [P] vx, vy, vz (v/c)
+    const uint32_t* n_nb;    // [P]
+    const uint32_t* cum_nb;  // [P]
+    const double4_32a* edge;     // [E] neighbour position x, y, z and its index (bits of w)
+    const uint32_t* p2b;     // [P]
+    const int32_t* bc;       // [B]
+    const double* bt;        // [B]
+    const double* raydir;    // [nrays][3]
+    const double* rayw;      // [nrays]
+    const uint32_t* antipod; // [nrays]
+    const double* line;      // [L]
+    const double* sorted_line;
+    const uint32_t* sorted_map;
+    double max_inv_mass;
+    const double* em;        // emissivity
+    const double* op;        // opacity
+    const double* iw;        // inverse width
+    const double* Sp;        // emissivity / opacity, the reference's per-call quotient
+    const double* crit;      // interpolation criterion opacity / population_tot
+    const float* em_f;
+    const float* op_f;
+    const float* iw_f;
+    const float* Sp_f;
+    const double* ub;        // [P] sqrt(2 kB/(amu c^2) max_inv_mass T + vturb2)
+    const double* T;         // [P]
+    const double* vt2;       // [P]
+    const double* dshift_max;// [P]
+    const float* dshift_max_f;
+    const double* nu;        // [P][F]
+    const uint32_t* corr_line;
+    const uint32_t* corr_lspec;
+    const uint32_t* corr_k;
+    const uint32_t* corr_z;
+    const uint8_t* in_line;
+    const uint32_t* nrad_cum;
+    const double* line_A;        // [L]
+    const double* lspec_inv_mass;// [nlspecs]
+    const double* quad_w;        // [nlspecs][Q]
+    double min_opacity;
+    double min_dtau;
+    double max_interp_diff;
+    double max_dist;
+    float log_max_interp_diff;   // logf((float)max_interp_diff)
+    int approx;
+};
+
+// ---------------------------------------------------------------------------------
+// Exactly rounded FP64 helpers for the trace (no contraction into FMA).
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double dot3_rn(double ax, double ay, double az, double bx, double by, double bz) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+}
+
+// Geometry::get_shift_general_geometry<CoMoving> (geometry.tpp:203-207):
+// 1 + (v[c] - v[o]) . n
+__device__ __forceinline__ double shift_comoving(const DevModel& m, uint32_t o, uint32_t c, const double* d) {
+    const double4_32a vc = m.vel[c];
+    const double4_32a vo = m.vel[o];
+    return __dadd_rn(1.0, dot3_rn(__dsub_rn(vc.x, vo.x), __dsub_rn(vc.y, vo.y), __dsub_rn(vc.z, vo.z), d[0], d[1], d[2]));
+}
+
+// Geometry::get_shift_general_geometry<Rest> and its reversal for r >= hnrays
+// (geometry.tpp:209-221, :428-465).
+__device__ __forceinline__ double shift_rest(const DevModel& m, uint32_t r, uint32_t c, const double* d) {
+    const double4_32a vc = m.vel[c];
+    double s = __dadd_rn(1.0, dot3_rn(vc.x, vc.y, vc.z, d[0], d[1], d[2]));
+    if (r >= m.hnrays) s = __dsub_rn(2.0, s);
+    return s;
+}
+
+// ---------------------------------------------------------------------------------
+// InterpHelper (solver_interp_helper.tpp:55-99)
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t n_interp_for_line(const DevModel& m, uint32_t l, uint32_t crt, uint32_t nxt) {
+    const double curr = m.crit[(size_t)crt * m.L + l];
+    const double next = m.crit[(size_t)nxt * m.L + l];
+    const double source_diff = fabsf(logf((float)(next / curr)));
+    const double q = source_diff / (double)m.log_max_interp_diff;
+    const double c = ceil(q);
+    // (Size)NaN is 0 on the reference's targets; keep that outcome explicitly.
+    const uint32_t n = (c == c && c > 0.0) ? (c < 4294967295.0 ? (uint32_t)c : 0xffffffffu) : 0u;
+    return n > 1 ? n : 1;
+}
+
+__device__ __forceinline__ uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt) {
+    double mx = -DBL_MAX;
+    for (uint32_t l = 0; l < m.L; l++) {
+        const double x = m.crit[(size_t)nxt * m.L + l];
+        const double y = m.crit[(size_t)crt * m.L + l];
+        const double d = fabsf(logf((float)(x / y)));
+        if (d > mx) mx = d;
+    }
+    const double c = ceil(mx / (double)m.log_max_interp_diff);
+    const uint32_t n = (c == c && c > 0.0) ? (c < 4294967295.0 ? (uint32_t)c : 0xffffffffu) : 0u;
+    return n > 1 ? n : 1;
+}
+
+template <typename R>
+__device__ __forceinline__ R interpolate_linear(R f_start, R f_end, R factor) {
+    if (factor == R(0)) return f_start;
+    if (factor == R(1)) return f_end;
+    return (f_end - f_start) * factor + f_start;
+}
+
+__device__ __forceinline__ double interpolate_log(double f_start, double f_end, double factor) {
+    if (factor == 0.0) return f_start;
+    if (factor == 1.0) return f_end;
+    return f_start * (double)powf((float)(f_end / f_start), (float)factor);
+}
+__device__ __forceinline__ float interpolate_log(float f_start, float f_end, float factor) {
+    if (factor == 0.0f) return f_start;
+    if (factor == 1.0f) return f_end;
+    return f_start * powf(f_end / f_start, factor);
+}
+
+// ---------------------------------------------------------------------------------
+// Profiles and boundary (solver.tpp:1106-1142, thermodynamics.tpp:8-35)
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double gaussian(double inverse_width, double diff) {
+    const double sqrt_exp = inverse_width * diff;
+    return inverse_width * INVERSE_SQRT_PI * (double)expf((float)(-sqrt_exp * sqrt_exp));
+}
+__device__ __forceinline__ float gaussian(float inverse_width, float diff) {
+    const float sqrt_exp = inverse_width * diff;
+    return inverse_width * (float)INVERSE_SQRT_PI * expf(-sqrt_exp * sqrt_exp);
+}
+
+__device__ __forceinline__ double planck(double temp, double freq) {
+    return TWO_HH_OVER_CC_SQUARED * (freq * freq * freq) / (double)expm1f((float)(HH_OVER_KB * freq / temp));
+}
+
+__device__ __forceinline__ double boundary_intensity(const DevModel& m, uint32_t p, double freq) {
+    const uint32_t b = m.p2b[p];
+    if (b >= m.B) return 0.0;  // interior point: no boundary condition
+    const int c = m.bc[b];
+    if (c == BC_ZERO) return 0.0;
+    if (c == BC_THERMAL) return planck(m.bt[b], freq);
+    return planck(T_CMB, freq);
+}
+
+__device__ __forceinline__ double thermo_profile(const DevModel& m, double inverse_mass, uint32_t p, double freq_line,
+                                                 double freq) {
+    const double width = freq_line * sqrt(TWO_KB_OVER_AMU_CC_SQUARED * inverse_mass * m.T[p] + m.vt2[p]);
+    const double inverse_width = 1.0 / width;
+    const double sqrtExponent = inverse_width * (freq - freq_line);
+    const double exponent = sqrtExponent * sqrtExponent;
+    return inverse_width * INVERSE_SQRT_PI * (double)expf((float)(-exponent));
+}
+
+template <typename T>
+__device__ __forceinline__ uint32_t lower_bound(const T* a, uint32_t n, T v) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+template <typename T>
+__device__ __forceinline__ uint32_t upper_bound(const T* a, uint32_t n, T v) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (!(v < a[mid])) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Solver::get_eta_and_chi<approx> (solver.tpp:1151-1165, :1197-1239, :1286-1294), FP64.
+// `sl` is the sorted line table staged in shared memory.
+__device__ __forceinline__ void get_eta_and_chi(const DevModel& m, const double* sl, uint32_t p, uint32_t ll,
+                                                double freq, double& eta, double& chi) {
+    const size_t base = (size_t)p * m.L;
+    if (m.approx == APPROX_ONELINE) {
+        const double prof = gaussian(m.iw[base + ll], freq - m.line[ll]);
+        eta = prof * m.em[base + ll];
+        chi = prof * m.op[base + ll] + m.min_opacity;
+        return;
+    }
+    eta = 0.0;
+    chi = m.min_opacity;
+    if (m.approx == APPROX_NONE) {
+        for (uint32_t l = 0; l < m.L; l++) {
+            const double prof = gaussian(m.iw[base + l], freq - m.line[l]);
+            eta += prof * m.em[base + l];
+            chi += prof * m.op[base + l];
+        }
+        return;
+    }
+    const double ub = m.max_dist * (freq * m.ub[p]);
+    const uint32_t lo = lower_bound(sl, m.L, freq - ub);
+    const uint32_t hi = upper_bound(sl, m.L, freq + ub);
+    for (uint32_t s = lo; s < hi; s++) {
+        const uint32_t l = m.sorted_map[s];
+        const double prof = gaussian(m.iw[base + l], freq - sl[s]);
+        eta += prof * m.em[base + l];
+        chi += prof * m.op[base + l];
+    }
+}
+
+}  // namespace mgr

@@ -1,0 +1,353 @@
+// Kernels of the formal-solve path and their launchers.
+#include "mgr_internal.h"
+#include "mgr_solve.cuh"
+
+namespace mgr {
+
+// ---------------------------------------------------------------------------------
+// Per-(point, line) tables: the source quotient emissivity/opacity the reference
+// recomputes per call (solver.tpp:1901-1908) and FP32 copies for split precision.
+// FP32 copies of positive values below the smallest normal float are raised to it
+// (the reference's 1e-50 emissivity floor is not representable in FP32).
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ float to_f32_floor(double x) {
+    const float f = (float)x;
+    return (x > 0.0 && f < FLT_MIN) ? FLT_MIN : f;
+}
+
+__global__ void line_tables_kernel(const double* __restrict__ em, const double* __restrict__ op,
+                                   const double* __restrict__ iw, double* __restrict__ Sp, float* __restrict__ em_f,
+                                   float* __restrict__ op_f, float* __restrict__ iw_f, float* __restrict__ Sp_f,
+                                   size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double e = em[i], o = op[i];
+        const double s = e / o;
+        Sp[i] = s;
+        em_f[i] = to_f32_floor(e);
+        op_f[i] = to_f32_floor(o);
+        iw_f[i] = (float)iw[i];
+        Sp_f[i] = to_f32_floor(s);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Longest half ray (base steps) over all points and rays: sizes the shared-memory
+// ray buffers.  One warp per (point, ray).
+// ---------------------------------------------------------------------------------
+__global__ void size_rays_kernel(DevModel m, uint32_t* d_max, int* status) {
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint64_t total = (uint64_t)m.P * m.nrays;
+    if (gw >= total) return;
+    const uint32_t o = (uint32_t)(gw / m.nrays);
+    const uint32_t r = (uint32_t)(gw % m.nrays);
+    HalfSmem h{nullptr, nullptr, nullptr, nullptr};
+    const int n = trace_half<false>(m, o, r, 0xffffffffu, h, lane, status);
+    if (lane == 0 && n > 0) atomicMax(d_max, (uint32_t)n);
+}
+
+// Shared-memory carve-up of one warp's two half-ray buffers.
+__device__ __forceinline__ void carve_halves(unsigned char* base, uint32_t cap, HalfSmem& bk, HalfSmem& fw) {
+    double* d = reinterpret_cast<double*>(base);
+    bk.shift = d;
+    bk.dZ = d + cap;
+    fw.shift = d + 2 * cap;
+    fw.dZ = d + 3 * cap;
+    uint32_t* u = reinterpret_cast<uint32_t*>(d + 4 * cap);
+    bk.ids = u;
+    fw.ids = u + cap;
+    float* f = reinterpret_cast<float*>(u + 2 * cap);
+    bk.dsh = f;
+    fw.dsh = f + cap;
+}
+
+__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 2 * 4 + 2 * 4); }
+
+// ---------------------------------------------------------------------------------
+// Reference ray-pair length (Solver::get_ray_lengths_max, solver.tpp:79-126):
+// elements of both halves with get_n_interp over all lines.
+// ---------------------------------------------------------------------------------
+__global__ void ray_lengths_kernel(DevModel m, uint32_t cap, uint32_t* d_max, int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + w;
+    if (gw >= (uint64_t)m.P * m.hnrays) return;
+    HalfSmem bk, fw;
+    carve_halves(smem + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
+    const uint32_t o = (uint32_t)(gw / m.hnrays);
+    const uint32_t rr = (uint32_t)(gw % m.hnrays);
+    const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
+    const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+    if (nb < 0 || nf < 0) return;
+    uint32_t len = 0;
+    for (int s = lane; s < nb; s += 32) len += n_interp_all_lines(m, s ? bk.ids[s - 1] : o, bk.ids[s]);
+    for (int s = lane; s < nf; s += 32) len += n_interp_all_lines(m, s ? fw.ids[s - 1] : o, fw.ids[s]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) len += __shfl_xor_sync(FULL_MASK, len, off);
+    if (lane == 0) atomicMax(d_max, len);
+}
+
+// ---------------------------------------------------------------------------------
+// Formal solve: one CTA per origin, one warp per ray pair, one lane per frequency.
+// ---------------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(256) fo2_kernel(DevModel m, uint32_t cap, double* __restrict__ J,
+                                                  double* __restrict__ u, double* __restrict__ lam, int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nw = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    double* sl = reinterpret_cast<double*>(smem);
+    const uint32_t Lpad = (m.L + 1) & ~1u;
+    double* Jw = sl + Lpad;
+    double* Lw = Jw + (size_t)nw * m.F;
+    unsigned char* tb = reinterpret_cast<unsigned char*>(Lw + (size_t)nw * m.F);
+    HalfSmem bk, fw;
+    carve_halves(tb + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
+    for (uint32_t i = threadIdx.x; i < m.L; i += blockDim.x) sl[i] = m.sorted_line[i];
+
+    for (uint32_t o = blockIdx.x; o < m.P; o += gridDim.x) {
+        for (uint32_t f = lane; f < m.F; f += 32) {
+            Jw[(size_t)w * m.F + f] = 0.0;
+            Lw[(size_t)w * m.F + f] = 0.0;
+        }
+        __syncthreads();
+        for (uint32_t rr = w; rr < m.hnrays; rr += nw) {
+            const uint32_t ar = m.antipod[rr];
+            const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
+            const int nf = trace_half<true>(m, o, ar, cap, fw, lane, status);
+            if (nb < 0 || nf < 0) continue;
+            const double wrr = m.rayw[rr];
+            for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
+                const uint32_t f = f0 + lane;
+                if (f < m.F) {
+                    LaneCtx c;
+                    c.o = o;
+                    c.f = f;
+                    c.l0 = m.corr_line[f];
+                    c.freq = m.nu[(size_t)o * m.F + f];
+                    c.fq = (float)c.freq;
+                    c.a0 = (float)(c.freq - m.line[c.l0]);
+                    const LaneResult r = solve_lane<MODE>(m, sl, c, bk, nb, fw, nf);
+                    double contribution;
+                    if (r.solved) contribution = r.u * 2.0 * wrr;
+                    else contribution = 2.0 * wrr * r.u;
+                    Jw[(size_t)w * m.F + f] += contribution;
+                    if (u) u[((size_t)rr * m.P + o) * m.F + f] = r.u;
+                    if (r.solved && m.in_line[f]) Lw[(size_t)w * m.F + f] += lambda_element(m, sl, o, rr, f, r.Ldiag);
+                    if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
+                }
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
+            double s = 0.0;
+            for (int ww = 0; ww < nw; ww++) s += Jw[(size_t)ww * m.F + f];
+            J[(size_t)o * m.F + f] = s;
+        }
+        if (lam) {
+            for (uint32_t lid = threadIdx.x; lid < m.L; lid += blockDim.x) {
+                double s = 0.0;
+                for (uint32_t z = 0; z < m.Q; z++) {
+                    const uint32_t f = lid * m.Q + z;
+                    for (int ww = 0; ww < nw; ww++) s += Lw[(size_t)ww * m.F + f];
+                }
+                lam[(size_t)o * m.L + lid] = s;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// One ray pair for one line in the reference's buffer layout (for parity checks).
+// meta = {n_tot, centre, status}.
+// ---------------------------------------------------------------------------------
+__global__ void trace_export_kernel(DevModel m, uint32_t o, uint32_t rr, uint32_t l, uint32_t cap, uint32_t capacity,
+                                    uint32_t* meta, uint32_t* nr, uint32_t* ni, double* fac, double* shift, double* dZ,
+                                    int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    HalfSmem bk, fw;
+    carve_halves(smem, cap, bk, fw);
+    const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
+    const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+    if (lane != 0) return;
+    if (nb < 0 || nf < 0) {
+        meta[0] = 0;
+        meta[1] = 0;
+        meta[2] = 1;
+        return;
+    }
+    // count elements of each half
+    uint32_t cb = 0, cf = 0;
+    for (int s = 0; s < nb; s++) cb += n_interp_for_line(m, l, s ? bk.ids[s - 1] : o, bk.ids[s]);
+    for (int s = 0; s < nf; s++) cf += n_interp_for_line(m, l, s ? fw.ids[s - 1] : o, fw.ids[s]);
+    const uint32_t n_tot = cb + 1 + cf;
+    if (n_tot > capacity) {
+        meta[0] = n_tot;
+        meta[1] = cb;
+        meta[2] = 2;
+        return;
+    }
+    // backward half: outer end first = array index 0
+    uint32_t idx = 0;
+    ElemIter it;
+    Elem e;
+    if (nb > 0) {
+        iter_begin(m, bk, o, l, nb, it);
+        while (iter_next(m, bk, o, l, it, e)) {
+            nr[idx] = e.nr;
+            ni[idx] = e.ni;
+            fac[idx] = e.fac;
+            shift[idx] = e.shift;
+            dZ[idx] = e.dzin;  // distance to the next (inner) element
+            idx++;
+        }
+    }
+    nr[idx] = o;
+    ni[idx] = 0;
+    fac[idx] = 0.0;
+    shift[idx] = 1.0;
+    const uint32_t centre = idx;
+    // forward half: elements centre+1 .. last are produced outer end first
+    if (nf > 0) {
+        iter_begin(m, fw, o, l, nf, it);
+        uint32_t j = n_tot - 1;
+        while (iter_next(m, fw, o, l, it, e)) {
+            nr[j] = e.nr;
+            ni[j] = e.ni;
+            fac[j] = e.fac;
+            shift[j] = e.shift;
+            dZ[j - 1] = e.dzin;  // distance to the previous (inner) element
+            j--;
+        }
+    }
+    meta[0] = n_tot;
+    meta[1] = centre;
+    meta[2] = 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------------
+cudaError_t launch_line_tables(MgrModel* model) {
+    const size_t n = (size_t)model->dm.P * model->dm.L;
+    const int threads = 256;
+    const int blocks = (int)((n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16);
+    count_launch();
+    line_tables_kernel<<<blocks > 0 ? blocks : 1, threads, 0, model->stream>>>(
+        model->em, model->op, model->iw, model->Sp, model->em_f, model->op_f, model->iw_f, model->Sp_f, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps) {
+    const uint64_t warps = (uint64_t)model->dm.P * model->dm.nrays;
+    const int threads = 256;
+    const uint64_t blocks = (warps * 32 + threads - 1) / threads;
+    count_launch();
+    size_rays_kernel<<<(unsigned)blocks, threads, 0, model->stream>>>(model->dm, d_max_steps, model->status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ray_lengths(MgrModel* model, uint32_t* d_max_len) {
+    const uint32_t cap = model->half_cap;
+    const int wpb = 4;
+    const size_t smem = wpb * half_bytes_per_warp(cap);
+    const uint64_t warps = (uint64_t)model->dm.P * model->dm.hnrays;
+    const uint64_t blocks = (warps + wpb - 1) / wpb;
+    cudaError_t e = cudaFuncSetAttribute(ray_lengths_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    ray_lengths_kernel<<<(unsigned)blocks, wpb * 32, smem, model->stream>>>(model->dm, cap, d_max_len, model->status);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// Work statistics of one formal solve: trace steps, neighbour records read by the
+// trace, and ray-pair elements summed over lines (for the algorithmic-bytes roofline).
+// stats = {steps, neighbour_reads, elements}.
+// ---------------------------------------------------------------------------------
+__global__ void ray_stats_kernel(DevModel m, uint32_t cap, unsigned long long* stats, int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + w;
+    if (gw >= (uint64_t)m.P * m.hnrays) return;
+    HalfSmem bk, fw;
+    carve_halves(smem + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
+    const uint32_t o = (uint32_t)(gw / m.hnrays);
+    const uint32_t rr = (uint32_t)(gw % m.hnrays);
+    const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
+    const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+    if (nb < 0 || nf < 0) return;
+    unsigned long long nbr = 0, elems = 0;
+    for (int s = lane; s < nb; s += 32) {
+        const uint32_t crt = s ? bk.ids[s - 1] : o;
+        nbr += m.n_nb[crt];
+        for (uint32_t l = 0; l < m.L; l++) elems += n_interp_for_line(m, l, crt, bk.ids[s]);
+    }
+    for (int s = lane; s < nf; s += 32) {
+        const uint32_t crt = s ? fw.ids[s - 1] : o;
+        nbr += m.n_nb[crt];
+        for (uint32_t l = 0; l < m.L; l++) elems += n_interp_for_line(m, l, crt, fw.ids[s]);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        nbr += __shfl_xor_sync(FULL_MASK, nbr, off);
+        elems += __shfl_xor_sync(FULL_MASK, elems, off);
+    }
+    if (lane == 0) {
+        atomicAdd(&stats[0], (unsigned long long)(nb + nf));
+        atomicAdd(&stats[1], nbr);
+        atomicAdd(&stats[2], elems + m.L);  // + the origin element of each line
+    }
+}
+
+cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats) {
+    const uint32_t cap = model->half_cap;
+    const int wpb = 4;
+    const size_t smem = wpb * half_bytes_per_warp(cap);
+    const uint64_t warps = (uint64_t)model->dm.P * model->dm.hnrays;
+    const uint64_t blocks = (warps + wpb - 1) / wpb;
+    cudaError_t e = cudaFuncSetAttribute(ray_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    ray_stats_kernel<<<(unsigned)blocks, wpb * 32, smem, model->stream>>>(model->dm, cap, d_stats, model->status);
+    return cudaGetLastError();
+}
+
+template <int MODE>
+static cudaError_t launch_fo2_mode(MgrModel* model, double* J, double* u, double* lam) {
+    const DevModel& m = model->dm;
+    const uint32_t cap = model->half_cap;
+    int nw = (int)(m.hnrays < 8 ? m.hnrays : 8);
+    if (nw < 1) nw = 1;
+    const uint32_t Lpad = (m.L + 1) & ~1u;
+    const size_t smem = (size_t)Lpad * 8 + 2ull * nw * m.F * 8 + (size_t)nw * half_bytes_per_warp(cap);
+    cudaError_t e = cudaFuncSetAttribute(fo2_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    fo2_kernel<MODE><<<m.P, nw * 32, smem, model->stream>>>(m, cap, J, u, lam, model->status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fo2(MgrModel* model, int precision, double* J, double* u, double* lam) {
+    if (precision == MGR_PRECISION_SPLIT) return launch_fo2_mode<MODE_SPLIT>(model, J, u, lam);
+    return launch_fo2_mode<MODE_FP64>(model, J, u, lam);
+}
+
+cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
+                                uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
+                                double* d_dZ) {
+    const uint32_t cap = model->half_cap;
+    const size_t smem = half_bytes_per_warp(cap);
+    cudaError_t e = cudaFuncSetAttribute(trace_export_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    trace_export_kernel<<<1, 32, smem, model->stream>>>(model->dm, o, rr, l, cap, capacity, d_meta, d_nr, d_ni, d_fac,
+                                                        d_shift, d_dZ, model->status);
+    return cudaGetLastError();
+}
+
+}  // namespace mgr

@@ -1,0 +1,54 @@
+// Host-side internals shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/magritte_gb300.h"
+#include "mgr_device.cuh"
+
+struct MgrModel {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    mgr::DevModel dm{};
+    std::vector<void*> allocations;  // every device allocation owned by the model
+    double* em = nullptr;
+    double* op = nullptr;
+    double* iw = nullptr;
+    double* Sp = nullptr;
+    double* crit = nullptr;
+    float* em_f = nullptr;
+    float* op_f = nullptr;
+    float* iw_f = nullptr;
+    float* Sp_f = nullptr;
+    int* status = nullptr;           // device status word
+    uint32_t half_cap = 0;           // longest half ray in base steps (0 = not sized yet)
+    size_t n_edges = 0;
+    // scratch outputs for the host-buffer entry points
+    double* J_scratch = nullptr;
+    size_t J_scratch_bytes = 0;
+    double* u_scratch = nullptr;
+    size_t u_scratch_bytes = 0;
+    double* lam_scratch = nullptr;
+    size_t lam_scratch_bytes = 0;
+};
+
+namespace mgr {
+
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+void count_launch();
+
+// Kernel launchers (mgr_fo2.cu).  All enqueue on model->stream.
+cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps);
+cudaError_t launch_fo2(MgrModel* model, int precision, double* J, double* u, double* lam);
+cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
+                                uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
+                                double* d_dZ);
+cudaError_t launch_line_tables(MgrModel* model);
+cudaError_t launch_ray_lengths(MgrModel* model, uint32_t* d_max_len);
+cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats);
+
+}  // namespace mgr

@@ -1,0 +1,322 @@
+"""Seeded synthetic Magritte models for the formal-solve workloads.
+
+No public dataset is involved: every model is generated from a seed with the
+shapes, sizes and value distributions of the workload it stands for.  A model is
+a ``RawModel``: exactly the fields a Magritte user sets through the Python API
+before calling ``compute_spectral_discretisation`` (positions, velocities as
+v/c, neighbour lists, boundary, rays, abundances, temperature, turbulence, line
+data, quadrature).  ``magritte_gb300.core.Model.from_raw`` loads one into the
+host model.
+
+Workloads:
+  * ``grid_cube``       -- 20^3 Cartesian grid, 26-neighbour lists, 12 HEALPix
+                           rays, 2-level CO-like line, nquads 11 (8000 points).
+  * ``grid_sphere``     -- 64^3 grid with a spherical cutout of radius half the
+                           box (rays of uneven length), 48 rays, 5-level linear
+                           rotor (4 lines), nquads 31.
+  * ``single_ray_1d``   -- the reference's 1D single-ray known-answer models
+                           (tests/benchmarks/analytic/all_constant_single_ray.py,
+                           all_zero_single_ray.py).
+The molecular mass of the CO-like species is not fixed by the workload
+descriptions; 28 amu is used throughout.
+"""
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import healpix
+
+# Physical constants, identical to src/tools/constants.hpp:15-40 of the reference.
+CC = 2.99792458e8
+HH = 6.62607004e-34
+KB = 1.38064852e-23
+AMU = 1.66053904e-27
+T_CMB = 2.7254800
+
+BC_ZERO, BC_THERMAL, BC_CMB = 0, 1, 2
+
+
+@dataclass
+class CollisionPartner:
+    num_col_partner: int
+    orth_or_para_H2: str
+    icol: np.ndarray
+    jcol: np.ndarray
+    tmp: np.ndarray
+    Cd: np.ndarray  # [ntmp][ncol] de-excitation rates [m^3/s]
+    Ce: np.ndarray  # [ntmp][ncol] excitation rates
+
+    @property
+    def ncol(self):
+        return len(self.icol)
+
+    @property
+    def ntmp(self):
+        return len(self.tmp)
+
+
+@dataclass
+class Linedata:
+    """Line data of one line-producing species (src/model/lines/lineProducingSpecies/
+    linedata/linedata.hpp:10-39)."""
+    num: int
+    sym: str
+    inverse_mass: float
+    energy: np.ndarray
+    weight: np.ndarray
+    irad: np.ndarray
+    jrad: np.ndarray
+    A: np.ndarray
+    colpar: List[CollisionPartner] = field(default_factory=list)
+
+    @property
+    def nlev(self):
+        return len(self.energy)
+
+    @property
+    def nrad(self):
+        return len(self.irad)
+
+    @property
+    def frequency(self):
+        return (self.energy[self.irad] - self.energy[self.jrad]) / HH
+
+    @property
+    def Bs(self):
+        f = self.frequency
+        return self.A * CC**2 / (2.0 * HH * f**3)
+
+    @property
+    def Ba(self):
+        return self.weight[self.irad] / self.weight[self.jrad] * self.Bs
+
+
+@dataclass
+class RawModel:
+    name: str
+    dimension: int
+    position: np.ndarray           # [P,3] m
+    velocity: np.ndarray           # [P,3] v/c
+    neighbors: np.ndarray          # flat CSR column indices
+    n_neighbors: np.ndarray        # [P]
+    boundary2point: np.ndarray     # [B]
+    boundary_condition: np.ndarray  # [B] 0 Zero, 1 Thermal, 2 CMB
+    boundary_temperature: np.ndarray  # [B]
+    ray_direction: np.ndarray      # [nrays,3]
+    ray_weight: np.ndarray         # [nrays]
+    abundance: np.ndarray          # [P, nspecs] number densities
+    temperature: np.ndarray        # [P]
+    vturb2: np.ndarray             # [P] (v_turb/c)^2
+    linedata: List[Linedata]
+    quad_roots: List[np.ndarray]
+    quad_weights: List[np.ndarray]
+    nquads: int
+    spherical_symmetry: bool = False
+
+    @property
+    def npoints(self):
+        return self.position.shape[0]
+
+    @property
+    def nrays(self):
+        return self.ray_direction.shape[0]
+
+
+def quadrature(nquads: int):
+    """Gauss-Hermite roots and normalised weights (magritte/setup.py:480-503)."""
+    roots, weights = np.polynomial.hermite.hermgauss(nquads)
+    return roots, weights / np.sum(weights)
+
+
+def linear_rotor(nlev: int, B_hz: float, A10: float, mass_amu: float, num: int = 0,
+                 collider: int = 1, seed: int = 0, ntmp: int = 8) -> Linedata:
+    """Synthetic linear rotor: E_J = h B J(J+1), g_J = 2J+1, transitions J -> J-1
+    with A_ul scaling as nu^3 from ``A10``.  One collision partner with
+    de-excitation rates C0 (T/100)^alpha (seeded) and excitation rates from
+    detailed balance (magritte/setup.py:731-735)."""
+    J = np.arange(nlev, dtype=np.float64)
+    energy = HH * B_hz * J * (J + 1.0)
+    weight = 2.0 * J + 1.0
+    irad = np.arange(1, nlev, dtype=np.uint32)
+    jrad = irad - 1
+    nu = (energy[irad] - energy[jrad]) / HH
+    A = A10 * (nu / nu[0]) ** 3
+    rng = np.random.default_rng(seed)
+    pairs = [(i, j) for i in range(1, nlev) for j in range(i)]
+    icol = np.array([p[0] for p in pairs], dtype=np.uint32)
+    jcol = np.array([p[1] for p in pairs], dtype=np.uint32)
+    tmp = np.geomspace(10.0, 1000.0, ntmp)
+    C0 = 10.0 ** rng.uniform(-17.0, -16.0, size=len(pairs))  # m^3/s
+    alpha = rng.uniform(0.0, 0.5, size=len(pairs))
+    Cd = np.array([C0 * (t / 100.0) ** alpha for t in tmp])
+    Ce = np.array([[Cd[t][k] * weight[icol[k]] / weight[jcol[k]]
+                    * np.exp(-(energy[icol[k]] - energy[jcol[k]]) / (KB * tmp[t]))
+                    for k in range(len(pairs))] for t in range(len(tmp))])
+    cp = CollisionPartner(collider, "n", icol, jcol, tmp, Cd, Ce)
+    return Linedata(num=num, sym="rotor", inverse_mass=1.0 / mass_amu, energy=energy, weight=weight,
+                    irad=irad, jrad=jrad, A=A, colpar=[cp])
+
+
+def two_level(nu_hz: float, A: float, g_ratio: float, mass_amu: float, num: int = 0,
+              collider: int = 1) -> Linedata:
+    """Two-level species with E_u = h nu, g_u/g_l = g_ratio."""
+    energy = np.array([0.0, HH * nu_hz])
+    weight = np.array([1.0, g_ratio])
+    irad = np.array([1], dtype=np.uint32)
+    jrad = np.array([0], dtype=np.uint32)
+    tmp = np.array([20.0])
+    Cd = np.array([[2.0e-16]])
+    Ce = np.array([[Cd[0][0] * weight[1] / weight[0] * np.exp(-energy[1] / (KB * tmp[0]))]])
+    cp = CollisionPartner(collider, "n", np.array([1], dtype=np.uint32), np.array([0], dtype=np.uint32),
+                          tmp, Cd, Ce)
+    return Linedata(num=num, sym="2lev", inverse_mass=1.0 / mass_amu, energy=energy, weight=weight,
+                    irad=irad, jrad=jrad, A=np.array([A]), colpar=[cp])
+
+
+def lamda_test_species() -> Linedata:
+    """The reference's fictitious 'test' species (tests/data/test.txt): 2 levels,
+    E = 0 and 6 cm^-1, g = 1 and 3, A = 1e-4 /s, molecular weight 1, one H2
+    collision rate 2e-10 cm^3/s at 20 K.  Energies are converted from cm^-1 to J
+    as the LAMDA reader does (magritte/setup.py:650-660: E[J] = E[cm^-1] * 100 h c)."""
+    energy = np.array([0.0, 6.0]) * 1.0e2 * HH * CC
+    weight = np.array([1.0, 3.0])
+    irad = np.array([1], dtype=np.uint32)
+    jrad = np.array([0], dtype=np.uint32)
+    tmp = np.array([20.0])
+    Cd = np.array([[2.0e-10 * 1.0e-6]])
+    Ce = np.array([[Cd[0][0] * weight[1] / weight[0] * np.exp(-(energy[1] - energy[0]) / (KB * tmp[0]))]])
+    cp = CollisionPartner(1, "n", np.array([1], dtype=np.uint32), np.array([0], dtype=np.uint32), tmp, Cd, Ce)
+    return Linedata(num=0, sym="test", inverse_mass=1.0, energy=energy, weight=weight, irad=irad,
+                    jrad=jrad, A=np.array([1.0e-4]), colpar=[cp])
+
+
+# --------------------------------------------------------------------------
+# Geometry builders
+# --------------------------------------------------------------------------
+_OFFSETS26 = [(dx, dy, dz) for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)
+              if (dx, dy, dz) != (0, 0, 0)]
+
+
+def grid_neighbors(keep: np.ndarray):
+    """26-neighbour CSR lists on an n^3 grid restricted to ``keep`` (bool [n,n,n]).
+    Point order: x fastest, then y, then z.  Neighbour order: offsets (dx, dy, dz)
+    in lexicographic order over {-1,0,1}^3.  Returns (index map, neighbors,
+    n_neighbors, full_mask) where full_mask marks points with all 26 neighbours."""
+    n = keep.shape[0]
+    idx = -np.ones(keep.shape, dtype=np.int64)
+    kz, ky, kx = np.nonzero(keep.transpose(2, 1, 0))  # order: x fastest
+    pts = np.stack([kx, ky, kz], axis=1)
+    idx[pts[:, 0], pts[:, 1], pts[:, 2]] = np.arange(len(pts))
+    nbs = []
+    counts = np.zeros(len(pts), dtype=np.uint32)
+    for off in _OFFSETS26:
+        q = pts + np.array(off)
+        ok = np.all((q >= 0) & (q < n), axis=1)
+        nb = np.full(len(pts), -1, dtype=np.int64)
+        nb[ok] = idx[q[ok, 0], q[ok, 1], q[ok, 2]]
+        nbs.append(nb)
+    nbs = np.stack(nbs, axis=1)  # [P, 26]
+    valid = nbs >= 0
+    counts = valid.sum(axis=1).astype(np.uint32)
+    flat = nbs[valid].astype(np.uint32)  # row-major keeps offset order per point
+    full = counts == 26
+    return pts, flat, counts, full
+
+
+def grid_cube(n: int = 20, box: float = 1.0e13, nside: int = 1, nquads: int = 11, seed: int = 0,
+              n_h2: float = 1.0e12, abundance: float = 1.0e-4, t_range=(20.0, 100.0),
+              v_turb: float = 150.0, sigma_v: float = 1.0e3) -> RawModel:
+    """Cartesian n^3 grid in a cube of side ``box``; surface points are CMB
+    boundaries; T ~ U(t_range); velocity i.i.d. Gaussian per component."""
+    rng = np.random.default_rng(seed)
+    keep = np.ones((n, n, n), dtype=bool)
+    pts, nbs, counts, full = grid_neighbors(keep)
+    dx = box / (n - 1)
+    position = pts.astype(np.float64) * dx
+    P = len(pts)
+    on_surface = np.any((pts == 0) | (pts == n - 1), axis=1)
+    b2p = np.nonzero(on_surface)[0].astype(np.uint32)
+    temperature = rng.uniform(t_range[0], t_range[1], size=P)
+    velocity = rng.normal(0.0, sigma_v, size=(P, 3)) / CC
+    direction, weight = healpix.uniform_rays(12 * nside * nside)
+    ld = two_level(1.1527e11, 7.2e-8, 3.0, 28.0)
+    roots, wts = quadrature(nquads)
+    abund = np.stack([np.full(P, n_h2 * abundance), np.full(P, n_h2)], axis=1)
+    return RawModel(
+        name=f"grid_cube_{n}", dimension=3, position=position, velocity=velocity, neighbors=nbs,
+        n_neighbors=counts, boundary2point=b2p, boundary_condition=np.full(len(b2p), BC_CMB, np.int32),
+        boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
+        abundance=abund, temperature=temperature, vturb2=np.full(P, (v_turb / CC) ** 2),
+        linedata=[ld], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
+
+
+def grid_sphere(n: int = 64, box: float = 1.0e13, nside: int = 2, nquads: int = 31, nlev: int = 5,
+                seed: int = 0, n_h2: float = 1.0e12, abundance: float = 1.0e-4, t0: float = 300.0,
+                v_in: float = 5.0e3, v_out: float = 15.0e3, sigma_v: float = 0.5e3,
+                v_turb: float = 150.0) -> RawModel:
+    """n^3 grid cut to the sphere of radius box/2 about the box centre; points
+    missing any of their 26 neighbours are CMB boundaries.  T = t0 (r/dx)^-0.5
+    (t0 inside one cell), radial velocity rising linearly from v_in at the centre
+    to v_out at the edge plus Gaussian noise, a 5-level linear rotor with
+    B = 57.6 GHz."""
+    rng = np.random.default_rng(seed)
+    dx = box / (n - 1)
+    g = np.arange(n, dtype=np.float64)
+    c = 0.5 * (n - 1)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    r_cells = np.sqrt((X - c) ** 2 + (Y - c) ** 2 + (Z - c) ** 2)
+    keep = r_cells <= 0.5 * (n - 1)
+    pts, nbs, counts, full = grid_neighbors(keep)
+    position = pts.astype(np.float64) * dx
+    P = len(pts)
+    b2p = np.nonzero(~full)[0].astype(np.uint32)
+    rel = (pts - c) * dx
+    r = np.sqrt(np.sum(rel * rel, axis=1))
+    rmax = 0.5 * (n - 1) * dx
+    temperature = t0 * np.maximum(r / dx, 1.0) ** -0.5
+    rhat = np.zeros_like(rel)
+    nz = r > 0
+    rhat[nz] = rel[nz] / r[nz, None]
+    vr = v_in + (v_out - v_in) * (r / rmax)
+    velocity = (vr[:, None] * rhat + rng.normal(0.0, sigma_v, size=(P, 3))) / CC
+    direction, weight = healpix.uniform_rays(12 * nside * nside)
+    ld = linear_rotor(nlev, 57.6e9, 7.2e-8, 28.0, seed=seed)
+    roots, wts = quadrature(nquads)
+    abund = np.stack([np.full(P, n_h2 * abundance), np.full(P, n_h2)], axis=1)
+    return RawModel(
+        name=f"grid_sphere_{n}", dimension=3, position=position, velocity=velocity, neighbors=nbs,
+        n_neighbors=counts, boundary2point=b2p, boundary_condition=np.full(len(b2p), BC_CMB, np.int32),
+        boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
+        abundance=abund, temperature=temperature, vturb2=np.full(P, (v_turb / CC) ** 2),
+        linedata=[ld], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
+
+
+def single_ray_1d(npoints: int = 50, dx: float = 1.0e12, nTT: float = 1.0e3, nH2: float = 1.0e12,
+                  temp: float = 4.5, turb: float = 0.0, dv: float = 0.0, nquads: int = 1,
+                  bc: int = BC_CMB) -> RawModel:
+    """The 1D single-ray models of the reference's analytic benchmarks
+    (tests/benchmarks/analytic/all_constant_single_ray.py:17-67): points on the x
+    axis, Delaunay neighbours in 1D (previous/next point, magritte/setup.py:60-70),
+    the two end points as boundary, rays [-1,0,0] and [1,0,0]."""
+    position = np.array([[i * dx, 0.0, 0.0] for i in range(npoints)])
+    velocity = np.array([[i * dv, 0.0, 0.0] for i in range(npoints)])
+    nbs = [1]
+    n_nbs = [1]
+    for p in range(1, npoints - 1):
+        nbs.extend([p - 1, p + 1])
+        n_nbs.append(2)
+    nbs.append(npoints - 2)
+    n_nbs.append(1)
+    b2p = np.array([0, npoints - 1], dtype=np.uint32)
+    direction = np.array([[-1.0, 0.0, 0.0], [1.0, 0.0, 0.0]])
+    weight = np.array([0.5, 0.5])
+    roots, wts = quadrature(nquads)
+    abund = np.array([[nTT, nH2, 0.0] for _ in range(npoints)])
+    return RawModel(
+        name="single_ray_1d", dimension=1, position=position, velocity=velocity,
+        neighbors=np.array(nbs, dtype=np.uint32), n_neighbors=np.array(n_nbs, dtype=np.uint32),
+        boundary2point=b2p, boundary_condition=np.full(2, bc, np.int32),
+        boundary_temperature=np.full(2, T_CMB), ray_direction=direction, ray_weight=weight,
+        abundance=abund, temperature=np.full(npoints, temp), vturb2=np.full(npoints, (turb / CC) ** 2),
+        linedata=[lamda_test_species()], quad_roots=[roots], quad_weights=[wts], nquads=nquads)

@@ -1,0 +1,916 @@
+/*
+ * Oracle for the Magritte formal-solve hot path -- TEST INFRASTRUCTURE ONLY.
+ * See mgr_oracle.h.  Every function cites the reference statement it restates
+ * (paths relative to the Magritte 0.9.3 source tree).
+ *
+ * Build: -O2 -ffp-contract=off -fopenmp (oracle/Makefile).  The -ffp-contract=off
+ * matters: the reference is compiled for x86-64 without FMA, so a*b+c rounds twice.
+ */
+#include "mgr_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* src/tools/constants.hpp:15-40 */
+#define ORC_PI 3.14159265358979323846
+static const double INVERSE_SQRT_PI            = 0.5 * 1.12837916709551257390; /* 0.5*M_2_SQRTPI */
+static const double CC                         = 2.99792458E+8;
+static const double HH                         = 6.62607004E-34;
+static const double KB                         = 1.38064852E-23;
+static const double AMU                        = 1.66053904E-27;
+static const double T_CMB                      = 2.7254800;
+static const double CC_SQUARED                 = 8.98755179E+16;
+#define TWO_KB_OVER_AMU_CC_SQUARED (2.0 * KB / (AMU * CC_SQUARED))
+#define TWO_HH_OVER_CC_SQUARED     (2.0 * HH / CC_SQUARED)
+#define HH_OVER_KB                 (HH / KB)
+
+/* ------------------------------------------------------------------ */
+/* Per-thread solver buffers, Solver::setup (solver.tpp:32-77).        */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    uint32_t length, centre;
+    uint32_t *nr, *nr_interp;
+    double *interp_factor, *shift, *dZ;
+    double *Su, *A, *C, *inverse_A, *inverse_C, *FF, *FI, *GG, *GP, *L_diag;
+    uint32_t first, last, n_tot;
+} Buf;
+
+static int buf_init(Buf* b, uint32_t length) {
+    memset(b, 0, sizeof(*b));
+    b->length        = length;
+    b->centre        = length / 2;
+    b->nr            = (uint32_t*)calloc(length, sizeof(uint32_t));
+    b->nr_interp     = (uint32_t*)calloc(length, sizeof(uint32_t));
+    b->interp_factor = (double*)calloc(length, sizeof(double));
+    b->shift         = (double*)calloc(length, sizeof(double));
+    b->dZ            = (double*)calloc(length, sizeof(double));
+    b->Su            = (double*)calloc(length, sizeof(double));
+    b->A             = (double*)calloc(length, sizeof(double));
+    b->C             = (double*)calloc(length, sizeof(double));
+    b->inverse_A     = (double*)calloc(length, sizeof(double));
+    b->inverse_C     = (double*)calloc(length, sizeof(double));
+    b->FF            = (double*)calloc(length, sizeof(double));
+    b->FI            = (double*)calloc(length, sizeof(double));
+    b->GG            = (double*)calloc(length, sizeof(double));
+    b->GP            = (double*)calloc(length, sizeof(double));
+    b->L_diag        = (double*)calloc(length, sizeof(double));
+    return (b->nr && b->nr_interp && b->interp_factor && b->shift && b->dZ && b->Su && b->A
+               && b->C && b->inverse_A && b->inverse_C && b->FF && b->FI && b->GG && b->GP
+               && b->L_diag)
+             ? 0
+             : -1;
+}
+
+static void buf_free(Buf* b) {
+    free(b->nr); free(b->nr_interp); free(b->interp_factor); free(b->shift); free(b->dZ);
+    free(b->Su); free(b->A); free(b->C); free(b->inverse_A); free(b->inverse_C);
+    free(b->FF); free(b->FI); free(b->GG); free(b->GP); free(b->L_diag);
+}
+
+/* ------------------------------------------------------------------ */
+/* Geometry                                                            */
+/* ------------------------------------------------------------------ */
+
+/* Vector3D::dot, summed x, y, z left to right. */
+static inline double dot3(double ax, double ay, double az, const double* b) {
+    return ax * b[0] + ay * b[1] + az * b[2];
+}
+
+/* Geometry::get_next_general_geometry<Defaulttracer> (geometry.tpp:13-44). */
+static uint32_t get_next(const OrcModel* m, const double* origin, const double* raydir,
+                         uint32_t c, double* Z, double* dZ) {
+    const uint32_t n_nbs     = m->n_neighbors[c];
+    const uint32_t cum_n_nbs = m->cum_n_neighbors[c];
+    double dmin              = DBL_MAX;
+    uint32_t next            = m->npoints;
+    for (uint32_t i = 0; i < n_nbs; i++) {
+        const uint32_t n   = m->neighbors[cum_n_nbs + i];
+        const double Rx    = m->position[3 * n + 0] - origin[0];
+        const double Ry    = m->position[3 * n + 1] - origin[1];
+        const double Rz    = m->position[3 * n + 2] - origin[2];
+        const double Z_new = dot3(Rx, Ry, Rz, raydir);
+        if (Z_new > *Z) {
+            const double RR                 = Rx * Rx + Ry * Ry + Rz * Rz;
+            const double distance_from_ray2 = RR - Z_new * Z_new;
+            if (distance_from_ray2 < dmin) {
+                dmin  = distance_from_ray2;
+                next  = n;
+                *dZ   = Z_new - *Z;
+            }
+        }
+    }
+    *Z += *dZ;
+    return next;
+}
+
+/* Geometry::get_shift_general_geometry<CoMoving|Rest> (geometry.tpp:203-221) and the
+ * reversal for the old imager (geometry.tpp:428-465).  frame: 0 CoMoving, 1 Rest. */
+static inline double get_shift(const OrcModel* m, int frame, uint32_t o, uint32_t r, uint32_t c) {
+    const double* d = m->ray_direction + 3 * r;
+    double shift;
+    if (frame == 0) {
+        const double vx = m->velocity[3 * c + 0] - m->velocity[3 * o + 0];
+        const double vy = m->velocity[3 * c + 1] - m->velocity[3 * o + 1];
+        const double vz = m->velocity[3 * c + 2] - m->velocity[3 * o + 2];
+        shift           = 1.0 + dot3(vx, vy, vz, d);
+    } else {
+        shift = 1.0 + dot3(m->velocity[3 * c + 0], m->velocity[3 * c + 1], m->velocity[3 * c + 2], d);
+        if (r >= m->hnrays) shift = 2.0 - shift;
+    }
+    return shift;
+}
+
+static inline int valid_point(const OrcModel* m, uint32_t p) { return p < m->npoints; }
+static inline int not_on_boundary(const OrcModel* m, uint32_t p) {
+    return m->point2boundary[p] == m->npoints;
+}
+
+/* ------------------------------------------------------------------ */
+/* InterpHelper (solver_interp_helper.tpp)                             */
+/* ------------------------------------------------------------------ */
+
+/* get_n_interp_for_line (solver_interp_helper.tpp:55-75). */
+static inline uint32_t get_n_interp_for_line(const OrcModel* m, uint32_t l, uint32_t crt, uint32_t nxt) {
+    const double curr_source = m->interp_criterion[(size_t)crt * m->nlines + l];
+    const double next_source = m->interp_criterion[(size_t)nxt * m->nlines + l];
+    const double source_diff = fabsf(logf((float)(next_source / curr_source)));
+    const double q           = source_diff / (double)logf((float)m->max_interpolation_diff);
+    const uint32_t n         = (uint32_t)ceil(q);
+    return n > 1 ? n : 1;
+}
+
+/* get_n_interp, over all lines (solver_interp_helper.tpp:10-46). */
+static inline uint32_t get_n_interp(const OrcModel* m, uint32_t crt, uint32_t nxt) {
+    double mx = -DBL_MAX;
+    for (uint32_t l = 0; l < m->nlines; l++) {
+        const double x = m->interp_criterion[(size_t)nxt * m->nlines + l];
+        const double y = m->interp_criterion[(size_t)crt * m->nlines + l];
+        const double d = fabsf(logf((float)(x / y)));
+        if (d > mx) mx = d;
+    }
+    const uint32_t n = (uint32_t)ceil(mx / (double)logf((float)m->max_interpolation_diff));
+    return n > 1 ? n : 1;
+}
+
+/* interpolate_linear / interpolate_log (solver_interp_helper.tpp:78-99). */
+static inline double interpolate_linear(double f_start, double f_end, double factor) {
+    if (factor == 0.0) return f_start;
+    if (factor == 1.0) return f_end;
+    return (f_end - f_start) * factor + f_start;
+}
+static inline double interpolate_log(double f_start, double f_end, double factor) {
+    if (factor == 0.0) return f_start;
+    if (factor == 1.0) return f_end;
+    return f_start * (double)powf((float)(f_end / f_start), (float)factor);
+}
+
+/* ------------------------------------------------------------------ */
+/* Ray tracing (solver.tpp:741-800, :1003-1097)                         */
+/* ------------------------------------------------------------------ */
+
+/* Solver::set_data / set_data_for_line; line = UINT32_MAX selects get_n_interp. */
+static void set_data(const OrcModel* m, Buf* b, uint32_t line, uint32_t crt, uint32_t nxt,
+                     double shift_crt, double shift_nxt, double dZ_loc, int increment,
+                     int64_t* id1, int64_t* id2, int* overflow) {
+    const double dshift = shift_nxt - shift_crt;
+    const uint32_t n_interp_points =
+        (line == UINT32_MAX) ? get_n_interp(m, crt, nxt) : get_n_interp_for_line(m, line, crt, nxt);
+    if (n_interp_points > 1) {
+        const double dZ_interpl     = dZ_loc / n_interp_points;
+        const double dshift_interpl = dshift / n_interp_points;
+        for (uint32_t i = 1; i <= n_interp_points; i++) {
+            if (*id1 < 0 || *id1 >= (int64_t)b->length || *id2 < 0 || *id2 >= (int64_t)b->length) {
+                *overflow = 1;
+                return;
+            }
+            b->nr[*id1]            = nxt;
+            b->shift[*id1]         = shift_crt + i * dshift_interpl;
+            b->nr_interp[*id1]     = crt;
+            b->interp_factor[*id1] = 1.0 - ((double)i) / n_interp_points;
+            b->dZ[*id2]            = dZ_interpl;
+            *id1 += increment;
+            *id2 += increment;
+        }
+    } else {
+        if (*id1 < 0 || *id1 >= (int64_t)b->length || *id2 < 0 || *id2 >= (int64_t)b->length) {
+            *overflow = 1;
+            return;
+        }
+        b->nr[*id1]            = nxt;
+        b->shift[*id1]         = shift_nxt;
+        b->nr_interp[*id1]     = crt;
+        b->interp_factor[*id1] = 0.0;
+        b->dZ[*id2]            = dZ_loc;
+        *id1 += increment;
+        *id2 += increment;
+    }
+}
+
+/* Solver::trace_ray_for_line (solver.tpp:773-800) / trace_ray (:741-768).
+ * frame 0 CoMoving, 1 Rest.  Returns the final id1. */
+static int64_t trace(const OrcModel* m, Buf* b, int frame, uint32_t line, uint32_t o, uint32_t r,
+                     int increment, int64_t id1, int64_t id2, int* err) {
+    double Z               = 0.0;
+    double dZ              = 0.0;
+    const double* origin   = m->position + 3 * o;
+    const double* raydir   = m->ray_direction + 3 * r;
+    uint32_t nxt           = get_next(m, origin, raydir, o, &Z, &dZ);
+    if (valid_point(m, nxt)) {
+        uint32_t crt     = o;
+        double shift_crt = get_shift(m, frame, o, r, crt);
+        double shift_nxt = get_shift(m, frame, o, r, nxt);
+        set_data(m, b, line, crt, nxt, shift_crt, shift_nxt, dZ, increment, &id1, &id2, err);
+        while (!*err && not_on_boundary(m, nxt)) {
+            crt       = nxt;
+            shift_crt = shift_nxt;
+            nxt       = get_next(m, origin, raydir, nxt, &Z, &dZ);
+            if (!valid_point(m, nxt)) { /* reference would read past point2boundary */
+                *err = 2;
+                break;
+            }
+            shift_nxt = get_shift(m, frame, o, r, nxt);
+            set_data(m, b, line, crt, nxt, shift_crt, shift_nxt, dZ, increment, &id1, &id2, err);
+        }
+    }
+    return id1;
+}
+
+/* Solver::get_ray_length (solver.tpp:79-103). */
+static uint32_t get_ray_length(const OrcModel* m, uint32_t o, uint32_t r) {
+    uint32_t l           = 0;
+    double Z             = 0.0;
+    double dZ            = 0.0;
+    const double* origin = m->position + 3 * o;
+    const double* raydir = m->ray_direction + 3 * r;
+    uint32_t nxt         = get_next(m, origin, raydir, o, &Z, &dZ);
+    if (valid_point(m, nxt)) {
+        uint32_t crt = o;
+        l += get_n_interp(m, crt, nxt);
+        while (not_on_boundary(m, nxt)) {
+            crt = nxt;
+            nxt = get_next(m, origin, raydir, nxt, &Z, &dZ);
+            if (!valid_point(m, nxt)) break;
+            l += get_n_interp(m, crt, nxt);
+        }
+    }
+    return l;
+}
+
+uint32_t orc_ray_lengths_max(const OrcModel* m, int nthreads) {
+    uint32_t mx = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    for (uint32_t rr = 0; rr < m->hnrays; rr++) {
+        const uint32_t ar = m->antipod[rr];
+#pragma omp parallel for reduction(max : mx) schedule(dynamic, 64)
+        for (int64_t o = 0; o < (int64_t)m->npoints; o++) {
+            const uint32_t len = get_ray_length(m, (uint32_t)o, rr) + get_ray_length(m, (uint32_t)o, ar);
+            if (len > mx) mx = len;
+        }
+    }
+    return mx;
+}
+
+/* ------------------------------------------------------------------ */
+/* Line data, profiles, boundary (solver.tpp:1106-1351)                */
+/* ------------------------------------------------------------------ */
+
+/* Solver::gaussian (solver.tpp:1106-1110). */
+static inline double gaussian(double inverse_width, double diff) {
+    const double sqrt_exp = inverse_width * diff;
+    return inverse_width * INVERSE_SQRT_PI * (double)expf((float)(-sqrt_exp * sqrt_exp));
+}
+
+/* Solver::planck (solver.tpp:1119-1121). */
+static inline double planck(double temp, double freq) {
+    return TWO_HH_OVER_CC_SQUARED * (freq * freq * freq) / (double)expm1f((float)(HH_OVER_KB * freq / temp));
+}
+
+/* Solver::boundary_intensity (solver.tpp:1130-1142). */
+static inline double boundary_intensity(const OrcModel* m, uint32_t p, double freq) {
+    const uint32_t bdy_id = m->point2boundary[p];
+    if (bdy_id >= m->nboundary) return 0.0; /* interior point: no boundary condition */
+    switch (m->boundary_condition[bdy_id]) {
+    case ORC_BC_ZERO: return 0.0;
+    case ORC_BC_THERMAL: return planck(m->boundary_temperature[bdy_id], freq);
+    default: return planck(T_CMB, freq);
+    }
+}
+
+/* Thermodynamics::profile_width_upper_bound_with_linefreq (thermodynamics.tpp:42-53). */
+static inline double upper_bound_width(const OrcModel* m, uint32_t p, double freq_line) {
+    return freq_line * sqrt(TWO_KB_OVER_AMU_CC_SQUARED * m->max_inverse_mass * m->temperature[p] + m->vturb2[p]);
+}
+
+/* Thermodynamics::profile (thermodynamics.tpp:8-35). */
+static inline double thermo_profile(const OrcModel* m, double inverse_mass, uint32_t p,
+                                    double freq_line, double freq) {
+    const double width = freq_line * sqrt(TWO_KB_OVER_AMU_CC_SQUARED * inverse_mass * m->temperature[p] + m->vturb2[p]);
+    const double inverse_width = 1.0 / width;
+    const double sqrtExponent  = inverse_width * (freq - freq_line);
+    const double exponent      = sqrtExponent * sqrtExponent;
+    return inverse_width * INVERSE_SQRT_PI * (double)expf((float)(-exponent));
+}
+
+/* std::lower_bound / std::upper_bound over sorted_line. */
+static inline uint32_t lower_bound(const double* a, uint32_t n, double v) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (a[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+static inline uint32_t upper_bound(const double* a, uint32_t n, double v) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (!(v < a[mid])) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+#define EM(p, l) m->emissivity[(size_t)(p) * m->nlines + (l)]
+#define OP(p, l) m->opacity[(size_t)(p) * m->nlines + (l)]
+#define IW(p, l) m->inverse_width[(size_t)(p) * m->nlines + (l)]
+
+/* Solver::get_eta_and_chi<None|CloseLines|OneLine> (solver.tpp:1151-1165, :1197-1239, :1286-1294). */
+static void get_eta_and_chi(const OrcModel* m, uint32_t p, uint32_t ll, double freq, double* eta, double* chi) {
+    if (m->approx == ORC_ONELINE) {
+        const double diff = freq - m->line[ll];
+        const double prof = gaussian(IW(p, ll), diff);
+        *eta              = prof * EM(p, ll);
+        *chi              = prof * OP(p, ll) + m->min_opacity;
+        return;
+    }
+    *eta = 0.0;
+    *chi = m->min_opacity;
+    if (m->approx == ORC_NONE) {
+        for (uint32_t l = 0; l < m->nlines; l++) {
+            const double diff = freq - m->line[l];
+            const double prof = gaussian(IW(p, l), diff);
+            *eta += prof * EM(p, l);
+            *chi += prof * OP(p, l);
+        }
+        return;
+    }
+    const double ub = m->max_distance_opacity_contribution * upper_bound_width(m, p, freq);
+    const uint32_t lo = lower_bound(m->sorted_line, m->nlines, freq - ub);
+    const uint32_t hi = upper_bound(m->sorted_line, m->nlines, freq + ub);
+    for (uint32_t s = lo; s < hi; s++) {
+        const uint32_t l  = m->sorted_line_map[s];
+        const double diff = freq - m->sorted_line[s];
+        const double prof = gaussian(IW(p, l), diff);
+        *eta += prof * EM(p, l);
+        *chi += prof * OP(p, l);
+    }
+}
+
+/* Solver::get_eta_and_chi_interpolated<None|CloseLines|OneLine> (solver.tpp:1176-1194, :1252-1283, :1306-1320). */
+static void get_eta_and_chi_interpolated(const OrcModel* m, uint32_t p1, uint32_t p2, double factor,
+                                         uint32_t ll, double freq, double* eta, double* chi) {
+    if (m->approx == ORC_ONELINE) {
+        const double diff = freq - m->line[ll];
+        const double iw   = interpolate_linear(IW(p1, ll), IW(p2, ll), factor);
+        const double prof = gaussian(iw, diff);
+        const double ie   = interpolate_log(EM(p1, ll), EM(p2, ll), factor);
+        const double io   = interpolate_log(OP(p1, ll), OP(p2, ll), factor);
+        *eta              = prof * ie;
+        *chi              = prof * io + m->min_opacity;
+        return;
+    }
+    *eta = 0.0;
+    *chi = m->min_opacity;
+    uint32_t lo = 0, hi = m->nlines;
+    if (m->approx == ORC_CLOSELINES) {
+        const double ub = m->max_distance_opacity_contribution * upper_bound_width(m, p1, freq);
+        lo              = lower_bound(m->sorted_line, m->nlines, freq - ub);
+        hi              = upper_bound(m->sorted_line, m->nlines, freq + ub);
+    }
+    for (uint32_t s = lo; s < hi; s++) {
+        uint32_t l;
+        double diff;
+        if (m->approx == ORC_CLOSELINES) {
+            l    = m->sorted_line_map[s];
+            diff = freq - m->sorted_line[s];
+        } else {
+            l    = s;
+            diff = freq - m->line[l];
+        }
+        const double iw   = interpolate_linear(IW(p1, l), IW(p2, l), factor);
+        const double prof = gaussian(iw, diff);
+        const double ie   = interpolate_log(EM(p1, l), EM(p2, l), factor);
+        const double io   = interpolate_log(OP(p1, l), OP(p2, l), factor);
+        *eta += prof * ie;
+        *chi += prof * io;
+    }
+}
+
+/* Solver::compute_dtau_single_line (solver.tpp:2374-2455). */
+static double compute_dtau_single_line(const OrcModel* m, uint32_t curridx, uint32_t nextidx,
+                                       uint32_t ci, uint32_t ni, uint32_t l, double curr_freq,
+                                       double next_freq, double curr_interp, double next_interp, double dz) {
+    const double linefreq = m->line[l];
+    const double iwc      = interpolate_linear(IW(curridx, l), IW(ci, l), curr_interp);
+    const double iwn      = interpolate_linear(IW(nextidx, l), IW(ni, l), next_interp);
+    const double avg_iw   = (iwc + iwn) / 2.0;
+    const double cop      = interpolate_log(OP(curridx, l), OP(ci, l), curr_interp);
+    const double nop      = interpolate_log(OP(nextidx, l), OP(ni, l), next_interp);
+    if (curr_freq == next_freq) {
+        const double diff            = curr_freq - m->line[l];
+        const double prof            = gaussian(avg_iw, diff);
+        const double average_opacity = (cop + nop) / 2.0;
+        return dz * (prof * average_opacity + m->min_opacity);
+    }
+    const double next_pos        = (linefreq - next_freq) * avg_iw;
+    const double curr_pos        = (linefreq - curr_freq) * avg_iw;
+    const double diff_pos        = next_pos - curr_pos;
+    const double average_opacity = (nop + cop) / 2.0;
+    const float  erfdiff         = erff((float)next_pos) - erff((float)curr_pos);
+    const double erfterm         = average_opacity / diff_pos / 2.0 * (double)erfdiff;
+    return dz * (avg_iw * erfterm + m->min_opacity);
+}
+
+/* Solver::compute_S_dtau_line_integrated<OneLine|None|CloseLines> (solver.tpp:1878-2111). */
+static void compute_S_dtau_line_integrated(const OrcModel* m, uint32_t cp, uint32_t np, uint32_t ci,
+                                           uint32_t ni, uint32_t lineidx, double currfreq,
+                                           double nextfreq, double curr_interp, double next_interp,
+                                           double dZ, double* dtau, double* Scurr, double* Snext) {
+    if (m->approx == ORC_ONELINE) {
+        const uint32_t l = lineidx;
+        *dtau = compute_dtau_single_line(m, cp, np, ci, ni, l, currfreq, nextfreq, curr_interp, next_interp, dZ);
+        const double Scp  = EM(cp, l) / OP(cp, l);
+        const double Snp  = EM(np, l) / OP(np, l);
+        const double Scip = EM(ci, l) / OP(ci, l);
+        const double Snip = EM(ni, l) / OP(ni, l);
+        *Scurr            = interpolate_log(Scp, Scip, curr_interp);
+        *Snext            = interpolate_log(Snp, Snip, next_interp);
+        return;
+    }
+    double sum_dtau = 0.0, sum_c = 0.0, sum_n = 0.0;
+    uint32_t lo = 0, hi = m->nlines;
+    if (m->approx == ORC_CLOSELINES) {
+        double left_freq, right_freq;
+        if (currfreq < nextfreq) { left_freq = currfreq; right_freq = nextfreq; }
+        else { right_freq = currfreq; left_freq = nextfreq; }
+        const double cb = m->max_distance_opacity_contribution * upper_bound_width(m, cp, right_freq);
+        const double nb = m->max_distance_opacity_contribution * upper_bound_width(m, np, right_freq);
+        const double ub = cb > nb ? cb : nb;
+        lo              = lower_bound(m->sorted_line, m->nlines, left_freq - ub);
+        hi              = upper_bound(m->sorted_line, m->nlines, right_freq + ub);
+    }
+    for (uint32_t s = lo; s < hi; s++) {
+        const uint32_t l = (m->approx == ORC_CLOSELINES) ? m->sorted_line_map[s] : s;
+        const double line_dtau =
+            compute_dtau_single_line(m, cp, np, ci, ni, l, currfreq, nextfreq, curr_interp, next_interp, dZ);
+        const double Scp  = EM(cp, l) / OP(cp, l);
+        const double Snp  = EM(np, l) / OP(np, l);
+        const double Scip = EM(ci, l) / OP(ci, l);
+        const double Snip = EM(ni, l) / OP(ni, l);
+        const double lsc  = interpolate_log(Scp, Scip, curr_interp);
+        const double lsn  = interpolate_log(Snp, Snip, next_interp);
+        sum_dtau += line_dtau;
+        sum_c += line_dtau * lsc;
+        sum_n += line_dtau * lsn;
+    }
+    if (m->approx == ORC_NONE) {
+        *dtau  = sum_dtau;
+        *Scurr = sum_c / sum_dtau;
+        *Snext = sum_n / sum_dtau;
+        return;
+    }
+    double d                    = sum_dtau;
+    const double bound_min_dtau = m->min_opacity * dZ;
+    if (-bound_min_dtau < d) d = (bound_min_dtau > d) ? bound_min_dtau : d;
+    *dtau  = d;
+    *Scurr = sum_c / d;
+    *Snext = sum_n / d;
+}
+
+/* Solver::compute_source_dtau (solver.tpp:2139-2186). */
+static void compute_source_dtau(const OrcModel* m, uint32_t cp, uint32_t np, uint32_t ci, uint32_t ni,
+                                uint32_t line, double curr_freq, double next_freq, double curr_shift,
+                                double next_shift, double dZ, double curr_interp, double next_interp,
+                                int* compute_curr_opacity, double* dtaunext, double* chicurr,
+                                double* chinext, double* Scurr, double* Snext) {
+    const double dshift     = next_shift - curr_shift;
+    const double dshift_abs = fabs(dshift);
+    const double dmc        = m->dshift_max[cp];
+    const double dmn        = m->dshift_max[np];
+    const double dshift_max = dmc < dmn ? dmc : dmn;
+    if (dshift_abs > dshift_max) {
+        *compute_curr_opacity = 1;
+        compute_S_dtau_line_integrated(m, cp, np, ci, ni, line, curr_freq, next_freq, curr_interp,
+                                       next_interp, dZ, dtaunext, Scurr, Snext);
+    } else {
+        if (*compute_curr_opacity) {
+            *compute_curr_opacity = 0;
+            double eta_c          = 0.0;
+            get_eta_and_chi_interpolated(m, cp, ci, curr_interp, line, curr_freq, &eta_c, chicurr);
+            *Scurr = eta_c / *chicurr;
+        }
+        double eta_n = 0.0;
+        get_eta_and_chi_interpolated(m, np, ni, next_interp, line, next_freq, &eta_n, chinext);
+        *Snext    = eta_n / *chinext;
+        *dtaunext = 0.5 * (*chicurr + *chinext) * dZ;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Feautrier (solver.tpp:2193-2318, n_off_diag == 0)                    */
+/* ------------------------------------------------------------------ */
+static void solve_feautrier_order_2(const OrcModel* m, Buf* b, uint32_t o, uint32_t f, int full_back) {
+    const double freq  = m->nu[(size_t)o * m->nfreqs + f];
+    const uint32_t l   = m->corr_line[f];
+    const uint32_t first = b->first, last = b->last, centre = b->centre;
+    double chi_c = 0.0, chi_n = 0.0, dtau_c, dtau_n = 0.0, term_c = 0.0, term_n = 0.0;
+    int cco = 1;
+    double* Su = b->Su; double* A = b->A; double* C = b->C; double* iA = b->inverse_A;
+    double* iC = b->inverse_C; double* FF = b->FF; double* FI = b->FI; double* GG = b->GG;
+    double* GP = b->GP;
+
+    compute_source_dtau(m, b->nr[first], b->nr[first + 1], b->nr_interp[first], b->nr_interp[first + 1], l,
+                        freq * b->shift[first], freq * b->shift[first + 1], b->shift[first],
+                        b->shift[first + 1], b->dZ[first], b->interp_factor[first],
+                        b->interp_factor[first + 1], &cco, &dtau_n, &chi_c, &chi_n, &term_c, &term_n);
+
+    const double inverse_dtau_f = 1.0 / dtau_n;
+    C[first]                    = 2.0 * inverse_dtau_f * inverse_dtau_f;
+    iC[first]                   = 1.0 / C[first];
+    const double Bf_min_Cf      = 1.0 + 2.0 * inverse_dtau_f;
+    const double Bf             = Bf_min_Cf + C[first];
+    const double I_bdy_f        = boundary_intensity(m, b->nr[first], freq * b->shift[first]);
+    Su[first]                   = term_c + 2.0 * I_bdy_f * inverse_dtau_f;
+    Su[first] /= Bf;
+    FF[first] = 0.5 * Bf_min_Cf * dtau_n * dtau_n;
+    FI[first] = 1.0 / (1.0 + FF[first]);
+
+    for (uint32_t n = first + 1; n < last; n++) {
+        term_c = term_n;
+        dtau_c = dtau_n;
+        chi_c  = chi_n;
+        compute_source_dtau(m, b->nr[n], b->nr[n + 1], b->nr_interp[n], b->nr_interp[n + 1], l,
+                            freq * b->shift[n], freq * b->shift[n + 1], b->shift[n], b->shift[n + 1],
+                            b->dZ[n], b->interp_factor[n], b->interp_factor[n + 1], &cco, &dtau_n,
+                            &chi_c, &chi_n, &term_c, &term_n);
+        const double dtau_avg = 0.5 * (dtau_c + dtau_n);
+        iA[n]                 = dtau_avg * dtau_c;
+        iC[n]                 = dtau_avg * dtau_n;
+        A[n]                  = 1.0 / iA[n];
+        C[n]                  = 1.0 / iC[n];
+        Su[n]                 = term_c;
+        FF[n]                 = (A[n] * FF[n - 1] * FI[n - 1] + 1.0) * iC[n];
+        FI[n]                 = 1.0 / (1.0 + FF[n]);
+        Su[n]                 = (A[n] * Su[n - 1] + Su[n]) * FI[n] * iC[n];
+    }
+
+    const double inverse_dtau_l = 1.0 / dtau_n;
+    A[last]                     = 2.0 * inverse_dtau_l * inverse_dtau_l;
+    const double Bl_min_Al      = 1.0 + 2.0 * inverse_dtau_l;
+    const double Bl             = Bl_min_Al + A[last];
+    const double denominator    = 1.0 / (Bl * FF[last - 1] + Bl_min_Al);
+    const double I_bdy_l        = boundary_intensity(m, b->nr[last], freq * b->shift[last]);
+    Su[last]                    = term_n + 2.0 * I_bdy_l * inverse_dtau_l;
+    Su[last]                    = (A[last] * Su[last - 1] + Su[last]) * (1.0 + FF[last - 1]) * denominator;
+
+    if (!full_back) return; /* imager: forward elimination only (solver.tpp:2462-2574) */
+
+    if (centre < last) {
+        GG[last] = 0.5 * Bl_min_Al * dtau_n * dtau_n;
+        GP[last] = GG[last] / (1.0 + GG[last]);
+        for (int64_t n = (int64_t)last - 1; n > (int64_t)centre; n--) {
+            Su[n] += Su[n + 1] * FI[n];
+            GG[n] = (C[n] * GP[n + 1] + 1.0) * iA[n];
+            GP[n] = GG[n] / (1.0 + GG[n]);
+        }
+        Su[centre] += Su[centre + 1] * FI[centre];
+        b->L_diag[centre] = iC[centre] / (FF[centre] + GP[centre + 1]);
+    } else {
+        b->L_diag[centre] = (1.0 + FF[centre - 1]) / (Bl_min_Al + Bl * FF[centre - 1]);
+    }
+}
+
+/* Solver::update_Lambda, n_off_diag == 0 (solver.tpp:1760-1800). */
+static void update_lambda(const OrcModel* m, Buf* b, uint32_t rr, uint32_t f, double* lambda_diag,
+                          uint8_t* lambda_has) {
+    if (!m->in_line_integral[f]) return;
+    const uint32_t c        = b->centre;
+    const uint32_t p        = b->nr[c];
+    const double w_ang      = 2.0 * m->ray_weight[rr];
+    const uint32_t ls       = m->corr_lspec[f];
+    const uint32_t k        = m->corr_k[f];
+    const uint32_t z        = m->corr_z[f];
+    const uint32_t lid      = m->nrad_cum[ls] + k;
+    const double freq_line  = m->line[lid];
+    const double invr_mass  = m->lspec_inverse_mass[ls];
+    const double constante  = m->line_A[lid] * m->quad_weights[(size_t)ls * m->nquads + z] * w_ang;
+    double eta, chi;
+    get_eta_and_chi(m, p, k, freq_line, &eta, &chi);
+    const double inverse_chi = 1.0 / chi;
+    const double frq         = m->nu[(size_t)p * m->nfreqs + f] * b->shift[c];
+    const double phi         = thermo_profile(m, invr_mass, p, freq_line, frq);
+    const double L           = constante * frq * phi * b->L_diag[c] * inverse_chi;
+    if (lambda_diag) lambda_diag[(size_t)p * m->nlines + lid] += L;
+    if (lambda_has) lambda_has[(size_t)p * m->nlines + lid] = 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* Public traces                                                       */
+/* ------------------------------------------------------------------ */
+int orc_trace_ray_pair_for_line(const OrcModel* m, uint32_t o, uint32_t rr, uint32_t l, OrcRay* ray) {
+    Buf b;
+    if (buf_init(&b, ray->capacity) != 0) return -1;
+    const uint32_t centre = b.centre;
+    const uint32_t ar     = m->antipod[rr];
+    int err               = 0;
+    b.nr[centre]          = o;
+    b.shift[centre]       = 1.0;
+    const int64_t first   = trace(m, &b, 0, l, o, rr, -1, (int64_t)centre - 1, (int64_t)centre - 1, &err) + 1;
+    const int64_t last    = trace(m, &b, 0, l, o, ar, +1, (int64_t)centre + 1, (int64_t)centre, &err) - 1;
+    ray->centre           = centre;
+    ray->first            = (uint32_t)first;
+    ray->last             = (uint32_t)last;
+    memcpy(ray->nr, b.nr, sizeof(uint32_t) * b.length);
+    memcpy(ray->nr_interp, b.nr_interp, sizeof(uint32_t) * b.length);
+    memcpy(ray->interp_factor, b.interp_factor, sizeof(double) * b.length);
+    memcpy(ray->shift, b.shift, sizeof(double) * b.length);
+    memcpy(ray->dZ, b.dZ, sizeof(double) * b.length);
+    buf_free(&b);
+    return err ? -2 : 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Formal solve driver (solver.tpp:458-540)                             */
+/* ------------------------------------------------------------------ */
+static int fo2_range(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0, uint32_t o1,
+                     double* J, double* u, double* lambda_diag, uint8_t* lambda_has, int nthreads) {
+    const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
+    const uint32_t P = m->npoints, F = m->nfreqs, Q = m->nquads;
+    int err_any = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+    {
+        Buf b;
+        int bad = buf_init(&b, length);
+        for (uint32_t rr = rr0; rr < rr1; rr++) {
+            const uint32_t ar = m->antipod[rr];
+            for (uint32_t ls = 0; ls < m->nlspecs; ls++) {
+#pragma omp for schedule(dynamic, 16)
+                for (int64_t oo = o0; oo < (int64_t)o1; oo++) {
+                    if (bad) continue;
+                    const uint32_t o = (uint32_t)oo;
+                    const uint32_t c = b.centre;
+                    b.nr[c]          = o;
+                    b.shift[c]       = 1.0;
+                    for (uint32_t k = 0; k < m->nrad[ls]; k++) {
+                        const uint32_t l = m->nrad_cum[ls] + k;
+                        int err          = 0;
+                        const int64_t first = trace(m, &b, 0, l, o, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
+                        const int64_t last  = trace(m, &b, 0, l, o, ar, +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
+                        if (err) {
+#pragma omp atomic write
+                            err_any = 1;
+                            continue;
+                        }
+                        b.first = (uint32_t)first;
+                        b.last  = (uint32_t)last;
+                        b.n_tot = (uint32_t)(last + 1 - first);
+                        for (uint32_t q = 0; q < Q; q++) {
+                            const uint32_t f = l * Q + q;
+                            double val;
+                            if (b.n_tot > 1) {
+                                solve_feautrier_order_2(m, &b, o, f, 1);
+                                val = b.Su[c];
+                                if (u) u[((size_t)rr * P + o) * F + f] = val;
+                                J[(size_t)o * F + f] += b.Su[c] * 2.0 * m->ray_weight[rr];
+                                update_lambda(m, &b, rr, f, lambda_diag, lambda_has);
+                            } else {
+                                val = boundary_intensity(m, o, m->nu[(size_t)o * F + f]);
+                                if (u) u[((size_t)rr * P + o) * F + f] = val;
+                                J[(size_t)o * F + f] += 2.0 * m->ray_weight[rr] * val;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        buf_free(&b);
+    }
+    return err_any ? -2 : 0;
+}
+
+int orc_formal_solve_fo2(const OrcModel* m, double* J, double* u, double* lambda_diag,
+                         uint8_t* lambda_has, int nthreads) {
+    const size_t PF = (size_t)m->npoints * m->nfreqs;
+    memset(J, 0, sizeof(double) * PF);
+    if (lambda_diag) memset(lambda_diag, 0, sizeof(double) * (size_t)m->npoints * m->nlines);
+    if (lambda_has) memset(lambda_has, 0, (size_t)m->npoints * m->nlines);
+    return fo2_range(m, 0, m->hnrays, 0, m->npoints, J, u, lambda_diag, lambda_has, nthreads);
+}
+
+int orc_formal_solve_fo2_range(const OrcModel* m, uint32_t rr_begin, uint32_t rr_end, uint32_t o_begin,
+                               uint32_t o_end, double* J, int nthreads) {
+    return fo2_range(m, rr_begin, rr_end, o_begin, o_end, J, NULL, NULL, NULL, nthreads);
+}
+
+/* ------------------------------------------------------------------ */
+/* Short characteristics, order 0 (solver.tpp:150-235, :1564-1757)      */
+/* ------------------------------------------------------------------ */
+static double sc0_lambda(const OrcModel* m, uint32_t o, uint32_t r, uint32_t f, double dtau, int have_dtau) {
+    if (!have_dtau) return 0.0; /* reference reads an unset dtau here; contribution taken as 0 */
+    const double factor     = (double)expm1f((float)(-dtau)) / dtau;
+    const uint32_t ls       = m->corr_lspec[f];
+    const uint32_t k        = m->corr_k[f];
+    const uint32_t z        = m->corr_z[f];
+    const uint32_t lid      = m->nrad_cum[ls] + k;
+    const double freq_line  = m->line[lid];
+    const double invr_mass  = m->lspec_inverse_mass[ls];
+    const double constante  = m->line_A[lid] * m->quad_weights[(size_t)ls * m->nquads + z] * m->ray_weight[r];
+    const double freq       = m->nu[(size_t)o * m->nfreqs + f];
+    double eta, chi;
+    get_eta_and_chi(m, o, k, freq_line, &eta, &chi);
+    const double inverse_chi = 1.0 / chi;
+    const double phi         = thermo_profile(m, invr_mass, o, freq_line, freq);
+    return constante * freq * phi * (factor + 1.0) * inverse_chi;
+}
+
+/* solve_shortchar_order_0_ray_forward (solver.tpp:1564-1640). */
+static double sc0_forward(const OrcModel* m, Buf* b, uint32_t o, uint32_t r, uint32_t f, double* L) {
+    const double freq = m->nu[(size_t)o * m->nfreqs + f];
+    const uint32_t l  = m->corr_line[f];
+    double chi_c = 0.0, chi_n = 0.0, source_c = 0.0, source_n = 0.0, dtau = 0.0;
+    int cco = 1, have = 0;
+    double I = boundary_intensity(m, b->nr[b->first], freq * b->shift[b->first]);
+    for (uint32_t idx = b->first + 1; idx <= b->centre; idx++) {
+        chi_c    = chi_n;
+        source_c = source_n;
+        compute_source_dtau(m, b->nr[idx - 1], b->nr[idx], b->nr_interp[idx - 1], b->nr_interp[idx], l,
+                            freq * b->shift[idx - 1], freq * b->shift[idx], b->shift[idx - 1], b->shift[idx],
+                            b->dZ[idx - 1], b->interp_factor[idx - 1], b->interp_factor[idx], &cco, &dtau,
+                            &chi_c, &chi_n, &source_c, &source_n);
+        dtau = (m->min_dtau > dtau) ? m->min_dtau : dtau;
+        I    = (double)expf((float)(-dtau)) * I
+            + (double)expm1f((float)(-dtau)) / dtau * (source_c - source_n * (1.0 + dtau)) + source_c - source_n;
+        have = 1;
+    }
+    *L = sc0_lambda(m, o, r, f, dtau, have);
+    return I;
+}
+
+/* solve_shortchar_order_0_ray_backward (solver.tpp:1664-1757). */
+static double sc0_backward(const OrcModel* m, Buf* b, uint32_t o, uint32_t r, uint32_t f, double* L) {
+    const double freq = m->nu[(size_t)o * m->nfreqs + f];
+    const uint32_t l  = m->corr_line[f];
+    double chi_c = 0.0, chi_n = 0.0, source_c = 0.0, source_n = 0.0, dtau = 0.0;
+    int cco = 1, have = 0;
+    double I = boundary_intensity(m, b->nr[b->last], freq * b->shift[b->last]);
+    for (uint32_t ip1 = b->last; ip1 >= b->centre + 1; ip1--) {
+        chi_c    = chi_n;
+        source_c = source_n;
+        compute_source_dtau(m, b->nr[ip1], b->nr[ip1 - 1], b->nr_interp[ip1], b->nr_interp[ip1 - 1], l,
+                            freq * b->shift[ip1], freq * b->shift[ip1 - 1], b->shift[ip1], b->shift[ip1 - 1],
+                            b->dZ[ip1 - 1], b->interp_factor[ip1], b->interp_factor[ip1 - 1], &cco, &dtau,
+                            &chi_c, &chi_n, &source_c, &source_n);
+        dtau = (m->min_dtau > dtau) ? m->min_dtau : dtau;
+        I    = (double)expf((float)(-dtau)) * I
+            + (double)expm1f((float)(-dtau)) / dtau * (source_c - source_n * (1.0 + dtau)) + source_c - source_n;
+        have = 1;
+    }
+    *L = sc0_lambda(m, o, r, f, dtau, have);
+    return I;
+}
+
+int orc_formal_solve_sc0(const OrcModel* m, double* J, double* I, double* u, double* v,
+                         double* lambda_diag, uint8_t* lambda_has, int nthreads) {
+    const uint32_t P = m->npoints, F = m->nfreqs, Q = m->nquads;
+    const size_t PF  = (size_t)P * F;
+    memset(J, 0, sizeof(double) * PF);
+    if (lambda_diag) memset(lambda_diag, 0, sizeof(double) * (size_t)P * m->nlines);
+    if (lambda_has) memset(lambda_has, 0, (size_t)P * m->nlines);
+    const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
+    int err_any           = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+    {
+        Buf b;
+        int bad = buf_init(&b, length);
+        for (uint32_t rr = 0; rr < m->hnrays; rr++) {
+            const uint32_t ar = m->antipod[rr];
+            for (uint32_t ls = 0; ls < m->nlspecs; ls++) {
+#pragma omp for schedule(dynamic, 16)
+                for (int64_t oo = 0; oo < (int64_t)P; oo++) {
+                    if (bad) continue;
+                    const uint32_t o  = (uint32_t)oo;
+                    const uint32_t c  = b.centre;
+                    const double wt   = m->ray_weight[rr] * 2.0;
+                    b.nr[c]           = o;
+                    b.shift[c]        = 1.0;
+                    for (uint32_t k = 0; k < m->nrad[ls]; k++) {
+                        const uint32_t l = m->nrad_cum[ls] + k;
+                        int err          = 0;
+                        const int64_t first = trace(m, &b, 0, l, o, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
+                        const int64_t last  = trace(m, &b, 0, l, o, ar, +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
+                        if (err) {
+#pragma omp atomic write
+                            err_any = 1;
+                            continue;
+                        }
+                        b.first = (uint32_t)first;
+                        b.last  = (uint32_t)last;
+                        b.n_tot = (uint32_t)(last + 1 - first);
+                        for (uint32_t z = 0; z < Q; z++) {
+                            const uint32_t f = l * Q + z;
+                            double If, Ib;
+                            if (b.n_tot > 1) {
+                                double Lf = 0.0, Lb = 0.0;
+                                If = sc0_forward(m, &b, o, rr, f, &Lf);
+                                Ib = sc0_backward(m, &b, o, rr, f, &Lb);
+                                if (m->in_line_integral[f]) {
+                                    if (lambda_diag) {
+                                        lambda_diag[(size_t)o * m->nlines + l] += Lf;
+                                        lambda_diag[(size_t)o * m->nlines + l] += Lb;
+                                    }
+                                    if (lambda_has) lambda_has[(size_t)o * m->nlines + l] = 1;
+                                }
+                                const double uu = 0.5 * (If + Ib);
+                                if (u) u[((size_t)rr * P + o) * F + f] = uu;
+                                if (v) v[((size_t)rr * P + o) * F + f] = 0.5 * (If - Ib);
+                                J[(size_t)o * F + f] += wt * uu;
+                            } else {
+                                const double bdy_I = boundary_intensity(m, o, m->nu[(size_t)o * F + f]);
+                                If = Ib = bdy_I;
+                                if (u) u[((size_t)rr * P + o) * F + f] = bdy_I;
+                                if (v) v[((size_t)rr * P + o) * F + f] = 0.0;
+                                J[(size_t)o * F + f] += wt * bdy_I;
+                            }
+                            if (I) {
+                                I[((size_t)rr * P + o) * F + f] = If;
+                                I[((size_t)ar * P + o) * F + f] = Ib;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        buf_free(&b);
+    }
+    return err_any ? -2 : 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Old imager (solver.tpp:542-574, :2462-2574)                          */
+/* ------------------------------------------------------------------ */
+int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads) {
+    const uint32_t P = m->npoints, F = m->nfreqs;
+    const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
+    const uint32_t ar     = m->antipod[rr];
+    int err_any           = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+    {
+        Buf b;
+        int bad = buf_init(&b, length);
+#pragma omp for schedule(dynamic, 16)
+        for (int64_t oo = 0; oo < (int64_t)P; oo++) {
+            if (bad) continue;
+            const uint32_t o = (uint32_t)oo;
+            const uint32_t c = b.centre;
+            int err          = 0;
+            b.nr[c]          = o;
+            b.shift[c]       = get_shift(m, 1, o, rr, o);
+            const int64_t first = trace(m, &b, 1, UINT32_MAX, o, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
+            const int64_t last  = trace(m, &b, 1, UINT32_MAX, o, ar, +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
+            if (err) {
+#pragma omp atomic write
+                err_any = 1;
+                continue;
+            }
+            b.first = (uint32_t)first;
+            b.last  = (uint32_t)last;
+            b.n_tot = (uint32_t)(last + 1 - first);
+            for (uint32_t f = 0; f < F; f++) {
+                if (b.n_tot > 1) {
+                    solve_feautrier_order_2(m, &b, o, f, 0);
+                    I[(size_t)o * F + f] = 2.0 * b.Su[b.last]
+                                         - boundary_intensity(m, b.nr[b.last], m->nu[(size_t)o * F + f]);
+                } else {
+                    I[(size_t)o * F + f] = boundary_intensity(m, o, m->nu[(size_t)o * F + f]);
+                }
+            }
+        }
+        buf_free(&b);
+    }
+    return err_any ? -2 : 0;
+}

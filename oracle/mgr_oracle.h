@@ -1,0 +1,122 @@
+/*
+ * Oracle for the Magritte formal-solve hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, FP64 restatement of the reference CPU algorithm (Magritte 0.9.3,
+ * src/solver/solver.tpp, src/model/geometry/geometry.tpp, src/model/model.cpp,
+ * src/model/lines/...).  It exists to check the CUDA product path and to time
+ * the reference algorithm on host cores.  Only the test-suite, the smoke check
+ * and the CPU-baseline leg of bench.py may load it; the product library never
+ * links or calls it.
+ *
+ * Arithmetic follows the reference statement by statement: FP64 storage with
+ * the single-precision libm calls the reference makes (expf, expm1f, erff,
+ * logf, powf), no FMA contraction (built with -ffp-contract=off), vector dot
+ * products summed x, y, z left to right.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Approximation used for summing lines (src/solver/solver.hpp:9). */
+enum { ORC_NONE = 0, ORC_ONELINE = 1, ORC_CLOSELINES = 2 };
+
+/* Boundary conditions (src/model/geometry/boundary/boundary.hpp:7). */
+enum { ORC_BC_ZERO = 0, ORC_BC_THERMAL = 1, ORC_BC_CMB = 2 };
+
+/* Flat view of the Model fields the formal solve reads.  All arrays are
+ * row-major with the reference's index conventions:
+ *   position/velocity [P][3] (velocity as v/c), emissivity/opacity/
+ *   inverse_width/interp_criterion [P][L] (index l + p*L, lines.tpp:8-10),
+ *   nu [P][F] (index f + p*F, radiation.tpp:3-5), ray_direction [nrays][3]. */
+typedef struct {
+    uint32_t npoints, nrays, hnrays, nlines, nquads, nfreqs, nlspecs, nboundary;
+    const double*   position;
+    const double*   velocity;
+    const uint32_t* n_neighbors;
+    const uint32_t* cum_n_neighbors;
+    const uint32_t* neighbors;
+    const uint32_t* point2boundary;       /* npoints for interior points */
+    const int32_t*  boundary_condition;   /* [nboundary] */
+    const double*   boundary_temperature; /* [nboundary] */
+    const double*   ray_direction;
+    const double*   ray_weight;           /* [nrays] */
+    const uint32_t* antipod;              /* [nrays] */
+    const double*   line;                 /* [L] line centre frequencies */
+    const double*   sorted_line;          /* [L] ascending */
+    const uint32_t* sorted_line_map;      /* [L] sorted -> original index */
+    double          max_inverse_mass;
+    const double*   emissivity;
+    const double*   opacity;
+    const double*   inverse_width;
+    const double*   interp_criterion;     /* opacity / population_tot */
+    const double*   temperature;          /* [P] */
+    const double*   vturb2;               /* [P] */
+    const double*   dshift_max;           /* [P] */
+    const double*   nu;                   /* [P][F] */
+    const uint32_t* corr_line;            /* [F] */
+    const uint32_t* corr_lspec;           /* [F] */
+    const uint32_t* corr_k;               /* [F] */
+    const uint32_t* corr_z;               /* [F] */
+    const uint8_t*  in_line_integral;     /* [F] */
+    const uint32_t* nrad;                 /* [nlspecs] */
+    const uint32_t* nrad_cum;             /* [nlspecs] */
+    const double*   line_A;               /* [L] Einstein A per global line */
+    const double*   lspec_inverse_mass;   /* [nlspecs] */
+    const double*   quad_weights;         /* [nlspecs][Q] */
+    const double*   quad_roots;           /* [nlspecs][Q] */
+    double min_opacity;
+    double min_dtau;
+    double max_interpolation_diff;
+    double max_distance_opacity_contribution;
+    int    approx;
+} OrcModel;
+
+/* One ray pair as the reference lays it out in its per-thread buffers
+ * (solver.tpp:484-496): elements first..last, centre = origin. */
+typedef struct {
+    uint32_t  capacity;   /* length of each array */
+    uint32_t  centre, first, last;
+    uint32_t* nr;
+    uint32_t* nr_interp;
+    double*   interp_factor;
+    double*   shift;
+    double*   dZ;
+} OrcRay;
+
+/* Maximum ray-pair length over all (rr, o), reference Solver::get_ray_lengths_max
+ * (solver.tpp:105-126) with get_n_interp over all lines. */
+uint32_t orc_ray_lengths_max(const OrcModel* m, int nthreads);
+
+/* Trace ray pair (o, rr) for global line l (trace_ray_for_line, solver.tpp:773-800). */
+int orc_trace_ray_pair_for_line(const OrcModel* m, uint32_t o, uint32_t rr, uint32_t l, OrcRay* ray);
+
+/* Model::compute_radiation_field_feautrier_order_2 -> Solver::solve_feautrier_order_2
+ * (model.cpp:353-390, solver.tpp:458-540).  n_off_diag = 0.
+ *   J          [P][F]      (required)
+ *   u          [hnrays][P][F] or NULL
+ *   lambda_diag [P][L]      summed diagonal ALO element per (point, global line), or NULL
+ *   lambda_has  [P][L]      1 where the reference would hold an ALO element, or NULL */
+int orc_formal_solve_fo2(const OrcModel* m, double* J, double* u, double* lambda_diag,
+                         uint8_t* lambda_has, int nthreads);
+
+/* Same driver restricted to the ray pairs [rr_begin, rr_end) and origins [o_begin, o_end);
+ * used to time a bounded sample.  Accumulates into J (not cleared). */
+int orc_formal_solve_fo2_range(const OrcModel* m, uint32_t rr_begin, uint32_t rr_end,
+                               uint32_t o_begin, uint32_t o_end, double* J, int nthreads);
+
+/* Model::compute_radiation_field_shortchar_order_0 -> Solver::solve_shortchar_order_0
+ * (model.cpp:313-349, solver.tpp:150-235, :1564-1757).
+ *   I [nrays][P][F], u, v [hnrays][P][F] (each may be NULL), J [P][F]. */
+int orc_formal_solve_sc0(const OrcModel* m, double* J, double* I, double* u, double* v,
+                         double* lambda_diag, uint8_t* lambda_has, int nthreads);
+
+/* Old imager, Solver::image_feautrier_order_2(model, rr) (solver.tpp:542-574) with
+ * Rest-frame shifts.  I [P][F]. */
+int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,299 @@
+"""Oracle for the Magritte formal-solve hot path -- TEST INFRASTRUCTURE ONLY.
+
+Two parts:
+  * ``reference_setup``: a numpy restatement of the reference's model set-up
+    (Model::compute_spectral_discretisation, model.cpp:70-161; LTE populations,
+    lineProducingSpecies.tpp:52-75; emissivity/opacity, :23-44;
+    Lines::set_inverse_width, lines.tpp:45-59; Model::set_dshift_max,
+    model.cpp:1158-1178; InterpHelper criterion, solver_interp_helper.hpp:15-24).
+    Populations are kept in double precision where the reference keeps long double.
+  * ctypes bindings to ``_build/libmgr_oracle.so`` (mgr_oracle.c).
+
+Only the test-suite, the smoke check and bench.py's CPU-baseline leg use this
+module; the product library never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmgr_oracle.so")
+
+CC = 2.99792458e8
+HH = 6.62607004e-34
+KB = 1.38064852e-23
+AMU = 1.66053904e-27
+CC_SQUARED = 8.98755179e16
+TWO_KB_OVER_AMU_CC_SQUARED = 2.0 * KB / (AMU * CC_SQUARED)
+HH_OVER_FOUR_PI = HH / (4.0 * np.pi)
+
+APPROX = {"None": 0, "OneLine": 1, "CloseLines": 2}
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# Reference model set-up (numpy restatement)
+# ---------------------------------------------------------------------------
+def reference_setup(raw, approx="CloseLines", max_width_fraction=0.35, min_opacity=1.0e-26,
+                    min_line_opacity=1.0e-13, min_line_emissivity=1.0e-50, min_dtau=1.0e-15,
+                    max_interpolation_diff=1.4, max_distance_opacity_contribution=10.0,
+                    populations=None):
+    """Arrays of the OrcModel struct for a ``magritte_gb300.synthetic.RawModel``.
+    ``populations`` (list per species of [P, nlev]) overrides the LTE populations."""
+    P = raw.npoints
+    nrays = raw.nrays
+    Q = raw.nquads
+    lds = raw.linedata
+    nlspecs = len(lds)
+    nrad = np.array([ld.nrad for ld in lds], dtype=np.uint32)
+    nrad_cum = np.zeros(nlspecs, dtype=np.uint32)
+    for l in range(1, nlspecs):
+        nrad_cum[l] = nrad_cum[l - 1] + nrad[l - 1]
+    L = int(nrad.sum())
+    F = L * Q
+    line = np.concatenate([ld.frequency for ld in lds]).astype(np.float64)
+    # Lines::read sorts with heapsort (lines.cpp:43-61); a stable sort gives the same
+    # order for distinct line frequencies.
+    sorted_line_map = np.argsort(line, kind="stable").astype(np.uint32)
+    sorted_line = line[sorted_line_map].copy()
+    max_inverse_mass = max(ld.inverse_mass for ld in lds)
+    T = raw.temperature.astype(np.float64)
+    vt2 = raw.vturb2.astype(np.float64)
+
+    # compute_spectral_discretisation (model.cpp:70-161)
+    nu = np.zeros((P, F))
+    corr_line = np.zeros(F, np.uint32)
+    corr_lspec = np.zeros(F, np.uint32)
+    corr_k = np.zeros(F, np.uint32)
+    corr_z = np.zeros(F, np.uint32)
+    in_line = np.ones(F, np.uint8)
+    for l, ld in enumerate(lds):
+        pw = np.sqrt(TWO_KB_OVER_AMU_CC_SQUARED * ld.inverse_mass * T + vt2)
+        for k in range(ld.nrad):
+            lid = int(nrad_cum[l]) + k
+            width = line[lid] * pw
+            for z in range(Q):
+                f = lid * Q + z
+                nu[:, f] = line[lid] + width * raw.quad_roots[l][z]
+                corr_line[f] = lid
+                corr_lspec[f] = l
+                corr_k[f] = k
+                corr_z[f] = z
+
+    # LTE populations (lineProducingSpecies.tpp:52-75) and emissivity/opacity (:23-44)
+    emissivity = np.zeros((P, L))
+    opacity = np.zeros((P, L))
+    inverse_width = np.zeros((P, L))
+    criterion = np.zeros((P, L))
+    pops = []
+    for l, ld in enumerate(lds):
+        pop_tot = raw.abundance[:, ld.num].astype(np.float64)
+        if populations is None:
+            pop = ld.weight[None, :] * np.exp(-ld.energy[None, :] / (KB * T[:, None]))
+            pf = np.zeros(P)
+            for i in range(ld.nlev):
+                pf = pf + pop[:, i]
+            pop = pop * (pop_tot / pf)[:, None]
+        else:
+            pop = np.asarray(populations[l], dtype=np.float64)
+        pops.append(pop)
+        freq = ld.frequency
+        for k in range(ld.nrad):
+            lid = int(nrad_cum[l]) + k
+            i, j = int(ld.irad[k]), int(ld.jrad[k])
+            em = freq[k] * HH_OVER_FOUR_PI * ld.A[k] * pop[:, i]
+            op = freq[k] * HH_OVER_FOUR_PI * (pop[:, j] * ld.Ba[k] - pop[:, i] * ld.Bs[k])
+            emissivity[:, lid] = np.maximum(em, min_line_emissivity)
+            opacity[:, lid] = np.maximum(op, min_line_opacity)
+            inverse_width[:, lid] = 1.0 / (freq[k] * np.sqrt(TWO_KB_OVER_AMU_CC_SQUARED * ld.inverse_mass * T + vt2))
+            criterion[:, lid] = opacity[:, lid] / pop_tot
+
+    # set_dshift_max (model.cpp:1158-1178)
+    dshift_max = np.full(P, np.finfo(np.float64).max)
+    for ld in lds:
+        cand = max_width_fraction * np.sqrt(TWO_KB_OVER_AMU_CC_SQUARED * ld.inverse_mass * T + vt2)
+        dshift_max = np.minimum(dshift_max, cand)
+
+    from magritte_gb300.healpix import antipodes  # geometry helper shared with the host side
+
+    cum = np.zeros(P, np.uint32)
+    cum[1:] = np.cumsum(raw.n_neighbors.astype(np.uint64))[:-1].astype(np.uint32)
+    p2b = np.full(P, P, np.uint32)
+    p2b[raw.boundary2point] = np.arange(len(raw.boundary2point), dtype=np.uint32)
+
+    return dict(
+        npoints=P, nrays=nrays, hnrays=nrays // 2, nlines=L, nquads=Q, nfreqs=F, nlspecs=nlspecs,
+        nboundary=len(raw.boundary2point),
+        position=np.ascontiguousarray(raw.position, np.float64),
+        velocity=np.ascontiguousarray(raw.velocity, np.float64),
+        n_neighbors=np.ascontiguousarray(raw.n_neighbors, np.uint32), cum_n_neighbors=cum,
+        neighbors=np.ascontiguousarray(raw.neighbors, np.uint32), point2boundary=p2b,
+        boundary_condition=np.ascontiguousarray(raw.boundary_condition, np.int32),
+        boundary_temperature=np.ascontiguousarray(raw.boundary_temperature, np.float64),
+        ray_direction=np.ascontiguousarray(raw.ray_direction, np.float64),
+        ray_weight=np.ascontiguousarray(raw.ray_weight, np.float64),
+        antipod=antipodes(raw.ray_direction),
+        line=line, sorted_line=sorted_line, sorted_line_map=sorted_line_map,
+        max_inverse_mass=float(max_inverse_mass),
+        emissivity=emissivity, opacity=opacity, inverse_width=inverse_width, interp_criterion=criterion,
+        temperature=T, vturb2=vt2, dshift_max=dshift_max, nu=nu,
+        corr_line=corr_line, corr_lspec=corr_lspec, corr_k=corr_k, corr_z=corr_z, in_line_integral=in_line,
+        nrad=nrad, nrad_cum=nrad_cum,
+        line_A=np.concatenate([ld.A for ld in lds]).astype(np.float64),
+        lspec_inverse_mass=np.array([ld.inverse_mass for ld in lds], np.float64),
+        quad_weights=np.ascontiguousarray(np.stack(raw.quad_weights), np.float64),
+        quad_roots=np.ascontiguousarray(np.stack(raw.quad_roots), np.float64),
+        min_opacity=min_opacity, min_dtau=min_dtau, max_interpolation_diff=max_interpolation_diff,
+        max_distance_opacity_contribution=max_distance_opacity_contribution,
+        approx=APPROX[approx], populations=pops,
+    )
+
+
+# ---------------------------------------------------------------------------
+# ctypes
+# ---------------------------------------------------------------------------
+_u32p = C.POINTER(C.c_uint32)
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+_u8p = C.POINTER(C.c_uint8)
+
+_FIELDS = [
+    ("npoints", C.c_uint32), ("nrays", C.c_uint32), ("hnrays", C.c_uint32), ("nlines", C.c_uint32),
+    ("nquads", C.c_uint32), ("nfreqs", C.c_uint32), ("nlspecs", C.c_uint32), ("nboundary", C.c_uint32),
+    ("position", _f64p), ("velocity", _f64p), ("n_neighbors", _u32p), ("cum_n_neighbors", _u32p),
+    ("neighbors", _u32p), ("point2boundary", _u32p), ("boundary_condition", _i32p),
+    ("boundary_temperature", _f64p), ("ray_direction", _f64p), ("ray_weight", _f64p), ("antipod", _u32p),
+    ("line", _f64p), ("sorted_line", _f64p), ("sorted_line_map", _u32p), ("max_inverse_mass", C.c_double),
+    ("emissivity", _f64p), ("opacity", _f64p), ("inverse_width", _f64p), ("interp_criterion", _f64p),
+    ("temperature", _f64p), ("vturb2", _f64p), ("dshift_max", _f64p), ("nu", _f64p),
+    ("corr_line", _u32p), ("corr_lspec", _u32p), ("corr_k", _u32p), ("corr_z", _u32p),
+    ("in_line_integral", _u8p), ("nrad", _u32p), ("nrad_cum", _u32p), ("line_A", _f64p),
+    ("lspec_inverse_mass", _f64p), ("quad_weights", _f64p), ("quad_roots", _f64p),
+    ("min_opacity", C.c_double), ("min_dtau", C.c_double), ("max_interpolation_diff", C.c_double),
+    ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int),
+]
+
+
+class OrcModel(C.Structure):
+    _fields_ = _FIELDS
+
+
+class OrcRay(C.Structure):
+    _fields_ = [("capacity", C.c_uint32), ("centre", C.c_uint32), ("first", C.c_uint32),
+                ("last", C.c_uint32), ("nr", _u32p), ("nr_interp", _u32p), ("interp_factor", _f64p),
+                ("shift", _f64p), ("dZ", _f64p)]
+
+
+def _declare(l):
+    l.orc_ray_lengths_max.restype = C.c_uint32
+    l.orc_ray_lengths_max.argtypes = [C.POINTER(OrcModel), C.c_int]
+    l.orc_trace_ray_pair_for_line.restype = C.c_int
+    l.orc_trace_ray_pair_for_line.argtypes = [C.POINTER(OrcModel), C.c_uint32, C.c_uint32, C.c_uint32,
+                                              C.POINTER(OrcRay)]
+    l.orc_formal_solve_fo2.restype = C.c_int
+    l.orc_formal_solve_fo2.argtypes = [C.POINTER(OrcModel), _f64p, _f64p, _f64p, _u8p, C.c_int]
+    l.orc_formal_solve_fo2_range.restype = C.c_int
+    l.orc_formal_solve_fo2_range.argtypes = [C.POINTER(OrcModel), C.c_uint32, C.c_uint32, C.c_uint32,
+                                             C.c_uint32, _f64p, C.c_int]
+    l.orc_formal_solve_sc0.restype = C.c_int
+    l.orc_formal_solve_sc0.argtypes = [C.POINTER(OrcModel), _f64p, _f64p, _f64p, _f64p, _f64p, _u8p, C.c_int]
+    l.orc_image_fo2.restype = C.c_int
+    l.orc_image_fo2.argtypes = [C.POINTER(OrcModel), C.c_uint32, _f64p, C.c_int]
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+class Oracle:
+    """Holds an OrcModel and the numpy arrays it points into."""
+
+    def __init__(self, arrays):
+        self.a = arrays
+        self.m = OrcModel()
+        for name, typ in _FIELDS:
+            v = arrays[name]
+            if typ in (_u32p, _i32p, _f64p, _u8p):
+                setattr(self.m, name, _ptr(v, typ))
+            else:
+                setattr(self.m, name, v)
+
+    def ray_lengths_max(self, nthreads=0):
+        return lib().orc_ray_lengths_max(C.byref(self.m), nthreads)
+
+    def trace(self, o, rr, l, capacity=None):
+        if capacity is None:
+            capacity = 2 * self.ray_lengths_max() + 1
+        nr = np.zeros(capacity, np.uint32)
+        ni = np.zeros(capacity, np.uint32)
+        fac = np.zeros(capacity)
+        sh = np.zeros(capacity)
+        dz = np.zeros(capacity)
+        ray = OrcRay(capacity, 0, 0, 0, _ptr(nr, _u32p), _ptr(ni, _u32p), _ptr(fac, _f64p), _ptr(sh, _f64p),
+                     _ptr(dz, _f64p))
+        rc = lib().orc_trace_ray_pair_for_line(C.byref(self.m), o, rr, l, C.byref(ray))
+        if rc != 0:
+            raise RuntimeError(f"oracle trace failed ({rc})")
+        s = slice(ray.first, ray.last + 1)
+        return dict(centre=ray.centre - ray.first, nr=nr[s].copy(), nr_interp=ni[s].copy(),
+                    interp_factor=fac[s].copy(), shift=sh[s].copy(), dZ=dz[ray.first:ray.last].copy())
+
+    def formal_solve_fo2(self, want_u=False, nthreads=0):
+        P, F, L, R = self.a["npoints"], self.a["nfreqs"], self.a["nlines"], self.a["hnrays"]
+        J = np.zeros((P, F))
+        u = np.zeros((R, P, F)) if want_u else None
+        lam = np.zeros((P, L))
+        has = np.zeros((P, L), np.uint8)
+        rc = lib().orc_formal_solve_fo2(C.byref(self.m), _ptr(J, _f64p), _ptr(u, _f64p), _ptr(lam, _f64p),
+                                        _ptr(has, _u8p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle formal solve failed ({rc})")
+        return dict(J=J, u=u, lambda_diag=lam, lambda_has=has)
+
+    def formal_solve_fo2_range(self, rr0, rr1, o0, o1, nthreads=0):
+        P, F = self.a["npoints"], self.a["nfreqs"]
+        J = np.zeros((P, F))
+        rc = lib().orc_formal_solve_fo2_range(C.byref(self.m), rr0, rr1, o0, o1, _ptr(J, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle formal solve failed ({rc})")
+        return J
+
+    def formal_solve_sc0(self, nthreads=0):
+        P, F, L, R = self.a["npoints"], self.a["nfreqs"], self.a["nlines"], self.a["hnrays"]
+        J = np.zeros((P, F))
+        I = np.zeros((2 * R, P, F))
+        u = np.zeros((R, P, F))
+        v = np.zeros((R, P, F))
+        lam = np.zeros((P, L))
+        has = np.zeros((P, L), np.uint8)
+        rc = lib().orc_formal_solve_sc0(C.byref(self.m), _ptr(J, _f64p), _ptr(I, _f64p), _ptr(u, _f64p),
+                                        _ptr(v, _f64p), _ptr(lam, _f64p), _ptr(has, _u8p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle short-char solve failed ({rc})")
+        return dict(J=J, I=I, u=u, v=v, lambda_diag=lam, lambda_has=has)
+
+    def image_fo2(self, rr, nthreads=0):
+        P, F = self.a["npoints"], self.a["nfreqs"]
+        I = np.zeros((P, F))
+        rc = lib().orc_image_fo2(C.byref(self.m), rr, _ptr(I, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle imager failed ({rc})")
+        return I

@@ -1,0 +1,119 @@
+"""GPU parity of the second-order Feautrier formal solve against the oracle.
+
+Bar: ray traces (point sequences, interpolation points, shifts, dZ) bit-exact;
+J, u and the ALO diagonal within 1e-5 relative in FP64 mode (the reference's
+single-precision libm calls differ by a few ulp between glibc and CUDA) and in
+split-precision mode."""
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+from magritte_gb300 import _abi
+from magritte_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1.0e-5
+TOL_SPLIT = 1.0e-5
+
+
+@pytest.fixture(scope="module")
+def cube(gpu_lib):
+    raw = S.grid_cube()  # 20^3 points, 12 rays, nquads 11, seed 0
+    a = H.setup(raw)
+    orc = O.Oracle(a)
+    ref = orc.formal_solve_fo2(want_u=True)
+    dev = _abi.DeviceModel(a)
+    yield raw, a, orc, ref, dev
+    dev.close()
+
+
+def test_traces_bit_exact(cube):
+    raw, a, orc, ref, dev = cube
+    rng = np.random.default_rng(1)
+    origins = rng.choice(a["npoints"], size=200, replace=False)
+    n_interp_pts = 0
+    for o in origins:
+        for rr in range(a["hnrays"]):
+            t_ref = orc.trace(int(o), rr, 0)
+            t_gpu = dev.trace(int(o), rr, 0)
+            assert t_gpu["centre"] == t_ref["centre"], (o, rr)
+            assert np.array_equal(t_gpu["nr"], t_ref["nr"]), (o, rr)
+            c = t_ref["centre"]
+            mask = np.ones(len(t_ref["nr"]), bool)
+            mask[c] = False  # the reference never writes nr_interp at the centre
+            assert np.array_equal(t_gpu["nr_interp"][mask], t_ref["nr_interp"][mask]), (o, rr)
+            assert np.array_equal(t_gpu["interp_factor"], t_ref["interp_factor"]), (o, rr)
+            assert np.array_equal(t_gpu["shift"], t_ref["shift"]), (o, rr)
+            assert np.array_equal(t_gpu["dZ"], t_ref["dZ"]), (o, rr)
+            n_interp_pts += int(np.sum(t_ref["interp_factor"] > 0))
+    assert n_interp_pts > 0  # the sample exercises interpolation points
+
+
+def test_ray_lengths_max(cube):
+    raw, a, orc, ref, dev = cube
+    assert dev.ray_lengths_max() == orc.ray_lengths_max()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL_FP64), ("split", TOL_SPLIT)])
+def test_formal_solve_J_u_lambda(cube, precision, tol):
+    raw, a, orc, ref, dev = cube
+    out = dev.formal_solve_fo2(precision, want_u=True)
+    assert H.max_rel(out["J"], ref["J"]) < tol
+    assert H.max_rel(out["u"], ref["u"]) < tol
+    has = ref["lambda_has"].astype(bool)
+    assert H.max_rel(out["lambda_diag"][has], ref["lambda_diag"][has]) < tol
+    assert np.all(out["lambda_diag"][~has] == 0.0)
+
+
+def test_formal_solve_deterministic(cube):
+    raw, a, orc, ref, dev = cube
+    r1 = dev.formal_solve_fo2("split")
+    r2 = dev.formal_solve_fo2("split")
+    assert np.array_equal(r1["J"], r2["J"])
+
+
+@pytest.mark.parametrize("approx", ["None", "OneLine", "CloseLines"])
+def test_approximations_sphere_subset(gpu_lib, approx):
+    """5-level rotor (4 lines) on a small spherical cutout: all three line-sum
+    approximations, both precisions."""
+    raw = S.grid_sphere(n=16, nside=1, nquads=7)
+    a = H.setup(raw, approx=approx)
+    ref = O.Oracle(a).formal_solve_fo2()
+    dev = _abi.DeviceModel(a)
+    for precision, tol in (("fp64", TOL_FP64), ("split", TOL_SPLIT)):
+        out = dev.formal_solve_fo2(precision)
+        assert H.max_rel(out["J"], ref["J"]) < tol, precision
+        has = ref["lambda_has"].astype(bool)
+        assert H.max_rel(out["lambda_diag"][has], ref["lambda_diag"][has]) < tol, precision
+    dev.close()
+
+
+@pytest.mark.parametrize("model,solution,tol", [
+    (H.all_constant_model, H.all_constant_solution, 1.7e-4),
+    (H.all_zero_model, H.all_zero_solution, 6.41e-6),
+])
+def test_known_answer_single_ray(gpu_lib, model, solution, tol):
+    """The reference's analytic benchmarks through the GPU path (both precisions)."""
+    raw = model()
+    a = H.setup(raw)
+    dev = _abi.DeviceModel(a)
+    for precision in ("fp64", "split"):
+        u = dev.formal_solve_fo2(precision, want_u=True)["u"]
+        err = np.abs(H.relative_error(solution(raw), u[0, :, 0]))
+        assert np.max(err) < tol, precision
+    dev.close()
+
+
+def test_velocity_gradient_sphere_parity(gpu_lib):
+    """Radial 5-15 km/s outflow: most steps take the line-integrated (erf) branch."""
+    raw = S.grid_sphere(n=24, nside=1, nquads=11)
+    a = H.setup(raw)
+    ref = O.Oracle(a).formal_solve_fo2(want_u=True)
+    dev = _abi.DeviceModel(a)
+    for precision in ("fp64", "split"):
+        out = dev.formal_solve_fo2(precision, want_u=True)
+        assert H.max_rel(out["J"], ref["J"]) < 1e-5, precision
+        assert H.max_rel(out["u"], ref["u"]) < 1e-5, precision
+    dev.close()
