@@ -76,6 +76,23 @@ def build_gpu(verbose=False, force=False):
     return GPU_LIB
 
 
+EMU_LIB = os.path.join(BUILD, "libmgr_emu.so")
+
+
+def build_emu(force=False):
+    """CPU emulation of the kernel's per-lane code, for the test-suite only."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(CSRC, "emu", "mgr_emu.cu")
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
+    if not force and _newer(EMU_LIB, [src] + headers + [__file__]):
+        return EMU_LIB
+    tmp = EMU_LIB + ".tmp"
+    _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp",
+                             "-I", os.path.join(ROOT, "include"), src, "-o", tmp, "-lgomp"])
+    os.replace(tmp, EMU_LIB)
+    return EMU_LIB
+
+
 def build(verbose=False, force=False):
     build_gpu(verbose=verbose, force=force)
     try:

@@ -1,0 +1,166 @@
+// CPU emulation of the formal-solve kernel for the test-suite.
+//
+// Runs the kernel's own per-lane code (solve_lane, lambda_element and everything
+// they call, compiled for the host) over all origins, ray pairs and frequencies,
+// with a sequential version of the warp trace.  It is never called by the product
+// API (which fails without a GPU); it lets the CPU tests check the kernel's
+// arithmetic against the oracle, and lets kernel logic be debugged without a GPU.
+#include <cstring>
+#include <vector>
+
+#include "../../../include/magritte_gb300.h"
+#include "../mgr_scale.h"
+#include "../mgr_solve.cuh"
+
+using namespace mgr;
+
+namespace {
+
+// Sequential restatement of trace_half (same arithmetic, neighbour order, strict <).
+int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem h) {
+    const double* d = m.raydir + 3 * r;
+    const double4_32a po = m.pos[o];
+    double Z = 0.0;
+    uint32_t crt = o;
+    int count = 0;
+    while (true) {
+        const uint32_t nnb = m.n_nb[crt];
+        const uint32_t cum = m.cum_nb[crt];
+        double best = DBL_MAX;
+        uint32_t besti = 0xffffffffu;
+        double bestZ = 0.0;
+        for (uint32_t i = 0; i < nnb; i++) {
+            const double4_32a e = m.edge[cum + i];
+            const double Rx = dsub_rn(e.x, po.x), Ry = dsub_rn(e.y, po.y), Rz = dsub_rn(e.z, po.z);
+            const double Zn = dot3_rn(Rx, Ry, Rz, d[0], d[1], d[2]);
+            if (Zn > Z) {
+                const double d2 = dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), dmul_rn(Zn, Zn));
+                if (d2 < best) {
+                    best = d2;
+                    besti = i;
+                    bestZ = Zn;
+                }
+            }
+        }
+        if (besti == 0xffffffffu) return count > 0 ? -1 : 0;
+        if ((uint32_t)count >= cap) return -1;
+        long long bits;
+        std::memcpy(&bits, &m.edge[cum + besti].w, 8);
+        const uint32_t nxt = (uint32_t)bits;
+        const double dZl = dsub_rn(bestZ, Z);
+        Z = dadd_rn(Z, dZl);
+        h.ids[count] = nxt;
+        h.dZ[count] = dZl;
+        const double s = shift_comoving(m, o, nxt, d);
+        h.shift[count] = s;
+        h.dsh[count] = (float)dsub_rn(s, 1.0);
+        count++;
+        if (m.p2b[nxt] != m.P) break;
+        crt = nxt;
+    }
+    return count;
+}
+
+float to_f32_floor_host(double x) {
+    const float f = (float)x;
+    return (x > 0.0 && f < FLT_MIN) ? FLT_MIN : f;
+}
+
+}  // namespace
+
+extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, double* J, double* lam) {
+    const uint32_t P = d->npoints, L = d->nlines, F = d->nfreqs;
+    size_t E = 0;
+    for (uint32_t p = 0; p < P; p++) E += d->n_neighbors[p];
+    std::vector<double4_32a> pos(P), vel(P), edge(E ? E : 1);
+    for (uint32_t p = 0; p < P; p++) {
+        pos[p] = make_double4_32a(d->position[3 * p], d->position[3 * p + 1], d->position[3 * p + 2], 0.0);
+        vel[p] = make_double4_32a(d->velocity[3 * p], d->velocity[3 * p + 1], d->velocity[3 * p + 2], 0.0);
+    }
+    for (size_t i = 0; i < E; i++) {
+        const uint32_t n = d->neighbors[i];
+        long long bits = (long long)n;
+        double w;
+        std::memcpy(&w, &bits, 8);
+        edge[i] = make_double4_32a(d->position[3 * n], d->position[3 * n + 1], d->position[3 * n + 2], w);
+    }
+    std::vector<double> ub(P), Sp((size_t)P * L);
+    std::vector<float> em_f(Sp.size()), op_f(Sp.size()), iw_f(Sp.size()), Sp_f(Sp.size()), dsm_f(P);
+    for (uint32_t p = 0; p < P; p++) {
+        ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
+        dsm_f[p] = (float)d->dshift_max[p];
+    }
+    const double Ke = pow2_scale_for_max(d->emissivity, Sp.size());
+    const double Ko = pow2_scale_for_max(d->opacity, Sp.size());
+    for (size_t i = 0; i < Sp.size(); i++) {
+        Sp[i] = d->emissivity[i] / d->opacity[i];
+        em_f[i] = to_f32_floor_host(d->emissivity[i] * Ke);
+        op_f[i] = to_f32_floor_host(d->opacity[i] * Ko);
+        iw_f[i] = (float)d->inverse_width[i];
+        Sp_f[i] = to_f32_floor_host(Sp[i] * (Ke / Ko));
+    }
+    DevModel m{};
+    m.P = P; m.nrays = d->nrays; m.hnrays = d->hnrays; m.L = L; m.Q = d->nquads; m.F = F;
+    m.nlspecs = d->nlspecs; m.B = d->nboundary;
+    m.pos = pos.data(); m.vel = vel.data(); m.n_nb = d->n_neighbors; m.cum_nb = d->cum_n_neighbors;
+    m.edge = edge.data(); m.p2b = d->point2boundary; m.bc = d->boundary_condition; m.bt = d->boundary_temperature;
+    m.raydir = d->ray_direction; m.rayw = d->ray_weight; m.antipod = d->antipod; m.line = d->line;
+    m.sorted_line = d->sorted_line; m.sorted_map = d->sorted_line_map; m.max_inv_mass = d->max_inverse_mass;
+    m.em = d->emissivity; m.op = d->opacity; m.iw = d->inverse_width; m.Sp = Sp.data(); m.crit = d->interp_criterion;
+    m.em_f = em_f.data(); m.op_f = op_f.data(); m.iw_f = iw_f.data(); m.Sp_f = Sp_f.data(); m.ub = ub.data();
+    m.T = d->temperature; m.vt2 = d->vturb2; m.dshift_max = d->dshift_max; m.dshift_max_f = dsm_f.data();
+    m.nu = d->nu; m.corr_line = d->corr_line; m.corr_lspec = d->corr_lspec; m.corr_k = d->corr_k;
+    m.corr_z = d->corr_z; m.in_line = d->in_line_integral; m.nrad_cum = d->nrad_cum; m.line_A = d->line_A;
+    m.lspec_inv_mass = d->lspec_inverse_mass; m.quad_w = d->quad_weights; m.min_opacity = d->min_opacity;
+    m.min_dtau = d->min_dtau; m.max_interp_diff = d->max_interpolation_diff;
+    m.max_dist = d->max_distance_opacity_contribution;
+    m.log_max_interp_diff = logf((float)d->max_interpolation_diff);
+    m.approx = d->approx;
+    m.min_op_s = (float)(d->min_opacity * Ko);
+    m.dz_scale = (float)(1.0 / Ko);
+    m.s_scale = (float)(Ko / Ke);
+
+    const uint32_t cap = 1u << 16;
+    int err = 0;
+#pragma omp parallel
+    {
+        std::vector<double> shb(cap), dzb(cap), shf(cap), dzf(cap);
+        std::vector<uint32_t> idb(cap), idf(cap);
+        std::vector<float> dsb(cap), dsf(cap);
+        HalfSmem bk{idb.data(), shb.data(), dzb.data(), dsb.data()};
+        HalfSmem fw{idf.data(), shf.data(), dzf.data(), dsf.data()};
+#pragma omp for schedule(dynamic, 16)
+        for (long long oo = 0; oo < (long long)P; oo++) {
+            const uint32_t o = (uint32_t)oo;
+            for (uint32_t f = 0; f < F; f++) J[(size_t)o * F + f] = 0.0;
+            if (lam)
+                for (uint32_t l = 0; l < L; l++) lam[(size_t)o * L + l] = 0.0;
+            for (uint32_t rr = 0; rr < m.hnrays; rr++) {
+                const int nb = trace_half_host(m, o, rr, cap, bk);
+                const int nf = trace_half_host(m, o, m.antipod[rr], cap, fw);
+                if (nb < 0 || nf < 0) {
+#pragma omp atomic write
+                    err = 1;
+                    continue;
+                }
+                for (uint32_t f = 0; f < F; f++) {
+                    LaneCtx c;
+                    c.o = o;
+                    c.f = f;
+                    c.l0 = m.corr_line[f];
+                    c.freq = m.nu[(size_t)o * F + f];
+                    c.fq = (float)c.freq;
+                    c.a0 = (float)(c.freq - m.line[c.l0]);
+                    const LaneResult r = precision == MGR_PRECISION_SPLIT
+                                             ? solve_lane<MODE_SPLIT>(m, m.sorted_line, c, bk, nb, fw, nf)
+                                             : solve_lane<MODE_FP64>(m, m.sorted_line, c, bk, nb, fw, nf);
+                    if (r.solved) J[(size_t)o * F + f] += r.u * 2.0 * m.rayw[rr];
+                    else J[(size_t)o * F + f] += 2.0 * m.rayw[rr] * r.u;
+                    if (lam && r.solved && m.in_line[f])
+                        lam[(size_t)o * L + m.corr_line[f]] += lambda_element(m, m.sorted_line, o, rr, f, r.Ldiag);
+                }
+            }
+        }
+    }
+    return err ? MGR_ERR_TRACE : MGR_OK;
+}

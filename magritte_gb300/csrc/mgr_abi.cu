@@ -83,6 +83,16 @@ static int ensure_scratch(MgrModel* m, double** p, size_t* have, size_t bytes) {
     return MGR_OK;
 }
 
+// FP32 table scales of split precision (see mgr_scale.h); NULL keeps a scale.
+static void apply_scales(MgrModel* m, const double* em, const double* op) {
+    const size_t n = (size_t)m->dm.P * m->dm.L;
+    if (em) m->scales.Ke = pow2_scale_for_max(em, n);
+    if (op) m->scales.Ko = pow2_scale_for_max(op, n);
+    m->dm.min_op_s = (float)(m->dm.min_opacity * m->scales.Ko);
+    m->dm.dz_scale = (float)(1.0 / m->scales.Ko);
+    m->dm.s_scale = (float)(m->scales.Ko / m->scales.Ke);
+}
+
 static int size_model(MgrModel* model) {
     uint32_t* d_max = nullptr;
     cudaError_t e = cudaMalloc(&d_max, sizeof(uint32_t));
@@ -303,6 +313,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.op_f = m->op_f;
     dm.iw_f = m->iw_f;
     dm.Sp_f = m->Sp_f;
+    apply_scales(m, d->emissivity, d->opacity);
     if ((e = launch_line_tables(m)) != cudaSuccess) {
         int rc = cuda_fail(e, "line tables");
         mgr_model_free(m);
@@ -329,6 +340,7 @@ int mgr_model_set_line_data(MgrModel* model, const double* emissivity, const dou
     if (opacity && e == cudaSuccess) e = cudaMemcpyAsync(model->op, opacity, bytes, cudaMemcpyHostToDevice, model->stream);
     if (inverse_width && e == cudaSuccess) e = cudaMemcpyAsync(model->iw, inverse_width, bytes, cudaMemcpyHostToDevice, model->stream);
     if (interp_criterion && e == cudaSuccess) e = cudaMemcpyAsync(model->crit, interp_criterion, bytes, cudaMemcpyHostToDevice, model->stream);
+    apply_scales(model, emissivity, opacity);
     if (e == cudaSuccess) e = launch_line_tables(model);
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     if (e != cudaSuccess) return cuda_fail(e, "line data update");

@@ -15,6 +15,13 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <math.h>
+
+// Functions marked MGR_HD are compiled for the GPU and, for the CPU emulation used by
+// the test-suite, for the host.
+#define MGR_HD __host__ __device__ __forceinline__
+
 namespace mgr {
 
 // src/tools/constants.hpp:15-40
@@ -83,37 +90,65 @@ struct DevModel {
     double max_interp_diff;
     double max_dist;
     float log_max_interp_diff;   // logf((float)max_interp_diff)
+    // Split precision keeps FP32 line data in scaled units (exact powers of two):
+    // em_f = em * Ke, op_f = op * Ko, Sp_f = Sp * Ke / Ko.
+    float min_op_s;              // min_opacity * Ko
+    float dz_scale;              // 1 / Ko  (true optical depth = chi_f * dz * dz_scale)
+    float s_scale;               // Ko / Ke (true source = scaled source * s_scale)
     int approx;
 };
 
 // ---------------------------------------------------------------------------------
-// Exactly rounded FP64 helpers for the trace (no contraction into FMA).
+// Exactly rounded FP64 helpers for the trace (no contraction into FMA).  The host
+// build of these headers is compiled with -ffp-contract=off.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ double dot3_rn(double ax, double ay, double az, double bx, double by, double bz) {
-    return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+MGR_HD double dadd_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+MGR_HD double dsub_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+MGR_HD double dmul_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+
+MGR_HD double dot3_rn(double ax, double ay, double az, double bx, double by, double bz) {
+    return dadd_rn(dadd_rn(dmul_rn(ax, bx), dmul_rn(ay, by)), dmul_rn(az, bz));
 }
 
 // Geometry::get_shift_general_geometry<CoMoving> (geometry.tpp:203-207):
 // 1 + (v[c] - v[o]) . n
-__device__ __forceinline__ double shift_comoving(const DevModel& m, uint32_t o, uint32_t c, const double* d) {
+MGR_HD double shift_comoving(const DevModel& m, uint32_t o, uint32_t c, const double* d) {
     const double4_32a vc = m.vel[c];
     const double4_32a vo = m.vel[o];
-    return __dadd_rn(1.0, dot3_rn(__dsub_rn(vc.x, vo.x), __dsub_rn(vc.y, vo.y), __dsub_rn(vc.z, vo.z), d[0], d[1], d[2]));
+    return dadd_rn(1.0, dot3_rn(dsub_rn(vc.x, vo.x), dsub_rn(vc.y, vo.y), dsub_rn(vc.z, vo.z), d[0], d[1], d[2]));
 }
 
 // Geometry::get_shift_general_geometry<Rest> and its reversal for r >= hnrays
 // (geometry.tpp:209-221, :428-465).
-__device__ __forceinline__ double shift_rest(const DevModel& m, uint32_t r, uint32_t c, const double* d) {
+MGR_HD double shift_rest(const DevModel& m, uint32_t r, uint32_t c, const double* d) {
     const double4_32a vc = m.vel[c];
-    double s = __dadd_rn(1.0, dot3_rn(vc.x, vc.y, vc.z, d[0], d[1], d[2]));
-    if (r >= m.hnrays) s = __dsub_rn(2.0, s);
+    double s = dadd_rn(1.0, dot3_rn(vc.x, vc.y, vc.z, d[0], d[1], d[2]));
+    if (r >= m.hnrays) s = dsub_rn(2.0, s);
     return s;
 }
 
 // ---------------------------------------------------------------------------------
 // InterpHelper (solver_interp_helper.tpp:55-99)
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t n_interp_for_line(const DevModel& m, uint32_t l, uint32_t crt, uint32_t nxt) {
+MGR_HD uint32_t n_interp_for_line(const DevModel& m, uint32_t l, uint32_t crt, uint32_t nxt) {
     const double curr = m.crit[(size_t)crt * m.L + l];
     const double next = m.crit[(size_t)nxt * m.L + l];
     const double source_diff = fabsf(logf((float)(next / curr)));
@@ -124,7 +159,7 @@ __device__ __forceinline__ uint32_t n_interp_for_line(const DevModel& m, uint32_
     return n > 1 ? n : 1;
 }
 
-__device__ __forceinline__ uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt) {
+MGR_HD uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt) {
     double mx = -DBL_MAX;
     for (uint32_t l = 0; l < m.L; l++) {
         const double x = m.crit[(size_t)nxt * m.L + l];
@@ -138,18 +173,18 @@ __device__ __forceinline__ uint32_t n_interp_all_lines(const DevModel& m, uint32
 }
 
 template <typename R>
-__device__ __forceinline__ R interpolate_linear(R f_start, R f_end, R factor) {
+MGR_HD R interpolate_linear(R f_start, R f_end, R factor) {
     if (factor == R(0)) return f_start;
     if (factor == R(1)) return f_end;
     return (f_end - f_start) * factor + f_start;
 }
 
-__device__ __forceinline__ double interpolate_log(double f_start, double f_end, double factor) {
+MGR_HD double interpolate_log(double f_start, double f_end, double factor) {
     if (factor == 0.0) return f_start;
     if (factor == 1.0) return f_end;
     return f_start * (double)powf((float)(f_end / f_start), (float)factor);
 }
-__device__ __forceinline__ float interpolate_log(float f_start, float f_end, float factor) {
+MGR_HD float interpolate_log(float f_start, float f_end, float factor) {
     if (factor == 0.0f) return f_start;
     if (factor == 1.0f) return f_end;
     return f_start * powf(f_end / f_start, factor);
@@ -158,20 +193,20 @@ __device__ __forceinline__ float interpolate_log(float f_start, float f_end, flo
 // ---------------------------------------------------------------------------------
 // Profiles and boundary (solver.tpp:1106-1142, thermodynamics.tpp:8-35)
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ double gaussian(double inverse_width, double diff) {
+MGR_HD double gaussian(double inverse_width, double diff) {
     const double sqrt_exp = inverse_width * diff;
     return inverse_width * INVERSE_SQRT_PI * (double)expf((float)(-sqrt_exp * sqrt_exp));
 }
-__device__ __forceinline__ float gaussian(float inverse_width, float diff) {
+MGR_HD float gaussian(float inverse_width, float diff) {
     const float sqrt_exp = inverse_width * diff;
     return inverse_width * (float)INVERSE_SQRT_PI * expf(-sqrt_exp * sqrt_exp);
 }
 
-__device__ __forceinline__ double planck(double temp, double freq) {
+MGR_HD double planck(double temp, double freq) {
     return TWO_HH_OVER_CC_SQUARED * (freq * freq * freq) / (double)expm1f((float)(HH_OVER_KB * freq / temp));
 }
 
-__device__ __forceinline__ double boundary_intensity(const DevModel& m, uint32_t p, double freq) {
+MGR_HD double boundary_intensity(const DevModel& m, uint32_t p, double freq) {
     const uint32_t b = m.p2b[p];
     if (b >= m.B) return 0.0;  // interior point: no boundary condition
     const int c = m.bc[b];
@@ -180,7 +215,7 @@ __device__ __forceinline__ double boundary_intensity(const DevModel& m, uint32_t
     return planck(T_CMB, freq);
 }
 
-__device__ __forceinline__ double thermo_profile(const DevModel& m, double inverse_mass, uint32_t p, double freq_line,
+MGR_HD double thermo_profile(const DevModel& m, double inverse_mass, uint32_t p, double freq_line,
                                                  double freq) {
     const double width = freq_line * sqrt(TWO_KB_OVER_AMU_CC_SQUARED * inverse_mass * m.T[p] + m.vt2[p]);
     const double inverse_width = 1.0 / width;
@@ -190,7 +225,7 @@ __device__ __forceinline__ double thermo_profile(const DevModel& m, double inver
 }
 
 template <typename T>
-__device__ __forceinline__ uint32_t lower_bound(const T* a, uint32_t n, T v) {
+MGR_HD uint32_t lower_bound(const T* a, uint32_t n, T v) {
     uint32_t lo = 0, hi = n;
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
@@ -199,7 +234,7 @@ __device__ __forceinline__ uint32_t lower_bound(const T* a, uint32_t n, T v) {
     return lo;
 }
 template <typename T>
-__device__ __forceinline__ uint32_t upper_bound(const T* a, uint32_t n, T v) {
+MGR_HD uint32_t upper_bound(const T* a, uint32_t n, T v) {
     uint32_t lo = 0, hi = n;
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
@@ -210,7 +245,7 @@ __device__ __forceinline__ uint32_t upper_bound(const T* a, uint32_t n, T v) {
 
 // Solver::get_eta_and_chi<approx> (solver.tpp:1151-1165, :1197-1239, :1286-1294), FP64.
 // `sl` is the sorted line table staged in shared memory.
-__device__ __forceinline__ void get_eta_and_chi(const DevModel& m, const double* sl, uint32_t p, uint32_t ll,
+MGR_HD void get_eta_and_chi(const DevModel& m, const double* sl, uint32_t p, uint32_t ll,
                                                 double freq, double& eta, double& chi) {
     const size_t base = (size_t)p * m.L;
     if (m.approx == APPROX_ONELINE) {

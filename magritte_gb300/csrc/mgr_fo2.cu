@@ -18,15 +18,16 @@ __device__ __forceinline__ float to_f32_floor(double x) {
 __global__ void line_tables_kernel(const double* __restrict__ em, const double* __restrict__ op,
                                    const double* __restrict__ iw, double* __restrict__ Sp, float* __restrict__ em_f,
                                    float* __restrict__ op_f, float* __restrict__ iw_f, float* __restrict__ Sp_f,
-                                   size_t n) {
+                                   size_t n, double Ke, double Ko) {
+    const double KeKo = Ke / Ko;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const double e = em[i], o = op[i];
         const double s = e / o;
         Sp[i] = s;
-        em_f[i] = to_f32_floor(e);
-        op_f[i] = to_f32_floor(o);
+        em_f[i] = to_f32_floor(e * Ke);
+        op_f[i] = to_f32_floor(o * Ko);
         iw_f[i] = (float)iw[i];
-        Sp_f[i] = to_f32_floor(s);
+        Sp_f[i] = to_f32_floor(s * KeKo);
     }
 }
 
@@ -238,7 +239,8 @@ cudaError_t launch_line_tables(MgrModel* model) {
     const int blocks = (int)((n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16);
     count_launch();
     line_tables_kernel<<<blocks > 0 ? blocks : 1, threads, 0, model->stream>>>(
-        model->em, model->op, model->iw, model->Sp, model->em_f, model->op_f, model->iw_f, model->Sp_f, n);
+        model->em, model->op, model->iw, model->Sp, model->em_f, model->op_f, model->iw_f, model->Sp_f, n,
+        model->scales.Ke, model->scales.Ko);
     return cudaGetLastError();
 }
 

@@ -8,6 +8,7 @@
 
 #include "../../include/magritte_gb300.h"
 #include "mgr_device.cuh"
+#include "mgr_scale.h"
 
 struct MgrModel {
     int device = 0;
@@ -24,6 +25,7 @@ struct MgrModel {
     float* iw_f = nullptr;
     float* Sp_f = nullptr;
     int* status = nullptr;           // device status word
+    mgr::LineScales scales;          // FP32 line-table scales (split precision)
     uint32_t half_cap = 0;           // longest half ray in base steps (0 = not sized yet)
     size_t n_edges = 0;
     // scratch outputs for the host-buffer entry points

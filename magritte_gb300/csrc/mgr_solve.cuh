@@ -56,12 +56,12 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
         double bestZ = 0.0;
         for (uint32_t i = lane; i < nnb; i += 32) {
             const double4_32a e = m.edge[cum + i];
-            const double Rx = __dsub_rn(e.x, po.x);
-            const double Ry = __dsub_rn(e.y, po.y);
-            const double Rz = __dsub_rn(e.z, po.z);
+            const double Rx = dsub_rn(e.x, po.x);
+            const double Ry = dsub_rn(e.y, po.y);
+            const double Rz = dsub_rn(e.z, po.z);
             const double Zn = dot3_rn(Rx, Ry, Rz, dx, dy, dz);
             if (Zn > Z) {
-                const double d2 = __dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), __dmul_rn(Zn, Zn));
+                const double d2 = dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), dmul_rn(Zn, Zn));
                 if (d2 < best) {
                     best = d2;
                     besti = i;
@@ -94,14 +94,14 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
             break;
         }
         const uint32_t nxt = (uint32_t)__double_as_longlong(m.edge[cum + besti].w);
-        const double dZl = __dsub_rn(bestZ, Z);
-        Z = __dadd_rn(Z, dZl);
+        const double dZl = dsub_rn(bestZ, Z);
+        Z = dadd_rn(Z, dZl);
         if (STORE && lane == 0) {
             h.ids[count] = nxt;
             h.dZ[count] = dZl;
             const double s = shift_comoving(m, o, nxt, d);
             h.shift[count] = s;
-            h.dsh[count] = (float)__dsub_rn(s, 1.0);
+            h.dsh[count] = (float)dsub_rn(s, 1.0);
         }
         count++;
         if (m.p2b[nxt] != m.P) break;
@@ -134,7 +134,7 @@ struct ElemIter {
     float dshc, dshn;
 };
 
-__device__ __forceinline__ void iter_load_step(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l,
+MGR_HD void iter_load_step(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l,
                                                ElemIter& it) {
     const int s = it.s;
     it.crt = s ? h.ids[s - 1] : o;
@@ -150,7 +150,7 @@ __device__ __forceinline__ void iter_load_step(const DevModel& m, const HalfSmem
 
 // Produces the next element (outer to inner).  Returns false when only the
 // centre element remains.
-__device__ __forceinline__ bool iter_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it,
+MGR_HD bool iter_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it,
                                           Elem& e) {
     if (it.i == 0) {
         if (it.s == 0) return false;
@@ -162,9 +162,9 @@ __device__ __forceinline__ bool iter_next(const DevModel& m, const HalfSmem& h, 
     e.nr = it.nxt;
     e.ni = it.crt;
     if (n > 1) {
-        const double dshift = __dsub_rn(it.shn, it.shc);
+        const double dshift = dsub_rn(it.shn, it.shc);
         const double dshift_interpl = dshift / (double)n;
-        e.shift = __dadd_rn(it.shc, __dmul_rn((double)i, dshift_interpl));
+        e.shift = dadd_rn(it.shc, dmul_rn((double)i, dshift_interpl));
         e.fac = 1.0 - ((double)i) / (double)n;
         e.dzin = it.dzs / (double)n;
         e.dsh = it.dshc + (float)i * ((it.dshn - it.dshc) / (float)n);
@@ -178,7 +178,7 @@ __device__ __forceinline__ bool iter_next(const DevModel& m, const HalfSmem& h, 
     return true;
 }
 
-__device__ __forceinline__ void iter_begin(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, int nsteps,
+MGR_HD void iter_begin(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, int nsteps,
                                            ElemIter& it) {
     if (nsteps <= 0) {
         it.s = 0;
@@ -189,7 +189,7 @@ __device__ __forceinline__ void iter_begin(const DevModel& m, const HalfSmem& h,
     iter_load_step(m, h, o, l, it);
 }
 
-__device__ __forceinline__ Elem centre_elem(uint32_t o) {
+MGR_HD Elem centre_elem(uint32_t o) {
     Elem e;
     e.nr = o;
     e.ni = o;  // never read: its interpolation factor is 0
@@ -220,7 +220,7 @@ struct PairOut {
 // FP64 (reference arithmetic) -------------------------------------------------------
 
 // get_eta_and_chi_interpolated<approx> (solver.tpp:1176-1194, :1252-1283, :1306-1320).
-__device__ __forceinline__ void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e,
+MGR_HD void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e,
                                              double& eta, double& chi) {
     const double freq = c.freq * e.shift;
     const size_t b1 = (size_t)e.nr * m.L, b2 = (size_t)e.ni * m.L;
@@ -258,7 +258,7 @@ __device__ __forceinline__ void eta_chi_fp64(const DevModel& m, const double* sl
 }
 
 // compute_dtau_single_line (solver.tpp:2374-2455).
-__device__ __forceinline__ double dtau_single_line_fp64(const DevModel& m, const Elem& lo, const Elem& hi, uint32_t l,
+MGR_HD double dtau_single_line_fp64(const DevModel& m, const Elem& lo, const Elem& hi, uint32_t l,
                                                         double cf, double nf, double dz) {
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
@@ -282,7 +282,7 @@ __device__ __forceinline__ double dtau_single_line_fp64(const DevModel& m, const
 }
 
 // compute_S_dtau_line_integrated<approx> (solver.tpp:1878-2111).
-__device__ __forceinline__ void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
+MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
                                              const Elem& hi, double dz, PairOut& out) {
     const double cf = c.freq * lo.shift;
     const double nf = c.freq * hi.shift;
@@ -334,16 +334,16 @@ __device__ __forceinline__ void pair_li_fp64(const DevModel& m, const double* sl
 // Frequencies are handled as FP32 offsets from the lane's own line centre:
 //   nu(o,f) * shift - line[l] = (nu(o,f) - line[l0]) + nu(o,f) (shift - 1) - (line[l] - line[l0]).
 
-__device__ __forceinline__ float offset_f32(const DevModel& m, const LaneCtx& c, float dsh, uint32_t l) {
+MGR_HD float offset_f32(const DevModel& m, const LaneCtx& c, float dsh, uint32_t l) {
     const float off0 = fmaf(c.fq, dsh, c.a0);
     return (l == c.l0) ? off0 : off0 - (float)(m.line[l] - m.line[c.l0]);
 }
 
-__device__ __forceinline__ void eta_chi_f32(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e,
+MGR_HD void eta_chi_f32(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e,
                                             float& eta, float& chi) {
     const size_t b1 = (size_t)e.nr * m.L, b2 = (size_t)e.ni * m.L;
     const float fac = (float)e.fac;
-    const float min_op = (float)m.min_opacity;
+    const float min_op = m.min_op_s;
     if (m.approx == APPROX_ONELINE) {
         const uint32_t l = c.l0;
         const float iw = interpolate_linear(m.iw_f[b1 + l], m.iw_f[b2 + l], fac);
@@ -356,26 +356,20 @@ __device__ __forceinline__ void eta_chi_f32(const DevModel& m, const double* sl,
     chi = min_op;
     uint32_t lo = 0, hi = m.L;
     if (m.approx == APPROX_CLOSELINES) {
-        if (m.L == 1) {
-            // a single line is always inside its own bracket
-            lo = 0;
-            hi = 1;
-        } else {
-            const float off0 = fmaf(c.fq, e.dsh, c.a0);
-            const float ub = (float)m.max_dist * ((c.fq + c.fq * e.dsh) * (float)m.ub[e.nr]);
-            // bracket lines with line[l] - line[l0] in [off0 - ub, off0 + ub]
-            const double base = m.line[c.l0];
-            lo = m.L;
-            hi = 0;
-            for (uint32_t s = 0; s < m.L; s++) {
-                const float dl = (float)(sl[s] - base);
-                if (dl >= off0 - ub && dl <= off0 + ub) {
-                    if (s < lo) lo = s;
-                    hi = s + 1;
-                }
+        // lines with line[l] - line[l0] inside [off0 - ub, off0 + ub] (solver.tpp:1216-1227)
+        const float off0 = fmaf(c.fq, e.dsh, c.a0);
+        const float ub = (float)m.max_dist * ((c.fq + c.fq * e.dsh) * (float)m.ub[e.nr]);
+        const double base = m.line[c.l0];
+        lo = m.L;
+        hi = 0;
+        for (uint32_t s = 0; s < m.L; s++) {
+            const float dl = (float)(sl[s] - base);
+            if (dl >= off0 - ub && dl <= off0 + ub) {
+                if (s < lo) lo = s;
+                hi = s + 1;
             }
-            if (hi < lo) hi = lo;
         }
+        if (hi < lo) hi = lo;
     }
     for (uint32_t s = lo; s < hi; s++) {
         const uint32_t l = (m.approx == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
@@ -386,7 +380,7 @@ __device__ __forceinline__ void eta_chi_f32(const DevModel& m, const double* sl,
     }
 }
 
-__device__ __forceinline__ float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Elem& lo,
+MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Elem& lo,
                                                       const Elem& hi, uint32_t l, float dz) {
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
@@ -398,7 +392,7 @@ __device__ __forceinline__ float dtau_single_line_f32(const DevModel& m, const L
     const float nop = interpolate_log(m.op_f[n1 + l], m.op_f[n2 + l], fn);
     const float offc = offset_f32(m, c, lo.dsh, l);
     const float offn = offset_f32(m, c, hi.dsh, l);
-    const float min_op = (float)m.min_opacity;
+    const float min_op = m.min_op_s;
     if (offc == offn) {
         const float prof = gaussian(avg_iw, offc);
         return dz * (prof * ((cop + nop) * 0.5f) + min_op);
@@ -411,22 +405,22 @@ __device__ __forceinline__ float dtau_single_line_f32(const DevModel& m, const L
     return dz * (avg_iw * erfterm + min_op);
 }
 
-__device__ __forceinline__ void pair_li_f32(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
+MGR_HD void pair_li_f32(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
                                             const Elem& hi, double dzd, float& dtau, float& Slo, float& Shi) {
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
     const float fc = (float)lo.fac, fn = (float)hi.fac;
-    const float dz = (float)dzd;
+    const float dz = (float)dzd * m.dz_scale;
     if (m.approx == APPROX_ONELINE) {
         const uint32_t l = c.l0;
         dtau = dtau_single_line_f32(m, c, lo, hi, l, dz);
-        Slo = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc);
-        Shi = interpolate_log(m.Sp_f[n1 + l], m.Sp_f[n2 + l], fn);
+        Slo = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc) * m.s_scale;
+        Shi = interpolate_log(m.Sp_f[n1 + l], m.Sp_f[n2 + l], fn) * m.s_scale;
         return;
     }
     float sum_dtau = 0.0f, sum_c = 0.0f, sum_n = 0.0f;
     uint32_t a = 0, b = m.L;
-    if (m.approx == APPROX_CLOSELINES && m.L > 1) {
+    if (m.approx == APPROX_CLOSELINES) {
         const float oc = fmaf(c.fq, lo.dsh, c.a0);
         const float on = fmaf(c.fq, hi.dsh, c.a0);
         const float left = fminf(oc, on), right = fmaxf(oc, on);
@@ -457,16 +451,16 @@ __device__ __forceinline__ void pair_li_f32(const DevModel& m, const double* sl,
     }
     if (m.approx == APPROX_NONE) {
         dtau = sum_dtau;
-        Slo = sum_c / sum_dtau;
-        Shi = sum_n / sum_dtau;
+        Slo = sum_c / sum_dtau * m.s_scale;
+        Shi = sum_n / sum_dtau * m.s_scale;
         return;
     }
     float d = sum_dtau;
-    const float bound_min_dtau = (float)m.min_opacity * dz;
+    const float bound_min_dtau = m.min_op_s * dz;
     if (-bound_min_dtau < d) d = fmaxf(bound_min_dtau, d);
     dtau = d;
-    Slo = sum_c / d;
-    Shi = sum_n / d;
+    Slo = sum_c / d * m.s_scale;
+    Shi = sum_n / d * m.s_scale;
 }
 
 // Source/opacity cache of one element (trapezoid branch quantities).
@@ -476,7 +470,7 @@ struct EC {
 };
 
 template <int MODE>
-__device__ __forceinline__ void elem_fresh(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e, EC& ec) {
+MGR_HD void elem_fresh(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e, EC& ec) {
     if (ec.ok) return;
     if (MODE == MODE_FP64) {
         double eta, chi;
@@ -486,7 +480,7 @@ __device__ __forceinline__ void elem_fresh(const DevModel& m, const double* sl, 
     } else {
         float eta, chi;
         eta_chi_f32(m, sl, c, e, eta, chi);
-        ec.S = (double)(eta / chi);
+        ec.S = (double)(eta / chi) * (double)m.s_scale;
         ec.chi = (double)chi;
     }
     ec.ok = true;
@@ -495,9 +489,9 @@ __device__ __forceinline__ void elem_fresh(const DevModel& m, const double* sl, 
 // compute_source_dtau (solver.tpp:2139-2186) for the pair (lo, hi) with lo the lower
 // array index.  Fills the caches of both elements when the trapezoid rule is used.
 template <int MODE>
-__device__ __forceinline__ void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
+MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
                                           const Elem& hi, double dz, EC& ecl, EC& ech, PairOut& out) {
-    const double dshift_abs = fabs(__dsub_rn(hi.shift, lo.shift));
+    const double dshift_abs = fabs(dsub_rn(hi.shift, lo.shift));
     const double a = m.dshift_max[lo.nr], b = m.dshift_max[hi.nr];
     out.large = dshift_abs > (a < b ? a : b);
     if (out.large) {
@@ -516,7 +510,7 @@ __device__ __forceinline__ void eval_pair(const DevModel& m, const double* sl, c
         if (MODE == MODE_FP64) {
             out.dtau = 0.5 * (ecl.chi + ech.chi) * dz;
         } else {
-            out.dtau = (double)(0.5f * ((float)ecl.chi + (float)ech.chi) * (float)dz);
+            out.dtau = (double)(0.5f * ((float)ecl.chi + (float)ech.chi) * ((float)dz * m.dz_scale));
         }
     }
 }
@@ -531,7 +525,7 @@ struct LaneResult {
 // Two-sided Feautrier solve of frequency c.f on the ray pair staged in `bk`
 // (backward half, direction rr) and `fw` (forward half, antipode).
 template <int MODE>
-__device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk, int nb,
+__host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk, int nb,
                                  const HalfSmem& fw, int nf) {
     LaneResult res;
     res.solved = (nb > 0) || (nf > 0);
@@ -696,7 +690,7 @@ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const Lane
 
 // update_Lambda, n_off_diag = 0 (solver.tpp:1760-1800): the ALO element of this
 // (origin, ray pair, frequency).
-__device__ __forceinline__ double lambda_element(const DevModel& m, const double* sl, uint32_t o, uint32_t rr,
+MGR_HD double lambda_element(const DevModel& m, const double* sl, uint32_t o, uint32_t rr,
                                                  uint32_t f, double Ldiag) {
     const double w_ang = 2.0 * m.rayw[rr];
     const uint32_t ls = m.corr_lspec[f];
