@@ -172,6 +172,9 @@ MGR_HD uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt
     return n > 1 ? n : 1;
 }
 
+// Correctly rounded single-precision erf (double erf rounded once to float).
+MGR_HD float erff_cr(float x) { return (float)erf((double)x); }
+
 template <typename R>
 MGR_HD R interpolate_linear(R f_start, R f_end, R factor) {
     if (factor == R(0)) return f_start;

@@ -276,7 +276,12 @@ MGR_HD double dtau_single_line_fp64(const DevModel& m, const Elem& lo, const Ele
     const double curr_pos = (linefreq - cf) * avg_iw;
     const double diff_pos = next_pos - curr_pos;
     const double average_opacity = (nop + cop) / 2.0;
-    const float erfdiff = erff((float)next_pos) - erff((float)curr_pos);
+    // The reference subtracts two single-precision erff values (solver.tpp:2450).
+    // For |pos| >~ 2 that difference cancels catastrophically, so a one-ulp change
+    // of erff moves J by up to ~1e-4 on strongly Doppler-shifted models: FP64 mode
+    // therefore uses the correctly rounded erff, (float)erf((double)x), which is the
+    // same on every platform (and in the oracle's matching mode).
+    const float erfdiff = erff_cr((float)next_pos) - erff_cr((float)curr_pos);
     const double erfterm = average_opacity / diff_pos / 2.0 * (double)erfdiff;
     return dz * (avg_iw * erfterm + m.min_opacity);
 }

@@ -412,6 +412,15 @@ static void get_eta_and_chi_interpolated(const OrcModel* m, uint32_t p1, uint32_
     }
 }
 
+/* erff used for the line-integrated optical depth.  Mode 0 (default): the libm
+ * erff, as the reference calls it.  Mode 1: the correctly rounded erff,
+ * (float)erf((double)x), which is platform independent; the GPU's FP64 mode uses
+ * it, so parity between the two is not at the mercy of libm ulps (the reference's
+ * erff(a) - erff(b) cancels for |a|, |b| >~ 2 and amplifies those ulps). */
+static int g_erf_mode = 0;
+void orc_set_erf_mode(int mode) { g_erf_mode = mode; }
+static inline float orc_erff(float x) { return g_erf_mode ? (float)erf((double)x) : erff(x); }
+
 /* Solver::compute_dtau_single_line (solver.tpp:2374-2455). */
 static double compute_dtau_single_line(const OrcModel* m, uint32_t curridx, uint32_t nextidx,
                                        uint32_t ci, uint32_t ni, uint32_t l, double curr_freq,
@@ -432,7 +441,7 @@ static double compute_dtau_single_line(const OrcModel* m, uint32_t curridx, uint
     const double curr_pos        = (linefreq - curr_freq) * avg_iw;
     const double diff_pos        = next_pos - curr_pos;
     const double average_opacity = (nop + cop) / 2.0;
-    const float  erfdiff         = erff((float)next_pos) - erff((float)curr_pos);
+    const float  erfdiff         = orc_erff((float)next_pos) - orc_erff((float)curr_pos);
     const double erfterm         = average_opacity / diff_pos / 2.0 * (double)erfdiff;
     return dz * (avg_iw * erfterm + m->min_opacity);
 }

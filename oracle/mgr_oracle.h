@@ -86,6 +86,10 @@ typedef struct {
     double*   dZ;
 } OrcRay;
 
+/* erff of the line-integrated optical depth: 0 = libm erff (the reference, default),
+ * 1 = correctly rounded erff (float)erf((double)x) (what the GPU FP64 mode uses). */
+void orc_set_erf_mode(int mode);
+
 /* Maximum ray-pair length over all (rr, o), reference Solver::get_ray_lengths_max
  * (solver.tpp:105-126) with get_n_interp over all lines. */
 uint32_t orc_ray_lengths_max(const OrcModel* m, int nthreads);

@@ -202,7 +202,14 @@ class OrcRay(C.Structure):
                 ("shift", _f64p), ("dZ", _f64p)]
 
 
+def set_erf_mode(mode):
+    """0: libm erff as the reference (default); 1: correctly rounded erff (GPU FP64 mode)."""
+    lib().orc_set_erf_mode(int(mode))
+
+
 def _declare(l):
+    l.orc_set_erf_mode.restype = None
+    l.orc_set_erf_mode.argtypes = [C.c_int]
     l.orc_ray_lengths_max.restype = C.c_uint32
     l.orc_ray_lengths_max.argtypes = [C.POINTER(OrcModel), C.c_int]
     l.orc_trace_ray_pair_for_line.restype = C.c_int

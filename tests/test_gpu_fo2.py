@@ -18,6 +18,14 @@ TOL_FP64 = 1.0e-5
 TOL_SPLIT = 1.0e-5
 
 
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_with_correctly_rounded_erf():
+    """FP64 mode uses the correctly rounded erff; the oracle's matching mode."""
+    O.set_erf_mode(1)
+    yield
+    O.set_erf_mode(0)
+
+
 @pytest.fixture(scope="module")
 def cube(gpu_lib):
     raw = S.grid_cube()  # 20^3 points, 12 rays, nquads 11, seed 0

@@ -16,6 +16,13 @@ from magritte_gb300 import _abi, build
 from magritte_gb300 import synthetic as S
 
 
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_with_correctly_rounded_erf():
+    O.set_erf_mode(1)
+    yield
+    O.set_erf_mode(0)
+
+
 @pytest.fixture(scope="module")
 def emu():
     lib = C.CDLL(build.build_emu())

@@ -70,3 +70,33 @@ def test_oracle_trace_reaches_boundary(built):
                 if t["centre"] < n - 1:
                     assert p2b[t["nr"][-1]] != a["npoints"]
                 assert np.all(t["dZ"] > 0)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_known_answers_hold_in_both_erf_modes(built, mode):
+    """The correctly rounded erff (mode 1, used by the GPU FP64 mode) passes the
+    reference's known-answer thresholds exactly as libm's erff (mode 0) does."""
+    O.set_erf_mode(mode)
+    try:
+        raw = H.all_constant_model()
+        r = O.Oracle(H.setup(raw)).formal_solve_fo2(want_u=True)
+        assert np.max(np.abs(H.relative_error(H.all_constant_solution(raw), r["u"][0, :, 0]))) < 1.7e-4
+        raw = H.all_zero_model()
+        r = O.Oracle(H.setup(raw)).formal_solve_fo2(want_u=True)
+        assert np.max(np.abs(H.relative_error(H.all_zero_solution(raw), r["u"][0, :, 0]))) < 6.41e-6
+    finally:
+        O.set_erf_mode(0)
+
+
+def test_reference_erf_sensitivity_is_bounded_on_single_line_grid(built):
+    """libm erff vs correctly rounded erff: the reference's own J moves by less than
+    1e-5 on the single-line grid (its erff difference cancels only in far wings)."""
+    from magritte_gb300 import synthetic as S
+    a = H.setup(S.grid_cube(n=10, nquads=7))
+    J0 = O.Oracle(a).formal_solve_fo2()["J"]
+    O.set_erf_mode(1)
+    try:
+        J1 = O.Oracle(a).formal_solve_fo2()["J"]
+    finally:
+        O.set_erf_mode(0)
+    assert H.max_rel(J1, J0) < 1e-5
