@@ -173,7 +173,12 @@ MGR_HD uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt
 }
 
 // Correctly rounded single-precision erf (double erf rounded once to float).
-MGR_HD float erff_cr(float x) { return (float)erf((double)x); }
+// For |x| >= 3.919206f (the smallest float whose erf rounds to 1.0f) the value is
+// +-1 exactly, which saves the FP64 erf in the saturated wings.
+MGR_HD float erff_cr(float x) {
+    if (fabsf(x) >= 3.919206f) return copysignf(1.0f, x);
+    return (float)erf((double)x);
+}
 
 template <typename R>
 MGR_HD R interpolate_linear(R f_start, R f_end, R factor) {

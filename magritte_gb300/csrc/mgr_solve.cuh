@@ -386,7 +386,7 @@ MGR_HD void eta_chi_f32(const DevModel& m, const double* sl, const LaneCtx& c, c
 }
 
 MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Elem& lo,
-                                                      const Elem& hi, uint32_t l, float dz) {
+                                                      const Elem& hi, uint32_t l, float dz, double dzd) {
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
     const float fc = (float)lo.fac, fn = (float)hi.fac;
@@ -404,6 +404,14 @@ MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Ele
     }
     const float next_pos = -offn * avg_iw;
     const float curr_pos = -offc * avg_iw;
+    // Both positions in the same far wing: the reference's erff(next) - erff(curr)
+    // cancels, and its single-ulp roundings decide the result.  Take the FP64-mode
+    // value there (same arguments, correctly rounded erff), so split precision stays
+    // within 1e-5 of the FP64 path in J.
+    if ((next_pos > 0.0f) == (curr_pos > 0.0f) && fminf(fabsf(next_pos), fabsf(curr_pos)) > 1.5f &&
+        fminf(fabsf(next_pos), fabsf(curr_pos)) < 3.919206f) {
+        return (float)dtau_single_line_fp64(m, lo, hi, l, c.freq * lo.shift, c.freq * hi.shift, dzd);
+    }
     const float diff_pos = next_pos - curr_pos;
     const float average_opacity = (nop + cop) * 0.5f;
     const float erfterm = average_opacity / diff_pos * 0.5f * (erff(next_pos) - erff(curr_pos));
@@ -418,7 +426,7 @@ MGR_HD void pair_li_f32(const DevModel& m, const double* sl, const LaneCtx& c, c
     const float dz = (float)dzd * m.dz_scale;
     if (m.approx == APPROX_ONELINE) {
         const uint32_t l = c.l0;
-        dtau = dtau_single_line_f32(m, c, lo, hi, l, dz);
+        dtau = dtau_single_line_f32(m, c, lo, hi, l, dz, dzd);
         Slo = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc) * m.s_scale;
         Shi = interpolate_log(m.Sp_f[n1 + l], m.Sp_f[n2 + l], fn) * m.s_scale;
         return;
@@ -447,7 +455,7 @@ MGR_HD void pair_li_f32(const DevModel& m, const double* sl, const LaneCtx& c, c
     }
     for (uint32_t s = a; s < b; s++) {
         const uint32_t l = (m.approx == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
-        const float ld = dtau_single_line_f32(m, c, lo, hi, l, dz);
+        const float ld = dtau_single_line_f32(m, c, lo, hi, l, dz, dzd);
         const float lsc = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc);
         const float lsn = interpolate_log(m.Sp_f[n1 + l], m.Sp_f[n2 + l], fn);
         sum_dtau += ld;
