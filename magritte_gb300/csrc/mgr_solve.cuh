@@ -414,7 +414,11 @@ MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Ele
     }
     const float diff_pos = next_pos - curr_pos;
     const float average_opacity = (nop + cop) * 0.5f;
-    const float erfterm = average_opacity / diff_pos * 0.5f * (erff(next_pos) - erff(curr_pos));
+    // Far from the line both positions can round to the same FP32 value (diff_pos = 0)
+    // where the FP64 positions still differ; both erf values saturate there and the
+    // reference's term is 0.
+    const float erfdiff = erff(next_pos) - erff(curr_pos);
+    const float erfterm = (erfdiff == 0.0f) ? 0.0f : average_opacity / diff_pos * 0.5f * erfdiff;
     return dz * (avg_iw * erfterm + min_op);
 }
 

@@ -47,6 +47,7 @@ MODELS = {
     "cube10": lambda: S.grid_cube(n=10, nquads=5),
     "cube12_seed3": lambda: S.grid_cube(n=12, nquads=7, seed=3),
     "sphere14": lambda: S.grid_sphere(n=14, nside=1, nquads=5),
+    "sphere16": lambda: S.grid_sphere(n=16, nside=1, nquads=7),
     "all_constant": H.all_constant_model,
     "all_zero": H.all_zero_model,
 }
