@@ -203,6 +203,7 @@ def run_ours(args, rank, ws):
     J = torch.empty((P, F), dtype=torch.float64, device=dev)
     lam = torch.empty((P, L), dtype=torch.float64, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    tuning = {p: _abi.autotune(handle, p) for p in sorted({args.precision, "fp64"})}
 
     def step():
         rc = lib.mgr_formal_solve_fo2_device(handle, prec, C.c_void_p(J.data_ptr()), None,
@@ -323,6 +324,7 @@ def run_ours(args, rank, ws):
         "fp64_gpu_solves_per_s": (solves / (fp64_ms / 1000.0)) if fp64_ms else None,
         "speedup_vs_fp64_gpu": (fp64_ms / (1000.0 * kernel_s / args.steps)) if fp64_ms else None,
         "work": {"trace_steps": st_steps.value, "neighbour_reads": st_nbr.value, "elements": st_elem.value},
+        "tuning": tuning,
     }
     print(json.dumps(line), flush=True)
 

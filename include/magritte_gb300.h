@@ -149,6 +149,18 @@ int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, d
  * (the n_tot of solver.tpp:492-496 per line).  Used for algorithmic-byte counts. */
 int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_reads, uint64_t* elements);
 
+/* Launch shape of the formal-solve kernel for one precision mode: the register budget
+ * (min_blocks_per_sm = 2, 3 or 4 CTAs of 256 threads per SM; 0 keeps the current value)
+ * and warps per CTA (1..8; 0 keeps it).  Results do not depend on either; they are
+ * picked by magritte_gb300.autotune for a given model. */
+int mgr_set_tuning(MgrModel* model, int precision, int min_blocks_per_sm, int warps_per_block);
+
+/* Time every launch shape of the formal-solve kernel for `precision` on a sample of
+ * `sample_points` origins of this model (0 = 16384) and keep the fastest.  Outputs
+ * may be NULL.  Blocks until done. */
+int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int* best_min_blocks,
+                     int* best_warps, float* best_ms);
+
 /* Block until all work on the model's stream has finished; returns the first
  * kernel-side status recorded since the last call (trace / capacity / non-finite). */
 int mgr_sync(MgrModel* model);

@@ -60,6 +60,9 @@ SIGNATURES = {
     "mgr_formal_solve_fo2_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint64)]),
+    "mgr_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "mgr_autotune_fo2": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_float)]),
     "mgr_sync": (C.c_int, [C.c_void_p]),
     "mgr_model_stream": (C.c_void_p, [C.c_void_p]),
     "mgr_launch_count": (C.c_uint64, []),
@@ -187,6 +190,17 @@ class DeviceModel:
 
     def sync(self):
         _check(load().mgr_sync(self.h))
+
+    def autotune(self, precision="split", sample_points=0):
+        return autotune(self.h, precision, sample_points)
+
+
+def autotune(handle, precision="split", sample_points=0):
+    """Pick the fastest launch shape of the formal solve for this model (mgr_autotune_fo2)."""
+    mb, w, ms = C.c_int(), C.c_int(), C.c_float()
+    _check(load().mgr_autotune_fo2(handle, PRECISION[precision], sample_points, C.byref(mb), C.byref(w),
+                                   C.byref(ms)))
+    return {"min_blocks_per_sm": mb.value, "warps_per_block": w.value, "sample_ms": ms.value}
 
     def stream(self):
         return load().mgr_model_stream(self.h)

@@ -50,6 +50,7 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
         const double dZl = dsub_rn(bestZ, Z);
         Z = dadd_rn(Z, dZl);
         h.ids[count] = nxt;
+        h.eid[count] = cum + besti;
         h.dZ[count] = dZl;
         const double s = shift_comoving(m, o, nxt, d);
         h.shift[count] = s;
@@ -66,69 +67,118 @@ float to_f32_floor_host(double x) {
     return (x > 0.0 && f < FLT_MIN) ? FLT_MIN : f;
 }
 
-}  // namespace
+// Host copies of the device-model tables mgr_model_create builds on the GPU.
+struct EmuModel {
+    std::vector<double4_32a> pos, vel, edge;
+    std::vector<double> ub, Sp;
+    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f;
+    std::vector<uint16_t> nint;
+    DevModel m{};
+};
 
-extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, double* J, double* lam) {
+void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     const uint32_t P = d->npoints, L = d->nlines, F = d->nfreqs;
     size_t E = 0;
     for (uint32_t p = 0; p < P; p++) E += d->n_neighbors[p];
-    std::vector<double4_32a> pos(P), vel(P), edge(E ? E : 1);
+    x.pos.resize(P);
+    x.vel.resize(P);
+    x.edge.resize(E ? E : 1);
     for (uint32_t p = 0; p < P; p++) {
-        pos[p] = make_double4_32a(d->position[3 * p], d->position[3 * p + 1], d->position[3 * p + 2], 0.0);
-        vel[p] = make_double4_32a(d->velocity[3 * p], d->velocity[3 * p + 1], d->velocity[3 * p + 2], 0.0);
+        x.pos[p] = make_double4_32a(d->position[3 * p], d->position[3 * p + 1], d->position[3 * p + 2], 0.0);
+        x.vel[p] = make_double4_32a(d->velocity[3 * p], d->velocity[3 * p + 1], d->velocity[3 * p + 2], 0.0);
     }
     for (size_t i = 0; i < E; i++) {
         const uint32_t n = d->neighbors[i];
         long long bits = (long long)n;
         double w;
         std::memcpy(&w, &bits, 8);
-        edge[i] = make_double4_32a(d->position[3 * n], d->position[3 * n + 1], d->position[3 * n + 2], w);
+        x.edge[i] = make_double4_32a(d->position[3 * n], d->position[3 * n + 1], d->position[3 * n + 2], w);
     }
-    std::vector<double> ub(P), Sp((size_t)P * L);
-    std::vector<float> em_f(Sp.size()), op_f(Sp.size()), iw_f(Sp.size()), Sp_f(Sp.size()), dsm_f(P);
+    const size_t PL = (size_t)P * L;
+    x.ub.resize(P);
+    x.Sp.resize(PL);
+    x.em_f.resize(PL);
+    x.op_f.resize(PL);
+    x.iw_f.resize(PL);
+    x.Sp_f.resize(PL);
+    x.dsm_f.resize(P);
     for (uint32_t p = 0; p < P; p++) {
-        ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
-        dsm_f[p] = (float)d->dshift_max[p];
+        x.ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
+        x.dsm_f[p] = (float)d->dshift_max[p];
     }
-    const double Ke = pow2_scale_for_max(d->emissivity, Sp.size());
-    const double Ko = pow2_scale_for_max(d->opacity, Sp.size());
-    for (size_t i = 0; i < Sp.size(); i++) {
-        Sp[i] = d->emissivity[i] / d->opacity[i];
-        em_f[i] = to_f32_floor_host(d->emissivity[i] * Ke);
-        op_f[i] = to_f32_floor_host(d->opacity[i] * Ko);
-        iw_f[i] = (float)d->inverse_width[i];
-        Sp_f[i] = to_f32_floor_host(Sp[i] * (Ke / Ko));
+    const double Ke = pow2_scale_for_max(d->emissivity, PL);
+    const double Ko = pow2_scale_for_max(d->opacity, PL);
+    for (size_t i = 0; i < PL; i++) {
+        x.Sp[i] = d->emissivity[i] / d->opacity[i];
+        x.em_f[i] = to_f32_floor_host(d->emissivity[i] * Ke);
+        x.op_f[i] = to_f32_floor_host(d->opacity[i] * Ko);
+        x.iw_f[i] = (float)d->inverse_width[i];
+        x.Sp_f[i] = to_f32_floor_host(x.Sp[i] * (Ke / Ko));
     }
-    DevModel m{};
+    DevModel& m = x.m;
     m.P = P; m.nrays = d->nrays; m.hnrays = d->hnrays; m.L = L; m.Q = d->nquads; m.F = F;
     m.nlspecs = d->nlspecs; m.B = d->nboundary;
-    m.pos = pos.data(); m.vel = vel.data(); m.n_nb = d->n_neighbors; m.cum_nb = d->cum_n_neighbors;
-    m.edge = edge.data(); m.p2b = d->point2boundary; m.bc = d->boundary_condition; m.bt = d->boundary_temperature;
-    m.raydir = d->ray_direction; m.rayw = d->ray_weight; m.antipod = d->antipod; m.line = d->line;
-    m.sorted_line = d->sorted_line; m.sorted_map = d->sorted_line_map; m.max_inv_mass = d->max_inverse_mass;
-    m.em = d->emissivity; m.op = d->opacity; m.iw = d->inverse_width; m.Sp = Sp.data(); m.crit = d->interp_criterion;
-    m.em_f = em_f.data(); m.op_f = op_f.data(); m.iw_f = iw_f.data(); m.Sp_f = Sp_f.data(); m.ub = ub.data();
-    m.T = d->temperature; m.vt2 = d->vturb2; m.dshift_max = d->dshift_max; m.dshift_max_f = dsm_f.data();
-    m.nu = d->nu; m.corr_line = d->corr_line; m.corr_lspec = d->corr_lspec; m.corr_k = d->corr_k;
-    m.corr_z = d->corr_z; m.in_line = d->in_line_integral; m.nrad_cum = d->nrad_cum; m.line_A = d->line_A;
-    m.lspec_inv_mass = d->lspec_inverse_mass; m.quad_w = d->quad_weights; m.min_opacity = d->min_opacity;
-    m.min_dtau = d->min_dtau; m.max_interp_diff = d->max_interpolation_diff;
-    m.max_dist = d->max_distance_opacity_contribution;
+    m.pos = x.pos.data(); m.vel = x.vel.data(); m.n_nb = d->n_neighbors; m.cum_nb = d->cum_n_neighbors;
+    m.edge = x.edge.data(); m.p2b = d->point2boundary; m.bc = d->boundary_condition;
+    m.bt = d->boundary_temperature; m.raydir = d->ray_direction; m.rayw = d->ray_weight; m.antipod = d->antipod;
+    m.line = d->line; m.sorted_line = d->sorted_line; m.sorted_map = d->sorted_line_map;
+    m.max_inv_mass = d->max_inverse_mass; m.em = d->emissivity; m.op = d->opacity; m.iw = d->inverse_width;
+    m.Sp = x.Sp.data(); m.crit = d->interp_criterion; m.em_f = x.em_f.data(); m.op_f = x.op_f.data();
+    m.iw_f = x.iw_f.data(); m.Sp_f = x.Sp_f.data(); m.ub = x.ub.data(); m.T = d->temperature; m.vt2 = d->vturb2;
+    m.dshift_max = d->dshift_max; m.dshift_max_f = x.dsm_f.data(); m.nu = d->nu; m.corr_line = d->corr_line;
+    m.corr_lspec = d->corr_lspec; m.corr_k = d->corr_k; m.corr_z = d->corr_z; m.in_line = d->in_line_integral;
+    m.nrad_cum = d->nrad_cum; m.line_A = d->line_A; m.lspec_inv_mass = d->lspec_inverse_mass;
+    m.quad_w = d->quad_weights; m.min_opacity = d->min_opacity; m.min_dtau = d->min_dtau;
+    m.max_interp_diff = d->max_interpolation_diff; m.max_dist = d->max_distance_opacity_contribution;
     m.log_max_interp_diff = logf((float)d->max_interpolation_diff);
     m.approx = d->approx;
     m.min_op_s = (float)(d->min_opacity * Ko);
     m.dz_scale = (float)(1.0 / Ko);
     m.s_scale = (float)(Ko / Ke);
+    x.nint.resize((E ? E : 1) * (size_t)L);
+    for (uint32_t p = 0; p < P; p++)
+        for (uint32_t k = 0; k < d->n_neighbors[p]; k++)
+            for (uint32_t l = 0; l < L; l++) {
+                const size_t e = (size_t)d->cum_n_neighbors[p] + k;
+                const uint32_t v = n_interp_for_line(m, l, p, d->neighbors[e]);
+                x.nint[e * L + l] = (uint16_t)(v > 0xffffu ? 0xffffu : v);
+            }
+    m.nint = x.nint.data();
+}
 
-    const uint32_t cap = 1u << 16;
+struct HalfBuf {
+    std::vector<double> sh, dz;
+    std::vector<uint32_t> id, ei;
+    std::vector<float> ds;
+    explicit HalfBuf(uint32_t cap) : sh(cap), dz(cap), id(cap), ei(cap), ds(cap) {}
+    HalfSmem view() { return HalfSmem{id.data(), sh.data(), dz.data(), ds.data(), ei.data()}; }
+};
+
+LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {
+    LaneCtx c;
+    c.o = o;
+    c.f = f;
+    c.l0 = m.corr_line[f];
+    c.freq = m.nu[(size_t)o * m.F + f];
+    c.fq = (float)c.freq;
+    c.a0 = (float)(c.freq - m.line[c.l0]);
+    return c;
+}
+
+constexpr uint32_t kCap = 1u << 16;
+
+}  // namespace
+
+extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, double* J, double* lam) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    const uint32_t P = m.P, L = m.L, F = m.F;
     int err = 0;
 #pragma omp parallel
     {
-        std::vector<double> shb(cap), dzb(cap), shf(cap), dzf(cap);
-        std::vector<uint32_t> idb(cap), idf(cap);
-        std::vector<float> dsb(cap), dsf(cap);
-        HalfSmem bk{idb.data(), shb.data(), dzb.data(), dsb.data()};
-        HalfSmem fw{idf.data(), shf.data(), dzf.data(), dsf.data()};
+        HalfBuf b(kCap), fbuf(kCap);
+        HalfSmem bk = b.view(), fw = fbuf.view();
 #pragma omp for schedule(dynamic, 16)
         for (long long oo = 0; oo < (long long)P; oo++) {
             const uint32_t o = (uint32_t)oo;
@@ -136,21 +186,15 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
             if (lam)
                 for (uint32_t l = 0; l < L; l++) lam[(size_t)o * L + l] = 0.0;
             for (uint32_t rr = 0; rr < m.hnrays; rr++) {
-                const int nb = trace_half_host(m, o, rr, cap, bk);
-                const int nf = trace_half_host(m, o, m.antipod[rr], cap, fw);
+                const int nb = trace_half_host(m, o, rr, kCap, bk);
+                const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
                 if (nb < 0 || nf < 0) {
 #pragma omp atomic write
                     err = 1;
                     continue;
                 }
                 for (uint32_t f = 0; f < F; f++) {
-                    LaneCtx c;
-                    c.o = o;
-                    c.f = f;
-                    c.l0 = m.corr_line[f];
-                    c.freq = m.nu[(size_t)o * F + f];
-                    c.fq = (float)c.freq;
-                    c.a0 = (float)(c.freq - m.line[c.l0]);
+                    const LaneCtx c = lane_ctx(m, o, f);
                     const LaneResult r = precision == MGR_PRECISION_SPLIT
                                              ? solve_lane<MODE_SPLIT>(m, m.sorted_line, c, bk, nb, fw, nf)
                                              : solve_lane<MODE_FP64>(m, m.sorted_line, c, bk, nb, fw, nf);
@@ -163,4 +207,24 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
         }
     }
     return err ? MGR_ERR_TRACE : MGR_OK;
+}
+
+// One lane's solve for (o, rr, f): out = {u, L_diag, solved}.
+extern "C" int mgr_emu_lane(const MgrModelDesc* d, int precision, uint32_t o, uint32_t rr, uint32_t f,
+                            double* out) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    HalfBuf b(kCap), fbuf(kCap);
+    const int nb = trace_half_host(m, o, rr, kCap, b.view());
+    const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fbuf.view());
+    if (nb < 0 || nf < 0) return MGR_ERR_TRACE;
+    const LaneCtx c = lane_ctx(m, o, f);
+    const LaneResult r = precision == MGR_PRECISION_SPLIT
+                             ? solve_lane<MODE_SPLIT>(m, m.sorted_line, c, b.view(), nb, fbuf.view(), nf)
+                             : solve_lane<MODE_FP64>(m, m.sorted_line, c, b.view(), nb, fbuf.view(), nf);
+    out[0] = r.u;
+    out[1] = r.Ldiag;
+    out[2] = r.solved ? 1.0 : 0.0;
+    return MGR_OK;
 }

@@ -277,6 +277,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = dalloc(m, &m->op_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->iw_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->Sp_f, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->nint, (E ? E : 1) * (size_t)L)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->em, d->emissivity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->op, d->opacity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->iw, d->inverse_width, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
@@ -313,8 +314,9 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.op_f = m->op_f;
     dm.iw_f = m->iw_f;
     dm.Sp_f = m->Sp_f;
+    dm.nint = m->nint;
     apply_scales(m, d->emissivity, d->opacity);
-    if ((e = launch_line_tables(m)) != cudaSuccess) {
+    if ((e = launch_line_tables(m)) != cudaSuccess || (e = launch_nint_table(m)) != cudaSuccess) {
         int rc = cuda_fail(e, "line tables");
         mgr_model_free(m);
         return rc;
@@ -342,6 +344,7 @@ int mgr_model_set_line_data(MgrModel* model, const double* emissivity, const dou
     if (interp_criterion && e == cudaSuccess) e = cudaMemcpyAsync(model->crit, interp_criterion, bytes, cudaMemcpyHostToDevice, model->stream);
     apply_scales(model, emissivity, opacity);
     if (e == cudaSuccess) e = launch_line_tables(model);
+    if (e == cudaSuccess && interp_criterion) e = launch_nint_table(model);
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     if (e != cudaSuccess) return cuda_fail(e, "line data update");
     return MGR_OK;
@@ -486,6 +489,77 @@ int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_read
     *neighbor_reads = h[1];
     *elements = h[2];
     return MGR_OK;
+}
+
+int mgr_set_tuning(MgrModel* model, int precision, int min_blocks_per_sm, int warps_per_block) {
+    if (!model || (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) ||
+        (min_blocks_per_sm != 0 && (min_blocks_per_sm < 2 || min_blocks_per_sm > 4)) || warps_per_block < 0 ||
+        warps_per_block > 8) {
+        set_error("mgr_set_tuning: min_blocks_per_sm must be 2..4 (0 keeps it), warps_per_block 1..8 (0 keeps it)");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (min_blocks_per_sm) {
+        if (precision == MGR_PRECISION_SPLIT) model->fo2_minb_split = min_blocks_per_sm;
+        else model->fo2_minb_fp64 = min_blocks_per_sm;
+    }
+    if (warps_per_block) model->fo2_warps = warps_per_block;
+    return MGR_OK;
+}
+
+int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int* best_min_blocks, int* best_warps,
+                     float* best_ms) {
+    if (!model || (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT)) {
+        set_error("mgr_autotune_fo2: invalid argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    const DevModel& dm = model->dm;
+    uint32_t n = sample_points ? sample_points : 16384;
+    if (n > dm.P) n = dm.P;
+    // an evenly spread sample of origins: a contiguous block from the middle of the index range
+    const uint32_t o0 = (dm.P - n) / 2, o1 = o0 + n;
+    int rc = ensure_scratch(model, &model->J_scratch, &model->J_scratch_bytes, (size_t)dm.P * dm.F * 8);
+    if (rc != MGR_OK) return rc;
+    int& minb = precision == MGR_PRECISION_SPLIT ? model->fo2_minb_split : model->fo2_minb_fp64;
+    const int keep_minb = minb, keep_warps = model->fo2_warps;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bm = keep_minb, bw = keep_warps;
+    const int minbs[3] = {2, 3, 4};
+    const int warps[2] = {4, 8};
+    cudaError_t e = cudaSuccess;
+    for (int mi = 0; mi < 3 && e == cudaSuccess; mi++) {
+        for (int wi = 0; wi < 2 && e == cudaSuccess; wi++) {
+            minb = minbs[mi];
+            model->fo2_warps = warps[wi];
+            e = launch_fo2_range(model, precision, o0, o1, model->J_scratch, nullptr, nullptr);  // warm
+            if (e == cudaSuccess) e = cudaEventRecord(e0, model->stream);
+            if (e == cudaSuccess) e = launch_fo2_range(model, precision, o0, o1, model->J_scratch, nullptr, nullptr);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, model->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e == cudaSuccess && ms < best) {
+                best = ms;
+                bm = minbs[mi];
+                bw = warps[wi];
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        minb = keep_minb;
+        model->fo2_warps = keep_warps;
+        return cuda_fail(e, "autotune");
+    }
+    minb = bm;
+    model->fo2_warps = bw;
+    if (best_min_blocks) *best_min_blocks = bm;
+    if (best_warps) *best_warps = bw;
+    if (best_ms) *best_ms = best;
+    return read_status(model);
 }
 
 int mgr_sync(MgrModel* model) {

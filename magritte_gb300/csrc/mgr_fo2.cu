@@ -42,7 +42,7 @@ __global__ void size_rays_kernel(DevModel m, uint32_t* d_max, int* status) {
     if (gw >= total) return;
     const uint32_t o = (uint32_t)(gw / m.nrays);
     const uint32_t r = (uint32_t)(gw % m.nrays);
-    HalfSmem h{nullptr, nullptr, nullptr, nullptr};
+    HalfSmem h{nullptr, nullptr, nullptr, nullptr, nullptr};
     const int n = trace_half<false>(m, o, r, 0xffffffffu, h, lane, status);
     if (lane == 0 && n > 0) atomicMax(d_max, (uint32_t)n);
 }
@@ -57,12 +57,47 @@ __device__ __forceinline__ void carve_halves(unsigned char* base, uint32_t cap, 
     uint32_t* u = reinterpret_cast<uint32_t*>(d + 4 * cap);
     bk.ids = u;
     fw.ids = u + cap;
-    float* f = reinterpret_cast<float*>(u + 2 * cap);
+    bk.eid = u + 2 * cap;
+    fw.eid = u + 3 * cap;
+    float* f = reinterpret_cast<float*>(u + 4 * cap);
     bk.dsh = f;
     fw.dsh = f + cap;
 }
 
-__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 2 * 4 + 2 * 4); }
+__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 4 * 4 + 2 * 4); }
+
+// ---------------------------------------------------------------------------------
+// Interpolation count of every CSR edge (crt -> nxt) and line:
+// InterpHelper::get_n_interp_for_line (solver_interp_helper.tpp:55-75), evaluated
+// once per edge instead of once per step, lane and frequency.
+// ---------------------------------------------------------------------------------
+__global__ void nint_table_kernel(DevModel m, uint16_t* __restrict__ nint, int* status) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)m.P * m.L;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = (uint32_t)(i / m.L), l = (uint32_t)(i % m.L);
+        const uint32_t cum = m.cum_nb[p], n = m.n_nb[p];
+        for (uint32_t k = 0; k < n; k++) {
+            const uint32_t nxt = (uint32_t)__double_as_longlong(m.edge[cum + k].w);
+            uint32_t v = n_interp_for_line(m, l, p, nxt);
+            if (v > 0xffffu) {
+                atomicOr(status, ST_CAPACITY);
+                v = 0xffffu;
+            }
+            nint[(size_t)(cum + k) * m.L + l] = (uint16_t)v;
+        }
+    }
+}
+
+cudaError_t launch_nint_table(MgrModel* model) {
+    const uint64_t n = (uint64_t)model->dm.P * model->dm.L;
+    const int threads = 256;
+    uint64_t blocks = (n + threads - 1) / threads;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    count_launch();
+    nint_table_kernel<<<(unsigned)(blocks ? blocks : 1), threads, 0, model->stream>>>(model->dm, model->nint,
+                                                                                       model->status);
+    return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------------------------
 // Reference ray-pair length (Solver::get_ray_lengths_max, solver.tpp:79-126):
@@ -91,9 +126,12 @@ __global__ void ray_lengths_kernel(DevModel m, uint32_t cap, uint32_t* d_max, in
 // ---------------------------------------------------------------------------------
 // Formal solve: one CTA per origin, one warp per ray pair, one lane per frequency.
 // ---------------------------------------------------------------------------------
-template <int MODE>
-__global__ void __launch_bounds__(256) fo2_kernel(DevModel m, uint32_t cap, double* __restrict__ J,
-                                                  double* __restrict__ u, double* __restrict__ lam, int* status) {
+// MINB = CTAs of 256 threads resident per SM the register budget is sized for
+// (2: 128, 3: 80, 4: 64 registers per thread); picked at run time by the tuner.
+template <int MODE, int MINB>
+__global__ void __launch_bounds__(256, MINB) fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end,
+                                                        double* __restrict__ J, double* __restrict__ u,
+                                                        double* __restrict__ lam, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
@@ -107,7 +145,7 @@ __global__ void __launch_bounds__(256) fo2_kernel(DevModel m, uint32_t cap, doub
     carve_halves(tb + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
     for (uint32_t i = threadIdx.x; i < m.L; i += blockDim.x) sl[i] = m.sorted_line[i];
 
-    for (uint32_t o = blockIdx.x; o < m.P; o += gridDim.x) {
+    for (uint32_t o = o_begin + blockIdx.x; o < o_end; o += gridDim.x) {
         for (uint32_t f = lane; f < m.F; f += 32) {
             Jw[(size_t)w * m.F + f] = 0.0;
             Lw[(size_t)w * m.F + f] = 0.0;
@@ -183,8 +221,8 @@ __global__ void trace_export_kernel(DevModel m, uint32_t o, uint32_t rr, uint32_
     }
     // count elements of each half
     uint32_t cb = 0, cf = 0;
-    for (int s = 0; s < nb; s++) cb += n_interp_for_line(m, l, s ? bk.ids[s - 1] : o, bk.ids[s]);
-    for (int s = 0; s < nf; s++) cf += n_interp_for_line(m, l, s ? fw.ids[s - 1] : o, fw.ids[s]);
+    for (int s = 0; s < nb; s++) cb += m.nint[(size_t)bk.eid[s] * m.L + l];
+    for (int s = 0; s < nf; s++) cf += m.nint[(size_t)fw.eid[s] * m.L + l];
     const uint32_t n_tot = cb + 1 + cf;
     if (n_tot > capacity) {
         meta[0] = n_tot;
@@ -287,12 +325,12 @@ __global__ void ray_stats_kernel(DevModel m, uint32_t cap, unsigned long long* s
     for (int s = lane; s < nb; s += 32) {
         const uint32_t crt = s ? bk.ids[s - 1] : o;
         nbr += m.n_nb[crt];
-        for (uint32_t l = 0; l < m.L; l++) elems += n_interp_for_line(m, l, crt, bk.ids[s]);
+        for (uint32_t l = 0; l < m.L; l++) elems += m.nint[(size_t)bk.eid[s] * m.L + l];
     }
     for (int s = lane; s < nf; s += 32) {
         const uint32_t crt = s ? fw.ids[s - 1] : o;
         nbr += m.n_nb[crt];
-        for (uint32_t l = 0; l < m.L; l++) elems += n_interp_for_line(m, l, crt, fw.ids[s]);
+        for (uint32_t l = 0; l < m.L; l++) elems += m.nint[(size_t)fw.eid[s] * m.L + l];
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -319,24 +357,43 @@ cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats) {
     return cudaGetLastError();
 }
 
-template <int MODE>
-static cudaError_t launch_fo2_mode(MgrModel* model, double* J, double* u, double* lam) {
+template <int MODE, int MINB>
+static cudaError_t launch_fo2_mode(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* J, double* u,
+                                   double* lam) {
     const DevModel& m = model->dm;
     const uint32_t cap = model->half_cap;
-    int nw = (int)(m.hnrays < 8 ? m.hnrays : 8);
+    int nw = model->fo2_warps > 0 ? model->fo2_warps : 8;
+    if (nw > 8) nw = 8;
+    if ((uint32_t)nw > m.hnrays) nw = (int)m.hnrays;
     if (nw < 1) nw = 1;
     const uint32_t Lpad = (m.L + 1) & ~1u;
     const size_t smem = (size_t)Lpad * 8 + 2ull * nw * m.F * 8 + (size_t)nw * half_bytes_per_warp(cap);
-    cudaError_t e = cudaFuncSetAttribute(fo2_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(fo2_kernel<MODE, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     count_launch();
-    fo2_kernel<MODE><<<m.P, nw * 32, smem, model->stream>>>(m, cap, J, u, lam, model->status);
+    const uint32_t grid = o_end > o_begin ? o_end - o_begin : 1;
+    fo2_kernel<MODE, MINB><<<grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, J, u, lam, model->status);
     return cudaGetLastError();
 }
 
+template <int MODE>
+static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* J, double* u,
+                                   double* lam) {
+    const int minb = (MODE == MODE_SPLIT) ? model->fo2_minb_split : model->fo2_minb_fp64;
+    if (minb == 2) return launch_fo2_mode<MODE, 2>(model, o_begin, o_end, J, u, lam);
+    if (minb == 4) return launch_fo2_mode<MODE, 4>(model, o_begin, o_end, J, u, lam);
+    return launch_fo2_mode<MODE, 3>(model, o_begin, o_end, J, u, lam);
+}
+
+cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
+                             double* lam) {
+    if (precision == MGR_PRECISION_SPLIT) return launch_fo2_minb<MODE_SPLIT>(model, o_begin, o_end, J, u, lam);
+    return launch_fo2_minb<MODE_FP64>(model, o_begin, o_end, J, u, lam);
+}
+
 cudaError_t launch_fo2(MgrModel* model, int precision, double* J, double* u, double* lam) {
-    if (precision == MGR_PRECISION_SPLIT) return launch_fo2_mode<MODE_SPLIT>(model, J, u, lam);
-    return launch_fo2_mode<MODE_FP64>(model, J, u, lam);
+    return launch_fo2_range(model, precision, 0, model->dm.P, J, u, lam);
 }
 
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,

@@ -24,6 +24,10 @@ struct MgrModel {
     float* op_f = nullptr;
     float* iw_f = nullptr;
     float* Sp_f = nullptr;
+    uint16_t* nint = nullptr;        // [E][L] interpolation counts
+    int fo2_warps = 8;               // warps (ray pairs in flight) per CTA of the formal solve
+    int fo2_minb_split = 3;          // register budget variant: CTAs per SM (2, 3 or 4)
+    int fo2_minb_fp64 = 3;
     int* status = nullptr;           // device status word
     mgr::LineScales scales;          // FP32 line-table scales (split precision)
     uint32_t half_cap = 0;           // longest half ray in base steps (0 = not sized yet)
@@ -46,11 +50,14 @@ void count_launch();
 // Kernel launchers (mgr_fo2.cu).  All enqueue on model->stream.
 cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps);
 cudaError_t launch_fo2(MgrModel* model, int precision, double* J, double* u, double* lam);
+cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
+                             double* lam);
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
                                 uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
                                 double* d_dZ);
 cudaError_t launch_line_tables(MgrModel* model);
 cudaError_t launch_ray_lengths(MgrModel* model, uint32_t* d_max_len);
 cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats);
+cudaError_t launch_nint_table(MgrModel* model);
 
 }  // namespace mgr

@@ -32,6 +32,7 @@ struct HalfSmem {
     double* shift;   // Doppler shift of ids[s]
     double* dZ;      // distance increment of step s
     float* dsh;      // (float)(shift - 1)
+    uint32_t* eid;   // CSR edge of step s (index into the interpolation-count table)
 };
 
 // Warp-cooperative Geometry::get_next_general_geometry<Defaulttracer> walk
@@ -98,6 +99,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
         Z = dadd_rn(Z, dZl);
         if (STORE && lane == 0) {
             h.ids[count] = nxt;
+            h.eid[count] = cum + besti;
             h.dZ[count] = dZl;
             const double s = shift_comoving(m, o, nxt, d);
             h.shift[count] = s;
@@ -144,7 +146,7 @@ MGR_HD void iter_load_step(const DevModel& m, const HalfSmem& h, uint32_t o, uin
     it.dshc = s ? h.dsh[s - 1] : 0.0f;
     it.dshn = h.dsh[s];
     it.dzs = h.dZ[s];
-    it.n = n_interp_for_line(m, l, it.crt, it.nxt);
+    it.n = m.nint[(size_t)h.eid[s] * m.L + l];
     it.i = it.n;
 }
 
@@ -532,6 +534,53 @@ MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, con
     }
 }
 
+// Reciprocal of an elimination pivot.  FP64 mode: IEEE division, as the reference.
+// Split mode: an FP32 reciprocal refined by one Newton step in FP64 (relative error
+// ~1e-14), which keeps the elimination in FP64 without the cost of FP64 division.
+template <int MODE>
+MGR_HD double rcp_pivot(double x) {
+    if (MODE == MODE_FP64) return 1.0 / x;
+    const float xf = (float)x;
+    if (!(xf > 1.0e-30f && xf < 1.0e30f)) return 1.0 / x;
+#ifdef __CUDA_ARCH__
+    const double r = (double)__frcp_rn(xf);
+#else
+    const double r = (double)(1.0f / xf);
+#endif
+    return fma(r, fma(-x, r, 1.0), r);
+}
+
+// One interior elimination row in the economical (1+B)/C form (solver.tpp:2266-2281
+// forward, :2304-2309 backward): `dt_out` is the optical depth of the pair already
+// eliminated, `dt_in` of the pair toward the origin.  F, FI = 1/(1+F) and the modified
+// source Su are updated in place.  Split mode computes the coefficients from the FP32
+// optical depths in FP32 and keeps the recurrence itself in FP64.
+template <int MODE>
+MGR_HD void elim_row(double dt_out, double dt_in, double S, double& F, double& FI, double& Su) {
+    double A, iC;
+    if (MODE == MODE_FP64) {
+        const double dtau_avg = 0.5 * (dt_out + dt_in);
+        const double iA = dtau_avg * dt_out;
+        iC = dtau_avg * dt_in;
+        A = 1.0 / iA;
+    } else {
+        const float a = (float)dt_out, b = (float)dt_in;
+        const float dtau_avg = 0.5f * (a + b);
+        const float iAf = dtau_avg * a, iCf = dtau_avg * b;
+        if (iAf > 1.0e-30f && iAf < 1.0e30f && iCf > 1.0e-30f && iCf < 1.0e30f) {
+            A = (double)(1.0f / iAf);
+            iC = (double)iCf;
+        } else {  // optical depths so small (or large) that their product leaves FP32 range
+            const double avg = 0.5 * (dt_out + dt_in);
+            A = 1.0 / (avg * dt_out);
+            iC = avg * dt_in;
+        }
+    }
+    F = (A * F * FI + 1.0) * iC;
+    FI = rcp_pivot<MODE>(1.0 + F);
+    Su = (A * Su + S) * FI * iC;
+}
+
 // Result of one lane's ray-pair solve.
 struct LaneResult {
     double u;       // Su[centre]
@@ -585,16 +634,10 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 const double Bf = Bf_min_Cf + Cf;
                 Su = (S + 2.0 * Ibdy * inverse_dtau_f) / Bf;
                 FF = 0.5 * Bf_min_Cf * po.dtau * po.dtau;
-                FI = 1.0 / (1.0 + FF);
+                FI = rcp_pivot<MODE>(1.0 + FF);
                 first = false;
             } else {
-                const double dtau_avg = 0.5 * (dt_top + po.dtau);
-                const double iA = dtau_avg * dt_top;
-                const double iC = dtau_avg * po.dtau;
-                const double A = 1.0 / iA;
-                FF = (A * FF * FI + 1.0) * iC;
-                FI = 1.0 / (1.0 + FF);
-                Su = (A * Su + S) * FI * iC;
+                elim_row<MODE>(dt_top, po.dtau, S, FF, FI, Su);
             }
             top_rows = true;
             dt_top = po.dtau;
@@ -640,17 +683,11 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 const double Bl = Bl_min_Al + Al;
                 Sb = (S_last + 2.0 * Ibdy * inverse_dtau_l) / Bl;
                 GG = 0.5 * Bl_min_Al * po.dtau * po.dtau;
-                GI = 1.0 / (1.0 + GG);
+                GI = rcp_pivot<MODE>(1.0 + GG);
                 first = false;
             } else {
-                // row `prev`: lower pair = this pair, upper pair = dt_bot
-                const double dtau_avg = 0.5 * (po.dtau + dt_bot);
-                const double iA = dtau_avg * po.dtau;
-                const double iC = dtau_avg * dt_bot;
-                const double C = 1.0 / iC;
-                GG = (C * GG * GI + 1.0) * iA;
-                GI = 1.0 / (1.0 + GG);
-                Sb = (C * Sb + S_prev_row) * GI * iA;
+                // row `prev`: upper pair dt_bot already eliminated, lower pair = this pair
+                elim_row<MODE>(dt_bot, po.dtau, S_prev_row, GG, GI, Sb);
             }
             bot_rows = true;
             dt_bot = po.dtau;
