@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the library's default launch shape (for profiling one production launch)")
     return p.parse_args()
 
 
@@ -203,7 +205,7 @@ def run_ours(args, rank, ws):
     J = torch.empty((P, F), dtype=torch.float64, device=dev)
     lam = torch.empty((P, L), dtype=torch.float64, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
-    tuning = {p: _abi.autotune(handle, p) for p in sorted({args.precision, "fp64"})}
+    tuning = None if args.no_autotune else {p: _abi.autotune(handle, p) for p in sorted({args.precision, "fp64"})}
 
     def step():
         rc = lib.mgr_formal_solve_fo2_device(handle, prec, C.c_void_p(J.data_ptr()), None,
@@ -313,7 +315,8 @@ def run_ours(args, rank, ws):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "note": "FP64-pipe bound kernel; bytes per SURVEY 8(d) formula"},
+                     "note": "algorithmic bytes = 28 per trace step and per neighbour record + 52 per ray-pair "
+                             "element + 32 per solve"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),

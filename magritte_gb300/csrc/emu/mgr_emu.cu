@@ -55,6 +55,7 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
         const double s = shift_comoving(m, o, nxt, d);
         h.shift[count] = s;
         h.dsh[count] = (float)dsub_rn(s, 1.0);
+        h.dzs[count] = (float)dZl * m.dz_scale;
         count++;
         if (m.p2b[nxt] != m.P) break;
         crt = nxt;
@@ -71,7 +72,7 @@ float to_f32_floor_host(double x) {
 struct EmuModel {
     std::vector<double4_32a> pos, vel, edge;
     std::vector<double> ub, Sp;
-    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f;
+    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll;
     std::vector<uint16_t> nint;
     DevModel m{};
 };
@@ -135,6 +136,9 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     m.min_op_s = (float)(d->min_opacity * Ko);
     m.dz_scale = (float)(1.0 / Ko);
     m.s_scale = (float)(Ko / Ke);
+    line_offset_tables(d->line, d->sorted_line, L, x.dls, x.dll);
+    m.dls = x.dls.data();
+    m.dll = x.dll.data();
     x.nint.resize((E ? E : 1) * (size_t)L);
     for (uint32_t p = 0; p < P; p++)
         for (uint32_t k = 0; k < d->n_neighbors[p]; k++)
@@ -149,9 +153,9 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
 struct HalfBuf {
     std::vector<double> sh, dz;
     std::vector<uint32_t> id, ei;
-    std::vector<float> ds;
-    explicit HalfBuf(uint32_t cap) : sh(cap), dz(cap), id(cap), ei(cap), ds(cap) {}
-    HalfSmem view() { return HalfSmem{id.data(), sh.data(), dz.data(), ds.data(), ei.data()}; }
+    std::vector<float> ds, dzs;
+    explicit HalfBuf(uint32_t cap) : sh(cap), dz(cap), id(cap), ei(cap), ds(cap), dzs(cap) {}
+    HalfSmem view() { return HalfSmem{id.data(), sh.data(), dz.data(), ds.data(), dzs.data(), ei.data()}; }
 };
 
 LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {

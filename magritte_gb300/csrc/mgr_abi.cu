@@ -251,6 +251,8 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
     std::vector<float> dsm_f(P);
     for (uint32_t p = 0; p < P; p++) dsm_f[p] = (float)d->dshift_max[p];
+    std::vector<float> dls, dll;
+    line_offset_tables(d->line, d->sorted_line, L, dls, dll);
 
     const size_t PL = (size_t)P * L;
     do {
@@ -268,6 +270,8 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.line, d->line, L)) != cudaSuccess) break;
         if ((e = upload(m, &dm.sorted_line, d->sorted_line, L)) != cudaSuccess) break;
         if ((e = upload(m, &dm.sorted_map, d->sorted_line_map, L)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.dls, dls.data(), (size_t)L * L)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.dll, dll.data(), (size_t)L * L)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->em, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->op, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->iw, PL)) != cudaSuccess) break;

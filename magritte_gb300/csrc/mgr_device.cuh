@@ -93,6 +93,8 @@ struct DevModel {
     float log_max_interp_diff;   // logf((float)max_interp_diff)
     // Split precision keeps FP32 line data in scaled units (exact powers of two):
     // em_f = em * Ke, op_f = op * Ko, Sp_f = Sp * Ke / Ko.
+    const float* dls;            // [L][L] (float)(sorted_line[s] - line[l0]) at l0*L + s
+    const float* dll;            // [L][L] (float)(line[l] - line[l0]) at l0*L + l
     float min_op_s;              // min_opacity * Ko
     float dz_scale;              // 1 / Ko  (true optical depth = chi_f * dz * dz_scale)
     float s_scale;               // Ko / Ke (true source = scaled source * s_scale)
@@ -122,6 +124,16 @@ MGR_HD double dmul_rn(double a, double b) {
     return __dmul_rn(a, b);
 #else
     return a * b;
+#endif
+}
+
+// FP32 quotient without IEEE division: on the device the approximate __fdividef
+// (2 ulp for |b| < 2^126; callers keep b in that range).
+MGR_HD float fast_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fdividef(a, b);
+#else
+    return a / b;
 #endif
 }
 
@@ -178,6 +190,26 @@ MGR_HD uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt
 // +-1 exactly, which saves the FP64 erf in the saturated wings.
 MGR_HD float erff_cr(float x) {
     if (fabsf(x) >= 3.919206f) return copysignf(1.0f, x);
+    return (float)erf((double)x);
+}
+
+// The same correctly rounded erff without FP64 in most of [1.5, 3.92): there
+// erf = 1 - erfc with erfc < 0.034, and an FP32 erfc (relative error of a few ulp of
+// erfc, far below one ulp of erf) decides the rounding of 1 - erfc exactly unless the
+// value lies within that error of a rounding midpoint; only then FP64 erf is used.
+// t = fl(1 - e) and delta = e - (1 - t) are exact (1 - t is a multiple of 2^-24 and
+// |delta| <= 2^-25).  The true erf rounds to t iff |delta + e*eps| < 2^-25; the test
+// below allows |eps| up to 2^-19 (>= 16 ulp of e; CUDA documents 4 ulp for erfcf) and
+// keeps a small margin for the rounding of the test itself.
+MGR_HD float erff_cr_fast(float x) {
+    const float ax = fabsf(x);
+    if (ax >= 3.919206f) return copysignf(1.0f, x);
+    if (ax >= 1.5f) {
+        const float e = erfcf(ax);
+        const float t = 1.0f - e;
+        const float delta = e - (1.0f - t);
+        if (fabsf(delta) + e * 0x1.0p-19f < 0x1.ffcp-26f) return copysignf(t, x);
+    }
     return (float)erf((double)x);
 }
 

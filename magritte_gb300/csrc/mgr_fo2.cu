@@ -42,7 +42,7 @@ __global__ void size_rays_kernel(DevModel m, uint32_t* d_max, int* status) {
     if (gw >= total) return;
     const uint32_t o = (uint32_t)(gw / m.nrays);
     const uint32_t r = (uint32_t)(gw % m.nrays);
-    HalfSmem h{nullptr, nullptr, nullptr, nullptr, nullptr};
+    HalfSmem h{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     const int n = trace_half<false>(m, o, r, 0xffffffffu, h, lane, status);
     if (lane == 0 && n > 0) atomicMax(d_max, (uint32_t)n);
 }
@@ -62,9 +62,11 @@ __device__ __forceinline__ void carve_halves(unsigned char* base, uint32_t cap, 
     float* f = reinterpret_cast<float*>(u + 4 * cap);
     bk.dsh = f;
     fw.dsh = f + cap;
+    bk.dzs = f + 2 * cap;
+    fw.dzs = f + 3 * cap;
 }
 
-__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 4 * 4 + 2 * 4); }
+__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 4 * 4 + 4 * 4); }
 
 // ---------------------------------------------------------------------------------
 // Interpolation count of every CSR edge (crt -> nxt) and line:
@@ -235,8 +237,8 @@ __global__ void trace_export_kernel(DevModel m, uint32_t o, uint32_t rr, uint32_
     ElemIter it;
     Elem e;
     if (nb > 0) {
-        iter_begin(m, bk, o, l, nb, it);
-        while (iter_next(m, bk, o, l, it, e)) {
+        iter_begin<MODE_FP64>(m, bk, o, l, nb, it);
+        while (iter_next<MODE_FP64>(m, bk, o, l, it, e)) {
             nr[idx] = e.nr;
             ni[idx] = e.ni;
             fac[idx] = e.fac;
@@ -252,9 +254,9 @@ __global__ void trace_export_kernel(DevModel m, uint32_t o, uint32_t rr, uint32_
     const uint32_t centre = idx;
     // forward half: elements centre+1 .. last are produced outer end first
     if (nf > 0) {
-        iter_begin(m, fw, o, l, nf, it);
+        iter_begin<MODE_FP64>(m, fw, o, l, nf, it);
         uint32_t j = n_tot - 1;
-        while (iter_next(m, fw, o, l, it, e)) {
+        while (iter_next<MODE_FP64>(m, fw, o, l, it, e)) {
             nr[j] = e.nr;
             ni[j] = e.ni;
             fac[j] = e.fac;

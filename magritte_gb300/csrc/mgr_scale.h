@@ -4,6 +4,8 @@
 #pragma once
 #include <cmath>
 #include <cstddef>
+#include <cstdint>
+#include <vector>
 
 namespace mgr {
 
@@ -20,6 +22,20 @@ inline double pow2_scale_for_max(const double* a, size_t n) {
     int e = 0;
     std::frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
     return std::ldexp(1.0, -e);
+}
+
+// Line-offset tables of split precision, [L][L] row l0:
+//   dls[l0 L + s] = (float)(sorted_line[s] - line[l0]),  dll[l0 L + l] = (float)(line[l] - line[l0]).
+// A lane of line l0 forms its frequency offsets from these without FP64 arithmetic.
+inline void line_offset_tables(const double* line, const double* sorted_line, uint32_t L, std::vector<float>& dls,
+                               std::vector<float>& dll) {
+    dls.resize((size_t)L * L);
+    dll.resize((size_t)L * L);
+    for (uint32_t a = 0; a < L; a++)
+        for (uint32_t b = 0; b < L; b++) {
+            dls[(size_t)a * L + b] = (float)(sorted_line[b] - line[a]);
+            dll[(size_t)a * L + b] = (float)(line[b] - line[a]);
+        }
 }
 
 }  // namespace mgr

@@ -32,6 +32,7 @@ struct HalfSmem {
     double* shift;   // Doppler shift of ids[s]
     double* dZ;      // distance increment of step s
     float* dsh;      // (float)(shift - 1)
+    float* dzs;      // (float)dZ * dz_scale (split precision)
     uint32_t* eid;   // CSR edge of step s (index into the interpolation-count table)
 };
 
@@ -104,6 +105,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
             const double s = shift_comoving(m, o, nxt, d);
             h.shift[count] = s;
             h.dsh[count] = (float)dsub_rn(s, 1.0);
+            h.dzs[count] = (float)dZl * m.dz_scale;
         }
         count++;
         if (m.p2b[nxt] != m.P) break;
@@ -115,13 +117,21 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
 
 // An element of the ray pair as the reference's per-thread buffers hold it
 // (nr, nr_interp, interp_factor, shift) plus its distance to the neighbouring
-// element on the origin side.
+// element on the origin side.  FP64 mode fills the double fields; split precision
+// fills the FP32 ones and keeps (s, i, n) so that the FP64 shift and factor can be
+// recomputed exactly where a pair needs them (elem_shift_fac).
 struct Elem {
     uint32_t nr, ni;
     double fac;
     double shift;
     double dzin;
-    float dsh;  // shift - 1 (FP32), split precision only
+    float dsh;   // shift - 1
+    float dshm;  // |shift - 1| of the step's two ends, summed (bound for FP32 rounding)
+    float facf;  // interpolation factor
+    float dzf;   // distance * dz_scale
+    int s;       // base step (split precision)
+    uint32_t i;  // sub-element i of n; n == 0 marks the origin
+    uint32_t n;
 };
 
 // Walks the elements of one half ray from its outer end toward the origin,
@@ -132,63 +142,82 @@ struct ElemIter {
     uint32_t i;     // current sub-element (n .. 1), 0 = step exhausted
     uint32_t n;     // interpolation count of step s
     uint32_t crt, nxt;
-    double shc, shn, dzs;
-    float dshc, dshn;
+    double shc, shn, dzs, dshi, dzi;  // FP64: step ends, distance, per-sub-element increments
+    float dshc, ddsh, dshm, dzi_f, rn;
 };
 
-MGR_HD void iter_load_step(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l,
-                                               ElemIter& it) {
+template <int MODE>
+MGR_HD void iter_load_step(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it) {
     const int s = it.s;
     it.crt = s ? h.ids[s - 1] : o;
     it.nxt = h.ids[s];
-    it.shc = s ? h.shift[s - 1] : 1.0;
-    it.shn = h.shift[s];
-    it.dshc = s ? h.dsh[s - 1] : 0.0f;
-    it.dshn = h.dsh[s];
-    it.dzs = h.dZ[s];
     it.n = m.nint[(size_t)h.eid[s] * m.L + l];
     it.i = it.n;
+    const uint32_t n = it.n;
+    if constexpr (MODE == MODE_FP64) {
+        it.shc = s ? h.shift[s - 1] : 1.0;
+        it.shn = h.shift[s];
+        it.dzs = h.dZ[s];
+        // per-step parts of the reference's per-element expressions (same roundings)
+        it.dshi = dsub_rn(it.shn, it.shc) / (double)n;
+        it.dzi = it.dzs / (double)n;
+    } else {
+        const float dshc = s ? h.dsh[s - 1] : 0.0f;
+        const float dshn = h.dsh[s];
+        const float rn = fast_div(1.0f, (float)n);
+        it.dshc = dshc;
+        it.ddsh = (dshn - dshc) * rn;
+        it.dshm = fabsf(dshc) + fabsf(dshn);
+        it.dzi_f = h.dzs[s] * rn;
+        it.rn = rn;
+    }
 }
 
 // Produces the next element (outer to inner).  Returns false when only the
 // centre element remains.
-MGR_HD bool iter_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it,
-                                          Elem& e) {
+template <int MODE>
+MGR_HD bool iter_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it, Elem& e) {
     if (it.i == 0) {
         if (it.s == 0) return false;
         it.s--;
-        iter_load_step(m, h, o, l, it);
+        iter_load_step<MODE>(m, h, o, l, it);
     }
     const uint32_t n = it.n;
     const uint32_t i = it.i;
     e.nr = it.nxt;
     e.ni = it.crt;
-    if (n > 1) {
-        const double dshift = dsub_rn(it.shn, it.shc);
-        const double dshift_interpl = dshift / (double)n;
-        e.shift = dadd_rn(it.shc, dmul_rn((double)i, dshift_interpl));
-        e.fac = 1.0 - ((double)i) / (double)n;
-        e.dzin = it.dzs / (double)n;
-        e.dsh = it.dshc + (float)i * ((it.dshn - it.dshc) / (float)n);
+    if constexpr (MODE == MODE_FP64) {
+        if (n > 1) {
+            e.shift = dadd_rn(it.shc, dmul_rn((double)i, it.dshi));
+            e.fac = 1.0 - ((double)i) / (double)n;
+            e.dzin = it.dzi;
+        } else {
+            e.shift = it.shn;
+            e.fac = 0.0;
+            e.dzin = it.dzs;
+        }
     } else {
-        e.shift = it.shn;
-        e.fac = 0.0;
-        e.dzin = it.dzs;
-        e.dsh = it.dshn;
+        e.dsh = fmaf((float)i, it.ddsh, it.dshc);
+        e.facf = fmaf(-(float)i, it.rn, 1.0f);
+        e.dzf = it.dzi_f;
+        e.dshm = it.dshm;
+        e.s = it.s;
+        e.i = i;
+        e.n = n;
     }
     it.i--;
     return true;
 }
 
-MGR_HD void iter_begin(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, int nsteps,
-                                           ElemIter& it) {
+template <int MODE>
+MGR_HD void iter_begin(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, int nsteps, ElemIter& it) {
     if (nsteps <= 0) {
         it.s = 0;
         it.i = 0;
         return;
     }
     it.s = nsteps - 1;
-    iter_load_step(m, h, o, l, it);
+    iter_load_step<MODE>(m, h, o, l, it);
 }
 
 MGR_HD Elem centre_elem(uint32_t o) {
@@ -199,7 +228,32 @@ MGR_HD Elem centre_elem(uint32_t o) {
     e.shift = 1.0;
     e.dzin = 0.0;
     e.dsh = 0.0f;
+    e.dshm = 0.0f;
+    e.facf = 0.0f;
+    e.dzf = 0.0f;
+    e.s = 0;
+    e.i = 0;
+    e.n = 0;
     return e;
+}
+
+// The FP64 shift and interpolation factor of a split-precision element, computed
+// exactly as the FP64 iterator does.
+MGR_HD void elem_shift_fac(const HalfSmem& h, const Elem& e, double& shift, double& fac) {
+    if (e.n == 0) {
+        shift = 1.0;
+        fac = 0.0;
+        return;
+    }
+    const double shn = h.shift[e.s];
+    if (e.n > 1) {
+        const double shc = e.s ? h.shift[e.s - 1] : 1.0;
+        shift = dadd_rn(shc, dmul_rn((double)e.i, dsub_rn(shn, shc) / (double)e.n));
+        fac = 1.0 - ((double)e.i) / (double)e.n;
+    } else {
+        shift = shn;
+        fac = 0.0;
+    }
 }
 
 // ---------------------------------------------------------------------------------
@@ -210,13 +264,6 @@ struct LaneCtx {
     double freq;   // nu(o, f)
     float fq;      // (float)freq
     float a0;      // (float)(freq - line[l0])
-};
-
-struct PairOut {
-    double dtau;   // optical depth increment between the two elements
-    double Slo;    // row source of the lower-index element if the pair is line-integrated
-    double Shi;    // source of the higher-index element if line-integrated
-    bool large;
 };
 
 // FP64 (reference arithmetic) -------------------------------------------------------
@@ -290,16 +337,17 @@ MGR_HD double dtau_single_line_fp64(const DevModel& m, const Elem& lo, const Ele
 
 // compute_S_dtau_line_integrated<approx> (solver.tpp:1878-2111).
 MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
-                                             const Elem& hi, double dz, PairOut& out) {
+                                             const Elem& hi, double dz, double& out_dtau, double& out_Slo,
+                                             double& out_Shi) {
     const double cf = c.freq * lo.shift;
     const double nf = c.freq * hi.shift;
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
     if (m.approx == APPROX_ONELINE) {
         const uint32_t l = c.l0;
-        out.dtau = dtau_single_line_fp64(m, lo, hi, l, cf, nf, dz);
-        out.Slo = interpolate_log(m.Sp[c1 + l], m.Sp[c2 + l], lo.fac);
-        out.Shi = interpolate_log(m.Sp[n1 + l], m.Sp[n2 + l], hi.fac);
+        out_dtau = dtau_single_line_fp64(m, lo, hi, l, cf, nf, dz);
+        out_Slo = interpolate_log(m.Sp[c1 + l], m.Sp[c2 + l], lo.fac);
+        out_Shi = interpolate_log(m.Sp[n1 + l], m.Sp[n2 + l], hi.fac);
         return;
     }
     double sum_dtau = 0.0, sum_c = 0.0, sum_n = 0.0;
@@ -324,32 +372,48 @@ MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
         sum_n += ld * lsn;
     }
     if (m.approx == APPROX_NONE) {
-        out.dtau = sum_dtau;
-        out.Slo = sum_c / sum_dtau;
-        out.Shi = sum_n / sum_dtau;
+        out_dtau = sum_dtau;
+        out_Slo = sum_c / sum_dtau;
+        out_Shi = sum_n / sum_dtau;
         return;
     }
     double d = sum_dtau;
     const double bound_min_dtau = m.min_opacity * dz;
     if (-bound_min_dtau < d) d = (bound_min_dtau > d) ? bound_min_dtau : d;
-    out.dtau = d;
-    out.Slo = sum_c / d;
-    out.Shi = sum_n / d;
+    out_dtau = d;
+    out_Slo = sum_c / d;
+    out_Shi = sum_n / d;
 }
 
 // FP32 (split precision) ------------------------------------------------------------
-// Frequencies are handled as FP32 offsets from the lane's own line centre:
-//   nu(o,f) * shift - line[l] = (nu(o,f) - line[l0]) + nu(o,f) (shift - 1) - (line[l] - line[l0]).
+// Frequencies are FP32 offsets from the lane's own line centre:
+//   nu(o,f) shift - line[l] = (nu(o,f) - line[l0]) + nu(o,f) (shift - 1) - (line[l] - line[l0]),
+// the last term from the [L][L] tables dll/dls.  Line data are the scaled FP32 tables
+// (DevModel::em_f, ...); element factors and distances arrive precomputed in FP32.
 
 MGR_HD float offset_f32(const DevModel& m, const LaneCtx& c, float dsh, uint32_t l) {
     const float off0 = fmaf(c.fq, dsh, c.a0);
-    return (l == c.l0) ? off0 : off0 - (float)(m.line[l] - m.line[c.l0]);
+    return (l == c.l0) ? off0 : off0 - m.dll[(size_t)c.l0 * m.L + l];
 }
 
-MGR_HD void eta_chi_f32(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e,
-                                            float& eta, float& chi) {
+// CloseLines bracket in offsets: the sorted lines s with dls[l0][s] in [lo_off, hi_off].
+MGR_HD void bracket_f32(const DevModel& m, const LaneCtx& c, float lo_off, float hi_off, uint32_t& a, uint32_t& b) {
+    const float* d = m.dls + (size_t)c.l0 * m.L;
+    a = m.L;
+    b = 0;
+    for (uint32_t s = 0; s < m.L; s++) {
+        const float dl = d[s];
+        if (dl >= lo_off && dl <= hi_off) {
+            if (s < a) a = s;
+            b = s + 1;
+        }
+    }
+    if (b < a) b = a;
+}
+
+MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, float& eta, float& chi) {
     const size_t b1 = (size_t)e.nr * m.L, b2 = (size_t)e.ni * m.L;
-    const float fac = (float)e.fac;
+    const float fac = e.facf;
     const float min_op = m.min_op_s;
     if (m.approx == APPROX_ONELINE) {
         const uint32_t l = c.l0;
@@ -363,20 +427,10 @@ MGR_HD void eta_chi_f32(const DevModel& m, const double* sl, const LaneCtx& c, c
     chi = min_op;
     uint32_t lo = 0, hi = m.L;
     if (m.approx == APPROX_CLOSELINES) {
-        // lines with line[l] - line[l0] inside [off0 - ub, off0 + ub] (solver.tpp:1216-1227)
+        // lines inside freq -+ max_dist * freq * ub[p] (solver.tpp:1216-1227)
         const float off0 = fmaf(c.fq, e.dsh, c.a0);
         const float ub = (float)m.max_dist * ((c.fq + c.fq * e.dsh) * (float)m.ub[e.nr]);
-        const double base = m.line[c.l0];
-        lo = m.L;
-        hi = 0;
-        for (uint32_t s = 0; s < m.L; s++) {
-            const float dl = (float)(sl[s] - base);
-            if (dl >= off0 - ub && dl <= off0 + ub) {
-                if (s < lo) lo = s;
-                hi = s + 1;
-            }
-        }
-        if (hi < lo) hi = lo;
+        bracket_f32(m, c, off0 - ub, off0 + ub, lo, hi);
     }
     for (uint32_t s = lo; s < hi; s++) {
         const uint32_t l = (m.approx == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
@@ -387,16 +441,34 @@ MGR_HD void eta_chi_f32(const DevModel& m, const double* sl, const LaneCtx& c, c
     }
 }
 
-MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Elem& lo,
-                                                      const Elem& hi, uint32_t l, float dz, double dzd) {
+// The FP64 mode's erf arguments (linefreq - nu shift) * avg_iw of a pair, computed
+// with the same expressions as dtau_single_line_fp64.
+MGR_HD void band_positions(const DevModel& m, const LaneCtx& c, const HalfSmem& h, const Elem& lo, const Elem& hi,
+                           uint32_t l, double& next_pos, double& curr_pos) {
+    double lo_shift, lo_fac, hi_shift, hi_fac;
+    elem_shift_fac(h, lo, lo_shift, lo_fac);
+    elem_shift_fac(h, hi, hi_shift, hi_fac);
+    const double cf = c.freq * lo_shift;
+    const double nf = c.freq * hi_shift;
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
-    const float fc = (float)lo.fac, fn = (float)hi.fac;
-    const float iwc = interpolate_linear(m.iw_f[c1 + l], m.iw_f[c2 + l], fc);
-    const float iwn = interpolate_linear(m.iw_f[n1 + l], m.iw_f[n2 + l], fn);
+    const double linefreq = m.line[l];
+    const double iwc = interpolate_linear(m.iw[c1 + l], m.iw[c2 + l], lo_fac);
+    const double iwn = interpolate_linear(m.iw[n1 + l], m.iw[n2 + l], hi_fac);
+    const double avg_iw = (iwc + iwn) / 2.0;
+    next_pos = (linefreq - nf) * avg_iw;
+    curr_pos = (linefreq - cf) * avg_iw;
+}
+
+MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, const Elem& lo,
+                                  const Elem& hi, uint32_t l, float dz) {
+    const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
+    const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
+    const float iwc = interpolate_linear(m.iw_f[c1 + l], m.iw_f[c2 + l], lo.facf);
+    const float iwn = interpolate_linear(m.iw_f[n1 + l], m.iw_f[n2 + l], hi.facf);
     const float avg_iw = (iwc + iwn) * 0.5f;
-    const float cop = interpolate_log(m.op_f[c1 + l], m.op_f[c2 + l], fc);
-    const float nop = interpolate_log(m.op_f[n1 + l], m.op_f[n2 + l], fn);
+    const float cop = interpolate_log(m.op_f[c1 + l], m.op_f[c2 + l], lo.facf);
+    const float nop = interpolate_log(m.op_f[n1 + l], m.op_f[n2 + l], hi.facf);
     const float offc = offset_f32(m, c, lo.dsh, l);
     const float offn = offset_f32(m, c, hi.dsh, l);
     const float min_op = m.min_op_s;
@@ -406,33 +478,37 @@ MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Ele
     }
     const float next_pos = -offn * avg_iw;
     const float curr_pos = -offc * avg_iw;
-    // Both positions in the same far wing: the reference's erff(next) - erff(curr)
-    // cancels, and its single-ulp roundings decide the result.  Take the FP64-mode
-    // value there (same arguments, correctly rounded erff), so split precision stays
-    // within 1e-5 of the FP64 path in J.
-    if ((next_pos > 0.0f) == (curr_pos > 0.0f) && fminf(fabsf(next_pos), fabsf(curr_pos)) > 1.5f &&
-        fminf(fabsf(next_pos), fabsf(curr_pos)) < 3.919206f) {
-        return (float)dtau_single_line_fp64(m, lo, hi, l, c.freq * lo.shift, c.freq * hi.shift, dzd);
+    float erfdiff, diff_pos;
+    const float amin = fminf(fabsf(next_pos), fabsf(curr_pos));
+    if ((next_pos > 0.0f) == (curr_pos > 0.0f) && amin > 1.5f && amin < 3.919206f) {
+        // Both positions in the same far wing: the reference's erff(next) - erff(curr)
+        // cancels and its single-ulp roundings decide the result, so take it on the
+        // FP64 mode's arguments with the correctly rounded erff (split precision then
+        // stays within 1e-5 of the FP64 path in J).
+        double np, cp;
+        band_positions(m, c, h, lo, hi, l, np, cp);
+        erfdiff = erff_cr_fast((float)np) - erff_cr_fast((float)cp);
+        diff_pos = (float)(np - cp);
+    } else {
+        erfdiff = erff(next_pos) - erff(curr_pos);
+        diff_pos = next_pos - curr_pos;
     }
-    const float diff_pos = next_pos - curr_pos;
     const float average_opacity = (nop + cop) * 0.5f;
-    // Far from the line both positions can round to the same FP32 value (diff_pos = 0)
-    // where the FP64 positions still differ; both erf values saturate there and the
-    // reference's term is 0.
-    const float erfdiff = erff(next_pos) - erff(curr_pos);
+    // Far from the line both FP32 positions can coincide while the FP64 ones differ;
+    // both erf values saturate there and the reference's term is 0.
     const float erfterm = (erfdiff == 0.0f) ? 0.0f : average_opacity / diff_pos * 0.5f * erfdiff;
     return dz * (avg_iw * erfterm + min_op);
 }
 
-MGR_HD void pair_li_f32(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
-                                            const Elem& hi, double dzd, float& dtau, float& Slo, float& Shi) {
+// compute_S_dtau_line_integrated<approx> in FP32; dz is the scaled FP32 distance.
+MGR_HD void pair_li_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, const Elem& lo, const Elem& hi,
+                        float dz, float& dtau, float& Slo, float& Shi) {
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
-    const float fc = (float)lo.fac, fn = (float)hi.fac;
-    const float dz = (float)dzd * m.dz_scale;
+    const float fc = lo.facf, fn = hi.facf;
     if (m.approx == APPROX_ONELINE) {
         const uint32_t l = c.l0;
-        dtau = dtau_single_line_f32(m, c, lo, hi, l, dz, dzd);
+        dtau = dtau_single_line_f32(m, c, h, lo, hi, l, dz);
         Slo = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc) * m.s_scale;
         Shi = interpolate_log(m.Sp_f[n1 + l], m.Sp_f[n2 + l], fn) * m.s_scale;
         return;
@@ -442,26 +518,15 @@ MGR_HD void pair_li_f32(const DevModel& m, const double* sl, const LaneCtx& c, c
     if (m.approx == APPROX_CLOSELINES) {
         const float oc = fmaf(c.fq, lo.dsh, c.a0);
         const float on = fmaf(c.fq, hi.dsh, c.a0);
-        const float left = fminf(oc, on), right = fmaxf(oc, on);
         const float rf = c.fq + fmaxf(c.fq * lo.dsh, c.fq * hi.dsh);
         const float cb = (float)m.max_dist * (rf * (float)m.ub[lo.nr]);
         const float nb = (float)m.max_dist * (rf * (float)m.ub[hi.nr]);
         const float ubw = fmaxf(cb, nb);
-        const double base = m.line[c.l0];
-        a = m.L;
-        b = 0;
-        for (uint32_t s = 0; s < m.L; s++) {
-            const float dl = (float)(sl[s] - base);
-            if (dl >= left - ubw && dl <= right + ubw) {
-                if (s < a) a = s;
-                b = s + 1;
-            }
-        }
-        if (b < a) b = a;
+        bracket_f32(m, c, fminf(oc, on) - ubw, fmaxf(oc, on) + ubw, a, b);
     }
     for (uint32_t s = a; s < b; s++) {
         const uint32_t l = (m.approx == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
-        const float ld = dtau_single_line_f32(m, c, lo, hi, l, dz, dzd);
+        const float ld = dtau_single_line_f32(m, c, h, lo, hi, l, dz);
         const float lsc = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc);
         const float lsn = interpolate_log(m.Sp_f[n1 + l], m.Sp_f[n2 + l], fn);
         sum_dtau += ld;
@@ -482,103 +547,143 @@ MGR_HD void pair_li_f32(const DevModel& m, const double* sl, const LaneCtx& c, c
     Shi = sum_n / d * m.s_scale;
 }
 
-// Source/opacity cache of one element (trapezoid branch quantities).
+// Precision-dependent scalar of the pair quantities (optical depths, sources, opacities).
+template <int MODE>
+struct Real_ {
+    using T = double;
+};
+template <>
+struct Real_<MODE_SPLIT> {
+    using T = float;
+};
+
+template <int MODE>
+struct PairOut {
+    typename Real_<MODE>::T dtau;  // optical depth increment between the two elements
+    typename Real_<MODE>::T Slo;   // row source of the lower-index element if line-integrated
+    typename Real_<MODE>::T Shi;   // source of the higher-index element if line-integrated
+    bool large;
+};
+
+// Source/opacity cache of one element (trapezoid branch quantities; in split mode
+// chi is in the scaled FP32 units).
+template <int MODE>
 struct EC {
-    double S, chi;
+    typename Real_<MODE>::T S, chi;
     bool ok;
 };
 
 template <int MODE>
-MGR_HD void elem_fresh(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e, EC& ec) {
+MGR_HD void elem_fresh(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e, EC<MODE>& ec) {
     if (ec.ok) return;
-    if (MODE == MODE_FP64) {
+    if constexpr (MODE == MODE_FP64) {
         double eta, chi;
         eta_chi_fp64(m, sl, c, e, eta, chi);
         ec.S = eta / chi;
         ec.chi = chi;
     } else {
         float eta, chi;
-        eta_chi_f32(m, sl, c, e, eta, chi);
-        ec.S = (double)(eta / chi) * (double)m.s_scale;
-        ec.chi = (double)chi;
+        eta_chi_f32(m, c, e, eta, chi);
+        ec.S = eta / chi * m.s_scale;
+        ec.chi = chi;
     }
     ec.ok = true;
 }
 
 // compute_source_dtau (solver.tpp:2139-2186) for the pair (lo, hi) with lo the lower
-// array index.  Fills the caches of both elements when the trapezoid rule is used.
+// array index, both elements of the half `h` (or the origin); dz (FP64 mode) or dzf
+// (split, scaled FP32) is the pair's distance.  Fills the caches of both elements
+// when the trapezoid rule is used.
 template <int MODE>
-MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
-                                          const Elem& hi, double dz, EC& ecl, EC& ech, PairOut& out) {
-    const double dshift_abs = fabs(dsub_rn(hi.shift, lo.shift));
-    const double a = m.dshift_max[lo.nr], b = m.dshift_max[hi.nr];
-    out.large = dshift_abs > (a < b ? a : b);
-    if (out.large) {
-        if (MODE == MODE_FP64) {
-            pair_li_fp64(m, sl, c, lo, hi, dz, out);
+MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& h, const Elem& lo,
+                      const Elem& hi, double dz, float dzf, EC<MODE>& ecl, EC<MODE>& ech, PairOut<MODE>& out) {
+    if constexpr (MODE == MODE_FP64) {
+        const double dshift_abs = fabs(dsub_rn(hi.shift, lo.shift));
+        const double a = m.dshift_max[lo.nr], b = m.dshift_max[hi.nr];
+        out.large = dshift_abs > (a < b ? a : b);
+    } else {
+        // the reference's branch test in FP32, and in FP64 within a margin of the
+        // threshold that covers the FP32 roundings of the shifts
+        const float dsf = fabsf(hi.dsh - lo.dsh);
+        const float thr = fminf(m.dshift_max_f[lo.nr], m.dshift_max_f[hi.nr]);
+        const float margin = 4.0e-3f * thr + 2.0e-6f * (lo.dshm + hi.dshm);
+        if (fabsf(dsf - thr) > margin) {
+            out.large = dsf > thr;
         } else {
-            float d, s1, s2;
-            pair_li_f32(m, sl, c, lo, hi, dz, d, s1, s2);
-            out.dtau = d;
-            out.Slo = s1;
-            out.Shi = s2;
+            double lsh, lfac, hsh, hfac;
+            elem_shift_fac(h, lo, lsh, lfac);
+            elem_shift_fac(h, hi, hsh, hfac);
+            const double dshift_abs = fabs(dsub_rn(hsh, lsh));
+            const double a = m.dshift_max[lo.nr], b = m.dshift_max[hi.nr];
+            out.large = dshift_abs > (a < b ? a : b);
+        }
+    }
+    if (out.large) {
+        if constexpr (MODE == MODE_FP64) {
+            pair_li_fp64(m, sl, c, lo, hi, dz, out.dtau, out.Slo, out.Shi);
+        } else {
+            pair_li_f32(m, c, h, lo, hi, dzf, out.dtau, out.Slo, out.Shi);
         }
     } else {
         elem_fresh<MODE>(m, sl, c, lo, ecl);
         elem_fresh<MODE>(m, sl, c, hi, ech);
-        if (MODE == MODE_FP64) {
+        if constexpr (MODE == MODE_FP64) {
             out.dtau = 0.5 * (ecl.chi + ech.chi) * dz;
         } else {
-            out.dtau = (double)(0.5f * ((float)ecl.chi + (float)ech.chi) * ((float)dz * m.dz_scale));
+            out.dtau = 0.5f * (ecl.chi + ech.chi) * dzf;
         }
     }
 }
 
-// Reciprocal of an elimination pivot.  FP64 mode: IEEE division, as the reference.
-// Split mode: an FP32 reciprocal refined by one Newton step in FP64 (relative error
-// ~1e-14), which keeps the elimination in FP64 without the cost of FP64 division.
+// Reciprocal of an elimination pivot (always >= 1).  FP64 mode: IEEE division, as
+// the reference.  Split mode: the hardware's approximate FP64 reciprocal (relative
+// error below 2^-22) refined by one Newton step (relative error ~1e-14).
 template <int MODE>
 MGR_HD double rcp_pivot(double x) {
     if (MODE == MODE_FP64) return 1.0 / x;
-    const float xf = (float)x;
-    if (!(xf > 1.0e-30f && xf < 1.0e30f)) return 1.0 / x;
 #ifdef __CUDA_ARCH__
-    const double r = (double)__frcp_rn(xf);
-#else
-    const double r = (double)(1.0f / xf);
-#endif
+    if (!(x < 1.0e300)) return 1.0 / x;
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
     return fma(r, fma(-x, r, 1.0), r);
+#else
+    return 1.0 / x;
+#endif
 }
 
 // One interior elimination row in the economical (1+B)/C form (solver.tpp:2266-2281
 // forward, :2304-2309 backward): `dt_out` is the optical depth of the pair already
 // eliminated, `dt_in` of the pair toward the origin.  F, FI = 1/(1+F) and the modified
-// source Su are updated in place.  Split mode computes the coefficients from the FP32
-// optical depths in FP32 and keeps the recurrence itself in FP64.
+// source Su are updated in place:
+//     F' = (A F FI + 1) C^-1,  FI' = 1/(1 + F'),  Su' = (A Su + S) FI' C^-1
+// with A = 1/(dtau_avg dt_out), C^-1 = dtau_avg dt_in.  Split mode forms the
+// coefficients A C^-1 = dt_in/dt_out and C^-1 from the FP32 optical depths and keeps
+// the recurrence in FP64.
 template <int MODE>
-MGR_HD void elim_row(double dt_out, double dt_in, double S, double& F, double& FI, double& Su) {
-    double A, iC;
-    if (MODE == MODE_FP64) {
+MGR_HD void elim_row(typename Real_<MODE>::T dt_out, typename Real_<MODE>::T dt_in, typename Real_<MODE>::T S,
+                     double& F, double& FI, double& Su) {
+    if constexpr (MODE == MODE_FP64) {
         const double dtau_avg = 0.5 * (dt_out + dt_in);
         const double iA = dtau_avg * dt_out;
-        iC = dtau_avg * dt_in;
-        A = 1.0 / iA;
+        const double iC = dtau_avg * dt_in;
+        const double A = 1.0 / iA;
+        F = (A * F * FI + 1.0) * iC;
+        FI = 1.0 / (1.0 + F);
+        Su = (A * Su + S) * FI * iC;
     } else {
-        const float a = (float)dt_out, b = (float)dt_in;
-        const float dtau_avg = 0.5f * (a + b);
-        const float iAf = dtau_avg * a, iCf = dtau_avg * b;
-        if (iAf > 1.0e-30f && iAf < 1.0e30f && iCf > 1.0e-30f && iCf < 1.0e30f) {
-            A = (double)(1.0f / iAf);
-            iC = (double)iCf;
-        } else {  // optical depths so small (or large) that their product leaves FP32 range
-            const double avg = 0.5 * (dt_out + dt_in);
-            A = 1.0 / (avg * dt_out);
-            iC = avg * dt_in;
+        double q, iC;
+        if (dt_out > 1.0e-18f && dt_out < 1.0e18f && dt_in > 1.0e-18f && dt_in < 1.0e18f) {
+            q = (double)fast_div(dt_in, dt_out);
+            iC = (double)(0.5f * (dt_out + dt_in) * dt_in);
+        } else {  // ratio or product would leave the FP32 range
+            const double o = dt_out, i = dt_in;
+            q = i / o;
+            iC = 0.5 * (o + i) * i;
         }
+        F = fma(q, F * FI, iC);
+        FI = rcp_pivot<MODE>(1.0 + F);
+        Su = fma(q, Su, (double)S * iC) * FI;
     }
-    F = (A * F * FI + 1.0) * iC;
-    FI = rcp_pivot<MODE>(1.0 + F);
-    Su = (A * Su + S) * FI * iC;
 }
 
 // Result of one lane's ray-pair solve.
@@ -591,8 +696,9 @@ struct LaneResult {
 // Two-sided Feautrier solve of frequency c.f on the ray pair staged in `bk`
 // (backward half, direction rr) and `fw` (forward half, antipode).
 template <int MODE>
-__host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk, int nb,
-                                 const HalfSmem& fw, int nf) {
+__host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
+                                          int nb, const HalfSmem& fw, int nf) {
+    using T = typename Real_<MODE>::T;
     LaneResult res;
     res.solved = (nb > 0) || (nf > 0);
     if (!res.solved) {
@@ -604,37 +710,44 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     const uint32_t l = c.l0;
 
     // ---- top sweep: elements first .. centre (backward half, outer end first) ----
-    double FF = 0.0, FI = 0.0, Su = 0.0, dt_top = 0.0;
-    bool top_rows = false;     // at least one row eliminated
-    bool top_large = false;    // last pair line-integrated
-    double top_Shi = 0.0;      // its upper source
-    EC ec_cen{0.0, 0.0, false};
+    double FF = 0.0, FI = 0.0, Su = 0.0;
+    T dt_top = T(0);
+    bool top_rows = false;   // at least one row eliminated
+    bool top_large = false;  // last pair line-integrated
+    T top_Shi = T(0);        // its upper source
+    EC<MODE> ec_cen{T(0), T(0), false};
     if (nb > 0) {
         ElemIter it;
-        iter_begin(m, bk, c.o, l, nb, it);
+        iter_begin<MODE>(m, bk, c.o, l, nb, it);
         Elem prev;
-        iter_next(m, bk, c.o, l, it, prev);
-        EC ec_prev{0.0, 0.0, false};
-        const double Ibdy = boundary_intensity(m, prev.nr, c.freq * prev.shift);
+        iter_next<MODE>(m, bk, c.o, l, it, prev);
+        EC<MODE> ec_prev{T(0), T(0), false};
+        double bshift = prev.shift;
+        if constexpr (MODE == MODE_SPLIT) {
+            double fac;
+            elem_shift_fac(bk, prev, bshift, fac);
+        }
+        const double Ibdy = boundary_intensity(m, prev.nr, c.freq * bshift);
         bool first = true;
         while (true) {
             Elem cur;
-            const bool more = iter_next(m, bk, c.o, l, it, cur);
+            const bool more = iter_next<MODE>(m, bk, c.o, l, it, cur);
             if (!more) cur = cen;
-            EC ec_cur{0.0, 0.0, false};
-            PairOut po;
-            eval_pair<MODE>(m, sl, c, prev, cur, prev.dzin, ec_prev, more ? ec_cur : ec_cen, po);
-            double S;
+            EC<MODE> ec_cur{T(0), T(0), false};
+            PairOut<MODE> po;
+            eval_pair<MODE>(m, sl, c, bk, prev, cur, prev.dzin, prev.dzf, ec_prev, more ? ec_cur : ec_cen, po);
+            T S;
             if (po.large) S = po.Slo;
             else { elem_fresh<MODE>(m, sl, c, prev, ec_prev); S = ec_prev.S; }
             if (first) {
-                const double inverse_dtau_f = 1.0 / po.dtau;
+                const double dt = po.dtau;
+                const double inverse_dtau_f = 1.0 / dt;
                 const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
                 const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
                 const double Bf = Bf_min_Cf + Cf;
-                Su = (S + 2.0 * Ibdy * inverse_dtau_f) / Bf;
-                FF = 0.5 * Bf_min_Cf * po.dtau * po.dtau;
-                FI = rcp_pivot<MODE>(1.0 + FF);
+                Su = ((double)S + 2.0 * Ibdy * inverse_dtau_f) / Bf;
+                FF = 0.5 * Bf_min_Cf * dt * dt;
+                FI = 1.0 / (1.0 + FF);
                 first = false;
             } else {
                 elim_row<MODE>(dt_top, po.dtau, S, FF, FI, Su);
@@ -650,40 +763,47 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     }
 
     // ---- bottom sweep: elements last .. centre+1 (forward half, outer end first) ----
-    double GG = 0.0, GI = 0.0, Sb = 0.0, dt_bot = 0.0, S_centre = 0.0;
+    double GG = 0.0, GI = 0.0, Sb = 0.0;
+    T dt_bot = T(0), S_centre = T(0);
     bool bot_rows = false;
     if (nf > 0) {
         ElemIter it;
-        iter_begin(m, fw, c.o, l, nf, it);
+        iter_begin<MODE>(m, fw, c.o, l, nf, it);
         Elem prev;  // higher index element
-        iter_next(m, fw, c.o, l, it, prev);
-        EC ec_prev{0.0, 0.0, false};
-        const double Ibdy = boundary_intensity(m, prev.nr, c.freq * prev.shift);
+        iter_next<MODE>(m, fw, c.o, l, it, prev);
+        EC<MODE> ec_prev{T(0), T(0), false};
+        double bshift = prev.shift;
+        if constexpr (MODE == MODE_SPLIT) {
+            double fac;
+            elem_shift_fac(fw, prev, bshift, fac);
+        }
+        const double Ibdy = boundary_intensity(m, prev.nr, c.freq * bshift);
         bool first = true;
-        double S_prev_row = 0.0;  // row source of `prev` (known once its upper pair was evaluated)
+        T S_prev_row = T(0);  // row source of `prev` (known once its upper pair was evaluated)
         while (true) {
             Elem cur;  // lower index element
-            const bool more = iter_next(m, fw, c.o, l, it, cur);
+            const bool more = iter_next<MODE>(m, fw, c.o, l, it, cur);
             if (!more) cur = cen;
-            EC ec_cur{0.0, 0.0, false};
-            EC& ecc = more ? ec_cur : ec_cen;
-            PairOut po;
-            eval_pair<MODE>(m, sl, c, cur, prev, prev.dzin, ecc, ec_prev, po);
+            EC<MODE> ec_cur{T(0), T(0), false};
+            EC<MODE>& ecc = more ? ec_cur : ec_cen;
+            PairOut<MODE> po;
+            eval_pair<MODE>(m, sl, c, fw, cur, prev, prev.dzin, prev.dzf, ecc, ec_prev, po);
             // Row source of the lower element `cur` (index < last).
-            double S_cur;
+            T S_cur;
             if (po.large) S_cur = po.Slo;
             else { elem_fresh<MODE>(m, sl, c, cur, ecc); S_cur = ecc.S; }
             if (first) {
-                double S_last;
+                T S_last;
                 if (po.large) S_last = po.Shi;
                 else { elem_fresh<MODE>(m, sl, c, prev, ec_prev); S_last = ec_prev.S; }
-                const double inverse_dtau_l = 1.0 / po.dtau;
+                const double dt = po.dtau;
+                const double inverse_dtau_l = 1.0 / dt;
                 const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
                 const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
                 const double Bl = Bl_min_Al + Al;
-                Sb = (S_last + 2.0 * Ibdy * inverse_dtau_l) / Bl;
-                GG = 0.5 * Bl_min_Al * po.dtau * po.dtau;
-                GI = rcp_pivot<MODE>(1.0 + GG);
+                Sb = ((double)S_last + 2.0 * Ibdy * inverse_dtau_l) / Bl;
+                GG = 0.5 * Bl_min_Al * dt * dt;
+                GI = 1.0 / (1.0 + GG);
                 first = false;
             } else {
                 // row `prev`: upper pair dt_bot already eliminated, lower pair = this pair
@@ -703,39 +823,42 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
 
     // ---- combine at the origin ----
     if (top_rows && bot_rows) {
-        const double dtau_avg = 0.5 * (dt_top + dt_bot);
-        const double iA = dtau_avg * dt_top;
-        const double iC = dtau_avg * dt_bot;
+        const double dtt = dt_top, dtb = dt_bot;
+        const double dtau_avg = 0.5 * (dtt + dtb);
+        const double iA = dtau_avg * dtt;
+        const double iC = dtau_avg * dtb;
         const double A = 1.0 / iA;
         const double FFc = (A * FF * FI + 1.0) * iC;
-        const double Su_pre = (A * Su + S_centre) * iC;
+        const double Su_pre = (A * Su + (double)S_centre) * iC;
         const double GP = GG * GI;
         const double D = 1.0 / (FFc + GP);
         res.u = (Su_pre + Sb) * D;
         res.Ldiag = iC * D;
     } else if (bot_rows) {  // origin is the first element
         const double Ibdy = boundary_intensity(m, c.o, c.freq);
-        const double inverse_dtau_f = 1.0 / dt_bot;
+        const double dtb = dt_bot;
+        const double inverse_dtau_f = 1.0 / dtb;
         const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
         const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
         const double Bf = Bf_min_Cf + Cf;
-        const double Suf = (S_centre + 2.0 * Ibdy * inverse_dtau_f) / Bf;
-        const double FFf = 0.5 * Bf_min_Cf * dt_bot * dt_bot;
+        const double Suf = ((double)S_centre + 2.0 * Ibdy * inverse_dtau_f) / Bf;
+        const double FFf = 0.5 * Bf_min_Cf * dtb * dtb;
         const double GP = GG * GI;
         const double D = 1.0 / (FFf + GP);
         res.u = (Suf * (1.0 + FFf) + Sb) * D;
         res.Ldiag = (1.0 / Cf) * D;
     } else {  // origin is the last element
         const double Ibdy = boundary_intensity(m, c.o, c.freq);
-        double S_last;
+        T S_last;
         if (top_large) S_last = top_Shi;
         else { elem_fresh<MODE>(m, sl, c, cen, ec_cen); S_last = ec_cen.S; }
-        const double inverse_dtau_l = 1.0 / dt_top;
+        const double dtt = dt_top;
+        const double inverse_dtau_l = 1.0 / dtt;
         const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
         const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
         const double Bl = Bl_min_Al + Al;
         const double denominator = 1.0 / (Bl * FF + Bl_min_Al);
-        const double Sl = S_last + 2.0 * Ibdy * inverse_dtau_l;
+        const double Sl = (double)S_last + 2.0 * Ibdy * inverse_dtau_l;
         res.u = (Al * Su + Sl) * (1.0 + FF) * denominator;
         res.Ldiag = (1.0 + FF) / (Bl_min_Al + Bl * FF);
     }
