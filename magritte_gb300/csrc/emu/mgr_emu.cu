@@ -74,6 +74,7 @@ struct EmuModel {
     std::vector<double> ub, Sp;
     std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll;
     std::vector<uint16_t> nint;
+    std::vector<uint32_t> lq2f;
     DevModel m{};
 };
 
@@ -139,6 +140,9 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     line_offset_tables(d->line, d->sorted_line, L, x.dls, x.dll);
     m.dls = x.dls.data();
     m.dll = x.dll.data();
+    x.lq2f.assign((size_t)L * d->nquads, 0xffffffffu);
+    for (uint32_t f = 0; f < F; f++) x.lq2f[(size_t)d->corr_line[f] * d->nquads + d->corr_z[f]] = f;
+    m.lq2f = x.lq2f.data();
     x.nint.resize((E ? E : 1) * (size_t)L);
     for (uint32_t p = 0; p < P; p++)
         for (uint32_t k = 0; k < d->n_neighbors[p]; k++)
@@ -171,42 +175,80 @@ LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {
 
 constexpr uint32_t kCap = 1u << 16;
 
+template <int MODE>
+LaneResult solve_any(const DevModel& m, const LaneCtx& c, const HalfSmem& bk, int nb, const HalfSmem& fw, int nf) {
+    switch (m.approx) {
+        case APPROX_ONELINE: return solve_lane<MODE, APPROX_ONELINE>(m, m.sorted_line, c, bk, nb, fw, nf);
+        case APPROX_CLOSELINES: return solve_lane<MODE, APPROX_CLOSELINES>(m, m.sorted_line, c, bk, nb, fw, nf);
+        default: return solve_lane<MODE, APPROX_NONE>(m, m.sorted_line, c, bk, nb, fw, nf);
+    }
+}
+
+LaneResult solve(const DevModel& m, int precision, const LaneCtx& c, const HalfSmem& bk, int nb, const HalfSmem& fw,
+                 int nf) {
+    return precision == MGR_PRECISION_SPLIT ? solve_any<MODE_SPLIT>(m, c, bk, nb, fw, nf)
+                                            : solve_any<MODE_FP64>(m, c, bk, nb, fw, nf);
+}
+
 }  // namespace
 
+// The kernel's two stages for every origin: per (rr, f) lane solves, then J and the
+// ALO summed in (rr, q) order as fo2_reduce_kernel does.
 extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, double* J, double* lam) {
     EmuModel x;
     build_emu_model(d, x);
     const DevModel& m = x.m;
-    const uint32_t P = m.P, L = m.L, F = m.F;
+    const uint32_t P = m.P, L = m.L, F = m.F, R = m.hnrays, Q = m.Q;
     int err = 0;
 #pragma omp parallel
     {
         HalfBuf b(kCap), fbuf(kCap);
         HalfSmem bk = b.view(), fw = fbuf.view();
+        std::vector<double> U((size_t)R * F), LD((size_t)R * F);
 #pragma omp for schedule(dynamic, 16)
         for (long long oo = 0; oo < (long long)P; oo++) {
             const uint32_t o = (uint32_t)oo;
-            for (uint32_t f = 0; f < F; f++) J[(size_t)o * F + f] = 0.0;
-            if (lam)
-                for (uint32_t l = 0; l < L; l++) lam[(size_t)o * L + l] = 0.0;
-            for (uint32_t rr = 0; rr < m.hnrays; rr++) {
+            bool ok = true;
+            for (uint32_t rr = 0; rr < R && ok; rr++) {
                 const int nb = trace_half_host(m, o, rr, kCap, bk);
                 const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
                 if (nb < 0 || nf < 0) {
-#pragma omp atomic write
-                    err = 1;
-                    continue;
+                    ok = false;
+                    break;
                 }
                 for (uint32_t f = 0; f < F; f++) {
-                    const LaneCtx c = lane_ctx(m, o, f);
-                    const LaneResult r = precision == MGR_PRECISION_SPLIT
-                                             ? solve_lane<MODE_SPLIT>(m, m.sorted_line, c, bk, nb, fw, nf)
-                                             : solve_lane<MODE_FP64>(m, m.sorted_line, c, bk, nb, fw, nf);
-                    if (r.solved) J[(size_t)o * F + f] += r.u * 2.0 * m.rayw[rr];
-                    else J[(size_t)o * F + f] += 2.0 * m.rayw[rr] * r.u;
-                    if (lam && r.solved && m.in_line[f])
-                        lam[(size_t)o * L + m.corr_line[f]] += lambda_element(m, m.sorted_line, o, rr, f, r.Ldiag);
+                    const LaneResult r = solve(m, precision, lane_ctx(m, o, f), bk, nb, fw, nf);
+                    U[(size_t)rr * F + f] = r.u;
+                    LD[(size_t)rr * F + f] = r.solved ? r.Ldiag : 0.0;
                 }
+            }
+            if (!ok) {
+#pragma omp atomic write
+                err = 1;
+                continue;
+            }
+            for (uint32_t f = 0; f < F; f++) {
+                double s = 0.0;
+                for (uint32_t rr = 0; rr < R; rr++) s += U[(size_t)rr * F + f] * 2.0 * m.rayw[rr];
+                J[(size_t)o * F + f] = s;
+            }
+            if (!lam) continue;
+            for (uint32_t l = 0; l < L; l++) {
+                std::vector<LambdaFactors> k(Q);
+                for (uint32_t q = 0; q < Q; q++) {
+                    const uint32_t f = m.lq2f[(size_t)l * Q + q];
+                    if (f != 0xffffffffu && m.in_line[f]) k[q] = lambda_factors(m, m.sorted_line, o, f);
+                }
+                double s = 0.0;
+                for (uint32_t rr = 0; rr < R; rr++)
+                    for (uint32_t q = 0; q < Q; q++) {
+                        const uint32_t f = m.lq2f[(size_t)l * Q + q];
+                        const double e = (f != 0xffffffffu && m.in_line[f])
+                                             ? lambda_element(k[q], m.rayw[rr], LD[(size_t)rr * F + f])
+                                             : 0.0;
+                        s += e;
+                    }
+                lam[(size_t)o * L + l] = s;
             }
         }
     }
@@ -224,9 +266,7 @@ extern "C" int mgr_emu_lane(const MgrModelDesc* d, int precision, uint32_t o, ui
     const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fbuf.view());
     if (nb < 0 || nf < 0) return MGR_ERR_TRACE;
     const LaneCtx c = lane_ctx(m, o, f);
-    const LaneResult r = precision == MGR_PRECISION_SPLIT
-                             ? solve_lane<MODE_SPLIT>(m, m.sorted_line, c, b.view(), nb, fbuf.view(), nf)
-                             : solve_lane<MODE_FP64>(m, m.sorted_line, c, b.view(), nb, fbuf.view(), nf);
+    const LaneResult r = solve(m, precision, c, b.view(), nb, fbuf.view(), nf);
     out[0] = r.u;
     out[1] = r.Ldiag;
     out[2] = r.solved ? 1.0 : 0.0;

@@ -140,6 +140,7 @@ void mgr_model_free(MgrModel* model) {
     if (model->J_scratch) cudaFree(model->J_scratch);
     if (model->u_scratch) cudaFree(model->u_scratch);
     if (model->lam_scratch) cudaFree(model->lam_scratch);
+    if (model->work) cudaFree(model->work);
     if (model->stream) cudaStreamDestroy(model->stream);
     delete model;
 }
@@ -210,6 +211,8 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
 
     MgrModel* m = new MgrModel();
     cudaGetDevice(&m->device);
+    cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device);
+    if (m->sm_count < 1) m->sm_count = 1;
     cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete m;
@@ -253,6 +256,11 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     for (uint32_t p = 0; p < P; p++) dsm_f[p] = (float)d->dshift_max[p];
     std::vector<float> dls, dll;
     line_offset_tables(d->line, d->sorted_line, L, dls, dll);
+    std::vector<uint32_t> lq2f((size_t)L * d->nquads, 0xffffffffu);
+    for (uint32_t f = 0; f < F; f++) {
+        const size_t i = (size_t)d->corr_line[f] * d->nquads + d->corr_z[f];
+        if (d->corr_line[f] < L && d->corr_z[f] < d->nquads) lq2f[i] = f;
+    }
 
     const size_t PL = (size_t)P * L;
     do {
@@ -271,6 +279,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.sorted_line, d->sorted_line, L)) != cudaSuccess) break;
         if ((e = upload(m, &dm.sorted_map, d->sorted_line_map, L)) != cudaSuccess) break;
         if ((e = upload(m, &dm.dls, dls.data(), (size_t)L * L)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.lq2f, lq2f.data(), lq2f.size())) != cudaSuccess) break;
         if ((e = upload(m, &dm.dll, dll.data(), (size_t)L * L)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->em, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->op, PL)) != cudaSuccess) break;
@@ -440,7 +449,11 @@ int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, d
         set_error("mgr_formal_solve_fo2_device: unknown precision mode");
         return MGR_ERR_ARGUMENT;
     }
-    cudaError_t e = launch_fo2(model, precision, J_dev, u_dev, lambda_diag_dev);
+    const size_t wb = fo2_work_bytes(model, model->dm.P, u_dev == nullptr, lambda_diag_dev != nullptr);
+    int rc = ensure_scratch(model, &model->work, &model->work_bytes, wb);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = launch_fo2_range(model, precision, 0, model->dm.P, J_dev, u_dev, lambda_diag_dev, model->work,
+                                     model->work_bytes);
     if (e != cudaSuccess) return cuda_fail(e, "formal solve launch");
     return MGR_OK;
 }
@@ -523,6 +536,8 @@ int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int
     const uint32_t o0 = (dm.P - n) / 2, o1 = o0 + n;
     int rc = ensure_scratch(model, &model->J_scratch, &model->J_scratch_bytes, (size_t)dm.P * dm.F * 8);
     if (rc != MGR_OK) return rc;
+    rc = ensure_scratch(model, &model->work, &model->work_bytes, fo2_work_bytes(model, n, true, false));
+    if (rc != MGR_OK) return rc;
     int& minb = precision == MGR_PRECISION_SPLIT ? model->fo2_minb_split : model->fo2_minb_fp64;
     const int keep_minb = minb, keep_warps = model->fo2_warps;
     cudaEvent_t e0, e1;
@@ -537,9 +552,12 @@ int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int
         for (int wi = 0; wi < 2 && e == cudaSuccess; wi++) {
             minb = minbs[mi];
             model->fo2_warps = warps[wi];
-            e = launch_fo2_range(model, precision, o0, o1, model->J_scratch, nullptr, nullptr);  // warm
+            e = launch_fo2_range(model, precision, o0, o1, model->J_scratch, nullptr, nullptr, model->work,
+                                 model->work_bytes);  // warm
             if (e == cudaSuccess) e = cudaEventRecord(e0, model->stream);
-            if (e == cudaSuccess) e = launch_fo2_range(model, precision, o0, o1, model->J_scratch, nullptr, nullptr);
+            if (e == cudaSuccess)
+                e = launch_fo2_range(model, precision, o0, o1, model->J_scratch, nullptr, nullptr, model->work,
+                                     model->work_bytes);
             if (e == cudaSuccess) e = cudaEventRecord(e1, model->stream);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float ms = 0.0f;

@@ -91,6 +91,7 @@ struct DevModel {
     double max_interp_diff;
     double max_dist;
     float log_max_interp_diff;   // logf((float)max_interp_diff)
+    const uint32_t* lq2f;        // [L][Q] frequency of (line, quadrature point), ~0u if none
     // Split precision keeps FP32 line data in scaled units (exact powers of two):
     // em_f = em * Ke, op_f = op * Ko, Sp_f = Sp * Ke / Ko.
     const float* dls;            // [L][L] (float)(sorted_line[s] - line[l0]) at l0*L + s

@@ -126,78 +126,111 @@ __global__ void ray_lengths_kernel(DevModel m, uint32_t cap, uint32_t* d_max, in
 }
 
 // ---------------------------------------------------------------------------------
-// Formal solve: one CTA per origin, one warp per ray pair, one lane per frequency.
+// Formal solve, stage 1: one warp per (origin, ray pair) item, one lane per frequency.
+// Warps take items in a grid-stride loop over a persistent grid (no block-level
+// synchronisation); items of one origin are adjacent, so the warps of a CTA share
+// the origin's neighbourhood in L1.  Each item writes u(rr, o, f) and, when the ALO
+// is wanted, L_diag(rr, o, f): U[rr * u_stride + (o - u_o0) * F + f].
 // ---------------------------------------------------------------------------------
 // MINB = CTAs of 256 threads resident per SM the register budget is sized for
 // (2: 128, 3: 80, 4: 64 registers per thread); picked at run time by the tuner.
-template <int MODE, int MINB>
-__global__ void __launch_bounds__(256, MINB) fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end,
-                                                        double* __restrict__ J, double* __restrict__ u,
-                                                        double* __restrict__ lam, int* status) {
+template <int MODE, int AP, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end, double* __restrict__ U, size_t u_stride,
+               uint32_t u_o0, double* __restrict__ LD, size_t ld_stride, uint32_t ld_o0, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     double* sl = reinterpret_cast<double*>(smem);
     const uint32_t Lpad = (m.L + 1) & ~1u;
-    double* Jw = sl + Lpad;
-    double* Lw = Jw + (size_t)nw * m.F;
-    unsigned char* tb = reinterpret_cast<unsigned char*>(Lw + (size_t)nw * m.F);
     HalfSmem bk, fw;
-    carve_halves(tb + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
+    carve_halves(smem + (size_t)Lpad * 8 + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
     for (uint32_t i = threadIdx.x; i < m.L; i += blockDim.x) sl[i] = m.sorted_line[i];
+    __syncthreads();
 
-    for (uint32_t o = o_begin + blockIdx.x; o < o_end; o += gridDim.x) {
-        for (uint32_t f = lane; f < m.F; f += 32) {
-            Jw[(size_t)w * m.F + f] = 0.0;
-            Lw[(size_t)w * m.F + f] = 0.0;
-        }
-        __syncthreads();
-        for (uint32_t rr = w; rr < m.hnrays; rr += nw) {
-            const uint32_t ar = m.antipod[rr];
-            const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-            const int nf = trace_half<true>(m, o, ar, cap, fw, lane, status);
-            if (nb < 0 || nf < 0) continue;
-            const double wrr = m.rayw[rr];
-            for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
-                const uint32_t f = f0 + lane;
-                if (f < m.F) {
-                    LaneCtx c;
-                    c.o = o;
-                    c.f = f;
-                    c.l0 = m.corr_line[f];
-                    c.freq = m.nu[(size_t)o * m.F + f];
-                    c.fq = (float)c.freq;
-                    c.a0 = (float)(c.freq - m.line[c.l0]);
-                    const LaneResult r = solve_lane<MODE>(m, sl, c, bk, nb, fw, nf);
-                    double contribution;
-                    if (r.solved) contribution = r.u * 2.0 * wrr;
-                    else contribution = 2.0 * wrr * r.u;
-                    Jw[(size_t)w * m.F + f] += contribution;
-                    if (u) u[((size_t)rr * m.P + o) * m.F + f] = r.u;
-                    if (r.solved && m.in_line[f]) Lw[(size_t)w * m.F + f] += lambda_element(m, sl, o, rr, f, r.Ldiag);
-                    if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
-                }
+    const uint32_t R = m.hnrays;
+    const uint64_t n_items = (uint64_t)(o_end - o_begin) * R;
+    const uint64_t stride = (uint64_t)gridDim.x * nw;
+    for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
+        const uint32_t o = o_begin + (uint32_t)(item / R);
+        const uint32_t rr = (uint32_t)(item % R);
+        const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
+        const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+        if (nb < 0 || nf < 0) continue;  // status recorded by the trace
+        double* Ui = U + (size_t)rr * u_stride + (size_t)(o - u_o0) * m.F;
+        double* Li = LD ? LD + (size_t)rr * ld_stride + (size_t)(o - ld_o0) * m.F : nullptr;
+        for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
+            const uint32_t f = f0 + lane;
+            if (f < m.F) {
+                LaneCtx c;
+                c.o = o;
+                c.f = f;
+                c.l0 = m.corr_line[f];
+                c.freq = m.nu[(size_t)o * m.F + f];
+                c.fq = (float)c.freq;
+                c.a0 = (float)(c.freq - m.line[c.l0]);
+                const LaneResult r = solve_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
+                Ui[f] = r.u;
+                if (Li) Li[f] = r.solved ? r.Ldiag : 0.0;
+                if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
             }
-            __syncwarp();
         }
-        __syncthreads();
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Formal solve, stage 2: J and the ALO diagonal per origin, summed over ray pairs in
+// the reference's order (ray pair outer, quadrature point inner):
+//   J(o, f)   = sum_rr u(rr, o, f) 2 w_rr                               (solver.tpp:497-504)
+//   Lambda(o, l) = sum_rr sum_q lambda_element(o, rr, f(l, q))          (update_Lambda)
+// One CTA per origin (grid-stride); J by threads over f, the ALO by warps over lines
+// with lanes over quadrature points.  lq2f[l * Q + q] is the frequency of (l, q).
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_begin, uint32_t o_end,
+                                                         const double* __restrict__ U, size_t u_stride, uint32_t u_o0,
+                                                         const double* __restrict__ LD, size_t ld_stride,
+                                                         uint32_t ld_o0, double* __restrict__ J,
+                                                         double* __restrict__ lam) {
+    const int nw = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint32_t R = m.hnrays;
+    for (uint32_t o = o_begin + blockIdx.x; o < o_end; o += gridDim.x) {
         for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
+            const double* Uo = U + (size_t)(o - u_o0) * m.F + f;
             double s = 0.0;
-            for (int ww = 0; ww < nw; ww++) s += Jw[(size_t)ww * m.F + f];
+            for (uint32_t rr = 0; rr < R; rr++) s += Uo[(size_t)rr * u_stride] * 2.0 * m.rayw[rr];
             J[(size_t)o * m.F + f] = s;
         }
-        if (lam) {
-            for (uint32_t lid = threadIdx.x; lid < m.L; lid += blockDim.x) {
-                double s = 0.0;
-                for (uint32_t z = 0; z < m.Q; z++) {
-                    const uint32_t f = lid * m.Q + z;
-                    for (int ww = 0; ww < nw; ww++) s += Lw[(size_t)ww * m.F + f];
+        if (!lam) continue;
+        for (uint32_t l = w; l < m.L; l += nw) {
+            // Lane q holds the ray-independent factors of quadrature point q (computed
+            // once when Q <= 32, per ray pair otherwise); each ray pair's elements are
+            // added lane by lane, i.e. in (rr, q) order.
+            const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
+            const bool once = m.Q <= 32;
+            LambdaFactors k{0.0, 0.0, 0.0, 0.0};
+            uint32_t f = lane < m.Q ? l2f[lane] : 0xffffffffu;
+            bool valid = f != 0xffffffffu && m.in_line[f];
+            if (once && valid) k = lambda_factors(m, m.sorted_line, o, f);
+            double s = 0.0;
+            for (uint32_t rr = 0; rr < R; rr++) {
+                const double* Lr = LD + (size_t)rr * ld_stride + (size_t)(o - ld_o0) * m.F;
+                for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
+                    if (!once) {
+                        f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
+                        valid = f != 0xffffffffu && m.in_line[f];
+                        if (valid) k = lambda_factors(m, m.sorted_line, o, f);
+                    }
+                    const double e = valid ? lambda_element(k, m.rayw[rr], Lr[f]) : 0.0;
+                    const uint32_t nq = min(32u, m.Q - q0);
+                    for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
                 }
-                lam[(size_t)o * m.L + lid] = s;
             }
+            if (lane == 0) lam[(size_t)o * m.L + l] = s;
         }
-        __syncthreads();
     }
 }
 
@@ -359,43 +392,111 @@ cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats) {
     return cudaGetLastError();
 }
 
-template <int MODE, int MINB>
-static cudaError_t launch_fo2_mode(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* J, double* u,
-                                   double* lam) {
+// Bytes of U / L_diag staging per origin and the origins one chunk may hold.
+static size_t fo2_bytes_per_origin(const MgrModel* model) {
+    return (size_t)model->dm.hnrays * model->dm.F * sizeof(double);
+}
+
+size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, bool stage_ld) {
+    const int k = (stage_u ? 1 : 0) + (stage_ld ? 1 : 0);
+    if (k == 0 || n_origins == 0) return 0;
+    const size_t per = fo2_bytes_per_origin(model) * k;
+    size_t chunk = kFo2WorkBudget / per;
+    if (chunk < 1) chunk = 1;
+    if (chunk > n_origins) chunk = n_origins;
+    return chunk * per;
+}
+
+template <int MODE, int AP, int MINB>
+static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* U, size_t u_stride,
+                                      uint32_t u_o0, double* LD, size_t ld_stride, uint32_t ld_o0) {
     const DevModel& m = model->dm;
     const uint32_t cap = model->half_cap;
     int nw = model->fo2_warps > 0 ? model->fo2_warps : 8;
     if (nw > 8) nw = 8;
-    if ((uint32_t)nw > m.hnrays) nw = (int)m.hnrays;
-    if (nw < 1) nw = 1;
     const uint32_t Lpad = (m.L + 1) & ~1u;
-    const size_t smem = (size_t)Lpad * 8 + 2ull * nw * m.F * 8 + (size_t)nw * half_bytes_per_warp(cap);
-    cudaError_t e =
-        cudaFuncSetAttribute(fo2_kernel<MODE, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = (size_t)Lpad * 8 + (size_t)nw * half_bytes_per_warp(cap);
+    auto kern = fo2_kernel<MODE, AP, MINB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nw * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;  // the ray buffers do not fit in shared memory
+    const uint64_t items = (uint64_t)(o_end - o_begin) * m.hnrays;
+    uint64_t grid = (uint64_t)model->sm_count * per_sm;
+    const uint64_t need = (items + nw - 1) / nw;
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
     count_launch();
-    const uint32_t grid = o_end > o_begin ? o_end - o_begin : 1;
-    fo2_kernel<MODE, MINB><<<grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, J, u, lam, model->status);
+    kern<<<(unsigned)grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, U, u_stride, u_o0, LD, ld_stride,
+                                                          ld_o0, model->status);
     return cudaGetLastError();
 }
 
-template <int MODE>
-static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* J, double* u,
-                                   double* lam) {
+template <int MODE, int AP>
+static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* U, size_t us,
+                                   uint32_t uo, double* LD, size_t ls, uint32_t lo) {
     const int minb = (MODE == MODE_SPLIT) ? model->fo2_minb_split : model->fo2_minb_fp64;
-    if (minb == 2) return launch_fo2_mode<MODE, 2>(model, o_begin, o_end, J, u, lam);
-    if (minb == 4) return launch_fo2_mode<MODE, 4>(model, o_begin, o_end, J, u, lam);
-    return launch_fo2_mode<MODE, 3>(model, o_begin, o_end, J, u, lam);
+    if (minb == 2) return launch_fo2_variant<MODE, AP, 2>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+    if (minb == 4) return launch_fo2_variant<MODE, AP, 4>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+    return launch_fo2_variant<MODE, AP, 3>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+}
+
+template <int MODE>
+static cudaError_t launch_fo2_approx(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* U, size_t us,
+                                     uint32_t uo, double* LD, size_t ls, uint32_t lo) {
+    switch (model->dm.approx) {
+        case APPROX_ONELINE: return launch_fo2_minb<MODE, APPROX_ONELINE>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+        case APPROX_CLOSELINES:
+            return launch_fo2_minb<MODE, APPROX_CLOSELINES>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+        default: return launch_fo2_minb<MODE, APPROX_NONE>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+    }
 }
 
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
-                             double* lam) {
-    if (precision == MGR_PRECISION_SPLIT) return launch_fo2_minb<MODE_SPLIT>(model, o_begin, o_end, J, u, lam);
-    return launch_fo2_minb<MODE_FP64>(model, o_begin, o_end, J, u, lam);
-}
-
-cudaError_t launch_fo2(MgrModel* model, int precision, double* J, double* u, double* lam) {
-    return launch_fo2_range(model, precision, 0, model->dm.P, J, u, lam);
+                             double* lam, double* work, size_t work_bytes) {
+    const DevModel& m = model->dm;
+    if (o_end <= o_begin) return cudaSuccess;
+    const int k = (u ? 0 : 1) + (lam ? 1 : 0);
+    const size_t per = fo2_bytes_per_origin(model);
+    uint32_t chunk = o_end - o_begin;
+    if (k) {
+        const size_t fit = work ? work_bytes / (per * k) : 0;
+        if (fit < 1) return cudaErrorInvalidValue;  // caller sizes the work area with fo2_work_bytes
+        if (fit < chunk) chunk = (uint32_t)fit;
+    }
+    int nsm = model->sm_count;
+    for (uint32_t c0 = o_begin; c0 < o_end; c0 += chunk) {
+        const uint32_t c1 = (o_end - c0 > chunk) ? c0 + chunk : o_end;
+        const uint32_t n = c1 - c0;
+        double* U;
+        size_t us;
+        uint32_t uo;
+        double* next = work;
+        if (u) {
+            U = u;
+            us = (size_t)m.P * m.F;
+            uo = 0;
+        } else {
+            U = work;
+            us = (size_t)n * m.F;
+            uo = c0;
+            next = work + (size_t)m.hnrays * n * m.F;
+        }
+        double* LD = lam ? next : nullptr;
+        const size_t ls = (size_t)n * m.F;
+        cudaError_t e = (precision == MGR_PRECISION_SPLIT)
+                            ? launch_fo2_approx<MODE_SPLIT>(model, c0, c1, U, us, uo, LD, ls, c0)
+                            : launch_fo2_approx<MODE_FP64>(model, c0, c1, U, us, uo, LD, ls, c0);
+        if (e != cudaSuccess) return e;
+        unsigned grid = n < (uint32_t)nsm * 16 ? n : (unsigned)nsm * 16;
+        count_launch();
+        fo2_reduce_kernel<<<grid, 128, 0, model->stream>>>(m, c0, c1, U, us, uo, LD, ls, c0, J, lam);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,

@@ -28,6 +28,7 @@ struct MgrModel {
     int fo2_warps = 8;               // warps (ray pairs in flight) per CTA of the formal solve
     int fo2_minb_split = 3;          // register budget variant: CTAs per SM (2, 3 or 4)
     int fo2_minb_fp64 = 3;
+    int sm_count = 1;                // multiprocessors of the model's device
     int* status = nullptr;           // device status word
     mgr::LineScales scales;          // FP32 line-table scales (split precision)
     uint32_t half_cap = 0;           // longest half ray in base steps (0 = not sized yet)
@@ -39,6 +40,9 @@ struct MgrModel {
     size_t u_scratch_bytes = 0;
     double* lam_scratch = nullptr;
     size_t lam_scratch_bytes = 0;
+    // staging of u(rr, o, f) / L_diag(rr, o, f) between the two formal-solve stages
+    double* work = nullptr;
+    size_t work_bytes = 0;
 };
 
 namespace mgr {
@@ -49,9 +53,13 @@ void count_launch();
 
 // Kernel launchers (mgr_fo2.cu).  All enqueue on model->stream.
 cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps);
-cudaError_t launch_fo2(MgrModel* model, int precision, double* J, double* u, double* lam);
+// Formal solve of origins [o_begin, o_end): J [P][F] and lam [P][L] rows of those
+// origins, u [hnrays][P][F] (may be NULL).  Per-ray results are staged in `work`
+// (sized by fo2_work_bytes for the same u / lam choice), in chunks of origins that fit.
+constexpr size_t kFo2WorkBudget = size_t(2) << 30;
+size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, bool stage_ld);
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
-                             double* lam);
+                             double* lam, double* work, size_t work_bytes);
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
                                 uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
                                 double* d_dZ);

@@ -269,11 +269,12 @@ struct LaneCtx {
 // FP64 (reference arithmetic) -------------------------------------------------------
 
 // get_eta_and_chi_interpolated<approx> (solver.tpp:1176-1194, :1252-1283, :1306-1320).
+template <int AP>
 MGR_HD void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e,
                                              double& eta, double& chi) {
     const double freq = c.freq * e.shift;
     const size_t b1 = (size_t)e.nr * m.L, b2 = (size_t)e.ni * m.L;
-    if (m.approx == APPROX_ONELINE) {
+    if (AP == APPROX_ONELINE) {
         const uint32_t l = c.l0;
         const double iw = interpolate_linear(m.iw[b1 + l], m.iw[b2 + l], e.fac);
         const double prof = gaussian(iw, freq - m.line[l]);
@@ -284,7 +285,7 @@ MGR_HD void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
     eta = 0.0;
     chi = m.min_opacity;
     uint32_t lo = 0, hi = m.L;
-    if (m.approx == APPROX_CLOSELINES) {
+    if (AP == APPROX_CLOSELINES) {
         const double ub = m.max_dist * (freq * m.ub[e.nr]);
         lo = lower_bound(sl, m.L, freq - ub);
         hi = upper_bound(sl, m.L, freq + ub);
@@ -292,7 +293,7 @@ MGR_HD void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
     for (uint32_t s = lo; s < hi; s++) {
         uint32_t l;
         double diff;
-        if (m.approx == APPROX_CLOSELINES) {
+        if (AP == APPROX_CLOSELINES) {
             l = m.sorted_map[s];
             diff = freq - sl[s];
         } else {
@@ -336,6 +337,7 @@ MGR_HD double dtau_single_line_fp64(const DevModel& m, const Elem& lo, const Ele
 }
 
 // compute_S_dtau_line_integrated<approx> (solver.tpp:1878-2111).
+template <int AP>
 MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
                                              const Elem& hi, double dz, double& out_dtau, double& out_Slo,
                                              double& out_Shi) {
@@ -343,7 +345,7 @@ MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
     const double nf = c.freq * hi.shift;
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
-    if (m.approx == APPROX_ONELINE) {
+    if (AP == APPROX_ONELINE) {
         const uint32_t l = c.l0;
         out_dtau = dtau_single_line_fp64(m, lo, hi, l, cf, nf, dz);
         out_Slo = interpolate_log(m.Sp[c1 + l], m.Sp[c2 + l], lo.fac);
@@ -352,7 +354,7 @@ MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
     }
     double sum_dtau = 0.0, sum_c = 0.0, sum_n = 0.0;
     uint32_t a = 0, b = m.L;
-    if (m.approx == APPROX_CLOSELINES) {
+    if (AP == APPROX_CLOSELINES) {
         double left_freq, right_freq;
         if (cf < nf) { left_freq = cf; right_freq = nf; }
         else { right_freq = cf; left_freq = nf; }
@@ -363,7 +365,7 @@ MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
         b = upper_bound(sl, m.L, right_freq + ubw);
     }
     for (uint32_t s = a; s < b; s++) {
-        const uint32_t l = (m.approx == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
+        const uint32_t l = (AP == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
         const double ld = dtau_single_line_fp64(m, lo, hi, l, cf, nf, dz);
         const double lsc = interpolate_log(m.Sp[c1 + l], m.Sp[c2 + l], lo.fac);
         const double lsn = interpolate_log(m.Sp[n1 + l], m.Sp[n2 + l], hi.fac);
@@ -371,7 +373,7 @@ MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
         sum_c += ld * lsc;
         sum_n += ld * lsn;
     }
-    if (m.approx == APPROX_NONE) {
+    if (AP == APPROX_NONE) {
         out_dtau = sum_dtau;
         out_Slo = sum_c / sum_dtau;
         out_Shi = sum_n / sum_dtau;
@@ -411,11 +413,12 @@ MGR_HD void bracket_f32(const DevModel& m, const LaneCtx& c, float lo_off, float
     if (b < a) b = a;
 }
 
+template <int AP>
 MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, float& eta, float& chi) {
     const size_t b1 = (size_t)e.nr * m.L, b2 = (size_t)e.ni * m.L;
     const float fac = e.facf;
     const float min_op = m.min_op_s;
-    if (m.approx == APPROX_ONELINE) {
+    if (AP == APPROX_ONELINE) {
         const uint32_t l = c.l0;
         const float iw = interpolate_linear(m.iw_f[b1 + l], m.iw_f[b2 + l], fac);
         const float prof = gaussian(iw, offset_f32(m, c, e.dsh, l));
@@ -426,14 +429,14 @@ MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, floa
     eta = 0.0f;
     chi = min_op;
     uint32_t lo = 0, hi = m.L;
-    if (m.approx == APPROX_CLOSELINES) {
+    if (AP == APPROX_CLOSELINES) {
         // lines inside freq -+ max_dist * freq * ub[p] (solver.tpp:1216-1227)
         const float off0 = fmaf(c.fq, e.dsh, c.a0);
         const float ub = (float)m.max_dist * ((c.fq + c.fq * e.dsh) * (float)m.ub[e.nr]);
         bracket_f32(m, c, off0 - ub, off0 + ub, lo, hi);
     }
     for (uint32_t s = lo; s < hi; s++) {
-        const uint32_t l = (m.approx == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
+        const uint32_t l = (AP == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
         const float iw = interpolate_linear(m.iw_f[b1 + l], m.iw_f[b2 + l], fac);
         const float prof = gaussian(iw, offset_f32(m, c, e.dsh, l));
         eta += prof * interpolate_log(m.em_f[b1 + l], m.em_f[b2 + l], fac);
@@ -441,23 +444,53 @@ MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, floa
     }
 }
 
-// The FP64 mode's erf arguments (linefreq - nu shift) * avg_iw of a pair, computed
-// with the same expressions as dtau_single_line_fp64.
-MGR_HD void band_positions(const DevModel& m, const LaneCtx& c, const HalfSmem& h, const Elem& lo, const Elem& hi,
-                           uint32_t l, double& next_pos, double& curr_pos) {
+// Out-of-line paths of split precision.  They run for a small fraction of pairs and
+// are kept out of the hot loop so that its code stays small.
+
+// Same-wing erf difference on the FP64 mode's arguments (linefreq - nu shift) * avg_iw,
+// computed with the expressions of dtau_single_line_fp64 and the correctly rounded
+// erff.  Returns {erff(next) - erff(curr), next - curr}.
+__host__ __device__ __noinline__ float2 band_erf(const double* iw, uint32_t L, double linefreq, double freq,
+                                                 const double* hshift, Elem lo, Elem hi, uint32_t l) {
     double lo_shift, lo_fac, hi_shift, hi_fac;
+    const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr};
     elem_shift_fac(h, lo, lo_shift, lo_fac);
     elem_shift_fac(h, hi, hi_shift, hi_fac);
-    const double cf = c.freq * lo_shift;
-    const double nf = c.freq * hi_shift;
-    const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
-    const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
-    const double linefreq = m.line[l];
-    const double iwc = interpolate_linear(m.iw[c1 + l], m.iw[c2 + l], lo_fac);
-    const double iwn = interpolate_linear(m.iw[n1 + l], m.iw[n2 + l], hi_fac);
+    const double cf = freq * lo_shift;
+    const double nf = freq * hi_shift;
+    const size_t c1 = (size_t)lo.nr * L, c2 = (size_t)lo.ni * L;
+    const size_t n1 = (size_t)hi.nr * L, n2 = (size_t)hi.ni * L;
+    const double iwc = interpolate_linear(iw[c1 + l], iw[c2 + l], lo_fac);
+    const double iwn = interpolate_linear(iw[n1 + l], iw[n2 + l], hi_fac);
     const double avg_iw = (iwc + iwn) / 2.0;
-    next_pos = (linefreq - nf) * avg_iw;
-    curr_pos = (linefreq - cf) * avg_iw;
+    const double np = (linefreq - nf) * avg_iw;
+    const double cp = (linefreq - cf) * avg_iw;
+    float2 r;
+    r.x = erff_cr_fast((float)np) - erff_cr_fast((float)cp);
+    r.y = (float)(np - cp);
+    return r;
+}
+
+// The reference's branch test |shift_hi - shift_lo| > min(dshift_max) on the FP64 shifts.
+__host__ __device__ __noinline__ bool large_shift_fp64(const double* hshift, const double* dshift_max, Elem lo,
+                                                       Elem hi) {
+    double lsh, lfac, hsh, hfac;
+    const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr};
+    elem_shift_fac(h, lo, lsh, lfac);
+    elem_shift_fac(h, hi, hsh, hfac);
+    const double dshift_abs = fabs(dsub_rn(hsh, lsh));
+    const double a = dshift_max[lo.nr], b = dshift_max[hi.nr];
+    return dshift_abs > (a < b ? a : b);
+}
+
+// Elimination coefficients {dt_in/dt_out, dtau_avg dt_in} in FP64 for optical depths
+// whose ratio or product would leave the FP32 range.
+__host__ __device__ __noinline__ double2 elim_coeffs_fp64(float dt_out, float dt_in) {
+    const double o = dt_out, i = dt_in;
+    double2 r;
+    r.x = i / o;
+    r.y = 0.5 * (o + i) * i;
+    return r;
 }
 
 MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, const Elem& lo,
@@ -485,10 +518,9 @@ MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Hal
         // cancels and its single-ulp roundings decide the result, so take it on the
         // FP64 mode's arguments with the correctly rounded erff (split precision then
         // stays within 1e-5 of the FP64 path in J).
-        double np, cp;
-        band_positions(m, c, h, lo, hi, l, np, cp);
-        erfdiff = erff_cr_fast((float)np) - erff_cr_fast((float)cp);
-        diff_pos = (float)(np - cp);
+        const float2 r = band_erf(m.iw, m.L, m.line[l], c.freq, h.shift, lo, hi, l);
+        erfdiff = r.x;
+        diff_pos = r.y;
     } else {
         erfdiff = erff(next_pos) - erff(curr_pos);
         diff_pos = next_pos - curr_pos;
@@ -501,12 +533,13 @@ MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Hal
 }
 
 // compute_S_dtau_line_integrated<approx> in FP32; dz is the scaled FP32 distance.
+template <int AP>
 MGR_HD void pair_li_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, const Elem& lo, const Elem& hi,
                         float dz, float& dtau, float& Slo, float& Shi) {
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
     const float fc = lo.facf, fn = hi.facf;
-    if (m.approx == APPROX_ONELINE) {
+    if (AP == APPROX_ONELINE) {
         const uint32_t l = c.l0;
         dtau = dtau_single_line_f32(m, c, h, lo, hi, l, dz);
         Slo = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc) * m.s_scale;
@@ -515,7 +548,7 @@ MGR_HD void pair_li_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, 
     }
     float sum_dtau = 0.0f, sum_c = 0.0f, sum_n = 0.0f;
     uint32_t a = 0, b = m.L;
-    if (m.approx == APPROX_CLOSELINES) {
+    if (AP == APPROX_CLOSELINES) {
         const float oc = fmaf(c.fq, lo.dsh, c.a0);
         const float on = fmaf(c.fq, hi.dsh, c.a0);
         const float rf = c.fq + fmaxf(c.fq * lo.dsh, c.fq * hi.dsh);
@@ -525,7 +558,7 @@ MGR_HD void pair_li_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, 
         bracket_f32(m, c, fminf(oc, on) - ubw, fmaxf(oc, on) + ubw, a, b);
     }
     for (uint32_t s = a; s < b; s++) {
-        const uint32_t l = (m.approx == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
+        const uint32_t l = (AP == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
         const float ld = dtau_single_line_f32(m, c, h, lo, hi, l, dz);
         const float lsc = interpolate_log(m.Sp_f[c1 + l], m.Sp_f[c2 + l], fc);
         const float lsn = interpolate_log(m.Sp_f[n1 + l], m.Sp_f[n2 + l], fn);
@@ -533,7 +566,7 @@ MGR_HD void pair_li_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, 
         sum_c += ld * lsc;
         sum_n += ld * lsn;
     }
-    if (m.approx == APPROX_NONE) {
+    if (AP == APPROX_NONE) {
         dtau = sum_dtau;
         Slo = sum_c / sum_dtau * m.s_scale;
         Shi = sum_n / sum_dtau * m.s_scale;
@@ -573,71 +606,68 @@ struct EC {
     bool ok;
 };
 
-template <int MODE>
+template <int MODE, int AP>
 MGR_HD void elem_fresh(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e, EC<MODE>& ec) {
     if (ec.ok) return;
     if constexpr (MODE == MODE_FP64) {
         double eta, chi;
-        eta_chi_fp64(m, sl, c, e, eta, chi);
+        eta_chi_fp64<AP>(m, sl, c, e, eta, chi);
         ec.S = eta / chi;
         ec.chi = chi;
     } else {
         float eta, chi;
-        eta_chi_f32(m, c, e, eta, chi);
-        ec.S = eta / chi * m.s_scale;
+        eta_chi_f32<AP>(m, c, e, eta, chi);
+        ec.S = fast_div(eta, chi) * m.s_scale;
         ec.chi = chi;
     }
     ec.ok = true;
 }
 
-// compute_source_dtau (solver.tpp:2139-2186) for the pair (lo, hi) with lo the lower
-// array index, both elements of the half `h` (or the origin); dz (FP64 mode) or dzf
-// (split, scaled FP32) is the pair's distance.  Fills the caches of both elements
-// when the trapezoid rule is used.
-template <int MODE>
-MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& h, const Elem& lo,
-                      const Elem& hi, double dz, float dzf, EC<MODE>& ecl, EC<MODE>& ech, PairOut<MODE>& out) {
+// compute_source_dtau (solver.tpp:2139-2186) for the pair of `outer` (farther from
+// the origin) and `inner`, both elements of the half `h` (or the origin); dz (FP64
+// mode) or dzf (split, scaled FP32) is the pair's distance.  Every pair quantity is
+// symmetric in its two elements (erf and position differences change sign together),
+// so the reference's (lower index, higher index) order need not be kept: out.Slo is
+// the source of `outer`, out.Shi that of `inner`, from the line integral or from the
+// element caches (trapezoid rule).
+template <int MODE, int AP>
+MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& h, const Elem& outer,
+                      const Elem& inner, double dz, float dzf, EC<MODE>& eco, EC<MODE>& eci, PairOut<MODE>& out) {
     if constexpr (MODE == MODE_FP64) {
-        const double dshift_abs = fabs(dsub_rn(hi.shift, lo.shift));
-        const double a = m.dshift_max[lo.nr], b = m.dshift_max[hi.nr];
+        const double dshift_abs = fabs(dsub_rn(inner.shift, outer.shift));
+        const double a = m.dshift_max[outer.nr], b = m.dshift_max[inner.nr];
         out.large = dshift_abs > (a < b ? a : b);
     } else {
         // the reference's branch test in FP32, and in FP64 within a margin of the
         // threshold that covers the FP32 roundings of the shifts
-        const float dsf = fabsf(hi.dsh - lo.dsh);
-        const float thr = fminf(m.dshift_max_f[lo.nr], m.dshift_max_f[hi.nr]);
-        const float margin = 4.0e-3f * thr + 2.0e-6f * (lo.dshm + hi.dshm);
-        if (fabsf(dsf - thr) > margin) {
-            out.large = dsf > thr;
-        } else {
-            double lsh, lfac, hsh, hfac;
-            elem_shift_fac(h, lo, lsh, lfac);
-            elem_shift_fac(h, hi, hsh, hfac);
-            const double dshift_abs = fabs(dsub_rn(hsh, lsh));
-            const double a = m.dshift_max[lo.nr], b = m.dshift_max[hi.nr];
-            out.large = dshift_abs > (a < b ? a : b);
-        }
+        const float dsf = fabsf(inner.dsh - outer.dsh);
+        const float thr = fminf(m.dshift_max_f[outer.nr], m.dshift_max_f[inner.nr]);
+        const float margin = 4.0e-3f * thr + 2.0e-6f * (outer.dshm + inner.dshm);
+        if (fabsf(dsf - thr) > margin) out.large = dsf > thr;
+        else out.large = large_shift_fp64(h.shift, m.dshift_max, outer, inner);
     }
     if (out.large) {
         if constexpr (MODE == MODE_FP64) {
-            pair_li_fp64(m, sl, c, lo, hi, dz, out.dtau, out.Slo, out.Shi);
+            pair_li_fp64<AP>(m, sl, c, outer, inner, dz, out.dtau, out.Slo, out.Shi);
         } else {
-            pair_li_f32(m, c, h, lo, hi, dzf, out.dtau, out.Slo, out.Shi);
+            pair_li_f32<AP>(m, c, h, outer, inner, dzf, out.dtau, out.Slo, out.Shi);
         }
     } else {
-        elem_fresh<MODE>(m, sl, c, lo, ecl);
-        elem_fresh<MODE>(m, sl, c, hi, ech);
+        elem_fresh<MODE, AP>(m, sl, c, outer, eco);
+        elem_fresh<MODE, AP>(m, sl, c, inner, eci);
+        out.Slo = eco.S;
+        out.Shi = eci.S;
         if constexpr (MODE == MODE_FP64) {
-            out.dtau = 0.5 * (ecl.chi + ech.chi) * dz;
+            out.dtau = 0.5 * (eco.chi + eci.chi) * dz;
         } else {
-            out.dtau = 0.5f * (ecl.chi + ech.chi) * dzf;
+            out.dtau = 0.5f * (eco.chi + eci.chi) * dzf;
         }
     }
 }
 
-// Reciprocal of an elimination pivot (always >= 1).  FP64 mode: IEEE division, as
-// the reference.  Split mode: the hardware's approximate FP64 reciprocal (relative
-// error below 2^-22) refined by one Newton step (relative error ~1e-14).
+// Reciprocal of a value >= 1 (elimination pivots and boundary rows).  FP64 mode: IEEE
+// division, as the reference.  Split mode: the hardware's approximate FP64 reciprocal
+// (relative error below 2^-22) refined by one Newton step (relative error ~1e-14).
 template <int MODE>
 MGR_HD double rcp_pivot(double x) {
     if (MODE == MODE_FP64) return 1.0 / x;
@@ -675,10 +705,10 @@ MGR_HD void elim_row(typename Real_<MODE>::T dt_out, typename Real_<MODE>::T dt_
         if (dt_out > 1.0e-18f && dt_out < 1.0e18f && dt_in > 1.0e-18f && dt_in < 1.0e18f) {
             q = (double)fast_div(dt_in, dt_out);
             iC = (double)(0.5f * (dt_out + dt_in) * dt_in);
-        } else {  // ratio or product would leave the FP32 range
-            const double o = dt_out, i = dt_in;
-            q = i / o;
-            iC = 0.5 * (o + i) * i;
+        } else {
+            const double2 k = elim_coeffs_fp64(dt_out, dt_in);
+            q = k.x;
+            iC = k.y;
         }
         F = fma(q, F * FI, iC);
         FI = rcp_pivot<MODE>(1.0 + F);
@@ -693,9 +723,23 @@ struct LaneResult {
     bool solved;    // n_tot > 1
 };
 
+// State of one elimination sweep toward the origin.
+struct Sweep {
+    double F, FI, Su;  // F (top) / G (bottom), 1/(1+F), modified source
+    double dt;         // optical depth of the last pair (next to the origin)
+    double S_in;       // source of the origin from the last pair (its inner element)
+    bool rows;         // at least one row eliminated
+};
+
 // Two-sided Feautrier solve of frequency c.f on the ray pair staged in `bk`
-// (backward half, direction rr) and `fw` (forward half, antipode).
-template <int MODE>
+// (backward half, direction rr) and `fw` (forward half, antipode).  Both halves run
+// through the same sweep code (outer end first):
+//   backward half: elements first .. centre, rows first .. centre-1 with row source
+//                  S[i] from pair (i, i+1) = this pair's outer element;
+//   forward half:  elements last .. centre+1, row `last` with the source of its own
+//                  pair, rows i < last with S[i] from pair (i, i+1) = the previous
+//                  pair's inner element.
+template <int MODE, int AP>
 __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
                                           int nb, const HalfSmem& fw, int nf) {
     using T = typename Real_<MODE>::T;
@@ -708,181 +752,135 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     }
     const Elem cen = centre_elem(c.o);
     const uint32_t l = c.l0;
-
-    // ---- top sweep: elements first .. centre (backward half, outer end first) ----
-    double FF = 0.0, FI = 0.0, Su = 0.0;
-    T dt_top = T(0);
-    bool top_rows = false;   // at least one row eliminated
-    bool top_large = false;  // last pair line-integrated
-    T top_Shi = T(0);        // its upper source
     EC<MODE> ec_cen{T(0), T(0), false};
-    if (nb > 0) {
-        ElemIter it;
-        iter_begin<MODE>(m, bk, c.o, l, nb, it);
-        Elem prev;
-        iter_next<MODE>(m, bk, c.o, l, it, prev);
-        EC<MODE> ec_prev{T(0), T(0), false};
-        double bshift = prev.shift;
-        if constexpr (MODE == MODE_SPLIT) {
-            double fac;
-            elem_shift_fac(bk, prev, bshift, fac);
-        }
-        const double Ibdy = boundary_intensity(m, prev.nr, c.freq * bshift);
-        bool first = true;
-        while (true) {
-            Elem cur;
-            const bool more = iter_next<MODE>(m, bk, c.o, l, it, cur);
-            if (!more) cur = cen;
-            EC<MODE> ec_cur{T(0), T(0), false};
-            PairOut<MODE> po;
-            eval_pair<MODE>(m, sl, c, bk, prev, cur, prev.dzin, prev.dzf, ec_prev, more ? ec_cur : ec_cen, po);
-            T S;
-            if (po.large) S = po.Slo;
-            else { elem_fresh<MODE>(m, sl, c, prev, ec_prev); S = ec_prev.S; }
-            if (first) {
-                const double dt = po.dtau;
-                const double inverse_dtau_f = 1.0 / dt;
-                const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
-                const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
-                const double Bf = Bf_min_Cf + Cf;
-                Su = ((double)S + 2.0 * Ibdy * inverse_dtau_f) / Bf;
-                FF = 0.5 * Bf_min_Cf * dt * dt;
-                FI = 1.0 / (1.0 + FF);
-                first = false;
-            } else {
-                elim_row<MODE>(dt_top, po.dtau, S, FF, FI, Su);
-            }
-            top_rows = true;
-            dt_top = po.dtau;
-            top_large = po.large;
-            top_Shi = po.Shi;
-            if (!more) break;
-            prev = cur;
-            ec_prev = ec_cur;
-        }
-    }
+    Sweep top{0.0, 0.0, 0.0, 0.0, 0.0, false}, bot = top;
 
-    // ---- bottom sweep: elements last .. centre+1 (forward half, outer end first) ----
-    double GG = 0.0, GI = 0.0, Sb = 0.0;
-    T dt_bot = T(0), S_centre = T(0);
-    bool bot_rows = false;
-    if (nf > 0) {
-        ElemIter it;
-        iter_begin<MODE>(m, fw, c.o, l, nf, it);
-        Elem prev;  // higher index element
-        iter_next<MODE>(m, fw, c.o, l, it, prev);
-        EC<MODE> ec_prev{T(0), T(0), false};
-        double bshift = prev.shift;
-        if constexpr (MODE == MODE_SPLIT) {
-            double fac;
-            elem_shift_fac(fw, prev, bshift, fac);
-        }
-        const double Ibdy = boundary_intensity(m, prev.nr, c.freq * bshift);
-        bool first = true;
-        T S_prev_row = T(0);  // row source of `prev` (known once its upper pair was evaluated)
-        while (true) {
-            Elem cur;  // lower index element
-            const bool more = iter_next<MODE>(m, fw, c.o, l, it, cur);
-            if (!more) cur = cen;
-            EC<MODE> ec_cur{T(0), T(0), false};
-            EC<MODE>& ecc = more ? ec_cur : ec_cen;
-            PairOut<MODE> po;
-            eval_pair<MODE>(m, sl, c, fw, cur, prev, prev.dzin, prev.dzf, ecc, ec_prev, po);
-            // Row source of the lower element `cur` (index < last).
-            T S_cur;
-            if (po.large) S_cur = po.Slo;
-            else { elem_fresh<MODE>(m, sl, c, cur, ecc); S_cur = ecc.S; }
-            if (first) {
-                T S_last;
-                if (po.large) S_last = po.Shi;
-                else { elem_fresh<MODE>(m, sl, c, prev, ec_prev); S_last = ec_prev.S; }
-                const double dt = po.dtau;
-                const double inverse_dtau_l = 1.0 / dt;
-                const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
-                const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
-                const double Bl = Bl_min_Al + Al;
-                Sb = ((double)S_last + 2.0 * Ibdy * inverse_dtau_l) / Bl;
-                GG = 0.5 * Bl_min_Al * dt * dt;
-                GI = 1.0 / (1.0 + GG);
-                first = false;
-            } else {
-                // row `prev`: upper pair dt_bot already eliminated, lower pair = this pair
-                elim_row<MODE>(dt_bot, po.dtau, S_prev_row, GG, GI, Sb);
+#pragma unroll 1
+    for (int side = 0; side < 2; side++) {
+        const HalfSmem& h = side ? fw : bk;
+        const int n = side ? nf : nb;
+        Sweep st{0.0, 0.0, 0.0, 0.0, 0.0, false};
+        if (n > 0) {
+            ElemIter it;
+            iter_begin<MODE>(m, h, c.o, l, n, it);
+            Elem outer;
+            iter_next<MODE>(m, h, c.o, l, it, outer);
+            EC<MODE> ec_out{T(0), T(0), false};
+            double bshift = outer.shift;
+            if constexpr (MODE == MODE_SPLIT) {
+                double fac;
+                elem_shift_fac(h, outer, bshift, fac);
             }
-            bot_rows = true;
-            dt_bot = po.dtau;
-            S_prev_row = S_cur;
-            if (!more) {
-                S_centre = S_cur;
-                break;
+            const double Ibdy = boundary_intensity(m, outer.nr, c.freq * bshift);
+            T dt_prev = T(0), S_carry = T(0);
+            bool first = true;
+            while (true) {
+                Elem inner;
+                const bool more = iter_next<MODE>(m, h, c.o, l, it, inner);
+                if (!more) inner = cen;
+                EC<MODE> ec_inn{T(0), T(0), false};
+                EC<MODE>& eci = more ? ec_inn : ec_cen;
+                PairOut<MODE> po;
+                eval_pair<MODE, AP>(m, sl, c, h, outer, inner, outer.dzin, outer.dzf, ec_out, eci, po);
+                const T rowS = (side == 0 || first) ? po.Slo : S_carry;
+                if (first) {
+                    // boundary row (solver.tpp:2239-2252 first, :2284-2293 last)
+                    const double dt = po.dtau;
+                    const double inverse_dtau = 1.0 / dt;
+                    const double Cb = 2.0 * inverse_dtau * inverse_dtau;
+                    const double Bb_min_Cb = 1.0 + 2.0 * inverse_dtau;
+                    const double Bb = Bb_min_Cb + Cb;
+                    st.Su = ((double)rowS + 2.0 * Ibdy * inverse_dtau) / Bb;
+                    st.F = 0.5 * Bb_min_Cb * dt * dt;
+                    st.FI = 1.0 / (1.0 + st.F);
+                    first = false;
+                } else {
+                    elim_row<MODE>(dt_prev, po.dtau, rowS, st.F, st.FI, st.Su);
+                }
+                dt_prev = po.dtau;
+                S_carry = po.Shi;
+                if (!more) break;
+                outer = inner;
+                ec_out = ec_inn;
             }
-            prev = cur;
-            ec_prev = ec_cur;
+            st.dt = dt_prev;
+            st.S_in = S_carry;
+            st.rows = true;
         }
+        if (side) bot = st;
+        else top = st;
     }
 
     // ---- combine at the origin ----
-    if (top_rows && bot_rows) {
-        const double dtt = dt_top, dtb = dt_bot;
-        const double dtau_avg = 0.5 * (dtt + dtb);
-        const double iA = dtau_avg * dtt;
-        const double iC = dtau_avg * dtb;
+    if (top.rows && bot.rows) {
+        const double dtau_avg = 0.5 * (top.dt + bot.dt);
+        const double iA = dtau_avg * top.dt;
+        const double iC = dtau_avg * bot.dt;
         const double A = 1.0 / iA;
-        const double FFc = (A * FF * FI + 1.0) * iC;
-        const double Su_pre = (A * Su + (double)S_centre) * iC;
-        const double GP = GG * GI;
+        const double FFc = (A * top.F * top.FI + 1.0) * iC;
+        const double Su_pre = (A * top.Su + bot.S_in) * iC;
+        const double GP = bot.F * bot.FI;
         const double D = 1.0 / (FFc + GP);
-        res.u = (Su_pre + Sb) * D;
+        res.u = (Su_pre + bot.Su) * D;
         res.Ldiag = iC * D;
-    } else if (bot_rows) {  // origin is the first element
+    } else if (bot.rows) {  // origin is the first element
         const double Ibdy = boundary_intensity(m, c.o, c.freq);
-        const double dtb = dt_bot;
-        const double inverse_dtau_f = 1.0 / dtb;
+        const double inverse_dtau_f = 1.0 / bot.dt;
         const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
         const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
         const double Bf = Bf_min_Cf + Cf;
-        const double Suf = ((double)S_centre + 2.0 * Ibdy * inverse_dtau_f) / Bf;
-        const double FFf = 0.5 * Bf_min_Cf * dtb * dtb;
-        const double GP = GG * GI;
+        const double Suf = (bot.S_in + 2.0 * Ibdy * inverse_dtau_f) / Bf;
+        const double FFf = 0.5 * Bf_min_Cf * bot.dt * bot.dt;
+        const double GP = bot.F * bot.FI;
         const double D = 1.0 / (FFf + GP);
-        res.u = (Suf * (1.0 + FFf) + Sb) * D;
+        res.u = (Suf * (1.0 + FFf) + bot.Su) * D;
         res.Ldiag = (1.0 / Cf) * D;
     } else {  // origin is the last element
         const double Ibdy = boundary_intensity(m, c.o, c.freq);
-        T S_last;
-        if (top_large) S_last = top_Shi;
-        else { elem_fresh<MODE>(m, sl, c, cen, ec_cen); S_last = ec_cen.S; }
-        const double dtt = dt_top;
-        const double inverse_dtau_l = 1.0 / dtt;
+        const double inverse_dtau_l = 1.0 / top.dt;
         const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
         const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
         const double Bl = Bl_min_Al + Al;
-        const double denominator = 1.0 / (Bl * FF + Bl_min_Al);
-        const double Sl = (double)S_last + 2.0 * Ibdy * inverse_dtau_l;
-        res.u = (Al * Su + Sl) * (1.0 + FF) * denominator;
-        res.Ldiag = (1.0 + FF) / (Bl_min_Al + Bl * FF);
+        const double denominator = 1.0 / (Bl * top.F + Bl_min_Al);
+        const double Sl = top.S_in + 2.0 * Ibdy * inverse_dtau_l;
+        res.u = (Al * top.Su + Sl) * (1.0 + top.F) * denominator;
+        res.Ldiag = (1.0 + top.F) / (Bl_min_Al + Bl * top.F);
     }
     return res;
 }
 
 // update_Lambda, n_off_diag = 0 (solver.tpp:1760-1800): the ALO element of this
 // (origin, ray pair, frequency).
-MGR_HD double lambda_element(const DevModel& m, const double* sl, uint32_t o, uint32_t rr,
-                                                 uint32_t f, double Ldiag) {
-    const double w_ang = 2.0 * m.rayw[rr];
+struct LambdaFactors {
+    double Aqw;          // line_A * quadrature weight
+    double frq;          // nu(o, f)
+    double phi;          // line profile at nu(o, f)
+    double inverse_chi;  // 1 / opacity at the origin
+};
+
+// The ray-independent factors of the ALO element of (origin o, frequency f).
+MGR_HD LambdaFactors lambda_factors(const DevModel& m, const double* sl, uint32_t o, uint32_t f) {
     const uint32_t ls = m.corr_lspec[f];
     const uint32_t k = m.corr_k[f];
     const uint32_t z = m.corr_z[f];
     const uint32_t lid = m.nrad_cum[ls] + k;
     const double freq_line = m.line[lid];
     const double invr_mass = m.lspec_inv_mass[ls];
-    const double constante = m.line_A[lid] * m.quad_w[(size_t)ls * m.Q + z] * w_ang;
+    LambdaFactors r;
+    r.Aqw = m.line_A[lid] * m.quad_w[(size_t)ls * m.Q + z];
     double eta, chi;
     get_eta_and_chi(m, sl, o, k, freq_line, eta, chi);  // the reference passes k as the line index here
-    const double inverse_chi = 1.0 / chi;
-    const double frq = m.nu[(size_t)o * m.F + f] * 1.0;
-    const double phi = thermo_profile(m, invr_mass, o, freq_line, frq);
-    return constante * frq * phi * Ldiag * inverse_chi;
+    r.inverse_chi = 1.0 / chi;
+    r.frq = m.nu[(size_t)o * m.F + f] * 1.0;
+    r.phi = thermo_profile(m, invr_mass, o, freq_line, r.frq);
+    return r;
+}
+
+// The element itself, with the reference's order of operations:
+// constante * frq * phi * L_diag * inverse_chi, constante = line_A * weight * 2 w_rr.
+MGR_HD double lambda_element(const LambdaFactors& k, double w_rr, double Ldiag) {
+    const double constante = k.Aqw * (2.0 * w_rr);
+    return constante * k.frq * k.phi * Ldiag * k.inverse_chi;
 }
 
 }  // namespace mgr
