@@ -36,6 +36,14 @@ struct HalfSmem {
     uint32_t* eid;   // CSR edge of step s (index into the interpolation-count table)
 };
 
+// Order-preserving 64-bit key of a finite double (total order, -0 below +0; the
+// squared distances compared here are never -0).  Lets the warp's argmin run on the
+// integer pipe.
+__device__ __forceinline__ unsigned long long dkey(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
 // Warp-cooperative Geometry::get_next_general_geometry<Defaulttracer> walk
 // (geometry.tpp:13-44) from origin o along ray r until a boundary point is met.
 // Lanes scan the neighbour list; the argmin of (distance to ray, neighbour order)
@@ -53,7 +61,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
     while (true) {
         const uint32_t nnb = m.n_nb[crt];
         const uint32_t cum = m.cum_nb[crt];
-        double best = DBL_MAX;
+        unsigned long long best = ~0ull;
         uint32_t besti = 0xffffffffu;
         double bestZ = 0.0;
         for (uint32_t i = lane; i < nnb; i += 32) {
@@ -64,8 +72,9 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
             const double Zn = dot3_rn(Rx, Ry, Rz, dx, dy, dz);
             if (Zn > Z) {
                 const double d2 = dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), dmul_rn(Zn, Zn));
-                if (d2 < best) {
-                    best = d2;
+                const unsigned long long k = dkey(d2);
+                if (k < best) {
+                    best = k;
                     besti = i;
                     bestZ = Zn;
                 }
@@ -73,7 +82,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
-            const double ob = __shfl_xor_sync(FULL_MASK, best, off);
+            const unsigned long long ob = __shfl_xor_sync(FULL_MASK, best, off);
             const uint32_t oi = __shfl_xor_sync(FULL_MASK, besti, off);
             const double oz = __shfl_xor_sync(FULL_MASK, bestZ, off);
             if (ob < best || (ob == best && oi < besti)) {
@@ -665,20 +674,50 @@ MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, con
     }
 }
 
-// Reciprocal of a value >= 1 (elimination pivots and boundary rows).  FP64 mode: IEEE
-// division, as the reference.  Split mode: the hardware's approximate FP64 reciprocal
-// (relative error below 2^-22) refined by one Newton step (relative error ~1e-14).
+// Reciprocal of a positive finite value.  FP64 mode: IEEE division, as the reference.
+// Split mode: the hardware's approximate FP64 reciprocal (relative error below 2^-22)
+// refined by one Newton step (relative error ~1e-14).
 template <int MODE>
-MGR_HD double rcp_pivot(double x) {
+MGR_HD double drcp(double x) {
     if (MODE == MODE_FP64) return 1.0 / x;
 #ifdef __CUDA_ARCH__
-    if (!(x < 1.0e300)) return 1.0 / x;
     double r;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
     return fma(r, fma(-x, r, 1.0), r);
 #else
     return 1.0 / x;
 #endif
+}
+
+// Exact conversion of a finite FP32 value to FP64 on the integer pipe (the FP64 pipe
+// is the scarce unit of this kernel).  Subnormal inputs become 0.
+MGR_HD double f2d(float x) {
+#ifdef __CUDA_ARCH__
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t mag = b & 0x7fffffffu;
+    if (mag < 0x00800000u) return 0.0;
+    const uint32_t hi = ((mag >> 3) + 0x38000000u) | (b & 0x80000000u);  // exponent bias 127 -> 1023
+    return __hiloint2double((int)hi, (int)(b << 29));
+#else
+    return (std::fabs(x) < FLT_MIN) ? 0.0 : (double)x;
+#endif
+}
+
+// Split-precision Planck function / boundary intensity: the reference's expressions
+// with the two divisions as reciprocals.
+template <int MODE>
+MGR_HD double boundary_intensity_m(const DevModel& m, uint32_t p, double freq) {
+    if constexpr (MODE == MODE_FP64) {
+        return boundary_intensity(m, p, freq);
+    } else {
+        const uint32_t b = m.p2b[p];
+        if (b >= m.B) return 0.0;
+        const int c = m.bc[b];
+        if (c == BC_ZERO) return 0.0;
+        const double temp = (c == BC_THERMAL) ? m.bt[b] : T_CMB;
+        const float x = (float)(HH_OVER_KB * freq * drcp<MODE>(temp));
+        return TWO_HH_OVER_CC_SQUARED * (freq * freq * freq) * drcp<MODE>((double)expm1f(x));
+    }
 }
 
 // One interior elimination row in the economical (1+B)/C form (solver.tpp:2266-2281
@@ -701,18 +740,19 @@ MGR_HD void elim_row(typename Real_<MODE>::T dt_out, typename Real_<MODE>::T dt_
         FI = 1.0 / (1.0 + F);
         Su = (A * Su + S) * FI * iC;
     } else {
-        double q, iC;
         if (dt_out > 1.0e-18f && dt_out < 1.0e18f && dt_in > 1.0e-18f && dt_in < 1.0e18f) {
-            q = (double)fast_div(dt_in, dt_out);
-            iC = (double)(0.5f * (dt_out + dt_in) * dt_in);
+            // q, iC in [1e-36, 1e36]: F = q G + iC stays below 2e36, a safe pivot range
+            const double q = f2d(fast_div(dt_in, dt_out));
+            const double iC = f2d(0.5f * (dt_out + dt_in) * dt_in);
+            F = fma(q, F * FI, iC);
+            FI = drcp<MODE>(1.0 + F);
+            Su = fma(q, Su, f2d(S) * iC) * FI;
         } else {
             const double2 k = elim_coeffs_fp64(dt_out, dt_in);
-            q = k.x;
-            iC = k.y;
+            F = fma(k.x, F * FI, k.y);
+            FI = 1.0 / (1.0 + F);
+            Su = fma(k.x, Su, (double)S * k.y) * FI;
         }
-        F = fma(q, F * FI, iC);
-        FI = rcp_pivot<MODE>(1.0 + F);
-        Su = fma(q, Su, (double)S * iC) * FI;
     }
 }
 
@@ -746,7 +786,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     LaneResult res;
     res.solved = (nb > 0) || (nf > 0);
     if (!res.solved) {
-        res.u = boundary_intensity(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
+        res.u = boundary_intensity_m<MODE>(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
         res.Ldiag = 0.0;
         return res;
     }
@@ -771,7 +811,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 double fac;
                 elem_shift_fac(h, outer, bshift, fac);
             }
-            const double Ibdy = boundary_intensity(m, outer.nr, c.freq * bshift);
+            const double Ibdy = boundary_intensity_m<MODE>(m, outer.nr, c.freq * bshift);
             T dt_prev = T(0), S_carry = T(0);
             bool first = true;
             while (true) {
@@ -786,13 +826,14 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 if (first) {
                     // boundary row (solver.tpp:2239-2252 first, :2284-2293 last)
                     const double dt = po.dtau;
-                    const double inverse_dtau = 1.0 / dt;
+                    const double inverse_dtau = drcp<MODE>(dt);
                     const double Cb = 2.0 * inverse_dtau * inverse_dtau;
                     const double Bb_min_Cb = 1.0 + 2.0 * inverse_dtau;
                     const double Bb = Bb_min_Cb + Cb;
-                    st.Su = ((double)rowS + 2.0 * Ibdy * inverse_dtau) / Bb;
+                    if constexpr (MODE == MODE_FP64) st.Su = ((double)rowS + 2.0 * Ibdy * inverse_dtau) / Bb;
+                    else st.Su = ((double)rowS + 2.0 * Ibdy * inverse_dtau) * drcp<MODE>(Bb);
                     st.F = 0.5 * Bb_min_Cb * dt * dt;
-                    st.FI = 1.0 / (1.0 + st.F);
+                    st.FI = drcp<MODE>(1.0 + st.F);
                     first = false;
                 } else {
                     elim_row<MODE>(dt_prev, po.dtau, rowS, st.F, st.FI, st.Su);
@@ -816,35 +857,38 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         const double dtau_avg = 0.5 * (top.dt + bot.dt);
         const double iA = dtau_avg * top.dt;
         const double iC = dtau_avg * bot.dt;
-        const double A = 1.0 / iA;
+        const double A = drcp<MODE>(iA);
         const double FFc = (A * top.F * top.FI + 1.0) * iC;
         const double Su_pre = (A * top.Su + bot.S_in) * iC;
         const double GP = bot.F * bot.FI;
-        const double D = 1.0 / (FFc + GP);
+        const double D = drcp<MODE>(FFc + GP);
         res.u = (Su_pre + bot.Su) * D;
         res.Ldiag = iC * D;
     } else if (bot.rows) {  // origin is the first element
-        const double Ibdy = boundary_intensity(m, c.o, c.freq);
-        const double inverse_dtau_f = 1.0 / bot.dt;
+        const double Ibdy = boundary_intensity_m<MODE>(m, c.o, c.freq);
+        const double inverse_dtau_f = drcp<MODE>(bot.dt);
         const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
         const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
         const double Bf = Bf_min_Cf + Cf;
-        const double Suf = (bot.S_in + 2.0 * Ibdy * inverse_dtau_f) / Bf;
+        double Suf;
+        if constexpr (MODE == MODE_FP64) Suf = (bot.S_in + 2.0 * Ibdy * inverse_dtau_f) / Bf;
+        else Suf = (bot.S_in + 2.0 * Ibdy * inverse_dtau_f) * drcp<MODE>(Bf);
         const double FFf = 0.5 * Bf_min_Cf * bot.dt * bot.dt;
         const double GP = bot.F * bot.FI;
-        const double D = 1.0 / (FFf + GP);
+        const double D = drcp<MODE>(FFf + GP);
         res.u = (Suf * (1.0 + FFf) + bot.Su) * D;
-        res.Ldiag = (1.0 / Cf) * D;
+        res.Ldiag = drcp<MODE>(Cf) * D;
     } else {  // origin is the last element
-        const double Ibdy = boundary_intensity(m, c.o, c.freq);
-        const double inverse_dtau_l = 1.0 / top.dt;
+        const double Ibdy = boundary_intensity_m<MODE>(m, c.o, c.freq);
+        const double inverse_dtau_l = drcp<MODE>(top.dt);
         const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
         const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
         const double Bl = Bl_min_Al + Al;
-        const double denominator = 1.0 / (Bl * top.F + Bl_min_Al);
+        const double denominator = drcp<MODE>(Bl * top.F + Bl_min_Al);
         const double Sl = top.S_in + 2.0 * Ibdy * inverse_dtau_l;
         res.u = (Al * top.Su + Sl) * (1.0 + top.F) * denominator;
-        res.Ldiag = (1.0 + top.F) / (Bl_min_Al + Bl * top.F);
+        if constexpr (MODE == MODE_FP64) res.Ldiag = (1.0 + top.F) / (Bl_min_Al + Bl * top.F);
+        else res.Ldiag = (1.0 + top.F) * denominator;
     }
     return res;
 }
