@@ -72,7 +72,7 @@ float to_f32_floor_host(double x) {
 struct EmuModel {
     std::vector<double4_32a> pos, vel, edge;
     std::vector<double> ub, Sp;
-    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll;
+    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f;
     std::vector<uint16_t> nint;
     std::vector<uint32_t> lq2f;
     DevModel m{};
@@ -104,9 +104,11 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     x.iw_f.resize(PL);
     x.Sp_f.resize(PL);
     x.dsm_f.resize(P);
+    x.ub_f.resize(P);
     for (uint32_t p = 0; p < P; p++) {
         x.ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
         x.dsm_f[p] = (float)d->dshift_max[p];
+        x.ub_f[p] = (float)x.ub[p];
     }
     const double Ke = pow2_scale_for_max(d->emissivity, PL);
     const double Ko = pow2_scale_for_max(d->opacity, PL);
@@ -126,12 +128,13 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     m.line = d->line; m.sorted_line = d->sorted_line; m.sorted_map = d->sorted_line_map;
     m.max_inv_mass = d->max_inverse_mass; m.em = d->emissivity; m.op = d->opacity; m.iw = d->inverse_width;
     m.Sp = x.Sp.data(); m.crit = d->interp_criterion; m.em_f = x.em_f.data(); m.op_f = x.op_f.data();
-    m.iw_f = x.iw_f.data(); m.Sp_f = x.Sp_f.data(); m.ub = x.ub.data(); m.T = d->temperature; m.vt2 = d->vturb2;
+    m.iw_f = x.iw_f.data(); m.Sp_f = x.Sp_f.data(); m.ub = x.ub.data(); m.ub_f = x.ub_f.data(); m.T = d->temperature; m.vt2 = d->vturb2;
     m.dshift_max = d->dshift_max; m.dshift_max_f = x.dsm_f.data(); m.nu = d->nu; m.corr_line = d->corr_line;
     m.corr_lspec = d->corr_lspec; m.corr_k = d->corr_k; m.corr_z = d->corr_z; m.in_line = d->in_line_integral;
     m.nrad_cum = d->nrad_cum; m.line_A = d->line_A; m.lspec_inv_mass = d->lspec_inverse_mass;
     m.quad_w = d->quad_weights; m.min_opacity = d->min_opacity; m.min_dtau = d->min_dtau;
     m.max_interp_diff = d->max_interpolation_diff; m.max_dist = d->max_distance_opacity_contribution;
+    m.max_dist_f = (float)m.max_dist;
     m.log_max_interp_diff = logf((float)d->max_interpolation_diff);
     m.approx = d->approx;
     m.min_op_s = (float)(d->min_opacity * Ko);

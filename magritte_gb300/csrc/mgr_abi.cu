@@ -232,6 +232,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.min_dtau = d->min_dtau;
     dm.max_interp_diff = d->max_interpolation_diff;
     dm.max_dist = d->max_distance_opacity_contribution;
+    dm.max_dist_f = (float)dm.max_dist;
     dm.log_max_interp_diff = logf((float)d->max_interpolation_diff);
     dm.approx = d->approx;
     m->n_edges = E;
@@ -252,8 +253,11 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     std::vector<double> ub(P);
     for (uint32_t p = 0; p < P; p++)
         ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
-    std::vector<float> dsm_f(P);
-    for (uint32_t p = 0; p < P; p++) dsm_f[p] = (float)d->dshift_max[p];
+    std::vector<float> dsm_f(P), ub_f(P);
+    for (uint32_t p = 0; p < P; p++) {
+        dsm_f[p] = (float)d->dshift_max[p];
+        ub_f[p] = (float)ub[p];
+    }
     std::vector<float> dls, dll;
     line_offset_tables(d->line, d->sorted_line, L, dls, dll);
     std::vector<uint32_t> lq2f((size_t)L * d->nquads, 0xffffffffu);
@@ -296,6 +300,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = cudaMemcpyAsync(m->iw, d->inverse_width, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->crit, d->interp_criterion, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = upload(m, &dm.ub, ub.data(), P)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.ub_f, ub_f.data(), P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.T, d->temperature, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.vt2, d->vturb2, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.dshift_max, d->dshift_max, P)) != cudaSuccess) break;

@@ -72,6 +72,7 @@ struct DevModel {
     const float* iw_f;
     const float* Sp_f;
     const double* ub;        // [P] sqrt(2 kB/(amu c^2) max_inv_mass T + vturb2)
+    const float* ub_f;       // [P] (float)ub
     const double* T;         // [P]
     const double* vt2;       // [P]
     const double* dshift_max;// [P]
@@ -96,6 +97,7 @@ struct DevModel {
     // em_f = em * Ke, op_f = op * Ko, Sp_f = Sp * Ke / Ko.
     const float* dls;            // [L][L] (float)(sorted_line[s] - line[l0]) at l0*L + s
     const float* dll;            // [L][L] (float)(line[l] - line[l0]) at l0*L + l
+    float max_dist_f;            // (float)max_dist
     float min_op_s;              // min_opacity * Ko
     float dz_scale;              // 1 / Ko  (true optical depth = chi_f * dz * dz_scale)
     float s_scale;               // Ko / Ke (true source = scaled source * s_scale)

@@ -61,6 +61,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
     while (true) {
         const uint32_t nnb = m.n_nb[crt];
         const uint32_t cum = m.cum_nb[crt];
+        const unsigned long long zkey = dkey(Z);
         unsigned long long best = ~0ull;
         uint32_t besti = 0xffffffffu;
         double bestZ = 0.0;
@@ -70,7 +71,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
             const double Ry = dsub_rn(e.y, po.y);
             const double Rz = dsub_rn(e.z, po.z);
             const double Zn = dot3_rn(Rx, Ry, Rz, dx, dy, dz);
-            if (Zn > Z) {
+            if (dkey(Zn) > zkey) {  // Zn > Z
                 const double d2 = dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), dmul_rn(Zn, Zn));
                 const unsigned long long k = dkey(d2);
                 if (k < best) {
@@ -111,16 +112,22 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
             h.ids[count] = nxt;
             h.eid[count] = cum + besti;
             h.dZ[count] = dZl;
-            const double s = shift_comoving(m, o, nxt, d);
-            h.shift[count] = s;
-            h.dsh[count] = (float)dsub_rn(s, 1.0);
-            h.dzs[count] = (float)dZl * m.dz_scale;
         }
         count++;
         if (m.p2b[nxt] != m.P) break;
         crt = nxt;
     }
     __syncwarp();
+    if (STORE && count > 0) {
+        // Per-step Doppler shifts and FP32 copies, one step per lane.
+        for (int s = lane; s < count; s += 32) {
+            const double sh = shift_comoving(m, o, h.ids[s], d);
+            h.shift[s] = sh;
+            h.dsh[s] = (float)dsub_rn(sh, 1.0);
+            h.dzs[s] = (float)h.dZ[s] * m.dz_scale;
+        }
+        __syncwarp();
+    }
     return count;
 }
 
@@ -441,7 +448,7 @@ MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, floa
     if (AP == APPROX_CLOSELINES) {
         // lines inside freq -+ max_dist * freq * ub[p] (solver.tpp:1216-1227)
         const float off0 = fmaf(c.fq, e.dsh, c.a0);
-        const float ub = (float)m.max_dist * ((c.fq + c.fq * e.dsh) * (float)m.ub[e.nr]);
+        const float ub = m.max_dist_f * ((c.fq + c.fq * e.dsh) * m.ub_f[e.nr]);
         bracket_f32(m, c, off0 - ub, off0 + ub, lo, hi);
     }
     for (uint32_t s = lo; s < hi; s++) {
@@ -561,8 +568,8 @@ MGR_HD void pair_li_f32(const DevModel& m, const LaneCtx& c, const HalfSmem& h, 
         const float oc = fmaf(c.fq, lo.dsh, c.a0);
         const float on = fmaf(c.fq, hi.dsh, c.a0);
         const float rf = c.fq + fmaxf(c.fq * lo.dsh, c.fq * hi.dsh);
-        const float cb = (float)m.max_dist * (rf * (float)m.ub[lo.nr]);
-        const float nb = (float)m.max_dist * (rf * (float)m.ub[hi.nr]);
+        const float cb = m.max_dist_f * (rf * m.ub_f[lo.nr]);
+        const float nb = m.max_dist_f * (rf * m.ub_f[hi.nr]);
         const float ubw = fmaxf(cb, nb);
         bracket_f32(m, c, fminf(oc, on) - ubw, fmaxf(oc, on) + ubw, a, b);
     }
