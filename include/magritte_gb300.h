@@ -143,6 +143,22 @@ int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, d
 int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, double* u_dev,
                                 double* lambda_diag_dev);
 
+/* Same as mgr_formal_solve_fo2_device, but the call allocates no device memory.
+ * No reference counterpart: an addition of this library for callers that cannot
+ * allocate at solve time.
+ * Per-ray results are staged in a fixed 64 MiB device array of the library (one
+ * per device, shared by all models), processed in chunks of origins that fit.
+ *  - Fails with MGR_ERR_CAPACITY if a single origin needs more than 64 MiB of
+ *    staging, i.e. if hnrays * nfreqs * 8 * k > 64 MiB, where k = (u_dev == NULL) +
+ *    (lambda_diag_dev != NULL).
+ *  - The first call on a device looks up the array's address (a one-time set-up
+ *    step); make it before any stream capture that includes this call.
+ *  - Nothing in the staging array needs to start at zero.
+ *  - Calls that run concurrently on one device (other threads, other models'
+ *    streams) race on the shared array: serialise them. */
+int mgr_formal_solve_fo2_device_noalloc(MgrModel* model, int precision, double* J_dev, double* u_dev,
+                                        double* lambda_diag_dev);
+
 /* Work counted over one formal solve (all origins, all ray pairs): trace steps,
  * neighbour records scanned by the trace (Geometry::get_next, geometry.tpp:22-38),
  * and ray-pair elements including interpolation points summed over lines

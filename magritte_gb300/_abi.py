@@ -58,6 +58,7 @@ SIGNATURES = {
                                      _u32p, _u32p, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgr_formal_solve_fo2_device_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint64)]),
     "mgr_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
@@ -194,6 +195,10 @@ class DeviceModel:
     def autotune(self, precision="split", sample_points=0):
         return autotune(self.h, precision, sample_points)
 
+    def stream(self):
+        """The model's CUDA stream handle (cudaStream_t as an int)."""
+        return load().mgr_model_stream(self.h)
+
 
 def autotune(handle, precision="split", sample_points=0):
     """Pick the fastest launch shape of the formal solve for this model (mgr_autotune_fo2)."""
@@ -201,9 +206,6 @@ def autotune(handle, precision="split", sample_points=0):
     _check(load().mgr_autotune_fo2(handle, PRECISION[precision], sample_points, C.byref(mb), C.byref(w),
                                    C.byref(ms)))
     return {"min_blocks_per_sm": mb.value, "warps_per_block": w.value, "sample_ms": ms.value}
-
-    def stream(self):
-        return load().mgr_model_stream(self.h)
 
 
 def launch_count():
