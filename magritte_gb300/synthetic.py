@@ -320,3 +320,50 @@ def single_ray_1d(npoints: int = 50, dx: float = 1.0e12, nTT: float = 1.0e3, nH2
         boundary_temperature=np.full(2, T_CMB), ray_direction=direction, ray_weight=weight,
         abundance=abund, temperature=np.full(npoints, temp), vturb2=np.full(npoints, (turb / CC) ** 2),
         linedata=[lamda_test_species()], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
+
+
+def delaunay_neighbors(position: np.ndarray):
+    """Neighbour CSR lists from a Delaunay triangulation of the points, as
+    ``set_Delaunay_neighbor_lists`` builds them in 3D (magritte/setup.py:82-93)."""
+    from scipy.spatial import Delaunay
+
+    indptr, indices = Delaunay(position).vertex_neighbor_vertices
+    n_nbs = np.diff(indptr).astype(np.uint32)
+    return np.ascontiguousarray(indices, dtype=np.uint32), n_nbs
+
+
+def van_zadelhoff_1(kind: str = "a", nshells: int = 20, nrays: int = 48, nquads: int = 11,
+                    seed: int = 0) -> RawModel:
+    """Problem 1 of the van Zadelhoff et al. (2002) non-LTE benchmark in the 3D form
+    of the reference's tests/benchmarks/numeric/vanZadelhoff_1_3D_healpix.py:
+    HEALPix shells (nside = 2 + s) at log-spaced radii 1e13..7.8e16 m, each shell
+    randomly rotated (seeded), Delaunay neighbours, the inner and outer shells as CMB
+    boundaries, n_H2 = 2e13 (r_in/r)^2 m^-3, X_mol = 1e-8 (a) or 1e-6 (b), T = 20 K,
+    v_turb = 150 m/s, no velocity, the 2-level 'test' species, ``nrays`` HEALPix rays."""
+    from scipy.spatial.transform import Rotation
+
+    r_in, r_out, nH2_in = 1.0e13, 7.8e16, 2.0e13
+    X_mol = {"a": 1.0e-8, "b": 1.0e-6}[kind]
+    rng = np.random.default_rng(seed)
+    r_shell = np.logspace(np.log10(r_in), np.log10(r_out), nshells, endpoint=True)
+    n_in_shell = [healpix.nside2npix(2 + s) for s in range(nshells)]
+    parts = []
+    for s, (r, n) in enumerate(zip(r_shell, n_in_shell)):
+        pos = r * healpix.pix2vec_ring(2 + s)
+        pos = Rotation.random(random_state=rng).apply(pos)
+        parts.append(pos)
+    position = np.concatenate(parts)
+    P = position.shape[0]
+    rs = np.linalg.norm(position, axis=1)
+    nH2 = nH2_in * (r_in / rs) ** 2
+    nbs, n_nbs = delaunay_neighbors(position)
+    b2p = np.concatenate([np.arange(n_in_shell[0]), np.arange(P - n_in_shell[-1], P)]).astype(np.uint32)
+    direction, weight = healpix.uniform_rays(nrays)
+    roots, wts = quadrature(nquads)
+    abund = np.stack([X_mol * nH2, nH2, np.zeros(P)], axis=1)
+    return RawModel(
+        name=f"vanZadelhoff_1{kind}_3D", dimension=3, position=position, velocity=np.zeros((P, 3)),
+        neighbors=nbs, n_neighbors=n_nbs, boundary2point=b2p, boundary_condition=np.full(len(b2p), BC_CMB, np.int32),
+        boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
+        abundance=abund, temperature=np.full(P, 20.0), vturb2=np.full(P, (150.0 / CC) ** 2),
+        linedata=[lamda_test_species()], quad_roots=[roots], quad_weights=[wts], nquads=nquads)

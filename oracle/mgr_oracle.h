@@ -121,6 +121,63 @@ int orc_formal_solve_sc0(const OrcModel* m, double* J, double* I, double* u, dou
  * Rest-frame shifts.  I [P][F]. */
 int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads);
 
+/* ------------------------------------------------------------------ */
+/* ALI level populations (mgr_oracle_ali.c)                             */
+/* ------------------------------------------------------------------ */
+
+/* One collision partner (collisionPartner.hpp): rates [ntmp][ncol] in m^3/s. */
+typedef struct {
+    uint32_t num_col_partner;   /* abundance column of the partner */
+    int32_t  ortho_para;        /* 0: 'n', 1: 'o', 2: 'p' (orth_or_para_H2) */
+    uint32_t ncol, ntmp;
+    const uint32_t* icol;
+    const uint32_t* jcol;
+    const double*   tmp;
+    const double*   Cd;
+    const double*   Ce;
+} OrcColPar;
+
+/* One line-producing species (linedata.hpp); irad = upper, jrad = lower level. */
+typedef struct {
+    uint32_t num, nlev, nrad, ncolpar, line_offset;
+    const double*   energy;
+    const double*   weight;
+    const uint32_t* irad;
+    const uint32_t* jrad;
+    const double*   A;
+    const double*   Bs;
+    const double*   Ba;
+    const double*   frequency;
+    const OrcColPar* colpar;
+} OrcSpecies;
+
+/* Parameters of compute_level_populations (parameters.hpp:76-104). */
+typedef struct {
+    double   pop_prec, min_rel_pop_for_convergence, convergence_fraction, population_inversion_fraction;
+    double   min_line_opacity, min_line_emissivity;
+    uint32_t Ng_acceleration_mem_limit, adaptive_Ng_acceleration_min_order, Ng_acceleration_remove_N_its;
+    int32_t  use_adaptive_Ng_acceleration, adaptive_Ng_acceleration_use_max_criterion;
+} OrcAliParams;
+
+/* Model::compute_Jeff (model.cpp:514-545) from J [P][F], the ALO diagonal lam [P][L]
+ * and populations (per species [P][nlev]); outputs per species [P][nrad]. */
+int orc_compute_jeff(const OrcModel* m, uint32_t nlspecs, const OrcSpecies* sp, const double* J, const double* lam,
+                     double* const* pops, double* const* Jlin, double* const* Jeff, double* const* Jdif);
+
+/* update_using_statistical_equilibrium of one species from Jeff and the ALO diagonal
+ * Ls (both [P][nrad]) and the current populations; abundance [P][nspecs]. */
+int orc_stateq(const OrcSpecies* s, uint32_t P, const double* abundance, uint32_t nspecs, const double* temperature,
+               const double* Jeff, const double* Ls, const double* pop_in, double min_line_opacity, double* pop_out);
+
+/* Model::compute_level_populations(use_ng, max_it) (model.cpp:654-747).  `em`, `op`,
+ * `crit` are the (writable) arrays m->emissivity/opacity/interp_criterion point to;
+ * pops (per species [P][nlev]) hold the initial populations and receive the result.
+ * err_mean / err_max receive relative_change_mean / _max per normal iteration and
+ * species (may be NULL).  Returns the number of normal iterations, < 0 on failure. */
+int orc_ali_run(OrcModel* m, double* em, double* op, double* crit, uint32_t nlspecs, const OrcSpecies* sp,
+                uint32_t nspecs, const double* abundance, const OrcAliParams* prm, int use_ng, long max_it,
+                double* const* pops, double* err_mean, double* err_max, double* const* Jeff_out, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -304,3 +304,153 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle imager failed ({rc})")
         return I
+
+
+# ---------------------------------------------------------------------------
+# ALI level populations (mgr_oracle_ali.c)
+# ---------------------------------------------------------------------------
+class OrcColPar(C.Structure):
+    _fields_ = [("num_col_partner", C.c_uint32), ("ortho_para", C.c_int32), ("ncol", C.c_uint32),
+                ("ntmp", C.c_uint32), ("icol", _u32p), ("jcol", _u32p), ("tmp", _f64p), ("Cd", _f64p),
+                ("Ce", _f64p)]
+
+
+class OrcSpecies(C.Structure):
+    _fields_ = [("num", C.c_uint32), ("nlev", C.c_uint32), ("nrad", C.c_uint32), ("ncolpar", C.c_uint32),
+                ("line_offset", C.c_uint32), ("energy", _f64p), ("weight", _f64p), ("irad", _u32p),
+                ("jrad", _u32p), ("A", _f64p), ("Bs", _f64p), ("Ba", _f64p), ("frequency", _f64p),
+                ("colpar", C.POINTER(OrcColPar))]
+
+
+class OrcAliParams(C.Structure):
+    _fields_ = [("pop_prec", C.c_double), ("min_rel_pop_for_convergence", C.c_double),
+                ("convergence_fraction", C.c_double), ("population_inversion_fraction", C.c_double),
+                ("min_line_opacity", C.c_double), ("min_line_emissivity", C.c_double),
+                ("Ng_acceleration_mem_limit", C.c_uint32), ("adaptive_Ng_acceleration_min_order", C.c_uint32),
+                ("Ng_acceleration_remove_N_its", C.c_uint32), ("use_adaptive_Ng_acceleration", C.c_int32),
+                ("adaptive_Ng_acceleration_use_max_criterion", C.c_int32)]
+
+
+# Defaults of src/model/parameters/parameters.hpp:76-103.
+ALI_DEFAULTS = dict(pop_prec=1.0e-6, min_rel_pop_for_convergence=1.0e-10, convergence_fraction=0.995,
+                    population_inversion_fraction=-1.0, min_line_opacity=1.0e-13, min_line_emissivity=1.0e-50,
+                    Ng_acceleration_mem_limit=9, adaptive_Ng_acceleration_min_order=2,
+                    Ng_acceleration_remove_N_its=0, use_adaptive_Ng_acceleration=1,
+                    adaptive_Ng_acceleration_use_max_criterion=1)
+
+_ORTHO_PARA = {"n": 0, "o": 1, "p": 2}
+
+
+def species_structs(raw, nrad_cum):
+    """(OrcSpecies array, keepalive list) for the line-producing species of a RawModel."""
+    keep = []
+
+    def arr(x, dt):
+        a = np.ascontiguousarray(x, dtype=dt)
+        keep.append(a)
+        return a
+
+    sp = (OrcSpecies * len(raw.linedata))()
+    for l, ld in enumerate(raw.linedata):
+        cps = (OrcColPar * max(1, len(ld.colpar)))()
+        keep.append(cps)
+        for c, cp in enumerate(ld.colpar):
+            cps[c].num_col_partner = cp.num_col_partner
+            cps[c].ortho_para = _ORTHO_PARA[cp.orth_or_para_H2]
+            cps[c].ncol = cp.ncol
+            cps[c].ntmp = cp.ntmp
+            cps[c].icol = _ptr(arr(cp.icol, np.uint32), _u32p)
+            cps[c].jcol = _ptr(arr(cp.jcol, np.uint32), _u32p)
+            cps[c].tmp = _ptr(arr(cp.tmp, np.float64), _f64p)
+            cps[c].Cd = _ptr(arr(cp.Cd, np.float64), _f64p)
+            cps[c].Ce = _ptr(arr(cp.Ce, np.float64), _f64p)
+        s = sp[l]
+        s.num, s.nlev, s.nrad, s.ncolpar = ld.num, ld.nlev, ld.nrad, len(ld.colpar)
+        s.line_offset = int(nrad_cum[l])
+        s.energy = _ptr(arr(ld.energy, np.float64), _f64p)
+        s.weight = _ptr(arr(ld.weight, np.float64), _f64p)
+        s.irad = _ptr(arr(ld.irad, np.uint32), _u32p)
+        s.jrad = _ptr(arr(ld.jrad, np.uint32), _u32p)
+        s.A = _ptr(arr(ld.A, np.float64), _f64p)
+        s.Bs = _ptr(arr(ld.Bs, np.float64), _f64p)
+        s.Ba = _ptr(arr(ld.Ba, np.float64), _f64p)
+        s.frequency = _ptr(arr(ld.frequency, np.float64), _f64p)
+        s.colpar = cps
+    return sp, keep
+
+
+def _declare_ali(l):
+    l.orc_compute_jeff.restype = C.c_int
+    l.orc_compute_jeff.argtypes = [C.POINTER(OrcModel), C.c_uint32, C.POINTER(OrcSpecies), _f64p, _f64p,
+                                   C.POINTER(_f64p), C.POINTER(_f64p), C.POINTER(_f64p), C.POINTER(_f64p)]
+    l.orc_stateq.restype = C.c_int
+    l.orc_stateq.argtypes = [C.POINTER(OrcSpecies), C.c_uint32, _f64p, C.c_uint32, _f64p, _f64p, _f64p, _f64p,
+                             C.c_double, _f64p]
+    l.orc_ali_run.restype = C.c_int
+    l.orc_ali_run.argtypes = [C.POINTER(OrcModel), _f64p, _f64p, _f64p, C.c_uint32, C.POINTER(OrcSpecies),
+                              C.c_uint32, _f64p, C.POINTER(OrcAliParams), C.c_int, C.c_long, C.POINTER(_f64p),
+                              _f64p, _f64p, C.POINTER(_f64p), C.c_int]
+
+
+def _ptr_array(arrays):
+    out = (_f64p * len(arrays))()
+    for i, a in enumerate(arrays):
+        out[i] = _ptr(a, _f64p)
+    return out
+
+
+class AliOracle:
+    """The oracle's compute_Jeff / statistical equilibrium / ALI loop on a RawModel.
+
+    ``arrays`` is the dict of ``reference_setup(raw)`` (its populations are the
+    initial, LTE, ones); emissivity, opacity and the interpolation criterion in it
+    are updated in place by ``run``."""
+
+    def __init__(self, raw, arrays):
+        self.raw = raw
+        self.a = arrays
+        self.orc = Oracle(arrays)
+        self.sp, self._keep = species_structs(raw, arrays["nrad_cum"])
+        self.abundance = np.ascontiguousarray(raw.abundance, np.float64)
+        _declare_ali(lib())
+
+    def compute_jeff(self, J, lam, pops):
+        P = self.a["npoints"]
+        pops = [np.ascontiguousarray(p, np.float64) for p in pops]
+        outs = [[np.zeros((P, ld.nrad)) for ld in self.raw.linedata] for _ in range(3)]
+        rc = lib().orc_compute_jeff(C.byref(self.orc.m), len(self.raw.linedata), self.sp,
+                                    _ptr(np.ascontiguousarray(J), _f64p), _ptr(np.ascontiguousarray(lam), _f64p),
+                                    _ptr_array(pops), _ptr_array(outs[0]), _ptr_array(outs[1]), _ptr_array(outs[2]))
+        if rc != 0:
+            raise RuntimeError("oracle Jeff failed")
+        return dict(Jlin=outs[0], Jeff=outs[1], Jdif=outs[2])
+
+    def stateq(self, l, Jeff, Ls, pop, min_line_opacity=1.0e-13):
+        P = self.a["npoints"]
+        out = np.zeros((P, self.raw.linedata[l].nlev))
+        rc = lib().orc_stateq(C.byref(self.sp[l]), P, _ptr(self.abundance, _f64p), self.abundance.shape[1],
+                              _ptr(self.a["temperature"], _f64p), _ptr(np.ascontiguousarray(Jeff), _f64p),
+                              _ptr(np.ascontiguousarray(Ls), _f64p), _ptr(np.ascontiguousarray(pop), _f64p),
+                              min_line_opacity, _ptr(out, _f64p))
+        if rc != 0:
+            raise RuntimeError("oracle statistical equilibrium failed")
+        return out
+
+    def run(self, use_ng=True, max_it=100, nthreads=0, **params):
+        prm = dict(ALI_DEFAULTS)
+        prm.update(params)
+        p = OrcAliParams(**prm)
+        pops = [np.ascontiguousarray(x, np.float64).copy() for x in self.a["populations"]]
+        nls = len(self.raw.linedata)
+        err_mean = np.zeros(max_it * nls)
+        err_max = np.zeros(max_it * nls)
+        Jeff = [np.zeros((self.a["npoints"], ld.nrad)) for ld in self.raw.linedata]
+        it = lib().orc_ali_run(C.byref(self.orc.m), _ptr(self.a["emissivity"], _f64p),
+                               _ptr(self.a["opacity"], _f64p), _ptr(self.a["interp_criterion"], _f64p), nls,
+                               self.sp, self.abundance.shape[1], _ptr(self.abundance, _f64p), C.byref(p),
+                               int(use_ng), max_it, _ptr_array(pops), _ptr(err_mean, _f64p), _ptr(err_max, _f64p),
+                               _ptr_array(Jeff), nthreads)
+        if it < 0:
+            raise RuntimeError(f"oracle ALI failed ({it})")
+        return dict(iterations=it, populations=pops, Jeff=Jeff, error_mean=err_mean[:it * nls],
+                    error_max=err_max[:it * nls])
