@@ -177,6 +177,84 @@ int mgr_set_tuning(MgrModel* model, int precision, int min_blocks_per_sm, int wa
 int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int* best_min_blocks,
                      int* best_warps, float* best_ms);
 
+/* ------------------------------------------------------------------------------
+ * Level populations: compute_Jeff and the ALI loop (compute_level_populations).
+ * ------------------------------------------------------------------------------ */
+
+/* One collision partner of a species (CollisionPartner, collisionPartner.hpp).
+ * Rates in m^3/s, [ntmp][ncol] row-major; icol = upper, jcol = lower level. */
+typedef struct {
+    uint32_t        num_col_partner;  /* abundance column of the partner        */
+    int32_t         ortho_para;       /* orth_or_para_H2: 0 'n', 1 'o', 2 'p'   */
+    uint32_t        ncol, ntmp;
+    const uint32_t* icol;
+    const uint32_t* jcol;
+    const double*   tmp;              /* [ntmp] ascending                       */
+    const double*   Cd;               /* de-excitation                          */
+    const double*   Ce;               /* excitation                             */
+} MgrCollisionPartnerDesc;
+
+/* One line-producing species (Linedata, linedata.hpp).  Its lines are the global
+ * lines nrad_cum .. nrad_cum + nrad - 1 of the model, in order; irad = upper,
+ * jrad = lower level of each radiative transition.  nlev <= 64. */
+typedef struct {
+    uint32_t        num;              /* abundance column of the species        */
+    uint32_t        nlev, nrad, ncolpar;
+    const double*   energy;           /* [nlev] J                               */
+    const double*   weight;           /* [nlev]                                 */
+    const uint32_t* irad;             /* [nrad]                                 */
+    const uint32_t* jrad;
+    const double*   A;
+    const double*   Bs;
+    const double*   Ba;
+    const double*   frequency;
+    const MgrCollisionPartnerDesc* colpar;  /* [ncolpar] */
+} MgrSpeciesDesc;
+
+/* Parameters of Model::compute_level_populations (parameters.hpp:76-104). */
+typedef struct {
+    double   pop_prec;                          /* 1e-6  */
+    double   min_rel_pop_for_convergence;       /* 1e-10 */
+    double   convergence_fraction;              /* 0.995 */
+    double   population_inversion_fraction;     /* -1    */
+    double   min_line_opacity;                  /* 1e-13 */
+    double   min_line_emissivity;               /* 1e-50 */
+    uint32_t Ng_acceleration_mem_limit;         /* 9, at most 16 */
+    uint32_t adaptive_Ng_acceleration_min_order;/* 2     */
+    uint32_t Ng_acceleration_remove_N_its;      /* 0     */
+    int32_t  use_adaptive_Ng_acceleration;      /* 1     */
+    int32_t  adaptive_Ng_acceleration_use_max_criterion; /* 1 */
+} MgrAliParams;
+
+/* Attach the line-producing species, abundances [P][nspecs] (number densities, the
+ * reference's chemistry.species.abundance) and current level populations (one
+ * [P][nlev] array per species) to a model.  Replaces earlier species data and
+ * starts a fresh population history (LineProducingSpecies::populations). */
+int mgr_model_set_species(MgrModel* model, uint32_t nlspecs, const MgrSpeciesDesc* species, uint32_t nspecs,
+                          const double* abundance, const double* const* populations);
+
+/* Model::compute_Jeff (model.cpp:514-545) from the J and ALO of the last formal solve
+ * on this model (its buffers must still be valid for the device entry points).
+ * Outputs of species l, [P][nrad] each; any may be NULL.  Blocks. */
+int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, double* Jdif);
+
+/* Model::compute_level_populations(use_ng, max_it) (model.cpp:654-747): formal
+ * solves in `precision`, Jeff, statistical equilibrium, corrections and Ng
+ * acceleration until convergence, all on the device.  *iterations receives the
+ * number of normal iterations; error_mean / error_max (may be NULL, room for
+ * err_capacity values) receive relative_change_mean / _max per normal iteration and
+ * species, as Model::error_mean / error_max.  Populations stay on the device
+ * (mgr_get_populations); the line emissivities and opacities are updated. */
+int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, long max_iterations,
+                                  const MgrAliParams* params, int* iterations, double* error_mean,
+                                  double* error_max, uint32_t err_capacity);
+
+/* Copy species l's level populations [P][nlev] to the host. */
+int mgr_get_populations(MgrModel* model, uint32_t l, double* populations);
+
+/* Copy the current line emissivity and opacity [P][L] to the host (either may be NULL). */
+int mgr_get_line_data(MgrModel* model, double* emissivity, double* opacity);
+
 /* Block until all work on the model's stream has finished; returns the first
  * kernel-side status recorded since the last call (trace / capacity / non-finite). */
 int mgr_sync(MgrModel* model);

@@ -45,6 +45,36 @@ class MgrModelDesc(C.Structure):
     _fields_ = DESC_FIELDS
 
 
+class MgrCollisionPartnerDesc(C.Structure):
+    _fields_ = [("num_col_partner", C.c_uint32), ("ortho_para", C.c_int32), ("ncol", C.c_uint32),
+                ("ntmp", C.c_uint32), ("icol", _u32p), ("jcol", _u32p), ("tmp", _f64p), ("Cd", _f64p),
+                ("Ce", _f64p)]
+
+
+class MgrSpeciesDesc(C.Structure):
+    _fields_ = [("num", C.c_uint32), ("nlev", C.c_uint32), ("nrad", C.c_uint32), ("ncolpar", C.c_uint32),
+                ("energy", _f64p), ("weight", _f64p), ("irad", _u32p), ("jrad", _u32p), ("A", _f64p),
+                ("Bs", _f64p), ("Ba", _f64p), ("frequency", _f64p),
+                ("colpar", C.POINTER(MgrCollisionPartnerDesc))]
+
+
+class MgrAliParams(C.Structure):
+    _fields_ = [("pop_prec", C.c_double), ("min_rel_pop_for_convergence", C.c_double),
+                ("convergence_fraction", C.c_double), ("population_inversion_fraction", C.c_double),
+                ("min_line_opacity", C.c_double), ("min_line_emissivity", C.c_double),
+                ("Ng_acceleration_mem_limit", C.c_uint32), ("adaptive_Ng_acceleration_min_order", C.c_uint32),
+                ("Ng_acceleration_remove_N_its", C.c_uint32), ("use_adaptive_Ng_acceleration", C.c_int32),
+                ("adaptive_Ng_acceleration_use_max_criterion", C.c_int32)]
+
+
+# Defaults of Magritte's Parameters (src/model/parameters/parameters.hpp:76-103).
+ALI_DEFAULTS = dict(pop_prec=1.0e-6, min_rel_pop_for_convergence=1.0e-10, convergence_fraction=0.995,
+                    population_inversion_fraction=-1.0, min_line_opacity=1.0e-13, min_line_emissivity=1.0e-50,
+                    Ng_acceleration_mem_limit=9, adaptive_Ng_acceleration_min_order=2,
+                    Ng_acceleration_remove_N_its=0, use_adaptive_Ng_acceleration=1,
+                    adaptive_Ng_acceleration_use_max_criterion=1)
+
+
 # Every exported symbol of include/magritte_gb300.h with its ctypes signature.
 SIGNATURES = {
     "mgr_last_error": (C.c_char_p, []),
@@ -64,6 +94,13 @@ SIGNATURES = {
     "mgr_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "mgr_autotune_fo2": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_float)]),
+    "mgr_model_set_species": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(MgrSpeciesDesc), C.c_uint32, _f64p,
+                                        C.POINTER(_f64p)]),
+    "mgr_compute_jeff": (C.c_int, [C.c_void_p, C.c_uint32, _f64p, _f64p, _f64p]),
+    "mgr_compute_level_populations": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_long, C.POINTER(MgrAliParams),
+                                                C.POINTER(C.c_int), _f64p, _f64p, C.c_uint32]),
+    "mgr_get_populations": (C.c_int, [C.c_void_p, C.c_uint32, _f64p]),
+    "mgr_get_line_data": (C.c_int, [C.c_void_p, _f64p, _f64p]),
     "mgr_sync": (C.c_int, [C.c_void_p]),
     "mgr_model_stream": (C.c_void_p, [C.c_void_p]),
     "mgr_launch_count": (C.c_uint64, []),
@@ -198,6 +235,75 @@ class DeviceModel:
     def stream(self):
         """The model's CUDA stream handle (cudaStream_t as an int)."""
         return load().mgr_model_stream(self.h)
+
+    # ---- level populations ----
+    def set_species(self, linedata, abundance, populations):
+        """Attach line-producing species (``magritte_gb300.synthetic.Linedata`` list),
+        abundances [P][nspecs] and populations (list of [P][nlev])."""
+        keep = []
+
+        def arr(x, dt):
+            a = np.ascontiguousarray(x, dtype=dt)
+            keep.append(a)
+            return a
+
+        sp = (MgrSpeciesDesc * len(linedata))()
+        for l, ld in enumerate(linedata):
+            cps = (MgrCollisionPartnerDesc * max(1, len(ld.colpar)))()
+            keep.append(cps)
+            for c, cp in enumerate(ld.colpar):
+                cps[c].num_col_partner = cp.num_col_partner
+                cps[c].ortho_para = {"n": 0, "o": 1, "p": 2}[cp.orth_or_para_H2]
+                cps[c].ncol, cps[c].ntmp = cp.ncol, cp.ntmp
+                cps[c].icol = _ptr(arr(cp.icol, np.uint32), _u32p)
+                cps[c].jcol = _ptr(arr(cp.jcol, np.uint32), _u32p)
+                cps[c].tmp = _ptr(arr(cp.tmp, np.float64), _f64p)
+                cps[c].Cd = _ptr(arr(cp.Cd, np.float64), _f64p)
+                cps[c].Ce = _ptr(arr(cp.Ce, np.float64), _f64p)
+            d = sp[l]
+            d.num, d.nlev, d.nrad, d.ncolpar = ld.num, ld.nlev, ld.nrad, len(ld.colpar)
+            d.energy = _ptr(arr(ld.energy, np.float64), _f64p)
+            d.weight = _ptr(arr(ld.weight, np.float64), _f64p)
+            d.irad = _ptr(arr(ld.irad, np.uint32), _u32p)
+            d.jrad = _ptr(arr(ld.jrad, np.uint32), _u32p)
+            d.A = _ptr(arr(ld.A, np.float64), _f64p)
+            d.Bs = _ptr(arr(ld.Bs, np.float64), _f64p)
+            d.Ba = _ptr(arr(ld.Ba, np.float64), _f64p)
+            d.frequency = _ptr(arr(ld.frequency, np.float64), _f64p)
+            d.colpar = cps
+        ab = arr(abundance, np.float64)
+        pops = [arr(p, np.float64) for p in populations]
+        pp = (_f64p * len(pops))(*[_ptr(p, _f64p) for p in pops])
+        self.nlev = [ld.nlev for ld in linedata]
+        self.nrad = [ld.nrad for ld in linedata]
+        _check(load().mgr_model_set_species(self.h, len(linedata), sp, ab.shape[1], _ptr(ab, _f64p), pp))
+
+    def compute_jeff(self, l=0):
+        out = [np.empty((self.P, self.nrad[l])) for _ in range(3)]
+        _check(load().mgr_compute_jeff(self.h, l, *[_ptr(o, _f64p) for o in out]))
+        return dict(Jlin=out[0], Jeff=out[1], Jdif=out[2])
+
+    def compute_level_populations(self, precision="fp64", use_ng=True, max_it=100, **params):
+        prm = dict(ALI_DEFAULTS)
+        prm.update(params)
+        p = MgrAliParams(**prm)
+        it = C.c_int()
+        cap = max_it * len(self.nlev)
+        em, ex = np.zeros(cap), np.zeros(cap)
+        _check(load().mgr_compute_level_populations(self.h, PRECISION[precision], int(use_ng), max_it, C.byref(p),
+                                                    C.byref(it), _ptr(em, _f64p), _ptr(ex, _f64p), cap))
+        n = it.value * len(self.nlev)
+        return dict(iterations=it.value, error_mean=em[:n], error_max=ex[:n])
+
+    def populations(self, l=0):
+        out = np.empty((self.P, self.nlev[l]))
+        _check(load().mgr_get_populations(self.h, l, _ptr(out, _f64p)))
+        return out
+
+    def line_data(self):
+        em, op = np.empty((self.P, self.L)), np.empty((self.P, self.L))
+        _check(load().mgr_get_line_data(self.h, _ptr(em, _f64p), _ptr(op, _f64p)))
+        return em, op
 
 
 def autotune(handle, precision="split", sample_points=0):

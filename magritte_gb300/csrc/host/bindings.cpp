@@ -252,6 +252,11 @@ PYBIND11_MODULE(core, m) {
         .def("set_dshift_max", &Model::set_dshift_max)
         .def("compute_radiation_field_feautrier_order_2", &Model::compute_radiation_field_feautrier_order_2,
              py::call_guard<py::gil_scoped_release>())
+        .def("compute_Jeff", &Model::compute_Jeff, py::call_guard<py::gil_scoped_release>())
+        .def("compute_level_populations", &Model::compute_level_populations, py::arg("use_Ng_acceleration"),
+             py::arg("max_niterations"), py::call_guard<py::gil_scoped_release>())
+        .def_readonly("error_mean", &Model::error_mean)
+        .def_readonly("error_max", &Model::error_max)
         .def("release_device", &Model::release_device)
         .def("upload", [](Model& m) { return (uintptr_t)m.upload(); },
              "Upload (or refresh) the device model; returns the MgrModel* handle as an integer")

@@ -546,4 +546,117 @@ int Model::compute_radiation_field_feautrier_order_2() {
     return 0;
 }
 
+// ---------------------------------------------------------------------------------
+// Level populations (model.cpp:514-545, :654-747) on the device
+// ---------------------------------------------------------------------------------
+void Model::attach_species() {
+    const Size P = parameters.npoints_.v;
+    const Size nls = parameters.nlspecs_.v;
+    std::vector<MgrSpeciesDesc> sd(nls);
+    std::vector<std::vector<MgrCollisionPartnerDesc>> cps(nls);
+    std::vector<std::vector<double>> cd_flat, ce_flat;
+    std::vector<const double*> pops(nls);
+    for (Size l = 0; l < nls; l++) {
+        const LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        const Linedata& ld = ls.linedata;
+        for (const CollisionPartner& c : ld.colpar) {
+            MgrCollisionPartnerDesc d{};
+            d.num_col_partner = c.num_col_partner;
+            d.ortho_para = c.orth_or_para_H2 == "o" ? 1 : c.orth_or_para_H2 == "p" ? 2 : 0;
+            d.ncol = c.ncol;
+            d.ntmp = c.ntmp;
+            d.icol = c.icol.data();
+            d.jcol = c.jcol.data();
+            d.tmp = c.tmp.data();
+            std::vector<double> cdv, cev;
+            for (Size t = 0; t < c.ntmp; t++)
+                for (Size k = 0; k < c.ncol; k++) {
+                    cdv.push_back(c.Cd[t][k]);
+                    cev.push_back(c.Ce[t][k]);
+                }
+            cd_flat.push_back(std::move(cdv));
+            ce_flat.push_back(std::move(cev));
+            d.Cd = cd_flat.back().data();
+            d.Ce = ce_flat.back().data();
+            cps[l].push_back(d);
+        }
+        MgrSpeciesDesc& d = sd[l];
+        d.num = ld.num;
+        d.nlev = ld.nlev;
+        d.nrad = ld.nrad;
+        d.ncolpar = (uint32_t)cps[l].size();
+        d.energy = ld.energy.data();
+        d.weight = ld.weight.data();
+        d.irad = ld.irad.data();
+        d.jrad = ld.jrad.data();
+        d.A = ld.A.data();
+        d.Bs = ld.Bs.data();
+        d.Ba = ld.Ba.data();
+        d.frequency = ld.frequency.data();
+        d.colpar = cps[l].data();
+        pops[l] = ls.population.data();
+    }
+    // cd_flat / ce_flat may have reallocated while growing: refresh the pointers
+    size_t c = 0;
+    for (Size l = 0; l < nls; l++)
+        for (auto& d : cps[l]) {
+            d.Cd = cd_flat[c].data();
+            d.Ce = ce_flat[c].data();
+            c++;
+        }
+    const Size nspecs = (Size)(chemistry.species.abundance.size() / P);
+    check(mgr_model_set_species(dev_, nls, sd.data(), nspecs, chemistry.species.abundance.data(), pops.data()));
+}
+
+int Model::compute_Jeff() {
+    if (!dev_ || radiation.J.size() == 0)
+        throw std::runtime_error("compute_Jeff needs a formal solve (compute_radiation_field_feautrier_order_2) first");
+    attach_species();
+    const Size P = parameters.npoints_.v;
+    for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+        LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        const Size nrad = ls.linedata.nrad;
+        ls.Jlin.resize({P, nrad});
+        ls.Jeff.resize({P, nrad});
+        ls.Jdif.resize({P, nrad});
+        check(mgr_compute_jeff(dev_, l, ls.Jlin.data(), ls.Jeff.data(), ls.Jdif.data()));
+    }
+    return 0;
+}
+
+int Model::compute_level_populations(bool use_Ng_acceleration, long max_niterations) {
+    if (spectralDiscretisation != SD_Lines) throw std::runtime_error("Spectral discretisation was not set for Lines!");
+    MgrModel* dev = upload();
+    attach_species();
+    MgrAliParams prm{};
+    prm.pop_prec = parameters.pop_prec;
+    prm.min_rel_pop_for_convergence = parameters.min_rel_pop_for_convergence;
+    prm.convergence_fraction = parameters.convergence_fraction;
+    prm.population_inversion_fraction = parameters.population_inversion_fraction;
+    prm.min_line_opacity = parameters.min_line_opacity;
+    prm.min_line_emissivity = parameters.min_line_emissivity;
+    prm.Ng_acceleration_mem_limit = parameters.Ng_acceleration_mem_limit;
+    prm.adaptive_Ng_acceleration_min_order = parameters.adaptive_Ng_acceleration_min_order;
+    prm.Ng_acceleration_remove_N_its = parameters.Ng_acceleration_remove_N_its;
+    prm.use_adaptive_Ng_acceleration = parameters.use_adaptive_Ng_acceleration ? 1 : 0;
+    prm.adaptive_Ng_acceleration_use_max_criterion = parameters.adaptive_Ng_acceleration_use_max_criterion ? 1 : 0;
+    const Size nls = parameters.nlspecs_.v;
+    const uint32_t cap = (uint32_t)(max_niterations > 0 ? max_niterations : 0) * nls;
+    std::vector<double> emean(cap), emax(cap);
+    int iterations = 0;
+    check(mgr_compute_level_populations(dev, parameters.precision, use_Ng_acceleration ? 1 : 0, max_niterations, &prm,
+                                        &iterations, emean.data(), emax.data(), cap));
+    error_mean.assign(emean.begin(), emean.begin() + (size_t)iterations * nls);
+    error_max.assign(emax.begin(), emax.begin() + (size_t)iterations * nls);
+    for (Size l = 0; l < nls; l++) {
+        LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        check(mgr_get_populations(dev, l, ls.population.data()));
+        ls.population.touch();
+    }
+    check(mgr_get_line_data(dev, lines.emissivity.data(), lines.opacity.data()));
+    lines.emissivity.touch();
+    lines.opacity.touch();
+    return iterations;
+}
+
 }  // namespace mgrhost

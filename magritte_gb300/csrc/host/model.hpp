@@ -250,6 +250,8 @@ class Model {
     int compute_LTE_level_populations();
     int set_dshift_max();
     int compute_radiation_field_feautrier_order_2();
+    int compute_Jeff();
+    int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
 
     // Device management (GB300): the MgrModel mirroring this Model.
     // upload(): prepare, dshift_max, and (re)create or refresh the device model.
@@ -264,6 +266,7 @@ class Model {
     std::vector<double> crit_;
     uint64_t signature() const;
     void fill_desc(MgrModelDesc& d);
+    void attach_species();
     void set_emissivity_and_opacity();
 };
 

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "mgr_ali.h"
 #include "mgr_internal.h"
 
 namespace mgr {
@@ -141,6 +142,7 @@ void mgr_model_free(MgrModel* model) {
     if (model->u_scratch) cudaFree(model->u_scratch);
     if (model->lam_scratch) cudaFree(model->lam_scratch);
     if (model->work) cudaFree(model->work);
+    ali_free(model);
     if (model->stream) cudaStreamDestroy(model->stream);
     delete model;
 }
@@ -460,6 +462,8 @@ int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, d
     cudaError_t e = launch_fo2_range(model, precision, 0, model->dm.P, J_dev, u_dev, lambda_diag_dev, model->work,
                                      model->work_bytes);
     if (e != cudaSuccess) return cuda_fail(e, "formal solve launch");
+    model->last_J = J_dev;
+    model->last_lam = lambda_diag_dev;
     return MGR_OK;
 }
 

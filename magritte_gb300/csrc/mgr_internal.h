@@ -10,6 +10,10 @@
 #include "mgr_device.cuh"
 #include "mgr_scale.h"
 
+namespace mgr {
+struct AliState;
+}
+
 struct MgrModel {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -43,6 +47,11 @@ struct MgrModel {
     // staging of u(rr, o, f) / L_diag(rr, o, f) between the two formal-solve stages
     double* work = nullptr;
     size_t work_bytes = 0;
+    // J [P][F] and ALO diagonal [P][L] of the last formal solve (device), for Jeff
+    const double* last_J = nullptr;
+    const double* last_lam = nullptr;
+    // line-producing species and the ALI loop (mgr_ali.cu)
+    mgr::AliState* ali = nullptr;
 };
 
 namespace mgr {

@@ -1,0 +1,117 @@
+"""GPU compute_Jeff and ALI level populations against the oracle, through the C ABI.
+
+Bar: Jeff from the same J and ALO bit-for-bit up to rounding (1e-13); level
+populations after the ALI loop within 1e-6 relative of the oracle (FP64 mode) with
+the same number of iterations, for the Default and the Adaptive Ng criteria."""
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+from magritte_gb300 import _abi
+from magritte_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_with_correctly_rounded_erf():
+    O.set_erf_mode(1)
+    yield
+    O.set_erf_mode(0)
+
+
+def _device(raw, a):
+    dev = _abi.DeviceModel(a)
+    dev.set_species(raw.linedata, raw.abundance, a["populations"])
+    return dev
+
+
+def _rel(x, ref, floor):
+    return np.max(np.abs(x - ref) / np.maximum(np.abs(ref), floor))
+
+
+def test_jeff_matches_oracle(gpu_lib):
+    raw = S.grid_cube(n=10, nquads=11)
+    a = H.setup(raw)
+    dev = _device(raw, a)
+    try:
+        out = dev.formal_solve_fo2("fp64")
+        g = dev.compute_jeff(0)
+        ali = O.AliOracle(raw, a)
+        ref = ali.compute_jeff(out["J"], out["lambda_diag"], a["populations"])
+        for k in ("Jlin", "Jeff", "Jdif"):
+            assert _rel(g[k], ref[k][0], 1e-300) < 1e-13, k
+    finally:
+        dev.close()
+
+
+@pytest.mark.parametrize("adaptive", [0, 1])
+def test_ali_matches_oracle_cube(gpu_lib, adaptive):
+    raw = S.grid_cube(n=10, nquads=11)
+    a = H.setup(raw)
+    params = dict(use_adaptive_Ng_acceleration=adaptive, Ng_acceleration_mem_limit=4)
+    ref = O.AliOracle(raw, H.setup(raw)).run(use_ng=True, max_it=30, **params)
+    dev = _device(raw, a)
+    try:
+        got = dev.compute_level_populations("fp64", use_ng=True, max_it=30, **params)
+        assert got["iterations"] == ref["iterations"]
+        pop = dev.populations(0)
+        tot = raw.abundance[:, raw.linedata[0].num][:, None]
+        assert _rel(pop, ref["populations"][0], 1e-10 * tot) < 1e-6
+        np.testing.assert_allclose(got["error_max"], ref["error_max"], rtol=1e-3, atol=1e-12)
+    finally:
+        dev.close()
+
+
+def test_ali_matches_oracle_van_zadelhoff(gpu_lib):
+    """The optically thick van Zadelhoff 1b model (6 shells): Ng accelerations of
+    several orders, 20 iterations."""
+    raw = S.van_zadelhoff_1("b", nshells=6)
+    a = H.setup(raw)
+    ref = O.AliOracle(raw, H.setup(raw)).run(use_ng=True, max_it=20)
+    dev = _device(raw, a)
+    try:
+        got = dev.compute_level_populations("fp64", use_ng=True, max_it=20)
+        assert got["iterations"] == ref["iterations"]
+        pop = dev.populations(0)
+        tot = raw.abundance[:, 0][:, None]
+        assert _rel(pop, ref["populations"][0], 1e-10 * tot) < 1e-6
+    finally:
+        dev.close()
+
+
+def test_ali_split_precision_close_to_fp64(gpu_lib):
+    raw = S.grid_cube(n=10, nquads=11)
+    a = H.setup(raw)
+    res = {}
+    for prec in ("fp64", "split"):
+        dev = _device(raw, a)
+        try:
+            dev.compute_level_populations(prec, use_ng=True, max_it=30)
+            res[prec] = dev.populations(0)
+        finally:
+            dev.close()
+    assert _rel(res["split"], res["fp64"], 1e-300) < 1e-5
+
+
+def test_core_model_compute_level_populations(gpu_lib):
+    """The drop-in API: core.Model.compute_level_populations(use_Ng, max_it) after
+    compute_LTE_level_populations, against the oracle's ALI loop."""
+    from magritte_gb300 import loader
+
+    raw = S.grid_cube(n=10, nquads=11)
+    ref = O.AliOracle(raw, H.setup(raw)).run(use_ng=True, max_it=30)
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    it = model.compute_level_populations(True, 30)
+    assert it == ref["iterations"]
+    pop = np.array(model.lines.lineProducingSpecies[0].population).reshape(raw.npoints, -1)
+    tot = raw.abundance[:, raw.linedata[0].num][:, None]
+    assert _rel(pop, ref["populations"][0], 1e-10 * tot) < 1e-6
+    assert len(model.error_max) == it
+    model.compute_radiation_field_feautrier_order_2()
+    model.compute_Jeff()
+    assert np.isfinite(np.array(model.lines.lineProducingSpecies[0].Jeff)).all()
