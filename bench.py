@@ -46,6 +46,10 @@ def parse():
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-ali", action="store_true", help="skip the ALI wall-time leg")
+    p.add_argument("--ali-points", type=int, default=50_000)
+    p.add_argument("--ali-nside", type=int, default=2)
+    p.add_argument("--ali-iterations", type=int, default=20)
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the library's default launch shape (for profiling one production launch)")
     return p.parse_args()
@@ -148,6 +152,37 @@ def cpu_baseline(raw, nthreads, rr_count=2, n_origins=40000):
     solves = n_o * rr_count * arrays["nfreqs"]
     return {"value": solves / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": f"ray pairs 0-{rr_count - 1} x origins 0-{n_o - 1} ({solves} solves, {dt:.2f} s)"}
+
+
+def run_ali(args):
+    """ALI wall time: compute_level_populations(use_Ng=True, N) through core.Model on
+    the non-LTE sphere workload (Delaunay points ~ r^-2, 10-level rotor, nquads 21),
+    Default Ng every 4 iterations, exactly N normal iterations (pop_prec = 0 keeps
+    the loop from stopping early), split-precision formal solves, graph-captured
+    iterations.  The timed call includes the model upload."""
+    import time as _t
+
+    from magritte_gb300 import loader, synthetic
+
+    raw = synthetic.nlte_sphere(npoints=args.ali_points, nside=args.ali_nside)
+    model = loader.to_core(raw, precision=args.precision)
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    prm = model.parameters
+    prm.store_u = False
+    prm.use_adaptive_Ng_acceleration = False
+    prm.Ng_acceleration_mem_limit = 4
+    prm.pop_prec = 0.0
+    t0 = _t.perf_counter()
+    it = model.compute_level_populations(True, args.ali_iterations)
+    wall = _t.perf_counter() - t0
+    P, F, R = prm.npoints(), prm.nfreqs(), prm.hnrays()
+    return {"workload": f"nlte_sphere {raw.npoints} points (Delaunay, density ~ r^-2), {raw.nrays} rays, "
+                        f"10-level rotor (9 lines) x nquads {raw.nquads}",
+            "iterations": it, "ng": "Default, every 4", "precision": args.precision, "wall_s": wall,
+            "s_per_iteration": wall / max(it, 1), "solves_per_iteration": float(P) * R * F,
+            "note": "config-2 family reduced to fit the bench time; no CPU leg (one oracle iteration takes minutes)"}
 
 
 def run_reference(args, rank, ws):
@@ -302,6 +337,7 @@ def run_ours(args, rank, ws):
 
     if rank != 0:
         return
+    ali = None if args.no_ali else run_ali(args)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(raw, os.cpu_count() or 1)
@@ -328,6 +364,7 @@ def run_ours(args, rank, ws):
         "speedup_vs_fp64_gpu": (fp64_ms / (1000.0 * kernel_s / args.steps)) if fp64_ms else None,
         "work": {"trace_steps": st_steps.value, "neighbour_reads": st_nbr.value, "elements": st_elem.value},
         "tuning": tuning,
+        "ali": ali,
     }
     print(json.dumps(line), flush=True)
 

@@ -367,3 +367,39 @@ def van_zadelhoff_1(kind: str = "a", nshells: int = 20, nrays: int = 48, nquads:
         boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
         abundance=abund, temperature=np.full(P, 20.0), vturb2=np.full(P, (150.0 / CC) ** 2),
         linedata=[lamda_test_species()], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
+
+
+def nlte_sphere(npoints: int = 500_000, nside: int = 4, nlev: int = 10, nquads: int = 21, seed: int = 0,
+                r_in: float = 1.0e12, r_out: float = 1.0e14, nH2_in: float = 1.0e14, X_mol: float = 1.0e-6,
+                v_out: float = 15.0e3, v_turb: float = 150.0, nside_in: int = 4, nside_out: int = 16) -> RawModel:
+    """The non-LTE ALI workload: ``npoints`` interior points with number density
+    ~ r^-2 (uniform in r) between r_in and r_out, HEALPix boundary shells (CMB) at
+    r_in (nside_in) and r_out (nside_out), Delaunay neighbours, 12 nside^2 rays,
+    a 10-level linear rotor (B = 57.6 GHz, A_10 = 7.2e-8 /s, 28 amu) with one seeded
+    collision partner (H2), n_H2 = nH2_in (r_in/r)^2, X_mol = 1e-6, outward wind
+    ``v_out``, v_turb 150 m/s.  The workload does not fix the temperature; it is
+    T = 100 K (r/r_in)^-0.4, at least 10 K."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(r_in, r_out, size=npoints)
+    d = rng.normal(size=(npoints, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    inner = r_in * healpix.pix2vec_ring(nside_in)
+    outer = r_out * healpix.pix2vec_ring(nside_out)
+    position = np.concatenate([inner, r[:, None] * d, outer])
+    P = position.shape[0]
+    b2p = np.concatenate([np.arange(len(inner)), np.arange(P - len(outer), P)]).astype(np.uint32)
+    rs = np.linalg.norm(position, axis=1)
+    nH2 = nH2_in * (r_in / rs) ** 2
+    velocity = (v_out / CC) * position / rs[:, None]
+    temperature = np.maximum(100.0 * (rs / r_in) ** -0.4, 10.0)
+    nbs, n_nbs = delaunay_neighbors(position)
+    direction, weight = healpix.uniform_rays(12 * nside * nside)
+    ld = linear_rotor(nlev, 57.6e9, 7.2e-8, 28.0, num=0, collider=1, seed=seed)
+    roots, wts = quadrature(nquads)
+    abund = np.stack([X_mol * nH2, nH2], axis=1)
+    return RawModel(
+        name=f"nlte_sphere_{npoints}", dimension=3, position=position, velocity=velocity, neighbors=nbs,
+        n_neighbors=n_nbs, boundary2point=b2p, boundary_condition=np.full(len(b2p), BC_CMB, np.int32),
+        boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
+        abundance=abund, temperature=temperature, vturb2=np.full(P, (v_turb / CC) ** 2),
+        linedata=[ld], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
