@@ -143,6 +143,21 @@ int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, d
 int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, double* u_dev,
                                 double* lambda_diag_dev);
 
+/* Model::compute_radiation_field_shortchar_order_0 (src/model/model.cpp:313-349 ->
+ * Solver::solve_shortchar_order_0, src/solver/solver.tpp:150-235, :1564-1757).
+ * Host buffers (any may be NULL except J):
+ *   J            [P][F]
+ *   I            [nrays][P][F]    intensity along each ray (radiation.I)
+ *   u, v         [hnrays][P][F]   (I(rr) + I(ar))/2, (I(rr) - I(ar))/2
+ *   lambda_diag  [P][L]           summed diagonal ALO element
+ * Blocks until the results are in host memory. */
+int mgr_formal_solve_sc0(MgrModel* model, int precision, double* J, double* I, double* u, double* v,
+                         double* lambda_diag);
+
+/* Device-pointer variant of mgr_formal_solve_sc0; enqueued on the model's stream. */
+int mgr_formal_solve_sc0_device(MgrModel* model, int precision, double* J_dev, double* I_dev, double* u_dev,
+                                double* v_dev, double* lambda_diag_dev);
+
 /* Same as mgr_formal_solve_fo2_device, but the call allocates no device memory.
  * No reference counterpart: an addition of this library for callers that cannot
  * allocate at solve time.

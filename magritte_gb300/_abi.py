@@ -88,6 +88,9 @@ SIGNATURES = {
                                      _u32p, _u32p, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgr_formal_solve_sc0": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p, _f64p, _f64p]),
+    "mgr_formal_solve_sc0_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p]),
     "mgr_formal_solve_fo2_device_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint64)]),
@@ -214,6 +217,16 @@ class DeviceModel:
         _check(load().mgr_formal_solve_fo2(self.h, PRECISION[precision], _ptr(J, _f64p), _ptr(u, _f64p),
                                            _ptr(lam, _f64p)))
         return dict(J=J, u=u, lambda_diag=lam)
+
+    def formal_solve_sc0(self, precision="fp64", want_I=False, want_uv=False, want_lambda=True):
+        J = np.empty((self.P, self.F))
+        I = np.empty((2 * self.R, self.P, self.F)) if want_I else None
+        u = np.empty((self.R, self.P, self.F)) if want_uv else None
+        v = np.empty((self.R, self.P, self.F)) if want_uv else None
+        lam = np.empty((self.P, self.L)) if want_lambda else None
+        _check(load().mgr_formal_solve_sc0(self.h, PRECISION[precision], _ptr(J, _f64p), _ptr(I, _f64p),
+                                           _ptr(u, _f64p), _ptr(v, _f64p), _ptr(lam, _f64p)))
+        return dict(J=J, I=I, u=u, v=v, lambda_diag=lam)
 
     def formal_solve_fo2_device(self, precision, J_dev, u_dev=None, lam_dev=None):
         """Enqueue on the model stream with device pointers (ints); no synchronisation."""

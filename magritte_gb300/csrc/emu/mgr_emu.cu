@@ -187,6 +187,16 @@ LaneResult solve_any(const DevModel& m, const LaneCtx& c, const HalfSmem& bk, in
     }
 }
 
+template <int MODE>
+LaneResultSC solve_any_sc0(const DevModel& m, const LaneCtx& c, const HalfSmem& bk, int nb, const HalfSmem& fw,
+                           int nf) {
+    switch (m.approx) {
+        case APPROX_ONELINE: return solve_lane_sc0<MODE, APPROX_ONELINE>(m, m.sorted_line, c, bk, nb, fw, nf);
+        case APPROX_CLOSELINES: return solve_lane_sc0<MODE, APPROX_CLOSELINES>(m, m.sorted_line, c, bk, nb, fw, nf);
+        default: return solve_lane_sc0<MODE, APPROX_NONE>(m, m.sorted_line, c, bk, nb, fw, nf);
+    }
+}
+
 LaneResult solve(const DevModel& m, int precision, const LaneCtx& c, const HalfSmem& bk, int nb, const HalfSmem& fw,
                  int nf) {
     return precision == MGR_PRECISION_SPLIT ? solve_any<MODE_SPLIT>(m, c, bk, nb, fw, nf)
@@ -250,6 +260,69 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
                                              ? lambda_element(k[q], m.rayw[rr], LD[(size_t)rr * F + f])
                                              : 0.0;
                         s += e;
+                    }
+                lam[(size_t)o * L + l] = s;
+            }
+        }
+    }
+    return err ? MGR_ERR_TRACE : MGR_OK;
+}
+
+// Short characteristics: the kernel's per-lane code and the reduction order of
+// sc0_reduce_kernel.  J [P][F], lam [P][L] (may be NULL).
+extern "C" int mgr_emu_formal_solve_sc0(const MgrModelDesc* d, int precision, double* J, double* lam) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    const uint32_t P = m.P, L = m.L, F = m.F, R = m.hnrays, Q = m.Q;
+    int err = 0;
+#pragma omp parallel
+    {
+        HalfBuf b(kCap), fbuf(kCap);
+        HalfSmem bk = b.view(), fw = fbuf.view();
+        std::vector<double> U((size_t)R * F), XF((size_t)R * F), XB((size_t)R * F);
+#pragma omp for schedule(dynamic, 16)
+        for (long long oo = 0; oo < (long long)P; oo++) {
+            const uint32_t o = (uint32_t)oo;
+            bool ok = true;
+            for (uint32_t rr = 0; rr < R && ok; rr++) {
+                const int nb = trace_half_host(m, o, rr, kCap, bk);
+                const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
+                if (nb < 0 || nf < 0) {
+                    ok = false;
+                    break;
+                }
+                for (uint32_t f = 0; f < F; f++) {
+                    const LaneCtx c = lane_ctx(m, o, f);
+                    const LaneResultSC r = precision == MGR_PRECISION_SPLIT ? solve_any_sc0<MODE_SPLIT>(m, c, bk, nb, fw, nf)
+                                                                            : solve_any_sc0<MODE_FP64>(m, c, bk, nb, fw, nf);
+                    U[(size_t)rr * F + f] = r.solved ? 0.5 * (r.If + r.Ib) : r.If;
+                    XF[(size_t)rr * F + f] = r.Xf;
+                    XB[(size_t)rr * F + f] = r.Xb;
+                }
+            }
+            if (!ok) {
+#pragma omp atomic write
+                err = 1;
+                continue;
+            }
+            for (uint32_t f = 0; f < F; f++) {
+                double s = 0.0;
+                for (uint32_t rr = 0; rr < R; rr++) s += (m.rayw[rr] * 2.0) * U[(size_t)rr * F + f];
+                J[(size_t)o * F + f] = s;
+            }
+            if (!lam) continue;
+            for (uint32_t l = 0; l < L; l++) {
+                double s = 0.0;
+                for (uint32_t rr = 0; rr < R; rr++)
+                    for (uint32_t q = 0; q < Q; q++) {
+                        const uint32_t f = m.lq2f[(size_t)l * Q + q];
+                        if (f == 0xffffffffu || !m.in_line[f]) continue;
+                        const double xf = XF[(size_t)rr * F + f], xb = XB[(size_t)rr * F + f];
+                        if (xf == 0.0 && xb == 0.0) continue;
+                        const LambdaFactors k = lambda_factors(m, m.sorted_line, o, f);
+                        s += lambda_element_sc0(k, m.rayw[rr], xf);
+                        s += lambda_element_sc0(k, m.rayw[rr], xb);
                     }
                 lam[(size_t)o * L + l] = s;
             }

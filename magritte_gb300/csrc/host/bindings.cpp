@@ -227,7 +227,9 @@ PYBIND11_MODULE(core, m) {
     py::class_<Radiation>(m, "Radiation")
         .def_readwrite("frequencies", &Radiation::frequencies)
         .def_readwrite("J", &Radiation::J)
-        .def_readwrite("u", &Radiation::u);
+        .def_readwrite("u", &Radiation::u)
+        .def_readwrite("v", &Radiation::v)
+        .def_readwrite("I", &Radiation::I);
 
     py::class_<Model>(m, "Model")
         .def(py::init<>())
@@ -251,6 +253,8 @@ PYBIND11_MODULE(core, m) {
         .def("compute_LTE_level_populations", &Model::compute_LTE_level_populations)
         .def("set_dshift_max", &Model::set_dshift_max)
         .def("compute_radiation_field_feautrier_order_2", &Model::compute_radiation_field_feautrier_order_2,
+             py::call_guard<py::gil_scoped_release>())
+        .def("compute_radiation_field_shortchar_order_0", &Model::compute_radiation_field_shortchar_order_0,
              py::call_guard<py::gil_scoped_release>())
         .def("compute_Jeff", &Model::compute_Jeff, py::call_guard<py::gil_scoped_release>())
         .def("compute_level_populations", &Model::compute_level_populations, py::arg("use_Ng_acceleration"),

@@ -530,7 +530,13 @@ int Model::compute_radiation_field_feautrier_order_2() {
     std::vector<double> lam((size_t)P * L);
     check(mgr_formal_solve_fo2(dev, parameters.precision, radiation.J.data(),
                                parameters.store_u ? radiation.u.data() : nullptr, lam.data()));
-    // Lambda::Ls diagonal per species (lambda.tpp:79-89)
+    store_lambda(lam);
+    return 0;
+}
+
+// Lambda::Ls diagonal per species (lambda.tpp:79-89) from the per-line ALO [P][L].
+void Model::store_lambda(const std::vector<double>& lam) {
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v;
     for (Size l = 0; l < parameters.nlspecs_.v; l++) {
         LineProducingSpecies& ls = lines.lineProducingSpecies[l];
         const Size nrad = ls.linedata.nrad;
@@ -543,6 +549,21 @@ int Model::compute_radiation_field_feautrier_order_2() {
                 ls.lambda_has[(size_t)p * nrad + k] = v != 0.0;
             }
     }
+}
+
+// Model::compute_radiation_field_shortchar_order_0 (model.cpp:313-349)
+int Model::compute_radiation_field_shortchar_order_0() {
+    MgrModel* dev = upload();
+    const Size P = parameters.npoints_.v, F = parameters.nfreqs_, L = parameters.nlines_.v;
+    const Size R = parameters.hnrays_.v, N = parameters.nrays_.v;
+    radiation.J.resize({P, F});
+    radiation.I.resize({N, P, F});
+    radiation.u.resize({R, P, F});
+    radiation.v.resize({R, P, F});
+    std::vector<double> lam((size_t)P * L);
+    check(mgr_formal_solve_sc0(dev, parameters.precision, radiation.J.data(), radiation.I.data(), radiation.u.data(),
+                               radiation.v.data(), lam.data()));
+    store_lambda(lam);
     return 0;
 }
 

@@ -218,6 +218,8 @@ struct Radiation {
     Frequencies frequencies;
     Array<double> J;  // [P][F]
     Array<double> u;  // [hnrays][P][F]
+    Array<double> v;  // [hnrays][P][F] (short characteristics)
+    Array<double> I;  // [nrays][P][F]  (short characteristics)
 };
 
 class Model {
@@ -250,6 +252,7 @@ class Model {
     int compute_LTE_level_populations();
     int set_dshift_max();
     int compute_radiation_field_feautrier_order_2();
+    int compute_radiation_field_shortchar_order_0();
     int compute_Jeff();
     int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
 
@@ -267,6 +270,7 @@ class Model {
     uint64_t signature() const;
     void fill_desc(MgrModelDesc& d);
     void attach_species();
+    void store_lambda(const std::vector<double>& lam);
     void set_emissivity_and_opacity();
 };
 

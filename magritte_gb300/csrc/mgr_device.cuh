@@ -196,6 +196,12 @@ MGR_HD float erff_cr(float x) {
     return (float)erf((double)x);
 }
 
+// Single-precision exp and expm1 rounded once from double, for the short-
+// characteristics update, whose (S_c - S_n) cancellation amplifies ulp differences
+// between libm implementations to ~1e-4 in J.
+MGR_HD float expf_cr(float x) { return (float)exp((double)x); }
+MGR_HD float expm1f_cr(float x) { return (float)expm1((double)x); }
+
 // The same correctly rounded erff without FP64 in most of [1.5, 3.92): there
 // erf = 1 - erfc with erfc < 0.034, and an FP32 erfc (relative error of a few ulp of
 // erfc, far below one ulp of erf) decides the rounding of 1 - erfc exactly unless the

@@ -47,26 +47,6 @@ __global__ void size_rays_kernel(DevModel m, uint32_t* d_max, int* status) {
     if (lane == 0 && n > 0) atomicMax(d_max, (uint32_t)n);
 }
 
-// Shared-memory carve-up of one warp's two half-ray buffers.
-__device__ __forceinline__ void carve_halves(unsigned char* base, uint32_t cap, HalfSmem& bk, HalfSmem& fw) {
-    double* d = reinterpret_cast<double*>(base);
-    bk.shift = d;
-    bk.dZ = d + cap;
-    fw.shift = d + 2 * cap;
-    fw.dZ = d + 3 * cap;
-    uint32_t* u = reinterpret_cast<uint32_t*>(d + 4 * cap);
-    bk.ids = u;
-    fw.ids = u + cap;
-    bk.eid = u + 2 * cap;
-    fw.eid = u + 3 * cap;
-    float* f = reinterpret_cast<float*>(u + 4 * cap);
-    bk.dsh = f;
-    fw.dsh = f + cap;
-    bk.dzs = f + 2 * cap;
-    fw.dzs = f + 3 * cap;
-}
-
-__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 4 * 4 + 4 * 4); }
 
 // ---------------------------------------------------------------------------------
 // Interpolation count of every CSR edge (crt -> nxt) and line:

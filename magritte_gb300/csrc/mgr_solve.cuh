@@ -36,6 +36,27 @@ struct HalfSmem {
     uint32_t* eid;   // CSR edge of step s (index into the interpolation-count table)
 };
 
+// Shared-memory carve-up of one warp's two half-ray buffers.
+__device__ __forceinline__ void carve_halves(unsigned char* base, uint32_t cap, HalfSmem& bk, HalfSmem& fw) {
+    double* d = reinterpret_cast<double*>(base);
+    bk.shift = d;
+    bk.dZ = d + cap;
+    fw.shift = d + 2 * cap;
+    fw.dZ = d + 3 * cap;
+    uint32_t* u = reinterpret_cast<uint32_t*>(d + 4 * cap);
+    bk.ids = u;
+    fw.ids = u + cap;
+    bk.eid = u + 2 * cap;
+    fw.eid = u + 3 * cap;
+    float* f = reinterpret_cast<float*>(u + 4 * cap);
+    bk.dsh = f;
+    fw.dsh = f + cap;
+    bk.dzs = f + 2 * cap;
+    fw.dzs = f + 3 * cap;
+}
+
+__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 4 * 4 + 4 * 4); }
+
 // Order-preserving 64-bit key of a finite double (total order, -0 below +0; the
 // squared distances compared here are never -0).  Lets the warp's argmin run on the
 // integer pipe.
@@ -466,7 +487,7 @@ MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, floa
 // Same-wing erf difference on the FP64 mode's arguments (linefreq - nu shift) * avg_iw,
 // computed with the expressions of dtau_single_line_fp64 and the correctly rounded
 // erff.  Returns {erff(next) - erff(curr), next - curr}.
-__host__ __device__ __noinline__ float2 band_erf(const double* iw, uint32_t L, double linefreq, double freq,
+static __host__ __device__ __noinline__ float2 band_erf(const double* iw, uint32_t L, double linefreq, double freq,
                                                  const double* hshift, Elem lo, Elem hi, uint32_t l) {
     double lo_shift, lo_fac, hi_shift, hi_fac;
     const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr};
@@ -488,7 +509,7 @@ __host__ __device__ __noinline__ float2 band_erf(const double* iw, uint32_t L, d
 }
 
 // The reference's branch test |shift_hi - shift_lo| > min(dshift_max) on the FP64 shifts.
-__host__ __device__ __noinline__ bool large_shift_fp64(const double* hshift, const double* dshift_max, Elem lo,
+static __host__ __device__ __noinline__ bool large_shift_fp64(const double* hshift, const double* dshift_max, Elem lo,
                                                        Elem hi) {
     double lsh, lfac, hsh, hfac;
     const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr};
@@ -501,7 +522,7 @@ __host__ __device__ __noinline__ bool large_shift_fp64(const double* hshift, con
 
 // Elimination coefficients {dt_in/dt_out, dtau_avg dt_in} in FP64 for optical depths
 // whose ratio or product would leave the FP32 range.
-__host__ __device__ __noinline__ double2 elim_coeffs_fp64(float dt_out, float dt_in) {
+static __host__ __device__ __noinline__ double2 elim_coeffs_fp64(float dt_out, float dt_in) {
     const double o = dt_out, i = dt_in;
     double2 r;
     r.x = i / o;
@@ -900,6 +921,95 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     return res;
 }
 
+// Result of one lane's short-characteristics solve.
+struct LaneResultSC {
+    double If;   // intensity at the origin along rr (integrated over the backward half)
+    double Ib;   // along the antipode (integrated over the forward half)
+    double Xf;   // (expm1f(-dtau)/dtau + 1) of the last pair of each half, 0 if the half is empty
+    double Xb;
+    bool solved; // n_tot > 1
+};
+
+// Solver::solve_shortchar_order_0_ray_forward / _backward (solver.tpp:1564-1757):
+// each half is integrated from its outer end to the origin,
+//   I = e^{-dtau} I + expm1(-dtau)/dtau (S_c - S_n (1 + dtau)) + S_c - S_n,
+// with S_c / S_n the sources of the pair's outer / inner element (the line-integrated
+// ones for large Doppler jumps) and dtau >= min_dtau.  The reference evaluates the
+// exponentials in single precision; FP64 mode uses correctly rounded single-precision
+// values (expf_cr / expm1f_cr, as the oracle's matching mode) because the update's
+// cancellation makes J depend on their last ulp.  The pair evaluation is the
+// Feautrier path's.
+template <int MODE, int AP>
+__host__ __device__ LaneResultSC solve_lane_sc0(const DevModel& m, const double* sl, const LaneCtx& c,
+                                                const HalfSmem& bk, int nb, const HalfSmem& fw, int nf) {
+    using T = typename Real_<MODE>::T;
+    LaneResultSC res;
+    res.solved = (nb > 0) || (nf > 0);
+    res.Xf = 0.0;
+    res.Xb = 0.0;
+    if (!res.solved) {
+        res.If = res.Ib = boundary_intensity(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
+        return res;
+    }
+    const Elem cen = centre_elem(c.o);
+    const uint32_t l = c.l0;
+    EC<MODE> ec_cen{T(0), T(0), false};
+#pragma unroll 1
+    for (int side = 0; side < 2; side++) {
+        const HalfSmem& h = side ? fw : bk;
+        const int n = side ? nf : nb;
+        double I, X = 0.0;
+        if (n == 0) {
+            I = boundary_intensity(m, c.o, c.freq);  // nr[first] = o, shift 1
+        } else {
+            ElemIter it;
+            iter_begin<MODE>(m, h, c.o, l, n, it);
+            Elem outer;
+            iter_next<MODE>(m, h, c.o, l, it, outer);
+            EC<MODE> ec_out{T(0), T(0), false};
+            double bshift = outer.shift;
+            if constexpr (MODE == MODE_SPLIT) {
+                double fac;
+                elem_shift_fac(h, outer, bshift, fac);
+            }
+            I = boundary_intensity(m, outer.nr, c.freq * bshift);
+            double dtau = 0.0;
+            while (true) {
+                Elem inner;
+                const bool more = iter_next<MODE>(m, h, c.o, l, it, inner);
+                if (!more) inner = cen;
+                EC<MODE> ec_inn{T(0), T(0), false};
+                EC<MODE>& eci = more ? ec_inn : ec_cen;
+                PairOut<MODE> po;
+                eval_pair<MODE, AP>(m, sl, c, h, outer, inner, outer.dzin, outer.dzf, ec_out, eci, po);
+                dtau = (double)po.dtau;
+                if (m.min_dtau > dtau) dtau = m.min_dtau;
+                const double Sc = (double)po.Slo, Sn = (double)po.Shi;
+                const float x = (float)(-dtau);
+                const double ex = (MODE == MODE_FP64) ? (double)expf_cr(x) : (double)expf(x);
+                const double em = (MODE == MODE_FP64) ? (double)expm1f_cr(x) : (double)expm1f(x);
+                // evaluated as the reference's uncontracted expression: for tiny dtau the
+                // terms cancel to rounding level, so a fused multiply-add would change J
+                const double t = dsub_rn(Sc, dmul_rn(Sn, dadd_rn(1.0, dtau)));
+                I = dsub_rn(dadd_rn(dadd_rn(dmul_rn(ex, I), dmul_rn(em / dtau, t)), Sc), Sn);
+                if (!more) break;
+                outer = inner;
+                ec_out = ec_inn;
+            }
+            const float x = (float)(-dtau);
+            X = (double)((MODE == MODE_FP64) ? expm1f_cr(x) : expm1f(x)) / dtau + 1.0;
+        }
+        if (side) {
+            res.Ib = I;
+            res.Xb = X;
+        } else {
+            res.If = I;
+            res.Xf = X;
+        }
+    }
+    return res;
+}
+
 // update_Lambda, n_off_diag = 0 (solver.tpp:1760-1800): the ALO element of this
 // (origin, ray pair, frequency).
 struct LambdaFactors {
@@ -932,6 +1042,13 @@ MGR_HD LambdaFactors lambda_factors(const DevModel& m, const double* sl, uint32_
 MGR_HD double lambda_element(const LambdaFactors& k, double w_rr, double Ldiag) {
     const double constante = k.Aqw * (2.0 * w_rr);
     return constante * k.frq * k.phi * Ldiag * k.inverse_chi;
+}
+
+// Short characteristics: one direction's element (solver.tpp:1624-1638),
+// constante * freq * phi * (factor + 1) * inverse_chi with constante = line_A * weight * w_rr.
+MGR_HD double lambda_element_sc0(const LambdaFactors& k, double w_rr, double X) {
+    const double constante = k.Aqw * w_rr;
+    return constante * k.frq * k.phi * X * k.inverse_chi;
 }
 
 }  // namespace mgr

@@ -420,6 +420,9 @@ static void get_eta_and_chi_interpolated(const OrcModel* m, uint32_t p1, uint32_
 static int g_erf_mode = 0;
 void orc_set_erf_mode(int mode) { g_erf_mode = mode; }
 static inline float orc_erff(float x) { return g_erf_mode ? (float)erf((double)x) : erff(x); }
+/* Mode 1 also rounds the short-characteristics update's expf / expm1f once from double. */
+static inline float orc_expf_sc(float x) { return g_erf_mode ? (float)exp((double)x) : expf(x); }
+static inline float orc_expm1f_sc(float x) { return g_erf_mode ? (float)expm1((double)x) : expm1f(x); }
 
 /* Solver::compute_dtau_single_line (solver.tpp:2374-2455). */
 static double compute_dtau_single_line(const OrcModel* m, uint32_t curridx, uint32_t nextidx,
@@ -735,7 +738,7 @@ int orc_formal_solve_fo2_range(const OrcModel* m, uint32_t rr_begin, uint32_t rr
 /* ------------------------------------------------------------------ */
 static double sc0_lambda(const OrcModel* m, uint32_t o, uint32_t r, uint32_t f, double dtau, int have_dtau) {
     if (!have_dtau) return 0.0; /* reference reads an unset dtau here; contribution taken as 0 */
-    const double factor     = (double)expm1f((float)(-dtau)) / dtau;
+    const double factor     = (double)orc_expm1f_sc((float)(-dtau)) / dtau;
     const uint32_t ls       = m->corr_lspec[f];
     const uint32_t k        = m->corr_k[f];
     const uint32_t z        = m->corr_z[f];
@@ -766,8 +769,8 @@ static double sc0_forward(const OrcModel* m, Buf* b, uint32_t o, uint32_t r, uin
                             b->dZ[idx - 1], b->interp_factor[idx - 1], b->interp_factor[idx], &cco, &dtau,
                             &chi_c, &chi_n, &source_c, &source_n);
         dtau = (m->min_dtau > dtau) ? m->min_dtau : dtau;
-        I    = (double)expf((float)(-dtau)) * I
-            + (double)expm1f((float)(-dtau)) / dtau * (source_c - source_n * (1.0 + dtau)) + source_c - source_n;
+        I    = (double)orc_expf_sc((float)(-dtau)) * I
+            + (double)orc_expm1f_sc((float)(-dtau)) / dtau * (source_c - source_n * (1.0 + dtau)) + source_c - source_n;
         have = 1;
     }
     *L = sc0_lambda(m, o, r, f, dtau, have);
@@ -789,8 +792,8 @@ static double sc0_backward(const OrcModel* m, Buf* b, uint32_t o, uint32_t r, ui
                             b->dZ[ip1 - 1], b->interp_factor[ip1], b->interp_factor[ip1 - 1], &cco, &dtau,
                             &chi_c, &chi_n, &source_c, &source_n);
         dtau = (m->min_dtau > dtau) ? m->min_dtau : dtau;
-        I    = (double)expf((float)(-dtau)) * I
-            + (double)expm1f((float)(-dtau)) / dtau * (source_c - source_n * (1.0 + dtau)) + source_c - source_n;
+        I    = (double)orc_expf_sc((float)(-dtau)) * I
+            + (double)orc_expm1f_sc((float)(-dtau)) / dtau * (source_c - source_n * (1.0 + dtau)) + source_c - source_n;
         have = 1;
     }
     *L = sc0_lambda(m, o, r, f, dtau, have);

@@ -86,8 +86,10 @@ typedef struct {
     double*   dZ;
 } OrcRay;
 
-/* erff of the line-integrated optical depth: 0 = libm erff (the reference, default),
- * 1 = correctly rounded erff (float)erf((double)x) (what the GPU FP64 mode uses). */
+/* Single-precision functions whose last ulp the results depend on: 0 = libm, as the
+ * reference (default); 1 = rounded once from double, as the GPU FP64 mode: erff of the
+ * line-integrated optical depth, (float)erf((double)x), and expf / expm1f of the
+ * short-characteristics update, (float)exp((double)x) / (float)expm1((double)x). */
 void orc_set_erf_mode(int mode);
 
 /* Maximum ray-pair length over all (rr, o), reference Solver::get_ray_lengths_max

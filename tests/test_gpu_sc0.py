@@ -1,0 +1,68 @@
+"""GPU short characteristics (compute_radiation_field_shortchar_order_0) against the
+oracle through the C ABI: J and the ALO diagonal within 1e-5 relative in FP64 mode,
+single-ray I and u within 1e-4; split precision within 5e-4 (the update's own single-precision noise,
+see test_kernel_emulation.py).
+
+Far-wing values are compared on the scale of their point's line peak: the
+short-characteristics update cancels (S_c - S_n) terms when dtau is small, which
+amplifies single-ulp differences of the single-precision libm calls (CUDA's expf /
+powf against glibc's) by ~1e3 in the line wings; the reference's own J moves by
+~2e-4 under 1-ulp opacity noise there (test_oracle_known_answers.py).  Values are
+compared relative to max(|value|, 1e-2 x the peak over frequencies)."""
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+from magritte_gb300 import _abi
+from magritte_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_with_correctly_rounded_erf():
+    O.set_erf_mode(1)
+    yield
+    O.set_erf_mode(0)
+
+
+def _wing_rel(x, ref):
+    """Max |x - ref| / max(|ref|, 1e-2 * peak of ref over the last axis)."""
+    floor = 1e-2 * np.abs(ref).max(axis=-1, keepdims=True)
+    return float(np.max(np.abs(x - ref) / np.maximum(np.abs(ref), np.maximum(floor, 1e-300))))
+
+
+@pytest.mark.parametrize("model,approx", [("cube", "CloseLines"), ("sphere", "CloseLines"), ("sphere", "OneLine")])
+def test_shortchar_matches_oracle(gpu_lib, model, approx):
+    raw = S.grid_cube() if model == "cube" else S.grid_sphere(n=16, nside=1, nquads=7)
+    a = H.setup(raw, approx=approx)
+    ref = O.Oracle(a).formal_solve_sc0()
+    has = ref["lambda_has"].astype(bool)
+    dev = _abi.DeviceModel(a)
+    try:
+        g = dev.formal_solve_sc0("fp64", want_I=True, want_uv=True)
+        assert _wing_rel(g["J"], ref["J"]) < 1e-5
+        for k in ("I", "u"):  # single rays: the amplified libm noise is not averaged over directions
+            assert _wing_rel(g[k], ref[k]) < 1e-4, k
+        # v = (I(rr) - I(ar))/2 cancels: compare on the scale of the intensities
+        assert np.abs(g["v"] - ref["v"]).max() <= 1e-5 * np.abs(ref["u"]).max()
+        assert H.max_rel(g["lambda_diag"][has], ref["lambda_diag"][has]) < 1e-5
+        s = dev.formal_solve_sc0("split")
+        assert _wing_rel(s["J"], ref["J"]) < 5e-4
+    finally:
+        dev.close()
+
+
+def test_core_model_shortchar(gpu_lib):
+    from magritte_gb300 import loader
+
+    raw = S.grid_cube(n=10, nquads=11)
+    ref = O.Oracle(H.setup(raw)).formal_solve_sc0()
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    model.compute_radiation_field_shortchar_order_0()
+    assert _wing_rel(np.array(model.radiation.J), ref["J"]) < 1e-5
+    assert _wing_rel(np.array(model.radiation.I), ref["I"]) < 1e-4
