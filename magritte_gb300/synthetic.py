@@ -403,3 +403,38 @@ def nlte_sphere(npoints: int = 500_000, nside: int = 4, nlev: int = 10, nquads: 
         boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
         abundance=abund, temperature=temperature, vturb2=np.full(P, (v_turb / CC) ** 2),
         linedata=[ld], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
+
+
+def velocity_gradient_shells(nshells: int = 10, dx: float = 1.0e4, dv: float = 2.5e2, nTT: float = 1.0e8,
+                             nH2: float = 1.0e12, temp: float = 45.0, turb: float = 0.0, nside: int = 1,
+                             nquads: int = 10, seed: int = 0) -> RawModel:
+    """The constant-velocity-gradient imaging benchmark in 3D (the reference's
+    tests/benchmarks/analytic/constant_velocity_gradient_3D_new_imager.py): HEALPix
+    shells (nside 2 + s) at radii dx, 2 dx, .., nshells dx, each randomly rotated
+    (seeded), radial velocity s dv at shell s, Delaunay neighbours, inner and outer
+    shells as CMB boundaries, the 2-level 'test' species in LTE at ``temp``."""
+    from scipy.spatial.transform import Rotation
+
+    rng = np.random.default_rng(seed)
+    r_shell = np.linspace(dx, nshells * dx, nshells, endpoint=True)
+    n_in_shell = [healpix.nside2npix(2 + s) for s in range(nshells)]
+    pos_parts, vel_parts = [], []
+    for s, (r, n) in enumerate(zip(r_shell, n_in_shell)):
+        pos = r * healpix.pix2vec_ring(2 + s)
+        pos = Rotation.random(random_state=rng).apply(pos)
+        pos_parts.append(pos)
+        vel_parts.append((r / dx) * (dv / CC) * pos / r)
+    position = np.concatenate(pos_parts)
+    velocity = np.concatenate(vel_parts)
+    P = position.shape[0]
+    nbs, n_nbs = delaunay_neighbors(position)
+    b2p = np.concatenate([np.arange(n_in_shell[0]), np.arange(P - n_in_shell[-1], P)]).astype(np.uint32)
+    direction, weight = healpix.uniform_rays(12 * nside * nside)
+    roots, wts = quadrature(nquads)
+    abund = np.array([[nTT, nH2, 0.0] for _ in range(P)])
+    return RawModel(
+        name="constant_velocity_gradient_3D", dimension=3, position=position, velocity=velocity, neighbors=nbs,
+        n_neighbors=n_nbs, boundary2point=b2p, boundary_condition=np.full(len(b2p), BC_CMB, np.int32),
+        boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
+        abundance=abund, temperature=np.full(P, temp), vturb2=np.full(P, (turb / CC) ** 2),
+        linedata=[lamda_test_species()], quad_roots=[roots], quad_weights=[wts], nquads=nquads)

@@ -926,3 +926,207 @@ int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads) {
     }
     return err_any ? -2 : 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* New imager (solver.tpp:576-627, :808-897; image.cpp:221-398;          */
+/* geometry.tpp:55-106, :167-193, :310-367)                              */
+/* ------------------------------------------------------------------ */
+
+/* Geometry::get_closest_bdy_point_in_custom_raydir (geometry.tpp:346-367).  The reference
+ * starts from point2boundary[0] read as a point index; where that is not a point index
+ * (point 0 interior), the first boundary point is used instead. */
+static uint32_t closest_bdy_point_in_raydir(const OrcModel* m, const uint32_t* b2p, const double* d) {
+    uint32_t best = m->point2boundary[0];
+    if (best >= m->npoints) best = b2p[0];
+    double pmin = dot3(m->position[3 * best], m->position[3 * best + 1], m->position[3 * best + 2], d);
+    for (uint32_t b = 1; b < m->nboundary; b++) {
+        const uint32_t p = b2p[b];
+        const double pd  = dot3(m->position[3 * p], m->position[3 * p + 1], m->position[3 * p + 2], d);
+        if (pd < pmin) {
+            best = p;
+            pmin = pd;
+        }
+    }
+    return best;
+}
+
+/* Geometry::get_boundary_point_closer_to_custom_ray (geometry.tpp:310-341). */
+static uint32_t bdy_point_closer(const OrcModel* m, const double* origin, const double* d, uint32_t crt) {
+    const double Rx = m->position[3 * crt] - origin[0], Ry = m->position[3 * crt + 1] - origin[1],
+                 Rz = m->position[3 * crt + 2] - origin[2];
+    const double Zc = dot3(Rx, Ry, Rz, d);
+    double dmin2    = (Rx * Rx + Ry * Ry + Rz * Rz) - Zc * Zc;
+    uint32_t next   = crt;
+    const uint32_t n_nbs = m->n_neighbors[crt], cum = m->cum_n_neighbors[crt];
+    for (uint32_t i = 0; i < n_nbs; i++) {
+        const uint32_t n = m->neighbors[cum + i];
+        if (!not_on_boundary(m, n)) {
+            const double Nx = m->position[3 * n] - origin[0], Ny = m->position[3 * n + 1] - origin[1],
+                         Nz = m->position[3 * n + 2] - origin[2];
+            const double Zn  = dot3(Nx, Ny, Nz, d);
+            const double d2  = (Nx * Nx + Ny * Ny + Nz * Nz) - Zn * Zn;
+            if (d2 < dmin2) {
+                dmin2 = d2;
+                next  = n;
+            }
+        }
+    }
+    return next;
+}
+
+/* Solver::trace_ray_imaging (solver.tpp:841-897), increment -1, Rest frame with a
+ * motionless origin: shift = 1 + v . raydir. */
+static int64_t trace_imaging(const OrcModel* m, Buf* b, const double* origin, uint32_t start, const double* d,
+                             double* Z, int64_t id1, int64_t id2, const double* center, int* err) {
+    double dZ = 0.0;
+    uint32_t crt = start;
+    uint32_t nxt = get_next(m, origin, d, start, Z, &dZ);
+    int accessed = 0;
+    const int64_t original_id1 = id1;
+#define SHIFT_REST(c) (1.0 + dot3(m->velocity[3 * (c)], m->velocity[3 * (c) + 1], m->velocity[3 * (c) + 2], d))
+    if (valid_point(m, nxt)) {
+        double shift_crt = SHIFT_REST(crt);
+        double shift_nxt = SHIFT_REST(nxt);
+        set_data(m, b, UINT32_MAX, crt, nxt, shift_crt, shift_nxt, dZ, -1, &id1, &id2, err);
+        while (!*err && (not_on_boundary(m, nxt) ||
+                         dot3(m->position[3 * nxt] - center[0], m->position[3 * nxt + 1] - center[1],
+                              m->position[3 * nxt + 2] - center[2], d) < 0)) {
+            crt       = nxt;
+            shift_crt = shift_nxt;
+            if (not_on_boundary(m, nxt)) accessed = 1;
+            nxt = get_next(m, origin, d, nxt, Z, &dZ);
+            if (!valid_point(m, nxt)) break;
+            shift_nxt = SHIFT_REST(nxt);
+            set_data(m, b, UINT32_MAX, crt, nxt, shift_crt, shift_nxt, dZ, -1, &id1, &id2, err);
+        }
+    }
+#undef SHIFT_REST
+    if (!accessed) return original_id1; /* no spherical symmetry here */
+    return id1;
+}
+
+int orc_image_new(const OrcModel* m, const double* raydir_in, uint32_t nx, uint32_t ny, double* I, double* ImX,
+                  double* ImY, int nthreads) {
+    const uint32_t P = m->npoints, F = m->nfreqs;
+    const double n2 = raydir_in[0] * raydir_in[0] + raydir_in[1] * raydir_in[1] + raydir_in[2] * raydir_in[2];
+    if (n2 == 0.0) return -1;
+    const double inv = 1 / sqrt(n2);
+    const double d[3] = {raydir_in[0] * inv, raydir_in[1] * inv, raydir_in[2] * inv};
+    /* Image::set_coordinates_projection_surface (image.cpp:221-366), 3D */
+    const double rx = d[0], ry = d[1], rz = d[2];
+    const double den = sqrt(rx * rx + ry * ry), iden = 1.0 / den;
+    const double ix = ry * iden, iy = -rx * iden, jx = rx * rz * iden, jy = ry * rz * iden, jz = -den;
+    /* boundary2point from point2boundary */
+    uint32_t* b2p = (uint32_t*)malloc(sizeof(uint32_t) * (m->nboundary ? m->nboundary : 1));
+    if (!b2p) return -3;
+    for (uint32_t p = 0; p < P; p++)
+        if (m->point2boundary[p] < m->nboundary) b2p[m->point2boundary[p]] = p;
+    double max_x = -DBL_MAX, max_y = -DBL_MAX, min_x = DBL_MAX, min_y = DBL_MAX;
+    for (uint32_t bi = 0; bi < m->nboundary; bi++) {
+        const uint32_t p = b2p[bi];
+        const double* x = m->position + 3 * p;
+        double X, Y;
+        if (den >= 1.0e-9) {
+            X = ix * x[0] + iy * x[1];
+            Y = jx * x[0] + jy * x[1] + jz * x[2];
+        } else {
+            X = x[0];
+            Y = x[1];
+        }
+        if (X < min_x) min_x = X;
+        if (X > max_x) max_x = X;
+        if (Y < min_y) min_y = Y;
+        if (Y > max_y) max_y = Y;
+    }
+    const uint32_t cbp = closest_bdy_point_in_raydir(m, b2p, d);
+    free(b2p);
+    const double dist  = dot3(m->position[3 * cbp], m->position[3 * cbp + 1], m->position[3 * cbp + 2], d);
+    const double scp[3] = {d[0] * dist, d[1] * dist, d[2] * dist};
+    const double deltax = (max_x - min_x) / nx, deltay = (max_y - min_y) / ny;
+    for (uint32_t xi = 0; xi < nx; xi++)
+        for (uint32_t yi = 0; yi < ny; yi++) {
+            ImX[yi + (size_t)ny * xi] = min_x + deltax / 2.0 + xi * deltax;
+            ImY[yi + (size_t)ny * xi] = min_y + deltay / 2.0 + yi * deltay;
+        }
+    /* Points::center: middle of the bounding box (points.cpp:30-42) */
+    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    for (uint32_t p = 0; p < P; p++)
+        for (int k = 0; k < 3; k++) {
+            const double v = m->position[3 * p + k];
+            if (v < lo[k]) lo[k] = v;
+            if (v > hi[k]) hi[k] = v;
+        }
+    const double center[3] = {(lo[0] + hi[0]) / 2, (lo[1] + hi[1]) / 2, (lo[2] + hi[2]) / 2};
+    const uint32_t npix = nx * ny;
+    int err_any = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+    {
+        uint32_t length = 2 * 4096 + 1;
+        Buf b;
+        int bad = buf_init(&b, length);
+#pragma omp for schedule(dynamic, 8)
+        for (int64_t pp = 0; pp < (int64_t)npix; pp++) {
+            if (bad) continue;
+            const double X = ImX[pp], Y = ImY[pp];
+            double origin[3];
+            if (den >= 1.0e-9) {
+                origin[0] = X * ix + Y * jx + scp[0];
+                origin[1] = X * iy + Y * jy + scp[1];
+                origin[2] = Y * jz + scp[2];
+            } else {
+                origin[0] = X + scp[0];
+                origin[1] = Y + scp[1];
+                origin[2] = 0.0 + scp[2];
+            }
+            /* trace_ray_imaging_get_start (solver.tpp:808-830) */
+            uint32_t start = cbp;
+            while (1) {
+                const uint32_t nxt = bdy_point_closer(m, origin, d, start);
+                if (nxt == start) break;
+                start = nxt;
+            }
+            int err = 0;
+            int64_t first = 0;
+            while (1) {
+                double Z = dot3(m->position[3 * start] - origin[0], m->position[3 * start + 1] - origin[1],
+                                m->position[3 * start + 2] - origin[2], d);
+                const uint32_t c = b.centre;
+                b.nr[c]    = start;
+                b.shift[c] = 1.0 + dot3(m->velocity[3 * start], m->velocity[3 * start + 1],
+                                        m->velocity[3 * start + 2], d);
+                err   = 0;
+                first = trace_imaging(m, &b, origin, start, d, &Z, (int64_t)c - 1, (int64_t)c - 1, center, &err) + 1;
+                if (err != 1) break;
+                /* buffer too short: grow it and trace again */
+                buf_free(&b);
+                length = 2 * length + 1;
+                if (buf_init(&b, length) != 0) {
+                    bad = 1;
+                    break;
+                }
+            }
+            if (bad || err) {
+#pragma omp atomic write
+                err_any = 1;
+                continue;
+            }
+            b.first = (uint32_t)first;
+            b.last  = b.centre;
+            b.n_tot = b.last + 1 - b.first;
+            for (uint32_t f = 0; f < F; f++) {
+                const double nu_f = m->nu[(size_t)start * F + f];
+                if (b.n_tot > 1) {
+                    solve_feautrier_order_2(m, &b, start, f, 0);
+                    I[(size_t)pp * F + f] = 2.0 * b.Su[b.last] - boundary_intensity(m, b.nr[b.last], nu_f);
+                } else {
+                    I[(size_t)pp * F + f] = boundary_intensity(m, start, nu_f);
+                }
+            }
+        }
+        buf_free(&b);
+    }
+    return err_any ? -2 : 0;
+}

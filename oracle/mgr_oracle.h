@@ -123,6 +123,13 @@ int orc_formal_solve_sc0(const OrcModel* m, double* J, double* I, double* u, dou
  * Rest-frame shifts.  I [P][F]. */
 int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads);
 
+/* New imager, Model::compute_image_new(raydir, nx, ny) (model.cpp:989-1013 ->
+ * Solver::image_feautrier_order_2_new_imager, solver.tpp:576-627): pixel rays from a
+ * projection plane outside the model.  I [nx*ny][F] (pixel index y + ny*x), ImX, ImY
+ * [nx*ny].  Returns 0, < 0 on failure. */
+int orc_image_new(const OrcModel* m, const double* raydir, uint32_t nx, uint32_t ny, double* I, double* ImX,
+                  double* ImY, int nthreads);
+
 /* ------------------------------------------------------------------ */
 /* ALI level populations (mgr_oracle_ali.c)                             */
 /* ------------------------------------------------------------------ */

@@ -55,9 +55,11 @@ def lib():
 def reference_setup(raw, approx="CloseLines", max_width_fraction=0.35, min_opacity=1.0e-26,
                     min_line_opacity=1.0e-13, min_line_emissivity=1.0e-50, min_dtau=1.0e-15,
                     max_interpolation_diff=1.4, max_distance_opacity_contribution=10.0,
-                    populations=None):
+                    populations=None, image_freqs=None):
     """Arrays of the OrcModel struct for a ``magritte_gb300.synthetic.RawModel``.
-    ``populations`` (list per species of [P, nlev]) overrides the LTE populations."""
+    ``populations`` (list per species of [P, nlev]) overrides the LTE populations.
+    ``image_freqs = (nu_min, nu_max, n)`` selects the imaging spectral discretisation
+    (model.cpp:229-275): n evenly spaced frequencies, the same at every point."""
     P = raw.npoints
     nrays = raw.nrays
     Q = raw.nquads
@@ -97,6 +99,18 @@ def reference_setup(raw, approx="CloseLines", max_width_fraction=0.35, min_opaci
                 corr_lspec[f] = l
                 corr_k[f] = k
                 corr_z[f] = z
+
+    if image_freqs is not None:
+        nu_min, nu_max, n = image_freqs
+        F = int(n)
+        dnu = (nu_max - nu_min) / (F - 1) if F > 1 else 0.0
+        row = np.array([nu_min + f * dnu for f in range(F)]) if F > 1 else np.array([(nu_min + nu_max) / 2.0])
+        nu = np.tile(row, (P, 1))
+        corr_line = np.zeros(F, np.uint32)  # not set by the reference for this discretisation
+        corr_lspec = np.full(F, F, np.uint32)
+        corr_k = np.full(F, F, np.uint32)
+        corr_z = np.full(F, F, np.uint32)
+        in_line = np.zeros(F, np.uint8)
 
     # LTE populations (lineProducingSpecies.tpp:52-75) and emissivity/opacity (:23-44)
     emissivity = np.zeros((P, L))
@@ -296,6 +310,21 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle short-char solve failed ({rc})")
         return dict(J=J, I=I, u=u, v=v, lambda_diag=lam, lambda_has=has)
+
+    def image_new(self, raydir, nx, ny, nthreads=0):
+        P, F = self.a["npoints"], self.a["nfreqs"]
+        I = np.zeros((nx * ny, F))
+        X = np.zeros(nx * ny)
+        Y = np.zeros(nx * ny)
+        d = np.ascontiguousarray(raydir, np.float64)
+        l = lib()
+        l.orc_image_new.restype = C.c_int
+        l.orc_image_new.argtypes = [C.POINTER(OrcModel), _f64p, C.c_uint32, C.c_uint32, _f64p, _f64p, _f64p, C.c_int]
+        rc = l.orc_image_new(C.byref(self.m), _ptr(d, _f64p), nx, ny, _ptr(I, _f64p), _ptr(X, _f64p),
+                             _ptr(Y, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle new imager failed ({rc})")
+        return dict(I=I, ImX=X, ImY=Y)
 
     def image_fo2(self, rr, nthreads=0):
         P, F = self.a["npoints"], self.a["nfreqs"]
