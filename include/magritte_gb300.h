@@ -158,6 +158,21 @@ int mgr_formal_solve_sc0(MgrModel* model, int precision, double* J, double* I, d
 int mgr_formal_solve_sc0_device(MgrModel* model, int precision, double* J_dev, double* I_dev, double* u_dev,
                                 double* v_dev, double* lambda_diag_dev);
 
+/* Model::compute_image(ray_nr) (src/model/model.cpp:957-975 ->
+ * Solver::image_feautrier_order_2(model, rr), src/solver/solver.tpp:542-574): the
+ * rest-frame image along ray ray_nr with one ray per model point.
+ *   I [P][F], ImX / ImY [P] image-plane coordinates (Image, image.cpp:154-219; may be
+ *   NULL).  CloseLines or None approximation (OneLine is rejected, as the reference
+ *   does).  Blocks. */
+int mgr_image(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY);
+
+/* Model::compute_image_new(raydir, nx, ny) (model.cpp:989-1013 ->
+ * Solver::image_feautrier_order_2_new_imager, solver.tpp:576-627): nx * ny pixel rays
+ * from a projection plane outside the model along the (normalised) direction raydir.
+ *   I [nx*ny][F], ImX / ImY [nx*ny], pixel index y + ny*x (image.cpp:221-366).  Blocks. */
+int mgr_image_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny, double* I,
+                  double* ImX, double* ImY);
+
 /* Same as mgr_formal_solve_fo2_device, but the call allocates no device memory.
  * No reference counterpart: an addition of this library for callers that cannot
  * allocate at solve time.

@@ -91,6 +91,8 @@ SIGNATURES = {
     "mgr_formal_solve_sc0": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_sc0_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_void_p]),
+    "mgr_image": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, _f64p, _f64p, _f64p]),
+    "mgr_image_new": (C.c_int, [C.c_void_p, C.c_int, _f64p, C.c_uint32, C.c_uint32, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2_device_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint64)]),
@@ -217,6 +219,21 @@ class DeviceModel:
         _check(load().mgr_formal_solve_fo2(self.h, PRECISION[precision], _ptr(J, _f64p), _ptr(u, _f64p),
                                            _ptr(lam, _f64p)))
         return dict(J=J, u=u, lambda_diag=lam)
+
+    def image(self, ray_nr, precision="fp64"):
+        I = np.empty((self.P, self.F))
+        X, Y = np.empty(self.P), np.empty(self.P)
+        _check(load().mgr_image(self.h, PRECISION[precision], ray_nr, _ptr(I, _f64p), _ptr(X, _f64p),
+                                _ptr(Y, _f64p)))
+        return dict(I=I, ImX=X, ImY=Y)
+
+    def image_new(self, raydir, nx, ny, precision="fp64"):
+        I = np.empty((nx * ny, self.F))
+        X, Y = np.empty(nx * ny), np.empty(nx * ny)
+        d = np.ascontiguousarray(raydir, np.float64)
+        _check(load().mgr_image_new(self.h, PRECISION[precision], _ptr(d, _f64p), nx, ny, _ptr(I, _f64p),
+                                    _ptr(X, _f64p), _ptr(Y, _f64p)))
+        return dict(I=I, ImX=X, ImY=Y)
 
     def formal_solve_sc0(self, precision="fp64", want_I=False, want_uv=False, want_lambda=True):
         J = np.empty((self.P, self.F))

@@ -17,7 +17,7 @@ using namespace mgr;
 namespace {
 
 // Sequential restatement of trace_half (same arithmetic, neighbour order, strict <).
-int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem h) {
+int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem h, int frame = 0) {
     const double* d = m.raydir + 3 * r;
     const double4_32a po = m.pos[o];
     double Z = 0.0;
@@ -52,7 +52,7 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
         h.ids[count] = nxt;
         h.eid[count] = cum + besti;
         h.dZ[count] = dZl;
-        const double s = shift_comoving(m, o, nxt, d);
+        const double s = frame ? shift_rest(m, r, nxt, d) : shift_comoving(m, o, nxt, d);
         h.shift[count] = s;
         h.dsh[count] = (float)dsub_rn(s, 1.0);
         h.dzs[count] = (float)dZl * m.dz_scale;
@@ -73,7 +73,7 @@ struct EmuModel {
     std::vector<double4_32a> pos, vel, edge;
     std::vector<double> ub, Sp;
     std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f;
-    std::vector<uint16_t> nint;
+    std::vector<uint16_t> nint, nint_all;
     std::vector<uint32_t> lq2f;
     DevModel m{};
 };
@@ -155,6 +155,14 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
                 x.nint[e * L + l] = (uint16_t)(v > 0xffffu ? 0xffffu : v);
             }
     m.nint = x.nint.data();
+    x.nint_all.resize(E ? E : 1);
+    for (uint32_t p = 0; p < P; p++)
+        for (uint32_t k = 0; k < d->n_neighbors[p]; k++) {
+            const size_t e = (size_t)d->cum_n_neighbors[p] + k;
+            const uint32_t v = n_interp_all_lines(m, p, d->neighbors[e]);
+            x.nint_all[e] = (uint16_t)(v > 0xffffu ? 0xffffu : v);
+        }
+    m.nint_all = x.nint_all.data();
 }
 
 struct HalfBuf {
@@ -325,6 +333,50 @@ extern "C" int mgr_emu_formal_solve_sc0(const MgrModelDesc* d, int precision, do
                         s += lambda_element_sc0(k, m.rayw[rr], xb);
                     }
                 lam[(size_t)o * L + l] = s;
+            }
+        }
+    }
+    return err ? MGR_ERR_TRACE : MGR_OK;
+}
+
+// The old imager's per-ray code (image_lane with rest-frame traces), I [P][F].
+extern "C" int mgr_emu_image(const MgrModelDesc* d, int precision, uint32_t rr, double* I) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    const uint32_t P = m.P, F = m.F;
+    int err = 0;
+#pragma omp parallel
+    {
+        HalfBuf b(kCap), fbuf(kCap);
+        HalfSmem bk = b.view(), fw = fbuf.view();
+#pragma omp for schedule(dynamic, 16)
+        for (long long oo = 0; oo < (long long)P; oo++) {
+            const uint32_t o = (uint32_t)oo;
+            const double* dd = m.raydir + 3 * rr;
+            const uint32_t ar = m.antipod[rr];
+            const double shb = shift_rest(m, rr, o, dd);
+            const double shf = shift_rest(m, ar, o, m.raydir + 3 * ar);
+            bk.shift0 = shb;
+            fw.shift0 = shf;
+            bk.dsh0 = (float)(shb - 1.0);
+            fw.dsh0 = (float)(shf - 1.0);
+            bk.cshift = fw.cshift = shb;
+            const int nb = trace_half_host(m, o, rr, kCap, bk, 1);
+            const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw, 1);
+            if (nb < 0 || nf < 0) {
+#pragma omp atomic write
+                err = 1;
+                continue;
+            }
+            for (uint32_t f = 0; f < F; f++) {
+                const LaneCtx c = lane_ctx(m, o, f);
+                I[(size_t)o * F + f] =
+                    precision == MGR_PRECISION_SPLIT
+                        ? (m.approx == APPROX_NONE ? image_lane<MODE_SPLIT, APPROX_NONE>(m, m.sorted_line, c, bk, nb, fw, nf)
+                                                   : image_lane<MODE_SPLIT, APPROX_CLOSELINES>(m, m.sorted_line, c, bk, nb, fw, nf))
+                        : (m.approx == APPROX_NONE ? image_lane<MODE_FP64, APPROX_NONE>(m, m.sorted_line, c, bk, nb, fw, nf)
+                                                   : image_lane<MODE_FP64, APPROX_CLOSELINES>(m, m.sorted_line, c, bk, nb, fw, nf));
             }
         }
     }

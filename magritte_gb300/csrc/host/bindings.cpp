@@ -231,6 +231,16 @@ PYBIND11_MODULE(core, m) {
         .def_readwrite("v", &Radiation::v)
         .def_readwrite("I", &Radiation::I);
 
+    py::class_<Image>(m, "Image")
+        .def_readonly("imagePointPosition", &Image::imagePointPosition)
+        .def_readonly("ray_nr", &Image::ray_nr)
+        .def_readwrite("ray_direction", &Image::ray_direction)
+        .def_readwrite("ImX", &Image::ImX)
+        .def_readwrite("ImY", &Image::ImY)
+        .def_readwrite("I", &Image::I)
+        .def_readwrite("freqs", &Image::freqs)
+        .def_readonly("nfreqs", &Image::nfreqs);
+
     py::class_<Model>(m, "Model")
         .def(py::init<>())
         .def_readwrite("parameters", &Model::parameters)
@@ -257,6 +267,14 @@ PYBIND11_MODULE(core, m) {
         .def("compute_radiation_field_shortchar_order_0", &Model::compute_radiation_field_shortchar_order_0,
              py::call_guard<py::gil_scoped_release>())
         .def("compute_Jeff", &Model::compute_Jeff, py::call_guard<py::gil_scoped_release>())
+        .def("compute_image", &Model::compute_image, py::call_guard<py::gil_scoped_release>())
+        .def("compute_image_new", py::overload_cast<Size>(&Model::compute_image_new),
+             py::call_guard<py::gil_scoped_release>())
+        .def("compute_image_new", py::overload_cast<Size, Size, Size>(&Model::compute_image_new),
+             py::call_guard<py::gil_scoped_release>())
+        .def("compute_image_new", py::overload_cast<double, double, double, Size, Size>(&Model::compute_image_new),
+             py::call_guard<py::gil_scoped_release>())
+        .def_readonly("images", &Model::images)
         .def("compute_level_populations", &Model::compute_level_populations, py::arg("use_Ng_acceleration"),
              py::arg("max_niterations"), py::call_guard<py::gil_scoped_release>())
         .def_readonly("error_mean", &Model::error_mean)

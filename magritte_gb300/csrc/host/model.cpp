@@ -680,4 +680,60 @@ int Model::compute_level_populations(bool use_Ng_acceleration, long max_niterati
     return iterations;
 }
 
+// ---------------------------------------------------------------------------------
+// Imagers (model.cpp:957-1013)
+// ---------------------------------------------------------------------------------
+int Model::compute_image(Size ray_nr) {
+    if (parameters.one_line_approximation)
+        throw std::runtime_error("One line approximation is currently not supported for imaging.");
+    MgrModel* dev = upload();
+    const Size P = parameters.npoints_.v, F = parameters.nfreqs_;
+    Image im;
+    im.imagePointPosition = 0;
+    im.ray_nr = (long)ray_nr;
+    im.ray_direction.assign({3}, geometry.rays.direction.data() + 3 * (size_t)ray_nr);
+    im.nfreqs = F;
+    im.freqs.resize({F});
+    for (Size f = 0; f < F; f++) im.freqs[f] = radiation.frequencies.nu[f];  // nu(0, f)
+    im.I.resize({P, F});
+    im.ImX.resize({P});
+    im.ImY.resize({P});
+    check(mgr_image(dev, parameters.precision, ray_nr, im.I.data(), im.ImX.data(), im.ImY.data()));
+    images.push_back(std::move(im));
+    return 0;
+}
+
+int Model::compute_image_new(Size ray_nr) { return compute_image_new(ray_nr, 256, 256); }
+
+int Model::compute_image_new(Size ray_nr, Size Nxpix, Size Nypix) {
+    const double* d = geometry.rays.direction.data() + 3 * (size_t)ray_nr;
+    return compute_image_new(d[0], d[1], d[2], Nxpix, Nypix);
+}
+
+int Model::compute_image_new(double rx, double ry, double rz, Size Nxpix, Size Nypix) {
+    if (rx * rx + ry * ry + rz * rz == 0.0)
+        throw std::runtime_error(
+            "The given ray direction vector does not point in a direction. Please use a non-zero (normed) direction "
+            "vector to generate an image.");
+    if (parameters.one_line_approximation) throw std::runtime_error("One line approximation is not supported for imaging.");
+    MgrModel* dev = upload();
+    const Size F = parameters.nfreqs_;
+    const size_t npix = (size_t)Nxpix * Nypix;
+    const double inv = 1 / std::sqrt(rx * rx + ry * ry + rz * rz);
+    const double d[3] = {rx * inv, ry * inv, rz * inv};
+    Image im;
+    im.imagePointPosition = 1;
+    im.ray_nr = -1;
+    im.ray_direction.assign({3}, d);
+    im.nfreqs = F;
+    im.freqs.resize({F});
+    for (Size f = 0; f < F; f++) im.freqs[f] = radiation.frequencies.nu[f];
+    im.I.resize({npix, F});
+    im.ImX.resize({npix});
+    im.ImY.resize({npix});
+    check(mgr_image_new(dev, parameters.precision, d, Nxpix, Nypix, im.I.data(), im.ImX.data(), im.ImY.data()));
+    images.push_back(std::move(im));
+    return 0;
+}
+
 }  // namespace mgrhost

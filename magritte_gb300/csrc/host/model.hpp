@@ -222,6 +222,18 @@ struct Radiation {
     Array<double> I;  // [nrays][P][F]  (short characteristics)
 };
 
+// One image (src/model/image/image.hpp:30-60): intensities I [npix][nfreqs] and the
+// image-plane coordinates of the pixels.
+struct Image {
+    int imagePointPosition = 0;  // 0 AllModelPoints (old imager), 1 ProjectionSurface
+    long ray_nr = -1;
+    Array<double> ray_direction;  // [3]
+    Array<double> ImX, ImY;       // [npix]
+    Array<double> I;              // [npix][nfreqs]
+    Array<double> freqs;          // [nfreqs]
+    Size nfreqs = 0;
+};
+
 class Model {
    public:
     Parameters parameters;
@@ -232,6 +244,7 @@ class Model {
     Radiation radiation;
     Array<double> dshift_max;
     std::vector<double> error_max, error_mean;
+    std::vector<Image> images;
 
     enum SpectralDiscretisation { SD_None, SD_Lines, SD_Image } spectralDiscretisation = SD_None;
 
@@ -253,6 +266,10 @@ class Model {
     int set_dshift_max();
     int compute_radiation_field_feautrier_order_2();
     int compute_radiation_field_shortchar_order_0();
+    int compute_image(Size ray_nr);
+    int compute_image_new(Size ray_nr);
+    int compute_image_new(Size ray_nr, Size Nxpix, Size Nypix);
+    int compute_image_new(double rx, double ry, double rz, Size Nxpix, Size Nypix);
     int compute_Jeff();
     int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
 

@@ -200,18 +200,31 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
             return MGR_ERR_ARGUMENT;
         }
     }
+    // A line spectral discretisation (compute_spectral_discretisation(), model.cpp:70-161)
+    // has every frequency mapped to (species, transition, quadrature point); the imaging
+    // ones (model.cpp:165-275) leave the maps unset and serve only the imagers.
+    bool line_disc = (F == L * d->nquads);
+    for (uint32_t f = 0; f < F && line_disc; f++)
+        if (d->corr_line[f] >= L || d->corr_lspec[f] >= d->nlspecs || d->corr_z[f] >= d->nquads) line_disc = false;
+    // the line each frequency is measured from in split precision: its own line, or
+    // for an imaging discretisation the nearest line
+    std::vector<uint32_t> corr_line(F);
     for (uint32_t f = 0; f < F; f++) {
-        if (d->corr_line[f] >= L || d->corr_lspec[f] >= d->nlspecs || d->corr_z[f] >= d->nquads) {
-            set_error("mgr_model_create: frequency maps out of range");
-            return MGR_ERR_ARGUMENT;
+        if (line_disc) {
+            corr_line[f] = d->corr_line[f];
+        } else {
+            uint32_t best = 0;
+            for (uint32_t l = 1; l < L; l++)
+                if (std::fabs(d->nu[f] - d->line[l]) < std::fabs(d->nu[f] - d->line[best])) best = l;
+            corr_line[f] = best;
         }
-    }
-    if (F != L * d->nquads) {
-        set_error("mgr_model_create: the formal solve needs a line spectral discretisation (nfreqs = nlines*nquads)");
-        return MGR_ERR_UNSUPPORTED;
     }
 
     MgrModel* m = new MgrModel();
+    m->line_disc = line_disc;
+    m->host_pos.assign(d->position, d->position + 3 * (size_t)P);
+    m->host_p2b.assign(d->point2boundary, d->point2boundary + P);
+    m->host_raydir.assign(d->ray_direction, d->ray_direction + 3 * (size_t)d->nrays);
     cudaGetDevice(&m->device);
     cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device);
     if (m->sm_count < 1) m->sm_count = 1;
@@ -297,6 +310,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = dalloc(m, &m->iw_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->Sp_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->nint, (E ? E : 1) * (size_t)L)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->nint_all, E ? E : 1)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->em, d->emissivity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->op, d->opacity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->iw, d->inverse_width, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
@@ -308,7 +322,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.dshift_max, d->dshift_max, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.dshift_max_f, dsm_f.data(), P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.nu, d->nu, (size_t)P * F)) != cudaSuccess) break;
-        if ((e = upload(m, &dm.corr_line, d->corr_line, F)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.corr_line, corr_line.data(), F)) != cudaSuccess) break;
         if ((e = upload(m, &dm.corr_lspec, d->corr_lspec, F)) != cudaSuccess) break;
         if ((e = upload(m, &dm.corr_k, d->corr_k, F)) != cudaSuccess) break;
         if ((e = upload(m, &dm.corr_z, d->corr_z, F)) != cudaSuccess) break;
@@ -335,6 +349,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.iw_f = m->iw_f;
     dm.Sp_f = m->Sp_f;
     dm.nint = m->nint;
+    dm.nint_all = m->nint_all;
     apply_scales(m, d->emissivity, d->opacity);
     if ((e = launch_line_tables(m)) != cudaSuccess || (e = launch_nint_table(m)) != cudaSuccess) {
         int rc = cuda_fail(e, "line tables");
@@ -455,6 +470,11 @@ int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, d
     if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
         set_error("mgr_formal_solve_fo2_device: unknown precision mode");
         return MGR_ERR_ARGUMENT;
+    }
+    if (!model->line_disc) {
+        set_error("mgr_formal_solve_fo2_device: the formal solve needs a line spectral discretisation "
+                  "(nfreqs = nlines*nquads with every frequency mapped to its line)");
+        return MGR_ERR_UNSUPPORTED;
     }
     const size_t wb = fo2_work_bytes(model, model->dm.P, u_dev == nullptr, lambda_diag_dev != nullptr);
     int rc = ensure_scratch(model, &model->work, &model->work_bytes, wb);

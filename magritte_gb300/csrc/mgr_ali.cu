@@ -951,6 +951,10 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
         set_error("mgr_compute_level_populations: unknown precision mode");
         return MGR_ERR_ARGUMENT;
     }
+    if (!model->line_disc) {
+        set_error("mgr_compute_level_populations: needs a line spectral discretisation");
+        return MGR_ERR_UNSUPPORTED;
+    }
     const MgrAliParams& prm = *params;
     if (prm.Ng_acceleration_mem_limit < 1 || prm.Ng_acceleration_mem_limit > (uint32_t)kMaxNgOrder ||
         prm.adaptive_Ng_acceleration_min_order < 1) {

@@ -67,6 +67,7 @@ struct DevModel {
     const double* Sp;        // emissivity / opacity, the reference's per-call quotient
     const double* crit;      // interpolation criterion opacity / population_tot
     const uint16_t* nint;    // [E][L] interpolation count of each CSR edge (crt -> nxt) per line
+    const uint16_t* nint_all;// [E] the same over all lines (imagers)
     const float* em_f;
     const float* op_f;
     const float* iw_f;

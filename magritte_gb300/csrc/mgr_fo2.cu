@@ -70,6 +70,23 @@ __global__ void nint_table_kernel(DevModel m, uint16_t* __restrict__ nint, int* 
     }
 }
 
+// The same over all lines (InterpHelper::get_n_interp, solver_interp_helper.tpp:10-46),
+// for the imagers' Solver::set_data.
+__global__ void nint_all_kernel(DevModel m, uint16_t* __restrict__ nint_all, int* status) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < m.P; p += gridDim.x * blockDim.x) {
+        const uint32_t cum = m.cum_nb[p], n = m.n_nb[p];
+        for (uint32_t k = 0; k < n; k++) {
+            const uint32_t nxt = (uint32_t)__double_as_longlong(m.edge[cum + k].w);
+            uint32_t v = n_interp_all_lines(m, p, nxt);
+            if (v > 0xffffu) {
+                atomicOr(status, ST_CAPACITY);
+                v = 0xffffu;
+            }
+            nint_all[cum + k] = (uint16_t)v;
+        }
+    }
+}
+
 cudaError_t launch_nint_table(MgrModel* model) {
     const uint64_t n = (uint64_t)model->dm.P * model->dm.L;
     const int threads = 256;
@@ -78,6 +95,12 @@ cudaError_t launch_nint_table(MgrModel* model) {
     count_launch();
     nint_table_kernel<<<(unsigned)(blocks ? blocks : 1), threads, 0, model->stream>>>(model->dm, model->nint,
                                                                                        model->status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    count_launch();
+    const uint64_t pb = ((uint64_t)model->dm.P + threads - 1) / threads;
+    nint_all_kernel<<<(unsigned)(pb < 152 * 32 ? (pb ? pb : 1) : 152 * 32), threads, 0, model->stream>>>(
+        model->dm, model->nint_all, model->status);
     return cudaGetLastError();
 }
 

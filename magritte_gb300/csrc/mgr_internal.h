@@ -29,10 +29,12 @@ struct MgrModel {
     float* iw_f = nullptr;
     float* Sp_f = nullptr;
     uint16_t* nint = nullptr;        // [E][L] interpolation counts
+    uint16_t* nint_all = nullptr;    // [E] interpolation counts over all lines (imagers)
     int fo2_warps = 8;               // warps (ray pairs in flight) per CTA of the formal solve
     int fo2_minb_split = 3;          // register budget variant: CTAs per SM (2, 3 or 4)
     int fo2_minb_fp64 = 3;
     int sm_count = 1;                // multiprocessors of the model's device
+    bool line_disc = true;           // frequencies form a line spectral discretisation
     int* status = nullptr;           // device status word
     mgr::LineScales scales;          // FP32 line-table scales (split precision)
     uint32_t half_cap = 0;           // longest half ray in base steps (0 = not sized yet)
@@ -52,6 +54,10 @@ struct MgrModel {
     const double* last_lam = nullptr;
     // line-producing species and the ALI loop (mgr_ali.cu)
     mgr::AliState* ali = nullptr;
+    // host copies for the image-plane set-up (mgr_image.cu)
+    std::vector<double> host_pos;     // [P][3]
+    std::vector<uint32_t> host_p2b;   // [P]
+    std::vector<double> host_raydir;  // [nrays][3]
 };
 
 namespace mgr {

@@ -240,6 +240,10 @@ int mgr_formal_solve_sc0_device(MgrModel* model, int precision, double* J_dev, d
         set_error("mgr_formal_solve_sc0_device: unknown precision mode");
         return MGR_ERR_ARGUMENT;
     }
+    if (!model->line_disc) {
+        set_error("mgr_formal_solve_sc0_device: needs a line spectral discretisation");
+        return MGR_ERR_UNSUPPORTED;
+    }
     const size_t wb = sc0_work_bytes(model, model->dm.P, u_dev == nullptr, lambda_diag_dev != nullptr);
     if (model->work_bytes < wb) {
         if (model->work) cudaFree(model->work);

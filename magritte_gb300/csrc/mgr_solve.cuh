@@ -34,7 +34,14 @@ struct HalfSmem {
     float* dsh;      // (float)(shift - 1)
     float* dzs;      // (float)dZ * dz_scale (split precision)
     uint32_t* eid;   // CSR edge of step s (index into the interpolation-count table)
+    double shift0 = 1.0;  // shift of the origin as this half's trace starts from it (1 comoving)
+    float dsh0 = 0.0f;    // shift0 - 1
+    double cshift = 1.0;  // shift of the origin element itself (the backward half's shift0)
 };
+
+// Interpolation over all lines (Solver::set_data, solver.tpp:1003-1043) instead of
+// one line's criterion, as the imagers trace.
+constexpr uint32_t kAllLines = 0xffffffffu;
 
 // Shared-memory carve-up of one warp's two half-ray buffers.
 __device__ __forceinline__ void carve_halves(unsigned char* base, uint32_t cap, HalfSmem& bk, HalfSmem& fw) {
@@ -70,7 +77,10 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
 // Lanes scan the neighbour list; the argmin of (distance to ray, neighbour order)
 // reproduces the reference's strict-< scan.  Returns the number of steps, or -1 on
 // capacity overflow / invalid geometry (status bits set).
-template <bool STORE>
+// FRAME 0: comoving shifts relative to the origin point (the formal solves);
+// FRAME 1: rest-frame shifts of the old imager (Geometry::get_shift<Rest>, reversed for
+// r >= hnrays, geometry.tpp:428-465).
+template <bool STORE, int FRAME = 0>
 __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem h, int lane,
                           int* status) {
     const double* d = m.raydir + 3 * r;
@@ -142,7 +152,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
     if (STORE && count > 0) {
         // Per-step Doppler shifts and FP32 copies, one step per lane.
         for (int s = lane; s < count; s += 32) {
-            const double sh = shift_comoving(m, o, h.ids[s], d);
+            const double sh = FRAME ? shift_rest(m, r, h.ids[s], d) : shift_comoving(m, o, h.ids[s], d);
             h.shift[s] = sh;
             h.dsh[s] = (float)dsub_rn(sh, 1.0);
             h.dzs[s] = (float)h.dZ[s] * m.dz_scale;
@@ -176,6 +186,7 @@ struct Elem {
 // (solver.tpp:1057-1097).  Elements of one step are visited i = n .. 1.
 struct ElemIter {
     int s;          // current base step
+    int nsteps;     // steps of the half (upward iteration)
     uint32_t i;     // current sub-element (n .. 1), 0 = step exhausted
     uint32_t n;     // interpolation count of step s
     uint32_t crt, nxt;
@@ -188,18 +199,18 @@ MGR_HD void iter_load_step(const DevModel& m, const HalfSmem& h, uint32_t o, uin
     const int s = it.s;
     it.crt = s ? h.ids[s - 1] : o;
     it.nxt = h.ids[s];
-    it.n = m.nint[(size_t)h.eid[s] * m.L + l];
+    it.n = (l == kAllLines) ? m.nint_all[h.eid[s]] : m.nint[(size_t)h.eid[s] * m.L + l];
     it.i = it.n;
     const uint32_t n = it.n;
     if constexpr (MODE == MODE_FP64) {
-        it.shc = s ? h.shift[s - 1] : 1.0;
+        it.shc = s ? h.shift[s - 1] : h.shift0;
         it.shn = h.shift[s];
         it.dzs = h.dZ[s];
         // per-step parts of the reference's per-element expressions (same roundings)
         it.dshi = dsub_rn(it.shn, it.shc) / (double)n;
         it.dzi = it.dzs / (double)n;
     } else {
-        const float dshc = s ? h.dsh[s - 1] : 0.0f;
+        const float dshc = s ? h.dsh[s - 1] : h.dsh0;
         const float dshn = h.dsh[s];
         const float rn = fast_div(1.0f, (float)n);
         it.dshc = dshc;
@@ -210,17 +221,11 @@ MGR_HD void iter_load_step(const DevModel& m, const HalfSmem& h, uint32_t o, uin
     }
 }
 
-// Produces the next element (outer to inner).  Returns false when only the
-// centre element remains.
+// Element (step it.s, sub-element i of n) of the loaded step, with the reference's
+// per-element expressions (set_data_for_line / set_data).
 template <int MODE>
-MGR_HD bool iter_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it, Elem& e) {
-    if (it.i == 0) {
-        if (it.s == 0) return false;
-        it.s--;
-        iter_load_step<MODE>(m, h, o, l, it);
-    }
+MGR_HD void step_elem(const ElemIter& it, uint32_t i, Elem& e) {
     const uint32_t n = it.n;
-    const uint32_t i = it.i;
     e.nr = it.nxt;
     e.ni = it.crt;
     if constexpr (MODE == MODE_FP64) {
@@ -242,7 +247,45 @@ MGR_HD bool iter_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t
         e.i = i;
         e.n = n;
     }
+}
+
+// Produces the next element (outer to inner).  Returns false when only the
+// centre element remains.
+template <int MODE>
+MGR_HD bool iter_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it, Elem& e) {
+    if (it.i == 0) {
+        if (it.s == 0) return false;
+        it.s--;
+        iter_load_step<MODE>(m, h, o, l, it);
+    }
+    step_elem<MODE>(it, it.i, e);
     it.i--;
+    return true;
+}
+
+// The same half from the origin outward (inner to outer, the array order of a forward
+// half): steps 0 .. nsteps-1, sub-elements 1 .. n.  it.s == nsteps when done.
+template <int MODE>
+MGR_HD void iter_up_begin(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, int nsteps, ElemIter& it) {
+    it.s = 0;
+    it.nsteps = nsteps;
+    if (nsteps > 0) {
+        iter_load_step<MODE>(m, h, o, l, it);
+        it.i = 1;
+    }
+}
+
+template <int MODE>
+MGR_HD bool iter_up_next(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_t l, ElemIter& it, Elem& e) {
+    if (it.s >= it.nsteps) return false;
+    step_elem<MODE>(it, it.i, e);
+    if (++it.i > it.n) {
+        it.s++;
+        if (it.s < it.nsteps) {
+            iter_load_step<MODE>(m, h, o, l, it);
+            it.i = 1;
+        }
+    }
     return true;
 }
 
@@ -257,15 +300,15 @@ MGR_HD void iter_begin(const DevModel& m, const HalfSmem& h, uint32_t o, uint32_
     iter_load_step<MODE>(m, h, o, l, it);
 }
 
-MGR_HD Elem centre_elem(uint32_t o) {
+MGR_HD Elem centre_elem(uint32_t o, double shift0 = 1.0, float dsh0 = 0.0f) {
     Elem e;
     e.nr = o;
     e.ni = o;  // never read: its interpolation factor is 0
     e.fac = 0.0;
-    e.shift = 1.0;
+    e.shift = shift0;
     e.dzin = 0.0;
-    e.dsh = 0.0f;
-    e.dshm = 0.0f;
+    e.dsh = dsh0;
+    e.dshm = fabsf(dsh0);
     e.facf = 0.0f;
     e.dzf = 0.0f;
     e.s = 0;
@@ -278,13 +321,13 @@ MGR_HD Elem centre_elem(uint32_t o) {
 // exactly as the FP64 iterator does.
 MGR_HD void elem_shift_fac(const HalfSmem& h, const Elem& e, double& shift, double& fac) {
     if (e.n == 0) {
-        shift = 1.0;
+        shift = h.cshift;
         fac = 0.0;
         return;
     }
     const double shn = h.shift[e.s];
     if (e.n > 1) {
-        const double shc = e.s ? h.shift[e.s - 1] : 1.0;
+        const double shc = e.s ? h.shift[e.s - 1] : h.shift0;
         shift = dadd_rn(shc, dmul_rn((double)e.i, dsub_rn(shn, shc) / (double)e.n));
         fac = 1.0 - ((double)e.i) / (double)e.n;
     } else {
@@ -488,9 +531,10 @@ MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, floa
 // computed with the expressions of dtau_single_line_fp64 and the correctly rounded
 // erff.  Returns {erff(next) - erff(curr), next - curr}.
 static __host__ __device__ __noinline__ float2 band_erf(const double* iw, uint32_t L, double linefreq, double freq,
-                                                 const double* hshift, Elem lo, Elem hi, uint32_t l) {
+                                                 const double* hshift, double shift0, double cshift, Elem lo, Elem hi,
+                                                 uint32_t l) {
     double lo_shift, lo_fac, hi_shift, hi_fac;
-    const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr};
+    const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr, shift0, 0.0f, cshift};
     elem_shift_fac(h, lo, lo_shift, lo_fac);
     elem_shift_fac(h, hi, hi_shift, hi_fac);
     const double cf = freq * lo_shift;
@@ -509,10 +553,10 @@ static __host__ __device__ __noinline__ float2 band_erf(const double* iw, uint32
 }
 
 // The reference's branch test |shift_hi - shift_lo| > min(dshift_max) on the FP64 shifts.
-static __host__ __device__ __noinline__ bool large_shift_fp64(const double* hshift, const double* dshift_max, Elem lo,
-                                                       Elem hi) {
+static __host__ __device__ __noinline__ bool large_shift_fp64(const double* hshift, double shift0, double cshift,
+                                                       const double* dshift_max, Elem lo, Elem hi) {
     double lsh, lfac, hsh, hfac;
-    const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr};
+    const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr, shift0, 0.0f, cshift};
     elem_shift_fac(h, lo, lsh, lfac);
     elem_shift_fac(h, hi, hsh, hfac);
     const double dshift_abs = fabs(dsub_rn(hsh, lsh));
@@ -555,7 +599,7 @@ MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Hal
         // cancels and its single-ulp roundings decide the result, so take it on the
         // FP64 mode's arguments with the correctly rounded erff (split precision then
         // stays within 1e-5 of the FP64 path in J).
-        const float2 r = band_erf(m.iw, m.L, m.line[l], c.freq, h.shift, lo, hi, l);
+        const float2 r = band_erf(m.iw, m.L, m.line[l], c.freq, h.shift, h.shift0, h.cshift, lo, hi, l);
         erfdiff = r.x;
         diff_pos = r.y;
     } else {
@@ -681,7 +725,7 @@ MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, con
         const float thr = fminf(m.dshift_max_f[outer.nr], m.dshift_max_f[inner.nr]);
         const float margin = 4.0e-3f * thr + 2.0e-6f * (outer.dshm + inner.dshm);
         if (fabsf(dsf - thr) > margin) out.large = dsf > thr;
-        else out.large = large_shift_fp64(h.shift, m.dshift_max, outer, inner);
+        else out.large = large_shift_fp64(h.shift, h.shift0, h.cshift, m.dshift_max, outer, inner);
     }
     if (out.large) {
         if constexpr (MODE == MODE_FP64) {
@@ -919,6 +963,103 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         else res.Ldiag = (1.0 + top.F) * denominator;
     }
     return res;
+}
+
+// Imagers (Solver::image_feautrier_order_2(model, o, f), solver.tpp:2462-2574): the
+// forward elimination over the whole ray, elements first .. last = the backward half
+// (outer to inner), the origin, and the forward half (inner to outer); the pixel is
+// 2 Su[last] - I_bdy(nr[last], nu(o, f)), Su[last] being the last row's solution.  The
+// ray's elements use all-line interpolation (kAllLines) and the halves' shift0.  With
+// nf = 0 (new imager) the origin itself is the last element.
+template <int MODE, int AP>
+__host__ __device__ double image_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
+                                      int nb, const HalfSmem& fw, int nf) {
+    using T = typename Real_<MODE>::T;
+    if (nb <= 0 && nf <= 0) return boundary_intensity(m, c.o, c.freq);
+    const Elem cen = centre_elem(c.o, bk.cshift, (float)dsub_rn(bk.cshift, 1.0));
+    ElemIter ib, iu;
+    int phase;  // 0: backward half, 2: forward half, 3: done
+    Elem prev;
+    if (nb > 0) {
+        iter_begin<MODE>(m, bk, c.o, kAllLines, nb, ib);
+        iter_next<MODE>(m, bk, c.o, kAllLines, ib, prev);
+        phase = 0;
+    } else {
+        prev = cen;
+        iter_up_begin<MODE>(m, fw, c.o, kAllLines, nf, iu);
+        phase = 2;
+    }
+    const HalfSmem& h_first = (nb > 0) ? bk : fw;
+    double bshift = prev.shift;
+    if constexpr (MODE == MODE_SPLIT) {
+        double fac;
+        elem_shift_fac(h_first, prev, bshift, fac);
+    }
+    const double Ibdy_f = boundary_intensity(m, prev.nr, c.freq * bshift);
+    EC<MODE> ec_prev{T(0), T(0), false};
+    Sweep st{0.0, 0.0, 0.0, 0.0, 0.0, false};
+    T dt_prev = T(0), S_last = T(0);
+    Elem last = prev;
+    bool first = true;
+    while (true) {
+        Elem cur;
+        bool from_fw = false;
+        if (phase == 0) {
+            if (!iter_next<MODE>(m, bk, c.o, kAllLines, ib, cur)) {
+                cur = cen;
+                phase = 1;
+            }
+        } else {
+            if (phase == 1) {
+                iter_up_begin<MODE>(m, fw, c.o, kAllLines, nf, iu);
+                phase = 2;
+            }
+            if (!iter_up_next<MODE>(m, fw, c.o, kAllLines, iu, cur)) break;
+            from_fw = true;
+        }
+        const HalfSmem& h = from_fw ? fw : bk;
+        const double dz = from_fw ? cur.dzin : prev.dzin;
+        const float dzf = from_fw ? cur.dzf : prev.dzf;
+        EC<MODE> ec_cur{T(0), T(0), false};
+        PairOut<MODE> po;
+        eval_pair<MODE, AP>(m, sl, c, h, prev, cur, dz, dzf, ec_prev, ec_cur, po);
+        if (first) {
+            const double dt = po.dtau;
+            const double inverse_dtau = drcp<MODE>(dt);
+            const double Cb = 2.0 * inverse_dtau * inverse_dtau;
+            const double Bb_min_Cb = 1.0 + 2.0 * inverse_dtau;
+            const double Bb = Bb_min_Cb + Cb;
+            if constexpr (MODE == MODE_FP64) st.Su = ((double)po.Slo + 2.0 * Ibdy_f * inverse_dtau) / Bb;
+            else st.Su = ((double)po.Slo + 2.0 * Ibdy_f * inverse_dtau) * drcp<MODE>(Bb);
+            st.F = 0.5 * Bb_min_Cb * dt * dt;
+            st.FI = drcp<MODE>(1.0 + st.F);
+            first = false;
+        } else {
+            elim_row<MODE>(dt_prev, po.dtau, po.Slo, st.F, st.FI, st.Su);
+        }
+        dt_prev = po.dtau;
+        S_last = po.Shi;
+        last = cur;
+        prev = cur;
+        ec_prev = ec_cur;
+        if (phase == 1 && nf <= 0) break;  // the origin is the last element
+    }
+    // last row (solver.tpp:2284-2297)
+    double lshift = last.shift;
+    if constexpr (MODE == MODE_SPLIT) {
+        double fac;
+        elem_shift_fac((nf > 0) ? fw : bk, last, lshift, fac);
+    }
+    const double Ibdy_l = boundary_intensity(m, last.nr, c.freq * lshift);
+    const double dtl = dt_prev;
+    const double inverse_dtau_l = drcp<MODE>(dtl);
+    const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
+    const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
+    const double Bl = Bl_min_Al + Al;
+    const double denominator = drcp<MODE>(Bl * st.F + Bl_min_Al);
+    const double Sl = (double)S_last + 2.0 * Ibdy_l * inverse_dtau_l;
+    const double u = (Al * st.Su + Sl) * (1.0 + st.F) * denominator;
+    return 2.0 * u - boundary_intensity(m, last.nr, c.freq);
 }
 
 // Result of one lane's short-characteristics solve.

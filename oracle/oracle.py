@@ -103,8 +103,10 @@ def reference_setup(raw, approx="CloseLines", max_width_fraction=0.35, min_opaci
     if image_freqs is not None:
         nu_min, nu_max, n = image_freqs
         F = int(n)
-        dnu = (nu_max - nu_min) / (F - 1) if F > 1 else 0.0
-        row = np.array([nu_min + f * dnu for f in range(F)]) if F > 1 else np.array([(nu_min + nu_max) / 2.0])
+        # long double step as the reference (model.cpp:257-262)
+        dnu = (np.longdouble(nu_max) - np.longdouble(nu_min)) / (F - 1) if F > 1 else np.longdouble(0)
+        row = (np.array([float(np.longdouble(nu_min) + f * dnu) for f in range(F)]) if F > 1
+               else np.array([(nu_min + nu_max) / 2.0]))
         nu = np.tile(row, (P, 1))
         corr_line = np.zeros(F, np.uint32)  # not set by the reference for this discretisation
         corr_lspec = np.full(F, F, np.uint32)

@@ -1,0 +1,87 @@
+"""GPU imagers (compute_image, compute_image_new) against the oracle, through the C
+ABI: images within 1e-5 relative in FP64 mode and in split precision; image-plane
+coordinates exact.  The new imager also meets the reference's analytic benchmark
+bound (constant velocity gradient, 1.5e-3; see test_oracle_images.py)."""
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+from magritte_gb300 import _abi
+from magritte_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_with_correctly_rounded_erf():
+    O.set_erf_mode(1)
+    yield
+    O.set_erf_mode(0)
+
+
+@pytest.mark.parametrize("approx", ["CloseLines", "None"])
+@pytest.mark.parametrize("rr", [0, 9])
+def test_old_imager_matches_oracle(gpu_lib, approx, rr):
+    raw = S.grid_sphere(n=16, nside=1, nquads=7)
+    a = H.setup(raw, approx=approx)
+    ref = O.Oracle(a).image_fo2(rr)
+    dev = _abi.DeviceModel(a)
+    try:
+        for precision in ("fp64", "split"):
+            g = dev.image(rr, precision)
+            assert H.max_rel(g["I"], ref) < 1e-5, precision
+        d = raw.ray_direction[rr]
+        den = np.sqrt(d[0] ** 2 + d[1] ** 2)
+        ix, iy = d[1] / den, -d[0] / den
+        x = raw.position
+        np.testing.assert_array_equal(g["ImX"], ix * x[:, 0] + iy * x[:, 1])
+    finally:
+        dev.close()
+
+
+def test_new_imager_matches_oracle(gpu_lib):
+    raw = S.velocity_gradient_shells(nshells=10)
+    fcen = raw.linedata[0].frequency[0]
+    dd = 1.0e4 / 2.99792458e8
+    a = H.setup(raw, max_width_fraction=0.5, image_freqs=(fcen - fcen * dd, fcen + fcen * dd, 10))
+    d = raw.ray_direction[raw.nrays // 2 - 1]
+    ref = O.Oracle(a).image_new(d, 50, 50)
+    dev = _abi.DeviceModel(a)
+    try:
+        for precision in ("fp64", "split"):
+            g = dev.image_new(d, 50, 50, precision)
+            np.testing.assert_array_equal(g["ImX"], ref["ImX"])
+            np.testing.assert_array_equal(g["ImY"], ref["ImY"])
+            assert H.max_rel(g["I"], ref["I"]) < 1e-5, precision
+        # an oblique direction through the same model
+        d2 = np.array([0.3, -0.5, 0.81])
+        ref2 = O.Oracle(a).image_new(d2, 24, 20)
+        g2 = dev.image_new(d2, 24, 20, "fp64")
+        assert H.max_rel(g2["I"], ref2["I"]) < 1e-5
+    finally:
+        dev.close()
+
+
+def test_core_model_compute_image_new(gpu_lib):
+    """The drop-in API on the imaging benchmark: core.Model.compute_image_new(ray_nr,
+    nx, ny) after the imaging spectral discretisation, against the oracle."""
+    from magritte_gb300 import loader
+
+    raw = S.velocity_gradient_shells(nshells=10)
+    fcen = raw.linedata[0].frequency[0]
+    dd = 1.0e4 / 2.99792458e8
+    a = H.setup(raw, max_width_fraction=0.5, image_freqs=(fcen - fcen * dd, fcen + fcen * dd, 10))
+    ray_nr = raw.nrays // 2 - 1
+    ref = O.Oracle(a).image_new(raw.ray_direction[ray_nr], 50, 50)
+    model = loader.to_core(raw, precision="fp64")
+    model.parameters.max_width_fraction = 0.5
+    model.compute_spectral_discretisation(fcen - fcen * dd, fcen + fcen * dd)
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    model.compute_image_new(ray_nr, 50, 50)
+    im = model.images[-1]
+    assert H.max_rel(np.array(im.I).reshape(2500, -1), ref["I"]) < 1e-5
+    np.testing.assert_array_equal(np.array(im.ImX), ref["ImX"])
+    model.compute_image(ray_nr)
+    assert np.isfinite(np.array(model.images[-1].I)).all()

@@ -105,3 +105,23 @@ def test_emulated_shortchar_matches_oracle(emu, name, approx):
         # all_zero has dtau = min_dtau everywhere, where the reference's factor + 1 =
         # expm1f(-dtau)/dtau + 1 is single-precision rounding noise (solver.tpp:1631-1637)
         assert H.max_rel(lam32[has], ref["lambda_diag"][has]) < 5e-4
+
+
+@pytest.mark.parametrize("name", ["cube10", "sphere14", "sphere16"])
+@pytest.mark.parametrize("approx", ["CloseLines", "None"])
+@pytest.mark.parametrize("rr", [0, 7])
+def test_emulated_old_imager_matches_oracle(emu, name, approx, rr):
+    """image_lane (the imager kernels' lane code) over rest-frame traces against the
+    oracle's image_feautrier_order_2."""
+    raw = MODELS[name]()
+    a = H.setup(raw, approx=approx)
+    rr = rr % a["nrays"]
+    ref = O.Oracle(a).image_fo2(rr)
+    desc, keep = _abi.make_desc(a)
+    emu.mgr_emu_image.argtypes = [C.POINTER(_abi.MgrModelDesc), C.c_int, C.c_uint32, C.POINTER(C.c_double)]
+    emu.mgr_emu_image.restype = C.c_int
+    for precision, tol in (("fp64", 1e-12), ("split", 1e-5)):
+        I = np.zeros((a["npoints"], a["nfreqs"]))
+        assert emu.mgr_emu_image(C.byref(desc), _abi.PRECISION[precision], rr,
+                                 I.ctypes.data_as(C.POINTER(C.c_double))) == 0
+        assert H.max_rel(I, ref) < tol, precision
