@@ -16,7 +16,11 @@ Arms:
                       host->device upload and the J/ALO read-back every step.
   --impl reference  : the reference algorithm on the host cores (the CPU oracle port,
                       all threads), on a bounded sample of the same workload.
-Under torchrun with N>1 every rank runs an independent replica (weak scaling).
+Under torchrun with N>1 the ray pairs of the one model are sharded over the ranks
+(contiguous blocks, magritte_gb300.distributed.ray_shard) and every step ends with
+one FP64 NCCL sum-allreduce of the packed partial J and ALO diagonal (strong
+scaling: the whole job solves the same model; `value` = its solves / the slowest
+rank's time).
 """
 import argparse
 import json
@@ -235,18 +239,31 @@ def run_ours(args, rank, ws):
     P, F, R, L = prm.npoints(), prm.nfreqs(), prm.hnrays(), prm.nlines()
     prec = _abi.PRECISION[args.precision]
 
+    from magritte_gb300 import distributed
+
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.ExternalStream(lib.mgr_model_stream(handle), device=dev)
-    J = torch.empty((P, F), dtype=torch.float64, device=dev)
-    lam = torch.empty((P, L), dtype=torch.float64, device=dev)
+    packed = torch.empty(P * F + P * L, dtype=torch.float64, device=dev)  # [J | ALO diagonal]
+    J = packed[:P * F].view(P, F)
+    lam = packed[P * F:].view(P, L)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
     tuning = None if args.no_autotune else {p: _abi.autotune(handle, p) for p in sorted({args.precision, "fp64"})}
+    rr0, rr1 = distributed.ray_shard(R, rank, ws)
+    if ws > 1 and rr1 <= rr0:
+        raise SystemExit(f"{ws} ranks for {R} ray pairs: every rank needs at least one")
 
     def step():
-        rc = lib.mgr_formal_solve_fo2_device(handle, prec, C.c_void_p(J.data_ptr()), None,
-                                             C.c_void_p(lam.data_ptr()))
+        if ws == 1:
+            rc = lib.mgr_formal_solve_fo2_device(handle, prec, C.c_void_p(J.data_ptr()), None,
+                                                 C.c_void_p(lam.data_ptr()))
+        else:
+            rc = lib.mgr_formal_solve_fo2_rays_device(handle, prec, rr0, rr1, C.c_void_p(J.data_ptr()),
+                                                      C.c_void_p(lam.data_ptr()))
         if rc != 0:
             raise RuntimeError(lib.mgr_last_error().decode())
+        if ws > 1:
+            import torch.distributed as dist
+            dist.all_reduce(packed, op=dist.ReduceOp.SUM)  # on the current (the model's) stream
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -277,12 +294,13 @@ def run_ours(args, rank, ws):
     kernel_s = sum(step_ms) / 1000.0
     kernel_s = max_over_ranks(kernel_s, ws)
     solves = float(P) * R * F
-    value = ws * solves * args.steps / kernel_s
+    value = solves * args.steps / kernel_s  # the whole job solves one model per step
 
     # work statistics for the algorithmic-bytes roofline
     st_steps, st_nbr, st_elem = C.c_uint64(), C.c_uint64(), C.c_uint64()
     _abi._check(lib.mgr_ray_statistics(handle, C.byref(st_steps), C.byref(st_nbr), C.byref(st_elem)))
     alg_bytes = 28.0 * (st_steps.value + st_nbr.value) + 52.0 * st_elem.value + 32.0 * solves
+    alg_bytes *= (rr1 - rr0) / R  # this rank's share of the ray pairs
     mean_launch_s = kernel_s / args.steps
     achieved = alg_bytes / mean_launch_s / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -316,7 +334,27 @@ def run_ours(args, rank, ws):
 
     # end to end through the public API: fresh upload, solve, read-back of J and the ALO
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and ws > 1:
+        # sharded: core.Model.upload, this rank's ray pairs, the allreduce, read-back
+        e2e_times = []
+        for _ in range(max(1, min(args.steps, 3))):
+            model.release_device()
+            torch.cuda.synchronize()
+            barrier(ws)
+            t0 = time.perf_counter()
+            h = model.upload()
+            Jd, ld = distributed.formal_solve_fo2_handle(h, P, F, L, R, args.precision)
+            Jh, lh = Jd.cpu(), ld.cpu()
+            e2e_times.append(time.perf_counter() - t0)
+        h2d = (P * 3 * 8 * 2 + len(raw.neighbors) * 4 + P * 4 * 3 + P * F * 8 + 4 * P * L * 8 + P * 8 * 3
+               + F * 4 * 4 + F)
+        d2h = P * F * 8 + P * L * 8
+        e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times), ws)
+        e2e = {"value": solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s,
+               "path": "core.Model.upload + distributed.formal_solve_fo2_handle (ray-pair shard + NCCL "
+                       "allreduce) + J/ALO read-back"}
+    elif not args.no_e2e:
         prm.store_u = False
         model.release_device()
         model.compute_radiation_field_feautrier_order_2()  # warm the host paths
@@ -331,7 +369,7 @@ def run_ours(args, rank, ws):
                + F * 4 * 4 + F)
         d2h = P * F * 8 + P * L * 8
         e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times), ws)
-        e2e = {"value": ws * solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s,
                "path": "core.Model.compute_radiation_field_feautrier_order_2 (upload + solve + J/ALO read-back)"}
 
@@ -343,11 +381,13 @@ def run_ours(args, rank, ws):
         cpu = cpu_baseline(raw, os.cpu_count() or 1)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * kernel_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1000.0 * kernel_s / args.steps, "higher_is_better": True,
+        "scaling": "strong" if ws > 1 else "weak",
         "vs_baseline": None, "dtype": "f32+f64" if args.precision == "split" else "f64", "data": "synthetic",
         "config": {"workload": desc, "npoints": P, "ray_pairs": R, "nfreqs": F, "precision": args.precision,
                    "approx": "CloseLines", "solves_per_step": solves, "l2": "flushed between steps (512 MB write)",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"ray-pair shards x{ws} + NCCL sum-allreduce" if ws > 1 else "1 GPU",
+                   "ray_pairs_rank0": [rr0, rr1]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes,

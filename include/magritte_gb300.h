@@ -143,6 +143,40 @@ int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, d
 int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, double* u_dev,
                                 double* lambda_diag_dev);
 
+/* Partial formal solve over the ray pairs [rr_begin, rr_end) only: J_dev [P][F] and
+ * lambda_diag_dev [P][L] (may be NULL) receive the sums over those ray pairs, so that
+ * the sum over disjoint ranges covering [0, hnrays) is the full solve's J and ALO
+ * diagonal up to the order of the additions.  This is the per-rank half of the
+ * reference's multi-process formal solve: Solver::solve_feautrier_order_2 loops over
+ * ray pairs (src/solver/solver.tpp:476), then combines the processes with
+ * Radiation::MPI_reduce_J (solver.tpp:531 -> src/model/radiation/radiation.cpp:76-86)
+ * and Lambda::MPI_gather (solver.tpp:537 ->
+ * src/model/lines/lineProducingSpecies/lambda/lambda.tpp:121-206); here each shard
+ * solves a block of ray pairs and the caller sums (e.g. an NCCL sum-allreduce).
+ * Device pointers, enqueued on the model's stream. */
+int mgr_formal_solve_fo2_rays_device(MgrModel* model, int precision, uint32_t rr_begin, uint32_t rr_end,
+                                     double* J_dev, double* lambda_diag_dev);
+
+/* Host-buffer variant of mgr_formal_solve_fo2_rays_device; blocks. */
+int mgr_formal_solve_fo2_rays(MgrModel* model, int precision, uint32_t rr_begin, uint32_t rr_end, double* J,
+                              double* lambda_diag);
+
+/* Sum of the shards' partial J [nJ] and ALO diagonal [nlam] (device pointers, in
+ * place), enqueued in order on `stream` (the model's cudaStream_t) or completed
+ * before returning.  Returns 0 on success. */
+typedef int (*mgr_reduce_fn)(void* user, double* J_dev, uint64_t nJ, double* lambda_diag_dev, uint64_t nlam,
+                             void* stream);
+
+/* Restricts the formal solves of mgr_compute_level_populations to the ray pairs
+ * [rr_begin, rr_end) and sums the shards with `reduce` after each of them, before
+ * Jeff and the rate equations, which every shard then runs on the same totals
+ * (replicated statistical equilibrium).  reduce may not be NULL for a partial range.
+ * capturable != 0 declares that reduce only enqueues stream work that a CUDA graph
+ * capture can record (e.g. ncclAllReduce); otherwise the iterations run uncaptured.
+ * rr_begin = 0, rr_end = hnrays and reduce = NULL restore the unsharded loop. */
+int mgr_set_ray_shard(MgrModel* model, uint32_t rr_begin, uint32_t rr_end, mgr_reduce_fn reduce, void* user,
+                      int capturable);
+
 /* Model::compute_radiation_field_shortchar_order_0 (src/model/model.cpp:313-349 ->
  * Solver::solve_shortchar_order_0, src/solver/solver.tpp:150-235, :1564-1757).
  * Host buffers (any may be NULL except J):

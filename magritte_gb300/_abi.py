@@ -75,6 +75,9 @@ ALI_DEFAULTS = dict(pop_prec=1.0e-6, min_rel_pop_for_convergence=1.0e-10, conver
                     adaptive_Ng_acceleration_use_max_criterion=1)
 
 
+# mgr_reduce_fn: (user, J_dev, nJ, lambda_diag_dev, nlam, stream) -> 0 on success.
+REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_void_p)
+
 # Every exported symbol of include/magritte_gb300.h with its ctypes signature.
 SIGNATURES = {
     "mgr_last_error": (C.c_char_p, []),
@@ -88,6 +91,10 @@ SIGNATURES = {
                                      _u32p, _u32p, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgr_formal_solve_fo2_rays": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, _f64p, _f64p]),
+    "mgr_formal_solve_fo2_rays_device": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p,
+                                                   C.c_void_p]),
+    "mgr_set_ray_shard": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, REDUCE_FN, C.c_void_p, C.c_int]),
     "mgr_formal_solve_sc0": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_sc0_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_void_p]),
@@ -220,6 +227,37 @@ class DeviceModel:
                                            _ptr(lam, _f64p)))
         return dict(J=J, u=u, lambda_diag=lam)
 
+    def formal_solve_fo2_rays(self, rr_begin, rr_end, precision="fp64", want_lambda=True):
+        """Partial J and ALO diagonal summed over the ray pairs [rr_begin, rr_end)."""
+        J = np.empty((self.P, self.F))
+        lam = np.empty((self.P, self.L)) if want_lambda else None
+        _check(load().mgr_formal_solve_fo2_rays(self.h, PRECISION[precision], rr_begin, rr_end, _ptr(J, _f64p),
+                                                _ptr(lam, _f64p)))
+        return dict(J=J, lambda_diag=lam)
+
+    def formal_solve_fo2_rays_device(self, precision, rr_begin, rr_end, J_dev, lam_dev=None):
+        """Enqueue the partial solve of [rr_begin, rr_end) on the model stream (device pointers)."""
+        _check(load().mgr_formal_solve_fo2_rays_device(self.h, PRECISION[precision], rr_begin, rr_end,
+                                                       C.c_void_p(J_dev), C.c_void_p(lam_dev) if lam_dev else None))
+
+    def set_ray_shard(self, rr_begin, rr_end, reduce=None, capturable=False):
+        """Restrict the ALI loop's formal solves to [rr_begin, rr_end); ``reduce`` is a
+        Python callable (J_dev, nJ, lam_dev, nlam, stream) -> None that sums the shards
+        in place (it may raise).  reduce=None with the full range restores the default."""
+        if reduce is None:
+            cb = REDUCE_FN()
+        else:
+            def _cb(user, J, nJ, lam, nlam, stream):
+                try:
+                    reduce(J, nJ, lam, nlam, stream)
+                    return 0
+                except Exception as e:  # reported as an error of the ALI call
+                    self._shard_error = e
+                    return 1
+            cb = REDUCE_FN(_cb)
+        self._shard_cb = cb  # the library keeps the pointer: hold the thunk
+        _check(load().mgr_set_ray_shard(self.h, rr_begin, rr_end, cb, None, int(bool(capturable))))
+
     def image(self, ray_nr, precision="fp64"):
         I = np.empty((self.P, self.F))
         X, Y = np.empty(self.P), np.empty(self.P)
@@ -320,8 +358,15 @@ class DeviceModel:
         it = C.c_int()
         cap = max_it * len(self.nlev)
         em, ex = np.zeros(cap), np.zeros(cap)
-        _check(load().mgr_compute_level_populations(self.h, PRECISION[precision], int(use_ng), max_it, C.byref(p),
-                                                    C.byref(it), _ptr(em, _f64p), _ptr(ex, _f64p), cap))
+        self._shard_error = None
+        try:
+            _check(load().mgr_compute_level_populations(self.h, PRECISION[precision], int(use_ng), max_it,
+                                                        C.byref(p), C.byref(it), _ptr(em, _f64p), _ptr(ex, _f64p),
+                                                        cap))
+        except MgrError as e:
+            if self._shard_error is not None:
+                raise e from self._shard_error
+            raise
         n = it.value * len(self.nlev)
         return dict(iterations=it.value, error_mean=em[:n], error_max=ex[:n])
 

@@ -213,13 +213,15 @@ LaneResult solve(const DevModel& m, int precision, const LaneCtx& c, const HalfS
 
 }  // namespace
 
-// The kernel's two stages for every origin: per (rr, f) lane solves, then J and the
-// ALO summed in (rr, q) order as fo2_reduce_kernel does.
-extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, double* J, double* lam) {
+// The kernel's two stages for every origin: per (rr, f) lane solves over the ray
+// pairs [rr0, rr1), then J and the ALO summed in (rr, q) order as fo2_reduce_kernel does.
+static int emu_fo2(const MgrModelDesc* d, int precision, uint32_t rr0, uint32_t rr1, double* J, double* lam) {
     EmuModel x;
     build_emu_model(d, x);
     const DevModel& m = x.m;
     const uint32_t P = m.P, L = m.L, F = m.F, R = m.hnrays, Q = m.Q;
+    if (rr1 > R) rr1 = R;
+    if (rr0 >= rr1) return MGR_ERR_ARGUMENT;
     int err = 0;
 #pragma omp parallel
     {
@@ -230,7 +232,7 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
         for (long long oo = 0; oo < (long long)P; oo++) {
             const uint32_t o = (uint32_t)oo;
             bool ok = true;
-            for (uint32_t rr = 0; rr < R && ok; rr++) {
+            for (uint32_t rr = rr0; rr < rr1 && ok; rr++) {
                 const int nb = trace_half_host(m, o, rr, kCap, bk);
                 const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
                 if (nb < 0 || nf < 0) {
@@ -250,7 +252,7 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
             }
             for (uint32_t f = 0; f < F; f++) {
                 double s = 0.0;
-                for (uint32_t rr = 0; rr < R; rr++) s += U[(size_t)rr * F + f] * 2.0 * m.rayw[rr];
+                for (uint32_t rr = rr0; rr < rr1; rr++) s += U[(size_t)rr * F + f] * 2.0 * m.rayw[rr];
                 J[(size_t)o * F + f] = s;
             }
             if (!lam) continue;
@@ -261,7 +263,7 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
                     if (f != 0xffffffffu && m.in_line[f]) k[q] = lambda_factors(m, m.sorted_line, o, f);
                 }
                 double s = 0.0;
-                for (uint32_t rr = 0; rr < R; rr++)
+                for (uint32_t rr = rr0; rr < rr1; rr++)
                     for (uint32_t q = 0; q < Q; q++) {
                         const uint32_t f = m.lq2f[(size_t)l * Q + q];
                         const double e = (f != 0xffffffffu && m.in_line[f])
@@ -274,6 +276,16 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
         }
     }
     return err ? MGR_ERR_TRACE : MGR_OK;
+}
+
+extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, double* J, double* lam) {
+    return emu_fo2(d, precision, 0, 0xffffffffu, J, lam);
+}
+
+// Partial sums over the ray pairs [rr_begin, rr_end), as mgr_formal_solve_fo2_rays_device.
+extern "C" int mgr_emu_formal_solve_fo2_rays(const MgrModelDesc* d, int precision, uint32_t rr_begin,
+                                             uint32_t rr_end, double* J, double* lam) {
+    return emu_fo2(d, precision, rr_begin, rr_end, J, lam);
 }
 
 // Short characteristics: the kernel's per-lane code and the reduction order of

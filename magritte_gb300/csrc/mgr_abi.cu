@@ -487,6 +487,82 @@ int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, d
     return MGR_OK;
 }
 
+int mgr_formal_solve_fo2_rays_device(MgrModel* model, int precision, uint32_t rr_begin, uint32_t rr_end,
+                                     double* J_dev, double* lambda_diag_dev) {
+    if (!model || !J_dev) {
+        set_error("mgr_formal_solve_fo2_rays_device: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
+        set_error("mgr_formal_solve_fo2_rays_device: unknown precision mode");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (rr_begin >= rr_end || rr_end > model->dm.hnrays) {
+        set_error("mgr_formal_solve_fo2_rays_device: ray-pair range [" + std::to_string(rr_begin) + ", " +
+                  std::to_string(rr_end) + ") is empty or beyond hnrays = " + std::to_string(model->dm.hnrays));
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!model->line_disc) {
+        set_error("mgr_formal_solve_fo2_rays_device: the formal solve needs a line spectral discretisation");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    const size_t wb = fo2_work_bytes(model, model->dm.P, true, lambda_diag_dev != nullptr);
+    int rc = ensure_scratch(model, &model->work, &model->work_bytes, wb);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = launch_fo2_range(model, precision, 0, model->dm.P, J_dev, nullptr, lambda_diag_dev, model->work,
+                                     model->work_bytes, rr_begin, rr_end);
+    if (e != cudaSuccess) return cuda_fail(e, "partial formal solve launch");
+    return MGR_OK;
+}
+
+int mgr_formal_solve_fo2_rays(MgrModel* model, int precision, uint32_t rr_begin, uint32_t rr_end, double* J,
+                              double* lambda_diag) {
+    if (!model || !J) {
+        set_error("mgr_formal_solve_fo2_rays: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    const DevModel& dm = model->dm;
+    const size_t PF = (size_t)dm.P * dm.F;
+    int rc = ensure_scratch(model, &model->J_scratch, &model->J_scratch_bytes, PF * 8);
+    if (rc != MGR_OK) return rc;
+    if (lambda_diag &&
+        (rc = ensure_scratch(model, &model->lam_scratch, &model->lam_scratch_bytes, (size_t)dm.P * dm.L * 8)) != MGR_OK)
+        return rc;
+    rc = mgr_formal_solve_fo2_rays_device(model, precision, rr_begin, rr_end, model->J_scratch,
+                                          lambda_diag ? model->lam_scratch : nullptr);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(J, model->J_scratch, PF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && lambda_diag)
+        e = cudaMemcpyAsync(lambda_diag, model->lam_scratch, (size_t)dm.P * dm.L * 8, cudaMemcpyDeviceToHost,
+                            model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "result copy");
+    return read_status(model);
+}
+
+int mgr_set_ray_shard(MgrModel* model, uint32_t rr_begin, uint32_t rr_end, mgr_reduce_fn reduce, void* user,
+                      int capturable) {
+    if (!model) {
+        set_error("mgr_set_ray_shard: null model");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (rr_begin >= rr_end || rr_end > model->dm.hnrays) {
+        set_error("mgr_set_ray_shard: ray-pair range is empty or beyond hnrays");
+        return MGR_ERR_ARGUMENT;
+    }
+    const bool full = rr_begin == 0 && rr_end == model->dm.hnrays;
+    if (!full && !reduce) {
+        set_error("mgr_set_ray_shard: a partial ray-pair range needs a reduce function");
+        return MGR_ERR_ARGUMENT;
+    }
+    model->shard_begin = rr_begin;
+    model->shard_end = rr_end;
+    model->shard_reduce = reduce;
+    model->shard_user = user;
+    model->shard_capturable = capturable != 0;
+    ali_shard_changed(model);
+    return MGR_OK;
+}
+
 int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, double* lambda_diag) {
     if (!model || !J) {
         set_error("mgr_formal_solve_fo2: null argument");

@@ -749,9 +749,19 @@ static int read_stats(MgrModel* model) {
 
 // One normal iteration after the history push: formal solve, Jeff, rate equations,
 // corrections, convergence, line data.
+// With a ray-pair shard, the formal solve covers the shard's ray pairs and the reduce
+// function sums J and the ALO diagonal over the shards before Jeff.
 static cudaError_t normal_iteration_launches(MgrModel* model, int precision) {
     cudaError_t e = launch_fo2_range(model, precision, 0, model->dm.P, model->J_scratch, nullptr, model->lam_scratch,
-                                     model->work, model->work_bytes);
+                                     model->work, model->work_bytes, model->shard_begin, model->shard_end);
+    if (e == cudaSuccess && model->shard_reduce) {
+        const DevModel& m = model->dm;
+        if (model->shard_reduce(model->shard_user, model->J_scratch, (uint64_t)m.P * m.F, model->lam_scratch,
+                                (uint64_t)m.P * m.L, (void*)model->stream) != 0) {
+            model->ali->reduce_failed = true;
+            e = cudaErrorUnknown;
+        }
+    }
     if (e == cudaSuccess) e = ali_launch_jeff(model, model->J_scratch, model->lam_scratch);
     if (e == cudaSuccess) e = ali_launch_stateq_and_refresh(model, model->lam_scratch);
     return e;
@@ -765,7 +775,8 @@ static cudaError_t normal_iteration(MgrModel* model, int precision) {
         cudaGraphExecDestroy(st.graph);
         st.graph = nullptr;
     }
-    if (!st.graph && !st.graph_failed) {
+    const bool capture = !model->shard_reduce || model->shard_capturable;
+    if (!st.graph && !st.graph_failed && capture) {
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamBeginCapture(model->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
@@ -783,11 +794,19 @@ static cudaError_t normal_iteration(MgrModel* model, int precision) {
             st.graph_precision = precision;
         }
     }
-    if (st.graph) {
+    if (st.graph && capture) {
         count_launch();  // the graph's kernels were counted when captured; one more per replay is not kept exact
         return cudaGraphLaunch(st.graph, model->stream);
     }
     return normal_iteration_launches(model, precision);
+}
+
+void ali_shard_changed(MgrModel* model) {
+    if (!model->ali) return;
+    AliState& st = *model->ali;
+    if (st.graph) cudaGraphExecDestroy(st.graph);
+    st.graph = nullptr;
+    st.graph_failed = false;
 }
 
 }  // namespace mgr
@@ -1057,7 +1076,14 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
         iteration++;
         some_not_converged = false;
         if ((e = ali_history_push_all(model)) != cudaSuccess) return cuda_fail(e, "population history");
-        if ((e = normal_iteration(model, precision)) != cudaSuccess) return cuda_fail(e, "ALI iteration");
+        if ((e = normal_iteration(model, precision)) != cudaSuccess) {
+            if (st.reduce_failed) {
+                st.reduce_failed = false;
+                set_error("mgr_compute_level_populations: the ray-shard reduce function failed");
+                return MGR_ERR_CUDA;
+            }
+            return cuda_fail(e, "ALI iteration");
+        }
         if ((rc = read_stats(model)) != MGR_OK) return rc;
         take_stats();
         iteration_normal++;

@@ -78,9 +78,12 @@ struct AliState {
     cudaGraphExec_t graph = nullptr;
     int graph_precision = -1;
     bool graph_failed = false;
+    bool reduce_failed = false;  // the ray-shard reduce function returned an error
 };
 
 cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam);
+// Drops the captured iteration after the ray-pair shard or its reduce function changed.
+void ali_shard_changed(MgrModel* model);
 cudaError_t ali_launch_stateq_and_refresh(MgrModel* model, const double* lam);
 cudaError_t ali_launch_line_refresh(MgrModel* model);
 cudaError_t ali_ng_step(MgrModel* model, int order);

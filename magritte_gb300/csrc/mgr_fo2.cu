@@ -139,8 +139,9 @@ __global__ void ray_lengths_kernel(DevModel m, uint32_t cap, uint32_t* d_max, in
 // (2: 128, 3: 80, 4: 64 registers per thread); picked at run time by the tuner.
 template <int MODE, int AP, int MINB>
 __global__ void __launch_bounds__(256, MINB)
-    fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end, double* __restrict__ U, size_t u_stride,
-               uint32_t u_o0, double* __restrict__ LD, size_t ld_stride, uint32_t ld_o0, int* status) {
+    fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
+               double* __restrict__ U, size_t u_stride, uint32_t u_o0, double* __restrict__ LD, size_t ld_stride,
+               uint32_t ld_o0, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
@@ -152,17 +153,16 @@ __global__ void __launch_bounds__(256, MINB)
     for (uint32_t i = threadIdx.x; i < m.L; i += blockDim.x) sl[i] = m.sorted_line[i];
     __syncthreads();
 
-    const uint32_t R = m.hnrays;
-    const uint64_t n_items = (uint64_t)(o_end - o_begin) * R;
+    const uint64_t n_items = (uint64_t)(o_end - o_begin) * nR;
     const uint64_t stride = (uint64_t)gridDim.x * nw;
     for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
-        const uint32_t o = o_begin + (uint32_t)(item / R);
-        const uint32_t rr = (uint32_t)(item % R);
+        const uint32_t o = o_begin + (uint32_t)(item / nR);
+        const uint32_t rr = rr0 + (uint32_t)(item % nR);
         const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
         const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
         if (nb < 0 || nf < 0) continue;  // status recorded by the trace
-        double* Ui = U + (size_t)rr * u_stride + (size_t)(o - u_o0) * m.F;
-        double* Li = LD ? LD + (size_t)rr * ld_stride + (size_t)(o - ld_o0) * m.F : nullptr;
+        double* Ui = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
+        double* Li = LD ? LD + (size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F : nullptr;
         for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
             const uint32_t f = f0 + lane;
             if (f < m.F) {
@@ -192,6 +192,7 @@ __global__ void __launch_bounds__(256, MINB)
 // with lanes over quadrature points.  lq2f[l * Q + q] is the frequency of (l, q).
 // ---------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_begin, uint32_t o_end,
+                                                         uint32_t rr0, uint32_t nR,
                                                          const double* __restrict__ U, size_t u_stride, uint32_t u_o0,
                                                          const double* __restrict__ LD, size_t ld_stride,
                                                          uint32_t ld_o0, double* __restrict__ J,
@@ -199,12 +200,11 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const uint32_t R = m.hnrays;
     for (uint32_t o = o_begin + blockIdx.x; o < o_end; o += gridDim.x) {
         for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
             const double* Uo = U + (size_t)(o - u_o0) * m.F + f;
             double s = 0.0;
-            for (uint32_t rr = 0; rr < R; rr++) s += Uo[(size_t)rr * u_stride] * 2.0 * m.rayw[rr];
+            for (uint32_t k = 0; k < nR; k++) s += Uo[(size_t)k * u_stride] * 2.0 * m.rayw[rr0 + k];
             J[(size_t)o * m.F + f] = s;
         }
         if (!lam) continue;
@@ -219,8 +219,8 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
             bool valid = f != 0xffffffffu && m.in_line[f];
             if (once && valid) k = lambda_factors(m, m.sorted_line, o, f);
             double s = 0.0;
-            for (uint32_t rr = 0; rr < R; rr++) {
-                const double* Lr = LD + (size_t)rr * ld_stride + (size_t)(o - ld_o0) * m.F;
+            for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
+                const double* Lr = LD + (size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F;
                 for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
                     if (!once) {
                         f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
@@ -411,8 +411,9 @@ size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, b
 }
 
 template <int MODE, int AP, int MINB>
-static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* U, size_t u_stride,
-                                      uint32_t u_o0, double* LD, size_t ld_stride, uint32_t ld_o0) {
+static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
+                                      double* U, size_t u_stride, uint32_t u_o0, double* LD, size_t ld_stride,
+                                      uint32_t ld_o0) {
     const DevModel& m = model->dm;
     const uint32_t cap = model->half_cap;
     int nw = model->fo2_warps > 0 ? model->fo2_warps : 8;
@@ -426,41 +427,46 @@ static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nw * 32, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;  // the ray buffers do not fit in shared memory
-    const uint64_t items = (uint64_t)(o_end - o_begin) * m.hnrays;
+    const uint64_t items = (uint64_t)(o_end - o_begin) * nR;
     uint64_t grid = (uint64_t)model->sm_count * per_sm;
     const uint64_t need = (items + nw - 1) / nw;
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
     count_launch();
-    kern<<<(unsigned)grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, U, u_stride, u_o0, LD, ld_stride,
-                                                          ld_o0, model->status);
+    kern<<<(unsigned)grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, rr0, nR, U, u_stride, u_o0, LD,
+                                                          ld_stride, ld_o0, model->status);
     return cudaGetLastError();
 }
 
 template <int MODE, int AP>
-static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* U, size_t us,
-                                   uint32_t uo, double* LD, size_t ls, uint32_t lo) {
+static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
+                                   double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo) {
     const int minb = (MODE == MODE_SPLIT) ? model->fo2_minb_split : model->fo2_minb_fp64;
-    if (minb == 2) return launch_fo2_variant<MODE, AP, 2>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
-    if (minb == 4) return launch_fo2_variant<MODE, AP, 4>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
-    return launch_fo2_variant<MODE, AP, 3>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+    if (minb == 2) return launch_fo2_variant<MODE, AP, 2>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
+    if (minb == 4) return launch_fo2_variant<MODE, AP, 4>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
+    return launch_fo2_variant<MODE, AP, 3>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
 }
 
 template <int MODE>
-static cudaError_t launch_fo2_approx(MgrModel* model, uint32_t o_begin, uint32_t o_end, double* U, size_t us,
-                                     uint32_t uo, double* LD, size_t ls, uint32_t lo) {
+static cudaError_t launch_fo2_approx(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
+                                     double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo) {
     switch (model->dm.approx) {
-        case APPROX_ONELINE: return launch_fo2_minb<MODE, APPROX_ONELINE>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+        case APPROX_ONELINE:
+            return launch_fo2_minb<MODE, APPROX_ONELINE>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
         case APPROX_CLOSELINES:
-            return launch_fo2_minb<MODE, APPROX_CLOSELINES>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
-        default: return launch_fo2_minb<MODE, APPROX_NONE>(model, o_begin, o_end, U, us, uo, LD, ls, lo);
+            return launch_fo2_minb<MODE, APPROX_CLOSELINES>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
+        default: return launch_fo2_minb<MODE, APPROX_NONE>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
     }
 }
 
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
-                             double* lam, double* work, size_t work_bytes) {
+                             double* lam, double* work, size_t work_bytes, uint32_t rr_begin, uint32_t rr_end) {
     const DevModel& m = model->dm;
     if (o_end <= o_begin) return cudaSuccess;
+    if (rr_end > m.hnrays) rr_end = m.hnrays;
+    if (rr_begin >= rr_end) return cudaErrorInvalidValue;
+    const uint32_t nR = rr_end - rr_begin;
+    if (u && nR != m.hnrays) return cudaErrorInvalidValue;  // u is written for full solves only
     const int k = (u ? 0 : 1) + (lam ? 1 : 0);
     const size_t per = fo2_bytes_per_origin(model);
     uint32_t chunk = o_end - o_begin;
@@ -485,17 +491,17 @@ cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, u
             U = work;
             us = (size_t)n * m.F;
             uo = c0;
-            next = work + (size_t)m.hnrays * n * m.F;
+            next = work + (size_t)nR * n * m.F;
         }
         double* LD = lam ? next : nullptr;
         const size_t ls = (size_t)n * m.F;
         cudaError_t e = (precision == MGR_PRECISION_SPLIT)
-                            ? launch_fo2_approx<MODE_SPLIT>(model, c0, c1, U, us, uo, LD, ls, c0)
-                            : launch_fo2_approx<MODE_FP64>(model, c0, c1, U, us, uo, LD, ls, c0);
+                            ? launch_fo2_approx<MODE_SPLIT>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0)
+                            : launch_fo2_approx<MODE_FP64>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0);
         if (e != cudaSuccess) return e;
         unsigned grid = n < (uint32_t)nsm * 16 ? n : (unsigned)nsm * 16;
         count_launch();
-        fo2_reduce_kernel<<<grid, 128, 0, model->stream>>>(m, c0, c1, U, us, uo, LD, ls, c0, J, lam);
+        fo2_reduce_kernel<<<grid, 128, 0, model->stream>>>(m, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, J, lam);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

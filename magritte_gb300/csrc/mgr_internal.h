@@ -54,6 +54,12 @@ struct MgrModel {
     const double* last_lam = nullptr;
     // line-producing species and the ALI loop (mgr_ali.cu)
     mgr::AliState* ali = nullptr;
+    // ray-pair shard of the ALI loop's formal solves and the sum over shards
+    uint32_t shard_begin = 0;
+    uint32_t shard_end = 0xffffffffu;
+    mgr_reduce_fn shard_reduce = nullptr;
+    void* shard_user = nullptr;
+    bool shard_capturable = false;
     // host copies for the image-plane set-up (mgr_image.cu)
     std::vector<double> host_pos;     // [P][3]
     std::vector<uint32_t> host_p2b;   // [P]
@@ -73,8 +79,10 @@ cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps);
 // (sized by fo2_work_bytes for the same u / lam choice), in chunks of origins that fit.
 constexpr size_t kFo2WorkBudget = size_t(2) << 30;
 size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, bool stage_ld);
+// Ray pairs [rr_begin, rr_end) only (partial J / ALO sums, u must then be NULL).
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
-                             double* lam, double* work, size_t work_bytes);
+                             double* lam, double* work, size_t work_bytes, uint32_t rr_begin = 0,
+                             uint32_t rr_end = 0xffffffffu);
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
                                 uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
                                 double* d_dZ);
