@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--ali-points", type=int, default=50_000)
     p.add_argument("--ali-nside", type=int, default=2)
     p.add_argument("--ali-iterations", type=int, default=20)
+    p.add_argument("--no-batch", action="store_true", help="skip the many-model batch leg")
+    p.add_argument("--batch-models", type=int, default=512)
+    p.add_argument("--batch-steps", type=int, default=1)
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the library's default launch shape (for profiling one production launch)")
     return p.parse_args()
@@ -187,6 +190,129 @@ def run_ali(args):
             "iterations": it, "ng": "Default, every 4", "precision": args.precision, "wall_s": wall,
             "s_per_iteration": wall / max(it, 1), "solves_per_iteration": float(P) * R * F,
             "note": "config-2 family reduced to fit the bench time; no CPU leg (one oracle iteration takes minutes)"}
+
+
+class _Handle:
+    """A core.Model's device handle with the sizes the batch wrapper reads."""
+
+    def __init__(self, model):
+        import ctypes as C
+        prm = model.parameters
+        self.h = C.c_void_p(model.upload())
+        self.P, self.F, self.L, self.R = prm.npoints(), prm.nfreqs(), prm.nlines(), prm.hnrays()
+
+
+def run_batch(args):
+    """Many-model batch: independent models (sphere cutouts, P log-uniform in
+    [2k, 60k], 12 or 48 rays, 2-5-level rotors, nquads 11/21/31, random T and v)
+    solved by one persistent launch per step."""
+    import numpy as np
+    import torch
+    from magritte_gb300 import _abi, loader, synthetic
+
+    t_setup = time.perf_counter()
+    specs = synthetic.many_models(args.batch_models)
+    models, devs = [], []
+    for sp in specs:
+        m = loader.to_core(synthetic.batch_model(**sp), precision=args.precision)
+        m.compute_spectral_discretisation()
+        m.compute_inverse_line_widths()
+        m.compute_LTE_level_populations()
+        models.append(m)
+        devs.append(_Handle(m))
+    setup_s = time.perf_counter() - t_setup
+    dev = torch.device("cuda", torch.cuda.current_device())
+    Js = [torch.empty(d.P * d.F, dtype=torch.float64, device=dev) for d in devs]
+    Ls = [torch.empty(d.P * d.L, dtype=torch.float64, device=dev) for d in devs]
+    solves = float(sum(d.P * d.R * d.F for d in devs))
+    batch = _abi.Batch(devs)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
+    jp, lp = [t.data_ptr() for t in Js], [t.data_ptr() for t in Ls]
+
+    def solve(b):
+        b.formal_solve_fo2_device(args.precision, jp, lp)
+
+    # tile shape (CTAs per SM x warps per CTA), timed on a sample of 16 models; the
+    # sample's runs also warm the kernels up
+    ns = min(16, len(devs))
+    sub = _abi.Batch(devs[:ns])
+    sub_stream = torch.cuda.ExternalStream(sub.stream(), device=dev)
+    best = None
+    for minb in (2, 3, 4):
+        for warps in (4, 8):
+            try:
+                sub.set_tuning(minb, warps)
+            except _abi.MgrError:
+                continue
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            sub.formal_solve_fo2_device(args.precision, jp[:ns], lp[:ns])  # first use of this shape
+            e0.record(sub_stream)
+            sub.formal_solve_fo2_device(args.precision, jp[:ns], lp[:ns])
+            e1.record(sub_stream)
+            sub_stream.synchronize()
+            ms = e0.elapsed_time(e1)
+            if best is None or ms < best[0]:
+                best = (ms, minb, warps)
+    sub.close()
+    batch.set_tuning(best[1], best[2])
+    stream.synchronize()
+    launches0 = _abi.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.batch_steps)]
+    for a, b in ev:
+        a.record(stream)
+        solve(batch)
+        b.record(stream)
+    stream.synchronize()
+    launches = _abi.launch_count() - launches0
+    start, finish = batch.timings()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    batch_s = sum(step_ms) / 1000.0 / len(step_ms)
+
+    # one call per model (each call its own persistent launch) against a batch of the
+    # same models, on a sample of 64 models
+    ns = min(64, len(devs))
+    lib = _abi.load()
+    sub = _abi.Batch(devs[:ns])
+    sub.set_tuning(best[1], best[2])
+    sub_solves = float(sum(d.P * d.R * d.F for d in devs[:ns]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sub.formal_solve_fo2_device(args.precision, jp[:ns], lp[:ns])
+    _abi._check(lib.mgr_sync(devs[0].h))
+    torch.cuda.ExternalStream(sub.stream(), device=dev).synchronize()
+    sub_s = time.perf_counter() - t0
+    sub.close()
+    t0 = time.perf_counter()
+    for d, j, l in zip(devs[:ns], jp[:ns], lp[:ns]):
+        _abi._check(lib.mgr_formal_solve_fo2_device(d.h, _abi.PRECISION[args.precision], C_void(j), None,
+                                                    C_void(l)))
+    for d in devs[:ns]:
+        _abi._check(lib.mgr_sync(d.h))
+    seq_s = time.perf_counter() - t0
+    batch.close()
+    for m in models:
+        m.release_device()
+    lat = finish
+    flight = finish - start
+    pct = lambda x, q: float(np.percentile(x, q))
+    return {"workload": f"{len(devs)} models, sphere cutouts P {min(d.P for d in devs)}-{max(d.P for d in devs)} "
+                        f"(mean {np.mean([d.P for d in devs]):.0f}), 12/48 rays, 2-5-level rotors, nquads 11/21/31",
+            "solves_per_step": solves, "value": solves / batch_s, "unit": UNIT, "ms_per_step": 1000 * batch_s,
+            "steps": len(step_ms), "step_ms": step_ms, "gpu_launches": int(launches),
+            "tuning": {"min_blocks_per_sm": best[1], "warps_per_block": best[2]},
+            "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max()),
+                           "definition": "model's last origin finished, since the launch began"},
+            "in_flight_ms": {"p50": pct(flight, 50), "p99": pct(flight, 99),
+                             "definition": "model's last origin finished minus its origin 0 started"},
+            "sample_64": {"batch_solves_per_s": sub_solves / sub_s, "one_call_per_model_solves_per_s":
+                          sub_solves / seq_s, "note": "host wall clock, first 64 models"},
+            "setup_s": setup_s, "precision": args.precision}
+
+
+def C_void(x):
+    import ctypes as C
+    return C.c_void_p(x)
 
 
 def run_reference(args, rank, ws):
@@ -376,6 +502,7 @@ def run_ours(args, rank, ws):
     if rank != 0:
         return
     ali = None if args.no_ali else run_ali(args)
+    batch = None if args.no_batch else run_batch(args)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(raw, os.cpu_count() or 1)
@@ -405,6 +532,7 @@ def run_ours(args, rank, ws):
         "work": {"trace_steps": st_steps.value, "neighbour_reads": st_nbr.value, "elements": st_elem.value},
         "tuning": tuning,
         "ali": ali,
+        "batch": batch,
     }
     print(json.dumps(line), flush=True)
 

@@ -223,6 +223,70 @@ int mgr_image_new(MgrModel* model, int precision, const double* raydir, uint32_t
 int mgr_formal_solve_fo2_device_noalloc(MgrModel* model, int precision, double* J_dev, double* u_dev,
                                         double* lambda_diag_dev);
 
+/* ---- Differentiable new imager ---------------------------------------------------
+ * No reference counterpart (the reference has no derivatives): a smooth FP64 form of
+ * Model::compute_image_new (model.cpp:977-1013 -> Solver::image_feautrier_order_2_new_imager,
+ * solver.tpp:576-627) and its adjoint.  The smooth form replaces the reference's
+ * single-precision powf / expf / expm1f / erff by double-precision pow / exp / expm1 /
+ * erf; the ray traces, interpolation points, CloseLines brackets, the large-shift
+ * branch and the dtau clamp are held fixed (they are piecewise constant).  Device
+ * pointers throughout; the calls block until done. */
+
+/* Replaces the model's velocities (v/c, [P][3], device pointer). */
+int mgr_model_set_velocity_device(MgrModel* model, const double* velocity_dev);
+
+/* mgr_model_set_line_data with device pointers (any may be NULL to keep the resident
+ * copy); the interpolation criterion is kept. */
+int mgr_model_set_line_data_device(MgrModel* model, const double* emissivity_dev, const double* opacity_dev,
+                                   const double* inverse_width_dev);
+
+/* Smooth image: I_dev [nx*ny][F]; ImX / ImY host [nx*ny] (may be NULL). */
+int mgr_image_new_smooth_device(MgrModel* model, const double* raydir, uint32_t nx, uint32_t ny, double* I_dev,
+                                double* ImX, double* ImY);
+
+/* Adjoint of mgr_image_new_smooth_device for d(loss)/d(I) = gI_dev [nx*ny][F]: adds
+ * d(loss)/d(emissivity, opacity, inverse width, source emissivity/opacity) [P][L]
+ * and d(loss)/d(velocity) [P][3] into the given device arrays (not zeroed). */
+int mgr_image_new_adjoint_device(MgrModel* model, const double* raydir, uint32_t nx, uint32_t ny,
+                                 const double* gI_dev, double* g_em_dev, double* g_op_dev, double* g_iw_dev,
+                                 double* g_Sp_dev, double* g_vel_dev);
+
+/* ---- Many-model batch ------------------------------------------------------------
+ * No single reference counterpart: the reference solves one Model per call
+ * (Model::compute_radiation_field_feautrier_order_2, src/model/model.cpp:353-390);
+ * a batch runs that call for many independent models in one persistent kernel
+ * launch.  Each model's J and ALO diagonal equal those of its own
+ * mgr_formal_solve_fo2 (same lane code, same order of the sums). */
+typedef struct MgrBatch MgrBatch;
+
+/* Collects n_models models (same device, same line approximation, line spectral
+ * discretisations) into a batch.  The models stay owned by the caller and must
+ * outlive the batch; their line data may change between solves. */
+int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out);
+void mgr_batch_free(MgrBatch* batch);
+
+/* Launch shape of the batch kernel: CTAs of 256 threads per SM the register budget
+ * is sized for (2, 3 or 4; 0 keeps) and warps per CTA (1..8; 0 keeps). */
+int mgr_batch_set_tuning(MgrBatch* batch, int min_blocks_per_sm, int warps_per_block);
+
+/* One formal solve of every model: J_dev[i] [P_i][F_i] and lambda_diag_dev[i]
+ * [P_i][L_i] (device pointers; lambda_diag_dev or any of its entries may be NULL).
+ * Enqueued on the batch's stream (mgr_batch_stream) after the models' own streams
+ * are idle; returns once the launch is enqueued. */
+int mgr_batch_formal_solve_fo2_device(MgrBatch* batch, int precision, double* const* J_dev,
+                                      double* const* lambda_diag_dev);
+
+/* Host-buffer variant (J[i] / lambda_diag[i] may be NULL to skip a result); blocks. */
+int mgr_batch_formal_solve_fo2(MgrBatch* batch, int precision, double* const* J, double* const* lambda_diag);
+
+/* Per-model timing of the last batch solve from the GPU's global timer, in ms since
+ * the first CTA of the launch started: when the model's first origin started and
+ * when its last origin finished.  Blocks until the solve is done. */
+int mgr_batch_timings(MgrBatch* batch, double* start_ms, double* finish_ms);
+
+/* The batch's CUDA stream (cudaStream_t). */
+void* mgr_batch_stream(MgrBatch* batch);
+
 /* Work counted over one formal solve (all origins, all ray pairs): trace steps,
  * neighbour records scanned by the trace (Geometry::get_next, geometry.tpp:22-38),
  * and ray-pair elements including interpolation points summed over lines

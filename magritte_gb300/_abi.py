@@ -113,6 +113,20 @@ SIGNATURES = {
                                                 C.POINTER(C.c_int), _f64p, _f64p, C.c_uint32]),
     "mgr_get_populations": (C.c_int, [C.c_void_p, C.c_uint32, _f64p]),
     "mgr_get_line_data": (C.c_int, [C.c_void_p, _f64p, _f64p]),
+    "mgr_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(C.c_void_p)]),
+    "mgr_batch_free": (None, [C.c_void_p]),
+    "mgr_batch_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "mgr_batch_formal_solve_fo2_device": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p),
+                                                    C.POINTER(C.c_void_p)]),
+    "mgr_batch_formal_solve_fo2": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(_f64p), C.POINTER(_f64p)]),
+    "mgr_batch_timings": (C.c_int, [C.c_void_p, _f64p, _f64p]),
+    "mgr_batch_stream": (C.c_void_p, [C.c_void_p]),
+    "mgr_model_set_velocity_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mgr_model_set_line_data_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgr_image_new_smooth_device": (C.c_int, [C.c_void_p, _f64p, C.c_uint32, C.c_uint32, C.c_void_p, _f64p,
+                                              _f64p]),
+    "mgr_image_new_adjoint_device": (C.c_int, [C.c_void_p, _f64p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_sync": (C.c_int, [C.c_void_p]),
     "mgr_model_stream": (C.c_void_p, [C.c_void_p]),
     "mgr_launch_count": (C.c_uint64, []),
@@ -379,6 +393,59 @@ class DeviceModel:
         em, op = np.empty((self.P, self.L)), np.empty((self.P, self.L))
         _check(load().mgr_get_line_data(self.h, _ptr(em, _f64p), _ptr(op, _f64p)))
         return em, op
+
+
+class Batch:
+    """Many DeviceModels solved in one persistent launch (mgr_batch_*).  The models
+    must stay open while the batch is used."""
+
+    def __init__(self, devs):
+        lib = load()
+        self.devs = list(devs)
+        hs = (C.c_void_p * len(self.devs))(*[d.h.value for d in self.devs])
+        h = C.c_void_p()
+        _check(lib.mgr_batch_create(hs, len(self.devs), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mgr_batch_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tuning(self, min_blocks_per_sm=0, warps_per_block=0):
+        _check(load().mgr_batch_set_tuning(self.h, min_blocks_per_sm, warps_per_block))
+
+    def formal_solve_fo2(self, precision="fp64", want_lambda=True):
+        n = len(self.devs)
+        Js = [np.empty((d.P, d.F)) for d in self.devs]
+        Ls = [np.empty((d.P, d.L)) if want_lambda else None for d in self.devs]
+        Jp = (_f64p * n)(*[_ptr(x, _f64p) for x in Js])
+        Lp = (_f64p * n)(*[_ptr(x, _f64p) for x in Ls]) if want_lambda else None
+        _check(load().mgr_batch_formal_solve_fo2(self.h, PRECISION[precision], Jp, Lp))
+        return [dict(J=J, lambda_diag=L) for J, L in zip(Js, Ls)]
+
+    def formal_solve_fo2_device(self, precision, J_ptrs, lam_ptrs=None):
+        """Enqueue on the batch stream with lists of device pointers (ints)."""
+        n = len(self.devs)
+        Jp = (C.c_void_p * n)(*J_ptrs)
+        Lp = (C.c_void_p * n)(*lam_ptrs) if lam_ptrs is not None else None
+        _check(load().mgr_batch_formal_solve_fo2_device(self.h, PRECISION[precision], Jp, Lp))
+
+    def timings(self):
+        """(start_ms, finish_ms) per model of the last solve, since the launch began."""
+        n = len(self.devs)
+        s, f = np.empty(n), np.empty(n)
+        _check(load().mgr_batch_timings(self.h, _ptr(s, _f64p), _ptr(f, _f64p)))
+        return s, f
+
+    def stream(self):
+        return load().mgr_batch_stream(self.h)
 
 
 def autotune(handle, precision="split", sample_points=0):

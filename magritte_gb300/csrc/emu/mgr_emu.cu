@@ -9,6 +9,8 @@
 #include <vector>
 
 #include "../../../include/magritte_gb300.h"
+#include "../mgr_adjoint.cuh"
+#include "../mgr_image.cuh"
 #include "../mgr_scale.h"
 #include "../mgr_solve.cuh"
 
@@ -411,4 +413,197 @@ extern "C" int mgr_emu_lane(const MgrModelDesc* d, int precision, uint32_t o, ui
     out[1] = r.Ldiag;
     out[2] = r.solved ? 1.0 : 0.0;
     return MGR_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Differentiable new imager: sequential pixel traces (bdy_point_closer, pixel_start,
+// trace_image restated for one thread) and the lane code of image_s_kernel /
+// image_adj_kernel.
+// ---------------------------------------------------------------------------------
+namespace {
+
+unsigned long long host_dkey(double x) {
+    unsigned long long b;
+    std::memcpy(&b, &x, 8);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+uint32_t edge_target(const DevModel& m, size_t i) {
+    long long bits;
+    std::memcpy(&bits, &m.edge[i].w, 8);
+    return (uint32_t)bits;
+}
+
+uint32_t bdy_point_closer_host(const DevModel& m, const double* org, const ImagePlane& ip, uint32_t crt) {
+    const double4_32a pc = m.pos[crt];
+    const double Rx = pc.x - org[0], Ry = pc.y - org[1], Rz = pc.z - org[2];
+    const double Zc = dot3_rn(Rx, Ry, Rz, ip.d[0], ip.d[1], ip.d[2]);
+    unsigned long long best = host_dkey(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz) - Zc * Zc);
+    uint32_t besti = 0xffffffffu;
+    const uint32_t nnb = m.n_nb[crt], cum = m.cum_nb[crt];
+    for (uint32_t i = 0; i < nnb; i++) {
+        const double4_32a e = m.edge[cum + i];
+        const uint32_t n = edge_target(m, cum + i);
+        if (m.p2b[n] == m.P) continue;
+        const double Nx = e.x - org[0], Ny = e.y - org[1], Nz = e.z - org[2];
+        const double Zn = dot3_rn(Nx, Ny, Nz, ip.d[0], ip.d[1], ip.d[2]);
+        const unsigned long long k = host_dkey(dot3_rn(Nx, Ny, Nz, Nx, Ny, Nz) - Zn * Zn);
+        if (k < best) {
+            best = k;
+            besti = i;
+        }
+    }
+    return besti == 0xffffffffu ? crt : edge_target(m, cum + besti);
+}
+
+uint32_t pixel_start_host(const DevModel& m, const double* org, const ImagePlane& ip, double& Z) {
+    uint32_t p = ip.start;
+    for (uint32_t it = 0; it < m.P; it++) {
+        const uint32_t q = bdy_point_closer_host(m, org, ip, p);
+        if (q == p) break;
+        p = q;
+    }
+    const double4_32a ps = m.pos[p];
+    Z = dot3_rn(ps.x - org[0], ps.y - org[1], ps.z - org[2], ip.d[0], ip.d[1], ip.d[2]);
+    return p;
+}
+
+int trace_image_host(const DevModel& m, const double* org, const ImagePlane& ip, uint32_t start, double Z,
+                     uint32_t cap, HalfSmem h) {
+    const double dx = ip.d[0], dy = ip.d[1], dz = ip.d[2];
+    uint32_t crt = start;
+    int count = 0;
+    bool accessed = false;
+    while (true) {
+        const uint32_t nnb = m.n_nb[crt], cum = m.cum_nb[crt];
+        const unsigned long long zkey = host_dkey(Z);
+        unsigned long long best = ~0ull;
+        uint32_t besti = 0xffffffffu;
+        double bestZ = 0.0;
+        for (uint32_t i = 0; i < nnb; i++) {
+            const double4_32a e = m.edge[cum + i];
+            const double Rx = e.x - org[0], Ry = e.y - org[1], Rz = e.z - org[2];
+            const double Zn = dot3_rn(Rx, Ry, Rz, dx, dy, dz);
+            if (host_dkey(Zn) > zkey) {
+                const unsigned long long k = host_dkey(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz) - Zn * Zn);
+                if (k < best) {
+                    best = k;
+                    besti = i;
+                    bestZ = Zn;
+                }
+            }
+        }
+        if (besti == 0xffffffffu) break;
+        if ((uint32_t)count >= cap) return -1;
+        const uint32_t nxt = edge_target(m, cum + besti);
+        const double dZl = bestZ - Z;
+        Z = Z + dZl;
+        h.ids[count] = nxt;
+        h.eid[count] = cum + besti;
+        h.dZ[count] = dZl;
+        count++;
+        if (m.p2b[nxt] != m.P) {
+            const double4_32a pn = m.pos[nxt];
+            const double side = dot3_rn(pn.x - ip.center[0], pn.y - ip.center[1], pn.z - ip.center[2], dx, dy, dz);
+            if (!(side < 0.0)) break;
+        } else {
+            accessed = true;
+        }
+        crt = nxt;
+    }
+    if (count > 0 && !accessed) count = 0;
+    for (int s = 0; s < count; s++) {
+        const double4_32a v = m.vel[h.ids[s]];
+        const double sh = 1.0 + dot3_rn(v.x, v.y, v.z, dx, dy, dz);
+        h.shift[s] = sh;
+        h.dsh[s] = (float)(sh - 1.0);
+        h.dzs[s] = (float)h.dZ[s] * m.dz_scale;
+    }
+    return count;
+}
+
+// Pixel rays of the new imager: calls fn(px, start, bk, nb) for every pixel.
+template <class Fn>
+int for_each_pixel(const MgrModelDesc* d, const EmuModel& x, const double* raydir, uint32_t nx, uint32_t ny,
+                   ImagePlane& ip, Fn fn) {
+    const DevModel& m = x.m;
+    std::vector<uint32_t> p2b(m.P);
+    for (uint32_t p = 0; p < m.P; p++) p2b[p] = m.p2b[p];
+    std::vector<double> hx, hy;
+    std::string err;
+    int rc = image_plane_compute(d->position, p2b.data(), m.P, m.B, raydir, nx, ny, ip, hx, hy, err);
+    if (rc != MGR_OK) return rc;
+    HalfBuf b(kCap);
+    HalfSmem bk = b.view();
+    for (uint32_t px = 0; px < nx * ny; px++) {
+        double org[3];
+        if (ip.tilted) {
+            org[0] = hx[px] * ip.ix + hy[px] * ip.jx + ip.scp[0];
+            org[1] = hx[px] * ip.iy + hy[px] * ip.jy + ip.scp[1];
+            org[2] = hy[px] * ip.jz + ip.scp[2];
+        } else {
+            org[0] = hx[px] + ip.scp[0];
+            org[1] = hy[px] + ip.scp[1];
+            org[2] = 0.0 + ip.scp[2];
+        }
+        double Z;
+        const uint32_t start = pixel_start_host(m, org, ip, Z);
+        const double4_32a vs = m.vel[start];
+        const double sh0 = 1.0 + dot3_rn(vs.x, vs.y, vs.z, ip.d[0], ip.d[1], ip.d[2]);
+        bk.shift0 = bk.cshift = sh0;
+        const int nb = trace_image_host(m, org, ip, start, Z, kCap, bk);
+        if (nb < 0) return MGR_ERR_CAPACITY;
+        fn(px, start, bk, nb);
+    }
+    return MGR_OK;
+}
+
+}  // namespace
+
+// Smooth new image I [nx*ny][F] (image_s_kernel's lane code).
+extern "C" int mgr_emu_image_new_smooth(const MgrModelDesc* d, const double* raydir, uint32_t nx, uint32_t ny,
+                                        double* I) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    ImagePlane ip{};
+    return for_each_pixel(d, x, raydir, nx, ny, ip, [&](uint32_t px, uint32_t start, const HalfSmem& bk, int nb) {
+        for (uint32_t f = 0; f < m.F; f++) {
+            uint32_t np;
+            const double nu = m.nu[(size_t)start * m.F + f];
+            I[(size_t)px * m.F + f] = m.approx == APPROX_NONE
+                                          ? image_lane_s<APPROX_NONE>(m, m.sorted_line, start, nu, bk, nb, nullptr, &np)
+                                          : image_lane_s<APPROX_CLOSELINES>(m, m.sorted_line, start, nu, bk, nb, nullptr, &np);
+        }
+    });
+}
+
+// Adjoint of mgr_emu_image_new_smooth (image_adj_kernel's lane code): adds the
+// derivatives of sum(gI * I) into g_em, g_op, g_iw, g_Sp [P][L] and g_vel [P][3].
+extern "C" int mgr_emu_image_new_adjoint(const MgrModelDesc* d, const double* raydir, uint32_t nx, uint32_t ny,
+                                         const double* gI, double* g_em, double* g_op, double* g_iw, double* g_Sp,
+                                         double* g_vel) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    ImagePlane ip{};
+    std::vector<double> scratch;
+    int fail = 0;
+    int rc = for_each_pixel(d, x, raydir, nx, ny, ip, [&](uint32_t px, uint32_t start, const HalfSmem& bk, int nb) {
+        size_t pairs = 1;
+        for (int s = 0; s < nb; s++) pairs += m.nint_all[bk.eid[s]];
+        if (scratch.size() < 3 * pairs) scratch.resize(3 * pairs);
+        const LaneScratch scr{scratch.data(), 1, (uint32_t)pairs};
+        const AdjAcc acc{AdjGrads{g_em, g_op, g_iw, g_Sp, g_vel, {ip.d[0], ip.d[1], ip.d[2]}}, m.L};
+        for (uint32_t f = 0; f < m.F; f++) {
+            const double nu = m.nu[(size_t)start * m.F + f];
+            const double g = gI[(size_t)px * m.F + f];
+            const bool ok = m.approx == APPROX_NONE
+                                ? image_lane_adj<APPROX_NONE>(m, m.sorted_line, start, nu, bk, nb, g, scr, acc)
+                                : image_lane_adj<APPROX_CLOSELINES>(m, m.sorted_line, start, nu, bk, nb, g, scr, acc);
+            if (!ok) fail = 1;
+        }
+    });
+    if (rc == MGR_OK && fail) rc = MGR_ERR_CAPACITY;
+    return rc;
 }

@@ -44,7 +44,7 @@ static cudaError_t upload(MgrModel* m, const T** dst, const T* src, size_t count
     return e;
 }
 
-static int decode_status(int st) {
+int decode_status(int st) {
     if (st & ST_TRACE) {
         set_error("ray left the point cloud on an interior point (neighbour lists or boundary incomplete)");
         return MGR_ERR_TRACE;
@@ -87,8 +87,12 @@ static int ensure_scratch(MgrModel* m, double** p, size_t* have, size_t bytes) {
 // FP32 table scales of split precision (see mgr_scale.h); NULL keeps a scale.
 static void apply_scales(MgrModel* m, const double* em, const double* op) {
     const size_t n = (size_t)m->dm.P * m->dm.L;
-    if (em) m->scales.Ke = pow2_scale_for_max(em, n);
-    if (op) m->scales.Ko = pow2_scale_for_max(op, n);
+    set_line_scales(m, em ? pow2_scale_for_max(em, n) : m->scales.Ke, op ? pow2_scale_for_max(op, n) : m->scales.Ko);
+}
+
+void set_line_scales(MgrModel* m, double Ke, double Ko) {
+    m->scales.Ke = Ke;
+    m->scales.Ko = Ko;
     m->dm.min_op_s = (float)(m->dm.min_opacity * m->scales.Ko);
     m->dm.dz_scale = (float)(1.0 / m->scales.Ko);
     m->dm.s_scale = (float)(m->scales.Ko / m->scales.Ke);

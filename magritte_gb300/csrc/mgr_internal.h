@@ -70,6 +70,10 @@ namespace mgr {
 
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
+// Device status word (ST_* bits) -> MGR_* code with the error message set.
+int decode_status(int st);
+// FP32 line-table scales of split precision (powers of two) and the derived DevModel fields.
+void set_line_scales(MgrModel* m, double Ke, double Ko);
 void count_launch();
 
 // Kernel launchers (mgr_fo2.cu).  All enqueue on model->stream.

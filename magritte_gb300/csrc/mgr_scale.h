@@ -14,14 +14,19 @@ struct LineScales {
     double Ko = 1.0;  // opacity scale
 };
 
+// 2^-e for the largest value mx = f 2^e (f in [0.5, 1)); 1 for no positive finite value.
+inline double pow2_scale_of(double mx) {
+    if (!(mx > 0.0) || !std::isfinite(mx)) return 1.0;
+    int e = 0;
+    std::frexp(mx, &e);
+    return std::ldexp(1.0, -e);
+}
+
 inline double pow2_scale_for_max(const double* a, size_t n) {
     double mx = 0.0;
     for (size_t i = 0; i < n; i++)
         if (a[i] > mx) mx = a[i];
-    if (!(mx > 0.0) || !std::isfinite(mx)) return 1.0;
-    int e = 0;
-    std::frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1)
-    return std::ldexp(1.0, -e);
+    return pow2_scale_of(mx);
 }
 
 // Line-offset tables of split precision, [L][L] row l0:

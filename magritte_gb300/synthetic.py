@@ -292,6 +292,62 @@ def grid_sphere(n: int = 64, box: float = 1.0e13, nside: int = 2, nquads: int = 
         linedata=[ld], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
 
 
+_CUTOUT_CACHE = {}
+
+
+def _sphere_cutout(n: int):
+    """Grid points of the n^3 sphere cutout (radius (n-1)/2 cells about the box
+    centre), their CSR neighbours and the boundary mask, cached per n."""
+    if n not in _CUTOUT_CACHE:
+        g = np.arange(n, dtype=np.float64)
+        c = 0.5 * (n - 1)
+        X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+        keep = np.sqrt((X - c) ** 2 + (Y - c) ** 2 + (Z - c) ** 2) <= 0.5 * (n - 1)
+        _CUTOUT_CACHE[n] = grid_neighbors(keep)
+    return _CUTOUT_CACHE[n]
+
+
+def batch_model(npoints: int, nside: int = 1, nlev: int = 2, nquads: int = 11, seed: int = 0,
+                box: float = 1.0e13, n_h2: float = 1.0e12, abundance: float = 1.0e-4,
+                t_range=(20.0, 100.0), v_turb: float = 150.0, sigma_v: float = 1.0e3) -> RawModel:
+    """One model of the many-model batch: the sphere cutout of an n^3 grid with n
+    chosen so that the cutout has about ``npoints`` points (pi/6 n^3), boundary
+    points those missing a neighbour (CMB), T ~ U(t_range), velocity i.i.d.
+    Gaussian per component, an ``nlev``-level linear rotor (B = 57.6 GHz)."""
+    rng = np.random.default_rng(seed)
+    n = max(4, int(round((6.0 * npoints / np.pi) ** (1.0 / 3.0))))
+    pts, nbs, counts, full = _sphere_cutout(n)
+    dx = box / (n - 1)
+    position = pts.astype(np.float64) * dx
+    P = len(pts)
+    b2p = np.nonzero(~full)[0].astype(np.uint32)
+    temperature = rng.uniform(t_range[0], t_range[1], size=P)
+    velocity = rng.normal(0.0, sigma_v, size=(P, 3)) / CC
+    direction, weight = healpix.uniform_rays(12 * nside * nside)
+    ld = linear_rotor(nlev, 57.6e9, 7.2e-8, 28.0, seed=seed)
+    roots, wts = quadrature(nquads)
+    abund = np.stack([np.full(P, n_h2 * abundance), np.full(P, n_h2)], axis=1)
+    return RawModel(
+        name=f"batch_{n}_{seed}", dimension=3, position=position, velocity=velocity, neighbors=nbs,
+        n_neighbors=counts, boundary2point=b2p, boundary_condition=np.full(len(b2p), BC_CMB, np.int32),
+        boundary_temperature=np.full(len(b2p), T_CMB), ray_direction=direction, ray_weight=weight,
+        abundance=abund, temperature=temperature, vturb2=np.full(P, (v_turb / CC) ** 2),
+        linedata=[ld], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
+
+
+def many_models(n_models: int = 512, p_range=(2000, 60000), seed: int = 0):
+    """Specifications of the many-model batch: point counts log-uniform in p_range,
+    nside in {1, 2} (12 or 48 rays), 2-5 levels, nquads in {11, 21, 31}.  Returns
+    a list of keyword dicts for batch_model."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_models):
+        out.append(dict(npoints=int(np.exp(rng.uniform(np.log(p_range[0]), np.log(p_range[1])))),
+                        nside=int(rng.integers(1, 3)), nlev=int(rng.integers(2, 6)),
+                        nquads=int(rng.choice([11, 21, 31])), seed=seed * 100003 + i))
+    return out
+
+
 def single_ray_1d(npoints: int = 50, dx: float = 1.0e12, nTT: float = 1.0e3, nH2: float = 1.0e12,
                   temp: float = 4.5, turb: float = 0.0, dv: float = 0.0, nquads: int = 1,
                   bc: int = BC_CMB) -> RawModel:

@@ -157,6 +157,12 @@ static inline uint32_t get_n_interp(const OrcModel* m, uint32_t crt, uint32_t nx
     return n > 1 ? n : 1;
 }
 
+/* Smooth mode (test support for gradient checks, off by default): the reference's
+ * single-precision powf / expf / expm1f / erff become their double-precision
+ * counterparts, so that finite differences of the image see a smooth function. */
+static int g_smooth = 0;
+void orc_set_smooth(int on) { g_smooth = on; }
+
 /* interpolate_linear / interpolate_log (solver_interp_helper.tpp:78-99). */
 static inline double interpolate_linear(double f_start, double f_end, double factor) {
     if (factor == 0.0) return f_start;
@@ -166,6 +172,7 @@ static inline double interpolate_linear(double f_start, double f_end, double fac
 static inline double interpolate_log(double f_start, double f_end, double factor) {
     if (factor == 0.0) return f_start;
     if (factor == 1.0) return f_end;
+    if (g_smooth) return f_start * pow(f_end / f_start, factor);
     return f_start * (double)powf((float)(f_end / f_start), (float)factor);
 }
 
@@ -284,11 +291,13 @@ uint32_t orc_ray_lengths_max(const OrcModel* m, int nthreads) {
 /* Solver::gaussian (solver.tpp:1106-1110). */
 static inline double gaussian(double inverse_width, double diff) {
     const double sqrt_exp = inverse_width * diff;
+    if (g_smooth) return inverse_width * INVERSE_SQRT_PI * exp(-sqrt_exp * sqrt_exp);
     return inverse_width * INVERSE_SQRT_PI * (double)expf((float)(-sqrt_exp * sqrt_exp));
 }
 
 /* Solver::planck (solver.tpp:1119-1121). */
 static inline double planck(double temp, double freq) {
+    if (g_smooth) return TWO_HH_OVER_CC_SQUARED * (freq * freq * freq) / expm1(HH_OVER_KB / temp * freq);
     return TWO_HH_OVER_CC_SQUARED * (freq * freq * freq) / (double)expm1f((float)(HH_OVER_KB * freq / temp));
 }
 
@@ -444,8 +453,9 @@ static double compute_dtau_single_line(const OrcModel* m, uint32_t curridx, uint
     const double curr_pos        = (linefreq - curr_freq) * avg_iw;
     const double diff_pos        = next_pos - curr_pos;
     const double average_opacity = (nop + cop) / 2.0;
-    const float  erfdiff         = orc_erff((float)next_pos) - orc_erff((float)curr_pos);
-    const double erfterm         = average_opacity / diff_pos / 2.0 * (double)erfdiff;
+    const double erfdiff         = g_smooth ? erf(next_pos) - erf(curr_pos)
+                                            : (double)(orc_erff((float)next_pos) - orc_erff((float)curr_pos));
+    const double erfterm         = average_opacity / diff_pos / 2.0 * erfdiff;
     return dz * (avg_iw * erfterm + m->min_opacity);
 }
 

@@ -92,6 +92,12 @@ typedef struct {
  * short-characteristics update, (float)exp((double)x) / (float)expm1((double)x). */
 void orc_set_erf_mode(int mode);
 
+/* Smooth arithmetic for gradient checks (0 = off, the default): interpolate_log,
+ * the Gaussian profile, the Planck function and the line-integrated erf difference
+ * use pow / exp / expm1 / erf in double precision instead of the reference's
+ * single-precision calls. */
+void orc_set_smooth(int on);
+
 /* Maximum ray-pair length over all (rr, o), reference Solver::get_ray_lengths_max
  * (solver.tpp:105-126) with get_n_interp over all lines. */
 uint32_t orc_ray_lengths_max(const OrcModel* m, int nthreads);

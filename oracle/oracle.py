@@ -42,8 +42,7 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            build()
+        build()  # make is incremental: rebuilds a library older than its sources
         _lib = C.CDLL(LIB_PATH)
         _declare(_lib)
     return _lib
@@ -223,9 +222,17 @@ def set_erf_mode(mode):
     lib().orc_set_erf_mode(int(mode))
 
 
+def set_smooth(on):
+    """Smooth arithmetic for gradient checks: pow / exp / expm1 / erf in double
+    precision instead of the reference's single-precision calls (off by default)."""
+    lib().orc_set_smooth(int(bool(on)))
+
+
 def _declare(l):
     l.orc_set_erf_mode.restype = None
     l.orc_set_erf_mode.argtypes = [C.c_int]
+    l.orc_set_smooth.restype = None
+    l.orc_set_smooth.argtypes = [C.c_int]
     l.orc_ray_lengths_max.restype = C.c_uint32
     l.orc_ray_lengths_max.argtypes = [C.POINTER(OrcModel), C.c_int]
     l.orc_trace_ray_pair_for_line.restype = C.c_int

@@ -1,0 +1,183 @@
+"""Differentiable new imager on the GPU (mgr_image_new_smooth_device,
+mgr_image_new_adjoint_device, magritte_gb300.adjoint).
+
+* The smooth image equals the emulated lane code (1e-12) and stays within the
+  imager's 1e-5 bar of the oracle's reference arithmetic.
+* The adjoint kernel equals the emulated adjoint (checked against the oracle's
+  finite differences in test_adjoint_emulation.py), entry by entry.
+* End to end through torch.autograd (NewImager): d(loss)/d(velocity, temperature,
+  turbulence, abundance) of a sum of squared image differences over two directions
+  against FP64 central differences of the same forward, along random directions of
+  each sampled point's parameters.  Bar: 1e-4 relative."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+from magritte_gb300 import _abi, build
+from magritte_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+_f64p = C.POINTER(C.c_double)
+
+
+def _p(x):
+    return x.ctypes.data_as(_f64p)
+
+
+def shells_model():
+    raw = S.velocity_gradient_shells(nshells=6)
+    fcen = raw.linedata[0].frequency[0]
+    dd = 1.0e4 / 2.99792458e8
+    return raw, H.setup(raw, max_width_fraction=0.5, image_freqs=(fcen - fcen * dd, fcen + fcen * dd, 9))
+
+
+def sphere_model(approx="CloseLines"):
+    raw = S.grid_sphere(n=12, nside=1, nquads=5)
+    f0 = raw.linedata[0].frequency[1]
+    dd = 8.0e3 / 2.99792458e8
+    return raw, H.setup(raw, approx=approx, image_freqs=(f0 * (1 - dd), f0 * (1 + dd), 37))
+
+
+DIRS = [np.array([0.0, 0.0, 1.0]), np.array([0.3, -0.5, 0.81])]
+
+
+@pytest.fixture(scope="module")
+def emu():
+    lib = C.CDLL(build.build_emu())
+    lib.mgr_emu_image_new_smooth.argtypes = [C.POINTER(_abi.MgrModelDesc), _f64p, C.c_uint32, C.c_uint32, _f64p]
+    lib.mgr_emu_image_new_adjoint.argtypes = [C.POINTER(_abi.MgrModelDesc), _f64p, C.c_uint32, C.c_uint32, _f64p,
+                                              _f64p, _f64p, _f64p, _f64p, _f64p]
+    return lib
+
+
+def gpu_smooth(dev, d, nx, ny):
+    import torch
+    I = torch.empty((nx * ny, dev.F), dtype=torch.float64, device="cuda")
+    dd = np.ascontiguousarray(d, np.float64)
+    _abi._check(_abi.load().mgr_image_new_smooth_device(dev.h, _p(dd), nx, ny, C.c_void_p(I.data_ptr()), None,
+                                                        None))
+    return I.cpu().numpy()
+
+
+def gpu_adjoint(dev, d, nx, ny, gI):
+    import torch
+    P, L = dev.P, dev.L
+    t = {k: torch.zeros((P, L), dtype=torch.float64, device="cuda") for k in ("em", "op", "iw", "Sp")}
+    t["vel"] = torch.zeros((P, 3), dtype=torch.float64, device="cuda")
+    g = torch.tensor(gI, dtype=torch.float64, device="cuda")
+    dd = np.ascontiguousarray(d, np.float64)
+    v = lambda x: C.c_void_p(x.data_ptr())
+    _abi._check(_abi.load().mgr_image_new_adjoint_device(dev.h, _p(dd), nx, ny, v(g), v(t["em"]), v(t["op"]),
+                                                         v(t["iw"]), v(t["Sp"]), v(t["vel"])))
+    return {k: x.cpu().numpy() for k, x in t.items()}
+
+
+@pytest.mark.parametrize("model", ["shells", "sphere", "sphere_none"])
+def test_smooth_image_matches_emulation_and_oracle(gpu_lib, emu, model):
+    raw, a = {"shells": shells_model, "sphere": sphere_model,
+              "sphere_none": lambda: sphere_model("None")}[model]()
+    dev = _abi.DeviceModel(a)
+    try:
+        for d in DIRS:
+            got = gpu_smooth(dev, d, 16, 12)
+            desc, keep = _abi.make_desc(a)
+            ref = np.zeros_like(got)
+            assert emu.mgr_emu_image_new_smooth(C.byref(desc), _p(np.ascontiguousarray(d)), 16, 12, _p(ref)) == 0
+            assert H.max_rel(got, ref, floor=1e-12 * np.abs(ref).max()) < 1e-12
+            O.set_erf_mode(1)
+            try:
+                orc = O.Oracle(a).image_new(d, 16, 12)["I"]
+            finally:
+                O.set_erf_mode(0)
+            assert H.max_rel(got, orc) < 1e-5
+    finally:
+        dev.close()
+
+
+@pytest.mark.parametrize("model", ["shells", "sphere"])
+def test_adjoint_kernel_matches_emulation(gpu_lib, emu, model):
+    raw, a = {"shells": shells_model, "sphere": sphere_model}[model]()
+    dev = _abi.DeviceModel(a)
+    rng = np.random.default_rng(3)
+    try:
+        for d in DIRS:
+            gI = rng.normal(size=(16 * 12, a["nfreqs"]))
+            got = gpu_adjoint(dev, d, 16, 12, gI)
+            desc, keep = _abi.make_desc(a)
+            ref = {k: np.zeros_like(x) for k, x in got.items()}
+            assert emu.mgr_emu_image_new_adjoint(C.byref(desc), _p(np.ascontiguousarray(d)), 16, 12,
+                                                 _p(np.ascontiguousarray(gI)), _p(ref["em"]), _p(ref["op"]),
+                                                 _p(ref["iw"]), _p(ref["Sp"]), _p(ref["vel"])) == 0
+            for k in got:
+                scale = np.abs(ref[k]).max()
+                assert scale > 0, k
+                assert np.abs(got[k] - ref[k]).max() <= 1e-11 * scale, k
+    finally:
+        dev.close()
+
+
+def _core_sphere():
+    from magritte_gb300 import loader
+    raw = S.grid_sphere(n=12, nside=1, nquads=5)
+    f0 = raw.linedata[0].frequency[0]
+    dd = 10.0e3 / 2.99792458e8
+    m = loader.to_core(raw, precision="fp64")
+    m.compute_spectral_discretisation(f0 * (1 - dd), f0 * (1 + dd), 21)
+    m.compute_inverse_line_widths()
+    m.compute_LTE_level_populations()
+    return raw, m
+
+
+def test_autograd_gradients_match_finite_differences(gpu_lib):
+    import torch
+    from magritte_gb300 import adjoint
+
+    raw, model = _core_sphere()
+    imager = adjoint.NewImager(model, 12, 10)
+    dev = dict(dtype=torch.float64, device="cuda")
+    v0 = torch.tensor(raw.velocity, **dev)
+    T0 = torch.tensor(raw.temperature, **dev)
+    vt0 = torch.tensor(raw.vturb2, **dev)
+    ab0 = torch.tensor(raw.abundance, **dev)
+    dirs = [adjoint.inclination_direction(0.0), adjoint.inclination_direction(45.0)]
+    rng = np.random.default_rng(11)
+    with torch.no_grad():
+        targets = [imager(d, v0 * 1.05, T0 * 1.1, vt0, ab0) for d in dirs]
+
+    def loss_of(v, T, vt, ab):
+        return sum(((imager(d, v, T, vt, ab) - t) ** 2).sum() for d, t in zip(dirs, targets))
+
+    params = [t.clone().requires_grad_(True) for t in (v0, T0, vt0, ab0)]
+    loss = loss_of(*params)
+    loss.backward()
+    grads = [p.grad.detach().clone() for p in params]
+    assert all(torch.isfinite(g).all() for g in grads)
+    # points with the largest velocity gradients plus random interior points
+    gv = grads[0].norm(dim=1).cpu().numpy()
+    pts = np.unique(np.concatenate([np.argsort(gv)[-4:], rng.choice(np.nonzero(gv > 1e-3 * gv.max())[0], 4)]))
+    checked = 0
+    for p in pts:
+        # a random direction over the point's velocity (3), T, vturb2 and abundance
+        dirv = [torch.zeros_like(t) for t in params]
+        scale = [1e-4 * v0.abs().max(), 1e-4 * T0[p], 1e-4 * vt0[p], 1e-4 * ab0[p, 0]]
+        u = rng.normal(size=6)
+        dirv[0][p] = torch.tensor(u[:3], **dev) * scale[0]
+        dirv[1][p] = u[3] * scale[1]
+        dirv[2][p] = u[4] * scale[2]
+        dirv[3][p, 0] = u[5] * scale[3]
+        an = sum(float((g * dv).sum()) for g, dv in zip(grads, dirv))
+
+        def central(eps):
+            with torch.no_grad():
+                lp = loss_of(*[t + eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
+                lm = loss_of(*[t - eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
+            return float(lp - lm) / (2 * eps)
+
+        fd = (4.0 * central(0.5) - central(1.0)) / 3.0
+        assert abs(an - fd) <= 1e-4 * abs(fd) + 1e-9 * abs(float(loss)), (p, an, fd)
+        checked += 1
+    assert checked >= 6

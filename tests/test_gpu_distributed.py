@@ -79,13 +79,16 @@ def test_sharded_ali_matches_unsharded(gpu_lib):
         ref_dev.close()
     dev, other = _device(raw, a), _abi.DeviceModel(a)
     R = dev.R
+    tot = raw.abundance[:, raw.linedata[0].num][:, None]
     calls = []
 
     def reduce(J_ptr, nJ, lam_ptr, nlam, stream_ptr):
         s = torch.cuda.ExternalStream(stream_ptr)
         s.synchronize()
+        # the line data and interpolation criterion (opacity / population_tot) the
+        # shard's solve used
         em, op = dev.line_data()
-        other.set_line_data(emissivity=em, opacity=op)
+        other.set_line_data(emissivity=em, opacity=op, interp_criterion=op / tot)
         part = other.formal_solve_fo2_rays(R // 2, R, "fp64")
         with torch.cuda.stream(s):
             J = torch.as_tensor(distributed._DeviceArray(J_ptr, nJ), device="cuda")
@@ -99,7 +102,6 @@ def test_sharded_ali_matches_unsharded(gpu_lib):
         got = dev.compute_level_populations("fp64", use_ng=True, max_it=12)
         assert got["iterations"] == ref["iterations"]
         assert len(calls) >= got["iterations"] - 2  # one per normal (non-Ng) iteration
-        tot = raw.abundance[:, raw.linedata[0].num][:, None]
         assert _rel(dev.populations(0), ref_pop, 1e-10 * tot) < 1e-9
         # restore the unsharded loop
         dev.set_ray_shard(0, R)
