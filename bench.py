@@ -57,6 +57,10 @@ def parse():
     p.add_argument("--no-batch", action="store_true", help="skip the many-model batch leg")
     p.add_argument("--batch-models", type=int, default=512)
     p.add_argument("--batch-steps", type=int, default=1)
+    p.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-imager leg")
+    p.add_argument("--adjoint-points", type=int, default=100_000)
+    p.add_argument("--adjoint-pixels", type=int, default=256)
+    p.add_argument("--adjoint-fd-points", type=int, default=64)
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the library's default launch shape (for profiling one production launch)")
     return p.parse_args()
@@ -310,6 +314,95 @@ def run_batch(args):
             "setup_s": setup_s, "precision": args.precision}
 
 
+def run_adjoint(args):
+    """Differentiable new imager: the non-LTE sphere family at 100k points (LTE level
+    populations), images of 256 x 256 pixels at inclinations 0, 45 and 90 degrees
+    over 41 frequencies spanning +-20 km/s about the J=1-0 line; loss = sum of
+    squared differences to the images of perturbed fields (velocity x (1 + 0.05 N),
+    temperature x 1.1); gradients with respect to velocity, temperature, turbulence
+    and abundance; checked against FP64 central differences (Richardson-extrapolated)
+    along a random direction of each of 64 random points' parameters."""
+    import numpy as np
+    import torch
+    from magritte_gb300 import adjoint, loader, synthetic
+
+    t_setup = time.perf_counter()
+    raw = synthetic.nlte_sphere(npoints=args.adjoint_points, nside=1)
+    f0 = raw.linedata[0].frequency[0]
+    dd = 20.0e3 / 2.99792458e8
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation(f0 * (1 - dd), f0 * (1 + dd), 41)
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    npx = args.adjoint_pixels
+    imager = adjoint.NewImager(model, npx, npx)
+    setup_s = time.perf_counter() - t_setup
+    dev = dict(dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(0)
+    v0 = torch.tensor(raw.velocity, **dev)
+    T0 = torch.tensor(raw.temperature, **dev)
+    vt0 = torch.tensor(raw.vturb2, **dev)
+    ab0 = torch.tensor(raw.abundance, **dev)
+    dirs = [adjoint.inclination_direction(a) for a in (0.0, 45.0, 90.0)]
+    with torch.no_grad():
+        vt = v0 * (1.0 + 0.05 * torch.tensor(rng.normal(size=(raw.npoints, 1)), **dev))
+        targets = [imager(d, vt, T0 * 1.10, vt0, ab0) for d in dirs]
+
+    def loss_of(v, T, vtu, ab):
+        return sum(((imager(d, v, T, vtu, ab) - t) ** 2).sum() for d, t in zip(dirs, targets))
+
+    # warm-up, then timed forward and forward + backward
+    params = [t.clone().requires_grad_(True) for t in (v0, T0, vt0, ab0)]
+    loss_of(*params).backward()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.no_grad():
+        loss_of(v0, T0, vt0, ab0)
+    torch.cuda.synchronize()
+    fwd_s = time.perf_counter() - t0
+    params = [t.clone().requires_grad_(True) for t in (v0, T0, vt0, ab0)]
+    t0 = time.perf_counter()
+    loss = loss_of(*params)
+    loss.backward()
+    torch.cuda.synchronize()
+    fb_s = time.perf_counter() - t0
+    grads = [p.grad.detach() for p in params]
+    # finite-difference check on random interior points
+    interior = np.setdiff1d(np.arange(raw.npoints), raw.boundary2point)
+    pts = rng.choice(interior, size=min(args.adjoint_fd_points, len(interior)), replace=False)
+    errs, t_fd = [], time.perf_counter()
+    for p in pts:
+        dirv = [torch.zeros_like(t) for t in (v0, T0, vt0, ab0)]
+        u = rng.normal(size=6)
+        dirv[0][p] = torch.tensor(u[:3], **dev) * 1e-4 * v0.abs().max()
+        dirv[1][p] = u[3] * 1e-4 * T0[p]
+        dirv[2][p] = u[4] * 1e-4 * vt0[p]
+        dirv[3][p, 0] = u[5] * 1e-4 * ab0[p, 0]
+        an = sum(float((g * dv).sum()) for g, dv in zip(grads, dirv))
+
+        def central(eps):
+            with torch.no_grad():
+                lp = loss_of(*[t + eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
+                lm = loss_of(*[t - eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
+            return float(lp - lm) / (2 * eps)
+
+        fd = (4.0 * central(0.5) - central(1.0)) / 3.0
+        if fd != 0.0:
+            errs.append(abs(an - fd) / abs(fd))
+    fd_s = time.perf_counter() - t_fd
+    solves = float(npx * npx * 41 * len(dirs))
+    return {"workload": f"nlte_sphere {raw.npoints} points (LTE), {npx}x{npx} pixels x 41 frequencies "
+                        f"(+-20 km/s), inclinations 0/45/90 deg",
+            "forward_s": fwd_s, "forward_backward_s": fb_s,
+            "forward_pixel_freq_solves_per_s": solves / fwd_s,
+            "forward_backward_pixel_freq_solves_per_s": solves / fb_s,
+            "fd_check": {"points": len(errs), "max_rel_err": max(errs) if errs else None,
+                         "median_rel_err": float(np.median(errs)) if errs else None, "bar": 1e-4,
+                         "method": "Richardson-extrapolated central differences along a random direction of "
+                                   "each point's (v_x, v_y, v_z, T, vturb2, abundance)", "s": fd_s},
+            "setup_s": setup_s, "loss": float(loss)}
+
+
 def C_void(x):
     import ctypes as C
     return C.c_void_p(x)
@@ -503,6 +596,7 @@ def run_ours(args, rank, ws):
         return
     ali = None if args.no_ali else run_ali(args)
     batch = None if args.no_batch else run_batch(args)
+    adj = None if args.no_adjoint else run_adjoint(args)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(raw, os.cpu_count() or 1)
@@ -533,6 +627,7 @@ def run_ours(args, rank, ws):
         "tuning": tuning,
         "ali": ali,
         "batch": batch,
+        "adjoint": adj,
     }
     print(json.dumps(line), flush=True)
 

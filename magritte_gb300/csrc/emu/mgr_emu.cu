@@ -76,7 +76,7 @@ struct EmuModel {
     std::vector<double> ub, Sp;
     std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f;
     std::vector<uint16_t> nint, nint_all;
-    std::vector<uint32_t> lq2f;
+    std::vector<uint32_t> lq2f, corr_line;
     DevModel m{};
 };
 
@@ -145,9 +145,28 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     line_offset_tables(d->line, d->sorted_line, L, x.dls, x.dll);
     m.dls = x.dls.data();
     m.dll = x.dll.data();
+    // the maps of an imaging spectral discretisation are unset: keep only valid
+    // (line, quadrature point) entries, and measure each frequency from its nearest
+    // line, as mgr_model_create does
     x.lq2f.assign((size_t)L * d->nquads, 0xffffffffu);
-    for (uint32_t f = 0; f < F; f++) x.lq2f[(size_t)d->corr_line[f] * d->nquads + d->corr_z[f]] = f;
+    for (uint32_t f = 0; f < F; f++)
+        if (d->corr_line[f] < L && d->corr_z[f] < d->nquads) x.lq2f[(size_t)d->corr_line[f] * d->nquads + d->corr_z[f]] = f;
     m.lq2f = x.lq2f.data();
+    bool line_disc = (F == L * d->nquads);
+    for (uint32_t f = 0; f < F && line_disc; f++)
+        if (d->corr_line[f] >= L || d->corr_lspec[f] >= d->nlspecs || d->corr_z[f] >= d->nquads) line_disc = false;
+    x.corr_line.resize(F);
+    for (uint32_t f = 0; f < F; f++) {
+        uint32_t best = 0;
+        if (line_disc) {
+            best = d->corr_line[f];
+        } else {
+            for (uint32_t l = 1; l < L; l++)
+                if (std::fabs(d->nu[f] - d->line[l]) < std::fabs(d->nu[f] - d->line[best])) best = l;
+        }
+        x.corr_line[f] = best;
+    }
+    m.corr_line = x.corr_line.data();
     x.nint.resize((E ? E : 1) * (size_t)L);
     for (uint32_t p = 0; p < P; p++)
         for (uint32_t k = 0; k < d->n_neighbors[p]; k++)

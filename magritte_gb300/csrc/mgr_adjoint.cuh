@@ -5,7 +5,8 @@
 // The forward follows image_lane's FP64 arithmetic with the reference's single-
 // precision library calls replaced by their FP64 counterparts (exp in the Gaussian
 // profile, pow in the logarithmic interpolation, erf in the line-integrated optical
-// depth, expm1 in the Planck function), so that the image is a smooth function of
+// depth - as a difference of erfc where both arguments have the same sign, free of
+// cancellation - and expm1 in the Planck function), so that the image is a smooth function of
 // the per-point line data and velocities.  The ray trace, the interpolation points,
 // the CloseLines brackets, the large-shift branch and the dtau clamp are held fixed
 // (trace-fixed differentiation): they are piecewise constant in the inputs.
@@ -33,6 +34,14 @@ MGR_HD double ilog_s(double a, double b, double f) {
     if (f == 0.0) return a;
     if (f == 1.0) return b;
     return a * pow(b / a, f);
+}
+
+// erf(a) - erf(b) without cancellation when a and b lie on the same side of 0
+// (differences of erfc there, which keeps its relative precision in the wings).
+MGR_HD double erf_diff_s(double a, double b) {
+    if (a > 0.0 && b > 0.0) return erfc(b) - erfc(a);
+    if (a < 0.0 && b < 0.0) return erfc(-a) - erfc(-b);
+    return erf(a) - erf(b);
 }
 
 // Boundary intensity at `freq` (boundary_intensity) and its derivative in freq.
@@ -213,7 +222,7 @@ MGR_HD double ld_s(const DevModel& m, const Elem& lo, const Elem& hi, uint32_t l
     const double next_pos = (linefreq - nf) * avg_iw;
     const double curr_pos = (linefreq - cf) * avg_iw;
     const double diff_pos = next_pos - curr_pos;
-    const double erfterm = (nop + cop) / 2.0 / diff_pos / 2.0 * (erf(next_pos) - erf(curr_pos));
+    const double erfterm = (nop + cop) / 2.0 / diff_pos / 2.0 * erf_diff_s(next_pos, curr_pos);
     return dz * (avg_iw * erfterm + m.min_opacity);
 }
 
@@ -248,7 +257,7 @@ MGR_HD LdAdj ld_s_adj(const DevModel& m, const Elem& lo, const Elem& hi, uint32_
     const double cp = (linefreq - cf) * avg;
     const double dp = np - cp;
     const double avg_op = (nop + cop) / 2.0;
-    const double E = erf(np) - erf(cp);
+    const double E = erf_diff_s(np, cp);
     const double erfterm = avg_op / dp / 2.0 * E;
     const double g_erfterm = gld * dz * avg;
     double gavg = gld * dz * erfterm;

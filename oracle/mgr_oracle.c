@@ -433,6 +433,14 @@ static inline float orc_erff(float x) { return g_erf_mode ? (float)erf((double)x
 static inline float orc_expf_sc(float x) { return g_erf_mode ? (float)exp((double)x) : expf(x); }
 static inline float orc_expm1f_sc(float x) { return g_erf_mode ? (float)expm1((double)x) : expm1f(x); }
 
+/* Smooth mode: erf(a) - erf(b) in double precision, as a difference of erfc when a
+ * and b have the same sign (no cancellation in the line wings). */
+static inline double orc_erf_diff(double a, double b) {
+    if (a > 0.0 && b > 0.0) return erfc(b) - erfc(a);
+    if (a < 0.0 && b < 0.0) return erfc(-a) - erfc(-b);
+    return erf(a) - erf(b);
+}
+
 /* Solver::compute_dtau_single_line (solver.tpp:2374-2455). */
 static double compute_dtau_single_line(const OrcModel* m, uint32_t curridx, uint32_t nextidx,
                                        uint32_t ci, uint32_t ni, uint32_t l, double curr_freq,
@@ -453,7 +461,7 @@ static double compute_dtau_single_line(const OrcModel* m, uint32_t curridx, uint
     const double curr_pos        = (linefreq - curr_freq) * avg_iw;
     const double diff_pos        = next_pos - curr_pos;
     const double average_opacity = (nop + cop) / 2.0;
-    const double erfdiff         = g_smooth ? erf(next_pos) - erf(curr_pos)
+    const double erfdiff         = g_smooth ? orc_erf_diff(next_pos, curr_pos)
                                             : (double)(orc_erff((float)next_pos) - orc_erff((float)curr_pos));
     const double erfterm         = average_opacity / diff_pos / 2.0 * erfdiff;
     return dz * (avg_iw * erfterm + m->min_opacity);

@@ -95,7 +95,8 @@ void orc_set_erf_mode(int mode);
 /* Smooth arithmetic for gradient checks (0 = off, the default): interpolate_log,
  * the Gaussian profile, the Planck function and the line-integrated erf difference
  * use pow / exp / expm1 / erf in double precision instead of the reference's
- * single-precision calls. */
+ * single-precision calls (the erf difference as a difference of erfc where both
+ * arguments have the same sign). */
 void orc_set_smooth(int on);
 
 /* Maximum ray-pair length over all (rr, o), reference Solver::get_ray_lengths_max
