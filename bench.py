@@ -370,7 +370,7 @@ def run_adjoint(args):
     # finite-difference check on random interior points
     interior = np.setdiff1d(np.arange(raw.npoints), raw.boundary2point)
     pts = rng.choice(interior, size=min(args.adjoint_fd_points, len(interior)), replace=False)
-    errs, t_fd = [], time.perf_counter()
+    errs, flips, t_fd = [], 0, time.perf_counter()
     for p in pts:
         dirv = [torch.zeros_like(t) for t in (v0, T0, vt0, ab0)]
         u = rng.normal(size=6)
@@ -386,8 +386,14 @@ def run_adjoint(args):
                 lm = loss_of(*[t - eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
             return float(lp - lm) / (2 * eps)
 
-        fd = (4.0 * central(0.5) - central(1.0)) / 3.0
-        if fd != 0.0:
+        c1, c2 = central(1.0), central(0.5)
+        fd = (4.0 * c2 - c1) / 3.0
+        if abs(c1 - c2) > 1e-3 * abs(c2):
+            # the two steps disagree: the perturbation crossed a branch of the held
+            # structure (large-shift test, line bracket), where the trace-fixed
+            # derivative and the differences of the full forward part ways
+            flips += 1
+        elif fd != 0.0:
             errs.append(abs(an - fd) / abs(fd))
     fd_s = time.perf_counter() - t_fd
     solves = float(npx * npx * 41 * len(dirs))
@@ -396,7 +402,8 @@ def run_adjoint(args):
             "forward_s": fwd_s, "forward_backward_s": fb_s,
             "forward_pixel_freq_solves_per_s": solves / fwd_s,
             "forward_backward_pixel_freq_solves_per_s": solves / fb_s,
-            "fd_check": {"points": len(errs), "max_rel_err": max(errs) if errs else None,
+            "fd_check": {"points": len(errs), "branch_crossings_skipped": flips,
+                         "max_rel_err": max(errs) if errs else None,
                          "median_rel_err": float(np.median(errs)) if errs else None, "bar": 1e-4,
                          "method": "Richardson-extrapolated central differences along a random direction of "
                                    "each point's (v_x, v_y, v_z, T, vturb2, abundance)", "s": fd_s},

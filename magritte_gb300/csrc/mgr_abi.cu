@@ -146,6 +146,7 @@ void mgr_model_free(MgrModel* model) {
     if (model->u_scratch) cudaFree(model->u_scratch);
     if (model->lam_scratch) cudaFree(model->lam_scratch);
     if (model->work) cudaFree(model->work);
+    if (model->adj_scratch) cudaFree(model->adj_scratch);
     ali_free(model);
     if (model->stream) cudaStreamDestroy(model->stream);
     delete model;

@@ -335,21 +335,27 @@ int mgr_image_new_adjoint_device(MgrModel* model, const double* raydir, uint32_t
     cudaFree(dmax);
     if (pairs < 1) pairs = 1;
     AdjGrads g{g_em_dev, g_op_dev, g_iw_dev, g_Sp_dev, g_vel_dev, {ip.d[0], ip.d[1], ip.d[2]}};
-    double* scratch = nullptr;
     auto run = [&](auto kern) -> cudaError_t {
         cudaError_t r = pixel_launch_shape(model, kern, cap, npix, &nw, &smem, &grid);
         if (r != cudaSuccess) return r;
-        r = cudaMalloc(&scratch, (size_t)grid * nw * pairs * 3 * 32 * sizeof(double));
-        if (r != cudaSuccess) return r;
+        const size_t need = (size_t)grid * nw * pairs * 3 * 32 * sizeof(double);
+        if (model->adj_scratch_bytes < need) {  // grown on demand, kept for the next call
+            cudaFree(model->adj_scratch);
+            model->adj_scratch = nullptr;
+            model->adj_scratch_bytes = 0;
+            r = cudaMalloc(&model->adj_scratch, need);
+            if (r != cudaSuccess) return r;
+            model->adj_scratch_bytes = need;
+        }
         count_launch();
-        kern<<<grid, nw * 32, smem, model->stream>>>(model->dm, ip, cap, gI_dev, g, scratch, pairs, model->status);
+        kern<<<grid, nw * 32, smem, model->stream>>>(model->dm, ip, cap, gI_dev, g, model->adj_scratch, pairs,
+                                                     model->status);
         return cudaGetLastError();
     };
     if (e == cudaSuccess)
         e = (model->dm.approx == APPROX_CLOSELINES) ? run(image_adj_kernel<APPROX_CLOSELINES>)
                                                      : run(image_adj_kernel<APPROX_NONE>);
     rc = finish(model, e, "mgr_image_new_adjoint_device");
-    cudaFree(scratch);
     cudaFree(dxy);
     return rc;
 }

@@ -434,19 +434,17 @@ MGR_HD double image_lane_s(const DevModel& m, const double* sl, uint32_t o, doub
         const PairS ps = pair_s<AP>(m, sl, nu, prev, cur, prev.dzin);
         const double dt = ps.dtau;
         if (k == 0) {
-            const double inv = 1.0 / dt;
-            const double Cb = 2.0 * inv * inv;
-            const double Bmc = 1.0 + 2.0 * inv;
-            const double Bb = Bmc + Cb;
-            Su = (ps.Slo + 2.0 * Ib * inv) / Bb;
-            F = 0.5 * Bmc * dt * dt;
+            // first row, Su = (S + 2 Ib/dt) / (1 + 2/dt + 2/dt^2) and F = (1 + 2/dt) dt^2/2,
+            // multiplied through by dt^2/2 (no 1/dt: well conditioned for thin pairs)
+            const double h = dt * (0.5 * dt + 1.0);
+            F = h;
+            Su = (ps.Slo * (0.5 * dt * dt) + Ib * dt) / (1.0 + h);
         } else {
-            const double avg = 0.5 * (dt_prev + dt);
-            const double A = 1.0 / (avg * dt_prev);
-            const double iC = avg * dt;
-            const double FI = 1.0 / (1.0 + F);
-            F = (A * F * FI + 1.0) * iC;
-            Su = (A * Su + ps.Slo) * (1.0 / (1.0 + F)) * iC;
+            // elimination row with q = A iC = dt / dt_prev
+            const double q = dt / dt_prev;
+            const double iC = 0.5 * (dt_prev + dt) * dt;
+            F = q * (F / (1.0 + F)) + iC;
+            Su = (q * Su + ps.Slo * iC) / (1.0 + F);
         }
         if (scr) {
             if (k >= scr->cap) {
@@ -463,14 +461,12 @@ MGR_HD double image_lane_s(const DevModel& m, const double* sl, uint32_t o, doub
         k++;
     }
     *npairs = k;
+    // last row, u = (Al Su + Sl)(1 + F) / (Bl F + Bl - Al) times dt^2/2 over dt^2/2
     const double Ibl = bdy_s(m, o, nu * cen.shift, dummy);
-    const double inv = 1.0 / dt_prev;
-    const double Al = 2.0 * inv * inv;
-    const double Blm = 1.0 + 2.0 * inv;
-    const double Bl = Blm + Al;
-    const double den = 1.0 / (Bl * F + Blm);
-    const double Sl = S_last + 2.0 * Ibl * inv;
-    const double u = (Al * Su + Sl) * (1.0 + F) * den;
+    const double e = dt_prev;
+    const double h = e * (0.5 * e + 1.0);
+    const double N = Su + S_last * (0.5 * e * e) + Ibl * e;
+    const double u = N * (1.0 + F) / (F + (1.0 + F) * h);
     return 2.0 * u - bdy_s(m, o, nu, dummy);
 }
 
@@ -491,18 +487,14 @@ MGR_HD bool image_lane_adj(const DevModel& m, const double* sl, uint32_t o, doub
     if (nb <= 0) return true;  // I = B(nu) of the start point: no dependence
     const Elem cen = centre_elem(o, bk.cshift);
     double dummy, dB;
-    // ---- end of the ray: u = (Al Su + Sl)(1 + F) / (Bl F + Blm), I = 2 u - B(nu) ----
+    // ---- end of the ray: u = N (1 + F) / (F + (1 + F) h), I = 2 u - B(nu) ----
     const double F_last = scr.at(M - 1, 0), Su_last = scr.at(M - 1, 1), dtl = scr.at(M - 1, 2);
     const double Ibl = bdy_s(m, o, nu * cen.shift, dB);
-    const double invl = 1.0 / dtl;
-    const double Al = 2.0 * invl * invl;
-    const double Blm = 1.0 + 2.0 * invl;
-    const double Bl = Blm + Al;
-    const double D = Bl * F_last + Blm;
-    const double den = 1.0 / D;
+    const double hl = dtl * (0.5 * dtl + 1.0);
+    const double Dn = F_last + (1.0 + F_last) * hl;
     const double gu = 2.0 * gI;
-    // adjoints of the elimination state (F, FI, Su) after the current pair and of its dtau
-    double gF = 0.0, gFI = 0.0, gSu = 0.0, gdt = 0.0;
+    // adjoints of the state (F, Su) after the current pair and of its dtau
+    double gF = 0.0, gSu = 0.0, gdt = 0.0;
     // Pairs in reverse: pair k joins element k (outer) and k + 1 (inner, the start point
     // for the last pair).  The last pair comes first; its Shi is the S_last of the end.
     ElemIter it;
@@ -517,121 +509,77 @@ MGR_HD bool image_lane_adj(const DevModel& m, const double* sl, uint32_t o, doub
         const PairS ps = pair_s<AP>(m, sl, nu, outer, inner, dz);
         double gSlo = 0.0, gShi = 0.0;
         if (kk == M - 1) {
-            const double Sl = ps.Shi + 2.0 * Ibl * invl;
-            const double X = Al * Su_last + Sl;
-            const double Y = 1.0 + F_last;
-            const double gX = gu * Y * den, gY = gu * X * den, gden = gu * X * Y;
-            gF += gY;
-            const double gD = -gden * den * den;
-            gF += gD * Bl;
-            double gBl = gD * F_last, gBlm = gD;
-            gSu += gX * Al;
-            double gAl = gX * Su_last;
-            const double gSl = gX;
-            gShi = gSl;
-            const double gIbl = gSl * 2.0 * invl;
-            double ginv = gSl * 2.0 * Ibl;
-            gBlm += gBl;
-            gAl += gBl;
-            ginv += gAl * 4.0 * invl;
-            ginv += 2.0 * gBlm;
-            gdt += -ginv * invl * invl;
-            // Ibl = B(nu shift(start))
-            acc.add_shift(o, gIbl * dB * nu);
+            const double N = Su_last + ps.Shi * (0.5 * dtl * dtl) + Ibl * dtl;
+            const double u = N * (1.0 + F_last) / Dn;
+            const double gN = gu * (1.0 + F_last) / Dn;
+            gF += gu * (N - u * (1.0 + hl)) / Dn;
+            const double gh = -gu * u * (1.0 + F_last) / Dn;
+            gSu += gN;
+            gShi = gN * (0.5 * dtl * dtl);
+            const double gIbl = gN * dtl;
+            gdt += gN * (ps.Shi * dtl + Ibl) + gh * (dtl + 1.0);
+            acc.add_shift(o, gIbl * dB * nu);  // Ibl = B(nu shift(start))
         }
         const double dt = ps.dtau;
+        double g_dt_k;
+        double g_sh_o = 0.0, g_sh_i = g_sh_inner_carry;
         if (kk > 0) {
-            // pair kk: F_k = (A F' FI' + 1) iC, FI_k = 1/(1+F_k), Su_k = (A Su' + S) FI_k iC
+            // pair kk: F_k = q G' + iC, Su_k = Z / (1 + F_k), G' = F'/(1 + F'),
+            // Z = q Su' + S iC, q = dt / dto, iC = (dto + dt) dt / 2
             const double Fp = scr.at(kk - 1, 0), Sup = scr.at(kk - 1, 1), dto = scr.at(kk - 1, 2);
-            const double FIp = 1.0 / (1.0 + Fp);
-            const double avg = 0.5 * (dto + dt);
-            const double iA = avg * dto, iC = avg * dt;
-            const double A = 1.0 / iA;
             const double Fk = scr.at(kk, 0);
+            const double q = dt / dto;
+            const double iC = 0.5 * (dto + dt) * dt;
+            const double FIp = 1.0 / (1.0 + Fp);
+            const double G = Fp * FIp;
             const double FIk = 1.0 / (1.0 + Fk);
-            const double Z = A * Sup + ps.Slo;
-            const double W = A * Fp * FIp + 1.0;
-            // Su_k
-            const double gZ = gSu * FIk * iC;
-            gFI += gSu * Z * iC;
-            double giC = gSu * Z * FIk;
-            double gA = gZ * Sup;
-            const double gSup = gZ * A;
-            gSlo = gZ;
-            // FI_k
-            gF += -gFI * FIk * FIk;
-            // F_k
-            const double gW = gF * iC;
-            giC += gF * W;
-            gA += gW * Fp * FIp;
-            const double gFp = gW * A * FIp;
-            const double gFIp = gW * A * Fp;
-            const double giA = -gA * A * A;
-            const double gavg = giA * dto + giC * dt;
-            const double gdto = giA * avg + 0.5 * gavg;
-            gdt += giC * avg + 0.5 * gavg;
+            const double Z = q * Sup + ps.Slo * iC;
+            const double gZ = gSu * FIk;
+            const double gFt = gF - gSu * Z * FIk * FIk;
+            const double gq = gFt * G + gZ * Sup;
+            const double giC = gFt + gZ * ps.Slo;
+            gSlo = gZ * iC;
+            g_dt_k = gdt + gq / dto + giC * (0.5 * dto + dt);
             // hand the state adjoint to pair kk - 1
-            gF = gFp;
-            gFI = gFIp;
-            gSu = gSup;
-            // pair kk's dtau is complete: propagate it with gSlo / gShi below
-            const double g_dt_k = gdt;
-            gdt = gdto;
-            // ---- pair adjoint ----
-            double g_sh_o = 0.0, g_sh_i = g_sh_inner_carry;
-            if (ps.large) {
-                pair_large_adj<AP>(m, sl, nu, outer, inner, dz, ps, g_dt_k, gSlo, gShi, acc, g_sh_o, g_sh_i);
-                // the inner element's eta/chi adjoint from the pair outside it is complete
-                if (have_carry) elem_s_adj<AP>(m, sl, nu, inner, carry_eta, carry_chi, acc, g_sh_i);
-                carry_eta = carry_chi = 0.0;
-                have_carry = false;
-            } else {
-                const double ce = carry_eta + gShi / ps.chi_i;
-                const double cc = carry_chi + 0.5 * dz * g_dt_k - gShi * ps.Shi / ps.chi_i;
-                elem_s_adj<AP>(m, sl, nu, inner, ce, cc, acc, g_sh_i);
-                carry_eta = gSlo / ps.chi_o;
-                carry_chi = 0.5 * dz * g_dt_k - gSlo * ps.Slo / ps.chi_o;
-                have_carry = true;
-            }
-            elem_shift_adj(inner, g_sh_i, acc);
-            g_sh_inner_carry = g_sh_o;
+            gF = gFt * q * FIp * FIp;
+            gSu = gZ * q;
+            gdt = -gq * q / dto + giC * 0.5 * dt;
         } else {
-            // pair 0: F_0 = 0.5 Bmc dt^2, Su_0 = (S0 + 2 Ib inv) / Bb
-            const double F0 = scr.at(0, 0), Su0 = scr.at(0, 1);
-            const double FI0 = 1.0 / (1.0 + F0);
-            gF += -gFI * FI0 * FI0;
-            const double inv = 1.0 / dt;
-            const double Cb = 2.0 * inv * inv;
-            const double Bmc = 1.0 + 2.0 * inv;
-            const double Bb = Bmc + Cb;
+            // pair 0: F_0 = h, Su_0 = N0 / (1 + h), N0 = S0 dt^2/2 + Ib dt, h = dt (dt/2 + 1)
             double dBf;
             const double Ib = bdy_s(m, outer.nr, nu * outer.shift, dBf);
-            double gBmc = gF * 0.5 * dt * dt;
-            gdt += gF * Bmc * dt;
-            const double gN = gSu / Bb;
-            const double gBb = -gSu * Su0 / Bb;
-            gSlo = gN;
-            const double gIb = gN * 2.0 * inv;
-            double ginv = gN * 2.0 * Ib;
-            gBmc += gBb;
-            const double gCb = gBb;
-            ginv += gCb * 4.0 * inv;
-            ginv += 2.0 * gBmc;
-            gdt += -ginv * inv * inv;
-            double g_sh_o = gIb * dBf * nu, g_sh_i = g_sh_inner_carry;
-            if (ps.large) {
-                pair_large_adj<AP>(m, sl, nu, outer, inner, dz, ps, gdt, gSlo, gShi, acc, g_sh_o, g_sh_i);
-                if (have_carry) elem_s_adj<AP>(m, sl, nu, inner, carry_eta, carry_chi, acc, g_sh_i);
-            } else {
-                const double ce = carry_eta + gShi / ps.chi_i;
-                const double cc = carry_chi + 0.5 * dz * gdt - gShi * ps.Shi / ps.chi_i;
-                elem_s_adj<AP>(m, sl, nu, inner, ce, cc, acc, g_sh_i);
-                elem_s_adj<AP>(m, sl, nu, outer, gSlo / ps.chi_o, 0.5 * dz * gdt - gSlo * ps.Slo / ps.chi_o, acc,
-                               g_sh_o);
-            }
-            elem_shift_adj(inner, g_sh_i, acc);
+            const double h = dt * (0.5 * dt + 1.0);
+            const double FI0 = 1.0 / (1.0 + h);
+            const double N0 = ps.Slo * (0.5 * dt * dt) + Ib * dt;
+            const double gN0 = gSu * FI0;
+            const double gh = gF - gSu * N0 * FI0 * FI0;
+            gSlo = gN0 * (0.5 * dt * dt);
+            const double gIb = gN0 * dt;
+            g_dt_k = gdt + gN0 * (ps.Slo * dt + Ib) + gh * (dt + 1.0);
+            g_sh_o = gIb * dBf * nu;
+        }
+        // ---- pair adjoint ----
+        if (ps.large) {
+            pair_large_adj<AP>(m, sl, nu, outer, inner, dz, ps, g_dt_k, gSlo, gShi, acc, g_sh_o, g_sh_i);
+            // the inner element's eta/chi adjoint from the pair outside it is complete
+            if (have_carry) elem_s_adj<AP>(m, sl, nu, inner, carry_eta, carry_chi, acc, g_sh_i);
+            carry_eta = carry_chi = 0.0;
+            have_carry = false;
+        } else {
+            const double ce = carry_eta + gShi / ps.chi_i;
+            const double cc = carry_chi + 0.5 * dz * g_dt_k - gShi * ps.Shi / ps.chi_i;
+            elem_s_adj<AP>(m, sl, nu, inner, ce, cc, acc, g_sh_i);
+            carry_eta = gSlo / ps.chi_o;
+            carry_chi = 0.5 * dz * g_dt_k - gSlo * ps.Slo / ps.chi_o;
+            have_carry = true;
+        }
+        elem_shift_adj(inner, g_sh_i, acc);
+        if (kk == 0) {
+            // element 0 (the far end) is complete
+            if (have_carry) elem_s_adj<AP>(m, sl, nu, outer, carry_eta, carry_chi, acc, g_sh_o);
             elem_shift_adj(outer, g_sh_o, acc);
         }
+        g_sh_inner_carry = g_sh_o;
         inner = outer;
     }
     (void)dummy;

@@ -50,10 +50,14 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Per-warp shared memory: sorted line centres [L_max], J accumulators [F_max], the
-// current ray pair's ALO diagonal factors [F_max], then the two trace halves.
+// current ray pair's L_diag values [F_max], the origin's ray-independent ALO factors
+// [F_max] (LambdaFactors), then the two trace halves.
+__host__ __device__ inline size_t batch_head_bytes(uint32_t F_max, uint32_t L_max) {
+    const size_t head = ((size_t)L_max + 2 * (size_t)F_max) * 8 + (size_t)F_max * sizeof(LambdaFactors);
+    return (head + 15) & ~size_t(15);
+}
 __host__ __device__ inline size_t batch_warp_bytes(uint32_t cap, uint32_t F_max, uint32_t L_max) {
-    const size_t head = ((size_t)L_max + 2 * (size_t)F_max) * 8;
-    return ((head + 15) & ~size_t(15)) + half_bytes_per_warp(cap);
+    return batch_head_bytes(F_max, L_max) + half_bytes_per_warp(cap);
 }
 
 template <int MODE, int AP, int MINB>
@@ -70,9 +74,9 @@ __global__ void __launch_bounds__(256, MINB)
     double* sl = reinterpret_cast<double*>(base);
     double* Jacc = sl + L_max;
     double* LDr = Jacc + F_max;
+    LambdaFactors* LF = reinterpret_cast<LambdaFactors*>(LDr + F_max);
     HalfSmem bk, fw;
-    const size_t head = ((size_t)L_max + 2 * (size_t)F_max) * 8;
-    carve_halves(base + ((head + 15) & ~size_t(15)), cap, bk, fw);
+    carve_halves(base + batch_head_bytes(F_max, L_max), cap, bk, fw);
     if (threadIdx.x == 0) atomicMin(&tstamp[2 * n_models], global_ns());
 
     const uint64_t n_items = offsets[n_models];
@@ -89,6 +93,10 @@ __global__ void __launch_bounds__(256, MINB)
         double lam_acc = 0.0;  // lane l: ALO diagonal of line l (l < 32), lines >= 32 in the loop below
         bool ok = true;
         const bool want_lam = Lout[mi] != nullptr;
+        __syncwarp();
+        if (want_lam)  // ray-independent factors of the origin's ALO elements, once per origin
+            for (uint32_t f = lane; f < m.F; f += 32)
+                if (m.in_line[f]) LF[f] = lambda_factors(m, sl, o, f);
         __syncwarp();
         for (uint32_t rr = 0; rr < m.hnrays && ok; rr++) {
             const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
@@ -125,7 +133,7 @@ __global__ void __launch_bounds__(256, MINB)
                         const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
                         const bool valid = f != 0xffffffffu && m.in_line[f];
                         double e = 0.0;
-                        if (valid) e = lambda_element(lambda_factors(m, sl, o, f), w2, LDr[f]);
+                        if (valid) e = lambda_element(LF[f], w2, LDr[f]);
                         const uint32_t nq = min(32u, m.Q - q0);
                         for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
                     }

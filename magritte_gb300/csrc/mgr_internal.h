@@ -60,6 +60,9 @@ struct MgrModel {
     mgr_reduce_fn shard_reduce = nullptr;
     void* shard_user = nullptr;
     bool shard_capturable = false;
+    // per-lane elimination scratch of the image adjoint (mgr_adjoint.cu), kept between calls
+    double* adj_scratch = nullptr;
+    size_t adj_scratch_bytes = 0;
     // host copies for the image-plane set-up (mgr_image.cu)
     std::vector<double> host_pos;     // [P][3]
     std::vector<uint32_t> host_p2b;   // [P]

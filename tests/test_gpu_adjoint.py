@@ -189,7 +189,10 @@ def test_autograd_gradients_match_finite_differences(gpu_lib):
                 lm = loss_of(*[t - eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
             return float(lp - lm) / (2 * eps)
 
-        fd = (4.0 * central(0.5) - central(1.0)) / 3.0
+        c1, c2 = central(1.0), central(0.5)
+        if abs(c1 - c2) > 1e-3 * abs(c2):
+            continue  # the step crossed a held branch (large-shift test, line bracket)
+        fd = (4.0 * c2 - c1) / 3.0
         assert abs(an - fd) <= 1e-4 * abs(fd) + 1e-9 * abs(loss.item()), (p, an, fd)
         checked += 1
     assert checked >= 6
