@@ -143,6 +143,17 @@ int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, d
 int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, double* u_dev,
                                 double* lambda_diag_dev);
 
+/* Model::compute_radiation_field_feautrier_order_2_sparse (model.cpp:474-510 ->
+ * Solver::solve_feautrier_order_2_sparse, solver.tpp:297-363), the memory-lean solve:
+ * instead of J per frequency it returns the line-integrated mean intensity
+ *   Jlin [P][L]  J(o, l) = sum_rr sum_z w_z (2 w_rr) u   (LineProducingSpecies::J, in
+ *                the reference's order: ray pair outer, quadrature point inner)
+ * and the ALO diagonal [P][L] (may be NULL).  Host buffers; blocks. */
+int mgr_formal_solve_fo2_sparse(MgrModel* model, int precision, double* Jlin, double* lambda_diag);
+
+/* Device-pointer variant; enqueued on the model's stream. */
+int mgr_formal_solve_fo2_sparse_device(MgrModel* model, int precision, double* Jlin_dev, double* lambda_diag_dev);
+
 /* Partial formal solve over the ray pairs [rr_begin, rr_end) only: J_dev [P][F] and
  * lambda_diag_dev [P][L] (may be NULL) receive the sums over those ray pairs, so that
  * the sum over disjoint ranges covering [0, hnrays) is the full solve's J and ALO
@@ -376,6 +387,18 @@ int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, do
 int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, long max_iterations,
                                   const MgrAliParams* params, int* iterations, double* error_mean,
                                   double* error_max, uint32_t err_capacity);
+
+/* Model::compute_level_populations_sparse (model.cpp:756-850): the same ALI loop with
+ * the memory-lean formal solve and compute_Jeff_sparse (model.cpp:549-570; Jlin taken
+ * from the solve, Jdif left unchanged) and the per-point rate solve of
+ * update_using_statistical_equilibrium_sparse (lineProducingSpecies.tpp:589-705). */
+int mgr_compute_level_populations_sparse(MgrModel* model, int precision, int use_ng, long max_iterations,
+                                         const MgrAliParams* params, int* iterations, double* error_mean,
+                                         double* error_max, uint32_t err_capacity);
+
+/* Model::compute_Jeff_sparse (model.cpp:549-570) for species l after
+ * mgr_formal_solve_fo2_sparse: Jlin, Jeff [P][nrad] (host, may be NULL). */
+int mgr_compute_jeff_sparse(MgrModel* model, uint32_t l, double* Jlin, double* Jeff);
 
 /* Copy species l's level populations [P][nlev] to the host. */
 int mgr_get_populations(MgrModel* model, uint32_t l, double* populations);

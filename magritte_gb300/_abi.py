@@ -109,6 +109,12 @@ SIGNATURES = {
     "mgr_model_set_species": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(MgrSpeciesDesc), C.c_uint32, _f64p,
                                         C.POINTER(_f64p)]),
     "mgr_compute_jeff": (C.c_int, [C.c_void_p, C.c_uint32, _f64p, _f64p, _f64p]),
+    "mgr_compute_jeff_sparse": (C.c_int, [C.c_void_p, C.c_uint32, _f64p, _f64p]),
+    "mgr_formal_solve_fo2_sparse": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p]),
+    "mgr_formal_solve_fo2_sparse_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "mgr_compute_level_populations_sparse": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_long,
+                                                       C.POINTER(MgrAliParams), C.POINTER(C.c_int), _f64p, _f64p,
+                                                       C.c_uint32]),
     "mgr_compute_level_populations": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_long, C.POINTER(MgrAliParams),
                                                 C.POINTER(C.c_int), _f64p, _f64p, C.c_uint32]),
     "mgr_get_populations": (C.c_int, [C.c_void_p, C.c_uint32, _f64p]),
@@ -365,7 +371,22 @@ class DeviceModel:
         _check(load().mgr_compute_jeff(self.h, l, *[_ptr(o, _f64p) for o in out]))
         return dict(Jlin=out[0], Jeff=out[1], Jdif=out[2])
 
-    def compute_level_populations(self, precision="fp64", use_ng=True, max_it=100, **params):
+    def formal_solve_fo2_sparse(self, precision="fp64"):
+        """Memory-lean solve: line-integrated J [P][L] and ALO diagonal [P][L]."""
+        Jl = np.empty((self.P, self.L))
+        lam = np.empty((self.P, self.L))
+        _check(load().mgr_formal_solve_fo2_sparse(self.h, PRECISION[precision], _ptr(Jl, _f64p), _ptr(lam, _f64p)))
+        return dict(Jlin=Jl, lambda_diag=lam)
+
+    def compute_jeff_sparse(self, l=0):
+        out = {k: np.empty((self.P, self.nrad[l])) for k in ("Jlin", "Jeff")}
+        _check(load().mgr_compute_jeff_sparse(self.h, l, _ptr(out["Jlin"], _f64p), _ptr(out["Jeff"], _f64p)))
+        return out
+
+    def compute_level_populations_sparse(self, precision="fp64", use_ng=True, max_it=100, **params):
+        return self.compute_level_populations(precision, use_ng, max_it, _sparse=True, **params)
+
+    def compute_level_populations(self, precision="fp64", use_ng=True, max_it=100, _sparse=False, **params):
         prm = dict(ALI_DEFAULTS)
         prm.update(params)
         p = MgrAliParams(**prm)
@@ -374,9 +395,9 @@ class DeviceModel:
         em, ex = np.zeros(cap), np.zeros(cap)
         self._shard_error = None
         try:
-            _check(load().mgr_compute_level_populations(self.h, PRECISION[precision], int(use_ng), max_it,
-                                                        C.byref(p), C.byref(it), _ptr(em, _f64p), _ptr(ex, _f64p),
-                                                        cap))
+            fn = load().mgr_compute_level_populations_sparse if _sparse else load().mgr_compute_level_populations
+            _check(fn(self.h, PRECISION[precision], int(use_ng), max_it, C.byref(p), C.byref(it), _ptr(em, _f64p),
+                      _ptr(ex, _f64p), cap))
         except MgrError as e:
             if self._shard_error is not None:
                 raise e from self._shard_error

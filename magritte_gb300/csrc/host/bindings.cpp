@@ -200,6 +200,7 @@ PYBIND11_MODULE(core, m) {
         .def_readwrite("quadrature", &LineProducingSpecies::quadrature)
         .def_readwrite("population", &LineProducingSpecies::population)
         .def_readwrite("population_tot", &LineProducingSpecies::population_tot)
+        .def_readwrite("J", &LineProducingSpecies::J)
         .def_readwrite("Jlin", &LineProducingSpecies::Jlin)
         .def_readwrite("Jeff", &LineProducingSpecies::Jeff)
         .def_readwrite("Jdif", &LineProducingSpecies::Jdif)
@@ -277,6 +278,11 @@ PYBIND11_MODULE(core, m) {
         .def_readonly("images", &Model::images)
         .def("compute_level_populations", &Model::compute_level_populations, py::arg("use_Ng_acceleration"),
              py::arg("max_niterations"), py::call_guard<py::gil_scoped_release>())
+        .def("compute_radiation_field_feautrier_order_2_sparse",
+             &Model::compute_radiation_field_feautrier_order_2_sparse, py::call_guard<py::gil_scoped_release>())
+        .def("compute_Jeff_sparse", &Model::compute_Jeff_sparse, py::call_guard<py::gil_scoped_release>())
+        .def("compute_level_populations_sparse", &Model::compute_level_populations_sparse,
+             py::arg("use_Ng_acceleration"), py::arg("max_niterations"), py::call_guard<py::gil_scoped_release>())
         .def_readonly("error_mean", &Model::error_mean)
         .def_readonly("error_max", &Model::error_max)
         .def("release_device", &Model::release_device)

@@ -645,7 +645,51 @@ int Model::compute_Jeff() {
     return 0;
 }
 
+// Model::compute_radiation_field_feautrier_order_2_sparse (model.cpp:474-510): the
+// line-integrated J per species (LineProducingSpecies::J) and the ALO diagonal.
+int Model::compute_radiation_field_feautrier_order_2_sparse() {
+    MgrModel* dev = upload();
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v;
+    std::vector<double> Jl((size_t)P * L), lam((size_t)P * L);
+    check(mgr_formal_solve_fo2_sparse(dev, parameters.precision, Jl.data(), lam.data()));
+    for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+        LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        const Size nrad = ls.linedata.nrad;
+        ls.J.resize({P, nrad});
+        for (Size p = 0; p < P; p++)
+            for (Size k = 0; k < nrad; k++) ls.J[(size_t)p * nrad + k] = Jl[(size_t)p * L + lines.nrad_cum[l] + k];
+    }
+    store_lambda(lam);
+    return 0;
+}
+
+// Model::compute_Jeff_sparse (model.cpp:549-570)
+int Model::compute_Jeff_sparse() {
+    if (!dev_ || lines.lineProducingSpecies.empty() || lines.lineProducingSpecies[0].J.size() == 0)
+        throw std::runtime_error(
+            "compute_Jeff_sparse needs a memory-lean formal solve (compute_radiation_field_feautrier_order_2_sparse) first");
+    attach_species();
+    const Size P = parameters.npoints_.v;
+    for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+        LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        const Size nrad = ls.linedata.nrad;
+        ls.Jlin.resize({P, nrad});
+        ls.Jeff.resize({P, nrad});
+        check(mgr_compute_jeff_sparse(dev_, l, ls.Jlin.data(), ls.Jeff.data()));
+    }
+    return 0;
+}
+
 int Model::compute_level_populations(bool use_Ng_acceleration, long max_niterations) {
+    return run_ali(use_Ng_acceleration, max_niterations, false);
+}
+
+// Model::compute_level_populations_sparse (model.cpp:756-850)
+int Model::compute_level_populations_sparse(bool use_Ng_acceleration, long max_niterations) {
+    return run_ali(use_Ng_acceleration, max_niterations, true);
+}
+
+int Model::run_ali(bool use_Ng_acceleration, long max_niterations, bool sparse) {
     if (spectralDiscretisation != SD_Lines) throw std::runtime_error("Spectral discretisation was not set for Lines!");
     MgrModel* dev = upload();
     attach_species();
@@ -665,8 +709,9 @@ int Model::compute_level_populations(bool use_Ng_acceleration, long max_niterati
     const uint32_t cap = (uint32_t)(max_niterations > 0 ? max_niterations : 0) * nls;
     std::vector<double> emean(cap), emax(cap);
     int iterations = 0;
-    check(mgr_compute_level_populations(dev, parameters.precision, use_Ng_acceleration ? 1 : 0, max_niterations, &prm,
-                                        &iterations, emean.data(), emax.data(), cap));
+    auto ali = sparse ? mgr_compute_level_populations_sparse : mgr_compute_level_populations;
+    check(ali(dev, parameters.precision, use_Ng_acceleration ? 1 : 0, max_niterations, &prm, &iterations,
+              emean.data(), emax.data(), cap));
     error_mean.assign(emean.begin(), emean.begin() + (size_t)iterations * nls);
     error_max.assign(emax.begin(), emax.begin() + (size_t)iterations * nls);
     for (Size l = 0; l < nls; l++) {

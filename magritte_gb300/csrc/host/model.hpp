@@ -190,6 +190,7 @@ struct LineProducingSpecies {
     Quadrature quadrature;
     Array<double> population;      // [P*nlev]
     Array<double> population_tot;  // [P]
+    Array<double> J;                 // [P][nrad] line-integrated J of the memory-lean solve
     Array<double> Jlin, Jeff, Jdif;  // [P][nrad]
     Array<double> lambda_diag;     // [P][nrad] summed diagonal ALO
     Array<uint8_t> lambda_has;     // [P][nrad]
@@ -272,6 +273,9 @@ class Model {
     int compute_image_new(double rx, double ry, double rz, Size Nxpix, Size Nypix);
     int compute_Jeff();
     int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
+    int compute_radiation_field_feautrier_order_2_sparse();
+    int compute_Jeff_sparse();
+    int compute_level_populations_sparse(bool use_Ng_acceleration, long max_niterations);
 
     // Device management (GB300): the MgrModel mirroring this Model.
     // upload(): prepare, dshift_max, and (re)create or refresh the device model.
@@ -288,6 +292,7 @@ class Model {
     void fill_desc(MgrModelDesc& d);
     void attach_species();
     void store_lambda(const std::vector<double>& lam);
+    int run_ali(bool use_Ng_acceleration, long max_niterations, bool sparse);
     void set_emissivity_and_opacity();
 };
 

@@ -1,5 +1,6 @@
 // C ABI of libmgr_gpu.so: model upload, formal-solve entry points, status handling.
 #include <atomic>
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -566,6 +567,52 @@ int mgr_set_ray_shard(MgrModel* model, uint32_t rr_begin, uint32_t rr_end, mgr_r
     model->shard_capturable = capturable != 0;
     ali_shard_changed(model);
     return MGR_OK;
+}
+
+int mgr_formal_solve_fo2_sparse_device(MgrModel* model, int precision, double* Jlin_dev, double* lambda_diag_dev) {
+    if (!model || !Jlin_dev) {
+        set_error("mgr_formal_solve_fo2_sparse_device: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
+        set_error("mgr_formal_solve_fo2_sparse_device: unknown precision mode");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!model->line_disc) {
+        set_error("mgr_formal_solve_fo2_sparse_device: the formal solve needs a line spectral discretisation");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    const size_t wb = fo2_work_bytes(model, model->dm.P, true, lambda_diag_dev != nullptr);
+    int rc = ensure_scratch(model, &model->work, &model->work_bytes, wb);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = launch_fo2_range(model, precision, 0, model->dm.P, nullptr, nullptr, lambda_diag_dev, model->work,
+                                     model->work_bytes, 0, model->dm.hnrays, Jlin_dev);
+    if (e != cudaSuccess) return cuda_fail(e, "memory-lean formal solve launch");
+    model->last_J = nullptr;
+    model->last_Jlin = Jlin_dev;
+    model->last_lam = lambda_diag_dev;
+    return MGR_OK;
+}
+
+int mgr_formal_solve_fo2_sparse(MgrModel* model, int precision, double* Jlin, double* lambda_diag) {
+    if (!model || !Jlin) {
+        set_error("mgr_formal_solve_fo2_sparse: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    const DevModel& dm = model->dm;
+    const size_t PL = (size_t)dm.P * dm.L;
+    // the line-integrated J lives in the J scratch (>= P*L doubles), the ALO in the lambda scratch
+    int rc = ensure_scratch(model, &model->J_scratch, &model->J_scratch_bytes,
+                            std::max(PL, (size_t)dm.P * dm.F) * 8);
+    if (rc != MGR_OK) return rc;
+    if ((rc = ensure_scratch(model, &model->lam_scratch, &model->lam_scratch_bytes, PL * 8)) != MGR_OK) return rc;
+    rc = mgr_formal_solve_fo2_sparse_device(model, precision, model->J_scratch, model->lam_scratch);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(Jlin, model->J_scratch, PL * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && lambda_diag)
+        e = cudaMemcpyAsync(lambda_diag, model->lam_scratch, PL * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "result copy");
+    return read_status(model);
 }
 
 int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, double* lambda_diag) {

@@ -29,20 +29,27 @@ constexpr double HH_OVER_FOUR_PI = HH / (4.0 * 3.14159265358979323846);  // cons
 // ---------------------------------------------------------------------------------
 // compute_Jeff, n_off_diag = 0 (model.cpp:514-545): thread per (p, k).
 // ---------------------------------------------------------------------------------
-__global__ void jeff_kernel(DevModel m, SpeciesView s, const double* __restrict__ J, const double* __restrict__ lam) {
+// With Jlin_in (the memory-lean solve's line-integrated J, [P][L]): compute_Jeff_sparse
+// (model.cpp:549-570), Jlin taken as it is and Jdif left unchanged.
+__global__ void jeff_kernel(DevModel m, SpeciesView s, const double* __restrict__ J, const double* __restrict__ lam,
+                            const double* __restrict__ Jlin_in) {
     const size_t n = (size_t)m.P * s.nrad;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
         const uint32_t p = (uint32_t)(t / s.nrad), k = (uint32_t)(t % s.nrad);
         const uint32_t lid = s.line_offset + k;
         double jl = 0.0;
-        for (uint32_t z = 0; z < m.Q; z++) {
-            const uint32_t f = m.lq2f[(size_t)lid * m.Q + z];  // nr_line[p][k][z]
-            jl = __dadd_rn(jl, __dmul_rn(m.quad_w[(size_t)m.corr_lspec[f] * m.Q + z], J[(size_t)p * m.F + f]));
+        if (Jlin_in) {
+            jl = Jlin_in[(size_t)p * m.L + lid];
+        } else {
+            for (uint32_t z = 0; z < m.Q; z++) {
+                const uint32_t f = m.lq2f[(size_t)lid * m.Q + z];  // nr_line[p][k][z]
+                jl = __dadd_rn(jl, __dmul_rn(m.quad_w[(size_t)m.corr_lspec[f] * m.Q + z], J[(size_t)p * m.F + f]));
+            }
         }
         const double diff = __dmul_rn(lam[(size_t)p * m.L + lid], s.pop[(size_t)p * s.nlev + s.irad[k]]);
         s.Jlin[t] = jl;
         s.Jeff[t] = __dsub_rn(jl, __dmul_rn(HH_OVER_FOUR_PI, diff));
-        s.Jdif[t] = __dmul_rn(HH_OVER_FOUR_PI, diff);
+        if (!Jlin_in) s.Jdif[t] = __dmul_rn(HH_OVER_FOUR_PI, diff);
     }
 }
 
@@ -484,11 +491,12 @@ static unsigned grid_for(size_t n, int threads, int cap) {
     return (unsigned)(b ? b : 1);
 }
 
-cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam) {
+cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam, const double* Jlin) {
     for (auto& sp : model->ali->species) {
         const size_t n = (size_t)model->dm.P * sp.view.nrad;
         count_launch();
-        jeff_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, model->stream>>>(model->dm, sp.view, J, lam);
+        jeff_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, model->stream>>>(model->dm, sp.view, J, lam,
+                                                                                      Jlin);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -692,6 +700,7 @@ void ali_free(MgrModel* model) {
     for (void* p : st->pool_allocs) cudaFree(p);
     for (void* p : st->allocs) cudaFree(p);
     if (st->stats_host) cudaFreeHost(st->stats_host);
+    if (st->Jlin_buf) cudaFree(st->Jlin_buf);
     delete st;
     model->ali = nullptr;
 }
@@ -751,18 +760,25 @@ static int read_stats(MgrModel* model) {
 // corrections, convergence, line data.
 // With a ray-pair shard, the formal solve covers the shard's ray pairs and the reduce
 // function sums J and the ALO diagonal over the shards before Jeff.
+// The memory-lean variant (compute_level_populations_sparse) sums the line-integrated
+// J in the formal solve instead of J per frequency.
 static cudaError_t normal_iteration_launches(MgrModel* model, int precision) {
-    cudaError_t e = launch_fo2_range(model, precision, 0, model->dm.P, model->J_scratch, nullptr, model->lam_scratch,
-                                     model->work, model->work_bytes, model->shard_begin, model->shard_end);
+    AliState& st = *model->ali;
+    const DevModel& m = model->dm;
+    double* J = st.sparse ? nullptr : model->J_scratch;
+    double* Jlin = st.sparse ? st.Jlin_buf : nullptr;
+    cudaError_t e = launch_fo2_range(model, precision, 0, m.P, J, nullptr, model->lam_scratch, model->work,
+                                     model->work_bytes, model->shard_begin, model->shard_end, Jlin);
     if (e == cudaSuccess && model->shard_reduce) {
-        const DevModel& m = model->dm;
-        if (model->shard_reduce(model->shard_user, model->J_scratch, (uint64_t)m.P * m.F, model->lam_scratch,
-                                (uint64_t)m.P * m.L, (void*)model->stream) != 0) {
-            model->ali->reduce_failed = true;
+        double* Jr = st.sparse ? Jlin : J;
+        const uint64_t nJ = st.sparse ? (uint64_t)m.P * m.L : (uint64_t)m.P * m.F;
+        if (model->shard_reduce(model->shard_user, Jr, nJ, model->lam_scratch, (uint64_t)m.P * m.L,
+                                (void*)model->stream) != 0) {
+            st.reduce_failed = true;
             e = cudaErrorUnknown;
         }
     }
-    if (e == cudaSuccess) e = ali_launch_jeff(model, model->J_scratch, model->lam_scratch);
+    if (e == cudaSuccess) e = ali_launch_jeff(model, J, model->lam_scratch, Jlin);
     if (e == cudaSuccess) e = ali_launch_stateq_and_refresh(model, model->lam_scratch);
     return e;
 }
@@ -771,7 +787,7 @@ static cudaError_t normal_iteration_launches(MgrModel* model, int precision) {
 // launches if the capture is refused.
 static cudaError_t normal_iteration(MgrModel* model, int precision) {
     AliState& st = *model->ali;
-    if (st.graph && st.graph_precision != precision) {
+    if (st.graph && (st.graph_precision != precision || st.graph_sparse != (int)st.sparse)) {
         cudaGraphExecDestroy(st.graph);
         st.graph = nullptr;
     }
@@ -792,6 +808,7 @@ static cudaError_t normal_iteration(MgrModel* model, int precision) {
             st.graph_failed = true;
         } else {
             st.graph_precision = precision;
+            st.graph_sparse = (int)st.sparse;
         }
     }
     if (st.graph && capture) {
@@ -948,7 +965,7 @@ int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, do
         set_error("mgr_compute_jeff: needs a formal solve with the ALO diagonal first");
         return MGR_ERR_ARGUMENT;
     }
-    cudaError_t e = ali_launch_jeff(model, model->last_J, model->last_lam);
+    cudaError_t e = ali_launch_jeff(model, model->last_J, model->last_lam, nullptr);
     const SpeciesView& v = model->ali->species[l].view;
     const size_t bytes = (size_t)model->dm.P * v.nrad * sizeof(double);
     if (e == cudaSuccess && Jlin) e = cudaMemcpyAsync(Jlin, v.Jlin, bytes, cudaMemcpyDeviceToHost, model->stream);
@@ -1004,6 +1021,7 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
     };
     if ((rc = scratch(&model->J_scratch, &model->J_scratch_bytes, PF * 8)) != MGR_OK) return rc;
     if ((rc = scratch(&model->lam_scratch, &model->lam_scratch_bytes, PL * 8)) != MGR_OK) return rc;
+    if (st.sparse && (rc = scratch(&st.Jlin_buf, &st.Jlin_bytes, PL * 8)) != MGR_OK) return rc;
     if ((rc = scratch(&model->work, &model->work_bytes, fo2_work_bytes(model, dm.P, true, true))) != MGR_OK) return rc;
     // Between two Ng steps the history grows by one residual and one population per
     // normal iteration (at most mem_limit + remove_N_its of them), plus the initial
@@ -1096,7 +1114,8 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
             if (fnc[l] > 1.0 - prm.convergence_fraction) some_not_converged = true;
         }
     }
-    model->last_J = model->J_scratch;
+    model->last_J = st.sparse ? nullptr : model->J_scratch;
+    model->last_Jlin = st.sparse ? st.Jlin_buf : nullptr;
     model->last_lam = model->lam_scratch;
     if (iterations) *iterations = iteration;
     int st_rc = MGR_OK;
@@ -1112,6 +1131,39 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
         }
     }
     return st_rc;
+}
+
+int mgr_compute_level_populations_sparse(MgrModel* model, int precision, int use_ng, long max_iterations,
+                                         const MgrAliParams* params, int* iterations, double* error_mean,
+                                         double* error_max, uint32_t err_capacity) {
+    if (!model || !model->ali) {
+        set_error("mgr_compute_level_populations_sparse: null argument or no species attached (mgr_model_set_species)");
+        return MGR_ERR_ARGUMENT;
+    }
+    model->ali->sparse = true;
+    const int rc = mgr_compute_level_populations(model, precision, use_ng, max_iterations, params, iterations,
+                                                 error_mean, error_max, err_capacity);
+    model->ali->sparse = false;
+    return rc;
+}
+
+int mgr_compute_jeff_sparse(MgrModel* model, uint32_t l, double* Jlin, double* Jeff) {
+    if (!model || !model->ali || l >= model->ali->species.size()) {
+        set_error("mgr_compute_jeff_sparse: no species attached (mgr_model_set_species) or species index out of range");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!model->last_Jlin || !model->last_lam) {
+        set_error("mgr_compute_jeff_sparse: needs a memory-lean formal solve (mgr_formal_solve_fo2_sparse) first");
+        return MGR_ERR_ARGUMENT;
+    }
+    cudaError_t e = ali_launch_jeff(model, nullptr, model->last_lam, model->last_Jlin);
+    const SpeciesView& v = model->ali->species[l].view;
+    const size_t bytes = (size_t)model->dm.P * v.nrad * sizeof(double);
+    if (e == cudaSuccess && Jlin) e = cudaMemcpyAsync(Jlin, v.Jlin, bytes, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && Jeff) e = cudaMemcpyAsync(Jeff, v.Jeff, bytes, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "compute_Jeff_sparse");
+    return MGR_OK;
 }
 
 int mgr_get_populations(MgrModel* model, uint32_t l, double* populations) {

@@ -79,9 +79,16 @@ struct AliState {
     int graph_precision = -1;
     bool graph_failed = false;
     bool reduce_failed = false;  // the ray-shard reduce function returned an error
+    // memory-lean variant (compute_level_populations_sparse): line-integrated J per
+    // iteration instead of J per frequency
+    bool sparse = false;
+    int graph_sparse = -1;
+    double* Jlin_buf = nullptr;  // [P][L]
+    size_t Jlin_bytes = 0;
 };
 
-cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam);
+// Jlin: the memory-lean solve's line-integrated J [P][L] (compute_Jeff_sparse), or NULL.
+cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam, const double* Jlin = nullptr);
 // Drops the captured iteration after the ray-pair shard or its reduce function changed.
 void ali_shard_changed(MgrModel* model);
 cudaError_t ali_launch_stateq_and_refresh(MgrModel* model, const double* lam);

@@ -196,16 +196,38 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
                                                          const double* __restrict__ U, size_t u_stride, uint32_t u_o0,
                                                          const double* __restrict__ LD, size_t ld_stride,
                                                          uint32_t ld_o0, double* __restrict__ J,
-                                                         double* __restrict__ lam) {
+                                                         double* __restrict__ lam, double* __restrict__ Jlin) {
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     for (uint32_t o = o_begin + blockIdx.x; o < o_end; o += gridDim.x) {
-        for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
-            const double* Uo = U + (size_t)(o - u_o0) * m.F + f;
-            double s = 0.0;
-            for (uint32_t k = 0; k < nR; k++) s += Uo[(size_t)k * u_stride] * 2.0 * m.rayw[rr0 + k];
-            J[(size_t)o * m.F + f] = s;
+        if (J) {
+            for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
+                const double* Uo = U + (size_t)(o - u_o0) * m.F + f;
+                double s = 0.0;
+                for (uint32_t k = 0; k < nR; k++) s += Uo[(size_t)k * u_stride] * 2.0 * m.rayw[rr0 + k];
+                J[(size_t)o * m.F + f] = s;
+            }
+        }
+        if (Jlin) {
+            // line-integrated J of the memory-lean solve (solve_feautrier_order_2_sparse,
+            // solver.tpp:297-363): J(o, l) += w_z (2 w_rr) u in (rr, z) order
+            for (uint32_t l = w; l < m.L; l += nw) {
+                const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
+                double s = 0.0;
+                for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
+                    const double* Ur = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
+                    const double wt = m.rayw[rr] * 2.0;
+                    for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
+                        const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
+                        const double e =
+                            f != 0xffffffffu ? (m.quad_w[(size_t)m.corr_lspec[f] * m.Q + q0 + lane] * wt) * Ur[f] : 0.0;
+                        const uint32_t nq = min(32u, m.Q - q0);
+                        for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
+                    }
+                }
+                if (lane == 0) Jlin[(size_t)o * m.L + l] = s;
+            }
         }
         if (!lam) continue;
         for (uint32_t l = w; l < m.L; l += nw) {
@@ -460,7 +482,8 @@ static cudaError_t launch_fo2_approx(MgrModel* model, uint32_t o_begin, uint32_t
 }
 
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
-                             double* lam, double* work, size_t work_bytes, uint32_t rr_begin, uint32_t rr_end) {
+                             double* lam, double* work, size_t work_bytes, uint32_t rr_begin, uint32_t rr_end,
+                             double* Jlin) {
     const DevModel& m = model->dm;
     if (o_end <= o_begin) return cudaSuccess;
     if (rr_end > m.hnrays) rr_end = m.hnrays;
@@ -501,7 +524,8 @@ cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, u
         if (e != cudaSuccess) return e;
         unsigned grid = n < (uint32_t)nsm * 16 ? n : (unsigned)nsm * 16;
         count_launch();
-        fo2_reduce_kernel<<<grid, 128, 0, model->stream>>>(m, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, J, lam);
+        fo2_reduce_kernel<<<grid, 128, 0, model->stream>>>(m, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, J, lam,
+                                                           Jlin);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

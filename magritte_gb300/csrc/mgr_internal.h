@@ -52,6 +52,7 @@ struct MgrModel {
     // J [P][F] and ALO diagonal [P][L] of the last formal solve (device), for Jeff
     const double* last_J = nullptr;
     const double* last_lam = nullptr;
+    const double* last_Jlin = nullptr;  // line-integrated J [P][L] of the last memory-lean solve
     // line-producing species and the ALI loop (mgr_ali.cu)
     mgr::AliState* ali = nullptr;
     // ray-pair shard of the ALI loop's formal solves and the sum over shards
@@ -87,9 +88,11 @@ cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps);
 constexpr size_t kFo2WorkBudget = size_t(2) << 30;
 size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, bool stage_ld);
 // Ray pairs [rr_begin, rr_end) only (partial J / ALO sums, u must then be NULL).
+// J may be NULL; Jlin [P][L] (may be NULL) receives the line-integrated J in the order
+// of the memory-lean solve.
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
                              double* lam, double* work, size_t work_bytes, uint32_t rr_begin = 0,
-                             uint32_t rr_end = 0xffffffffu);
+                             uint32_t rr_end = 0xffffffffu, double* Jlin = nullptr);
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
                                 uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
                                 double* d_dZ);
