@@ -218,6 +218,16 @@ int mgr_image(MgrModel* model, int precision, uint32_t ray_nr, double* I, double
 int mgr_image_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny, double* I,
                   double* ImX, double* ImY);
 
+/* Model::compute_image_optical_depth(ray_nr) (model.cpp:1061-1079 ->
+ * Solver::image_optical_depth, solver.tpp:655-684) and compute_image_optical_depth_new
+ * (model.cpp:1081-1127 -> image_optical_depth_new_imager, solver.tpp:686-736): the
+ * rays of mgr_image / mgr_image_new, I = the optical depth summed over the ray's pairs
+ * (Solver::image_optical_depth(model, o, f), solver.tpp:2718-2760), 0 for a ray
+ * without pairs.  Same arguments and outputs as mgr_image / mgr_image_new. */
+int mgr_image_optical_depth(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY);
+int mgr_image_optical_depth_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny,
+                                double* I, double* ImX, double* ImY);
+
 /* Same as mgr_formal_solve_fo2_device, but the call allocates no device memory.
  * No reference counterpart: an addition of this library for callers that cannot
  * allocate at solve time.

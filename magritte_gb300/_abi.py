@@ -100,6 +100,9 @@ SIGNATURES = {
                                               C.c_void_p, C.c_void_p]),
     "mgr_image": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, _f64p, _f64p, _f64p]),
     "mgr_image_new": (C.c_int, [C.c_void_p, C.c_int, _f64p, C.c_uint32, C.c_uint32, _f64p, _f64p, _f64p]),
+    "mgr_image_optical_depth": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, _f64p, _f64p, _f64p]),
+    "mgr_image_optical_depth_new": (C.c_int, [C.c_void_p, C.c_int, _f64p, C.c_uint32, C.c_uint32, _f64p, _f64p,
+                                              _f64p]),
     "mgr_formal_solve_fo2_device_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint64)]),
@@ -283,6 +286,21 @@ class DeviceModel:
         X, Y = np.empty(self.P), np.empty(self.P)
         _check(load().mgr_image(self.h, PRECISION[precision], ray_nr, _ptr(I, _f64p), _ptr(X, _f64p),
                                 _ptr(Y, _f64p)))
+        return dict(I=I, ImX=X, ImY=Y)
+
+    def image_optical_depth(self, ray_nr, precision="fp64"):
+        I = np.empty((self.P, self.F))
+        X, Y = np.empty(self.P), np.empty(self.P)
+        _check(load().mgr_image_optical_depth(self.h, PRECISION[precision], ray_nr, _ptr(I, _f64p), _ptr(X, _f64p),
+                                              _ptr(Y, _f64p)))
+        return dict(I=I, ImX=X, ImY=Y)
+
+    def image_optical_depth_new(self, raydir, nx, ny, precision="fp64"):
+        I = np.empty((nx * ny, self.F))
+        X, Y = np.empty(nx * ny), np.empty(nx * ny)
+        d = np.ascontiguousarray(raydir, np.float64)
+        _check(load().mgr_image_optical_depth_new(self.h, PRECISION[precision], _ptr(d, _f64p), nx, ny,
+                                                  _ptr(I, _f64p), _ptr(X, _f64p), _ptr(Y, _f64p)))
         return dict(I=I, ImX=X, ImY=Y)
 
     def image_new(self, raydir, nx, ny, precision="fp64"):

@@ -233,6 +233,7 @@ PYBIND11_MODULE(core, m) {
         .def_readwrite("I", &Radiation::I);
 
     py::class_<Image>(m, "Image")
+        .def_readonly("imageType", &Image::imageType)
         .def_readonly("imagePointPosition", &Image::imagePointPosition)
         .def_readonly("ray_nr", &Image::ray_nr)
         .def_readwrite("ray_direction", &Image::ray_direction)
@@ -274,6 +275,16 @@ PYBIND11_MODULE(core, m) {
         .def("compute_image_new", py::overload_cast<Size, Size, Size>(&Model::compute_image_new),
              py::call_guard<py::gil_scoped_release>())
         .def("compute_image_new", py::overload_cast<double, double, double, Size, Size>(&Model::compute_image_new),
+             py::call_guard<py::gil_scoped_release>())
+        .def("compute_image_optical_depth", &Model::compute_image_optical_depth,
+             py::call_guard<py::gil_scoped_release>())
+        .def("compute_image_optical_depth_new", py::overload_cast<Size>(&Model::compute_image_optical_depth_new),
+             py::call_guard<py::gil_scoped_release>())
+        .def("compute_image_optical_depth_new",
+             py::overload_cast<Size, Size, Size>(&Model::compute_image_optical_depth_new),
+             py::call_guard<py::gil_scoped_release>())
+        .def("compute_image_optical_depth_new",
+             py::overload_cast<double, double, double, Size, Size>(&Model::compute_image_optical_depth_new),
              py::call_guard<py::gil_scoped_release>())
         .def_readonly("images", &Model::images)
         .def("compute_level_populations", &Model::compute_level_populations, py::arg("use_Ng_acceleration"),

@@ -728,12 +728,19 @@ int Model::run_ali(bool use_Ng_acceleration, long max_niterations, bool sparse) 
 // ---------------------------------------------------------------------------------
 // Imagers (model.cpp:957-1013)
 // ---------------------------------------------------------------------------------
-int Model::compute_image(Size ray_nr) {
+int Model::compute_image(Size ray_nr) { return image_old(ray_nr, false); }
+
+// Model::compute_image_optical_depth (model.cpp:1061-1079 -> Solver::image_optical_depth,
+// solver.tpp:655-684): the old imager's rays, the summed optical depth per frequency.
+int Model::compute_image_optical_depth(Size ray_nr) { return image_old(ray_nr, true); }
+
+int Model::image_old(Size ray_nr, bool tau) {
     if (parameters.one_line_approximation)
         throw std::runtime_error("One line approximation is currently not supported for imaging.");
     MgrModel* dev = upload();
     const Size P = parameters.npoints_.v, F = parameters.nfreqs_;
     Image im;
+    im.imageType = tau ? 1 : 0;
     im.imagePointPosition = 0;
     im.ray_nr = (long)ray_nr;
     im.ray_direction.assign({3}, geometry.rays.direction.data() + 3 * (size_t)ray_nr);
@@ -743,7 +750,8 @@ int Model::compute_image(Size ray_nr) {
     im.I.resize({P, F});
     im.ImX.resize({P});
     im.ImY.resize({P});
-    check(mgr_image(dev, parameters.precision, ray_nr, im.I.data(), im.ImX.data(), im.ImY.data()));
+    auto fn = tau ? mgr_image_optical_depth : mgr_image;
+    check(fn(dev, parameters.precision, ray_nr, im.I.data(), im.ImX.data(), im.ImY.data()));
     images.push_back(std::move(im));
     return 0;
 }
@@ -756,6 +764,23 @@ int Model::compute_image_new(Size ray_nr, Size Nxpix, Size Nypix) {
 }
 
 int Model::compute_image_new(double rx, double ry, double rz, Size Nxpix, Size Nypix) {
+    return image_new(rx, ry, rz, Nxpix, Nypix, false);
+}
+
+// Model::compute_image_optical_depth_new (model.cpp:1081-1127 ->
+// Solver::image_optical_depth_new_imager, solver.tpp:686-736)
+int Model::compute_image_optical_depth_new(Size ray_nr) { return compute_image_optical_depth_new(ray_nr, 256, 256); }
+
+int Model::compute_image_optical_depth_new(Size ray_nr, Size Nxpix, Size Nypix) {
+    const double* d = geometry.rays.direction.data() + 3 * (size_t)ray_nr;
+    return image_new(d[0], d[1], d[2], Nxpix, Nypix, true);
+}
+
+int Model::compute_image_optical_depth_new(double rx, double ry, double rz, Size Nxpix, Size Nypix) {
+    return image_new(rx, ry, rz, Nxpix, Nypix, true);
+}
+
+int Model::image_new(double rx, double ry, double rz, Size Nxpix, Size Nypix, bool tau) {
     if (rx * rx + ry * ry + rz * rz == 0.0)
         throw std::runtime_error(
             "The given ray direction vector does not point in a direction. Please use a non-zero (normed) direction "
@@ -767,6 +792,7 @@ int Model::compute_image_new(double rx, double ry, double rz, Size Nxpix, Size N
     const double inv = 1 / std::sqrt(rx * rx + ry * ry + rz * rz);
     const double d[3] = {rx * inv, ry * inv, rz * inv};
     Image im;
+    im.imageType = tau ? 1 : 0;
     im.imagePointPosition = 1;
     im.ray_nr = -1;
     im.ray_direction.assign({3}, d);
@@ -776,7 +802,8 @@ int Model::compute_image_new(double rx, double ry, double rz, Size Nxpix, Size N
     im.I.resize({npix, F});
     im.ImX.resize({npix});
     im.ImY.resize({npix});
-    check(mgr_image_new(dev, parameters.precision, d, Nxpix, Nypix, im.I.data(), im.ImX.data(), im.ImY.data()));
+    auto fn = tau ? mgr_image_optical_depth_new : mgr_image_new;
+    check(fn(dev, parameters.precision, d, Nxpix, Nypix, im.I.data(), im.ImX.data(), im.ImY.data()));
     images.push_back(std::move(im));
     return 0;
 }

@@ -226,6 +226,7 @@ struct Radiation {
 // One image (src/model/image/image.hpp:30-60): intensities I [npix][nfreqs] and the
 // image-plane coordinates of the pixels.
 struct Image {
+    int imageType = 0;           // 0 Intensity, 1 OpticalDepth
     int imagePointPosition = 0;  // 0 AllModelPoints (old imager), 1 ProjectionSurface
     long ray_nr = -1;
     Array<double> ray_direction;  // [3]
@@ -271,6 +272,10 @@ class Model {
     int compute_image_new(Size ray_nr);
     int compute_image_new(Size ray_nr, Size Nxpix, Size Nypix);
     int compute_image_new(double rx, double ry, double rz, Size Nxpix, Size Nypix);
+    int compute_image_optical_depth(Size ray_nr);
+    int compute_image_optical_depth_new(Size ray_nr);
+    int compute_image_optical_depth_new(Size ray_nr, Size Nxpix, Size Nypix);
+    int compute_image_optical_depth_new(double rx, double ry, double rz, Size Nxpix, Size Nypix);
     int compute_Jeff();
     int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
     int compute_radiation_field_feautrier_order_2_sparse();
@@ -293,6 +298,8 @@ class Model {
     void attach_species();
     void store_lambda(const std::vector<double>& lam);
     int run_ali(bool use_Ng_acceleration, long max_niterations, bool sparse);
+    int image_old(Size ray_nr, bool tau);
+    int image_new(double rx, double ry, double rz, Size Nxpix, Size Nypix, bool tau);
     void set_emissivity_and_opacity();
 };
 

@@ -18,7 +18,7 @@ namespace mgr {
 // ---------------------------------------------------------------------------------
 // Old imager: warp per model point o, ray rr / antipode, rest-frame shifts.
 // ---------------------------------------------------------------------------------
-template <int MODE, int AP>
+template <int MODE, int AP, bool TAU>
 __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, uint32_t rr, double* __restrict__ I,
                                                     int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, ui
                 c.freq = m.nu[(size_t)o * m.F + f];
                 c.fq = (float)c.freq;
                 c.a0 = (float)(c.freq - m.line[c.l0]);
-                const double v = image_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
+                const double v = image_lane<MODE, AP, TAU>(m, sl, c, bk, nb, fw, nf);
                 I[(size_t)o * m.F + f] = v;
                 if (!isfinite(v)) atomicOr(status, ST_NONFINITE);
             }
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, ui
     }
 }
 
-template <int MODE, int AP>
+template <int MODE, int AP, bool TAU>
 __global__ void __launch_bounds__(256) image_new_kernel(DevModel m, ImagePlane ip, uint32_t cap,
                                                         double* __restrict__ I, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) image_new_kernel(DevModel m, ImagePlane i
                 c.freq = m.nu[(size_t)start * m.F + f];
                 c.fq = (float)c.freq;
                 c.a0 = (float)(c.freq - m.line[c.l0]);
-                const double v = image_lane<MODE, AP>(m, sl, c, bk, nb, fw, 0);
+                const double v = image_lane<MODE, AP, TAU>(m, sl, c, bk, nb, fw, 0);
                 I[(size_t)px * m.F + f] = v;
                 if (!isfinite(v)) atomicOr(status, ST_NONFINITE);
             }
@@ -132,11 +132,11 @@ static cudaError_t launch_warp_kernel(MgrModel* model, K kern, uint32_t cap, uin
     return cudaSuccess;
 }
 
-template <int MODE, int AP>
+template <int MODE, int AP, bool TAU>
 static cudaError_t launch_image_t(MgrModel* model, uint32_t rr, double* I) {
     size_t smem;
     unsigned grid;
-    auto kern = image_kernel<MODE, AP>;
+    auto kern = image_kernel<MODE, AP, TAU>;
     cudaError_t e = launch_warp_kernel(model, kern, model->half_cap, model->dm.P, &smem, &grid);
     if (e != cudaSuccess) return e;
     const int nw = (int)((smem - (size_t)((model->dm.L + 1) & ~1u) * 8) / half_bytes_per_warp(model->half_cap));
@@ -145,11 +145,11 @@ static cudaError_t launch_image_t(MgrModel* model, uint32_t rr, double* I) {
     return cudaGetLastError();
 }
 
-template <int MODE, int AP>
+template <int MODE, int AP, bool TAU>
 static cudaError_t launch_image_new_t(MgrModel* model, const ImagePlane& ip, uint32_t cap, double* I) {
     size_t smem;
     unsigned grid;
-    auto kern = image_new_kernel<MODE, AP>;
+    auto kern = image_new_kernel<MODE, AP, TAU>;
     cudaError_t e = launch_warp_kernel(model, kern, cap, (uint64_t)ip.nx * ip.ny, &smem, &grid);
     if (e != cudaSuccess) return e;
     const int nw = (int)((smem - (size_t)((model->dm.L + 1) & ~1u) * 8) / half_bytes_per_warp(cap));
@@ -158,16 +158,16 @@ static cudaError_t launch_image_new_t(MgrModel* model, const ImagePlane& ip, uin
     return cudaGetLastError();
 }
 
-template <int MODE>
+template <int MODE, bool TAU = false>
 static cudaError_t dispatch_image(MgrModel* model, uint32_t rr, double* I) {
-    if (model->dm.approx == APPROX_NONE) return launch_image_t<MODE, APPROX_NONE>(model, rr, I);
-    return launch_image_t<MODE, APPROX_CLOSELINES>(model, rr, I);
+    if (model->dm.approx == APPROX_NONE) return launch_image_t<MODE, APPROX_NONE, TAU>(model, rr, I);
+    return launch_image_t<MODE, APPROX_CLOSELINES, TAU>(model, rr, I);
 }
 
-template <int MODE>
+template <int MODE, bool TAU = false>
 static cudaError_t dispatch_image_new(MgrModel* model, const ImagePlane& ip, uint32_t cap, double* I) {
-    if (model->dm.approx == APPROX_NONE) return launch_image_new_t<MODE, APPROX_NONE>(model, ip, cap, I);
-    return launch_image_new_t<MODE, APPROX_CLOSELINES>(model, ip, cap, I);
+    if (model->dm.approx == APPROX_NONE) return launch_image_new_t<MODE, APPROX_NONE, TAU>(model, ip, cap, I);
+    return launch_image_new_t<MODE, APPROX_CLOSELINES, TAU>(model, ip, cap, I);
 }
 
 // Image::set_coordinates_all_model_points, 3D (image.cpp:154-219).
@@ -205,39 +205,40 @@ cudaError_t image_plane_upload(MgrModel* model, ImagePlane& ip, const std::vecto
     return e;
 }
 
-}  // namespace mgr
-
-using namespace mgr;
-
-extern "C" {
-
-int mgr_image(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY) {
+static int image_old_impl(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY,
+                          bool tau, const std::string& who) {
     if (!model || !I) {
-        set_error("mgr_image: null argument");
+        set_error(who + ": null argument");
         return MGR_ERR_ARGUMENT;
     }
     if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
-        set_error("mgr_image: unknown precision mode");
+        set_error(who + ": unknown precision mode");
         return MGR_ERR_ARGUMENT;
     }
     if (model->dm.approx == APPROX_ONELINE) {
-        set_error("mgr_image: One line approximation is currently not supported for imaging.");
+        set_error(who + ": One line approximation is currently not supported for imaging.");
         return MGR_ERR_UNSUPPORTED;
     }
     const DevModel& dm = model->dm;
     if (ray_nr >= dm.nrays) {
-        set_error("mgr_image: ray number out of range");
+        set_error(who + ": ray number out of range");
         return MGR_ERR_ARGUMENT;
     }
     const size_t PF = (size_t)dm.P * dm.F;
     double* dI = nullptr;
     cudaError_t e = cudaMalloc(&dI, PF * 8);
-    if (e == cudaSuccess) e = (precision == MGR_PRECISION_SPLIT) ? dispatch_image<MODE_SPLIT>(model, ray_nr, dI)
-                                                                : dispatch_image<MODE_FP64>(model, ray_nr, dI);
+    if (e == cudaSuccess) {
+        if (tau)
+            e = (precision == MGR_PRECISION_SPLIT) ? dispatch_image<MODE_SPLIT, true>(model, ray_nr, dI)
+                                                   : dispatch_image<MODE_FP64, true>(model, ray_nr, dI);
+        else
+            e = (precision == MGR_PRECISION_SPLIT) ? dispatch_image<MODE_SPLIT>(model, ray_nr, dI)
+                                                   : dispatch_image<MODE_FP64>(model, ray_nr, dI);
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(I, dI, PF * 8, cudaMemcpyDeviceToHost, model->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     cudaFree(dI);
-    if (e != cudaSuccess) return cuda_fail(e, "image");
+    if (e != cudaSuccess) return cuda_fail(e, who.c_str());
     if (ImX && ImY) {
         const double* d = model->host_raydir.data() + 3 * (size_t)ray_nr;
         double ix, iy, jx, jy, jz;
@@ -257,19 +258,19 @@ int mgr_image(MgrModel* model, int precision, uint32_t ray_nr, double* I, double
     return mgr_sync(model);
 }
 
-int mgr_image_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny, double* I,
-                  double* ImX, double* ImY) {
+static int image_new_impl(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny,
+                          double* I, double* ImX, double* ImY, bool tau, const std::string& who) {
     if (!model || !I) {
-        set_error("mgr_image_new: null argument");
+        set_error(who + ": null argument");
         return MGR_ERR_ARGUMENT;
     }
     if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
-        set_error("mgr_image_new: unknown precision mode");
+        set_error(who + ": unknown precision mode");
         return MGR_ERR_ARGUMENT;
     }
     ImagePlane ip{};
     std::vector<double> hx, hy;
-    int rc = image_plane_setup(model, "mgr_image_new", raydir, nx, ny, ip, hx, hy);
+    int rc = image_plane_setup(model, who.c_str(), raydir, nx, ny, ip, hx, hy);
     if (rc != MGR_OK) return rc;
     const DevModel& dm = model->dm;
     const size_t npix = (size_t)nx * ny;
@@ -280,18 +281,49 @@ int mgr_image_new(MgrModel* model, int precision, const double* raydir, uint32_t
     if (e == cudaSuccess) e = cudaMalloc(&dI, npix * dm.F * 8);
     if (e == cudaSuccess) e = cudaMalloc(&dmax, sizeof(uint32_t));
     if (e == cudaSuccess) e = image_plane_upload(model, ip, hx, hy, dxy, dmax, &cap);
-    if (e == cudaSuccess)
-        e = (precision == MGR_PRECISION_SPLIT) ? dispatch_image_new<MODE_SPLIT>(model, ip, cap, dI)
-                                               : dispatch_image_new<MODE_FP64>(model, ip, cap, dI);
+    if (e == cudaSuccess) {
+        if (tau)
+            e = (precision == MGR_PRECISION_SPLIT) ? dispatch_image_new<MODE_SPLIT, true>(model, ip, cap, dI)
+                                                   : dispatch_image_new<MODE_FP64, true>(model, ip, cap, dI);
+        else
+            e = (precision == MGR_PRECISION_SPLIT) ? dispatch_image_new<MODE_SPLIT>(model, ip, cap, dI)
+                                                   : dispatch_image_new<MODE_FP64>(model, ip, cap, dI);
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(I, dI, npix * dm.F * 8, cudaMemcpyDeviceToHost, model->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     cudaFree(dxy);
     cudaFree(dI);
     cudaFree(dmax);
-    if (e != cudaSuccess) return cuda_fail(e, "image_new");
+    if (e != cudaSuccess) return cuda_fail(e, who.c_str());
     if (ImX) std::copy(hx.begin(), hx.end(), ImX);
     if (ImY) std::copy(hy.begin(), hy.end(), ImY);
     return mgr_sync(model);
 }
+
+}  // namespace mgr
+
+using namespace mgr;
+
+extern "C" {
+
+int mgr_image(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY) {
+    return image_old_impl(model, precision, ray_nr, I, ImX, ImY, false, "mgr_image");
+}
+
+int mgr_image_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny, double* I,
+                  double* ImX, double* ImY) {
+    return image_new_impl(model, precision, raydir, nx, ny, I, ImX, ImY, false, "mgr_image_new");
+}
+
+int mgr_image_optical_depth(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY) {
+    return image_old_impl(model, precision, ray_nr, I, ImX, ImY, true, "mgr_image_optical_depth");
+}
+
+int mgr_image_optical_depth_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny,
+                                double* I, double* ImX, double* ImY) {
+    return image_new_impl(model, precision, raydir, nx, ny, I, ImX, ImY, true, "mgr_image_optical_depth_new");
+}
+
+
 
 }  // extern "C"

@@ -971,11 +971,11 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
 // 2 Su[last] - I_bdy(nr[last], nu(o, f)), Su[last] being the last row's solution.  The
 // ray's elements use all-line interpolation (kAllLines) and the halves' shift0.  With
 // nf = 0 (new imager) the origin itself is the last element.
-template <int MODE, int AP>
+template <int MODE, int AP, bool TAU = false>
 __host__ __device__ double image_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
                                       int nb, const HalfSmem& fw, int nf) {
     using T = typename Real_<MODE>::T;
-    if (nb <= 0 && nf <= 0) return boundary_intensity(m, c.o, c.freq);
+    if (nb <= 0 && nf <= 0) return TAU ? 0.0 : boundary_intensity(m, c.o, c.freq);
     const Elem cen = centre_elem(c.o, bk.cshift, (float)dsub_rn(bk.cshift, 1.0));
     ElemIter ib, iu;
     int phase;  // 0: backward half, 2: forward half, 3: done
@@ -997,6 +997,7 @@ __host__ __device__ double image_lane(const DevModel& m, const double* sl, const
     }
     const double Ibdy_f = boundary_intensity(m, prev.nr, c.freq * bshift);
     EC<MODE> ec_prev{T(0), T(0), false};
+    double tau = 0.0;
     Sweep st{0.0, 0.0, 0.0, 0.0, 0.0, false};
     T dt_prev = T(0), S_last = T(0);
     Elem last = prev;
@@ -1023,7 +1024,11 @@ __host__ __device__ double image_lane(const DevModel& m, const double* sl, const
         EC<MODE> ec_cur{T(0), T(0), false};
         PairOut<MODE> po;
         eval_pair<MODE, AP>(m, sl, c, h, prev, cur, dz, dzf, ec_prev, ec_cur, po);
-        if (first) {
+        if constexpr (TAU) {
+            // image_optical_depth (solver.tpp:2718-2760): the pairs' optical depths summed
+            // from first to last
+            tau += (double)po.dtau;
+        } else if (first) {
             const double dt = po.dtau;
             const double inverse_dtau = drcp<MODE>(dt);
             const double Cb = 2.0 * inverse_dtau * inverse_dtau;
@@ -1044,6 +1049,7 @@ __host__ __device__ double image_lane(const DevModel& m, const double* sl, const
         ec_prev = ec_cur;
         if (phase == 1 && nf <= 0) break;  // the origin is the last element
     }
+    if constexpr (TAU) return tau;
     // last row (solver.tpp:2284-2297)
     double lshift = last.shift;
     if constexpr (MODE == MODE_SPLIT) {

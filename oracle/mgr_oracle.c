@@ -900,7 +900,44 @@ int orc_formal_solve_sc0(const OrcModel* m, double* J, double* I, double* u, dou
 /* ------------------------------------------------------------------ */
 /* Old imager (solver.tpp:542-574, :2462-2574)                          */
 /* ------------------------------------------------------------------ */
+/* Solver::image_optical_depth(model, o, f) (solver.tpp:2718-2760): the sum of the pair
+ * optical depths from first to last. */
+static double optical_depth(const OrcModel* m, Buf* b, uint32_t o, uint32_t f) {
+    const double freq = m->nu[(size_t)o * m->nfreqs + f];
+    const uint32_t l  = m->corr_line[f];
+    const uint32_t first = b->first, last = b->last;
+    double chi_c = 0.0, chi_n = 0.0, dtau_n = 0.0, term_c = 0.0, term_n = 0.0;
+    int cco = 1;
+    double tau = 0.0;
+    compute_source_dtau(m, b->nr[first], b->nr[first + 1], b->nr_interp[first], b->nr_interp[first + 1], l,
+                        freq * b->shift[first], freq * b->shift[first + 1], b->shift[first],
+                        b->shift[first + 1], b->dZ[first], b->interp_factor[first],
+                        b->interp_factor[first + 1], &cco, &dtau_n, &chi_c, &chi_n, &term_c, &term_n);
+    tau += dtau_n;
+    for (uint32_t n = first + 1; n < last; n++) {
+        term_c = term_n;
+        chi_c  = chi_n;
+        compute_source_dtau(m, b->nr[n], b->nr[n + 1], b->nr_interp[n], b->nr_interp[n + 1], l,
+                            freq * b->shift[n], freq * b->shift[n + 1], b->shift[n], b->shift[n + 1],
+                            b->dZ[n], b->interp_factor[n], b->interp_factor[n + 1], &cco, &dtau_n,
+                            &chi_c, &chi_n, &term_c, &term_n);
+        tau += dtau_n;
+    }
+    return tau;
+}
+
+static int image_fo2_impl(const OrcModel* m, uint32_t rr, double* I, int nthreads, int tau);
+
 int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads) {
+    return image_fo2_impl(m, rr, I, nthreads, 0);
+}
+
+/* Solver::image_optical_depth(model, rr) (solver.tpp:655-684). */
+int orc_image_optical_depth(const OrcModel* m, uint32_t rr, double* I, int nthreads) {
+    return image_fo2_impl(m, rr, I, nthreads, 1);
+}
+
+static int image_fo2_impl(const OrcModel* m, uint32_t rr, double* I, int nthreads, int tau) {
     const uint32_t P = m->npoints, F = m->nfreqs;
     const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
     const uint32_t ar     = m->antipod[rr];
@@ -931,7 +968,9 @@ int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads) {
             b.last  = (uint32_t)last;
             b.n_tot = (uint32_t)(last + 1 - first);
             for (uint32_t f = 0; f < F; f++) {
-                if (b.n_tot > 1) {
+                if (tau) {
+                    I[(size_t)o * F + f] = b.n_tot > 1 ? optical_depth(m, &b, o, f) : 0.0;
+                } else if (b.n_tot > 1) {
                     solve_feautrier_order_2(m, &b, o, f, 0);
                     I[(size_t)o * F + f] = 2.0 * b.Su[b.last]
                                          - boundary_intensity(m, b.nr[b.last], m->nu[(size_t)o * F + f]);
@@ -1023,8 +1062,22 @@ static int64_t trace_imaging(const OrcModel* m, Buf* b, const double* origin, ui
     return id1;
 }
 
+static int image_new_impl(const OrcModel* m, const double* raydir_in, uint32_t nx, uint32_t ny, double* I,
+                          double* ImX, double* ImY, int nthreads, int tau);
+
 int orc_image_new(const OrcModel* m, const double* raydir_in, uint32_t nx, uint32_t ny, double* I, double* ImX,
                   double* ImY, int nthreads) {
+    return image_new_impl(m, raydir_in, nx, ny, I, ImX, ImY, nthreads, 0);
+}
+
+/* Solver::image_optical_depth_new_imager (solver.tpp:686-736). */
+int orc_image_optical_depth_new(const OrcModel* m, const double* raydir_in, uint32_t nx, uint32_t ny, double* I,
+                                double* ImX, double* ImY, int nthreads) {
+    return image_new_impl(m, raydir_in, nx, ny, I, ImX, ImY, nthreads, 1);
+}
+
+static int image_new_impl(const OrcModel* m, const double* raydir_in, uint32_t nx, uint32_t ny, double* I,
+                          double* ImX, double* ImY, int nthreads, int tau) {
     const uint32_t P = m->npoints, F = m->nfreqs;
     const double n2 = raydir_in[0] * raydir_in[0] + raydir_in[1] * raydir_in[1] + raydir_in[2] * raydir_in[2];
     if (n2 == 0.0) return -1;
@@ -1136,7 +1189,9 @@ int orc_image_new(const OrcModel* m, const double* raydir_in, uint32_t nx, uint3
             b.n_tot = b.last + 1 - b.first;
             for (uint32_t f = 0; f < F; f++) {
                 const double nu_f = m->nu[(size_t)start * F + f];
-                if (b.n_tot > 1) {
+                if (tau) {
+                    I[(size_t)pp * F + f] = b.n_tot > 1 ? optical_depth(m, &b, start, f) : 0.0;
+                } else if (b.n_tot > 1) {
                     solve_feautrier_order_2(m, &b, start, f, 0);
                     I[(size_t)pp * F + f] = 2.0 * b.Su[b.last] - boundary_intensity(m, b.nr[b.last], nu_f);
                 } else {

@@ -137,6 +137,14 @@ int orc_image_fo2(const OrcModel* m, uint32_t rr, double* I, int nthreads);
 int orc_image_new(const OrcModel* m, const double* raydir, uint32_t nx, uint32_t ny, double* I, double* ImX,
                   double* ImY, int nthreads);
 
+/* Solver::image_optical_depth(model, rr) (solver.tpp:655-684) and
+ * image_optical_depth_new_imager (solver.tpp:686-736): the same rays as orc_image_fo2 /
+ * orc_image_new, I = the summed optical depth from first to last
+ * (image_optical_depth(model, o, f), solver.tpp:2718-2760), 0 for a ray of one point. */
+int orc_image_optical_depth(const OrcModel* m, uint32_t rr, double* I, int nthreads);
+int orc_image_optical_depth_new(const OrcModel* m, const double* raydir, uint32_t nx, uint32_t ny, double* I,
+                                double* ImX, double* ImY, int nthreads);
+
 /* ------------------------------------------------------------------ */
 /* ALI level populations (mgr_oracle_ali.c)                             */
 /* ------------------------------------------------------------------ */

@@ -335,6 +335,33 @@ class Oracle:
             raise RuntimeError(f"oracle new imager failed ({rc})")
         return dict(I=I, ImX=X, ImY=Y)
 
+    def image_optical_depth(self, rr, nthreads=0):
+        P, F = self.a["npoints"], self.a["nfreqs"]
+        I = np.zeros((P, F))
+        l = lib()
+        l.orc_image_optical_depth.restype = C.c_int
+        l.orc_image_optical_depth.argtypes = [C.POINTER(OrcModel), C.c_uint32, _f64p, C.c_int]
+        rc = l.orc_image_optical_depth(C.byref(self.m), rr, _ptr(I, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle optical-depth imager failed ({rc})")
+        return I
+
+    def image_optical_depth_new(self, raydir, nx, ny, nthreads=0):
+        F = self.a["nfreqs"]
+        I = np.zeros((nx * ny, F))
+        X = np.zeros(nx * ny)
+        Y = np.zeros(nx * ny)
+        d = np.ascontiguousarray(raydir, np.float64)
+        l = lib()
+        l.orc_image_optical_depth_new.restype = C.c_int
+        l.orc_image_optical_depth_new.argtypes = [C.POINTER(OrcModel), _f64p, C.c_uint32, C.c_uint32, _f64p, _f64p,
+                                                  _f64p, C.c_int]
+        rc = l.orc_image_optical_depth_new(C.byref(self.m), _ptr(d, _f64p), nx, ny, _ptr(I, _f64p), _ptr(X, _f64p),
+                                           _ptr(Y, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle optical-depth new imager failed ({rc})")
+        return dict(I=I, ImX=X, ImY=Y)
+
     def image_fo2(self, rr, nthreads=0):
         P, F = self.a["npoints"], self.a["nfreqs"]
         I = np.zeros((P, F))

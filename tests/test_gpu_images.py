@@ -85,3 +85,42 @@ def test_core_model_compute_image_new(gpu_lib):
     np.testing.assert_array_equal(np.array(im.ImX), ref["ImX"])
     model.compute_image(ray_nr)
     assert np.isfinite(np.array(model.images[-1].I)).all()
+
+
+@pytest.mark.parametrize("approx", ["CloseLines", "None"])
+def test_optical_depth_images_match_oracle(gpu_lib, approx):
+    """compute_image_optical_depth(_new): the imagers' rays, optical depth summed over
+    the pairs; 1e-5 of the oracle in FP64 and split precision."""
+    raw = S.grid_sphere(n=16, nside=1, nquads=7)
+    a = H.setup(raw, approx=approx)
+    orc = O.Oracle(a)
+    ref_old = orc.image_optical_depth(3)
+    d = np.array([0.3, -0.5, 0.81])
+    ref_new = orc.image_optical_depth_new(d, 24, 20)
+    dev = _abi.DeviceModel(a)
+    try:
+        for precision in ("fp64", "split"):
+            g = dev.image_optical_depth(3, precision)
+            assert H.max_rel(g["I"], ref_old, floor=1e-12 * np.abs(ref_old).max()) < 1e-5, precision
+            g2 = dev.image_optical_depth_new(d, 24, 20, precision)
+            np.testing.assert_array_equal(g2["ImX"], ref_new["ImX"])
+            assert H.max_rel(g2["I"], ref_new["I"], floor=1e-12 * np.abs(ref_new["I"]).max()) < 1e-5, precision
+    finally:
+        dev.close()
+
+
+def test_core_model_optical_depth_images(gpu_lib):
+    from magritte_gb300 import loader
+
+    raw = S.grid_cube(n=10, nquads=5)
+    a = H.setup(raw)
+    ref = O.Oracle(a).image_optical_depth(1)
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    model.compute_image_optical_depth(1)
+    model.compute_image_optical_depth_new(1, 16, 16)
+    assert [im.imageType for im in model.images] == [1, 1]
+    assert H.max_rel(np.array(model.images[0].I), ref, floor=1e-12 * np.abs(ref).max()) < 1e-5
+    assert np.array(model.images[1].I).shape == (256, raw.nquads)

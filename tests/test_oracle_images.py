@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 from scipy.special import erf
 
+import helpers as H
 import oracle as O
 from magritte_gb300 import synthetic as S
 
@@ -74,3 +75,40 @@ def test_new_imager_constant_velocity_gradient_3d():
     err = np.abs(2.0 * (im - im_a) / (im + im_a))[:-1]
     assert np.isfinite(im).all()
     assert err.max() < 1.5e-3, err.max()
+
+
+def test_optical_depth_image_all_constant_known_answer():
+    """Optical-depth images (Solver::image_optical_depth, solver.tpp:655-684, 2718-2760)
+    of the all-constant single ray: along the ray the optical depth is chi times the
+    ray's length, for every model point (each point's ray spans the whole line)."""
+    raw = H.all_constant_model()
+    a = H.setup(raw)
+    tau = O.Oracle(a).image_optical_depth(0)
+    ld = raw.linedata[0]
+    temp, nTT = raw.temperature[0], raw.abundance[0, 0]
+    frq = ld.frequency[0]
+    pop = ld.weight * np.exp(-ld.energy / (H.KB * temp))
+    pop = pop / pop.sum() * nTT
+    width = frq * np.sqrt(2.0 * H.KB * temp / (H.AMU * H.CC**2) * ld.inverse_mass + raw.vturb2[0])
+    phi = 1.0 / (width * np.sqrt(np.pi))
+    op = H.HH * frq / (4.0 * np.pi) * (ld.Ba[0] * pop[0] - ld.Bs[0] * pop[1])
+    length = raw.position[-1, 0] - raw.position[0, 0]
+    expect = (op * phi + a["min_opacity"]) * length
+    assert np.max(np.abs(tau - expect) / expect) < 1e-5
+
+
+def test_optical_depth_new_image_sums_the_imager_pairs():
+    """The new optical-depth imager traces the same pixel rays as the new imager: a
+    model without emission still has a positive optical depth where a pixel ray
+    crosses the model and zero where it only touches a boundary point."""
+    raw = S.velocity_gradient_shells(nshells=6)
+    fcen = raw.linedata[0].frequency[0]
+    dd = 1.0e4 / 2.99792458e8
+    a = H.setup(raw, max_width_fraction=0.5, image_freqs=(fcen - fcen * dd, fcen + fcen * dd, 9))
+    d = raw.ray_direction[raw.nrays // 2 - 1]
+    orc = O.Oracle(a)
+    t = orc.image_optical_depth_new(d, 20, 20)
+    img = orc.image_new(d, 20, 20)
+    np.testing.assert_array_equal(t["ImX"], img["ImX"])
+    assert np.all(t["I"] >= 0.0)
+    assert (t["I"] > 0.0).any()
