@@ -154,6 +154,17 @@ int mgr_formal_solve_fo2_sparse(MgrModel* model, int precision, double* Jlin, do
 /* Device-pointer variant; enqueued on the model's stream. */
 int mgr_formal_solve_fo2_sparse_device(MgrModel* model, int precision, double* Jlin_dev, double* lambda_diag_dev);
 
+/* Model::compute_radiation_field_feautrier_order_2_anis (model.cpp:435-472 ->
+ * Solver::solve_feautrier_order_2_anis, solver.tpp:366-456): per line, with
+ * du = w_z w_rr u summed over ray pairs and quadrature points (ray pair outer):
+ *   J [P][L]        sum 2 du                                 (LineProducingSpecies::J)
+ *   J2_0            sum (3 n_z^2 - 1)/sqrt(2) du
+ *   J2_1_Re, _Im    sum -sqrt(3) n_x n_z du, -sqrt(3) n_y n_z du
+ *   J2_2_Re, _Im    sum sqrt(3)/2 (n_x^2 - n_y^2) du, sqrt(3) n_x n_y du
+ * n the ray pair's direction.  Host buffers (all but J may be NULL); blocks. */
+int mgr_formal_solve_fo2_anis(MgrModel* model, int precision, double* J, double* J2_0, double* J2_1_Re,
+                              double* J2_1_Im, double* J2_2_Re, double* J2_2_Im);
+
 /* Partial formal solve over the ray pairs [rr_begin, rr_end) only: J_dev [P][F] and
  * lambda_diag_dev [P][L] (may be NULL) receive the sums over those ray pairs, so that
  * the sum over disjoint ranges covering [0, hnrays) is the full solve's J and ALO

@@ -114,6 +114,7 @@ SIGNATURES = {
     "mgr_compute_jeff": (C.c_int, [C.c_void_p, C.c_uint32, _f64p, _f64p, _f64p]),
     "mgr_compute_jeff_sparse": (C.c_int, [C.c_void_p, C.c_uint32, _f64p, _f64p]),
     "mgr_formal_solve_fo2_sparse": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p]),
+    "mgr_formal_solve_fo2_anis": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]),
     "mgr_formal_solve_fo2_sparse_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "mgr_compute_level_populations_sparse": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_long,
                                                        C.POINTER(MgrAliParams), C.POINTER(C.c_int), _f64p, _f64p,
@@ -395,6 +396,13 @@ class DeviceModel:
         lam = np.empty((self.P, self.L))
         _check(load().mgr_formal_solve_fo2_sparse(self.h, PRECISION[precision], _ptr(Jl, _f64p), _ptr(lam, _f64p)))
         return dict(Jlin=Jl, lambda_diag=lam)
+
+    def formal_solve_fo2_anis(self, precision="fp64"):
+        """Anisotropic solve: line-integrated J and the J2 tensor elements [P][L]."""
+        keys = ("J", "J2_0", "J2_1_Re", "J2_1_Im", "J2_2_Re", "J2_2_Im")
+        out = {k: np.empty((self.P, self.L)) for k in keys}
+        _check(load().mgr_formal_solve_fo2_anis(self.h, PRECISION[precision], *[_ptr(out[k], _f64p) for k in keys]))
+        return out
 
     def compute_jeff_sparse(self, l=0):
         out = {k: np.empty((self.P, self.nrad[l])) for k in ("Jlin", "Jeff")}

@@ -201,6 +201,11 @@ PYBIND11_MODULE(core, m) {
         .def_readwrite("population", &LineProducingSpecies::population)
         .def_readwrite("population_tot", &LineProducingSpecies::population_tot)
         .def_readwrite("J", &LineProducingSpecies::J)
+        .def_readwrite("J2_0", &LineProducingSpecies::J2_0)
+        .def_readwrite("J2_1_Re", &LineProducingSpecies::J2_1_Re)
+        .def_readwrite("J2_1_Im", &LineProducingSpecies::J2_1_Im)
+        .def_readwrite("J2_2_Re", &LineProducingSpecies::J2_2_Re)
+        .def_readwrite("J2_2_Im", &LineProducingSpecies::J2_2_Im)
         .def_readwrite("Jlin", &LineProducingSpecies::Jlin)
         .def_readwrite("Jeff", &LineProducingSpecies::Jeff)
         .def_readwrite("Jdif", &LineProducingSpecies::Jdif)
@@ -292,6 +297,8 @@ PYBIND11_MODULE(core, m) {
         .def("compute_radiation_field_feautrier_order_2_sparse",
              &Model::compute_radiation_field_feautrier_order_2_sparse, py::call_guard<py::gil_scoped_release>())
         .def("compute_Jeff_sparse", &Model::compute_Jeff_sparse, py::call_guard<py::gil_scoped_release>())
+        .def("compute_radiation_field_feautrier_order_2_anis", &Model::compute_radiation_field_feautrier_order_2_anis,
+             py::call_guard<py::gil_scoped_release>())
         .def("compute_level_populations_sparse", &Model::compute_level_populations_sparse,
              py::arg("use_Ng_acceleration"), py::arg("max_niterations"), py::call_guard<py::gil_scoped_release>())
         .def_readonly("error_mean", &Model::error_mean)

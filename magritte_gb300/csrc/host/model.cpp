@@ -663,6 +663,29 @@ int Model::compute_radiation_field_feautrier_order_2_sparse() {
     return 0;
 }
 
+// Model::compute_radiation_field_feautrier_order_2_anis (model.cpp:435-472): J and the
+// anisotropy tensor elements per species.
+int Model::compute_radiation_field_feautrier_order_2_anis() {
+    MgrModel* dev = upload();
+    const Size P = parameters.npoints_.v, L = parameters.nlines_.v;
+    std::vector<double> buf(6 * (size_t)P * L);
+    double* o[6];
+    for (int k = 0; k < 6; k++) o[k] = buf.data() + k * (size_t)P * L;
+    check(mgr_formal_solve_fo2_anis(dev, parameters.precision, o[0], o[1], o[2], o[3], o[4], o[5]));
+    for (Size l = 0; l < parameters.nlspecs_.v; l++) {
+        LineProducingSpecies& ls = lines.lineProducingSpecies[l];
+        const Size nrad = ls.linedata.nrad;
+        Array<double>* dst[6] = {&ls.J, &ls.J2_0, &ls.J2_1_Re, &ls.J2_1_Im, &ls.J2_2_Re, &ls.J2_2_Im};
+        for (int k = 0; k < 6; k++) {
+            dst[k]->resize({P, nrad});
+            for (Size p = 0; p < P; p++)
+                for (Size r = 0; r < nrad; r++)
+                    (*dst[k])[(size_t)p * nrad + r] = o[k][(size_t)p * L + lines.nrad_cum[l] + r];
+        }
+    }
+    return 0;
+}
+
 // Model::compute_Jeff_sparse (model.cpp:549-570)
 int Model::compute_Jeff_sparse() {
     if (!dev_ || lines.lineProducingSpecies.empty() || lines.lineProducingSpecies[0].J.size() == 0)

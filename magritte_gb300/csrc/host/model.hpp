@@ -190,7 +190,8 @@ struct LineProducingSpecies {
     Quadrature quadrature;
     Array<double> population;      // [P*nlev]
     Array<double> population_tot;  // [P]
-    Array<double> J;                 // [P][nrad] line-integrated J of the memory-lean solve
+    Array<double> J;                 // [P][nrad] line-integrated J of the memory-lean / anisotropic solves
+    Array<double> J2_0, J2_1_Re, J2_1_Im, J2_2_Re, J2_2_Im;  // [P][nrad] anisotropy tensor elements
     Array<double> Jlin, Jeff, Jdif;  // [P][nrad]
     Array<double> lambda_diag;     // [P][nrad] summed diagonal ALO
     Array<uint8_t> lambda_has;     // [P][nrad]
@@ -279,6 +280,7 @@ class Model {
     int compute_Jeff();
     int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
     int compute_radiation_field_feautrier_order_2_sparse();
+    int compute_radiation_field_feautrier_order_2_anis();
     int compute_Jeff_sparse();
     int compute_level_populations_sparse(bool use_Ng_acceleration, long max_niterations);
 

@@ -615,6 +615,35 @@ int mgr_formal_solve_fo2_sparse(MgrModel* model, int precision, double* Jlin, do
     return read_status(model);
 }
 
+int mgr_formal_solve_fo2_anis(MgrModel* model, int precision, double* J, double* J2_0, double* J2_1_Re,
+                              double* J2_1_Im, double* J2_2_Re, double* J2_2_Im) {
+    if (!model || !J) {
+        set_error("mgr_formal_solve_fo2_anis: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
+        set_error("mgr_formal_solve_fo2_anis: unknown precision mode");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!model->line_disc) {
+        set_error("mgr_formal_solve_fo2_anis: the formal solve needs a line spectral discretisation");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    const DevModel& dm = model->dm;
+    const size_t PL = (size_t)dm.P * dm.L;
+    int rc = ensure_scratch(model, &model->work, &model->work_bytes, fo2_work_bytes(model, dm.P, true, false));
+    if (rc != MGR_OK) return rc;
+    // the six [P][L] results live in the u scratch
+    if ((rc = ensure_scratch(model, &model->u_scratch, &model->u_scratch_bytes, 6 * PL * 8)) != MGR_OK) return rc;
+    cudaError_t e = launch_fo2_range(model, precision, 0, dm.P, nullptr, nullptr, nullptr, model->work,
+                                     model->work_bytes, 0, dm.hnrays, nullptr, model->u_scratch);
+    double* outs[6] = {J, J2_0, J2_1_Re, J2_1_Im, J2_2_Re, J2_2_Im};
+    for (int k = 0; k < 6 && e == cudaSuccess; k++)
+        if (outs[k]) e = cudaMemcpyAsync(outs[k], model->u_scratch + k * PL, PL * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "anisotropic formal solve");
+    return read_status(model);
+}
+
 int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, double* lambda_diag) {
     if (!model || !J) {
         set_error("mgr_formal_solve_fo2: null argument");

@@ -2,12 +2,10 @@
 //
 // Each model is an ordinary MgrModel (mgr_model_create); a batch collects their device
 // descriptions into one device array and solves all of them with one kernel launch.
-// The unit of work is one (model, origin) item handled by one warp: the warp walks the
-// origin's (ray pair, frequency) tasks 32 at a time, one per lane, with the traces of
-// the ray pairs a pass touches (up to four) held in shared memory, so that models with
-// few frequencies still fill the lanes; every lane runs the single-model kernel's
-// solve_lane.  J and the ALO diagonal of the
-// origin are kept in shared memory, summed in the reference's order (ray pair outer,
+// The unit of work is one (model, origin) item handled by one warp: the warp traces
+// and solves every ray pair of its origin in turn (lanes over frequencies, the same
+// solve_lane code as the single-model kernel) and keeps J and the ALO diagonal of the
+// origin in shared memory, summed in the reference's order (ray pair outer,
 // quadrature point inner; Solver::solve_feautrier_order_2, solver.tpp:476-540, and
 // Lambda via update_Lambda, solver.tpp:1760-1850).  Every model's J and ALO diagonal
 // are therefore the values its own mgr_formal_solve_fo2 returns, bit for bit, with no
@@ -51,22 +49,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Ray pairs whose traces a warp holds at once: the lanes of one pass take 32
-// consecutive (ray pair, frequency) tasks of the origin, which span at most kSlots
-// ray pairs (fewer lanes run when a model has fewer than 32 / (kSlots - 1) frequencies).
-constexpr uint32_t kSlots = 4;
-
 // Per-warp shared memory: sorted line centres [L_max], J accumulators [F_max], the
-// L_diag values of the held ray pairs [kSlots][F_max], the origin's ray-independent
-// ALO factors [F_max] (LambdaFactors), the held traces' lengths [2 kSlots], then the
-// trace halves of the held ray pairs [kSlots].
+// current ray pair's L_diag values [F_max], the origin's ray-independent ALO factors
+// [F_max] (LambdaFactors), then the two trace halves.
 __host__ __device__ inline size_t batch_head_bytes(uint32_t F_max, uint32_t L_max) {
-    const size_t head = ((size_t)L_max + (1 + kSlots) * (size_t)F_max) * 8 +
-                        (size_t)F_max * sizeof(LambdaFactors) + 2 * kSlots * sizeof(int);
+    const size_t head = ((size_t)L_max + 2 * (size_t)F_max) * 8 + (size_t)F_max * sizeof(LambdaFactors);
     return (head + 15) & ~size_t(15);
 }
 __host__ __device__ inline size_t batch_warp_bytes(uint32_t cap, uint32_t F_max, uint32_t L_max) {
-    return batch_head_bytes(F_max, L_max) + kSlots * half_bytes_per_warp(cap);
+    return batch_head_bytes(F_max, L_max) + half_bytes_per_warp(cap);
 }
 
 template <int MODE, int AP, int MINB>
@@ -82,11 +73,10 @@ __global__ void __launch_bounds__(256, MINB)
     unsigned char* base = smem + (size_t)w * batch_warp_bytes(cap, F_max, L_max);
     double* sl = reinterpret_cast<double*>(base);
     double* Jacc = sl + L_max;
-    double* LDr = Jacc + F_max;  // [kSlots][F_max]
-    LambdaFactors* LF = reinterpret_cast<LambdaFactors*>(LDr + kSlots * F_max);
-    int* nbf = reinterpret_cast<int*>(LF + F_max);  // [kSlots] nb, then [kSlots] nf
-    unsigned char* traces = base + batch_head_bytes(F_max, L_max);
-    const size_t tbytes = half_bytes_per_warp(cap);
+    double* LDr = Jacc + F_max;
+    LambdaFactors* LF = reinterpret_cast<LambdaFactors*>(LDr + F_max);
+    HalfSmem bk, fw;
+    carve_halves(base + batch_head_bytes(F_max, L_max), cap, bk, fw);
     if (threadIdx.x == 0) atomicMin(&tstamp[2 * n_models], global_ns());
 
     const uint64_t n_items = offsets[n_models];
@@ -108,72 +98,42 @@ __global__ void __launch_bounds__(256, MINB)
             for (uint32_t f = lane; f < m.F; f += 32)
                 if (m.in_line[f]) LF[f] = lambda_factors(m, sl, o, f);
         __syncwarp();
-        const uint32_t F = m.F, R = m.hnrays;
-        const uint64_t T = (uint64_t)R * F;  // (ray pair, frequency) tasks of the origin
-        uint64_t t0 = 0;
-        uint32_t traced = 0, lam_next = 0;
-        while (t0 < T) {
-            const uint32_t rr_lo = (uint32_t)(t0 / F);
-            uint64_t t_end = t0 + 32;
-            if (t_end > T) t_end = T;
-            if (t_end > (uint64_t)(rr_lo + kSlots) * F) t_end = (uint64_t)(rr_lo + kSlots) * F;
-            const uint32_t rr_hi = (uint32_t)((t_end - 1) / F);
-            // trace the pass's new ray pairs into their slots (slot = rr mod kSlots; a
-            // slot's previous ray pair is finished, its ALO included)
-            for (uint32_t rr = traced; rr <= rr_hi; rr++) {
-                HalfSmem bk, fw;
-                carve_halves(traces + (size_t)(rr % kSlots) * tbytes, cap, bk, fw);
-                const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-                const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
-                if (lane == 0) {
-                    nbf[rr % kSlots] = nb;
-                    nbf[kSlots + rr % kSlots] = nf;
+        for (uint32_t rr = 0; rr < m.hnrays && ok; rr++) {
+            const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
+            const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+            if (nb < 0 || nf < 0) {  // status recorded by the trace
+                ok = false;
+                break;
+            }
+            const double w2 = m.rayw[rr];
+            for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
+                const uint32_t f = f0 + lane;
+                if (f < m.F) {
+                    LaneCtx c;
+                    c.o = o;
+                    c.f = f;
+                    c.l0 = m.corr_line[f];
+                    c.freq = m.nu[(size_t)o * m.F + f];
+                    c.fq = (float)c.freq;
+                    c.a0 = (float)(c.freq - m.line[c.l0]);
+                    const LaneResult r = solve_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
+                    Jacc[f] += r.u * 2.0 * w2;
+                    LDr[f] = r.solved ? r.Ldiag : 0.0;
+                    if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
                 }
-                if (nb < 0 || nf < 0) ok = false;  // status recorded by the trace
             }
-            traced = rr_hi + 1;
             __syncwarp();
-            if (!ok) break;
-            // one task per lane
-            const uint64_t t = t0 + lane;
-            const bool active = t < t_end;
-            const uint32_t rr = active ? (uint32_t)(t / F) : rr_lo;
-            const uint32_t f = active ? (uint32_t)(t % F) : 0;
-            const uint32_t slot = rr % kSlots;
-            LaneResult r{0.0, 0.0, false};
-            if (active) {
-                HalfSmem bk, fw;
-                carve_halves(traces + (size_t)slot * tbytes, cap, bk, fw);
-                LaneCtx c;
-                c.o = o;
-                c.f = f;
-                c.l0 = m.corr_line[f];
-                c.freq = m.nu[(size_t)o * F + f];
-                c.fq = (float)c.freq;
-                c.a0 = (float)(c.freq - m.line[c.l0]);
-                r = solve_lane<MODE, AP>(m, sl, c, bk, nbf[slot], fw, nbf[kSlots + slot]);
-                LDr[(size_t)slot * F_max + f] = r.solved ? r.Ldiag : 0.0;
-                if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
-            }
-            // J in the reference's order: ray pairs of the pass one after the other
-            for (uint32_t g = rr_lo; g <= rr_hi; g++) {
-                if (active && rr == g) Jacc[f] += r.u * 2.0 * m.rayw[g];
-                __syncwarp();
-            }
-            // ALO of the ray pairs this pass completed, in ray-pair order
-            for (; want_lam && (uint64_t)(lam_next + 1) * F <= t_end; lam_next++) {
-                const double w2 = m.rayw[lam_next];
-                const double* LDs = LDr + (size_t)(lam_next % kSlots) * F_max;
+            if (want_lam) {
                 // line l: lane q holds the element of quadrature point q, added in q order
                 for (uint32_t l = 0; l < m.L; l++) {
                     const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
                     double s = __shfl_sync(FULL_MASK, lam_acc, l & 31);
-                    if (l >= 32) s = lam_next ? Lout[mi][(size_t)o * m.L + l] : 0.0;  // running sum kept in the output
+                    if (l >= 32) s = rr ? Lout[mi][(size_t)o * m.L + l] : 0.0;  // running sum kept in the output
                     for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
-                        const uint32_t fq = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
-                        const bool valid = fq != 0xffffffffu && m.in_line[fq];
+                        const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
+                        const bool valid = f != 0xffffffffu && m.in_line[f];
                         double e = 0.0;
-                        if (valid) e = lambda_element(LF[fq], w2, LDs[fq]);
+                        if (valid) e = lambda_element(LF[f], w2, LDr[f]);
                         const uint32_t nq = min(32u, m.Q - q0);
                         for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
                     }
@@ -186,7 +146,6 @@ __global__ void __launch_bounds__(256, MINB)
                     __syncwarp();
                 }
             }
-            t0 = t_end;
         }
         if (ok) {
             double* J = Jout[mi] + (size_t)o * m.F;

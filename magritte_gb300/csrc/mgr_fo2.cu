@@ -196,7 +196,8 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
                                                          const double* __restrict__ U, size_t u_stride, uint32_t u_o0,
                                                          const double* __restrict__ LD, size_t ld_stride,
                                                          uint32_t ld_o0, double* __restrict__ J,
-                                                         double* __restrict__ lam, double* __restrict__ Jlin) {
+                                                         double* __restrict__ lam, double* __restrict__ Jlin,
+                                                         double* __restrict__ anis) {
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -227,6 +228,50 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
                     }
                 }
                 if (lane == 0) Jlin[(size_t)o * m.L + l] = s;
+            }
+        }
+        if (anis) {
+            // line-integrated J and anisotropy tensor elements (solve_feautrier_order_2_anis,
+            // solver.tpp:366-456): du = w_z w_rr u, J += 2 du, J2_x += wt_x(n) du, in (rr, z) order
+            const double sqrt3 = sqrt(3.0), inv_sqrt2 = 1.0 / sqrt(2.0);
+            const size_t PL = (size_t)m.P * m.L;
+            for (uint32_t l = w; l < m.L; l += nw) {
+                const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
+                double sJ = 0.0, s0 = 0.0, s1r = 0.0, s1i = 0.0, s2r = 0.0, s2i = 0.0;
+                for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
+                    const double* Ur = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
+                    const double wt = m.rayw[rr];
+                    const double nx = m.raydir[3 * rr], ny = m.raydir[3 * rr + 1], nz = m.raydir[3 * rr + 2];
+                    const double wt_0 = inv_sqrt2 * (3.0 * nz * nz - 1.0);
+                    const double wt_1_Re = -sqrt3 * nx * nz;
+                    const double wt_1_Im = -sqrt3 * ny * nz;
+                    const double wt_2_Re = 0.5 * sqrt3 * (nx * nx - ny * ny);
+                    const double wt_2_Im = sqrt3 * nx * ny;
+                    for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
+                        const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
+                        const double du =
+                            f != 0xffffffffu ? (m.quad_w[(size_t)m.corr_lspec[f] * m.Q + q0 + lane] * wt) * Ur[f] : 0.0;
+                        const uint32_t nq = min(32u, m.Q - q0);
+                        for (uint32_t j = 0; j < nq; j++) {
+                            const double d = __shfl_sync(FULL_MASK, du, j);
+                            sJ += 2.0 * d;
+                            s0 += wt_0 * d;
+                            s1r += wt_1_Re * d;
+                            s1i += wt_1_Im * d;
+                            s2r += wt_2_Re * d;
+                            s2i += wt_2_Im * d;
+                        }
+                    }
+                }
+                if (lane == 0) {
+                    const size_t i = (size_t)o * m.L + l;
+                    anis[i] = sJ;
+                    anis[PL + i] = s0;
+                    anis[2 * PL + i] = s1r;
+                    anis[3 * PL + i] = s1i;
+                    anis[4 * PL + i] = s2r;
+                    anis[5 * PL + i] = s2i;
+                }
             }
         }
         if (!lam) continue;
@@ -483,7 +528,7 @@ static cudaError_t launch_fo2_approx(MgrModel* model, uint32_t o_begin, uint32_t
 
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
                              double* lam, double* work, size_t work_bytes, uint32_t rr_begin, uint32_t rr_end,
-                             double* Jlin) {
+                             double* Jlin, double* anis) {
     const DevModel& m = model->dm;
     if (o_end <= o_begin) return cudaSuccess;
     if (rr_end > m.hnrays) rr_end = m.hnrays;
@@ -525,7 +570,7 @@ cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, u
         unsigned grid = n < (uint32_t)nsm * 16 ? n : (unsigned)nsm * 16;
         count_launch();
         fo2_reduce_kernel<<<grid, 128, 0, model->stream>>>(m, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, J, lam,
-                                                           Jlin);
+                                                           Jlin, anis);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

@@ -89,10 +89,11 @@ constexpr size_t kFo2WorkBudget = size_t(2) << 30;
 size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, bool stage_ld);
 // Ray pairs [rr_begin, rr_end) only (partial J / ALO sums, u must then be NULL).
 // J may be NULL; Jlin [P][L] (may be NULL) receives the line-integrated J in the order
-// of the memory-lean solve.
+// of the memory-lean solve; anis [6][P][L] (may be NULL) the line-integrated J and
+// anisotropy tensor elements of the anisotropic solve.
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
                              double* lam, double* work, size_t work_bytes, uint32_t rr_begin = 0,
-                             uint32_t rr_end = 0xffffffffu, double* Jlin = nullptr);
+                             uint32_t rr_end = 0xffffffffu, double* Jlin = nullptr, double* anis = nullptr);
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
                                 uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
                                 double* d_dZ);

@@ -298,6 +298,33 @@ class Oracle:
             raise RuntimeError(f"oracle formal solve failed ({rc})")
         return dict(J=J, u=u, lambda_diag=lam, lambda_has=has)
 
+    def formal_solve_fo2_anis(self):
+        """Solver::solve_feautrier_order_2_anis (solver.tpp:366-456) from this oracle's u:
+        per line, du = (w_z w_rr) u, J += 2 du and the J2 tensor elements += wt_x(n) du,
+        ray pair outer, quadrature point inner.  Returns [P][L] arrays."""
+        a = self.a
+        P, L, R = a["npoints"], a["nlines"], a["hnrays"]
+        u = self.formal_solve_fo2(want_u=True)["u"]
+        sqrt3, inv_sqrt2 = np.sqrt(3.0), 1.0 / np.sqrt(2.0)
+        out = {k: np.zeros((P, L)) for k in ("J", "J2_0", "J2_1_Re", "J2_1_Im", "J2_2_Re", "J2_2_Im")}
+        fq = [[None] * a["nquads"] for _ in range(L)]
+        for f in range(a["nfreqs"]):
+            fq[a["corr_line"][f]][a["corr_z"][f]] = f
+        for rr in range(R):
+            nx, ny, nz = a["ray_direction"][rr]
+            wt = a["ray_weight"][rr]
+            w = {"J2_0": inv_sqrt2 * (3.0 * nz * nz - 1.0), "J2_1_Re": -sqrt3 * nx * nz,
+                 "J2_1_Im": -sqrt3 * ny * nz, "J2_2_Re": 0.5 * sqrt3 * (nx * nx - ny * ny),
+                 "J2_2_Im": sqrt3 * nx * ny}
+            for l in range(L):
+                for z in range(a["nquads"]):
+                    f = fq[l][z]
+                    du = (a["quad_weights"][a["corr_lspec"][f], z] * wt) * u[rr, :, f]
+                    out["J"][:, l] += 2.0 * du
+                    for k, wk in w.items():
+                        out[k][:, l] += wk * du
+        return out
+
     def formal_solve_fo2_range(self, rr0, rr1, o0, o1, nthreads=0):
         P, F = self.a["npoints"], self.a["nfreqs"]
         J = np.zeros((P, F))
