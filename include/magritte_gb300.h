@@ -154,6 +154,13 @@ int mgr_formal_solve_fo2_sparse(MgrModel* model, int precision, double* Jlin, do
 /* Device-pointer variant; enqueued on the model's stream. */
 int mgr_formal_solve_fo2_sparse_device(MgrModel* model, int precision, double* Jlin_dev, double* lambda_diag_dev);
 
+/* Model::compute_radiation_field_feautrier_order_2_uv (model.cpp:395-433 ->
+ * Solver::solve_feautrier_order_2_uv, solver.tpp:238-295, :2767-2921): u and v
+ * [hnrays][P][F] per ray pair (radiation.u, radiation.v), v at the origin from the
+ * u of its two neighbours (a boundary difference when the origin ends the ray; 0 for
+ * a ray pair of one point).  Host buffers; blocks. */
+int mgr_formal_solve_fo2_uv(MgrModel* model, int precision, double* u, double* v);
+
 /* Model::compute_radiation_field_feautrier_order_2_anis (model.cpp:435-472 ->
  * Solver::solve_feautrier_order_2_anis, solver.tpp:366-456): per line, with
  * du = w_z w_rr u summed over ray pairs and quadrature points (ray pair outer):

@@ -115,6 +115,7 @@ SIGNATURES = {
     "mgr_compute_jeff_sparse": (C.c_int, [C.c_void_p, C.c_uint32, _f64p, _f64p]),
     "mgr_formal_solve_fo2_sparse": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p]),
     "mgr_formal_solve_fo2_anis": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]),
+    "mgr_formal_solve_fo2_uv": (C.c_int, [C.c_void_p, C.c_int, _f64p, _f64p]),
     "mgr_formal_solve_fo2_sparse_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "mgr_compute_level_populations_sparse": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_long,
                                                        C.POINTER(MgrAliParams), C.POINTER(C.c_int), _f64p, _f64p,
@@ -396,6 +397,12 @@ class DeviceModel:
         lam = np.empty((self.P, self.L))
         _check(load().mgr_formal_solve_fo2_sparse(self.h, PRECISION[precision], _ptr(Jl, _f64p), _ptr(lam, _f64p)))
         return dict(Jlin=Jl, lambda_diag=lam)
+
+    def formal_solve_fo2_uv(self, precision="fp64"):
+        u = np.empty((self.R, self.P, self.F))
+        v = np.empty((self.R, self.P, self.F))
+        _check(load().mgr_formal_solve_fo2_uv(self.h, PRECISION[precision], _ptr(u, _f64p), _ptr(v, _f64p)))
+        return dict(u=u, v=v)
 
     def formal_solve_fo2_anis(self, precision="fp64"):
         """Anisotropic solve: line-integrated J and the J2 tensor elements [P][L]."""

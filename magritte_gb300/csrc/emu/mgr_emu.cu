@@ -207,12 +207,12 @@ LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {
 
 constexpr uint32_t kCap = 1u << 16;
 
-template <int MODE>
+template <int MODE, bool UV = false>
 LaneResult solve_any(const DevModel& m, const LaneCtx& c, const HalfSmem& bk, int nb, const HalfSmem& fw, int nf) {
     switch (m.approx) {
-        case APPROX_ONELINE: return solve_lane<MODE, APPROX_ONELINE>(m, m.sorted_line, c, bk, nb, fw, nf);
-        case APPROX_CLOSELINES: return solve_lane<MODE, APPROX_CLOSELINES>(m, m.sorted_line, c, bk, nb, fw, nf);
-        default: return solve_lane<MODE, APPROX_NONE>(m, m.sorted_line, c, bk, nb, fw, nf);
+        case APPROX_ONELINE: return solve_lane<MODE, APPROX_ONELINE, UV>(m, m.sorted_line, c, bk, nb, fw, nf);
+        case APPROX_CLOSELINES: return solve_lane<MODE, APPROX_CLOSELINES, UV>(m, m.sorted_line, c, bk, nb, fw, nf);
+        default: return solve_lane<MODE, APPROX_NONE, UV>(m, m.sorted_line, c, bk, nb, fw, nf);
     }
 }
 
@@ -307,6 +307,47 @@ extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, do
 extern "C" int mgr_emu_formal_solve_fo2_rays(const MgrModelDesc* d, int precision, uint32_t rr_begin,
                                              uint32_t rr_end, double* J, double* lam) {
     return emu_fo2(d, precision, rr_begin, rr_end, J, lam);
+}
+
+// The uv solve (solve_lane<..., UV = true>): u and v [hnrays][P][F], and (may be NULL)
+// the optical depths of the pairs on either side of the origin used by v.
+extern "C" int mgr_emu_formal_solve_fo2_uv(const MgrModelDesc* d, int precision, double* u, double* v, double* dtm,
+                                           double* dtp) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    const uint32_t P = m.P, F = m.F, R = m.hnrays;
+    int err = 0;
+#pragma omp parallel
+    {
+        HalfBuf b(kCap), fbuf(kCap);
+        HalfSmem bk = b.view(), fw = fbuf.view();
+#pragma omp for schedule(dynamic, 16)
+        for (long long oo = 0; oo < (long long)P; oo++) {
+            const uint32_t o = (uint32_t)oo;
+            for (uint32_t rr = 0; rr < R; rr++) {
+                const int nb = trace_half_host(m, o, rr, kCap, bk);
+                const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
+                if (nb < 0 || nf < 0) {
+#pragma omp atomic write
+                    err = 1;
+                    break;
+                }
+                for (uint32_t f = 0; f < F; f++) {
+                    const LaneCtx c = lane_ctx(m, o, f);
+                    const LaneResult r = precision == MGR_PRECISION_SPLIT
+                                             ? solve_any<MODE_SPLIT, true>(m, c, bk, nb, fw, nf)
+                                             : solve_any<MODE_FP64, true>(m, c, bk, nb, fw, nf);
+                    const size_t i = ((size_t)rr * P + o) * F + f;
+                    u[i] = r.u;
+                    v[i] = r.v;
+                    if (dtm) dtm[i] = r.dtm;
+                    if (dtp) dtp[i] = r.dtp;
+                }
+            }
+        }
+    }
+    return err ? MGR_ERR_TRACE : MGR_OK;
 }
 
 // Short characteristics: the kernel's per-lane code and the reduction order of

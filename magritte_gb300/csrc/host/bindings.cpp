@@ -299,6 +299,8 @@ PYBIND11_MODULE(core, m) {
         .def("compute_Jeff_sparse", &Model::compute_Jeff_sparse, py::call_guard<py::gil_scoped_release>())
         .def("compute_radiation_field_feautrier_order_2_anis", &Model::compute_radiation_field_feautrier_order_2_anis,
              py::call_guard<py::gil_scoped_release>())
+        .def("compute_radiation_field_feautrier_order_2_uv", &Model::compute_radiation_field_feautrier_order_2_uv,
+             py::call_guard<py::gil_scoped_release>())
         .def("compute_level_populations_sparse", &Model::compute_level_populations_sparse,
              py::arg("use_Ng_acceleration"), py::arg("max_niterations"), py::call_guard<py::gil_scoped_release>())
         .def_readonly("error_mean", &Model::error_mean)

@@ -686,6 +686,16 @@ int Model::compute_radiation_field_feautrier_order_2_anis() {
     return 0;
 }
 
+// Model::compute_radiation_field_feautrier_order_2_uv (model.cpp:395-433): radiation.u and .v
+int Model::compute_radiation_field_feautrier_order_2_uv() {
+    MgrModel* dev = upload();
+    const Size P = parameters.npoints_.v, F = parameters.nfreqs_, R = parameters.hnrays_.v;
+    radiation.u.resize({R, P, F});
+    radiation.v.resize({R, P, F});
+    check(mgr_formal_solve_fo2_uv(dev, parameters.precision, radiation.u.data(), radiation.v.data()));
+    return 0;
+}
+
 // Model::compute_Jeff_sparse (model.cpp:549-570)
 int Model::compute_Jeff_sparse() {
     if (!dev_ || lines.lineProducingSpecies.empty() || lines.lineProducingSpecies[0].J.size() == 0)

@@ -281,6 +281,7 @@ class Model {
     int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
     int compute_radiation_field_feautrier_order_2_sparse();
     int compute_radiation_field_feautrier_order_2_anis();
+    int compute_radiation_field_feautrier_order_2_uv();
     int compute_Jeff_sparse();
     int compute_level_populations_sparse(bool use_Ng_acceleration, long max_niterations);
 

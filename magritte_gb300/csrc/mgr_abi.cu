@@ -148,6 +148,7 @@ void mgr_model_free(MgrModel* model) {
     if (model->lam_scratch) cudaFree(model->lam_scratch);
     if (model->work) cudaFree(model->work);
     if (model->adj_scratch) cudaFree(model->adj_scratch);
+    if (model->v_scratch) cudaFree(model->v_scratch);
     ali_free(model);
     if (model->stream) cudaStreamDestroy(model->stream);
     delete model;
@@ -641,6 +642,33 @@ int mgr_formal_solve_fo2_anis(MgrModel* model, int precision, double* J, double*
     for (int k = 0; k < 6 && e == cudaSuccess; k++)
         if (outs[k]) e = cudaMemcpyAsync(outs[k], model->u_scratch + k * PL, PL * 8, cudaMemcpyDeviceToHost, model->stream);
     if (e != cudaSuccess) return cuda_fail(e, "anisotropic formal solve");
+    return read_status(model);
+}
+
+int mgr_formal_solve_fo2_uv(MgrModel* model, int precision, double* u, double* v) {
+    if (!model || !u || !v) {
+        set_error("mgr_formal_solve_fo2_uv: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
+        set_error("mgr_formal_solve_fo2_uv: unknown precision mode");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!model->line_disc) {
+        set_error("mgr_formal_solve_fo2_uv: the formal solve needs a line spectral discretisation");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    const DevModel& dm = model->dm;
+    const size_t RPF = (size_t)dm.hnrays * dm.P * dm.F;
+    int rc = ensure_scratch(model, &model->u_scratch, &model->u_scratch_bytes, RPF * 8);
+    if (rc != MGR_OK) return rc;
+    if ((rc = ensure_scratch(model, &model->v_scratch, &model->v_scratch_bytes, RPF * 8)) != MGR_OK) return rc;
+    // the solve writes u and v directly; J and the ALO are not part of this call
+    cudaError_t e = launch_fo2_range(model, precision, 0, dm.P, nullptr, model->u_scratch, nullptr, nullptr, 0, 0,
+                                     dm.hnrays, nullptr, nullptr, model->v_scratch);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(u, model->u_scratch, RPF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v, model->v_scratch, RPF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "uv formal solve");
     return read_status(model);
 }
 

@@ -137,11 +137,12 @@ __global__ void ray_lengths_kernel(DevModel m, uint32_t cap, uint32_t* d_max, in
 // ---------------------------------------------------------------------------------
 // MINB = CTAs of 256 threads resident per SM the register budget is sized for
 // (2: 128, 3: 80, 4: 64 registers per thread); picked at run time by the tuner.
-template <int MODE, int AP, int MINB>
+// UV: also v (solve_feautrier_order_2_uv), written to V with U's layout.
+template <int MODE, int AP, int MINB, bool UV = false>
 __global__ void __launch_bounds__(256, MINB)
     fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                double* __restrict__ U, size_t u_stride, uint32_t u_o0, double* __restrict__ LD, size_t ld_stride,
-               uint32_t ld_o0, int* status) {
+               uint32_t ld_o0, double* __restrict__ V, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
@@ -173,8 +174,9 @@ __global__ void __launch_bounds__(256, MINB)
                 c.freq = m.nu[(size_t)o * m.F + f];
                 c.fq = (float)c.freq;
                 c.a0 = (float)(c.freq - m.line[c.l0]);
-                const LaneResult r = solve_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
+                const LaneResult r = solve_lane<MODE, AP, UV>(m, sl, c, bk, nb, fw, nf);
                 Ui[f] = r.u;
+                if constexpr (UV) V[(size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F + f] = r.v;
                 if (Li) Li[f] = r.solved ? r.Ldiag : 0.0;
                 if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
             }
@@ -477,17 +479,17 @@ size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, b
     return chunk * per;
 }
 
-template <int MODE, int AP, int MINB>
+template <int MODE, int AP, int MINB, bool UV = false>
 static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                                       double* U, size_t u_stride, uint32_t u_o0, double* LD, size_t ld_stride,
-                                      uint32_t ld_o0) {
+                                      uint32_t ld_o0, double* V = nullptr) {
     const DevModel& m = model->dm;
     const uint32_t cap = model->half_cap;
     int nw = model->fo2_warps > 0 ? model->fo2_warps : 8;
     if (nw > 8) nw = 8;
     const uint32_t Lpad = (m.L + 1) & ~1u;
     const size_t smem = (size_t)Lpad * 8 + (size_t)nw * half_bytes_per_warp(cap);
-    auto kern = fo2_kernel<MODE, AP, MINB>;
+    auto kern = fo2_kernel<MODE, AP, MINB, UV>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -501,7 +503,7 @@ static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_
     if (grid < 1) grid = 1;
     count_launch();
     kern<<<(unsigned)grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, rr0, nR, U, u_stride, u_o0, LD,
-                                                          ld_stride, ld_o0, model->status);
+                                                          ld_stride, ld_o0, V, model->status);
     return cudaGetLastError();
 }
 
@@ -512,6 +514,23 @@ static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o
     if (minb == 2) return launch_fo2_variant<MODE, AP, 2>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
     if (minb == 4) return launch_fo2_variant<MODE, AP, 4>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
     return launch_fo2_variant<MODE, AP, 3>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
+}
+
+// The uv solve: one register budget (MINB 3), no tuning.
+template <int MODE>
+static cudaError_t launch_fo2_uv(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
+                                 double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo, double* V) {
+    switch (model->dm.approx) {
+        case APPROX_ONELINE:
+            return launch_fo2_variant<MODE, APPROX_ONELINE, 3, true>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls,
+                                                                     lo, V);
+        case APPROX_CLOSELINES:
+            return launch_fo2_variant<MODE, APPROX_CLOSELINES, 3, true>(model, o_begin, o_end, rr0, nR, U, us, uo, LD,
+                                                                        ls, lo, V);
+        default:
+            return launch_fo2_variant<MODE, APPROX_NONE, 3, true>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls,
+                                                                  lo, V);
+    }
 }
 
 template <int MODE>
@@ -528,7 +547,7 @@ static cudaError_t launch_fo2_approx(MgrModel* model, uint32_t o_begin, uint32_t
 
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
                              double* lam, double* work, size_t work_bytes, uint32_t rr_begin, uint32_t rr_end,
-                             double* Jlin, double* anis) {
+                             double* Jlin, double* anis, double* v) {
     const DevModel& m = model->dm;
     if (o_end <= o_begin) return cudaSuccess;
     if (rr_end > m.hnrays) rr_end = m.hnrays;
@@ -563,10 +582,17 @@ cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, u
         }
         double* LD = lam ? next : nullptr;
         const size_t ls = (size_t)n * m.F;
-        cudaError_t e = (precision == MGR_PRECISION_SPLIT)
-                            ? launch_fo2_approx<MODE_SPLIT>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0)
-                            : launch_fo2_approx<MODE_FP64>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0);
+        cudaError_t e;
+        if (v)  // v has u's layout: u is given (no chunked staging of U)
+            e = (precision == MGR_PRECISION_SPLIT)
+                    ? launch_fo2_uv<MODE_SPLIT>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, v)
+                    : launch_fo2_uv<MODE_FP64>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, v);
+        else
+            e = (precision == MGR_PRECISION_SPLIT)
+                    ? launch_fo2_approx<MODE_SPLIT>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0)
+                    : launch_fo2_approx<MODE_FP64>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0);
         if (e != cudaSuccess) return e;
+        if (!J && !lam && !Jlin && !anis) continue;  // u (and v) only
         unsigned grid = n < (uint32_t)nsm * 16 ? n : (unsigned)nsm * 16;
         count_launch();
         fo2_reduce_kernel<<<grid, 128, 0, model->stream>>>(m, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, J, lam,

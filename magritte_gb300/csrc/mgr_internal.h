@@ -46,6 +46,8 @@ struct MgrModel {
     size_t u_scratch_bytes = 0;
     double* lam_scratch = nullptr;
     size_t lam_scratch_bytes = 0;
+    double* v_scratch = nullptr;  // v of the uv solve
+    size_t v_scratch_bytes = 0;
     // staging of u(rr, o, f) / L_diag(rr, o, f) between the two formal-solve stages
     double* work = nullptr;
     size_t work_bytes = 0;
@@ -90,10 +92,12 @@ size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, b
 // Ray pairs [rr_begin, rr_end) only (partial J / ALO sums, u must then be NULL).
 // J may be NULL; Jlin [P][L] (may be NULL) receives the line-integrated J in the order
 // of the memory-lean solve; anis [6][P][L] (may be NULL) the line-integrated J and
-// anisotropy tensor elements of the anisotropic solve.
+// anisotropy tensor elements of the anisotropic solve; v [hnrays][P][F] (may be NULL,
+// needs u) the uv solve's v.
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
                              double* lam, double* work, size_t work_bytes, uint32_t rr_begin = 0,
-                             uint32_t rr_end = 0xffffffffu, double* Jlin = nullptr, double* anis = nullptr);
+                             uint32_t rr_end = 0xffffffffu, double* Jlin = nullptr, double* anis = nullptr,
+                             double* v = nullptr);
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
                                 uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
                                 double* d_dZ);

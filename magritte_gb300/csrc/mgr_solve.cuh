@@ -833,6 +833,8 @@ struct LaneResult {
     double u;       // Su[centre]
     double Ldiag;   // L_diag[centre]
     bool solved;    // n_tot > 1
+    double v;       // Sv[centre] of the uv solve (solve_lane<..., UV = true> only)
+    double dtm, dtp;  // the uv solve's optical depths of the pairs before / after the origin
 };
 
 // State of one elimination sweep toward the origin.
@@ -841,6 +843,9 @@ struct Sweep {
     double dt;         // optical depth of the last pair (next to the origin)
     double S_in;       // source of the origin from the last pair (its inner element)
     bool rows;         // at least one row eliminated
+    // uv solve only: the last pair's branch, its outer element's opacity, its distance
+    bool last_large;
+    double chi_out, dz_last;
 };
 
 // Two-sided Feautrier solve of frequency c.f on the ray pair staged in `bk`
@@ -851,12 +856,14 @@ struct Sweep {
 //   forward half:  elements last .. centre+1, row `last` with the source of its own
 //                  pair, rows i < last with S[i] from pair (i, i+1) = the previous
 //                  pair's inner element.
-template <int MODE, int AP>
+template <int MODE, int AP, bool UV = false>
 __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
                                           int nb, const HalfSmem& fw, int nf) {
     using T = typename Real_<MODE>::T;
     LaneResult res;
     res.solved = (nb > 0) || (nf > 0);
+    res.v = 0.0;
+    res.dtm = res.dtp = 0.0;
     if (!res.solved) {
         res.u = boundary_intensity_m<MODE>(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
         res.Ldiag = 0.0;
@@ -865,13 +872,13 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     const Elem cen = centre_elem(c.o);
     const uint32_t l = c.l0;
     EC<MODE> ec_cen{T(0), T(0), false};
-    Sweep top{0.0, 0.0, 0.0, 0.0, 0.0, false}, bot = top;
+    Sweep top{0.0, 0.0, 0.0, 0.0, 0.0, false, false, 0.0, 0.0}, bot = top;
 
 #pragma unroll 1
     for (int side = 0; side < 2; side++) {
         const HalfSmem& h = side ? fw : bk;
         const int n = side ? nf : nb;
-        Sweep st{0.0, 0.0, 0.0, 0.0, 0.0, false};
+        Sweep st{0.0, 0.0, 0.0, 0.0, 0.0, false, false, 0.0, 0.0};
         if (n > 0) {
             ElemIter it;
             iter_begin<MODE>(m, h, c.o, l, n, it);
@@ -894,6 +901,11 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 EC<MODE>& eci = more ? ec_inn : ec_cen;
                 PairOut<MODE> po;
                 eval_pair<MODE, AP>(m, sl, c, h, outer, inner, outer.dzin, outer.dzf, ec_out, eci, po);
+                if constexpr (UV) {
+                    st.last_large = po.large;
+                    st.chi_out = (double)ec_out.chi;
+                    st.dz_last = (MODE == MODE_FP64) ? outer.dzin : (double)outer.dzf;
+                }
                 const T rowS = (side == 0 || first) ? po.Slo : S_carry;
                 if (first) {
                     // boundary row (solver.tpp:2239-2252 first, :2284-2293 last)
@@ -936,6 +948,27 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         const double D = drcp<MODE>(FFc + GP);
         res.u = (Su_pre + bot.Su) * D;
         res.Ldiag = iC * D;
+        if constexpr (UV) {
+            // solve_feautrier_order_2_uv (solver.tpp:2896-2916): u at the neighbours of the
+            // origin from each side's last row, v the finite-difference derivative
+            const double u_min = top.Su + res.u * top.FI;
+            const double u_plus = bot.Su + res.u * bot.FI;
+            const double dtaumin = (double)top.dt;
+            double dtauplus = (double)bot.dt;
+            if (!top.last_large && !bot.last_large) {
+                // The reference evaluates the pair (origin, next) with compute_curr_opacity
+                // left false by the pair (previous, origin), so its "current" opacity is
+                // that of the previous element (solver.tpp:2899-2907, :2161-2170).
+                if constexpr (MODE == MODE_FP64) dtauplus = 0.5 * (top.chi_out + bot.chi_out) * bot.dz_last;
+                else dtauplus = (double)(0.5f * ((float)top.chi_out + (float)bot.chi_out) * (float)bot.dz_last);
+            }
+            res.dtm = dtaumin;
+            res.dtp = dtauplus;
+            const double coeffmin = -dtauplus / (dtaumin * dtaumin + dtaumin * dtauplus);
+            const double coeffplus = dtaumin / (dtaumin * dtauplus + dtauplus * dtauplus);
+            const double coeffzero = -coeffmin - coeffplus;
+            res.v = -(coeffmin * u_min + coeffplus * u_plus + coeffzero * res.u);
+        }
     } else if (bot.rows) {  // origin is the first element
         const double Ibdy = boundary_intensity_m<MODE>(m, c.o, c.freq);
         const double inverse_dtau_f = drcp<MODE>(bot.dt);
@@ -950,6 +983,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         const double D = drcp<MODE>(FFf + GP);
         res.u = (Suf * (1.0 + FFf) + bot.Su) * D;
         res.Ldiag = drcp<MODE>(Cf) * D;
+        if constexpr (UV) res.v = Ibdy - res.u;  // Sv[first] = I_bdy_f - Su[first]
     } else {  // origin is the last element
         const double Ibdy = boundary_intensity_m<MODE>(m, c.o, c.freq);
         const double inverse_dtau_l = drcp<MODE>(top.dt);
@@ -959,6 +993,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         const double denominator = drcp<MODE>(Bl * top.F + Bl_min_Al);
         const double Sl = top.S_in + 2.0 * Ibdy * inverse_dtau_l;
         res.u = (Al * top.Su + Sl) * (1.0 + top.F) * denominator;
+        if constexpr (UV) res.v = res.u - Ibdy;  // Sv[last] = Su[last] - I_bdy_l
         if constexpr (MODE == MODE_FP64) res.Ldiag = (1.0 + top.F) / (Bl_min_Al + Bl * top.F);
         else res.Ldiag = (1.0 + top.F) * denominator;
     }

@@ -678,8 +678,63 @@ int orc_trace_ray_pair_for_line(const OrcModel* m, uint32_t o, uint32_t rr, uint
 /* ------------------------------------------------------------------ */
 /* Formal solve driver (solver.tpp:458-540)                             */
 /* ------------------------------------------------------------------ */
+static int fo2_range_v(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0, uint32_t o1,
+                       double* J, double* u, double* v, double* lambda_diag, uint8_t* lambda_has, int nthreads);
+
+/* The v part of Solver::solve_feautrier_order_2_uv(model, o, f) (solver.tpp:2767-2921)
+ * after solve_feautrier_order_2 with full back substitution (Su[centre .. last] hold u):
+ * a boundary difference when the origin ends the ray, else the finite-difference
+ * derivative of u at the origin from u[centre - 1], u[centre] and u[centre + 1]. */
+static double feautrier_v(const OrcModel* m, Buf* b, uint32_t o, uint32_t f) {
+    const double freq = m->nu[(size_t)o * m->nfreqs + f];
+    const uint32_t l  = m->corr_line[f];
+    const uint32_t first = b->first, last = b->last, centre = b->centre;
+    double* Su = b->Su;
+    if (centre == last) {
+        const double I_bdy_l = boundary_intensity(m, b->nr[last], freq * b->shift[last]);
+        return Su[last] - I_bdy_l;
+    }
+    if (centre > first) {
+        Su[centre - 1] += Su[centre] * b->FI[centre - 1];
+        double chi_c = 0.0, chi_n = 0.0, dtau_n = 0.0, term_c = 0.0, term_n = 0.0;
+        int cco = 1;
+        compute_source_dtau(m, b->nr[centre - 1], b->nr[centre], b->nr_interp[centre - 1], b->nr_interp[centre], l,
+                            freq * b->shift[centre - 1], freq * b->shift[centre], b->shift[centre - 1],
+                            b->shift[centre], b->dZ[centre - 1], b->interp_factor[centre - 1],
+                            b->interp_factor[centre], &cco, &dtau_n, &chi_c, &chi_n, &term_c, &term_n);
+        const double dtaumin = dtau_n;
+        compute_source_dtau(m, b->nr[centre], b->nr[centre + 1], b->nr_interp[centre], b->nr_interp[centre + 1], l,
+                            freq * b->shift[centre], freq * b->shift[centre + 1], b->shift[centre],
+                            b->shift[centre + 1], b->dZ[centre], b->interp_factor[centre],
+                            b->interp_factor[centre + 1], &cco, &dtau_n, &chi_c, &chi_n, &term_c, &term_n);
+        const double dtauplus  = dtau_n;
+        const double coeffmin  = -dtauplus / (dtaumin * dtaumin + dtaumin * dtauplus);
+        const double coeffplus = dtaumin / (dtaumin * dtauplus + dtauplus * dtauplus);
+        const double coeffzero = -coeffmin - coeffplus;
+        return -(coeffmin * Su[centre - 1] + coeffplus * Su[centre + 1] + coeffzero * Su[centre]);
+    }
+    const double I_bdy_f = boundary_intensity(m, b->nr[first], freq * b->shift[first]);
+    return I_bdy_f - Su[first];
+}
+
 static int fo2_range(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0, uint32_t o1,
                      double* J, double* u, double* lambda_diag, uint8_t* lambda_has, int nthreads) {
+    return fo2_range_v(m, rr0, rr1, o0, o1, J, u, NULL, lambda_diag, lambda_has, nthreads);
+}
+
+/* Model::compute_radiation_field_feautrier_order_2_uv (model.cpp:395-433 ->
+ * Solver::solve_feautrier_order_2_uv, solver.tpp:238-295): u and v per ray pair. */
+int orc_formal_solve_fo2_uv(const OrcModel* m, double* u, double* v, int nthreads) {
+    const size_t PF = (size_t)m->npoints * m->nfreqs;
+    double* J = (double*)calloc(PF ? PF : 1, sizeof(double));
+    if (!J) return -3;
+    const int rc = fo2_range_v(m, 0, m->hnrays, 0, m->npoints, J, u, v, NULL, NULL, nthreads);
+    free(J);
+    return rc;
+}
+
+static int fo2_range_v(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0, uint32_t o1,
+                       double* J, double* u, double* v, double* lambda_diag, uint8_t* lambda_has, int nthreads) {
     const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
     const uint32_t P = m->npoints, F = m->nfreqs, Q = m->nquads;
     int err_any = 0;
@@ -720,11 +775,13 @@ static int fo2_range(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0,
                                 solve_feautrier_order_2(m, &b, o, f, 1);
                                 val = b.Su[c];
                                 if (u) u[((size_t)rr * P + o) * F + f] = val;
+                                if (v) v[((size_t)rr * P + o) * F + f] = feautrier_v(m, &b, o, f);
                                 J[(size_t)o * F + f] += b.Su[c] * 2.0 * m->ray_weight[rr];
                                 update_lambda(m, &b, rr, f, lambda_diag, lambda_has);
                             } else {
                                 val = boundary_intensity(m, o, m->nu[(size_t)o * F + f]);
                                 if (u) u[((size_t)rr * P + o) * F + f] = val;
+                                if (v) v[((size_t)rr * P + o) * F + f] = 0.0;
                                 J[(size_t)o * F + f] += 2.0 * m->ray_weight[rr] * val;
                             }
                         }

@@ -115,6 +115,11 @@ int orc_trace_ray_pair_for_line(const OrcModel* m, uint32_t o, uint32_t rr, uint
 int orc_formal_solve_fo2(const OrcModel* m, double* J, double* u, double* lambda_diag,
                          uint8_t* lambda_has, int nthreads);
 
+/* Model::compute_radiation_field_feautrier_order_2_uv (model.cpp:395-433 ->
+ * Solver::solve_feautrier_order_2_uv, solver.tpp:238-295, :2767-2921): u and v
+ * [hnrays][P][F] per ray pair (v = 0 where the ray pair has one point). */
+int orc_formal_solve_fo2_uv(const OrcModel* m, double* u, double* v, int nthreads);
+
 /* Same driver restricted to the ray pairs [rr_begin, rr_end) and origins [o_begin, o_end);
  * used to time a bounded sample.  Accumulates into J (not cleared). */
 int orc_formal_solve_fo2_range(const OrcModel* m, uint32_t rr_begin, uint32_t rr_end,

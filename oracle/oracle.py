@@ -298,6 +298,18 @@ class Oracle:
             raise RuntimeError(f"oracle formal solve failed ({rc})")
         return dict(J=J, u=u, lambda_diag=lam, lambda_has=has)
 
+    def formal_solve_fo2_uv(self, nthreads=0):
+        P, F, R = self.a["npoints"], self.a["nfreqs"], self.a["hnrays"]
+        u = np.zeros((R, P, F))
+        v = np.zeros((R, P, F))
+        l = lib()
+        l.orc_formal_solve_fo2_uv.restype = C.c_int
+        l.orc_formal_solve_fo2_uv.argtypes = [C.POINTER(OrcModel), _f64p, _f64p, C.c_int]
+        rc = l.orc_formal_solve_fo2_uv(C.byref(self.m), _ptr(u, _f64p), _ptr(v, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle uv solve failed ({rc})")
+        return dict(u=u, v=v)
+
     def formal_solve_fo2_anis(self):
         """Solver::solve_feautrier_order_2_anis (solver.tpp:366-456) from this oracle's u:
         per line, du = (w_z w_rr) u, J += 2 du and the J2 tensor elements += wt_x(n) du,

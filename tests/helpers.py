@@ -43,6 +43,25 @@ def all_constant_solution(raw):
     return 0.5 * (I0 + I1)
 
 
+def all_constant_intensities(raw):
+    """all_constant_single_ray.py:121-136: the two directions' intensities I_0, I_1."""
+    u = all_constant_solution(raw)
+    ld = raw.linedata[0]
+    temp, nTT = raw.temperature[0], raw.abundance[0, 0]
+    frq = ld.frequency[0]
+    pop = ld.weight * np.exp(-ld.energy / (KB * temp))
+    pop = pop / pop.sum() * nTT
+    width = frq * np.sqrt(2.0 * KB * temp / (AMU * CC**2) * ld.inverse_mass + raw.vturb2[0])
+    phi = 1.0 / (width * np.sqrt(np.pi))
+    em = HH * frq / (4.0 * np.pi) * ld.A[0] * pop[1]
+    op = HH * frq / (4.0 * np.pi) * (ld.Ba[0] * pop[0] - ld.Bs[0] * pop[1])
+    chi = op * phi
+    src = em / op
+    bdy = planck(S.T_CMB, frq)
+    x = raw.position[:, 0]
+    return src + (bdy - src) * np.exp(-chi * x), src + (bdy - src) * np.exp(-chi * (x[-1] - x))
+
+
 def all_zero_model():
     """tests/benchmarks/analytic/all_zero_single_ray.py:20-78 (velocity 0 up to the
     middle point, then rising by 150 m/s per point)."""

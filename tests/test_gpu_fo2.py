@@ -165,3 +165,52 @@ def test_core_model_anisotropic_solve(gpu_lib):
     model.compute_Jeff()
     # J of the anisotropic solve is the line-integrated mean intensity
     assert np.max(np.abs(J - np.array(ls.Jlin)) / np.array(ls.Jlin)) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_uv_solve_matches_emulated_lane_code(gpu_lib, precision):
+    """compute_radiation_field_feautrier_order_2_uv on the GPU against the same lane
+    code on the CPU (which test_kernel_emulation.py checks against the oracle): u to
+    1e-12 (FP64), v to 1e-9 of u plus the rounding of u amplified by v's
+    finite-difference coefficients (~1/dtau)."""
+    import ctypes as C
+    from magritte_gb300 import build
+
+    raw = S.grid_sphere(n=14, nside=1, nquads=5)
+    a = H.setup(raw)
+    dev = _abi.DeviceModel(a)
+    try:
+        got = dev.formal_solve_fo2_uv(precision)
+    finally:
+        dev.close()
+    emu = C.CDLL(build.build_emu())
+    p = C.POINTER(C.c_double)
+    emu.mgr_emu_formal_solve_fo2_uv.argtypes = [C.POINTER(_abi.MgrModelDesc), C.c_int, p, p, p, p]
+    desc, keep = _abi.make_desc(a)
+    u, v, dtm, dtp = (np.zeros_like(got["u"]) for _ in range(4))
+    assert emu.mgr_emu_formal_solve_fo2_uv(C.byref(desc), _abi.PRECISION[precision],
+                                           *[x.ctypes.data_as(p) for x in (u, v, dtm, dtp)]) == 0
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert H.max_rel(got["u"], u) < tol
+    both = (dtm > 0) & (dtp > 0)
+    cm = np.where(both, dtp / np.where(both, dtm * dtm + dtm * dtp, 1.0), 0.0)
+    cp = np.where(both, dtm / np.where(both, dtm * dtp + dtp * dtp, 1.0), 0.0)
+    noise = 64 * np.finfo(float).eps * np.abs(u) * (cm + cp + np.abs(cm - cp))
+    assert np.all(np.abs(got["v"] - v) <= max(tol, 1e-9) * np.abs(u) + noise)
+
+
+def test_core_model_uv_known_answer(gpu_lib):
+    """all_constant_single_ray.py:135-136, :182: I_0 = u + v and I_1 = u - v within 2e-4."""
+    from magritte_gb300 import loader
+
+    raw = H.all_constant_model()
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    model.compute_radiation_field_feautrier_order_2_uv()
+    u = np.array(model.radiation.u)[0, :, 0]
+    v = np.array(model.radiation.v)[0, :, 0]
+    I0, I1 = H.all_constant_intensities(raw)
+    assert np.max(np.abs(H.relative_error(I0, u + v))) < 2.0e-4
+    assert np.max(np.abs(H.relative_error(I1, u - v))) < 2.0e-4

@@ -125,3 +125,31 @@ def test_emulated_old_imager_matches_oracle(emu, name, approx, rr):
         assert emu.mgr_emu_image(C.byref(desc), _abi.PRECISION[precision], rr,
                                  I.ctypes.data_as(C.POINTER(C.c_double))) == 0
         assert H.max_rel(I, ref) < tol, precision
+
+
+@pytest.mark.parametrize("name", ["cube10", "sphere14", "all_constant", "all_zero"])
+@pytest.mark.parametrize("approx", ["CloseLines", "None"])
+def test_emulated_uv_matches_oracle(emu, name, approx):
+    """solve_lane<..., UV> (the uv kernel's lane code) against the oracle's
+    solve_feautrier_order_2_uv.  u to 1e-12.  v is the finite-difference derivative
+    -(c_- u[c-1] + c_+ u[c+1] + c_0 u[c]) with |c| ~ 1/dtau; the neighbour values come
+    from the two sweeps here and from the back substitution in the reference, so the
+    two agree to 1e-9 of u plus the rounding of u amplified by the coefficients
+    (which dominates on optically thin pairs, where the reference's own v is noise)."""
+    raw = MODELS[name]()
+    a = H.setup(raw, approx=approx)
+    ref = O.Oracle(a).formal_solve_fo2_uv()
+    desc, keep = _abi.make_desc(a)
+    p = C.POINTER(C.c_double)
+    emu.mgr_emu_formal_solve_fo2_uv.argtypes = [C.POINTER(_abi.MgrModelDesc), C.c_int, p, p, p, p]
+    for precision, tol_u, tol_v in (("fp64", 1e-12, 1e-9), ("split", 1e-5, 1e-5)):
+        u, v, dtm, dtp = (np.zeros_like(ref["u"]) for _ in range(4))
+        assert emu.mgr_emu_formal_solve_fo2_uv(C.byref(desc), _abi.PRECISION[precision],
+                                               *[x.ctypes.data_as(p) for x in (u, v, dtm, dtp)]) == 0
+        assert H.max_rel(u, ref["u"]) < tol_u, precision
+        both = (dtm > 0) & (dtp > 0)
+        cm = np.where(both, dtp / np.where(both, dtm * dtm + dtm * dtp, 1.0), 0.0)
+        cp = np.where(both, dtm / np.where(both, dtm * dtp + dtp * dtp, 1.0), 0.0)
+        noise = 64 * np.finfo(float).eps * np.abs(ref["u"]) * (cm + cp + np.abs(cm - cp))
+        bound = (tol_v if precision == "split" else 1e-9) * np.abs(ref["u"]) + noise
+        assert np.all(np.abs(v - ref["v"]) <= bound), precision

@@ -31,6 +31,17 @@ def test_all_constant_single_ray_shortchar(built):
     assert np.max(err) < 1.7e-7
 
 
+def test_all_constant_single_ray_feautrier_uv(built):
+    """all_constant_single_ray.py:135-136, :182: I_0 = u + v and I_1 = u - v of the uv
+    solver within the reference's 2e-4."""
+    raw = H.all_constant_model()
+    r = O.Oracle(H.setup(raw)).formal_solve_fo2_uv()
+    I0, I1 = H.all_constant_intensities(raw)
+    u, v = r["u"][0, :, 0], r["v"][0, :, 0]
+    assert np.max(np.abs(H.relative_error(I0, u + v))) < 2.0e-4
+    assert np.max(np.abs(H.relative_error(I1, u - v))) < 2.0e-4
+
+
 def test_all_zero_single_ray_feautrier(built):
     raw = H.all_zero_model()
     r = O.Oracle(H.setup(raw)).formal_solve_fo2(want_u=True)
