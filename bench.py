@@ -410,7 +410,7 @@ def run_adjoint(args):
                          "median_rel_err": float(np.median(errs)) if errs else None, "bar": 1e-4,
                          "method": "Richardson-extrapolated central differences along a random direction of "
                                    "each point's (v_x, v_y, v_z, T, vturb2, abundance)", "s": fd_s},
-            "setup_s": setup_s, "loss": float(loss)}
+            "setup_s": setup_s, "loss": float(loss.detach())}
 
 
 def C_void(x):

@@ -246,6 +246,29 @@ int mgr_image_optical_depth(MgrModel* model, int precision, uint32_t ray_nr, dou
 int mgr_image_optical_depth_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny,
                                 double* I, double* ImX, double* ImY);
 
+/* Model::compute_image_for_point(ray_nr, p) (src/model/model.cpp:1039-1058 ->
+ * Solver::image_feautrier_order_2_for_point, src/solver/solver.tpp:629-653, :2582-2715):
+ * the old imager's ray through point p along ray_nr (rest-frame shifts, all-line
+ * interpolation points), eliminated and back-substituted along the whole ray.
+ *  - *n_tot: the ray's element count (Model::S_ray / dtau_ray / u_ray rows).  With
+ *    S_ray, dtau_ray, u_ray NULL and capacity 0 the call only returns it.
+ *  - S_ray, dtau_ray, u_ray [capacity][nfreqs] host arrays: rows 0 .. n_tot-1 are
+ *    written (row k = element first + k: the source at the far end of the pair ending
+ *    there (row 0: the first pair's near end), that pair's optical depth (row 0: 0),
+ *    and the Feautrier mean intensity u).  A ray of one element is written as zeros
+ *    (the reference solves nothing there).  MGR_ERR_CAPACITY when n_tot > capacity.
+ *  - OneLine is not supported for imaging (MGR_ERR_UNSUPPORTED), as in the reference. */
+int mgr_image_for_point(MgrModel* model, int precision, uint32_t ray_nr, uint32_t p, uint32_t* n_tot, double* S_ray,
+                        double* dtau_ray, double* u_ray, uint32_t capacity);
+
+/* Model::set_column() (src/model/model.cpp:1143-1153 -> Solver::set_column / get_column,
+ * src/solver/solver.tpp:2953-2991), general geometry with the model's own rays:
+ * column [nrays][npoints] (host) = for each ray pair rr < hnrays and its antipode, the
+ * trapezoid integral sum (density[crt] + density[nxt]) / 2 * dZ from each point to the
+ * boundary (0 where the point has no next point); rows of rays no pair names are 0.
+ * density [npoints] host (Model::density). */
+int mgr_set_column(MgrModel* model, const double* density, double* column);
+
 /* Same as mgr_formal_solve_fo2_device, but the call allocates no device memory.
  * No reference counterpart: an addition of this library for callers that cannot
  * allocate at solve time.

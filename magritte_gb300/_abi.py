@@ -103,6 +103,9 @@ SIGNATURES = {
     "mgr_image_optical_depth": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, _f64p, _f64p, _f64p]),
     "mgr_image_optical_depth_new": (C.c_int, [C.c_void_p, C.c_int, _f64p, C.c_uint32, C.c_uint32, _f64p, _f64p,
                                               _f64p]),
+    "mgr_image_for_point": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32), _f64p,
+                                      _f64p, _f64p, C.c_uint32]),
+    "mgr_set_column": (C.c_int, [C.c_void_p, _f64p, _f64p]),
     "mgr_formal_solve_fo2_device_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint64)]),
@@ -289,6 +292,24 @@ class DeviceModel:
         _check(load().mgr_image(self.h, PRECISION[precision], ray_nr, _ptr(I, _f64p), _ptr(X, _f64p),
                                 _ptr(Y, _f64p)))
         return dict(I=I, ImX=X, ImY=Y)
+
+    def image_for_point(self, ray_nr, p, precision="fp64"):
+        """S_ray, dtau_ray, u_ray [n_tot][F] of point p's ray ray_nr."""
+        lib = load()
+        n = C.c_uint32(0)
+        _check(lib.mgr_image_for_point(self.h, PRECISION[precision], ray_nr, p, C.byref(n), None, None, None, 0))
+        out = {k: np.empty((n.value, self.F)) for k in ("S_ray", "dtau_ray", "u_ray")}
+        _check(lib.mgr_image_for_point(self.h, PRECISION[precision], ray_nr, p, C.byref(n),
+                                       _ptr(out["S_ray"], _f64p), _ptr(out["dtau_ray"], _f64p),
+                                       _ptr(out["u_ray"], _f64p), n.value))
+        return out
+
+    def set_column(self, density):
+        """column [nrays][P] of density [P]."""
+        rho = np.ascontiguousarray(density, np.float64)
+        col = np.empty((int(self.a["nrays"]), self.P))
+        _check(load().mgr_set_column(self.h, _ptr(rho, _f64p), _ptr(col, _f64p)))
+        return col
 
     def image_optical_depth(self, ray_nr, precision="fp64"):
         I = np.empty((self.P, self.F))

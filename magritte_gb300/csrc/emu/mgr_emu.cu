@@ -1,3 +1,4 @@
+#include <algorithm>
 // CPU emulation of the formal-solve kernel for the test-suite.
 //
 // Runs the kernel's own per-lane code (solve_lane, lambda_element and everything
@@ -455,6 +456,52 @@ extern "C" int mgr_emu_image(const MgrModelDesc* d, int precision, uint32_t rr, 
         }
     }
     return err ? MGR_ERR_TRACE : MGR_OK;
+}
+
+// The image_for_point rows (image_lane with ROWS) of point p's ray rr: n_tot and, when
+// it fits capacity, S / dtau / u [n_tot][F] (zeros for a one-element ray).
+extern "C" int mgr_emu_image_for_point(const MgrModelDesc* d, int precision, uint32_t rr, uint32_t p,
+                                       uint32_t* n_tot, double* S, double* dtau, double* u, uint32_t capacity) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    const uint32_t F = m.F;
+    HalfBuf b(kCap), fbuf(kCap);
+    HalfSmem bk = b.view(), fw = fbuf.view();
+    const uint32_t ar = m.antipod[rr];
+    const double shb = shift_rest(m, rr, p, m.raydir + 3 * rr);
+    const double shf = shift_rest(m, ar, p, m.raydir + 3 * ar);
+    bk.shift0 = shb;
+    fw.shift0 = shf;
+    bk.dsh0 = (float)(shb - 1.0);
+    fw.dsh0 = (float)(shf - 1.0);
+    bk.cshift = fw.cshift = shb;
+    const int nb = trace_half_host(m, p, rr, kCap, bk, 1);
+    const int nf = trace_half_host(m, p, ar, kCap, fw, 1);
+    if (nb < 0 || nf < 0) return MGR_ERR_TRACE;
+    uint32_t n = 1;
+    for (int s = 0; s < nb; s++) n += m.nint_all[bk.eid[s]];
+    for (int s = 0; s < nf; s++) n += m.nint_all[fw.eid[s]];
+    *n_tot = n;
+    if (n > capacity) return MGR_ERR_CAPACITY;
+    const size_t NF = (size_t)n * F;
+    std::fill(S, S + NF, 0.0);
+    std::fill(dtau, dtau + NF, 0.0);
+    std::fill(u, u + NF, 0.0);
+    if (n <= 1) return MGR_OK;
+    std::vector<double> FI(NF);
+    const RowOut ro{S, dtau, u, FI.data(), F};
+    for (uint32_t f = 0; f < F; f++) {
+        const LaneCtx c = lane_ctx(m, p, f);
+        if (precision == MGR_PRECISION_SPLIT) {
+            if (m.approx == APPROX_NONE) image_lane<MODE_SPLIT, APPROX_NONE, false, true>(m, m.sorted_line, c, bk, nb, fw, nf, &ro);
+            else image_lane<MODE_SPLIT, APPROX_CLOSELINES, false, true>(m, m.sorted_line, c, bk, nb, fw, nf, &ro);
+        } else {
+            if (m.approx == APPROX_NONE) image_lane<MODE_FP64, APPROX_NONE, false, true>(m, m.sorted_line, c, bk, nb, fw, nf, &ro);
+            else image_lane<MODE_FP64, APPROX_CLOSELINES, false, true>(m, m.sorted_line, c, bk, nb, fw, nf, &ro);
+        }
+    }
+    return MGR_OK;
 }
 
 // One lane's solve for (o, rr, f): out = {u, L_diag, solved}.

@@ -292,6 +292,13 @@ PYBIND11_MODULE(core, m) {
              py::overload_cast<double, double, double, Size, Size>(&Model::compute_image_optical_depth_new),
              py::call_guard<py::gil_scoped_release>())
         .def_readonly("images", &Model::images)
+        .def_readonly("S_ray", &Model::S_ray)
+        .def_readonly("dtau_ray", &Model::dtau_ray)
+        .def_readonly("u_ray", &Model::u_ray)
+        .def_readwrite("density", &Model::density)
+        .def_readwrite("column", &Model::column)
+        .def("compute_image_for_point", &Model::compute_image_for_point, py::call_guard<py::gil_scoped_release>())
+        .def("set_column", &Model::set_column, "Set column (internally).", py::call_guard<py::gil_scoped_release>())
         .def("compute_level_populations", &Model::compute_level_populations, py::arg("use_Ng_acceleration"),
              py::arg("max_niterations"), py::call_guard<py::gil_scoped_release>())
         .def("compute_radiation_field_feautrier_order_2_sparse",

@@ -789,6 +789,37 @@ int Model::image_old(Size ray_nr, bool tau) {
     return 0;
 }
 
+// Model::compute_image_for_point (model.cpp:1039-1058 ->
+// Solver::image_feautrier_order_2_for_point, solver.tpp:629-653): S_ray, dtau_ray and
+// u_ray [n_tot][F] of point p's ray ray_nr.
+int Model::compute_image_for_point(Size ray_nr, Size p) {
+    if (parameters.one_line_approximation)
+        throw std::runtime_error("One line approximation is currently not supported for imaging.");
+    MgrModel* dev = upload();
+    const Size F = parameters.nfreqs_;
+    uint32_t n_tot = 0;
+    check(mgr_image_for_point(dev, parameters.precision, ray_nr, p, &n_tot, nullptr, nullptr, nullptr, 0));
+    S_ray.resize({n_tot, F});
+    dtau_ray.resize({n_tot, F});
+    u_ray.resize({n_tot, F});
+    check(mgr_image_for_point(dev, parameters.precision, ray_nr, p, &n_tot, S_ray.data(), dtau_ray.data(),
+                              u_ray.data(), n_tot));
+    return 0;
+}
+
+// Model::set_column (model.cpp:1143-1153 -> Solver::set_column, solver.tpp:2953-2991):
+// column [nrays][P] of the per-point density.
+int Model::set_column() {
+    if (geometry.rays.use_adaptive_directions)
+        throw std::runtime_error("set_column: adaptive ray directions are not supported.");
+    const Size P = parameters.npoints_.v;
+    if (density.size() != P) throw std::runtime_error("set_column: density must have npoints entries.");
+    MgrModel* dev = upload();
+    column.resize({(Size)parameters.nrays_.v, P});
+    check(mgr_set_column(dev, density.data(), column.data()));
+    return 0;
+}
+
 int Model::compute_image_new(Size ray_nr) { return compute_image_new(ray_nr, 256, 256); }
 
 int Model::compute_image_new(Size ray_nr, Size Nxpix, Size Nypix) {

@@ -248,6 +248,9 @@ class Model {
     Array<double> dshift_max;
     std::vector<double> error_max, error_mean;
     std::vector<Image> images;
+    Array<double> S_ray, dtau_ray, u_ray;  // [n_tot][F] of compute_image_for_point (model.hpp:97-99)
+    Array<double> density;                 // [P], set by the caller (model.hpp:118)
+    Array<double> column;                  // [nrays][P] of set_column (model.hpp:119)
 
     enum SpectralDiscretisation { SD_None, SD_Lines, SD_Image } spectralDiscretisation = SD_None;
 
@@ -277,6 +280,8 @@ class Model {
     int compute_image_optical_depth_new(Size ray_nr);
     int compute_image_optical_depth_new(Size ray_nr, Size Nxpix, Size Nypix);
     int compute_image_optical_depth_new(double rx, double ry, double rz, Size Nxpix, Size Nypix);
+    int compute_image_for_point(Size ray_nr, Size p);
+    int set_column();
     int compute_Jeff();
     int compute_level_populations(bool use_Ng_acceleration, long max_niterations);
     int compute_radiation_field_feautrier_order_2_sparse();

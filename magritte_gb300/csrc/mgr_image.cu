@@ -9,6 +9,8 @@
 // surface) is set up on the host from the model's positions, as Image does
 // (src/model/image/image.cpp:154-398).
 #include <cmath>
+#include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "mgr_image.cuh"
@@ -300,6 +302,219 @@ static int image_new_impl(MgrModel* model, int precision, const double* raydir, 
     return mgr_sync(model);
 }
 
+// ---------------------------------------------------------------------------------
+// Model::compute_image_for_point (model.cpp:1039-1058 ->
+// Solver::image_feautrier_order_2_for_point, solver.tpp:629-653): the old imager's ray
+// through one point, every element's S, dtau and u.  A counting launch gives the ray's
+// element count (traced steps plus interpolation points, both halves, the origin);
+// the solve launch runs one warp per 32 frequencies, each retracing the ray.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(32) image_point_count_kernel(DevModel m, uint32_t cap, uint32_t rr, uint32_t p,
+                                                               int* out, int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    HalfSmem bk, fw;
+    carve_halves(smem, cap, bk, fw);
+    const uint32_t ar = m.antipod[rr];
+    const int nb = trace_half<true, 1>(m, p, rr, cap, bk, lane, status);
+    const int nf = trace_half<true, 1>(m, p, ar, cap, fw, lane, status);
+    uint32_t n = 0;
+    if (nb >= 0 && nf >= 0) {
+        for (int s = lane; s < nb; s += 32) n += m.nint_all[bk.eid[s]];
+        for (int s = lane; s < nf; s += 32) n += m.nint_all[fw.eid[s]];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(FULL_MASK, n, off);
+    if (lane == 0) {
+        out[0] = (nb < 0 || nf < 0) ? -1 : (int)(n + 1);
+        out[1] = nb;
+        out[2] = nf;
+    }
+}
+
+template <int MODE, int AP>
+__global__ void __launch_bounds__(32) image_point_kernel(DevModel m, uint32_t cap, uint32_t rr, uint32_t p, RowOut ro,
+                                                         int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    double* sl = reinterpret_cast<double*>(smem);
+    const uint32_t Lpad = (m.L + 1) & ~1u;
+    HalfSmem bk, fw;
+    carve_halves(smem + (size_t)Lpad * 8, cap, bk, fw);
+    for (uint32_t i = lane; i < m.L; i += 32) sl[i] = m.sorted_line[i];
+    __syncwarp();
+    const uint32_t ar = m.antipod[rr];
+    const double shb = shift_rest(m, rr, p, m.raydir + 3 * rr);
+    const double shf = shift_rest(m, ar, p, m.raydir + 3 * ar);
+    bk.shift0 = shb;
+    fw.shift0 = shf;
+    bk.dsh0 = (float)dsub_rn(shb, 1.0);
+    fw.dsh0 = (float)dsub_rn(shf, 1.0);
+    bk.cshift = fw.cshift = shb;
+    const int nb = trace_half<true, 1>(m, p, rr, cap, bk, lane, status);
+    const int nf = trace_half<true, 1>(m, p, ar, cap, fw, lane, status);
+    if (nb < 0 || nf < 0) return;
+    const uint32_t f = blockIdx.x * 32 + lane;
+    if (f >= m.F) return;
+    LaneCtx c;
+    c.o = p;
+    c.f = f;
+    c.l0 = m.corr_line[f];
+    c.freq = m.nu[(size_t)p * m.F + f];
+    c.fq = (float)c.freq;
+    c.a0 = (float)(c.freq - m.line[c.l0]);
+    image_lane<MODE, AP, false, true>(m, sl, c, bk, nb, fw, nf, &ro);
+    if (!isfinite(ro.u[f])) atomicOr(status, ST_NONFINITE);
+}
+
+template <int MODE>
+static cudaError_t launch_image_point(MgrModel* model, uint32_t rr, uint32_t p, const RowOut& ro) {
+    const uint32_t Lpad = (model->dm.L + 1) & ~1u;
+    const size_t smem = (size_t)Lpad * 8 + half_bytes_per_warp(model->half_cap);
+    auto kern = (model->dm.approx == APPROX_NONE) ? image_point_kernel<MODE, APPROX_NONE>
+                                                  : image_point_kernel<MODE, APPROX_CLOSELINES>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    kern<<<(model->dm.F + 31) / 32, 32, smem, model->stream>>>(model->dm, model->half_cap, rr, p, ro, model->status);
+    return cudaGetLastError();
+}
+
+static int image_for_point_impl(MgrModel* model, int precision, uint32_t ray_nr, uint32_t p, uint32_t* n_tot,
+                                double* S_ray, double* dtau_ray, double* u_ray, uint32_t capacity) {
+    const char* who = "mgr_image_for_point";
+    if (!model || !n_tot) {
+        set_error(std::string(who) + ": null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
+        set_error(std::string(who) + ": unknown precision mode");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (model->dm.approx == APPROX_ONELINE) {
+        set_error(std::string(who) + ": One line approximation is currently not supported for imaging.");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    const DevModel& dm = model->dm;
+    if (ray_nr >= dm.nrays || p >= dm.P) {
+        set_error(std::string(who) + ": ray or point number out of range");
+        return MGR_ERR_ARGUMENT;
+    }
+    int* d_cnt = nullptr;
+    int cnt[3] = {0, 0, 0};
+    cudaError_t e = cudaMalloc(&d_cnt, 3 * sizeof(int));
+    if (e == cudaSuccess) {
+        const size_t smem = half_bytes_per_warp(model->half_cap);
+        e = cudaFuncSetAttribute(image_point_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) {
+            count_launch();
+            image_point_count_kernel<<<1, 32, smem, model->stream>>>(dm, model->half_cap, ray_nr, p, d_cnt,
+                                                                     model->status);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    cudaFree(d_cnt);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    if (cnt[0] < 0) return mgr_sync(model);  // the trace's status bits say why
+    *n_tot = (uint32_t)cnt[0];
+    if (!S_ray && !dtau_ray && !u_ray && capacity == 0) return MGR_OK;  // size query
+    if (!S_ray || !dtau_ray || !u_ray) {
+        set_error(std::string(who) + ": null output array");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (*n_tot > capacity) {
+        set_error(std::string(who) + ": the ray has more elements than the output arrays' rows");
+        return MGR_ERR_CAPACITY;
+    }
+    const size_t NF = (size_t)*n_tot * dm.F;
+    std::memset(S_ray, 0, NF * 8);
+    std::memset(dtau_ray, 0, NF * 8);
+    std::memset(u_ray, 0, NF * 8);
+    if (*n_tot <= 1) return MGR_OK;  // solver.tpp:646: nothing is solved on a one-element ray
+    double* buf = nullptr;
+    e = cudaMalloc(&buf, 4 * NF * 8);
+    if (e == cudaSuccess) {
+        const RowOut ro{buf, buf + NF, buf + 2 * NF, buf + 3 * NF, dm.F};
+        e = (precision == MGR_PRECISION_SPLIT) ? launch_image_point<MODE_SPLIT>(model, ray_nr, p, ro)
+                                               : launch_image_point<MODE_FP64>(model, ray_nr, p, ro);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(S_ray, buf, NF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dtau_ray, buf + NF, NF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(u_ray, buf + 2 * NF, NF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return mgr_sync(model);
+}
+
+// ---------------------------------------------------------------------------------
+// Model::set_column (model.cpp:1143-1153 -> Solver::set_column / get_column,
+// solver.tpp:2953-2991): column[r][o] = sum over the ray's steps of
+// (density[crt] + density[nxt]) / 2 * dZ, from o along r to the boundary, for every ray
+// pair rr < hnrays and its antipode.  Warp per (ray, point) walk with the solves'
+// next-point argmin; the sum in FP64 with the reference's roundings.
+// ---------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) column_kernel(DevModel m, const double* __restrict__ density,
+                                                     double* __restrict__ column, int* status) {
+    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t items = (uint64_t)m.hnrays * 2 * m.P;
+    for (uint64_t it = (uint64_t)blockIdx.x * nw + (threadIdx.x >> 5); it < items; it += (uint64_t)gridDim.x * nw) {
+        const uint32_t o = (uint32_t)(it % m.P);
+        const uint32_t side = (uint32_t)((it / m.P) & 1);
+        const uint32_t rr = (uint32_t)(it / (2ull * m.P));
+        const uint32_t r = side ? m.antipod[rr] : rr;
+        const double* d = m.raydir + 3 * r;
+        const double dx = d[0], dy = d[1], dz = d[2];
+        const double4_32a po = m.pos[o];
+        double Z = 0.0, col = 0.0;
+        uint32_t crt = o;
+        int steps = 0;
+        while (true) {
+            uint32_t nxt, eid;
+            double bestZ;
+            if (!warp_next_point(m, po, dx, dy, dz, crt, Z, lane, nxt, bestZ, eid)) {
+                if (steps > 0 && lane == 0) atomicOr(status, ST_TRACE);
+                break;
+            }
+            const double dZl = dsub_rn(bestZ, Z);
+            Z = dadd_rn(Z, dZl);
+            col = dadd_rn(col, dmul_rn(dmul_rn(0.5, dadd_rn(density[crt], density[nxt])), dZl));
+            steps++;
+            if (m.p2b[nxt] != m.P) break;
+            crt = nxt;
+        }
+        if (lane == 0) column[(size_t)r * m.P + o] = col;
+    }
+}
+
+static int set_column_impl(MgrModel* model, const double* density, double* column) {
+    const char* who = "mgr_set_column";
+    if (!model || !density || !column) {
+        set_error(std::string(who) + ": null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    const DevModel& dm = model->dm;
+    const size_t RP = (size_t)dm.nrays * dm.P;
+    double* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, (RP + dm.P) * 8);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf + RP, density, (size_t)dm.P * 8, cudaMemcpyHostToDevice, model->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(buf, 0, RP * 8, model->stream);
+    if (e == cudaSuccess) {
+        const uint64_t warps = (uint64_t)dm.hnrays * 2 * dm.P;
+        const unsigned blocks = (unsigned)std::min<uint64_t>((warps + 7) / 8, (uint64_t)model->sm_count * 8);
+        count_launch();
+        column_kernel<<<blocks ? blocks : 1, 256, 0, model->stream>>>(dm, buf + RP, buf, model->status);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(column, buf, RP * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, who);
+    return mgr_sync(model);
+}
+
 }  // namespace mgr
 
 using namespace mgr;
@@ -322,6 +537,15 @@ int mgr_image_optical_depth(MgrModel* model, int precision, uint32_t ray_nr, dou
 int mgr_image_optical_depth_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny,
                                 double* I, double* ImX, double* ImY) {
     return image_new_impl(model, precision, raydir, nx, ny, I, ImX, ImY, true, "mgr_image_optical_depth_new");
+}
+
+int mgr_image_for_point(MgrModel* model, int precision, uint32_t ray_nr, uint32_t p, uint32_t* n_tot, double* S_ray,
+                        double* dtau_ray, double* u_ray, uint32_t capacity) {
+    return image_for_point_impl(model, precision, ray_nr, p, n_tot, S_ray, dtau_ray, u_ray, capacity);
+}
+
+int mgr_set_column(MgrModel* model, const double* density, double* column) {
+    return set_column_impl(model, density, column);
 }
 
 

@@ -72,11 +72,59 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// One step of Geometry::get_next_general_geometry<Defaulttracer> (geometry.tpp:13-44),
+// warp-cooperative: among crt's neighbours with Zn > Z (Zn the distance along the ray
+// from the origin po), the one closest to the ray; lanes scan the neighbour list and the
+// argmin of (distance to ray, neighbour order) reproduces the reference's strict-< scan.
+// Every lane returns the same result: false when no neighbour lies further along the
+// ray, else the next point, its Zn and its neighbour-record index.
+__device__ __forceinline__ bool warp_next_point(const DevModel& m, const double4_32a& po, double dx, double dy,
+                                                double dz, uint32_t crt, double Z, int lane, uint32_t& nxt,
+                                                double& Znext, uint32_t& eid) {
+    const uint32_t nnb = m.n_nb[crt];
+    const uint32_t cum = m.cum_nb[crt];
+    const unsigned long long zkey = dkey(Z);
+    unsigned long long best = ~0ull;
+    uint32_t besti = 0xffffffffu;
+    double bestZ = 0.0;
+    for (uint32_t i = lane; i < nnb; i += 32) {
+        const double4_32a e = m.edge[cum + i];
+        const double Rx = dsub_rn(e.x, po.x);
+        const double Ry = dsub_rn(e.y, po.y);
+        const double Rz = dsub_rn(e.z, po.z);
+        const double Zn = dot3_rn(Rx, Ry, Rz, dx, dy, dz);
+        if (dkey(Zn) > zkey) {  // Zn > Z
+            const double d2 = dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), dmul_rn(Zn, Zn));
+            const unsigned long long k = dkey(d2);
+            if (k < best) {
+                best = k;
+                besti = i;
+                bestZ = Zn;
+            }
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long ob = __shfl_xor_sync(FULL_MASK, best, off);
+        const uint32_t oi = __shfl_xor_sync(FULL_MASK, besti, off);
+        const double oz = __shfl_xor_sync(FULL_MASK, bestZ, off);
+        if (ob < best || (ob == best && oi < besti)) {
+            best = ob;
+            besti = oi;
+            bestZ = oz;
+        }
+    }
+    if (besti == 0xffffffffu) return false;
+    eid = cum + besti;
+    nxt = (uint32_t)__double_as_longlong(m.edge[eid].w);
+    Znext = bestZ;
+    return true;
+}
+
 // Warp-cooperative Geometry::get_next_general_geometry<Defaulttracer> walk
-// (geometry.tpp:13-44) from origin o along ray r until a boundary point is met.
-// Lanes scan the neighbour list; the argmin of (distance to ray, neighbour order)
-// reproduces the reference's strict-< scan.  Returns the number of steps, or -1 on
-// capacity overflow / invalid geometry (status bits set).
+// (geometry.tpp:13-44) from origin o along ray r until a boundary point is met
+// (warp_next_point per step).  Returns the number of steps, or -1 on capacity
+// overflow / invalid geometry (status bits set).
 // FRAME 0: comoving shifts relative to the origin point (the formal solves);
 // FRAME 1: rest-frame shifts of the old imager (Geometry::get_shift<Rest>, reversed for
 // r >= hnrays, geometry.tpp:428-465).
@@ -90,40 +138,9 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
     uint32_t crt = o;
     int count = 0;
     while (true) {
-        const uint32_t nnb = m.n_nb[crt];
-        const uint32_t cum = m.cum_nb[crt];
-        const unsigned long long zkey = dkey(Z);
-        unsigned long long best = ~0ull;
-        uint32_t besti = 0xffffffffu;
-        double bestZ = 0.0;
-        for (uint32_t i = lane; i < nnb; i += 32) {
-            const double4_32a e = m.edge[cum + i];
-            const double Rx = dsub_rn(e.x, po.x);
-            const double Ry = dsub_rn(e.y, po.y);
-            const double Rz = dsub_rn(e.z, po.z);
-            const double Zn = dot3_rn(Rx, Ry, Rz, dx, dy, dz);
-            if (dkey(Zn) > zkey) {  // Zn > Z
-                const double d2 = dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), dmul_rn(Zn, Zn));
-                const unsigned long long k = dkey(d2);
-                if (k < best) {
-                    best = k;
-                    besti = i;
-                    bestZ = Zn;
-                }
-            }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const unsigned long long ob = __shfl_xor_sync(FULL_MASK, best, off);
-            const uint32_t oi = __shfl_xor_sync(FULL_MASK, besti, off);
-            const double oz = __shfl_xor_sync(FULL_MASK, bestZ, off);
-            if (ob < best || (ob == best && oi < besti)) {
-                best = ob;
-                besti = oi;
-                bestZ = oz;
-            }
-        }
-        if (besti == 0xffffffffu) {
+        uint32_t nxt, eid;
+        double bestZ;
+        if (!warp_next_point(m, po, dx, dy, dz, crt, Z, lane, nxt, bestZ, eid)) {
             // No point further along the ray.  From the origin this is an empty half;
             // after a step it means the walk left the grid on an interior point, where
             // the reference would index point2boundary out of range.
@@ -136,12 +153,11 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
             count = -1;
             break;
         }
-        const uint32_t nxt = (uint32_t)__double_as_longlong(m.edge[cum + besti].w);
         const double dZl = dsub_rn(bestZ, Z);
         Z = dadd_rn(Z, dZl);
         if (STORE && lane == 0) {
             h.ids[count] = nxt;
-            h.eid[count] = cum + besti;
+            h.eid[count] = eid;
             h.dZ[count] = dZl;
         }
         count++;
@@ -1006,11 +1022,27 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
 // 2 Su[last] - I_bdy(nr[last], nu(o, f)), Su[last] being the last row's solution.  The
 // ray's elements use all-line interpolation (kAllLines) and the halves' shift0.  With
 // nf = 0 (new imager) the origin itself is the last element.
-template <int MODE, int AP, bool TAU = false>
+//
+// ROWS (Solver::image_feautrier_order_2_for_point_loc, solver.tpp:2582-2715): the lane
+// also writes, per element k of the ray (row k, stride ro->F, column c.f), the source at
+// the far end of the pair ending there (row 0: the first pair's near end), that pair's
+// optical depth (row 0: 0) and, after back substitution u[k] = Su[k] + FI[k] u[k+1], the
+// Feautrier mean intensity; ro->FI holds the rows' FI meanwhile.
+struct RowOut {
+    double* S;
+    double* dtau;
+    double* u;
+    double* FI;
+    uint32_t F;
+};
+
+template <int MODE, int AP, bool TAU = false, bool ROWS = false>
 __host__ __device__ double image_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
-                                      int nb, const HalfSmem& fw, int nf) {
+                                      int nb, const HalfSmem& fw, int nf, const RowOut* ro = nullptr) {
     using T = typename Real_<MODE>::T;
     if (nb <= 0 && nf <= 0) return TAU ? 0.0 : boundary_intensity(m, c.o, c.freq);
+    size_t row = 0;  // ROWS: index of the row the current pair ends on, times F
+    const size_t rstep = ROWS ? ro->F : 0;
     const Elem cen = centre_elem(c.o, bk.cshift, (float)dsub_rn(bk.cshift, 1.0));
     ElemIter ib, iu;
     int phase;  // 0: backward half, 2: forward half, 3: done
@@ -1074,8 +1106,19 @@ __host__ __device__ double image_lane(const DevModel& m, const double* sl, const
             st.F = 0.5 * Bb_min_Cb * dt * dt;
             st.FI = drcp<MODE>(1.0 + st.F);
             first = false;
+            if constexpr (ROWS) {
+                ro->S[c.f] = (double)po.Slo;
+                ro->dtau[c.f] = 0.0;
+            }
         } else {
             elim_row<MODE>(dt_prev, po.dtau, po.Slo, st.F, st.FI, st.Su);
+        }
+        if constexpr (ROWS) {
+            ro->u[row + c.f] = st.Su;
+            ro->FI[row + c.f] = st.FI;
+            row += rstep;
+            ro->S[row + c.f] = (double)po.Shi;
+            ro->dtau[row + c.f] = (double)po.dtau;
         }
         dt_prev = po.dtau;
         S_last = po.Shi;
@@ -1100,6 +1143,15 @@ __host__ __device__ double image_lane(const DevModel& m, const double* sl, const
     const double denominator = drcp<MODE>(Bl * st.F + Bl_min_Al);
     const double Sl = (double)S_last + 2.0 * Ibdy_l * inverse_dtau_l;
     const double u = (Al * st.Su + Sl) * (1.0 + st.F) * denominator;
+    if constexpr (ROWS) {
+        double un = u;
+        ro->u[row + c.f] = un;
+        while (row > 0) {
+            row -= rstep;
+            un = ro->u[row + c.f] + un * ro->FI[row + c.f];
+            ro->u[row + c.f] = un;
+        }
+    }
     return 2.0 * u - boundary_intensity(m, last.nr, c.freq);
 }
 

@@ -1041,6 +1041,150 @@ static int image_fo2_impl(const OrcModel* m, uint32_t rr, double* I, int nthread
     return err_any ? -2 : 0;
 }
 
+/* Solver::image_feautrier_order_2_for_point_loc (solver.tpp:2582-2715): the old imager's
+ * ray through o, eliminated forward and then back-substituted along the whole ray.
+ * Row k of S / dtau / u (stride F) is element first + k: S holds each pair's source at
+ * its far end (the first pair's near end in row 0), dtau the pair's optical depth
+ * ending at that element (0 in row 0), u the Feautrier mean intensity. */
+static void solve_for_point(const OrcModel* m, Buf* b, uint32_t o, uint32_t f, double* S, double* dtau,
+                            double* u) {
+    const uint32_t F     = m->nfreqs;
+    const double freq    = m->nu[(size_t)o * F + f];
+    const uint32_t l     = m->corr_line[f];
+    const uint32_t first = b->first, last = b->last;
+    double chi_c = 0.0, chi_n = 0.0, dtau_c, dtau_n = 0.0, term_c = 0.0, term_n = 0.0;
+    int cco = 1;
+    double* Su = b->Su; double* A = b->A; double* C = b->C; double* iA = b->inverse_A;
+    double* iC = b->inverse_C; double* FF = b->FF; double* FI = b->FI;
+
+    compute_source_dtau(m, b->nr[first], b->nr[first + 1], b->nr_interp[first], b->nr_interp[first + 1], l,
+                        freq * b->shift[first], freq * b->shift[first + 1], b->shift[first],
+                        b->shift[first + 1], b->dZ[first], b->interp_factor[first],
+                        b->interp_factor[first + 1], &cco, &dtau_n, &chi_c, &chi_n, &term_c, &term_n);
+    S[f]        = term_c;
+    S[F + f]    = term_n;
+    dtau[f]     = 0.0;
+    dtau[F + f] = dtau_n;
+
+    const double inverse_dtau_f = 1.0 / dtau_n;
+    C[first]                    = 2.0 * inverse_dtau_f * inverse_dtau_f;
+    const double Bf_min_Cf      = 1.0 + 2.0 * inverse_dtau_f;
+    const double Bf             = Bf_min_Cf + C[first];
+    const double I_bdy_f        = boundary_intensity(m, b->nr[first], freq * b->shift[first]);
+    Su[first]                   = term_c + 2.0 * I_bdy_f * inverse_dtau_f;
+    Su[first] /= Bf;
+    FF[first] = 0.5 * Bf_min_Cf * dtau_n * dtau_n;
+    FI[first] = 1.0 / (1.0 + FF[first]);
+
+    for (uint32_t n = first + 1; n < last; n++) {
+        term_c = term_n;
+        dtau_c = dtau_n;
+        chi_c  = chi_n;
+        compute_source_dtau(m, b->nr[n], b->nr[n + 1], b->nr_interp[n], b->nr_interp[n + 1], l,
+                            freq * b->shift[n], freq * b->shift[n + 1], b->shift[n], b->shift[n + 1],
+                            b->dZ[n], b->interp_factor[n], b->interp_factor[n + 1], &cco, &dtau_n,
+                            &chi_c, &chi_n, &term_c, &term_n);
+        const double dtau_avg = 0.5 * (dtau_c + dtau_n);
+        iA[n]                 = dtau_avg * dtau_c;
+        iC[n]                 = dtau_avg * dtau_n;
+        S[(size_t)(n + 1 - first) * F + f]    = term_n;
+        dtau[(size_t)(n + 1 - first) * F + f] = dtau_n;
+        A[n]  = 1.0 / iA[n];
+        C[n]  = 1.0 / iC[n];
+        Su[n] = term_c;
+        FF[n] = (A[n] * FF[n - 1] * FI[n - 1] + 1.0) * iC[n];
+        FI[n] = 1.0 / (1.0 + FF[n]);
+        Su[n] = (A[n] * Su[n - 1] + Su[n]) * FI[n] * iC[n];
+    }
+
+    const double inverse_dtau_l = 1.0 / dtau_n;
+    A[last]                     = 2.0 * inverse_dtau_l * inverse_dtau_l;
+    const double Bl_min_Al      = 1.0 + 2.0 * inverse_dtau_l;
+    const double Bl             = Bl_min_Al + A[last];
+    const double denominator    = 1.0 / (Bl * FF[last - 1] + Bl_min_Al);
+    const double I_bdy_l        = boundary_intensity(m, b->nr[last], freq * b->shift[last]);
+    Su[last]                    = term_n + 2.0 * I_bdy_l * inverse_dtau_l;
+    Su[last]                    = (A[last] * Su[last - 1] + Su[last]) * (1.0 + FF[last - 1]) * denominator;
+    u[(size_t)(last - first) * F + f] = Su[last];
+    for (int64_t n = (int64_t)last - 1; n >= (int64_t)first; n--) {
+        Su[n] += Su[n + 1] * FI[n];
+        u[(size_t)(n - first) * F + f] = Su[n];
+    }
+}
+
+/* Solver::image_feautrier_order_2_for_point (solver.tpp:629-653) for point p along ray
+ * rr.  *n_tot receives the ray's element count; the rows are written when it is at most
+ * capacity (S / dtau / u are [capacity][F], rows past n_tot untouched; a ray of one
+ * element writes nothing).  Returns -3 when the ray does not fit. */
+int orc_image_for_point(const OrcModel* m, uint32_t rr, uint32_t p, uint32_t* n_tot, double* S, double* dtau,
+                        double* u, uint32_t capacity) {
+    const uint32_t length = 2 * orc_ray_lengths_max(m, 1) + 1;
+    Buf b;
+    if (buf_init(&b, length) != 0) return -1;
+    const uint32_t c  = b.centre;
+    const uint32_t ar = m->antipod[rr];
+    int err           = 0;
+    b.nr[c]           = p;
+    b.shift[c]        = get_shift(m, 1, p, rr, p);
+    const int64_t first = trace(m, &b, 1, UINT32_MAX, p, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
+    const int64_t last  = trace(m, &b, 1, UINT32_MAX, p, ar, +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
+    if (err) {
+        buf_free(&b);
+        return -2;
+    }
+    b.first = (uint32_t)first;
+    b.last  = (uint32_t)last;
+    b.n_tot = (uint32_t)(last + 1 - first);
+    *n_tot  = b.n_tot;
+    int rc  = 0;
+    if (b.n_tot > capacity) rc = -3;
+    else if (b.n_tot > 1)
+        for (uint32_t f = 0; f < m->nfreqs; f++) solve_for_point(m, &b, p, f, S, dtau, u);
+    buf_free(&b);
+    return rc;
+}
+
+/* Solver::set_column / get_column (solver.tpp:2953-2991): column[r][o] is the trapezoid
+ * integral of density from o along ray r to the boundary, for every ray pair (rr and its
+ * antipode).  Rays that no pair names stay as given. */
+int orc_set_column(const OrcModel* m, const double* density, double* column, int nthreads) {
+    const uint32_t P = m->npoints;
+    int err_any      = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    for (uint32_t rr = 0; rr < m->hnrays; rr++) {
+        const uint32_t ar = m->antipod[rr];
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t oo = 0; oo < (int64_t)P; oo++) {
+            const uint32_t o = (uint32_t)oo;
+            for (int side = 0; side < 2; side++) {
+                const uint32_t r     = side ? ar : rr;
+                const double* origin = m->position + 3 * o;
+                const double* raydir = m->ray_direction + 3 * r;
+                double col = 0.0, Z = 0.0, dZ = 0.0;
+                uint32_t nxt = get_next(m, origin, raydir, o, &Z, &dZ);
+                if (valid_point(m, nxt)) {
+                    uint32_t crt = o;
+                    col += 0.5 * (density[crt] + density[nxt]) * dZ;
+                    while (not_on_boundary(m, nxt)) {
+                        crt = nxt;
+                        nxt = get_next(m, origin, raydir, nxt, &Z, &dZ);
+                        if (!valid_point(m, nxt)) { /* the reference would read past point2boundary */
+#pragma omp atomic write
+                            err_any = 1;
+                            break;
+                        }
+                        col += 0.5 * (density[crt] + density[nxt]) * dZ;
+                    }
+                }
+                column[(size_t)r * P + o] = col;
+            }
+        }
+    }
+    return err_any ? -2 : 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* New imager (solver.tpp:576-627, :808-897; image.cpp:221-398;          */
 /* geometry.tpp:55-106, :167-193, :310-367)                              */

@@ -147,6 +147,13 @@ int orc_image_new(const OrcModel* m, const double* raydir, uint32_t nx, uint32_t
  * orc_image_new, I = the summed optical depth from first to last
  * (image_optical_depth(model, o, f), solver.tpp:2718-2760), 0 for a ray of one point. */
 int orc_image_optical_depth(const OrcModel* m, uint32_t rr, double* I, int nthreads);
+/* Solver::image_feautrier_order_2_for_point (solver.tpp:629-653, :2582-2715): the rows
+ * S_ray / dtau_ray / u_ray [n_tot][F] of point p's ray rr (capacity rows given; -3 when
+ * n_tot exceeds it, *n_tot always set). */
+int orc_image_for_point(const OrcModel* m, uint32_t rr, uint32_t p, uint32_t* n_tot, double* S, double* dtau,
+                        double* u, uint32_t capacity);
+/* Solver::set_column (solver.tpp:2953-2991): column [nrays][P] from density [P]. */
+int orc_set_column(const OrcModel* m, const double* density, double* column, int nthreads);
 int orc_image_optical_depth_new(const OrcModel* m, const double* raydir, uint32_t nx, uint32_t ny, double* I,
                                 double* ImX, double* ImY, int nthreads);
 

@@ -401,6 +401,38 @@ class Oracle:
             raise RuntimeError(f"oracle optical-depth new imager failed ({rc})")
         return dict(I=I, ImX=X, ImY=Y)
 
+    def image_for_point(self, rr, p):
+        """Solver::image_feautrier_order_2_for_point (solver.tpp:629-653): S_ray, dtau_ray,
+        u_ray [n_tot][F] of point p's ray rr (zeros for a ray of one element)."""
+        F = self.a["nfreqs"]
+        l = lib()
+        l.orc_image_for_point.restype = C.c_int
+        l.orc_image_for_point.argtypes = [C.POINTER(OrcModel), C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
+                                          _f64p, _f64p, _f64p, C.c_uint32]
+        n = C.c_uint32(0)
+        rc = l.orc_image_for_point(C.byref(self.m), rr, p, C.byref(n), None, None, None, 0)
+        if rc not in (0, -3):
+            raise RuntimeError(f"oracle image_for_point failed ({rc})")
+        out = {k: np.zeros((n.value, F)) for k in ("S_ray", "dtau_ray", "u_ray")}
+        rc = l.orc_image_for_point(C.byref(self.m), rr, p, C.byref(n), _ptr(out["S_ray"], _f64p),
+                                   _ptr(out["dtau_ray"], _f64p), _ptr(out["u_ray"], _f64p), n.value)
+        if rc != 0:
+            raise RuntimeError(f"oracle image_for_point failed ({rc})")
+        return out
+
+    def set_column(self, density, nthreads=0):
+        """Solver::set_column (solver.tpp:2953-2991): column [nrays][P]."""
+        P, R = self.a["npoints"], self.a["nrays"]
+        rho = np.ascontiguousarray(density, np.float64)
+        col = np.zeros((R, P))
+        l = lib()
+        l.orc_set_column.restype = C.c_int
+        l.orc_set_column.argtypes = [C.POINTER(OrcModel), _f64p, _f64p, C.c_int]
+        rc = l.orc_set_column(C.byref(self.m), _ptr(rho, _f64p), _ptr(col, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle set_column failed ({rc})")
+        return col
+
     def image_fo2(self, rr, nthreads=0):
         P, F = self.a["npoints"], self.a["nfreqs"]
         I = np.zeros((P, F))

@@ -170,9 +170,11 @@ def test_core_model_anisotropic_solve(gpu_lib):
 @pytest.mark.parametrize("precision", ["fp64", "split"])
 def test_uv_solve_matches_emulated_lane_code(gpu_lib, precision):
     """compute_radiation_field_feautrier_order_2_uv on the GPU against the same lane
-    code on the CPU (which test_kernel_emulation.py checks against the oracle): u to
-    1e-12 (FP64), v to 1e-9 of u plus the rounding of u amplified by v's
-    finite-difference coefficients (~1/dtau)."""
+    code on the CPU (which test_kernel_emulation.py checks against the oracle).  The
+    reference's arithmetic calls single-precision erff / expf, whose CUDA and host
+    results differ by ulps, so u agrees to 1e-6 in FP64 (whose bar against the oracle
+    is 1e-5) and to split precision's 1e-5 bar (its physics is single precision), v to that difference of u amplified by v's finite-difference
+    coefficients (~1/dtau), plus the same relative change of the coefficients."""
     import ctypes as C
     from magritte_gb300 import build
 
@@ -190,13 +192,14 @@ def test_uv_solve_matches_emulated_lane_code(gpu_lib, precision):
     u, v, dtm, dtp = (np.zeros_like(got["u"]) for _ in range(4))
     assert emu.mgr_emu_formal_solve_fo2_uv(C.byref(desc), _abi.PRECISION[precision],
                                            *[x.ctypes.data_as(p) for x in (u, v, dtm, dtp)]) == 0
-    tol = 1e-12 if precision == "fp64" else 1e-6
+    tol = 1e-6 if precision == "fp64" else 1e-5
     assert H.max_rel(got["u"], u) < tol
     both = (dtm > 0) & (dtp > 0)
     cm = np.where(both, dtp / np.where(both, dtm * dtm + dtm * dtp, 1.0), 0.0)
     cp = np.where(both, dtm / np.where(both, dtm * dtp + dtp * dtp, 1.0), 0.0)
-    noise = 64 * np.finfo(float).eps * np.abs(u) * (cm + cp + np.abs(cm - cp))
-    assert np.all(np.abs(got["v"] - v) <= max(tol, 1e-9) * np.abs(u) + noise)
+    amp = np.abs(u) * (cm + cp + np.abs(cm - cp))
+    bound = tol * (amp + np.abs(v)) + 1e-9 * np.abs(u) + 64 * np.finfo(float).eps * amp
+    assert np.all(np.abs(got["v"] - v) <= bound)
 
 
 def test_core_model_uv_known_answer(gpu_lib):

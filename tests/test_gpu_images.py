@@ -124,3 +124,67 @@ def test_core_model_optical_depth_images(gpu_lib):
     assert [im.imageType for im in model.images] == [1, 1]
     assert H.max_rel(np.array(model.images[0].I), ref, floor=1e-12 * np.abs(ref).max()) < 1e-5
     assert np.array(model.images[1].I).shape == (256, raw.nquads)
+
+
+@pytest.mark.parametrize("approx", ["CloseLines", "None"])
+def test_image_for_point_matches_oracle(gpu_lib, approx):
+    """compute_image_for_point (solver.tpp:629-653, :2582-2715): the rows S_ray,
+    dtau_ray, u_ray of interior and boundary points' rays, FP64 and split precision,
+    within the imagers' 1e-5 (split: above 1e-10 of the largest entry); the row count
+    (traced points plus interpolation points) exact."""
+    raw = S.grid_sphere(n=16, nside=1, nquads=7)
+    a = H.setup(raw, approx=approx)
+    orc = O.Oracle(a)
+    b0 = int(np.nonzero(np.asarray(a["point2boundary"]) != a["npoints"])[0][0])
+    dev = _abi.DeviceModel(a)
+    try:
+        for rr, p in ((0, a["npoints"] // 2), (9, 123), (5, b0)):
+            ref = orc.image_for_point(rr, p)
+            for precision in ("fp64", "split"):
+                g = dev.image_for_point(rr, p, precision)
+                assert g["u_ray"].shape == ref["u_ray"].shape, (rr, p)
+                for k in ("S_ray", "dtau_ray", "u_ray"):
+                    # split precision's single-precision sources underflow far in the line wings
+                    floor = 1e-300 if precision == "fp64" else 1e-10 * np.abs(ref[k]).max()
+                    assert H.max_rel(g[k], ref[k], floor=floor) < 1e-5, (rr, p, precision, k)
+    finally:
+        dev.close()
+
+
+def test_set_column_matches_oracle_bit_exact(gpu_lib):
+    """set_column (solver.tpp:2953-2991): the same walk and the same FP64 roundings, so
+    every column equals the oracle's bit for bit."""
+    raw = S.grid_sphere(n=16, nside=1, nquads=7)
+    a = H.setup(raw)
+    rho = np.random.default_rng(2).uniform(1e6, 1e8, a["npoints"])
+    ref = O.Oracle(a).set_column(rho)
+    dev = _abi.DeviceModel(a)
+    try:
+        np.testing.assert_array_equal(dev.set_column(rho), ref)
+    finally:
+        dev.close()
+
+
+def test_core_model_image_for_point_and_column(gpu_lib):
+    """The drop-in calls: core.Model.compute_image_for_point fills S_ray / dtau_ray /
+    u_ray, set_column fills column from density."""
+    from magritte_gb300 import loader
+
+    raw = H.all_constant_model()
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    model.compute_image_for_point(0, 17)
+    u = np.array(model.u_ray)[:, 0]
+    if raw.ray_direction[0][0] > 0:
+        u = u[::-1]
+    assert np.max(np.abs(H.relative_error(H.all_constant_solution(raw), u))) < 1.7e-4
+    assert np.array(model.S_ray).shape == np.array(model.dtau_ray).shape == (raw.npoints, 1)
+    model.density.set(np.ones(raw.npoints))
+    model.set_column()
+    col = np.array(model.column)
+    x = raw.position[:, 0]
+    for r in range(raw.nrays):
+        expect = (x[-1] - x) if raw.ray_direction[r][0] > 0 else (x - x[0])
+        np.testing.assert_allclose(col[r], expect, rtol=1e-14, atol=1e-3)

@@ -153,3 +153,36 @@ def test_emulated_uv_matches_oracle(emu, name, approx):
         noise = 64 * np.finfo(float).eps * np.abs(ref["u"]) * (cm + cp + np.abs(cm - cp))
         bound = (tol_v if precision == "split" else 1e-9) * np.abs(ref["u"]) + noise
         assert np.all(np.abs(v - ref["v"]) <= bound), precision
+
+
+@pytest.mark.parametrize("name", ["cube10", "sphere14", "all_constant"])
+@pytest.mark.parametrize("approx", ["CloseLines", "None"])
+def test_emulated_image_for_point_matches_oracle(emu, name, approx):
+    """image_lane with its per-row outputs (the image_for_point kernel's lane code) against
+    the oracle's image_feautrier_order_2_for_point: row count exact, S_ray / dtau_ray /
+    u_ray to 1e-12 in FP64 and 1e-5 in split precision (above 1e-10 of the largest entry:
+    single-precision sources underflow far in the line wings)."""
+    raw = MODELS[name]()
+    a = H.setup(raw, approx=approx)
+    orc = O.Oracle(a)
+    p64 = C.POINTER(C.c_double)
+    emu.mgr_emu_image_for_point.argtypes = [C.POINTER(_abi.MgrModelDesc), C.c_int, C.c_uint32, C.c_uint32,
+                                            C.POINTER(C.c_uint32), p64, p64, p64, C.c_uint32]
+    emu.mgr_emu_image_for_point.restype = C.c_int
+    desc, keep = _abi.make_desc(a)
+    P = a["npoints"]
+    bnd = np.nonzero(np.asarray(a["point2boundary"]) != P)[0]
+    for rr, p in ((0, P // 2), (1 % a["nrays"], P // 3), (0, int(bnd[0]))):
+        ref = orc.image_for_point(rr, p)
+        n = ref["u_ray"].shape[0]
+        for precision, tol in (("fp64", 1e-12), ("split", 1e-5)):
+            got = {k: np.zeros((n, a["nfreqs"])) for k in ("S_ray", "dtau_ray", "u_ray")}
+            nt = C.c_uint32(0)
+            assert emu.mgr_emu_image_for_point(C.byref(desc), _abi.PRECISION[precision], rr, p, C.byref(nt),
+                                               got["S_ray"].ctypes.data_as(p64), got["dtau_ray"].ctypes.data_as(p64),
+                                               got["u_ray"].ctypes.data_as(p64), n) == 0
+            assert nt.value == n
+            for k in got:
+                # split precision's single-precision sources underflow far in the line wings
+                floor = 1e-300 if precision == "fp64" else 1e-10 * np.abs(ref[k]).max()
+                assert H.max_rel(got[k], ref[k], floor=floor) < tol, (rr, p, precision, k)

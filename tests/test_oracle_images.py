@@ -112,3 +112,63 @@ def test_optical_depth_new_image_sums_the_imager_pairs():
     np.testing.assert_array_equal(t["ImX"], img["ImX"])
     assert np.all(t["I"] >= 0.0)
     assert (t["I"] > 0.0).any()
+
+
+def test_image_for_point_all_constant_known_answer(built):
+    """image_feautrier_order_2_for_point (solver.tpp:629-653, :2582-2715) on the
+    all-constant single ray (all_constant_single_ray.py:121-131): the ray through any
+    point is the whole line, so u_ray holds the analytic u at every point (the
+    reference's formal-solve bound 1.7e-4), S_ray the constant source em/op and dtau_ray
+    chi dx."""
+    raw = H.all_constant_model()
+    a = H.setup(raw)
+    orc = O.Oracle(a)
+    u_ref = H.all_constant_solution(raw)
+    x = raw.position[:, 0]
+    for p in (0, 17, raw.npoints - 1):
+        r = orc.image_for_point(0, p)
+        assert r["u_ray"].shape == (raw.npoints, a["nfreqs"])
+        u = r["u_ray"][:, 0]
+        # rows run from the far end of ray 0's backward half to the far end of its antipode
+        if raw.ray_direction[0][0] > 0:
+            u = u[::-1]
+        assert np.max(np.abs(H.relative_error(u_ref, u))) < 1.7e-4
+        S_row = r["S_ray"][:, 0]
+        assert np.max(np.abs(S_row / S_row[0] - 1.0)) < 1e-6
+        dt = r["dtau_ray"][1:, 0]
+        assert r["dtau_ray"][0, 0] == 0.0 and np.max(np.abs(dt / dt[0] - 1.0)) < 1e-5
+    # the old imager's pixel is 2 u[last] - I_bdy of the same elimination
+    img = orc.image_fo2(0)
+    r = orc.image_for_point(0, 17)
+    ibdy = 2.0 * r["u_ray"][-1] - img[17]
+    assert np.all(ibdy > 0) and np.max(np.abs(ibdy / ibdy[0] - 1.0)) < 1e-3
+
+
+def test_set_column_known_answers(built):
+    """set_column / get_column (solver.tpp:2953-2991): on the single ray a unit density
+    gives each point's distance to the line's end in the ray's direction; a linear
+    density profile is integrated exactly by the trapezoid rule; columns are linear in
+    the density."""
+    raw = H.all_constant_model()
+    a = H.setup(raw)
+    orc = O.Oracle(a)
+    x = raw.position[:, 0]
+    P = raw.npoints
+    col = orc.set_column(np.ones(P))
+    for r in range(raw.nrays):
+        if raw.ray_direction[r][0] > 0:
+            np.testing.assert_allclose(col[r], x[-1] - x, rtol=1e-14, atol=1e-3)
+        else:
+            np.testing.assert_allclose(col[r], x - x[0], rtol=1e-14, atol=1e-3)
+    rho = 1.0 + x / x[-1]
+    colr = orc.set_column(rho)
+    r_plus = [r for r in range(raw.nrays) if raw.ray_direction[r][0] > 0][0]
+    exact = (x[-1] - x) + (x[-1] ** 2 - x ** 2) / (2.0 * x[-1])
+    np.testing.assert_allclose(colr[r_plus], exact, rtol=1e-12, atol=1e-3)
+    # linearity on a 3D model
+    a3 = H.setup(S.grid_sphere(n=10, nside=1, nquads=5))
+    o3 = O.Oracle(a3)
+    rng = np.random.default_rng(5)
+    r1, r2 = rng.uniform(1, 2, a3["npoints"]), rng.uniform(1, 2, a3["npoints"])
+    c1, c2, c12 = o3.set_column(r1), o3.set_column(r2), o3.set_column(2.0 * r1 + 3.0 * r2)
+    np.testing.assert_allclose(c12, 2.0 * c1 + 3.0 * c2, rtol=1e-12, atol=0)
