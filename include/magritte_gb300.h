@@ -94,6 +94,12 @@ typedef struct {
     double max_interpolation_diff;
     double max_distance_opacity_contribution;
     int32_t approx;                       /* MgrApprox */
+    /* Parameters::spherical_symmetry (src/model/parameters/parameters.hpp:50): 1D model
+     * of shells on the x axis in ascending radius (position [P][3] = (r, 0, 0)), rays in
+     * the x-y plane; traced by Geometry::get_next_spherical_symmetry
+     * (src/model/geometry/geometry.tpp:118-159) with the Z-dependent shifts of
+     * get_shift_spherical_symmetry (:378-417).  The neighbour lists are not used. */
+    int32_t spherical_symmetry;
 } MgrModelDesc;
 
 typedef struct MgrModel MgrModel;
@@ -225,8 +231,10 @@ int mgr_formal_solve_sc0_device(MgrModel* model, int precision, double* J_dev, d
  * Solver::image_feautrier_order_2(model, rr), src/solver/solver.tpp:542-574): the
  * rest-frame image along ray ray_nr with one ray per model point.
  *   I [P][F], ImX / ImY [P] image-plane coordinates (Image, image.cpp:154-219; may be
- *   NULL).  CloseLines or None approximation (OneLine is rejected, as the reference
- *   does).  Blocks. */
+ *   NULL): the 3D plane of the ray, or (x, 0) for a spherically symmetric model (the
+ *   reference's 1D rule, which a caller with other 1D models applies itself).
+ *   CloseLines or None approximation (OneLine is rejected, as the reference does).
+ *   Blocks. */
 int mgr_image(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY);
 
 /* Model::compute_image_new(raydir, nx, ny) (model.cpp:989-1013 ->

@@ -35,7 +35,7 @@ DESC_FIELDS = [
     ("in_line_integral", _u8p), ("nrad", _u32p), ("nrad_cum", _u32p), ("line_A", _f64p),
     ("lspec_inverse_mass", _f64p), ("quad_weights", _f64p), ("quad_roots", _f64p),
     ("min_opacity", C.c_double), ("min_dtau", C.c_double), ("max_interpolation_diff", C.c_double),
-    ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int32),
+    ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int32), ("spherical_symmetry", C.c_int32),
 ]
 
 _PTR_TYPES = {_u32p: np.uint32, _i32p: np.int32, _f64p: np.float64, _u8p: np.uint8}
@@ -185,7 +185,7 @@ def make_desc(arrays):
     desc = MgrModelDesc()
     keep = []
     for name, typ in DESC_FIELDS:
-        v = arrays[name]
+        v = arrays[name] if name != "spherical_symmetry" else int(arrays.get(name, 0))
         if typ in _PTR_TYPES:
             a = np.ascontiguousarray(v, dtype=_PTR_TYPES[typ])
             keep.append(a)

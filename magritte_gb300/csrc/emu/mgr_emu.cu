@@ -20,12 +20,37 @@ using namespace mgr;
 namespace {
 
 // Sequential restatement of trace_half (same arithmetic, neighbour order, strict <).
-int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem h, int frame = 0) {
+int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int frame = 0) {
     const double* d = m.raydir + 3 * r;
     const double4_32a po = m.pos[o];
     double Z = 0.0;
     uint32_t crt = o;
     int count = 0;
+    if (m.sph) {
+        // trace_half_sph
+        const double Rcos = dot3_rn(po.x, po.y, po.z, d[0], d[1], d[2]);
+        const double Rsin2 = dsub_rn(sqnorm_rn(po), dmul_rn(Rcos, Rcos));
+        h.shift0 = origin_shift(m, frame, o, r);
+        h.dsh0 = (float)dsub_rn(h.shift0, 1.0);
+        while (true) {
+            uint32_t nxt;
+            double dZl;
+            if (!next_point_sph(m, Rcos, Rsin2, crt, Z, nxt, dZl)) return count > 0 ? -1 : 0;
+            if ((uint32_t)count >= cap) return -1;
+            Z = dadd_rn(Z, dZl);
+            h.ids[count] = nxt;
+            h.eid[count] = sph_eid(crt, nxt);
+            h.dZ[count] = dZl;
+            const double s = shift_sph(m, frame, o, r, nxt, Z);
+            h.shift[count] = s;
+            h.dsh[count] = (float)dsub_rn(s, 1.0);
+            h.dzs[count] = (float)dZl * m.dz_scale;
+            count++;
+            if (m.p2b[nxt] != m.P) break;
+            crt = nxt;
+        }
+        return count;
+    }
     while (true) {
         const uint32_t nnb = m.n_nb[crt];
         const uint32_t cum = m.cum_nb[crt];
@@ -140,6 +165,7 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     m.max_dist_f = (float)m.max_dist;
     m.log_max_interp_diff = logf((float)d->max_interpolation_diff);
     m.approx = d->approx;
+    m.sph = d->spherical_symmetry ? 1u : 0u;
     m.min_op_s = (float)(d->min_opacity * Ko);
     m.dz_scale = (float)(1.0 / Ko);
     m.s_scale = (float)(Ko / Ke);
@@ -185,6 +211,24 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
             x.nint_all[e] = (uint16_t)(v > 0xffffu ? 0xffffu : v);
         }
     m.nint_all = x.nint_all.data();
+    if (m.sph) {
+        // three slots per point (sph_eid): p -> p, p -> p - 1, p -> p + 1
+        x.nint.assign(3 * (size_t)P * L, 1);
+        x.nint_all.assign(3 * (size_t)P, 1);
+        for (uint32_t p = 0; p < P; p++)
+            for (uint32_t k = 0; k < 3; k++) {
+                const uint32_t nxt = sph_slot_point(p, k);
+                if (nxt >= P) continue;
+                for (uint32_t l = 0; l < L; l++) {
+                    const uint32_t v = n_interp_for_line(m, l, p, nxt);
+                    x.nint[(3 * (size_t)p + k) * L + l] = (uint16_t)(v > 0xffffu ? 0xffffu : v);
+                }
+                const uint32_t v = n_interp_all_lines(m, p, nxt);
+                x.nint_all[3 * (size_t)p + k] = (uint16_t)(v > 0xffffu ? 0xffffu : v);
+            }
+        m.nint = x.nint.data();
+        m.nint_all = x.nint_all.data();
+    }
 }
 
 struct HalfBuf {
@@ -430,8 +474,8 @@ extern "C" int mgr_emu_image(const MgrModelDesc* d, int precision, uint32_t rr, 
             const uint32_t o = (uint32_t)oo;
             const double* dd = m.raydir + 3 * rr;
             const uint32_t ar = m.antipod[rr];
-            const double shb = shift_rest(m, rr, o, dd);
-            const double shf = shift_rest(m, ar, o, m.raydir + 3 * ar);
+            const double shb = origin_shift(m, 1, o, rr);
+            const double shf = origin_shift(m, 1, o, ar);
             bk.shift0 = shb;
             fw.shift0 = shf;
             bk.dsh0 = (float)(shb - 1.0);
@@ -469,8 +513,8 @@ extern "C" int mgr_emu_image_for_point(const MgrModelDesc* d, int precision, uin
     HalfBuf b(kCap), fbuf(kCap);
     HalfSmem bk = b.view(), fw = fbuf.view();
     const uint32_t ar = m.antipod[rr];
-    const double shb = shift_rest(m, rr, p, m.raydir + 3 * rr);
-    const double shf = shift_rest(m, ar, p, m.raydir + 3 * ar);
+    const double shb = origin_shift(m, 1, p, rr);
+    const double shf = origin_shift(m, 1, p, ar);
     bk.shift0 = shb;
     fw.shift0 = shf;
     bk.dsh0 = (float)(shb - 1.0);
@@ -511,11 +555,12 @@ extern "C" int mgr_emu_lane(const MgrModelDesc* d, int precision, uint32_t o, ui
     build_emu_model(d, x);
     const DevModel& m = x.m;
     HalfBuf b(kCap), fbuf(kCap);
-    const int nb = trace_half_host(m, o, rr, kCap, b.view());
-    const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fbuf.view());
+    HalfSmem bk = b.view(), fw = fbuf.view();
+    const int nb = trace_half_host(m, o, rr, kCap, bk);
+    const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
     if (nb < 0 || nf < 0) return MGR_ERR_TRACE;
     const LaneCtx c = lane_ctx(m, o, f);
-    const LaneResult r = solve(m, precision, c, b.view(), nb, fbuf.view(), nf);
+    const LaneResult r = solve(m, precision, c, bk, nb, fw, nf);
     out[0] = r.u;
     out[1] = r.Ldiag;
     out[2] = r.solved ? 1.0 : 0.0;

@@ -402,6 +402,7 @@ uint64_t Model::signature() const {
     mix(radiation.frequencies.nu.version);
     mix(dshift_max.version);
     mix((uint64_t)parameters.approx());
+    mix((uint64_t)parameters.spherical_symmetry_);
     double knobs[4] = {parameters.min_opacity, parameters.min_dtau, parameters.max_interpolation_diff,
                        parameters.max_distance_opacity_contribution};
     for (double k : knobs) {
@@ -462,6 +463,7 @@ void Model::fill_desc(MgrModelDesc& d) {
     d.max_interpolation_diff = parameters.max_interpolation_diff;
     d.max_distance_opacity_contribution = parameters.max_distance_opacity_contribution;
     d.approx = parameters.approx();
+    d.spherical_symmetry = parameters.spherical_symmetry_ ? 1 : 0;
 }
 
 MgrModel* Model::device_model() {
@@ -785,6 +787,13 @@ int Model::image_old(Size ray_nr, bool tau) {
     im.ImY.resize({P});
     auto fn = tau ? mgr_image_optical_depth : mgr_image;
     check(fn(dev, parameters.precision, ray_nr, im.I.data(), im.ImX.data(), im.ImY.data()));
+    if (parameters.dimension_.v == 1) {
+        // Image::set_coordinates_all_model_points, 1D (image.cpp:160-171)
+        for (Size p = 0; p < P; p++) {
+            im.ImX[p] = geometry.points.position.data()[3 * (size_t)p];
+            im.ImY[p] = 0.0;
+        }
+    }
     images.push_back(std::move(im));
     return 0;
 }

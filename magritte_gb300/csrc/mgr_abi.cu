@@ -257,7 +257,10 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.max_dist_f = (float)dm.max_dist;
     dm.log_max_interp_diff = logf((float)d->max_interpolation_diff);
     dm.approx = d->approx;
+    dm.sph = d->spherical_symmetry ? 1u : 0u;
     m->n_edges = E;
+    // interpolation-table slots: one per CSR edge, or three per point in spherical symmetry
+    const size_t ET = dm.sph ? 3 * (size_t)P : E;
 
     // host-side derived tables
     std::vector<double4_32a> pos4(P), vel4(P), edge(E ? E : 1);
@@ -316,8 +319,8 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = dalloc(m, &m->op_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->iw_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->Sp_f, PL)) != cudaSuccess) break;
-        if ((e = dalloc(m, &m->nint, (E ? E : 1) * (size_t)L)) != cudaSuccess) break;
-        if ((e = dalloc(m, &m->nint_all, E ? E : 1)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->nint, (ET ? ET : 1) * (size_t)L)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->nint_all, ET ? ET : 1)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->em, d->emissivity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->op, d->opacity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->iw, d->inverse_width, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;

@@ -103,6 +103,7 @@ struct DevModel {
     float dz_scale;              // 1 / Ko  (true optical depth = chi_f * dz * dz_scale)
     float s_scale;               // Ko / Ke (true source = scaled source * s_scale)
     int approx;
+    uint32_t sph;                // 1D spherical symmetry (Parameters::spherical_symmetry)
 };
 
 // ---------------------------------------------------------------------------------
@@ -128,6 +129,21 @@ MGR_HD double dmul_rn(double a, double b) {
     return __dmul_rn(a, b);
 #else
     return a * b;
+#endif
+}
+
+MGR_HD double ddiv_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __ddiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+MGR_HD double dsqrt_rn(double a) {
+#ifdef __CUDA_ARCH__
+    return __dsqrt_rn(a);
+#else
+    return std::sqrt(a);
 #endif
 }
 
@@ -160,6 +176,76 @@ MGR_HD double shift_rest(const DevModel& m, uint32_t r, uint32_t c, const double
     double s = dadd_rn(1.0, dot3_rn(vc.x, vc.y, vc.z, d[0], d[1], d[2]));
     if (r >= m.hnrays) s = dsub_rn(2.0, s);
     return s;
+}
+
+// ---------------------------------------------------------------------------------
+// 1D spherical symmetry (Parameters::spherical_symmetry): points are shells on the x
+// axis in ascending radius, rays lie in the x-y plane.
+// ---------------------------------------------------------------------------------
+MGR_HD double sqnorm_rn(const double4_32a& a) { return dot3_rn(a.x, a.y, a.z, a.x, a.y, a.z); }
+
+// Geometry::get_shift_spherical_symmetry<CoMoving|Rest> (geometry.tpp:378-417) of point c
+// at distance Z along ray r from origin o, reversed for r >= hnrays in the rest frame
+// (geometry.tpp:428-465).  frame: 0 CoMoving, 1 Rest.
+MGR_HD double shift_sph(const DevModel& m, int frame, uint32_t o, uint32_t r, uint32_t c, double Z) {
+    const double* d = m.raydir + 3 * r;
+    const double4_32a po = m.pos[o];
+    const double xc = m.pos[c].x;
+    double s;
+    if (frame == 0) {
+        if (sqnorm_rn(po) == 0.0) return 1.0;
+        const double4_32a vo = m.vel[o];
+        const double vd = dot3_rn(vo.x, vo.y, vo.z, d[0], d[1], d[2]);
+        if (xc == 0.0) return dsub_rn(1.0, vd);
+        const double RcZ = dadd_rn(dot3_rn(po.x, po.y, po.z, d[0], d[1], d[2]), Z);
+        s = dadd_rn(1.0, dsub_rn(ddiv_rn(dmul_rn(m.vel[c].x, RcZ), xc), vd));
+    } else {
+        if (xc == 0.0) {
+            s = 1.0;
+        } else {
+            const double RcZ = dadd_rn(dot3_rn(po.x, po.y, po.z, d[0], d[1], d[2]), Z);
+            s = dadd_rn(1.0, ddiv_rn(dmul_rn(m.vel[c].x, RcZ), xc));
+        }
+        if (r >= m.hnrays) s = dsub_rn(2.0, s);
+    }
+    return s;
+}
+
+// Geometry::get_shift<frame>(o, r, o, 0.0): the origin's shift as a half's trace starts
+// from it (solver.tpp:751; exactly 1 comoving in general geometry).
+MGR_HD double origin_shift(const DevModel& m, int frame, uint32_t o, uint32_t r) {
+    if (m.sph) return shift_sph(m, frame, o, r, o, 0.0);
+    return frame ? shift_rest(m, r, o, m.raydir + 3 * r) : 1.0;
+}
+
+// Interpolation-table slot of a spherical step crt -> nxt: three per point (the tangent
+// crossing back to the same shell, the next shell inward, the next shell outward).
+MGR_HD uint32_t sph_eid(uint32_t crt, uint32_t nxt) { return 3u * crt + (nxt == crt ? 0u : (nxt < crt ? 1u : 2u)); }
+MGR_HD uint32_t sph_slot_point(uint32_t p, uint32_t k) { return k == 0 ? p : (k == 1 ? p - 1u : p + 1u); }
+
+// Geometry::get_next_spherical_symmetry (geometry.tpp:118-159) for a ray with
+// Rcos = origin . raydir and Rsin2 = |origin|^2 - Rcos^2: inward (Z < -Rcos) to the next
+// smaller shell the ray meets, or across the tangent point back to the same shell; then
+// outward.  Returns false when the ray leaves the grid (point 0 inward, the last point
+// outward).
+MGR_HD bool next_point_sph(const DevModel& m, double Rcos, double Rsin2, uint32_t c, double Z, uint32_t& nxt,
+                           double& dZ) {
+    const double Rcos_plus_Z = dadd_rn(Rcos, Z);
+    if (Z < -Rcos) {
+        if (c == 0) return false;
+        if (sqnorm_rn(m.pos[c - 1]) >= Rsin2) {
+            nxt = c - 1;
+            dZ = dsub_rn(-dsqrt_rn(dsub_rn(sqnorm_rn(m.pos[nxt]), Rsin2)), Rcos_plus_Z);
+        } else {
+            nxt = c;
+            dZ = dmul_rn(-2.0, Rcos_plus_Z);
+        }
+    } else {
+        if (c >= m.P - 1) return false;
+        nxt = c + 1;
+        dZ = dsub_rn(dsqrt_rn(dsub_rn(sqnorm_rn(m.pos[nxt]), Rsin2)), Rcos_plus_Z);
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------------------------

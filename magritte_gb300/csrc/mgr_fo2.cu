@@ -53,10 +53,24 @@ __global__ void size_rays_kernel(DevModel m, uint32_t* d_max, int* status) {
 // InterpHelper::get_n_interp_for_line (solver_interp_helper.tpp:55-75), evaluated
 // once per edge instead of once per step, lane and frequency.
 // ---------------------------------------------------------------------------------
+// Spherical models (trace_half_sph) index the tables by sph_eid instead: three slots per
+// point for the steps p -> p, p -> p - 1 and p -> p + 1.
 __global__ void nint_table_kernel(DevModel m, uint16_t* __restrict__ nint, int* status) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (uint64_t)m.P * m.L;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t p = (uint32_t)(i / m.L), l = (uint32_t)(i % m.L);
+        if (m.sph) {
+            for (uint32_t k = 0; k < 3; k++) {
+                const uint32_t nxt = sph_slot_point(p, k);
+                uint32_t v = (nxt < m.P) ? n_interp_for_line(m, l, p, nxt) : 1u;
+                if (v > 0xffffu) {
+                    atomicOr(status, ST_CAPACITY);
+                    v = 0xffffu;
+                }
+                nint[(size_t)(3u * p + k) * m.L + l] = (uint16_t)v;
+            }
+            continue;
+        }
         const uint32_t cum = m.cum_nb[p], n = m.n_nb[p];
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t nxt = (uint32_t)__double_as_longlong(m.edge[cum + k].w);
@@ -74,6 +88,18 @@ __global__ void nint_table_kernel(DevModel m, uint16_t* __restrict__ nint, int* 
 // for the imagers' Solver::set_data.
 __global__ void nint_all_kernel(DevModel m, uint16_t* __restrict__ nint_all, int* status) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < m.P; p += gridDim.x * blockDim.x) {
+        if (m.sph) {
+            for (uint32_t k = 0; k < 3; k++) {
+                const uint32_t nxt = sph_slot_point(p, k);
+                uint32_t v = (nxt < m.P) ? n_interp_all_lines(m, p, nxt) : 1u;
+                if (v > 0xffffu) {
+                    atomicOr(status, ST_CAPACITY);
+                    v = 0xffffu;
+                }
+                nint_all[3u * p + k] = (uint16_t)v;
+            }
+            continue;
+        }
         const uint32_t cum = m.cum_nb[p], n = m.n_nb[p];
         for (uint32_t k = 0; k < n; k++) {
             const uint32_t nxt = (uint32_t)__double_as_longlong(m.edge[cum + k].w);

@@ -36,8 +36,8 @@ __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, ui
     for (uint32_t o = blockIdx.x * nw + w; o < m.P; o += gridDim.x * nw) {
         // Geometry::get_shift<Rest, false>(o, r, o, 0): the origin's shift along each
         // half's own ray (the antipode's is reversed), the element's that of rr
-        const double shb = shift_rest(m, rr, o, d);
-        const double shf = shift_rest(m, ar, o, m.raydir + 3 * ar);
+        const double shb = origin_shift(m, 1, o, rr);
+        const double shf = origin_shift(m, 1, o, ar);
         bk.shift0 = shb;
         fw.shift0 = shf;
         bk.dsh0 = (float)dsub_rn(shb, 1.0);
@@ -179,6 +179,11 @@ int image_plane_setup(MgrModel* model, const char* who, const double* raydir, ui
         set_error(std::string(who) + ": One line approximation is not supported for imaging.");
         return MGR_ERR_UNSUPPORTED;
     }
+    if (model->dm.sph) {
+        set_error(std::string(who) + ": the projection-plane imager is not available for spherically symmetric "
+                                     "models (use mgr_image).");
+        return MGR_ERR_UNSUPPORTED;
+    }
     std::string err;
     const int rc = image_plane_compute(model->host_pos.data(), model->host_p2b.data(), model->dm.P, model->dm.B,
                                        raydir, nx, ny, ip, hx, hy, err);
@@ -241,7 +246,13 @@ static int image_old_impl(MgrModel* model, int precision, uint32_t ray_nr, doubl
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     cudaFree(dI);
     if (e != cudaSuccess) return cuda_fail(e, who.c_str());
-    if (ImX && ImY) {
+    if (ImX && ImY && model->dm.sph) {
+        // Image::set_coordinates_all_model_points, 1D (image.cpp:160-171)
+        for (uint32_t p = 0; p < dm.P; p++) {
+            ImX[p] = model->host_pos[3 * (size_t)p];
+            ImY[p] = 0.0;
+        }
+    } else if (ImX && ImY) {
         const double* d = model->host_raydir.data() + 3 * (size_t)ray_nr;
         double ix, iy, jx, jy, jz;
         bool tilted;
@@ -344,8 +355,8 @@ __global__ void __launch_bounds__(32) image_point_kernel(DevModel m, uint32_t ca
     for (uint32_t i = lane; i < m.L; i += 32) sl[i] = m.sorted_line[i];
     __syncwarp();
     const uint32_t ar = m.antipod[rr];
-    const double shb = shift_rest(m, rr, p, m.raydir + 3 * rr);
-    const double shf = shift_rest(m, ar, p, m.raydir + 3 * ar);
+    const double shb = origin_shift(m, 1, p, rr);
+    const double shf = origin_shift(m, 1, p, ar);
     bk.shift0 = shb;
     fw.shift0 = shf;
     bk.dsh0 = (float)dsub_rn(shb, 1.0);
@@ -454,7 +465,8 @@ static int image_for_point_impl(MgrModel* model, int precision, uint32_t ray_nr,
 // solver.tpp:2953-2991): column[r][o] = sum over the ray's steps of
 // (density[crt] + density[nxt]) / 2 * dZ, from o along r to the boundary, for every ray
 // pair rr < hnrays and its antipode.  Warp per (ray, point) walk with the solves'
-// next-point argmin; the sum in FP64 with the reference's roundings.
+// next-point argmin (shell steps in spherical symmetry); the sum in FP64 with the
+// reference's roundings.
 // ---------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) column_kernel(DevModel m, const double* __restrict__ density,
                                                      double* __restrict__ column, int* status) {
@@ -468,17 +480,26 @@ __global__ void __launch_bounds__(256) column_kernel(DevModel m, const double* _
         const double* d = m.raydir + 3 * r;
         const double dx = d[0], dy = d[1], dz = d[2];
         const double4_32a po = m.pos[o];
+        const double Rcos = dot3_rn(po.x, po.y, po.z, dx, dy, dz);
+        const double Rsin2 = dsub_rn(sqnorm_rn(po), dmul_rn(Rcos, Rcos));
         double Z = 0.0, col = 0.0;
         uint32_t crt = o;
         int steps = 0;
         while (true) {
             uint32_t nxt, eid;
-            double bestZ;
-            if (!warp_next_point(m, po, dx, dy, dz, crt, Z, lane, nxt, bestZ, eid)) {
+            double dZl;
+            bool ok;
+            if (m.sph) {
+                ok = next_point_sph(m, Rcos, Rsin2, crt, Z, nxt, dZl);
+            } else {
+                double bestZ;
+                ok = warp_next_point(m, po, dx, dy, dz, crt, Z, lane, nxt, bestZ, eid);
+                dZl = dsub_rn(bestZ, Z);
+            }
+            if (!ok) {
                 if (steps > 0 && lane == 0) atomicOr(status, ST_TRACE);
                 break;
             }
-            const double dZl = dsub_rn(bestZ, Z);
             Z = dadd_rn(Z, dZl);
             col = dadd_rn(col, dmul_rn(dmul_rn(0.5, dadd_rn(density[crt], density[nxt])), dZl));
             steps++;

@@ -121,16 +121,67 @@ __device__ __forceinline__ bool warp_next_point(const DevModel& m, const double4
     return true;
 }
 
+// The walk of trace_half in 1D spherical symmetry (Geometry::get_next_spherical_symmetry,
+// geometry.tpp:118-159): every lane steps the same shells; lane 0 stores the steps, with
+// each step's shift at its distance along the ray (get_shift_spherical_symmetry) and the
+// half's origin shift (shift0, not 1 in the comoving frame there).
+template <bool STORE, int FRAME>
+__device__ int trace_half_sph(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int lane,
+                              int* status) {
+    const double* d = m.raydir + 3 * r;
+    const double4_32a po = m.pos[o];
+    const double Rcos = dot3_rn(po.x, po.y, po.z, d[0], d[1], d[2]);
+    const double Rsin2 = dsub_rn(sqnorm_rn(po), dmul_rn(Rcos, Rcos));
+    if (STORE) {
+        h.shift0 = origin_shift(m, FRAME, o, r);
+        h.dsh0 = (float)dsub_rn(h.shift0, 1.0);
+    }
+    double Z = 0.0;
+    uint32_t crt = o;
+    int count = 0;
+    while (true) {
+        uint32_t nxt;
+        double dZl;
+        if (!next_point_sph(m, Rcos, Rsin2, crt, Z, nxt, dZl)) {
+            if (count > 0 && lane == 0) atomicOr(status, ST_TRACE);
+            if (count > 0) count = -1;
+            break;
+        }
+        if (STORE && (uint32_t)count >= cap) {
+            if (lane == 0) atomicOr(status, ST_CAPACITY);
+            count = -1;
+            break;
+        }
+        Z = dadd_rn(Z, dZl);
+        if (STORE && lane == 0) {
+            h.ids[count] = nxt;
+            h.eid[count] = sph_eid(crt, nxt);
+            h.dZ[count] = dZl;
+            const double sh = shift_sph(m, FRAME, o, r, nxt, Z);
+            h.shift[count] = sh;
+            h.dsh[count] = (float)dsub_rn(sh, 1.0);
+            h.dzs[count] = (float)dZl * m.dz_scale;
+        }
+        count++;
+        if (m.p2b[nxt] != m.P) break;
+        crt = nxt;
+    }
+    __syncwarp();
+    return count;
+}
+
 // Warp-cooperative Geometry::get_next_general_geometry<Defaulttracer> walk
 // (geometry.tpp:13-44) from origin o along ray r until a boundary point is met
 // (warp_next_point per step).  Returns the number of steps, or -1 on capacity
-// overflow / invalid geometry (status bits set).
+// overflow / invalid geometry (status bits set).  Spherical models walk shells
+// (trace_half_sph).
 // FRAME 0: comoving shifts relative to the origin point (the formal solves);
 // FRAME 1: rest-frame shifts of the old imager (Geometry::get_shift<Rest>, reversed for
 // r >= hnrays, geometry.tpp:428-465).
 template <bool STORE, int FRAME = 0>
-__device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem h, int lane,
+__device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int lane,
                           int* status) {
+    if (m.sph) return trace_half_sph<STORE, FRAME>(m, o, r, cap, h, lane, status);
     const double* d = m.raydir + 3 * r;
     const double dx = d[0], dy = d[1], dz = d[2];
     const double4_32a po = m.pos[o];

@@ -378,6 +378,93 @@ def single_ray_1d(npoints: int = 50, dx: float = 1.0e12, nTT: float = 1.0e3, nH2
         linedata=[lamda_test_species()], quad_roots=[roots], quad_weights=[wts], nquads=nquads)
 
 
+def rays_spherical_symmetry(nrays: int):
+    """Ray directions and weights of a 1D spherically symmetric model, uniform variant of
+    setup.set_rays_spherical_symmetry (magritte/setup.py:226-330): nrays/2 directions in
+    the upper x-y half plane from +x to +y at equal angles, each weighted by the cosine
+    difference of the half-way directions to its neighbours (the integral of sin theta
+    over its sector), then their antipodes with the same weights; weights normalised."""
+    h = nrays // 2
+    nextra = h - 1
+    Rx, Ry = [1.0], [0.0]
+    step = 0.5 * np.pi / nextra
+    for k in range(1, nextra):
+        Rx.append(np.cos(k * step))
+        Ry.append(np.sin(k * step))
+    Rx.append(0.0)
+    Ry.append(1.0)
+    Wt = []
+    for n in range(h):
+        if n == 0:
+            ux, uy = 0.5 * (Rx[n] + Rx[n + 1]), 0.5 * (Ry[n] + Ry[n + 1])
+            lx, ly = Rx[0], Ry[0]
+        elif n == h - 1:
+            ux, uy = Rx[-1], Ry[-1]
+            lx, ly = 0.5 * (Rx[n] + Rx[n - 1]), 0.5 * (Ry[n] + Ry[n - 1])
+        else:
+            ux, uy = 0.5 * (Rx[n] + Rx[n + 1]), 0.5 * (Ry[n] + Ry[n + 1])
+            lx, ly = 0.5 * (Rx[n] + Rx[n - 1]), 0.5 * (Ry[n] + Ry[n - 1])
+        Wt.append(lx / np.sqrt(lx ** 2 + ly ** 2) - ux / np.sqrt(ux ** 2 + uy ** 2))
+    direction = np.array([[x, y, 0.0] for x, y in zip(Rx, Ry)] + [[-x, -y, -0.0] for x, y in zip(Rx, Ry)])
+    weight = np.array(Wt + Wt)
+    return direction, weight / weight.sum()
+
+
+def spherical_1d(name: str, radius: np.ndarray, v_radial: np.ndarray, abundance: np.ndarray,
+                 temperature: np.ndarray, vturb2: np.ndarray, nrays: int, nquads: int,
+                 linedata: List[Linedata]) -> RawModel:
+    """A 1D spherically symmetric model as the reference's 1D benchmarks build it: shells
+    at ``radius`` (ascending) on the x axis with radial velocities, 1D Delaunay
+    neighbours (magritte/setup.py:59-70), the innermost and outermost shells as CMB
+    boundaries (setup.py:392-396) and the uniform spherical-symmetry rays."""
+    P = len(radius)
+    position = np.stack([radius, np.zeros(P), np.zeros(P)], axis=1)
+    velocity = np.stack([v_radial, np.zeros(P), np.zeros(P)], axis=1)
+    nbs = [1]
+    n_nbs = [1]
+    for p in range(1, P - 1):
+        nbs.extend([p - 1, p + 1])
+        n_nbs.append(2)
+    nbs.append(P - 2)
+    n_nbs.append(1)
+    b2p = np.array([0, P - 1], dtype=np.uint32)
+    direction, weight = rays_spherical_symmetry(nrays)
+    roots, wts = quadrature(nquads)
+    return RawModel(
+        name=name, dimension=1, position=position, velocity=velocity,
+        neighbors=np.array(nbs, dtype=np.uint32), n_neighbors=np.array(n_nbs, dtype=np.uint32),
+        boundary2point=b2p, boundary_condition=np.full(2, BC_CMB, np.int32), boundary_temperature=np.full(2, T_CMB),
+        ray_direction=direction, ray_weight=weight, abundance=abundance, temperature=temperature, vturb2=vturb2,
+        linedata=linedata, quad_roots=[roots], quad_weights=[wts], nquads=nquads, spherical_symmetry=True)
+
+
+def density_distribution_1d(kind: str = "a", npoints: int = 200, nrays: int = 50, nquads: int = 50) -> RawModel:
+    """The reference's 1D density-distribution benchmark
+    (tests/benchmarks/analytic/density_distribution_1D.py:17-87): shells log-spaced over
+    1e13..7.8e16 m, n_H2 = 2e13 (r_in/r)^2 m^-3, X_mol 1e-8 (a) or 1e-6 (b), T = 20 K,
+    v_turb = 150 m/s, no velocity, the 2-level 'test' species."""
+    r_in, r_out, nH2_in = 1.0e13, 7.8e16, 2.0e13
+    X_mol = {"a": 1.0e-8, "b": 1.0e-6}[kind]
+    rs = np.logspace(np.log10(r_in), np.log10(r_out), npoints, endpoint=True)
+    nH2 = nH2_in * (r_in / rs) ** 2
+    abund = np.stack([X_mol * nH2, nH2, np.zeros(npoints)], axis=1)
+    return spherical_1d(f"density_distribution_VZ{kind}_1D", rs, np.zeros(npoints), abund,
+                        np.full(npoints, 20.0), np.full(npoints, (150.0 / CC) ** 2), nrays, nquads,
+                        [lamda_test_species()])
+
+
+def velocity_gradient_1d(npoints: int = 100, nrays: int = 100, nquads: int = 100) -> RawModel:
+    """The reference's 1D constant-velocity-gradient benchmark
+    (tests/benchmarks/analytic/constant_velocity_gradient_1D.py:14-73): shells at
+    (i+1) 1e4 m moving outward at (i+1) 250 m/s, n_TT = 1e8, n_H2 = 1e12 m^-3, T = 45 K,
+    no turbulence, the 2-level 'test' species."""
+    dx, dv = 1.0e4, 2.5e2 / CC
+    i = np.arange(npoints, dtype=np.float64)
+    abund = np.tile(np.array([1.0e8, 1.0e12, 0.0]), (npoints, 1))
+    return spherical_1d("constant_velocity_gradient_1D", (i + 1.0) * dx, (i + 1.0) * dv, abund,
+                        np.full(npoints, 45.0), np.zeros(npoints), nrays, nquads, [lamda_test_species()])
+
+
 def delaunay_neighbors(position: np.ndarray):
     """Neighbour CSR lists from a Delaunay triangulation of the points, as
     ``set_Delaunay_neighbor_lists`` builds them in 3D (magritte/setup.py:82-93)."""

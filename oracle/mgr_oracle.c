@@ -81,9 +81,50 @@ static inline double dot3(double ax, double ay, double az, const double* b) {
     return ax * b[0] + ay * b[1] + az * b[2];
 }
 
+/* Vector3D::squaredNorm, summed x, y, z left to right. */
+static inline double sqnorm(const double* a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
+
+/* Geometry::get_next_spherical_symmetry (geometry.tpp:118-159): points are shells on the
+ * x axis in ascending radius; inward (before the tangent point) to the next smaller shell
+ * the ray meets, or across the tangent point back to the same shell; then outward. */
+static uint32_t get_next_spherical(const OrcModel* m, const double* origin, const double* raydir, uint32_t c,
+                                   double* Z, double* dZ) {
+    uint32_t next;
+    const double Rcos        = dot3(origin[0], origin[1], origin[2], raydir);
+    const double R2          = sqnorm(origin);
+    const double Rsin2       = R2 - Rcos * Rcos;
+    const double Rcos_plus_Z = Rcos + *Z;
+    if (*Z < -Rcos) {
+        if (c == 0) return m->npoints;
+        if (sqnorm(m->position + 3 * (c - 1)) >= Rsin2) {
+            next = c - 1;
+            *dZ  = -sqrt(sqnorm(m->position + 3 * next) - Rsin2) - Rcos_plus_Z;
+        } else {
+            next = c;
+            *dZ  = -2.0 * Rcos_plus_Z;
+        }
+    } else {
+        if (c >= m->npoints - 1) return m->npoints;
+        next = c + 1;
+        *dZ  = +sqrt(sqnorm(m->position + 3 * next) - Rsin2) - Rcos_plus_Z;
+    }
+    *Z += *dZ;
+    return next;
+}
+
+static uint32_t get_next_general(const OrcModel* m, const double* origin, const double* raydir, uint32_t c,
+                                 double* Z, double* dZ);
+
+/* Geometry::get_next (geometry.tpp:246-258): spherical symmetry or general geometry. */
+static uint32_t get_next(const OrcModel* m, const double* origin, const double* raydir, uint32_t c, double* Z,
+                         double* dZ) {
+    return m->spherical_symmetry ? get_next_spherical(m, origin, raydir, c, Z, dZ)
+                                 : get_next_general(m, origin, raydir, c, Z, dZ);
+}
+
 /* Geometry::get_next_general_geometry<Defaulttracer> (geometry.tpp:13-44). */
-static uint32_t get_next(const OrcModel* m, const double* origin, const double* raydir,
-                         uint32_t c, double* Z, double* dZ) {
+static uint32_t get_next_general(const OrcModel* m, const double* origin, const double* raydir,
+                                 uint32_t c, double* Z, double* dZ) {
     const uint32_t n_nbs     = m->n_neighbors[c];
     const uint32_t cum_n_nbs = m->cum_n_neighbors[c];
     double dmin              = DBL_MAX;
@@ -108,11 +149,33 @@ static uint32_t get_next(const OrcModel* m, const double* origin, const double* 
     return next;
 }
 
-/* Geometry::get_shift_general_geometry<CoMoving|Rest> (geometry.tpp:203-221) and the
+/* Geometry::get_shift_general_geometry<CoMoving|Rest> (geometry.tpp:203-221), the
+ * spherical-symmetry shifts at distance Z along the ray (geometry.tpp:378-417) and the
  * reversal for the old imager (geometry.tpp:428-465).  frame: 0 CoMoving, 1 Rest. */
-static inline double get_shift(const OrcModel* m, int frame, uint32_t o, uint32_t r, uint32_t c) {
+static inline double get_shift(const OrcModel* m, int frame, uint32_t o, uint32_t r, uint32_t c, double Z) {
     const double* d = m->ray_direction + 3 * r;
     double shift;
+    if (m->spherical_symmetry) {
+        const double* org = m->position + 3 * o;
+        const double* vo  = m->velocity + 3 * o;
+        const double xc   = m->position[3 * c];
+        if (frame == 0) {
+            if (sqnorm(org) == 0.0) shift = 1.0;
+            else if (xc == 0.0) shift = 1.0 - dot3(vo[0], vo[1], vo[2], d);
+            else {
+                const double Rcos_plus_Z = dot3(org[0], org[1], org[2], d) + Z;
+                shift = 1.0 + (m->velocity[3 * c] * Rcos_plus_Z / xc - dot3(vo[0], vo[1], vo[2], d));
+            }
+        } else {
+            if (xc == 0.0) shift = 1.0;
+            else {
+                const double Rcos_plus_Z = dot3(org[0], org[1], org[2], d) + Z;
+                shift = 1.0 + m->velocity[3 * c] * Rcos_plus_Z / xc;
+            }
+            if (r >= m->hnrays) shift = 2.0 - shift;
+        }
+        return shift;
+    }
     if (frame == 0) {
         const double vx = m->velocity[3 * c + 0] - m->velocity[3 * o + 0];
         const double vy = m->velocity[3 * c + 1] - m->velocity[3 * o + 1];
@@ -229,8 +292,8 @@ static int64_t trace(const OrcModel* m, Buf* b, int frame, uint32_t line, uint32
     uint32_t nxt           = get_next(m, origin, raydir, o, &Z, &dZ);
     if (valid_point(m, nxt)) {
         uint32_t crt     = o;
-        double shift_crt = get_shift(m, frame, o, r, crt);
-        double shift_nxt = get_shift(m, frame, o, r, nxt);
+        double shift_crt = get_shift(m, frame, o, r, crt, 0.0);
+        double shift_nxt = get_shift(m, frame, o, r, nxt, Z);
         set_data(m, b, line, crt, nxt, shift_crt, shift_nxt, dZ, increment, &id1, &id2, err);
         while (!*err && not_on_boundary(m, nxt)) {
             crt       = nxt;
@@ -240,7 +303,7 @@ static int64_t trace(const OrcModel* m, Buf* b, int frame, uint32_t line, uint32
                 *err = 2;
                 break;
             }
-            shift_nxt = get_shift(m, frame, o, r, nxt);
+            shift_nxt = get_shift(m, frame, o, r, nxt, Z);
             set_data(m, b, line, crt, nxt, shift_crt, shift_nxt, dZ, increment, &id1, &id2, err);
         }
     }
@@ -1013,7 +1076,7 @@ static int image_fo2_impl(const OrcModel* m, uint32_t rr, double* I, int nthread
             const uint32_t c = b.centre;
             int err          = 0;
             b.nr[c]          = o;
-            b.shift[c]       = get_shift(m, 1, o, rr, o);
+            b.shift[c]       = get_shift(m, 1, o, rr, o, 0.0);
             const int64_t first = trace(m, &b, 1, UINT32_MAX, o, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
             const int64_t last  = trace(m, &b, 1, UINT32_MAX, o, ar, +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
             if (err) {
@@ -1125,7 +1188,7 @@ int orc_image_for_point(const OrcModel* m, uint32_t rr, uint32_t p, uint32_t* n_
     const uint32_t ar = m->antipod[rr];
     int err           = 0;
     b.nr[c]           = p;
-    b.shift[c]        = get_shift(m, 1, p, rr, p);
+    b.shift[c]        = get_shift(m, 1, p, rr, p, 0.0);
     const int64_t first = trace(m, &b, 1, UINT32_MAX, p, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
     const int64_t last  = trace(m, &b, 1, UINT32_MAX, p, ar, +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
     if (err) {
@@ -1282,6 +1345,7 @@ static int image_new_impl(const OrcModel* m, const double* raydir_in, uint32_t n
     const uint32_t P = m->npoints, F = m->nfreqs;
     const double n2 = raydir_in[0] * raydir_in[0] + raydir_in[1] * raydir_in[1] + raydir_in[2] * raydir_in[2];
     if (n2 == 0.0) return -1;
+    if (m->spherical_symmetry) return -4; /* the 1D projection-plane imager is not restated */
     const double inv = 1 / sqrt(n2);
     const double d[3] = {raydir_in[0] * inv, raydir_in[1] * inv, raydir_in[2] * inv};
     /* Image::set_coordinates_projection_surface (image.cpp:221-366), 3D */

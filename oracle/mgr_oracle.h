@@ -72,6 +72,7 @@ typedef struct {
     double max_interpolation_diff;
     double max_distance_opacity_contribution;
     int    approx;
+    int    spherical_symmetry;            /* 1D spherical symmetry: points on the x axis by radius */
 } OrcModel;
 
 /* One ray pair as the reference lays it out in its per-thread buffers

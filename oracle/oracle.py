@@ -178,7 +178,8 @@ def reference_setup(raw, approx="CloseLines", max_width_fraction=0.35, min_opaci
         quad_roots=np.ascontiguousarray(np.stack(raw.quad_roots), np.float64),
         min_opacity=min_opacity, min_dtau=min_dtau, max_interpolation_diff=max_interpolation_diff,
         max_distance_opacity_contribution=max_distance_opacity_contribution,
-        approx=APPROX[approx], populations=pops,
+        approx=APPROX[approx], spherical_symmetry=int(bool(getattr(raw, "spherical_symmetry", False))),
+        populations=pops,
     )
 
 
@@ -203,7 +204,7 @@ _FIELDS = [
     ("in_line_integral", _u8p), ("nrad", _u32p), ("nrad_cum", _u32p), ("line_A", _f64p),
     ("lspec_inverse_mass", _f64p), ("quad_weights", _f64p), ("quad_roots", _f64p),
     ("min_opacity", C.c_double), ("min_dtau", C.c_double), ("max_interpolation_diff", C.c_double),
-    ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int),
+    ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int), ("spherical_symmetry", C.c_int),
 ]
 
 
@@ -260,7 +261,7 @@ class Oracle:
         self.a = arrays
         self.m = OrcModel()
         for name, typ in _FIELDS:
-            v = arrays[name]
+            v = arrays[name] if name != "spherical_symmetry" else int(arrays.get(name, 0))
             if typ in (_u32p, _i32p, _f64p, _u8p):
                 setattr(self.m, name, _ptr(v, typ))
             else:

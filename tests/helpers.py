@@ -87,3 +87,98 @@ def max_rel(a, b, floor=0.0):
     b = np.asarray(b, np.float64)
     den = np.maximum(np.abs(b), floor)
     return float(np.max(np.abs(a - b) / np.where(den > 0, den, 1.0)))
+
+
+def _line_constants(ld, temp, nTT, vturb2):
+    """LTE populations scaled by nTT and the first line's opacity, source and width
+    (magritte/tools.py:76-230)."""
+    pop = ld.weight * np.exp(-ld.energy / (KB * temp))
+    pop = pop / pop.sum() * nTT
+    i, j = ld.irad[0], ld.jrad[0]
+    frq = ld.frequency[0]
+    em = HH * frq / (4.0 * np.pi) * ld.A[0] * pop[i]
+    op = HH * frq / (4.0 * np.pi) * (ld.Ba[0] * pop[j] - ld.Bs[0] * pop[i])
+    dnu = frq * np.sqrt(2.0 * KB * temp / (AMU * CC**2) * ld.inverse_mass + vturb2)
+    return frq, op, em / op, dnu
+
+
+def density_distribution_1d_solution(raw, nu, angles, kind="a"):
+    """u [angle][point][freq] of tests/benchmarks/analytic/density_distribution_1D.py:126-178:
+    optical depths of the r^-2 opacity along a ray at angle theta from the radial
+    direction, to the inner core (theta < asin(r_in/r)) or to the outer edge."""
+    r_in, r_out, nH2_in = 1.0e13, 7.8e16, 2.0e13
+    X_mol = {"a": 1.0e-8, "b": 1.0e-6}[kind]
+    ld = raw.linedata[0]
+    frq, chi, src, dnu = _line_constants(ld, 20.0, X_mol * nH2_in, (150.0 / CC) ** 2)
+    rs = raw.position[:, 0]
+
+    def phi(f):
+        x = (f - frq) / dnu
+        return np.exp(-x**2) / (np.sqrt(np.pi) * dnu)
+
+    def tau(f, r, theta):
+        pref = chi * phi(f) * r_in**2
+        if theta == 0.0:
+            return pref * (1.0 / r_in - 1.0 / r)
+        if theta == np.pi:
+            return pref * (1.0 / r - 1.0 / r_out)
+        if theta < np.arcsin(r_in / r):
+            closest = r * np.sin(theta)
+            in_vertical = np.sqrt(r_in**2 - closest**2)
+            out_vertical = np.sqrt(r**2 - closest**2)
+            return pref * (np.arctan(out_vertical / closest) - np.arctan(in_vertical / closest)) / closest
+        factor = np.arccos(r * np.sin(theta) / r_out) + 0.5 * np.pi - theta
+        return pref / (r * np.sin(theta)) * factor
+
+    def I_(f, r, theta):
+        return src + (planck(S.T_CMB, f) - src) * np.exp(-tau(f, r, theta))
+
+    return np.array([[[0.5 * (I_(f, r, a) + I_(f, r, np.pi + a)) for f in nu] for r in rs] for a in angles])
+
+
+def velocity_gradient_1d_solution(raw, nu, angles):
+    """u [angle][point][freq] of tests/benchmarks/analytic/constant_velocity_gradient_1D.py:127-187:
+    the erf optical depth of a linear velocity field along the ray to the inner or outer
+    boundary, with the boundary's CMB seen at its Doppler-shifted frequency."""
+    from scipy.special import erf
+
+    npoints = raw.npoints
+    dx, dv = 1.0e4, 2.5e2 / CC
+    L, vmax = dx * npoints, dv * npoints
+    ld = raw.linedata[0]
+    frq, chi, src, dnu = _line_constants(ld, 45.0, 1.0e8, 0.0)
+    rs = raw.position[:, 0]
+    r_in, r_out = rs[0], rs[-1]
+
+    def v_(r):
+        return dv * (1 + (r - r_in) / dx)
+
+    def bdy(f, r, theta):
+        r_shift = np.cos(theta) * v_(r)
+        if theta < np.arcsin(r_in / r):
+            edge = np.sqrt(1 - ((r / r_in) * np.abs(np.sin(theta))) ** 2) * v_(r_in)
+        else:
+            edge = np.sqrt(1 - ((r / r_out) * np.abs(np.sin(theta))) ** 2) * v_(r_out)
+        return planck(S.T_CMB, f * (1.0 + (edge - r_shift)))
+
+    def z_max(r, theta):
+        if theta < np.arcsin(r_in / r):
+            return r * np.cos(theta) - np.sqrt(r_in**2 - (r * np.sin(theta)) ** 2)
+        return r * np.cos(theta) + np.sqrt(L**2 - (r * np.sin(theta)) ** 2)
+
+    def tau(f, r, theta):
+        l = float(z_max(r, theta))
+        arg = float((f - frq) / dnu)
+        fct = float(vmax * f / dnu)
+        return chi * L / (fct * dnu) * 0.5 * (erf(-arg) + erf(fct * l / L + arg))
+
+    def I_(f, r, theta):
+        return src + (bdy(f, r, theta) - src) * np.exp(-tau(f, r, theta))
+
+    return np.array([[[0.5 * (I_(f, r, a) + I_(f, r, np.pi + a)) for f in nu] for r in rs] for a in angles])
+
+
+def ray_angles(raw):
+    """The first hnrays rays' angles arctan2(y, x), as the 1D benchmarks take them."""
+    d = raw.ray_direction[: raw.nrays // 2]
+    return np.arctan2(d[:, 1], d[:, 0])

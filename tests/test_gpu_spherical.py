@@ -1,0 +1,149 @@
+"""1D spherical symmetry on the GPU (trace_half_sph: Geometry::get_next_spherical_symmetry,
+geometry.tpp:118-159, and get_shift_spherical_symmetry, :378-417).
+
+* Ray traces bit-exact against the oracle (shell sequence with the tangent crossing,
+  interpolation points, Z-dependent shifts, dZ).
+* J, u and the ALO diagonal of the Feautrier solve and the short-characteristics solve
+  within the formal solve's 1e-5 (FP64 and split precision) of the oracle.
+* The reference's analytic 1D benchmarks through the library: density_distribution_1D
+  (tests/benchmarks/analytic/density_distribution_1D.py:235-236, mean relative error of u
+  below 4.4e-4 Feautrier / 4.1e-4 short characteristics) and
+  constant_velocity_gradient_1D (constant_velocity_gradient_1D.py:245-253, three
+  max_width_fraction settings).
+* The old imager and compute_image's 1D image coordinates."""
+import numpy as np
+import pytest
+
+import helpers as H
+import oracle as O
+from magritte_gb300 import _abi
+from magritte_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_with_correctly_rounded_erf():
+    O.set_erf_mode(1)
+    yield
+    O.set_erf_mode(0)
+
+
+MODELS = {
+    "density": lambda: S.density_distribution_1d("a", npoints=80, nrays=20, nquads=11),
+    "velocity": lambda: S.velocity_gradient_1d(npoints=50, nrays=24, nquads=21),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MODELS))
+def test_spherical_traces_bit_exact(gpu_lib, name):
+    raw = MODELS[name]()
+    a = H.setup(raw)
+    orc = O.Oracle(a)
+    dev = _abi.DeviceModel(a)
+    tangents = 0
+    try:
+        for o in range(0, a["npoints"], 7):
+            for rr in range(a["hnrays"]):
+                t_ref = orc.trace(o, rr, 0)
+                t_gpu = dev.trace(o, rr, 0)
+                assert t_gpu["centre"] == t_ref["centre"], (o, rr)
+                assert np.array_equal(t_gpu["nr"], t_ref["nr"]), (o, rr)
+                c = t_ref["centre"]
+                mask = np.ones(len(t_ref["nr"]), bool)
+                mask[c] = False
+                assert np.array_equal(t_gpu["nr_interp"][mask], t_ref["nr_interp"][mask]), (o, rr)
+                assert np.array_equal(t_gpu["interp_factor"], t_ref["interp_factor"]), (o, rr)
+                assert np.array_equal(t_gpu["shift"], t_ref["shift"]), (o, rr)
+                assert np.array_equal(t_gpu["dZ"], t_ref["dZ"]), (o, rr)
+                tangents += int(np.sum(t_ref["nr"][1:] == t_ref["nr"][:-1]))
+        assert dev.ray_lengths_max() == orc.ray_lengths_max()
+    finally:
+        dev.close()
+    assert tangents > 0  # the sample crosses tangent points (a shell met twice)
+
+
+@pytest.mark.parametrize("name", sorted(MODELS))
+@pytest.mark.parametrize("approx", ["CloseLines", "None"])
+def test_spherical_solves_match_oracle(gpu_lib, name, approx):
+    raw = MODELS[name]()
+    a = H.setup(raw, approx=approx)
+    orc = O.Oracle(a)
+    ref = orc.formal_solve_fo2(want_u=True)
+    ref0 = orc.formal_solve_sc0()
+    has = ref["lambda_has"].astype(bool)
+    dev = _abi.DeviceModel(a)
+    try:
+        for precision in ("fp64", "split"):
+            g = dev.formal_solve_fo2(precision, want_u=True)
+            assert H.max_rel(g["J"], ref["J"]) < 1e-5, precision
+            assert H.max_rel(g["u"], ref["u"]) < 1e-5, precision
+            assert H.max_rel(g["lambda_diag"][has], ref["lambda_diag"][has]) < 1e-5, precision
+        g0 = dev.formal_solve_sc0("fp64")
+        assert H.max_rel(g0["J"], ref0["J"]) < 1e-5
+    finally:
+        dev.close()
+
+
+def _u_of(dev, precision, solver):
+    if solver == "fo2":
+        return dev.formal_solve_fo2(precision, want_u=True)["u"]
+    return dev.formal_solve_sc0(precision, want_uv=True)["u"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_density_distribution_1d_known_answer(gpu_lib, precision):
+    raw = S.density_distribution_1d("a")
+    a = H.setup(raw)
+    us = H.density_distribution_1d_solution(raw, a["nu"][0], H.ray_angles(raw))
+    dev = _abi.DeviceModel(a)
+    try:
+        for solver, bound in (("fo2", 4.4e-4), ("sc0", 4.1e-4)):
+            err = np.abs(H.relative_error(us, _u_of(dev, precision, solver)))[:-1, :-1, :]
+            assert np.mean(err) < bound, (solver, np.mean(err))
+    finally:
+        dev.close()
+
+
+@pytest.mark.parametrize("mwf, b2, b0", [(0.5, 1.0e-6, 1.1e-6), (0.35, 5.0e-7, 5.1e-7), (0.10, 5.31e-8, 5.91e-8)])
+def test_constant_velocity_gradient_1d_known_answer(gpu_lib, mwf, b2, b0):
+    raw = S.velocity_gradient_1d()
+    a = H.setup(raw, max_width_fraction=mwf)
+    us = H.velocity_gradient_1d_solution(raw, a["nu"][0], H.ray_angles(raw))
+    dev = _abi.DeviceModel(a)
+    try:
+        for solver, bound in (("fo2", b2), ("sc0", b0)):
+            err = np.abs(H.relative_error(us, _u_of(dev, "fp64", solver)))
+            assert np.mean(err) < bound, (solver, np.mean(err))
+    finally:
+        dev.close()
+
+
+def test_spherical_old_imager_and_core_model(gpu_lib):
+    """mgr_image on a spherical model against the oracle (1e-5), image coordinates
+    (r, 0); the drop-in core.Model path runs the 1D benchmark's Feautrier solve."""
+    from magritte_gb300 import loader
+
+    raw = MODELS["velocity"]()
+    a = H.setup(raw)
+    ref = O.Oracle(a).image_fo2(3)
+    dev = _abi.DeviceModel(a)
+    try:
+        for precision in ("fp64", "split"):
+            g = dev.image(3, precision)
+            assert H.max_rel(g["I"], ref) < 1e-5, precision
+        np.testing.assert_array_equal(g["ImX"], raw.position[:, 0])
+        np.testing.assert_array_equal(g["ImY"], np.zeros(raw.npoints))
+    finally:
+        dev.close()
+    raw = S.density_distribution_1d("a")
+    model = loader.to_core(raw, precision="fp64")
+    assert model.parameters.spherical_symmetry()
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    model.compute_radiation_field_feautrier_order_2()
+    u = np.array(model.radiation.u)
+    nu = np.array(model.radiation.frequencies.nu)[0]
+    us = H.density_distribution_1d_solution(raw, nu, H.ray_angles(raw))
+    assert np.mean(np.abs(H.relative_error(us, u))[:-1, :-1, :]) < 4.4e-4

@@ -130,3 +130,31 @@ def test_reference_shortchar_amplifies_opacity_rounding(built):
     rel = lambda x, y: float(np.max(np.abs(x - y) / np.abs(y)))
     assert rel(f1["J"], f0["J"]) < 1e-6
     assert rel(r1["J"], r0["J"]) > 1e-5
+
+
+def test_density_distribution_1d_spherical(built):
+    """tests/benchmarks/analytic/density_distribution_1D.py:126-178, :235-236 (case a):
+    1D spherical symmetry (shell walk and shifts, geometry.tpp:118-159, :378-417); the
+    mean relative error of u over all rays but the last pair and all points but the
+    outermost below 4.4e-4 (Feautrier) and 4.1e-4 (short characteristics)."""
+    raw = S.density_distribution_1d("a")
+    a = H.setup(raw)
+    orc = O.Oracle(a)
+    us = H.density_distribution_1d_solution(raw, a["nu"][0], H.ray_angles(raw))
+    e2 = np.abs(H.relative_error(us, orc.formal_solve_fo2(want_u=True)["u"]))[:-1, :-1, :]
+    e0 = np.abs(H.relative_error(us, orc.formal_solve_sc0()["u"]))[:-1, :-1, :]
+    assert np.mean(e2) < 4.4e-4
+    assert np.mean(e0) < 4.1e-4
+
+
+@pytest.mark.parametrize("mwf, b2, b0", [(0.5, 1.0e-6, 1.1e-6), (0.35, 5.0e-7, 5.1e-7), (0.10, 5.31e-8, 5.91e-8)])
+def test_constant_velocity_gradient_1d_spherical(built, mwf, b2, b0):
+    """tests/benchmarks/analytic/constant_velocity_gradient_1D.py:127-187, :245-253: the
+    three max_width_fraction settings (erf optical depths) with their mean-error bounds
+    for Feautrier and short characteristics."""
+    raw = S.velocity_gradient_1d()
+    a = H.setup(raw, max_width_fraction=mwf)
+    orc = O.Oracle(a)
+    us = H.velocity_gradient_1d_solution(raw, a["nu"][0], H.ray_angles(raw))
+    assert np.mean(np.abs(H.relative_error(us, orc.formal_solve_fo2(want_u=True)["u"]))) < b2
+    assert np.mean(np.abs(H.relative_error(us, orc.formal_solve_sc0()["u"]))) < b0
