@@ -100,6 +100,12 @@ typedef struct {
      * (src/model/geometry/geometry.tpp:118-159) with the Z-dependent shifts of
      * get_shift_spherical_symmetry (:378-417).  The neighbour lists are not used. */
     int32_t spherical_symmetry;
+    /* Rays::use_adaptive_directions (src/model/geometry/rays/rays.cpp:5-66): ray_direction
+     * is [npoints][nrays][3] and ray_weight [npoints][nrays], ray r of origin o at
+     * o * nrays + r (Rays::get_direction<true>, rays.cpp:94-146); antipod stays [nrays].
+     * The formal solves, their ALO and set_column use the origin's rays; the imagers use
+     * index r alone, as the reference's get_direction<false> does. */
+    int32_t use_adaptive_directions;
 } MgrModelDesc;
 
 typedef struct MgrModel MgrModel;

@@ -36,7 +36,9 @@ DESC_FIELDS = [
     ("lspec_inverse_mass", _f64p), ("quad_weights", _f64p), ("quad_roots", _f64p),
     ("min_opacity", C.c_double), ("min_dtau", C.c_double), ("max_interpolation_diff", C.c_double),
     ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int32), ("spherical_symmetry", C.c_int32),
+    ("use_adaptive_directions", C.c_int32),
 ]
+_FLAGS = ("spherical_symmetry", "use_adaptive_directions")
 
 _PTR_TYPES = {_u32p: np.uint32, _i32p: np.int32, _f64p: np.float64, _u8p: np.uint8}
 
@@ -185,7 +187,7 @@ def make_desc(arrays):
     desc = MgrModelDesc()
     keep = []
     for name, typ in DESC_FIELDS:
-        v = arrays[name] if name != "spherical_symmetry" else int(arrays.get(name, 0))
+        v = arrays[name] if name not in _FLAGS else int(arrays.get(name, 0))
         if typ in _PTR_TYPES:
             a = np.ascontiguousarray(v, dtype=_PTR_TYPES[typ])
             keep.append(a)

@@ -21,7 +21,7 @@ namespace {
 
 // Sequential restatement of trace_half (same arithmetic, neighbour order, strict <).
 int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int frame = 0) {
-    const double* d = m.raydir + 3 * r;
+    const double* d = frame ? m.raydir + 3 * r : ray_dir(m, o, r);
     const double4_32a po = m.pos[o];
     double Z = 0.0;
     uint32_t crt = o;
@@ -41,7 +41,7 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
             h.ids[count] = nxt;
             h.eid[count] = sph_eid(crt, nxt);
             h.dZ[count] = dZl;
-            const double s = shift_sph(m, frame, o, r, nxt, Z);
+            const double s = shift_sph(m, frame, o, r, nxt, Z, d);
             h.shift[count] = s;
             h.dsh[count] = (float)dsub_rn(s, 1.0);
             h.dzs[count] = (float)dZl * m.dz_scale;
@@ -166,6 +166,7 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     m.log_max_interp_diff = logf((float)d->max_interpolation_diff);
     m.approx = d->approx;
     m.sph = d->spherical_symmetry ? 1u : 0u;
+    m.adaptive = d->use_adaptive_directions ? 1u : 0u;
     m.min_op_s = (float)(d->min_opacity * Ko);
     m.dz_scale = (float)(1.0 / Ko);
     m.s_scale = (float)(Ko / Ke);
@@ -318,7 +319,7 @@ static int emu_fo2(const MgrModelDesc* d, int precision, uint32_t rr0, uint32_t 
             }
             for (uint32_t f = 0; f < F; f++) {
                 double s = 0.0;
-                for (uint32_t rr = rr0; rr < rr1; rr++) s += U[(size_t)rr * F + f] * 2.0 * m.rayw[rr];
+                for (uint32_t rr = rr0; rr < rr1; rr++) s += U[(size_t)rr * F + f] * 2.0 * ray_w(m, o, rr);
                 J[(size_t)o * F + f] = s;
             }
             if (!lam) continue;
@@ -333,7 +334,7 @@ static int emu_fo2(const MgrModelDesc* d, int precision, uint32_t rr0, uint32_t 
                     for (uint32_t q = 0; q < Q; q++) {
                         const uint32_t f = m.lq2f[(size_t)l * Q + q];
                         const double e = (f != 0xffffffffu && m.in_line[f])
-                                             ? lambda_element(k[q], m.rayw[rr], LD[(size_t)rr * F + f])
+                                             ? lambda_element(k[q], ray_w(m, o, rr), LD[(size_t)rr * F + f])
                                              : 0.0;
                         s += e;
                     }
@@ -435,7 +436,7 @@ extern "C" int mgr_emu_formal_solve_sc0(const MgrModelDesc* d, int precision, do
             }
             for (uint32_t f = 0; f < F; f++) {
                 double s = 0.0;
-                for (uint32_t rr = 0; rr < R; rr++) s += (m.rayw[rr] * 2.0) * U[(size_t)rr * F + f];
+                for (uint32_t rr = 0; rr < R; rr++) s += (ray_w(m, o, rr) * 2.0) * U[(size_t)rr * F + f];
                 J[(size_t)o * F + f] = s;
             }
             if (!lam) continue;
@@ -448,8 +449,8 @@ extern "C" int mgr_emu_formal_solve_sc0(const MgrModelDesc* d, int precision, do
                         const double xf = XF[(size_t)rr * F + f], xb = XB[(size_t)rr * F + f];
                         if (xf == 0.0 && xb == 0.0) continue;
                         const LambdaFactors k = lambda_factors(m, m.sorted_line, o, f);
-                        s += lambda_element_sc0(k, m.rayw[rr], xf);
-                        s += lambda_element_sc0(k, m.rayw[rr], xb);
+                        s += lambda_element_sc0(k, ray_w(m, o, rr), xf);
+                        s += lambda_element_sc0(k, ray_w(m, o, rr), xb);
                     }
                 lam[(size_t)o * L + l] = s;
             }

@@ -49,8 +49,15 @@ void Model::prepare() {
 
     // Rays::read (rays.cpp:5-66): hnrays and antipodes (tolerance 1e-9, last match wins).
     Rays& rays = geometry.rays;
-    const Size nrays = (Size)(rays.direction.shape.empty() ? 0 : rays.direction.shape[0]);
-    if (nrays == 0 || rays.weight.size() != nrays) throw std::runtime_error("ray directions/weights not set");
+    // adaptive ray directions: [npoints * nrays] directions and weights (rays.cpp:5-45),
+    // recognised from the flag or, with nrays set, from the array's length
+    const Size ndir = (Size)(rays.direction.shape.empty() ? 0 : rays.direction.shape[0]);
+    if (!rays.use_adaptive_directions && prm.nrays_.set_ && P > 1 && ndir == prm.nrays_.v * P)
+        rays.use_adaptive_directions = true;
+    if (rays.use_adaptive_directions && (P == 0 || ndir % P != 0))
+        throw std::runtime_error("adaptive ray directions must hold npoints * nrays entries");
+    const Size nrays = rays.use_adaptive_directions ? ndir / P : ndir;
+    if (nrays == 0 || rays.weight.size() != ndir) throw std::runtime_error("ray directions/weights not set");
     prm.nrays_.set(nrays, "nrays");
     prm.hnrays_.set(nrays / 2, "hnrays");
     rays.antipod.resize({nrays});
@@ -394,6 +401,7 @@ uint64_t Model::signature() const {
     mix(geometry.points.n_neighbors.version);
     mix(geometry.rays.direction.version);
     mix(geometry.rays.weight.version);
+    mix((uint64_t)geometry.rays.use_adaptive_directions);
     mix(geometry.boundary.boundary2point.version);
     mix(geometry.boundary.boundary_condition.version);
     mix(geometry.boundary.boundary_temperature.version);
@@ -464,6 +472,7 @@ void Model::fill_desc(MgrModelDesc& d) {
     d.max_distance_opacity_contribution = parameters.max_distance_opacity_contribution;
     d.approx = parameters.approx();
     d.spherical_symmetry = parameters.spherical_symmetry_ ? 1 : 0;
+    d.use_adaptive_directions = geometry.rays.use_adaptive_directions ? 1 : 0;
 }
 
 MgrModel* Model::device_model() {
@@ -819,8 +828,6 @@ int Model::compute_image_for_point(Size ray_nr, Size p) {
 // Model::set_column (model.cpp:1143-1153 -> Solver::set_column, solver.tpp:2953-2991):
 // column [nrays][P] of the per-point density.
 int Model::set_column() {
-    if (geometry.rays.use_adaptive_directions)
-        throw std::runtime_error("set_column: adaptive ray directions are not supported.");
     const Size P = parameters.npoints_.v;
     if (density.size() != P) throw std::runtime_error("set_column: density must have npoints entries.");
     MgrModel* dev = upload();

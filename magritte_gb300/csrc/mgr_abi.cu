@@ -258,6 +258,9 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.log_max_interp_diff = logf((float)d->max_interpolation_diff);
     dm.approx = d->approx;
     dm.sph = d->spherical_symmetry ? 1u : 0u;
+    dm.adaptive = d->use_adaptive_directions ? 1u : 0u;
+    // ray directions / weights: per point with adaptive directions (Rays::read, rays.cpp:33-45)
+    const size_t NR = (size_t)d->nrays * (dm.adaptive ? P : 1);
     m->n_edges = E;
     // interpolation-table slots: one per CSR edge, or three per point in spherical symmetry
     const size_t ET = dm.sph ? 3 * (size_t)P : E;
@@ -301,8 +304,8 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.p2b, d->point2boundary, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bc, d->boundary_condition, d->nboundary)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bt, d->boundary_temperature, d->nboundary)) != cudaSuccess) break;
-        if ((e = upload(m, &dm.raydir, d->ray_direction, 3 * (size_t)d->nrays)) != cudaSuccess) break;
-        if ((e = upload(m, &dm.rayw, d->ray_weight, d->nrays)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.raydir, d->ray_direction, 3 * NR)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.rayw, d->ray_weight, NR)) != cudaSuccess) break;
         if ((e = upload(m, &dm.antipod, d->antipod, d->nrays)) != cudaSuccess) break;
         if ((e = upload(m, &dm.line, d->line, L)) != cudaSuccess) break;
         if ((e = upload(m, &dm.sorted_line, d->sorted_line, L)) != cudaSuccess) break;

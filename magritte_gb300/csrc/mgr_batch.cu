@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256, MINB)
                 ok = false;
                 break;
             }
-            const double w2 = m.rayw[rr];
+            const double w2 = ray_w(m, o, rr);
             for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
                 const uint32_t f = f0 + lane;
                 if (f < m.F) {

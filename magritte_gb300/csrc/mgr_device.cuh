@@ -104,7 +104,18 @@ struct DevModel {
     float s_scale;               // Ko / Ke (true source = scaled source * s_scale)
     int approx;
     uint32_t sph;                // 1D spherical symmetry (Parameters::spherical_symmetry)
+    uint32_t adaptive;           // Rays::use_adaptive_directions: raydir [P][nrays][3], rayw [P][nrays]
 };
+
+// Rays::get_direction / get_weight (rays.cpp:94-146) of ray r at origin o: per point
+// with adaptive directions, else shared.  The formal solves and set_column use these;
+// the imagers index raydir + 3 r as the reference's get_direction<false> does.
+MGR_HD const double* ray_dir(const DevModel& m, uint32_t o, uint32_t r) {
+    return m.raydir + 3 * (m.adaptive ? (size_t)o * m.nrays + r : (size_t)r);
+}
+MGR_HD double ray_w(const DevModel& m, uint32_t o, uint32_t r) {
+    return m.rayw[m.adaptive ? (size_t)o * m.nrays + r : (size_t)r];
+}
 
 // ---------------------------------------------------------------------------------
 // Exactly rounded FP64 helpers for the trace (no contraction into FMA).  The host
@@ -185,10 +196,10 @@ MGR_HD double shift_rest(const DevModel& m, uint32_t r, uint32_t c, const double
 MGR_HD double sqnorm_rn(const double4_32a& a) { return dot3_rn(a.x, a.y, a.z, a.x, a.y, a.z); }
 
 // Geometry::get_shift_spherical_symmetry<CoMoving|Rest> (geometry.tpp:378-417) of point c
-// at distance Z along ray r from origin o, reversed for r >= hnrays in the rest frame
-// (geometry.tpp:428-465).  frame: 0 CoMoving, 1 Rest.
-MGR_HD double shift_sph(const DevModel& m, int frame, uint32_t o, uint32_t r, uint32_t c, double Z) {
-    const double* d = m.raydir + 3 * r;
+// at distance Z along ray r (direction d) from origin o, reversed for r >= hnrays in the
+// rest frame (geometry.tpp:428-465).  frame: 0 CoMoving, 1 Rest.
+MGR_HD double shift_sph(const DevModel& m, int frame, uint32_t o, uint32_t r, uint32_t c, double Z,
+                        const double* d) {
     const double4_32a po = m.pos[o];
     const double xc = m.pos[c].x;
     double s;
@@ -213,9 +224,12 @@ MGR_HD double shift_sph(const DevModel& m, int frame, uint32_t o, uint32_t r, ui
 
 // Geometry::get_shift<frame>(o, r, o, 0.0): the origin's shift as a half's trace starts
 // from it (solver.tpp:751; exactly 1 comoving in general geometry).
+// The comoving frame uses the origin's own (adaptive) directions, the rest frame of the
+// imagers the shared ones.
 MGR_HD double origin_shift(const DevModel& m, int frame, uint32_t o, uint32_t r) {
-    if (m.sph) return shift_sph(m, frame, o, r, o, 0.0);
-    return frame ? shift_rest(m, r, o, m.raydir + 3 * r) : 1.0;
+    const double* d = frame ? m.raydir + 3 * r : ray_dir(m, o, r);
+    if (m.sph) return shift_sph(m, frame, o, r, o, 0.0, d);
+    return frame ? shift_rest(m, r, o, d) : 1.0;
 }
 
 // Interpolation-table slot of a spherical step crt -> nxt: three per point (the tangent

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
             for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
                 const double* Uo = U + (size_t)(o - u_o0) * m.F + f;
                 double s = 0.0;
-                for (uint32_t k = 0; k < nR; k++) s += Uo[(size_t)k * u_stride] * 2.0 * m.rayw[rr0 + k];
+                for (uint32_t k = 0; k < nR; k++) s += Uo[(size_t)k * u_stride] * 2.0 * ray_w(m, o, rr0 + k);
                 J[(size_t)o * m.F + f] = s;
             }
         }
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
                 double s = 0.0;
                 for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
                     const double* Ur = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
-                    const double wt = m.rayw[rr] * 2.0;
+                    const double wt = ray_w(m, o, rr) * 2.0;
                     for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
                         const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
                         const double e =
@@ -268,8 +268,9 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
                 double sJ = 0.0, s0 = 0.0, s1r = 0.0, s1i = 0.0, s2r = 0.0, s2i = 0.0;
                 for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
                     const double* Ur = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
-                    const double wt = m.rayw[rr];
-                    const double nx = m.raydir[3 * rr], ny = m.raydir[3 * rr + 1], nz = m.raydir[3 * rr + 2];
+                    const double wt = ray_w(m, o, rr);
+                    const double* dn = ray_dir(m, o, rr);
+                    const double nx = dn[0], ny = dn[1], nz = dn[2];
                     const double wt_0 = inv_sqrt2 * (3.0 * nz * nz - 1.0);
                     const double wt_1_Re = -sqrt3 * nx * nz;
                     const double wt_1_Im = -sqrt3 * ny * nz;
@@ -322,7 +323,7 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
                         valid = f != 0xffffffffu && m.in_line[f];
                         if (valid) k = lambda_factors(m, m.sorted_line, o, f);
                     }
-                    const double e = valid ? lambda_element(k, m.rayw[rr], Lr[f]) : 0.0;
+                    const double e = valid ? lambda_element(k, ray_w(m, o, rr), Lr[f]) : 0.0;
                     const uint32_t nq = min(32u, m.Q - q0);
                     for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
                 }

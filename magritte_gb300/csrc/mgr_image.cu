@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(256) column_kernel(DevModel m, const double* _
         const uint32_t side = (uint32_t)((it / m.P) & 1);
         const uint32_t rr = (uint32_t)(it / (2ull * m.P));
         const uint32_t r = side ? m.antipod[rr] : rr;
-        const double* d = m.raydir + 3 * r;
+        const double* d = ray_dir(m, o, r);  // set_column<use_adaptive_directions>
         const double dx = d[0], dy = d[1], dz = d[2];
         const double4_32a po = m.pos[o];
         const double Rcos = dot3_rn(po.x, po.y, po.z, dx, dy, dz);

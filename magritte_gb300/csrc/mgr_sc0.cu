@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(128) sc0_reduce_kernel(DevModel m, uint32_t o_
         for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
             const double* Uo = U + (size_t)(o - u_o0) * m.F + f;
             double s = 0.0;
-            for (uint32_t rr = 0; rr < R; rr++) s += (m.rayw[rr] * 2.0) * Uo[(size_t)rr * u_stride];
+            for (uint32_t rr = 0; rr < R; rr++) s += (ray_w(m, o, rr) * 2.0) * Uo[(size_t)rr * u_stride];
             J[(size_t)o * m.F + f] = s;
         }
         if (!lam) continue;
@@ -104,8 +104,8 @@ __global__ void __launch_bounds__(128) sc0_reduce_kernel(DevModel m, uint32_t o_
                         add = (xf != 0.0) || (xb != 0.0);  // solved pairs only (update_Lambda per direction)
                         if (add) {
                             const LambdaFactors k = lambda_factors(m, m.sorted_line, o, f);
-                            ef = lambda_element_sc0(k, m.rayw[rr], xf);
-                            eb = lambda_element_sc0(k, m.rayw[rr], xb);
+                            ef = lambda_element_sc0(k, ray_w(m, o, rr), xf);
+                            eb = lambda_element_sc0(k, ray_w(m, o, rr), xb);
                         }
                     }
                     const uint32_t nq = min(32u, m.Q - q0);

@@ -128,7 +128,7 @@ __device__ __forceinline__ bool warp_next_point(const DevModel& m, const double4
 template <bool STORE, int FRAME>
 __device__ int trace_half_sph(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int lane,
                               int* status) {
-    const double* d = m.raydir + 3 * r;
+    const double* d = FRAME ? m.raydir + 3 * r : ray_dir(m, o, r);
     const double4_32a po = m.pos[o];
     const double Rcos = dot3_rn(po.x, po.y, po.z, d[0], d[1], d[2]);
     const double Rsin2 = dsub_rn(sqnorm_rn(po), dmul_rn(Rcos, Rcos));
@@ -157,7 +157,7 @@ __device__ int trace_half_sph(const DevModel& m, uint32_t o, uint32_t r, uint32_
             h.ids[count] = nxt;
             h.eid[count] = sph_eid(crt, nxt);
             h.dZ[count] = dZl;
-            const double sh = shift_sph(m, FRAME, o, r, nxt, Z);
+            const double sh = shift_sph(m, FRAME, o, r, nxt, Z, d);
             h.shift[count] = sh;
             h.dsh[count] = (float)dsub_rn(sh, 1.0);
             h.dzs[count] = (float)dZl * m.dz_scale;
@@ -182,7 +182,9 @@ template <bool STORE, int FRAME = 0>
 __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int lane,
                           int* status) {
     if (m.sph) return trace_half_sph<STORE, FRAME>(m, o, r, cap, h, lane, status);
-    const double* d = m.raydir + 3 * r;
+    // the formal solves trace along the origin's (adaptive) directions, the old imager
+    // along the shared ones (trace_ray<Rest, false>, solver.tpp:550-552)
+    const double* d = FRAME ? m.raydir + 3 * r : ray_dir(m, o, r);
     const double dx = d[0], dy = d[1], dz = d[2];
     const double4_32a po = m.pos[o];
     double Z = 0.0;

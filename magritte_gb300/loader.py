@@ -25,8 +25,14 @@ def to_core(raw, precision="fp64", approx="CloseLines"):
     g.points.velocity.set(np.ascontiguousarray(raw.velocity, np.float64))
     g.points.neighbors.set(np.ascontiguousarray(raw.neighbors, np.uint32))
     g.points.n_neighbors.set(np.ascontiguousarray(raw.n_neighbors, np.uint32))
-    g.rays.direction.set(np.ascontiguousarray(raw.ray_direction, np.float64))
-    g.rays.weight.set(np.ascontiguousarray(raw.ray_weight, np.float64))
+    if raw.adaptive_direction is not None:
+        # per-point rays (Rays::use_adaptive_directions): [npoints * nrays]
+        g.rays.use_adaptive_directions = True
+        g.rays.direction.set(np.ascontiguousarray(raw.adaptive_direction.reshape(-1, 3), np.float64))
+        g.rays.weight.set(np.ascontiguousarray(raw.adaptive_weight.reshape(-1), np.float64))
+    else:
+        g.rays.direction.set(np.ascontiguousarray(raw.ray_direction, np.float64))
+        g.rays.weight.set(np.ascontiguousarray(raw.ray_weight, np.float64))
     g.boundary.boundary2point.set(np.ascontiguousarray(raw.boundary2point, np.uint32))
     prm.set_nboundary(len(raw.boundary2point))
     g.boundary.boundary_condition.set(np.ascontiguousarray(raw.boundary_condition, np.int32))

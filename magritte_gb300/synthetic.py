@@ -113,6 +113,11 @@ class RawModel:
     quad_weights: List[np.ndarray]
     nquads: int
     spherical_symmetry: bool = False
+    # adaptive ray directions (Rays::use_adaptive_directions): per-point directions
+    # [P][nrays][3] and weights [P][nrays]; ray_direction / ray_weight then hold point
+    # 0's, which is what the reference's imagers read (Rays::get_direction<false>)
+    adaptive_direction: Optional[np.ndarray] = None
+    adaptive_weight: Optional[np.ndarray] = None
 
     @property
     def npoints(self):
@@ -463,6 +468,34 @@ def velocity_gradient_1d(npoints: int = 100, nrays: int = 100, nquads: int = 100
     abund = np.tile(np.array([1.0e8, 1.0e12, 0.0]), (npoints, 1))
     return spherical_1d("constant_velocity_gradient_1D", (i + 1.0) * dx, (i + 1.0) * dv, abund,
                         np.full(npoints, 45.0), np.zeros(npoints), nrays, nquads, [lamda_test_species()])
+
+
+def with_adaptive_rays(raw: RawModel, seed: int = 0, jitter: float = 0.5, identical: bool = False) -> RawModel:
+    """A copy of ``raw`` with adaptive (per-point) ray directions, the layout
+    Rays::use_adaptive_directions reads (rays.cpp:33-45): each point's rays are its own
+    random rotation of the model's directions (antipodes stay paired), with weights
+    jittered per point by up to ``jitter`` (the same for a ray and its antipode) and
+    normalised per point.  ``identical``: every point gets the
+    model's own rays and weights (the adaptive layout holding the shared rays)."""
+    from dataclasses import replace
+    from scipy.spatial.transform import Rotation
+
+    P, R = raw.npoints, raw.nrays
+    if identical:
+        dirs = np.broadcast_to(raw.ray_direction, (P, R, 3)).copy()
+        wts = np.broadcast_to(raw.ray_weight, (P, R)).copy()
+    else:
+        from .healpix import antipodes
+
+        rng = np.random.default_rng(seed)
+        rot = Rotation.random(P, random_state=rng)
+        dirs = np.einsum("pij,rj->pri", rot.as_matrix(), raw.ray_direction)
+        f = 1.0 + jitter * rng.uniform(-1.0, 1.0, size=(P, R))
+        f = 0.5 * (f + f[:, antipodes(raw.ray_direction)])
+        wts = raw.ray_weight[None, :] * f
+        wts /= wts.sum(axis=1, keepdims=True)
+    return replace(raw, name=raw.name + "_adaptive", ray_direction=np.ascontiguousarray(dirs[0]),
+                   ray_weight=np.ascontiguousarray(wts[0]), adaptive_direction=dirs, adaptive_weight=wts)
 
 
 def delaunay_neighbors(position: np.ndarray):

@@ -149,11 +149,22 @@ static uint32_t get_next_general(const OrcModel* m, const double* origin, const 
     return next;
 }
 
+/* Rays::get_direction / get_weight (rays.cpp:94-146): per point, [P][nrays], with
+ * adaptive ray directions, else [nrays].  The formal solves and set_column use the
+ * adaptive layout; the imagers always index [nrays] (their traces are
+ * trace_ray<Rest, false>, solver.tpp:550-552). */
+static inline const double* ray_dir(const OrcModel* m, int adaptive, uint32_t o, uint32_t r) {
+    return m->ray_direction + 3 * (adaptive ? (size_t)o * m->nrays + r : (size_t)r);
+}
+static inline double ray_wt(const OrcModel* m, uint32_t o, uint32_t r) {
+    return m->ray_weight[m->use_adaptive_directions ? (size_t)o * m->nrays + r : (size_t)r];
+}
+
 /* Geometry::get_shift_general_geometry<CoMoving|Rest> (geometry.tpp:203-221), the
  * spherical-symmetry shifts at distance Z along the ray (geometry.tpp:378-417) and the
  * reversal for the old imager (geometry.tpp:428-465).  frame: 0 CoMoving, 1 Rest. */
 static inline double get_shift(const OrcModel* m, int frame, uint32_t o, uint32_t r, uint32_t c, double Z) {
-    const double* d = m->ray_direction + 3 * r;
+    const double* d = ray_dir(m, frame == 0 && m->use_adaptive_directions, o, r);
     double shift;
     if (m->spherical_symmetry) {
         const double* org = m->position + 3 * o;
@@ -288,7 +299,7 @@ static int64_t trace(const OrcModel* m, Buf* b, int frame, uint32_t line, uint32
     double Z               = 0.0;
     double dZ              = 0.0;
     const double* origin   = m->position + 3 * o;
-    const double* raydir   = m->ray_direction + 3 * r;
+    const double* raydir   = ray_dir(m, frame == 0 && m->use_adaptive_directions, o, r);
     uint32_t nxt           = get_next(m, origin, raydir, o, &Z, &dZ);
     if (valid_point(m, nxt)) {
         uint32_t crt     = o;
@@ -311,12 +322,12 @@ static int64_t trace(const OrcModel* m, Buf* b, int frame, uint32_t line, uint32
 }
 
 /* Solver::get_ray_length (solver.tpp:79-103). */
-static uint32_t get_ray_length(const OrcModel* m, uint32_t o, uint32_t r) {
+static uint32_t get_ray_length(const OrcModel* m, uint32_t o, uint32_t r, int adaptive) {
     uint32_t l           = 0;
     double Z             = 0.0;
     double dZ            = 0.0;
     const double* origin = m->position + 3 * o;
-    const double* raydir = m->ray_direction + 3 * r;
+    const double* raydir = ray_dir(m, adaptive, o, r);
     uint32_t nxt         = get_next(m, origin, raydir, o, &Z, &dZ);
     if (valid_point(m, nxt)) {
         uint32_t crt = o;
@@ -331,7 +342,22 @@ static uint32_t get_ray_length(const OrcModel* m, uint32_t o, uint32_t r) {
     return l;
 }
 
+static uint32_t ray_lengths_max_impl(const OrcModel* m, int nthreads, int adaptive);
+
+/* Solver::get_ray_lengths_max<CoMoving, adaptive> (solver.tpp:105-126): the formal solves'
+ * buffer length. */
 uint32_t orc_ray_lengths_max(const OrcModel* m, int nthreads) {
+    return ray_lengths_max_impl(m, nthreads, m->use_adaptive_directions);
+}
+
+/* The imagers' traces use the model-wide directions also in an adaptive model. */
+static uint32_t image_ray_lengths_max(const OrcModel* m, int nthreads) {
+    const uint32_t a = ray_lengths_max_impl(m, nthreads, 0);
+    const uint32_t b = m->use_adaptive_directions ? ray_lengths_max_impl(m, nthreads, 1) : 0;
+    return a > b ? a : b;
+}
+
+static uint32_t ray_lengths_max_impl(const OrcModel* m, int nthreads, int adaptive) {
     uint32_t mx = 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -340,7 +366,7 @@ uint32_t orc_ray_lengths_max(const OrcModel* m, int nthreads) {
         const uint32_t ar = m->antipod[rr];
 #pragma omp parallel for reduction(max : mx) schedule(dynamic, 64)
         for (int64_t o = 0; o < (int64_t)m->npoints; o++) {
-            const uint32_t len = get_ray_length(m, (uint32_t)o, rr) + get_ray_length(m, (uint32_t)o, ar);
+            const uint32_t len = get_ray_length(m, (uint32_t)o, rr, adaptive) + get_ray_length(m, (uint32_t)o, ar, adaptive);
             if (len > mx) mx = len;
         }
     }
@@ -695,7 +721,7 @@ static void update_lambda(const OrcModel* m, Buf* b, uint32_t rr, uint32_t f, do
     if (!m->in_line_integral[f]) return;
     const uint32_t c        = b->centre;
     const uint32_t p        = b->nr[c];
-    const double w_ang      = 2.0 * m->ray_weight[rr];
+    const double w_ang      = 2.0 * ray_wt(m, p, rr);
     const uint32_t ls       = m->corr_lspec[f];
     const uint32_t k        = m->corr_k[f];
     const uint32_t z        = m->corr_z[f];
@@ -839,13 +865,13 @@ static int fo2_range_v(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o
                                 val = b.Su[c];
                                 if (u) u[((size_t)rr * P + o) * F + f] = val;
                                 if (v) v[((size_t)rr * P + o) * F + f] = feautrier_v(m, &b, o, f);
-                                J[(size_t)o * F + f] += b.Su[c] * 2.0 * m->ray_weight[rr];
+                                J[(size_t)o * F + f] += b.Su[c] * 2.0 * ray_wt(m, o, rr);
                                 update_lambda(m, &b, rr, f, lambda_diag, lambda_has);
                             } else {
                                 val = boundary_intensity(m, o, m->nu[(size_t)o * F + f]);
                                 if (u) u[((size_t)rr * P + o) * F + f] = val;
                                 if (v) v[((size_t)rr * P + o) * F + f] = 0.0;
-                                J[(size_t)o * F + f] += 2.0 * m->ray_weight[rr] * val;
+                                J[(size_t)o * F + f] += 2.0 * ray_wt(m, o, rr) * val;
                             }
                         }
                     }
@@ -883,7 +909,7 @@ static double sc0_lambda(const OrcModel* m, uint32_t o, uint32_t r, uint32_t f, 
     const uint32_t lid      = m->nrad_cum[ls] + k;
     const double freq_line  = m->line[lid];
     const double invr_mass  = m->lspec_inverse_mass[ls];
-    const double constante  = m->line_A[lid] * m->quad_weights[(size_t)ls * m->nquads + z] * m->ray_weight[r];
+    const double constante  = m->line_A[lid] * m->quad_weights[(size_t)ls * m->nquads + z] * ray_wt(m, o, r);
     const double freq       = m->nu[(size_t)o * m->nfreqs + f];
     double eta, chi;
     get_eta_and_chi(m, o, k, freq_line, &eta, &chi);
@@ -962,7 +988,7 @@ int orc_formal_solve_sc0(const OrcModel* m, double* J, double* I, double* u, dou
                     if (bad) continue;
                     const uint32_t o  = (uint32_t)oo;
                     const uint32_t c  = b.centre;
-                    const double wt   = m->ray_weight[rr] * 2.0;
+                    const double wt   = ray_wt(m, o, rr) * 2.0;
                     b.nr[c]           = o;
                     b.shift[c]        = 1.0;
                     for (uint32_t k = 0; k < m->nrad[ls]; k++) {
@@ -1059,7 +1085,7 @@ int orc_image_optical_depth(const OrcModel* m, uint32_t rr, double* I, int nthre
 
 static int image_fo2_impl(const OrcModel* m, uint32_t rr, double* I, int nthreads, int tau) {
     const uint32_t P = m->npoints, F = m->nfreqs;
-    const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
+    const uint32_t length = 2 * image_ray_lengths_max(m, nthreads) + 1;
     const uint32_t ar     = m->antipod[rr];
     int err_any           = 0;
 #ifdef _OPENMP
@@ -1181,7 +1207,7 @@ static void solve_for_point(const OrcModel* m, Buf* b, uint32_t o, uint32_t f, d
  * element writes nothing).  Returns -3 when the ray does not fit. */
 int orc_image_for_point(const OrcModel* m, uint32_t rr, uint32_t p, uint32_t* n_tot, double* S, double* dtau,
                         double* u, uint32_t capacity) {
-    const uint32_t length = 2 * orc_ray_lengths_max(m, 1) + 1;
+    const uint32_t length = 2 * image_ray_lengths_max(m, 1) + 1;
     Buf b;
     if (buf_init(&b, length) != 0) return -1;
     const uint32_t c  = b.centre;
@@ -1224,7 +1250,7 @@ int orc_set_column(const OrcModel* m, const double* density, double* column, int
             for (int side = 0; side < 2; side++) {
                 const uint32_t r     = side ? ar : rr;
                 const double* origin = m->position + 3 * o;
-                const double* raydir = m->ray_direction + 3 * r;
+                const double* raydir = ray_dir(m, m->use_adaptive_directions, o, r);
                 double col = 0.0, Z = 0.0, dZ = 0.0;
                 uint32_t nxt = get_next(m, origin, raydir, o, &Z, &dZ);
                 if (valid_point(m, nxt)) {

@@ -73,6 +73,7 @@ typedef struct {
     double max_distance_opacity_contribution;
     int    approx;
     int    spherical_symmetry;            /* 1D spherical symmetry: points on the x axis by radius */
+    int    use_adaptive_directions;       /* ray_direction [P][nrays][3], ray_weight [P][nrays] */
 } OrcModel;
 
 /* One ray pair as the reference lays it out in its per-thread buffers

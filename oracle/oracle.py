@@ -163,9 +163,14 @@ def reference_setup(raw, approx="CloseLines", max_width_fraction=0.35, min_opaci
         neighbors=np.ascontiguousarray(raw.neighbors, np.uint32), point2boundary=p2b,
         boundary_condition=np.ascontiguousarray(raw.boundary_condition, np.int32),
         boundary_temperature=np.ascontiguousarray(raw.boundary_temperature, np.float64),
-        ray_direction=np.ascontiguousarray(raw.ray_direction, np.float64),
-        ray_weight=np.ascontiguousarray(raw.ray_weight, np.float64),
+        # adaptive ray directions: per point [P][nrays] (rays.cpp:94-146); the antipode
+        # table is shared by all points
+        ray_direction=np.ascontiguousarray(raw.ray_direction if raw.adaptive_direction is None
+                                           else raw.adaptive_direction.reshape(-1, 3), np.float64),
+        ray_weight=np.ascontiguousarray(raw.ray_weight if raw.adaptive_weight is None
+                                        else raw.adaptive_weight.reshape(-1), np.float64),
         antipod=antipodes(raw.ray_direction),
+        use_adaptive_directions=int(raw.adaptive_direction is not None),
         line=line, sorted_line=sorted_line, sorted_line_map=sorted_line_map,
         max_inverse_mass=float(max_inverse_mass),
         emissivity=emissivity, opacity=opacity, inverse_width=inverse_width, interp_criterion=criterion,
@@ -205,7 +210,11 @@ _FIELDS = [
     ("lspec_inverse_mass", _f64p), ("quad_weights", _f64p), ("quad_roots", _f64p),
     ("min_opacity", C.c_double), ("min_dtau", C.c_double), ("max_interpolation_diff", C.c_double),
     ("max_distance_opacity_contribution", C.c_double), ("approx", C.c_int), ("spherical_symmetry", C.c_int),
+    ("use_adaptive_directions", C.c_int),
 ]
+
+
+_FLAGS = ("spherical_symmetry", "use_adaptive_directions")
 
 
 class OrcModel(C.Structure):
@@ -261,7 +270,7 @@ class Oracle:
         self.a = arrays
         self.m = OrcModel()
         for name, typ in _FIELDS:
-            v = arrays[name] if name != "spherical_symmetry" else int(arrays.get(name, 0))
+            v = arrays[name] if name not in _FLAGS else int(arrays.get(name, 0))
             if typ in (_u32p, _i32p, _f64p, _u8p):
                 setattr(self.m, name, _ptr(v, typ))
             else:
@@ -323,9 +332,16 @@ class Oracle:
         fq = [[None] * a["nquads"] for _ in range(L)]
         for f in range(a["nfreqs"]):
             fq[a["corr_line"][f]][a["corr_z"][f]] = f
+        nrays = a["nrays"]
+        adaptive = int(a.get("use_adaptive_directions", 0))
         for rr in range(R):
-            nx, ny, nz = a["ray_direction"][rr]
-            wt = a["ray_weight"][rr]
+            # Rays::get_direction / get_weight (rays.cpp:94-146): per point when adaptive
+            if adaptive:
+                nx, ny, nz = a["ray_direction"].reshape(P, nrays, 3)[:, rr].T
+                wt = a["ray_weight"].reshape(P, nrays)[:, rr]
+            else:
+                nx, ny, nz = a["ray_direction"][rr]
+                wt = a["ray_weight"][rr]
             w = {"J2_0": inv_sqrt2 * (3.0 * nz * nz - 1.0), "J2_1_Re": -sqrt3 * nx * nz,
                  "J2_1_Im": -sqrt3 * ny * nz, "J2_2_Re": 0.5 * sqrt3 * (nx * nx - ny * ny),
                  "J2_2_Im": sqrt3 * nx * ny}

@@ -107,14 +107,27 @@ def test_density_distribution_1d_known_answer(gpu_lib, precision):
 
 @pytest.mark.parametrize("mwf, b2, b0", [(0.5, 1.0e-6, 1.1e-6), (0.35, 5.0e-7, 5.1e-7), (0.10, 5.31e-8, 5.91e-8)])
 def test_constant_velocity_gradient_1d_known_answer(gpu_lib, mwf, b2, b0):
+    """The reference's bounds sit within 0.05 % (0.10) and 11 % (0.35) of the mean errors
+    its CPU arithmetic reaches (the oracle meets them exactly in
+    test_oracle_known_answers.py).  The GPU's FP64 mode differs from that arithmetic by
+    the single-precision libm calls the reference makes (expf, logf, erff: CUDA's and
+    glibc's round differently), which moves u by ~1e-8 relative - far inside the 1e-5
+    parity bar, but a visible share of a 5e-8 mean error.  So here: u within 1e-6 of the
+    oracle, and each mean error within the reference's bound plus 10 % of the bound."""
     raw = S.velocity_gradient_1d()
     a = H.setup(raw, max_width_fraction=mwf)
     us = H.velocity_gradient_1d_solution(raw, a["nu"][0], H.ray_angles(raw))
+    orc = O.Oracle(a)
+    ref = {"fo2": orc.formal_solve_fo2(want_u=True)["u"], "sc0": orc.formal_solve_sc0()["u"]}
     dev = _abi.DeviceModel(a)
     try:
         for solver, bound in (("fo2", b2), ("sc0", b0)):
-            err = np.abs(H.relative_error(us, _u_of(dev, "fp64", solver)))
-            assert np.mean(err) < bound, (solver, np.mean(err))
+            u = _u_of(dev, "fp64", solver)
+            assert H.max_rel(u, ref[solver]) < 1e-6, solver
+            err = np.mean(np.abs(H.relative_error(us, u)))
+            err_ref = np.mean(np.abs(H.relative_error(us, ref[solver])))
+            print(f"mwf {mwf} {solver}: GPU mean error {err:.6e}, oracle {err_ref:.6e}, bound {bound:.3e}")
+            assert err < 1.1 * bound, (solver, err, err_ref)
     finally:
         dev.close()
 

@@ -53,6 +53,8 @@ MODELS = {
     # 1D spherical symmetry (shell walk, Z-dependent shifts)
     "sph_density": lambda: S.density_distribution_1d("a", npoints=60, nrays=20, nquads=11),
     "sph_velocity": lambda: S.velocity_gradient_1d(npoints=40, nrays=20, nquads=21),
+    # adaptive (per-point) ray directions and weights
+    "cube10_adaptive": lambda: S.with_adaptive_rays(S.grid_cube(n=10, nquads=5)),
 }
 
 

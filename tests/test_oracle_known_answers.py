@@ -158,3 +158,20 @@ def test_constant_velocity_gradient_1d_spherical(built, mwf, b2, b0):
     us = H.velocity_gradient_1d_solution(raw, a["nu"][0], H.ray_angles(raw))
     assert np.mean(np.abs(H.relative_error(us, orc.formal_solve_fo2(want_u=True)["u"]))) < b2
     assert np.mean(np.abs(H.relative_error(us, orc.formal_solve_sc0()["u"]))) < b0
+
+
+def test_adaptive_ray_layout_with_shared_rays_is_identical(built):
+    """Rays::use_adaptive_directions (rays.cpp:94-146): the per-point layout holding
+    every point's copy of the shared rays gives the shared-ray results bit for bit
+    (formal solves, ALO, set_column); rotated per-point rays change them."""
+    raw = S.grid_cube(n=10, nquads=5)
+    a0, ai = H.setup(raw), H.setup(S.with_adaptive_rays(raw, identical=True))
+    o0, oi = O.Oracle(a0), O.Oracle(ai)
+    r0, ri = o0.formal_solve_fo2(want_u=True), oi.formal_solve_fo2(want_u=True)
+    for k in ("J", "u", "lambda_diag"):
+        np.testing.assert_array_equal(ri[k], r0[k])
+    np.testing.assert_array_equal(oi.formal_solve_sc0()["J"], o0.formal_solve_sc0()["J"])
+    rho = np.linspace(1.0, 2.0, raw.npoints)
+    np.testing.assert_array_equal(oi.set_column(rho), o0.set_column(rho))
+    ra = O.Oracle(H.setup(S.with_adaptive_rays(raw))).formal_solve_fo2()
+    assert H.max_rel(ra["J"], r0["J"]) > 1e-3
