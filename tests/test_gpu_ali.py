@@ -173,3 +173,35 @@ def test_core_model_memory_lean(gpu_lib):
     ls = model.lines.lineProducingSpecies[0]
     np.testing.assert_array_equal(np.array(ls.Jlin), np.array(ls.J))
     assert np.isfinite(np.array(ls.Jeff)).all()
+
+
+def test_core_model_van_zadelhoff_1a_1d_against_ratran(gpu_lib):
+    """tests/benchmarks/numeric/vanZadelhoff_1_1D.py:88-165 through the drop-in API on the
+    GPU: the 1D spherically symmetric problem 1a (250 shells, 200 rays, nquads 11),
+    compute_level_populations(True, 100), fractional populations against the RATRAN
+    results (tests/golden/ratran_vanZadelhoff_1a.npz) within the reference's 0.12 / 0.13,
+    and the level populations within 1e-6 of the oracle's ALI."""
+    import os
+
+    from scipy.interpolate import interp1d
+
+    from magritte_gb300 import loader
+
+    raw = S.density_distribution_1d("a", npoints=250, nrays=200, nquads=11)
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    it = model.compute_level_populations(True, 100)
+    pops = np.array(model.lines.lineProducingSpecies[0].population).reshape(raw.npoints, 2)
+    ref = O.AliOracle(raw, H.setup(raw)).run(use_ng=True, max_it=100)
+    assert it == ref["iterations"]
+    tot = raw.abundance[:, 0][:, None]
+    assert _rel(pops, ref["populations"][0], 1e-10 * tot) < 1e-6
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ratran_vanZadelhoff_1a.npz"))
+    mid = 0.5 * (g["ra"] + g["rb"])
+    rs = raw.position[:, 0]
+    abun = raw.abundance[:, 0]
+    e0 = np.abs(H.relative_error(pops[:, 0] / abun, interp1d(mid, g["lp0"], fill_value="extrapolate")(rs)))
+    e1 = np.abs(H.relative_error(pops[:, 1] / abun, interp1d(mid, g["lp1"], fill_value="extrapolate")(rs)))
+    assert e0[1:].max() < 0.12 and e1[1:].max() < 0.13, (e0[1:].max(), e1[1:].max())

@@ -1,12 +1,12 @@
 """Pins the oracle's ALI level-population loop.
 
-* van Zadelhoff et al. (2002) problem 1a/1b in the 3D HEALPix-shell form of the
-  reference's tests/benchmarks/numeric/vanZadelhoff_1_3D_healpix.py: the fractional
-  level populations must agree with the RATRAN results the reference ships
-  (tests/benchmarks/numeric/Ratran_results/vanZadelhoff_1{a,b}.out) within the
-  reference test's own bound, 0.2 relative (vanZadelhoff_1_3D_healpix.py:173).
-  The RATRAN files are read from the reference tree when it is present.  The model
-  uses 14 shells instead of 20 and 30 ALI iterations to keep the CPU suite short.
+* van Zadelhoff et al. (2002) problem 1a in the 1D spherically symmetric form of the
+  reference's tests/benchmarks/numeric/vanZadelhoff_1_1D.py (250 shells, 200 rays,
+  nquads 11, Ng acceleration, at most 100 iterations): the fractional level populations
+  agree with the RATRAN results the reference ships
+  (tests/benchmarks/numeric/Ratran_results/vanZadelhoff_1a.out, committed as
+  tests/golden/ratran_vanZadelhoff_1a.npz) within the reference test's own bounds,
+  0.12 and 0.13 relative (vanZadelhoff_1_1D.py:160), skipping the inner boundary.
 * Statistical equilibrium in the collision-dominated limit reproduces LTE.
 * compute_Jeff's line integral and ALO correction (model.cpp:514-545)."""
 import os
@@ -17,7 +17,7 @@ import pytest
 import oracle as O
 from magritte_gb300 import synthetic as S
 
-RATRAN = "/root/reference/tests/benchmarks/numeric/Ratran_results/vanZadelhoff_1{}.out"
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -25,27 +25,33 @@ def built():
     O.build()
 
 
-@pytest.mark.parametrize("kind", ["a", "b"])
-def test_van_zadelhoff_1_against_ratran(kind):
-    path = RATRAN.format(kind)
-    if not os.path.exists(path):
-        pytest.skip("reference RATRAN results not available here")
+def ratran_errors(raw, pops, kind):
+    """Relative errors of the fractional populations against RATRAN at each shell
+    (vanZadelhoff_1_1D.py:113-123)."""
     from scipy.interpolate import interp1d
 
-    raw = S.van_zadelhoff_1(kind, nshells=14)
-    a = O.reference_setup(raw)
-    r = O.AliOracle(raw, a).run(use_ng=True, max_it=30)
-    pops = r["populations"][0]
+    g = np.load(os.path.join(GOLDEN, f"ratran_vanZadelhoff_1{kind}.npz"))
+    mid = 0.5 * (g["ra"] + g["rb"])
+    i0 = interp1d(mid, g["lp0"], fill_value="extrapolate")
+    i1 = interp1d(mid, g["lp1"], fill_value="extrapolate")
     abun = raw.abundance[:, 0]
     rs = np.linalg.norm(raw.position, axis=1)
-    cols = np.loadtxt(path, skiprows=14, unpack=True)
-    ra, rb, lp0, lp1 = cols[1], cols[2], cols[9], cols[10]
-    i0 = interp1d(0.5 * (ra + rb), lp0, fill_value="extrapolate")
-    i1 = interp1d(0.5 * (ra + rb), lp1, fill_value="extrapolate")
     rel = lambda x, y: 2.0 * (x - y) / (x + y)  # magritte/tools.py:69-73
-    e0 = np.abs(rel(pops[:, 0] / abun, i0(rs)))
-    e1 = np.abs(rel(pops[:, 1] / abun, i1(rs)))
-    assert e0[1:].max() < 0.2 and e1[1:].max() < 0.2, (e0[1:].max(), e1[1:].max())
+    return np.abs(rel(pops[:, 0] / abun, i0(rs))), np.abs(rel(pops[:, 1] / abun, i1(rs)))
+
+
+def van_zadelhoff_1_1d(kind="a"):
+    """vanZadelhoff_1_1D.py:20-85: the density-distribution shells at 250 points with
+    200 rays and nquads 11."""
+    return S.density_distribution_1d(kind, npoints=250, nrays=200, nquads=11)
+
+
+def test_van_zadelhoff_1a_1d_against_ratran():
+    raw = van_zadelhoff_1_1d("a")
+    a = O.reference_setup(raw)
+    r = O.AliOracle(raw, a).run(use_ng=True, max_it=100)
+    e0, e1 = ratran_errors(raw, r["populations"][0], "a")
+    assert e0[1:].max() < 0.12 and e1[1:].max() < 0.13, (e0[1:].max(), e1[1:].max())
 
 
 def test_statistical_equilibrium_collision_limit_is_lte():
