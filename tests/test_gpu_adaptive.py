@@ -2,7 +2,8 @@
 rays.cpp:5-146): each origin traces, shifts and weights its own rays.
 
 * J, u and the ALO diagonal of the Feautrier solve (FP64 and split precision), the
-  short-characteristics J, and the anisotropic J2 elements within 1e-5 of the oracle.
+  short-characteristics J (far wings on the scale of the line peak, as in
+  test_gpu_sc0.py), and the anisotropic J2 elements within 1e-5 of the oracle.
 * set_column along each point's own rays bit-exact.
 * The drop-in path: core.Model with an [npoints * nrays] direction array."""
 import numpy as np
@@ -41,7 +42,11 @@ def test_adaptive_formal_solves_match_oracle(adaptive):
         for k in ("J", "u"):
             assert H.max_rel(g[k], ref[k]) < 1e-5, (precision, k)
         assert H.max_rel(g["lambda_diag"][has], ref["lambda_diag"][has]) < 1e-5, precision
-    assert H.max_rel(dev.formal_solve_sc0("fp64")["J"], orc.formal_solve_sc0()["J"]) < 1e-5
+    # short characteristics: far-wing values on the scale of the point's line peak, as in
+    # test_gpu_sc0.py (its update amplifies single-ulp libm differences where dtau is small)
+    J0, J0_ref = dev.formal_solve_sc0("fp64")["J"], orc.formal_solve_sc0()["J"]
+    floor = 1e-2 * np.abs(J0_ref).max(axis=-1, keepdims=True)
+    assert np.max(np.abs(J0 - J0_ref) / np.maximum(np.abs(J0_ref), floor)) < 1e-5
     an = dev.formal_solve_fo2_anis("fp64")
     an_ref = orc.formal_solve_fo2_anis()
     scale = np.abs(an_ref["J"]).max()
