@@ -167,6 +167,10 @@ static int adj_plane(MgrModel* model, const char* who, const double* raydir, uin
         set_error(std::string(who) + ": One line approximation is not supported for imaging.");
         return MGR_ERR_UNSUPPORTED;
     }
+    if (model->dm.sph) {
+        set_error(std::string(who) + ": the differentiable imager does not support spherically symmetric models.");
+        return MGR_ERR_UNSUPPORTED;
+    }
     std::vector<double> hx, hy;
     int rc = image_plane_setup(model, who, raydir, nx, ny, ip, hx, hy);
     if (rc != MGR_OK) return rc;

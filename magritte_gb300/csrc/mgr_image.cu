@@ -82,8 +82,7 @@ __global__ void __launch_bounds__(256) image_new_kernel(DevModel m, ImagePlane i
         pixel_origin(ip, ip.ImX[px], ip.ImY[px], org);
         double Z;
         const uint32_t start = pixel_start(m, org, ip, lane, Z);
-        const double4_32a vs = m.vel[start];
-        const double sh0 = dadd_rn(1.0, dot3_rn(vs.x, vs.y, vs.z, ip.d[0], ip.d[1], ip.d[2]));
+        const double sh0 = image_shift(m, org, ip, start, Z);
         bk.shift0 = fw.shift0 = bk.cshift = fw.cshift = sh0;
         bk.dsh0 = fw.dsh0 = (float)dsub_rn(sh0, 1.0);
         const int nb = trace_image<true>(m, org, ip, start, Z, cap, bk, lane, status);
@@ -179,14 +178,9 @@ int image_plane_setup(MgrModel* model, const char* who, const double* raydir, ui
         set_error(std::string(who) + ": One line approximation is not supported for imaging.");
         return MGR_ERR_UNSUPPORTED;
     }
-    if (model->dm.sph) {
-        set_error(std::string(who) + ": the projection-plane imager is not available for spherically symmetric "
-                                     "models (use mgr_image).");
-        return MGR_ERR_UNSUPPORTED;
-    }
     std::string err;
     const int rc = image_plane_compute(model->host_pos.data(), model->host_p2b.data(), model->dm.P, model->dm.B,
-                                       raydir, nx, ny, ip, hx, hy, err);
+                                       raydir, nx, ny, ip, hx, hy, err, model->dm.sph != 0);
     if (rc != MGR_OK) set_error(std::string(who) + ": " + err);
     return rc;
 }

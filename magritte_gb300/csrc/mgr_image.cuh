@@ -20,6 +20,7 @@ struct ImagePlane {
     double d[3];                // normalised ray direction
     double center[3];           // Points::center (points.cpp:30-42)
     uint32_t start;             // get_closest_bdy_point_in_custom_raydir
+    bool sph;                   // 1D spherical symmetry (shell walk from the pixel origin)
     uint32_t nx, ny;
     const double* ImX;          // [nx*ny] device
     const double* ImY;
@@ -76,6 +77,21 @@ static __device__ uint32_t bdy_point_closer(const DevModel& m, const double* org
     return (uint32_t)__double_as_longlong(m.edge[cum + besti].w);
 }
 
+// Geometry::get_shift<Rest>(origin, 0, raydir, c, Z, false) of a pixel ray (motionless
+// origin): 1 + v[c] . d, or in spherical symmetry 1 + v_x[c] (origin . d + Z) / x[c]
+// (geometry.tpp:407-417; 1 at x[c] = 0).
+static __host__ __device__ __forceinline__ double image_shift(const DevModel& m, const double* org,
+                                                              const ImagePlane& ip, uint32_t c, double Z) {
+    if (ip.sph) {
+        const double xc = m.pos[c].x;
+        if (xc == 0.0) return 1.0;
+        const double RcZ = dadd_rn(dot3_rn(org[0], org[1], org[2], ip.d[0], ip.d[1], ip.d[2]), Z);
+        return dadd_rn(1.0, ddiv_rn(dmul_rn(m.vel[c].x, RcZ), xc));
+    }
+    const double4_32a v = m.vel[c];
+    return dadd_rn(1.0, dot3_rn(v.x, v.y, v.z, ip.d[0], ip.d[1], ip.d[2]));
+}
+
 // Solver::trace_ray_imaging (solver.tpp:841-897), increment -1: walks from the start
 // boundary point through the model until it leaves on the far side; rest-frame
 // shifts 1 + v . d of a motionless observer.  Returns the steps stored, 0 if the ray
@@ -88,6 +104,42 @@ static __device__ int trace_image(const DevModel& m, const double* org, const Im
     uint32_t crt = start;
     int count = 0;
     bool accessed = false;
+    if (ip.sph) {
+        // Geometry::get_next_spherical_symmetry from the pixel origin (every lane steps the
+        // same shells; lane 0 stores each step with its shift at its distance Z)
+        const double Rcos = dot3_rn(org[0], org[1], org[2], dx, dy, dz);
+        const double Rsin2 = dsub_rn(dot3_rn(org[0], org[1], org[2], org[0], org[1], org[2]), dmul_rn(Rcos, Rcos));
+        while (true) {
+            uint32_t nxt;
+            double dZl;
+            if (!next_point_sph(m, Rcos, Rsin2, crt, Z, nxt, dZl)) break;
+            if (STORE && (uint32_t)count >= cap) {
+                if (lane == 0) atomicOr(status, ST_CAPACITY);
+                count = -1;
+                break;
+            }
+            Z = dadd_rn(Z, dZl);
+            if (STORE && lane == 0) {
+                h.ids[count] = nxt;
+                h.eid[count] = sph_eid(crt, nxt);
+                h.dZ[count] = dZl;
+                const double sh = image_shift(m, org, ip, nxt, Z);
+                h.shift[count] = sh;
+                h.dsh[count] = (float)dsub_rn(sh, 1.0);
+                h.dzs[count] = (float)dZl * m.dz_scale;
+            }
+            count++;
+            if (m.p2b[nxt] != m.P) {
+                const double4_32a pn = m.pos[nxt];
+                const double side = dot3_rn(dsub_rn(pn.x, ip.center[0]), dsub_rn(pn.y, ip.center[1]),
+                                            dsub_rn(pn.z, ip.center[2]), dx, dy, dz);
+                if (!(side < 0.0)) break;
+            }
+            crt = nxt;
+        }
+        __syncwarp();
+        return count;  // spherically symmetric models keep boundary-only rays (solver.tpp:891-896)
+    }
     while (true) {
         const uint32_t nnb = m.n_nb[crt];
         const uint32_t cum = m.cum_nb[crt];
@@ -173,6 +225,13 @@ static __device__ uint32_t pixel_start(const DevModel& m, const double* org, con
     }
     const double4_32a ps = m.pos[p];
     Z = dot3_rn(dsub_rn(ps.x, org[0]), dsub_rn(ps.y, org[1]), dsub_rn(ps.z, org[2]), ip.d[0], ip.d[1], ip.d[2]);
+    if (ip.sph) {
+        // Geometry::get_distance_origin_to_boundary in spherical symmetry (geometry.tpp:172-190)
+        const double Rcos = dot3_rn(org[0], org[1], org[2], ip.d[0], ip.d[1], ip.d[2]);
+        const double Rsin2 = dsub_rn(dot3_rn(org[0], org[1], org[2], org[0], org[1], org[2]), dmul_rn(Rcos, Rcos));
+        const double horz2 = dsub_rn(sqnorm_rn(ps), Rsin2);
+        Z = horz2 > 0 ? dsub_rn(-dsqrt_rn(horz2), Rcos) : -Rcos;
+    }
     return p;
 }
 
@@ -209,7 +268,7 @@ inline void plane_axes(const double* d, double& ix, double& iy, double& jx, doub
 // [P][3] and point2boundary map (host computation; err receives the message).
 inline int image_plane_compute(const double* pos, const uint32_t* p2b, uint32_t P, uint32_t B, const double* raydir,
                                uint32_t nx, uint32_t ny, ImagePlane& ip, std::vector<double>& hx,
-                               std::vector<double>& hy, std::string& err) {
+                               std::vector<double>& hy, std::string& err, bool sph = false) {
     if (!raydir || nx == 0 || ny == 0) {
         err = "null direction or empty image";
         return MGR_ERR_ARGUMENT;
@@ -233,6 +292,12 @@ inline int image_plane_compute(const double* pos, const uint32_t* p2b, uint32_t 
     for (uint32_t b = 0; b < B; b++) {
         const double* x = pos + 3 * (size_t)b2p[b];
         double X, Y;
+        if (sph) {
+            // 1D (image.cpp:257-269): the boundary shells' x, mirrored below
+            min_x = std::fmin(min_x, x[0]);
+            max_x = std::fmax(max_x, x[0]);
+            continue;
+        }
         if (ip.tilted) {
             X = ip.ix * x[0] + ip.iy * x[1];
             Y = ip.jx * x[0] + ip.jy * x[1] + ip.jz * x[2];
@@ -252,6 +317,12 @@ inline int image_plane_compute(const double* pos, const uint32_t* p2b, uint32_t 
         const double* x = pos + 3 * (size_t)p;
         return (ip.d[0] * x[0] + ip.d[1] * x[1]) + ip.d[2] * x[2];
     };
+    if (sph) {
+        max_x = std::fmax(std::fabs(min_x), max_x);
+        min_x = -max_x;
+        min_y = min_x;
+        max_y = max_x;
+    }
     uint32_t cbp = p2b[0] < P ? p2b[0] : (B ? b2p[0] : 0);
     double pmin = proj(cbp);
     for (uint32_t b = 1; b < B; b++) {
@@ -261,8 +332,12 @@ inline int image_plane_compute(const double* pos, const uint32_t* p2b, uint32_t 
             pmin = pd;
         }
     }
+    // spherical symmetry: the last point, and the plane at -x of it (geometry.tpp:348-350,
+    // image.cpp:341-346)
+    if (sph) cbp = P - 1;
     ip.start = cbp;
-    const double dist = proj(cbp);
+    ip.sph = sph;
+    const double dist = sph ? -pos[3 * (size_t)cbp] : proj(cbp);
     for (int k = 0; k < 3; k++) ip.scp[k] = ip.d[k] * dist;
     double lo[3] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308};
     double hi[3] = {-1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308};

@@ -1321,8 +1321,20 @@ static uint32_t bdy_point_closer(const OrcModel* m, const double* origin, const 
     return next;
 }
 
+/* Geometry::get_shift<Rest>(origin, 0, raydir, c, Z, false) of a pixel ray (motionless
+ * origin): 1 + v[c] . raydir, or in spherical symmetry 1 + v_x[c] (origin . raydir + Z)
+ * / x[c] (geometry.tpp:407-417, 1 at x[c] = 0). */
+static inline double image_shift(const OrcModel* m, const double* origin, const double* d, uint32_t c, double Z) {
+    if (m->spherical_symmetry) {
+        const double xc = m->position[3 * c];
+        if (xc == 0.0) return 1.0;
+        return 1.0 + m->velocity[3 * c] * (dot3(origin[0], origin[1], origin[2], d) + Z) / xc;
+    }
+    return 1.0 + dot3(m->velocity[3 * c], m->velocity[3 * c + 1], m->velocity[3 * c + 2], d);
+}
+
 /* Solver::trace_ray_imaging (solver.tpp:841-897), increment -1, Rest frame with a
- * motionless origin: shift = 1 + v . raydir. */
+ * motionless origin. */
 static int64_t trace_imaging(const OrcModel* m, Buf* b, const double* origin, uint32_t start, const double* d,
                              double* Z, int64_t id1, int64_t id2, const double* center, int* err) {
     double dZ = 0.0;
@@ -1330,9 +1342,9 @@ static int64_t trace_imaging(const OrcModel* m, Buf* b, const double* origin, ui
     uint32_t nxt = get_next(m, origin, d, start, Z, &dZ);
     int accessed = 0;
     const int64_t original_id1 = id1;
-#define SHIFT_REST(c) (1.0 + dot3(m->velocity[3 * (c)], m->velocity[3 * (c) + 1], m->velocity[3 * (c) + 2], d))
+#define SHIFT_REST(c) image_shift(m, origin, d, (c), *Z)
     if (valid_point(m, nxt)) {
-        double shift_crt = SHIFT_REST(crt);
+        double shift_crt = image_shift(m, origin, d, crt, *Z - dZ);
         double shift_nxt = SHIFT_REST(nxt);
         set_data(m, b, UINT32_MAX, crt, nxt, shift_crt, shift_nxt, dZ, -1, &id1, &id2, err);
         while (!*err && (not_on_boundary(m, nxt) ||
@@ -1348,7 +1360,8 @@ static int64_t trace_imaging(const OrcModel* m, Buf* b, const double* origin, ui
         }
     }
 #undef SHIFT_REST
-    if (!accessed) return original_id1; /* no spherical symmetry here */
+    /* spherically symmetric models keep boundary-only rays (solver.tpp:891-896) */
+    if (!accessed && !m->spherical_symmetry) return original_id1;
     return id1;
 }
 
@@ -1371,7 +1384,6 @@ static int image_new_impl(const OrcModel* m, const double* raydir_in, uint32_t n
     const uint32_t P = m->npoints, F = m->nfreqs;
     const double n2 = raydir_in[0] * raydir_in[0] + raydir_in[1] * raydir_in[1] + raydir_in[2] * raydir_in[2];
     if (n2 == 0.0) return -1;
-    if (m->spherical_symmetry) return -4; /* the 1D projection-plane imager is not restated */
     const double inv = 1 / sqrt(n2);
     const double d[3] = {raydir_in[0] * inv, raydir_in[1] * inv, raydir_in[2] * inv};
     /* Image::set_coordinates_projection_surface (image.cpp:221-366), 3D */
@@ -1388,6 +1400,12 @@ static int image_new_impl(const OrcModel* m, const double* raydir_in, uint32_t n
         const uint32_t p = b2p[bi];
         const double* x = m->position + 3 * p;
         double X, Y;
+        if (m->spherical_symmetry) {
+            /* 1D (image.cpp:257-269): the boundary shells' x, mirrored below */
+            if (x[0] > max_x) max_x = x[0];
+            if (x[0] < min_x) min_x = x[0];
+            continue;
+        }
         if (den >= 1.0e-9) {
             X = ix * x[0] + iy * x[1];
             Y = jx * x[0] + jy * x[1] + jz * x[2];
@@ -1400,9 +1418,19 @@ static int image_new_impl(const OrcModel* m, const double* raydir_in, uint32_t n
         if (Y < min_y) min_y = Y;
         if (Y > max_y) max_y = Y;
     }
-    const uint32_t cbp = closest_bdy_point_in_raydir(m, b2p, d);
+    if (m->spherical_symmetry) {
+        max_x = fabs(min_x) > max_x ? fabs(min_x) : max_x;
+        min_x = -max_x;
+        min_y = min_x;
+        max_y = max_x;
+    }
+    /* get_closest_bdy_point_in_custom_raydir: the last point in spherical symmetry
+     * (geometry.tpp:346-350); the plane at -x of it there (image.cpp:341-346) */
+    const uint32_t cbp = m->spherical_symmetry ? P - 1 : closest_bdy_point_in_raydir(m, b2p, d);
     free(b2p);
-    const double dist  = dot3(m->position[3 * cbp], m->position[3 * cbp + 1], m->position[3 * cbp + 2], d);
+    const double dist  = m->spherical_symmetry
+                             ? -m->position[3 * cbp]
+                             : dot3(m->position[3 * cbp], m->position[3 * cbp + 1], m->position[3 * cbp + 2], d);
     const double scp[3] = {d[0] * dist, d[1] * dist, d[2] * dist};
     const double deltax = (max_x - min_x) / nx, deltay = (max_y - min_y) / ny;
     for (uint32_t xi = 0; xi < nx; xi++)
@@ -1453,12 +1481,19 @@ static int image_new_impl(const OrcModel* m, const double* raydir_in, uint32_t n
             int err = 0;
             int64_t first = 0;
             while (1) {
+                /* Geometry::get_distance_origin_to_boundary (geometry.tpp:167-193) */
                 double Z = dot3(m->position[3 * start] - origin[0], m->position[3 * start + 1] - origin[1],
                                 m->position[3 * start + 2] - origin[2], d);
+                if (m->spherical_symmetry) {
+                    const double Rcos  = dot3(origin[0], origin[1], origin[2], d);
+                    const double R2    = origin[0] * origin[0] + origin[1] * origin[1] + origin[2] * origin[2];
+                    const double Rsin2 = R2 - Rcos * Rcos;
+                    const double horz2 = sqnorm(m->position + 3 * start) - Rsin2;
+                    Z = horz2 > 0 ? -sqrt(horz2) - Rcos : -Rcos;
+                }
                 const uint32_t c = b.centre;
                 b.nr[c]    = start;
-                b.shift[c] = 1.0 + dot3(m->velocity[3 * start], m->velocity[3 * start + 1],
-                                        m->velocity[3 * start + 2], d);
+                b.shift[c] = image_shift(m, origin, d, start, Z);
                 err   = 0;
                 first = trace_imaging(m, &b, origin, start, d, &Z, (int64_t)c - 1, (int64_t)c - 1, center, &err) + 1;
                 if (err != 1) break;

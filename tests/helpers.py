@@ -182,3 +182,39 @@ def ray_angles(raw):
     """The first hnrays rays' angles arctan2(y, x), as the 1D benchmarks take them."""
     d = raw.ray_direction[: raw.nrays // 2]
     return np.arctan2(d[:, 1], d[:, 0])
+
+
+def velocity_gradient_1d_image_solution(raw, nu, imx, imy):
+    """I [pixel][freq] of tests/benchmarks/analytic/constant_velocity_gradient_1D_new_imager.py:117-165:
+    the image along +y of the 1D velocity gradient, at impact parameter r = |(x, y)|, the
+    frequency measured from the outer edge's Doppler shift."""
+    from scipy.special import erf
+
+    npoints = raw.npoints
+    dx, dv = 1.0e4, 2.5e2 / CC
+    L, vmax = dx * npoints, dv * npoints
+    ld = raw.linedata[0]
+    frq, chi, src, dnu = _line_constants(ld, 45.0, 1.0e8, 0.0)
+    r_in, r_out = raw.position[0, 0], raw.position[-1, 0]
+
+    def z_max(r, theta):
+        if r >= r_out:
+            return 0.0
+        if theta < np.arcsin(r_in / r):
+            return r * np.cos(theta) - np.sqrt(r_in**2 - (r * np.sin(theta)) ** 2)
+        return r * np.cos(theta) + np.sqrt(L**2 - (r * np.sin(theta)) ** 2)
+
+    def tau(f, r, theta):
+        l = float(z_max(r, theta))
+        arg = float((f - frq) / dnu)
+        fct = float(vmax * f / dnu)
+        up = chi * L / (fct * dnu) * 0.5 * (erf(arg) - erf(arg - fct * l / L))
+        down = chi * L / (-fct * dnu) * 0.5 * (erf(arg) - erf(arg + fct * l / L))
+        return up + down
+
+    def I_im(f, r):
+        f = f + vmax / CC * frq
+        return src + (planck(S.T_CMB, f) - src) * np.exp(-tau(f, r, 0.5 * np.pi))
+
+    rs = np.sqrt(imx**2 + imy**2)
+    return np.array([[I_im(f, r) for f in nu] for r in rs])

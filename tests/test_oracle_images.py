@@ -172,3 +172,20 @@ def test_set_column_known_answers(built):
     r1, r2 = rng.uniform(1, 2, a3["npoints"]), rng.uniform(1, 2, a3["npoints"])
     c1, c2, c12 = o3.set_column(r1), o3.set_column(r2), o3.set_column(2.0 * r1 + 3.0 * r2)
     np.testing.assert_allclose(c12, 2.0 * c1 + 3.0 * c2, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("mwf, bound", [(0.5, 1.6e-5), (0.35, 1.2e-5), (0.10, 3.3e-7)])
+def test_new_imager_constant_velocity_gradient_1d(mwf, bound):
+    """tests/benchmarks/analytic/constant_velocity_gradient_1D_new_imager.py:86-165, 220-226:
+    the projection-plane imager on the 1D spherically symmetric velocity gradient (50
+    shells, 4 rays, image along ray hnrays-1 = +y, 50 x 50 pixels, 10 frequencies over
+    +-10 km/s): max relative error against the closed form below the reference's bound
+    for each max_width_fraction setting (all pixels but the last)."""
+    raw = S.velocity_gradient_1d(npoints=50, nrays=4, nquads=10)
+    fcen = raw.linedata[0].frequency[0]
+    dd = 1.0e4 / H.CC
+    a = H.setup(raw, max_width_fraction=mwf, image_freqs=(fcen - fcen * dd, fcen + fcen * dd, 10))
+    d = raw.ray_direction[raw.nrays // 2 - 1]
+    r = O.Oracle(a).image_new(d, 50, 50)
+    ana = H.velocity_gradient_1d_image_solution(raw, a["nu"][0], r["ImX"], r["ImY"])
+    assert np.max(np.abs(H.relative_error(r["I"], ana))[:-1]) < bound
