@@ -473,7 +473,6 @@ extern "C" int mgr_emu_image(const MgrModelDesc* d, int precision, uint32_t rr, 
 #pragma omp for schedule(dynamic, 16)
         for (long long oo = 0; oo < (long long)P; oo++) {
             const uint32_t o = (uint32_t)oo;
-            const double* dd = m.raydir + 3 * rr;
             const uint32_t ar = m.antipod[rr];
             const double shb = origin_shift(m, 1, o, rr);
             const double shf = origin_shift(m, 1, o, ar);

@@ -32,7 +32,6 @@ __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, ui
     for (uint32_t i = threadIdx.x; i < m.L; i += blockDim.x) sl[i] = m.sorted_line[i];
     __syncthreads();
     const uint32_t ar = m.antipod[rr];
-    const double* d = m.raydir + 3 * rr;
     for (uint32_t o = blockIdx.x * nw + w; o < m.P; o += gridDim.x * nw) {
         // Geometry::get_shift<Rest, false>(o, r, o, 0): the origin's shift along each
         // half's own ray (the antipode's is reversed), the element's that of rr
