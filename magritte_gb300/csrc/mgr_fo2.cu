@@ -164,7 +164,7 @@ __global__ void ray_lengths_kernel(DevModel m, uint32_t cap, uint32_t* d_max, in
 // MINB = CTAs of 256 threads resident per SM the register budget is sized for
 // (2: 128, 3: 80, 4: 64 registers per thread); picked at run time by the tuner.
 // UV: also v (solve_feautrier_order_2_uv), written to V with U's layout.
-template <int MODE, int AP, int MINB, bool UV = false>
+template <int MODE, int AP, int MINB, bool UV = false, int GEO = 0>
 __global__ void __launch_bounds__(256, MINB)
     fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                double* __restrict__ U, size_t u_stride, uint32_t u_o0, double* __restrict__ LD, size_t ld_stride,
@@ -185,8 +185,8 @@ __global__ void __launch_bounds__(256, MINB)
     for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
         const uint32_t o = o_begin + (uint32_t)(item / nR);
         const uint32_t rr = rr0 + (uint32_t)(item % nR);
-        const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-        const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+        const int nb = trace_half<true, 0, GEO>(m, o, rr, cap, bk, lane, status);
+        const int nf = trace_half<true, 0, GEO>(m, o, m.antipod[rr], cap, fw, lane, status);
         if (nb < 0 || nf < 0) continue;  // status recorded by the trace
         double* Ui = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
         double* Li = LD ? LD + (size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F : nullptr;
@@ -506,7 +506,7 @@ size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, b
     return chunk * per;
 }
 
-template <int MODE, int AP, int MINB, bool UV = false>
+template <int MODE, int AP, int MINB, bool UV = false, int GEO = 0>
 static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                                       double* U, size_t u_stride, uint32_t u_o0, double* LD, size_t ld_stride,
                                       uint32_t ld_o0, double* V = nullptr) {
@@ -516,7 +516,7 @@ static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_
     if (nw > 8) nw = 8;
     const uint32_t Lpad = (m.L + 1) & ~1u;
     const size_t smem = (size_t)Lpad * 8 + (size_t)nw * half_bytes_per_warp(cap);
-    auto kern = fo2_kernel<MODE, AP, MINB, UV>;
+    auto kern = fo2_kernel<MODE, AP, MINB, UV, GEO>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -537,6 +537,9 @@ static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_
 template <int MODE, int AP>
 static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                                    double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo) {
+    // spherical symmetry and adaptive rays: the run-time geometry variant, one tile
+    if (model->dm.sph || model->dm.adaptive)
+        return launch_fo2_variant<MODE, AP, 3, false, 1>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
     const int minb = (MODE == MODE_SPLIT) ? model->fo2_minb_split : model->fo2_minb_fp64;
     if (minb == 2) return launch_fo2_variant<MODE, AP, 2>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
     if (minb == 4) return launch_fo2_variant<MODE, AP, 4>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
@@ -549,13 +552,13 @@ static cudaError_t launch_fo2_uv(MgrModel* model, uint32_t o_begin, uint32_t o_e
                                  double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo, double* V) {
     switch (model->dm.approx) {
         case APPROX_ONELINE:
-            return launch_fo2_variant<MODE, APPROX_ONELINE, 3, true>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls,
+            return launch_fo2_variant<MODE, APPROX_ONELINE, 3, true, 1>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls,
                                                                      lo, V);
         case APPROX_CLOSELINES:
-            return launch_fo2_variant<MODE, APPROX_CLOSELINES, 3, true>(model, o_begin, o_end, rr0, nR, U, us, uo, LD,
+            return launch_fo2_variant<MODE, APPROX_CLOSELINES, 3, true, 1>(model, o_begin, o_end, rr0, nR, U, us, uo, LD,
                                                                         ls, lo, V);
         default:
-            return launch_fo2_variant<MODE, APPROX_NONE, 3, true>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls,
+            return launch_fo2_variant<MODE, APPROX_NONE, 3, true, 1>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls,
                                                                   lo, V);
     }
 }

@@ -178,13 +178,15 @@ __device__ int trace_half_sph(const DevModel& m, uint32_t o, uint32_t r, uint32_
 // FRAME 0: comoving shifts relative to the origin point (the formal solves);
 // FRAME 1: rest-frame shifts of the old imager (Geometry::get_shift<Rest>, reversed for
 // r >= hnrays, geometry.tpp:428-465).
-template <bool STORE, int FRAME = 0>
+// GEO 0 compiles the general geometry with shared rays only (the caller has checked the
+// model); GEO 1 handles every geometry at run time.
+template <bool STORE, int FRAME = 0, int GEO = 1>
 __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int lane,
                           int* status) {
-    if (m.sph) return trace_half_sph<STORE, FRAME>(m, o, r, cap, h, lane, status);
+    if (GEO && m.sph) return trace_half_sph<STORE, FRAME>(m, o, r, cap, h, lane, status);
     // the formal solves trace along the origin's (adaptive) directions, the old imager
     // along the shared ones (trace_ray<Rest, false>, solver.tpp:550-552)
-    const double* d = FRAME ? m.raydir + 3 * r : ray_dir(m, o, r);
+    const double* d = (FRAME || !GEO) ? m.raydir + 3 * r : ray_dir(m, o, r);
     const double dx = d[0], dy = d[1], dz = d[2];
     const double4_32a po = m.pos[o];
     double Z = 0.0;
