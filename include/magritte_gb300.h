@@ -332,12 +332,14 @@ int mgr_image_new_adjoint_device(MgrModel* model, const double* raydir, uint32_t
  * (Model::compute_radiation_field_feautrier_order_2, src/model/model.cpp:353-390);
  * a batch runs that call for many independent models in one persistent kernel
  * launch.  Each model's J and ALO diagonal equal those of its own
- * mgr_formal_solve_fo2 (same lane code, same order of the sums). */
+ * mgr_formal_solve_fo2 (same lane code, same order of the sums; in FP64 mode up to a
+ * differently contracted multiply-add, a few ulp). */
 typedef struct MgrBatch MgrBatch;
 
 /* Collects n_models models (same device, same line approximation, line spectral
- * discretisations) into a batch.  The models stay owned by the caller and must
- * outlive the batch; their line data may change between solves. */
+ * discretisations, general geometry with shared rays: spherically symmetric models and
+ * adaptive rays give MGR_ERR_UNSUPPORTED) into a batch.  The models stay owned by the
+ * caller and must outlive the batch; their line data may change between solves. */
 int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out);
 void mgr_batch_free(MgrBatch* batch);
 

@@ -99,8 +99,9 @@ __global__ void __launch_bounds__(256, MINB)
                 if (m.in_line[f]) LF[f] = lambda_factors(m, sl, o, f);
         __syncwarp();
         for (uint32_t rr = 0; rr < m.hnrays && ok; rr++) {
-            const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-            const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+            // general geometry with shared rays (mgr_batch_create refuses the other kinds)
+            const int nb = trace_half<true, 0, 0>(m, o, rr, cap, bk, lane, status);
+            const int nf = trace_half<true, 0, 0>(m, o, m.antipod[rr], cap, fw, lane, status);
             if (nb < 0 || nf < 0) {  // status recorded by the trace
                 ok = false;
                 break;
@@ -270,6 +271,13 @@ int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out)
         if (!m->line_disc) {
             delete b;
             set_error("mgr_batch_create: model " + std::to_string(i) + " has no line spectral discretisation");
+            return MGR_ERR_UNSUPPORTED;
+        }
+        if (m->dm.sph || m->dm.adaptive) {
+            delete b;
+            set_error("mgr_batch_create: model " + std::to_string(i) +
+                      " is spherically symmetric or has adaptive rays; batches take general-geometry models with "
+                      "shared rays (solve such models with mgr_formal_solve_fo2)");
             return MGR_ERR_UNSUPPORTED;
         }
         b->cap = std::max(b->cap, m->half_cap);

@@ -94,3 +94,16 @@ def test_batch_rejects_mixed_approximations(gpu_lib):
     finally:
         da.close()
         db.close()
+
+
+def test_batch_refuses_other_geometries(gpu_lib):
+    """Batches take general-geometry models with shared rays; a spherically symmetric
+    model is refused with an error (it is solved by its own mgr_formal_solve_fo2)."""
+    devs = [_abi.DeviceModel(H.setup(S.grid_cube(n=6, nquads=3))),
+            _abi.DeviceModel(H.setup(S.density_distribution_1d("a", npoints=20, nrays=8, nquads=3)))]
+    try:
+        with pytest.raises(_abi.MgrError, match="spherically symmetric"):
+            _abi.Batch(devs)
+    finally:
+        for d in devs:
+            d.close()
