@@ -739,6 +739,124 @@ static void update_lambda(const OrcModel* m, Buf* b, uint32_t rr, uint32_t f, do
     if (lambda_has) lambda_has[(size_t)p * m->nlines + lid] = 1;
 }
 
+/* Solver::solve_feautrier_order_2 with n_off_diag > 0 (solver.tpp:2193-2298 and the
+ * banded branch :2319-2355) for one (o, rr, f): the elimination of the whole ray, then
+ * L_diag on every element and the off-diagonal bands L_upper(m, n) / L_lower(m, n) of
+ * the inverse Feautrier matrix.  Rows are elements first .. last (index n - first);
+ * A and C are the reference's per-row coefficients (A[first], C[last] unused), the
+ * bands [n_off_diag][n_tot] row-major (entries the reference does not set stay 0). */
+static void feautrier_bands(const OrcModel* m, Buf* b, uint32_t o, uint32_t f, uint32_t n_off_diag, double* Aout,
+                            double* Cout, double* Ld, double* Lu, double* Ll) {
+    const double freq  = m->nu[(size_t)o * m->nfreqs + f];
+    const uint32_t l   = m->corr_line[f];
+    const uint32_t first = b->first, last = b->last;
+    const uint32_t N     = last + 1 - first;
+    double chi_c = 0.0, chi_n = 0.0, dtau_c, dtau_n = 0.0, term_c = 0.0, term_n = 0.0;
+    int cco = 1;
+    double* Su = b->Su; double* A = b->A; double* C = b->C; double* iA = b->inverse_A;
+    double* iC = b->inverse_C; double* FF = b->FF; double* FI = b->FI; double* GG = b->GG;
+    double* GP = b->GP;
+    double* GI = (double*)calloc(b->length, sizeof(double));
+    double* LD = (double*)calloc(b->length, sizeof(double));
+
+    compute_source_dtau(m, b->nr[first], b->nr[first + 1], b->nr_interp[first], b->nr_interp[first + 1], l,
+                        freq * b->shift[first], freq * b->shift[first + 1], b->shift[first],
+                        b->shift[first + 1], b->dZ[first], b->interp_factor[first],
+                        b->interp_factor[first + 1], &cco, &dtau_n, &chi_c, &chi_n, &term_c, &term_n);
+    const double inverse_dtau_f = 1.0 / dtau_n;
+    C[first]                    = 2.0 * inverse_dtau_f * inverse_dtau_f;
+    const double Bf_min_Cf      = 1.0 + 2.0 * inverse_dtau_f;
+    const double Bf             = Bf_min_Cf + C[first];
+    FF[first] = 0.5 * Bf_min_Cf * dtau_n * dtau_n;
+    FI[first] = 1.0 / (1.0 + FF[first]);
+    for (uint32_t n = first + 1; n < last; n++) {
+        term_c = term_n;
+        dtau_c = dtau_n;
+        chi_c  = chi_n;
+        compute_source_dtau(m, b->nr[n], b->nr[n + 1], b->nr_interp[n], b->nr_interp[n + 1], l,
+                            freq * b->shift[n], freq * b->shift[n + 1], b->shift[n], b->shift[n + 1],
+                            b->dZ[n], b->interp_factor[n], b->interp_factor[n + 1], &cco, &dtau_n,
+                            &chi_c, &chi_n, &term_c, &term_n);
+        const double dtau_avg = 0.5 * (dtau_c + dtau_n);
+        iA[n] = dtau_avg * dtau_c;
+        iC[n] = dtau_avg * dtau_n;
+        A[n]  = 1.0 / iA[n];
+        C[n]  = 1.0 / iC[n];
+        FF[n] = (A[n] * FF[n - 1] * FI[n - 1] + 1.0) * iC[n];
+        FI[n] = 1.0 / (1.0 + FF[n]);
+    }
+    const double inverse_dtau_l = 1.0 / dtau_n;
+    A[last]                     = 2.0 * inverse_dtau_l * inverse_dtau_l;
+    const double Bl_min_Al      = 1.0 + 2.0 * inverse_dtau_l;
+    const double Bl             = Bl_min_Al + A[last];
+
+    GG[last] = 0.5 * Bl_min_Al * dtau_n * dtau_n;
+    GI[last] = 1.0 / (1.0 + GG[last]);
+    GP[last] = GG[last] * GI[last];
+    LD[last] = (1.0 + FF[last - 1]) / (Bl_min_Al + Bl * FF[last - 1]);
+    for (int64_t n = (int64_t)last - 1; n > (int64_t)first; n--) {
+        GG[n] = (C[n] * GP[n + 1] + 1.0) * iA[n];
+        GI[n] = 1.0 / (1.0 + GG[n]);
+        GP[n] = GG[n] * GI[n];
+        LD[n] = iC[n] / (FF[n] + GP[n + 1]);
+    }
+    LD[first] = (1.0 + GG[first + 1]) / (Bf_min_Cf + Bf * GG[first + 1]);
+    for (int64_t n = (int64_t)last - 1; n >= (int64_t)first; n--) {
+        if (n_off_diag > 0) {
+            Lu[0 * (size_t)N + (n + 1 - first)] = LD[n + 1] * FI[n];
+            Ll[0 * (size_t)N + (n - first)]     = LD[n] * GI[n + 1];
+        }
+    }
+    for (uint32_t mm = 1; mm < n_off_diag && mm < N - 1; mm++)
+        for (int64_t n = (int64_t)last - 1 - mm; n >= (int64_t)first; n--) {
+            Lu[(size_t)mm * N + (n + mm + 1 - first)] = Lu[(size_t)(mm - 1) * N + (n + mm + 1 - first)] * FI[n];
+            Ll[(size_t)mm * N + (n - first)]          = Ll[(size_t)(mm - 1) * N + (n - first)] * GI[n + mm + 1];
+        }
+    for (uint32_t n = 0; n < N; n++) {
+        Ld[n]   = LD[first + n];
+        Aout[n] = A[first + n];
+        Cout[n] = C[first + n];
+    }
+    free(GI);
+    free(LD);
+}
+
+/* The banded ALO of one ray pair (o, rr) at frequency f, traced for f's line as the
+ * formal solve traces it.  *n_tot receives the element count; A, C, L_diag [capacity],
+ * L_upper, L_lower [n_off_diag][capacity] are written (zeroed first) when n_tot fits
+ * capacity and exceeds 2.  Returns -3 when it does not fit. */
+int orc_feautrier_bands(const OrcModel* m, uint32_t o, uint32_t rr, uint32_t f, uint32_t n_off_diag,
+                        uint32_t* n_tot, double* A, double* C, double* L_diag, double* L_upper, double* L_lower,
+                        uint32_t capacity) {
+    const uint32_t length = 2 * orc_ray_lengths_max(m, 1) + 1;
+    Buf b;
+    if (buf_init(&b, length) != 0) return -1;
+    const uint32_t c = b.centre;
+    int err          = 0;
+    b.nr[c]          = o;
+    b.shift[c]       = 1.0;
+    const uint32_t l = m->corr_line[f];
+    const int64_t first = trace(m, &b, 0, l, o, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
+    const int64_t last  = trace(m, &b, 0, l, o, m->antipod[rr], +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
+    if (err) {
+        buf_free(&b);
+        return -2;
+    }
+    b.first = (uint32_t)first;
+    b.last  = (uint32_t)last;
+    b.n_tot = (uint32_t)(last + 1 - first);
+    *n_tot  = b.n_tot;
+    int rc  = 0;
+    if (b.n_tot > capacity) rc = -3;
+    else if (b.n_tot > 2) {
+        memset(L_upper, 0, sizeof(double) * (size_t)n_off_diag * capacity);
+        memset(L_lower, 0, sizeof(double) * (size_t)n_off_diag * capacity);
+        feautrier_bands(m, &b, o, f, n_off_diag, A, C, L_diag, L_upper, L_lower);
+    }
+    buf_free(&b);
+    return rc;
+}
+
 /* ------------------------------------------------------------------ */
 /* Public traces                                                       */
 /* ------------------------------------------------------------------ */

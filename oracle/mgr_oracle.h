@@ -156,6 +156,11 @@ int orc_image_for_point(const OrcModel* m, uint32_t rr, uint32_t p, uint32_t* n_
                         double* u, uint32_t capacity);
 /* Solver::set_column (solver.tpp:2953-2991): column [nrays][P] from density [P]. */
 int orc_set_column(const OrcModel* m, const double* density, double* column, int nthreads);
+/* Solver::solve_feautrier_order_2 with n_off_diag > 0 (solver.tpp:2319-2355): L_diag and
+ * the off-diagonal bands of one ray pair at one frequency (see mgr_oracle.c). */
+int orc_feautrier_bands(const OrcModel* m, uint32_t o, uint32_t rr, uint32_t f, uint32_t n_off_diag,
+                        uint32_t* n_tot, double* A, double* C, double* L_diag, double* L_upper, double* L_lower,
+                        uint32_t capacity);
 int orc_image_optical_depth_new(const OrcModel* m, const double* raydir, uint32_t nx, uint32_t ny, double* I,
                                 double* ImX, double* ImY, int nthreads);
 

@@ -437,6 +437,32 @@ class Oracle:
             raise RuntimeError(f"oracle image_for_point failed ({rc})")
         return out
 
+    def feautrier_bands(self, o, rr, f, n_off_diag):
+        """Solver::solve_feautrier_order_2 with n_off_diag > 0 (solver.tpp:2319-2355) for one
+        ray pair and frequency: A, C, L_diag [n_tot] and L_upper, L_lower [n_off_diag][n_tot]
+        indexed from the first element (None for a ray of at most two elements)."""
+        l = lib()
+        l.orc_feautrier_bands.restype = C.c_int
+        l.orc_feautrier_bands.argtypes = [C.POINTER(OrcModel), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                          C.POINTER(C.c_uint32), _f64p, _f64p, _f64p, _f64p, _f64p, C.c_uint32]
+        n = C.c_uint32(0)
+        z = np.zeros(1)
+        rc = l.orc_feautrier_bands(C.byref(self.m), o, rr, f, n_off_diag, C.byref(n), _ptr(z, _f64p),
+                                   _ptr(z, _f64p), _ptr(z, _f64p), _ptr(z, _f64p), _ptr(z, _f64p), 0)
+        if rc not in (0, -3):
+            raise RuntimeError(f"oracle feautrier_bands failed ({rc})")
+        N = n.value
+        if N <= 2:
+            return None
+        out = dict(A=np.zeros(N), C=np.zeros(N), L_diag=np.zeros(N), L_upper=np.zeros((n_off_diag, N)),
+                   L_lower=np.zeros((n_off_diag, N)))
+        rc = l.orc_feautrier_bands(C.byref(self.m), o, rr, f, n_off_diag, C.byref(n), _ptr(out["A"], _f64p),
+                                   _ptr(out["C"], _f64p), _ptr(out["L_diag"], _f64p), _ptr(out["L_upper"], _f64p),
+                                   _ptr(out["L_lower"], _f64p), N)
+        if rc != 0:
+            raise RuntimeError(f"oracle feautrier_bands failed ({rc})")
+        return out
+
     def set_column(self, density, nthreads=0):
         """Solver::set_column (solver.tpp:2953-2991): column [nrays][P]."""
         P, R = self.a["npoints"], self.a["nrays"]

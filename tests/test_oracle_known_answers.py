@@ -175,3 +175,45 @@ def test_adaptive_ray_layout_with_shared_rays_is_identical(built):
     np.testing.assert_array_equal(oi.set_column(rho), o0.set_column(rho))
     ra = O.Oracle(H.setup(S.with_adaptive_rays(raw))).formal_solve_fo2()
     assert H.max_rel(ra["J"], r0["J"]) > 1e-3
+
+
+def test_banded_alo_is_the_inverse_feautrier_matrix(built):
+    """tests/test_solver_lambda.cpp:15-88: with n_off_diag > 0 the ALO's diagonal and its
+    off-diagonal bands (solver.tpp:2319-2355) are those of the inverse of the Feautrier
+    matrix T, built from the rows' A and C with the boundary rows
+    1 + C + 2 sqrt(C/2) and 1 + A + 2 sqrt(A/2).  The oracle's restatement of the
+    banded ALO is checked against numpy's inverse of T on rays of a 3D grid (with
+    interpolation points) and of a 1D spherical model, where T is well conditioned
+    (cond < 1e8: rows with optical depths near min_dtau make T singular to FP64)."""
+    n_off = 3
+    checked = 0
+    for raw in (S.grid_cube(n=10, nquads=5), S.velocity_gradient_1d(npoints=30, nrays=8, nquads=5)):
+        a = H.setup(raw)
+        orc = O.Oracle(a)
+        Q = a["nquads"]
+        centres = [l * Q + Q // 2 for l in range(a["nlines"])]  # line centres: the largest optical depths
+        for o in range(0, a["npoints"], max(1, a["npoints"] // 30)):
+            for rr in range(a["hnrays"]):
+                for f in centres:
+                    b = orc.feautrier_bands(o, rr, f, n_off)
+                    if b is None:
+                        continue
+                    A, Cc = b["A"], b["C"]
+                    N = len(A)
+                    T = np.zeros((N, N))
+                    T[0, 0] = 1.0 + Cc[0] + 2.0 * np.sqrt(0.5 * Cc[0])
+                    T[0, 1] = -Cc[0]
+                    for n in range(1, N - 1):
+                        T[n, n - 1], T[n, n], T[n, n + 1] = -A[n], 1.0 + A[n] + Cc[n], -Cc[n]
+                    T[N - 1, N - 2] = -A[N - 1]
+                    T[N - 1, N - 1] = 1.0 + A[N - 1] + 2.0 * np.sqrt(0.5 * A[N - 1])
+                    if np.linalg.cond(T) > 1e8:
+                        continue  # optically thin rows (dtau near min_dtau): no reliable dense inverse
+                    Ti = np.linalg.inv(T)
+                    np.testing.assert_allclose(b["L_diag"], np.diag(Ti), rtol=1e-9)
+                    for m in range(min(n_off, N - 1)):
+                        n = np.arange(N - m - 1)
+                        np.testing.assert_allclose(b["L_upper"][m, n + m + 1], Ti[n, n + m + 1], rtol=1e-9)
+                        np.testing.assert_allclose(b["L_lower"][m, n], Ti[n + m + 1, n], rtol=1e-9)
+                    checked += 1
+    assert checked >= 30  # well-conditioned rays of both models
