@@ -51,7 +51,8 @@ int decode_status(int st) {
         return MGR_ERR_TRACE;
     }
     if (st & ST_CAPACITY) {
-        set_error("ray longer than the sized ray buffer");
+        set_error("capacity exceeded: a ray longer than the sized ray buffer, or an interpolation count above "
+                  "the per-edge table's 65535 (an interpolation-criterion jump too large for FP32)");
         return MGR_ERR_CAPACITY;
     }
     if (st & ST_NONFINITE) {
@@ -141,6 +142,7 @@ int mgr_device_count(int* count) {
 
 void mgr_model_free(MgrModel* model) {
     if (!model) return;
+    DeviceScope on_device(model->device);
     if (model->stream) cudaStreamSynchronize(model->stream);
     for (void* p : model->allocations) cudaFree(p);
     if (model->J_scratch) cudaFree(model->J_scratch);
@@ -380,6 +382,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
 
 int mgr_model_set_line_data(MgrModel* model, const double* emissivity, const double* opacity,
                             const double* inverse_width, const double* interp_criterion) {
+    MGR_MODEL_DEVICE(model);
     if (!model) {
         set_error("mgr_model_set_line_data: null model");
         return MGR_ERR_ARGUMENT;
@@ -399,6 +402,7 @@ int mgr_model_set_line_data(MgrModel* model, const double* emissivity, const dou
 }
 
 int mgr_ray_lengths_max(MgrModel* model, uint32_t* length) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !length) {
         set_error("mgr_ray_lengths_max: null argument");
         return MGR_ERR_ARGUMENT;
@@ -422,6 +426,7 @@ int mgr_ray_lengths_max(MgrModel* model, uint32_t* length) {
 int mgr_trace_ray_pair(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity, uint32_t* n_tot,
                        uint32_t* centre, uint32_t* nr, uint32_t* nr_interp, double* interp_factor, double* shift,
                        double* dZ) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !n_tot || !centre || !nr || !nr_interp || !interp_factor || !shift || !dZ || capacity == 0) {
         set_error("mgr_trace_ray_pair: null argument");
         return MGR_ERR_ARGUMENT;
@@ -476,6 +481,7 @@ int mgr_trace_ray_pair(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uin
 
 int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, double* u_dev,
                                 double* lambda_diag_dev) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !J_dev) {
         set_error("mgr_formal_solve_fo2_device: null argument");
         return MGR_ERR_ARGUMENT;
@@ -502,6 +508,7 @@ int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, d
 
 int mgr_formal_solve_fo2_rays_device(MgrModel* model, int precision, uint32_t rr_begin, uint32_t rr_end,
                                      double* J_dev, double* lambda_diag_dev) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !J_dev) {
         set_error("mgr_formal_solve_fo2_rays_device: null argument");
         return MGR_ERR_ARGUMENT;
@@ -530,6 +537,7 @@ int mgr_formal_solve_fo2_rays_device(MgrModel* model, int precision, uint32_t rr
 
 int mgr_formal_solve_fo2_rays(MgrModel* model, int precision, uint32_t rr_begin, uint32_t rr_end, double* J,
                               double* lambda_diag) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !J) {
         set_error("mgr_formal_solve_fo2_rays: null argument");
         return MGR_ERR_ARGUMENT;
@@ -554,6 +562,7 @@ int mgr_formal_solve_fo2_rays(MgrModel* model, int precision, uint32_t rr_begin,
 
 int mgr_set_ray_shard(MgrModel* model, uint32_t rr_begin, uint32_t rr_end, mgr_reduce_fn reduce, void* user,
                       int capturable) {
+    MGR_MODEL_DEVICE(model);
     if (!model) {
         set_error("mgr_set_ray_shard: null model");
         return MGR_ERR_ARGUMENT;
@@ -577,6 +586,7 @@ int mgr_set_ray_shard(MgrModel* model, uint32_t rr_begin, uint32_t rr_end, mgr_r
 }
 
 int mgr_formal_solve_fo2_sparse_device(MgrModel* model, int precision, double* Jlin_dev, double* lambda_diag_dev) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !Jlin_dev) {
         set_error("mgr_formal_solve_fo2_sparse_device: null argument");
         return MGR_ERR_ARGUMENT;
@@ -602,6 +612,7 @@ int mgr_formal_solve_fo2_sparse_device(MgrModel* model, int precision, double* J
 }
 
 int mgr_formal_solve_fo2_sparse(MgrModel* model, int precision, double* Jlin, double* lambda_diag) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !Jlin) {
         set_error("mgr_formal_solve_fo2_sparse: null argument");
         return MGR_ERR_ARGUMENT;
@@ -624,6 +635,7 @@ int mgr_formal_solve_fo2_sparse(MgrModel* model, int precision, double* Jlin, do
 
 int mgr_formal_solve_fo2_anis(MgrModel* model, int precision, double* J, double* J2_0, double* J2_1_Re,
                               double* J2_1_Im, double* J2_2_Re, double* J2_2_Im) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !J) {
         set_error("mgr_formal_solve_fo2_anis: null argument");
         return MGR_ERR_ARGUMENT;
@@ -652,6 +664,7 @@ int mgr_formal_solve_fo2_anis(MgrModel* model, int precision, double* J, double*
 }
 
 int mgr_formal_solve_fo2_uv(MgrModel* model, int precision, double* u, double* v) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !u || !v) {
         set_error("mgr_formal_solve_fo2_uv: null argument");
         return MGR_ERR_ARGUMENT;
@@ -679,6 +692,7 @@ int mgr_formal_solve_fo2_uv(MgrModel* model, int precision, double* u, double* v
 }
 
 int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, double* lambda_diag) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !J) {
         set_error("mgr_formal_solve_fo2: null argument");
         return MGR_ERR_ARGUMENT;
@@ -706,6 +720,7 @@ int mgr_formal_solve_fo2(MgrModel* model, int precision, double* J, double* u, d
 }
 
 int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_reads, uint64_t* elements) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !steps || !neighbor_reads || !elements) {
         set_error("mgr_ray_statistics: null argument");
         return MGR_ERR_ARGUMENT;
@@ -729,6 +744,7 @@ int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_read
 }
 
 int mgr_set_tuning(MgrModel* model, int precision, int min_blocks_per_sm, int warps_per_block) {
+    MGR_MODEL_DEVICE(model);
     if (!model || (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) ||
         (min_blocks_per_sm != 0 && (min_blocks_per_sm < 2 || min_blocks_per_sm > 4)) || warps_per_block < 0 ||
         warps_per_block > 8) {
@@ -745,6 +761,7 @@ int mgr_set_tuning(MgrModel* model, int precision, int min_blocks_per_sm, int wa
 
 int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int* best_min_blocks, int* best_warps,
                      float* best_ms) {
+    MGR_MODEL_DEVICE(model);
     if (!model || (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT)) {
         set_error("mgr_autotune_fo2: invalid argument");
         return MGR_ERR_ARGUMENT;
@@ -805,6 +822,7 @@ int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int
 }
 
 int mgr_sync(MgrModel* model) {
+    MGR_MODEL_DEVICE(model);
     if (!model) {
         set_error("mgr_sync: null model");
         return MGR_ERR_ARGUMENT;

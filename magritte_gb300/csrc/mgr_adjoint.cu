@@ -206,6 +206,7 @@ using namespace mgr;
 extern "C" {
 
 int mgr_model_set_velocity_device(MgrModel* model, const double* velocity_dev) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !velocity_dev) {
         set_error("mgr_model_set_velocity_device: null argument");
         return MGR_ERR_ARGUMENT;
@@ -222,6 +223,7 @@ int mgr_model_set_velocity_device(MgrModel* model, const double* velocity_dev) {
 
 int mgr_model_set_line_data_device(MgrModel* model, const double* emissivity_dev, const double* opacity_dev,
                                    const double* inverse_width_dev) {
+    MGR_MODEL_DEVICE(model);
     if (!model) {
         set_error("mgr_model_set_line_data_device: null model");
         return MGR_ERR_ARGUMENT;
@@ -264,6 +266,7 @@ int mgr_model_set_line_data_device(MgrModel* model, const double* emissivity_dev
 
 int mgr_image_new_smooth_device(MgrModel* model, const double* raydir, uint32_t nx, uint32_t ny, double* I_dev,
                                 double* ImX, double* ImY) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !I_dev) {
         set_error("mgr_image_new_smooth_device: null argument");
         return MGR_ERR_ARGUMENT;
@@ -308,6 +311,7 @@ int mgr_image_new_smooth_device(MgrModel* model, const double* raydir, uint32_t 
 int mgr_image_new_adjoint_device(MgrModel* model, const double* raydir, uint32_t nx, uint32_t ny,
                                  const double* gI_dev, double* g_em_dev, double* g_op_dev, double* g_iw_dev,
                                  double* g_Sp_dev, double* g_vel_dev) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !gI_dev || !g_em_dev || !g_op_dev || !g_iw_dev || !g_Sp_dev || !g_vel_dev) {
         set_error("mgr_image_new_adjoint_device: null argument");
         return MGR_ERR_ARGUMENT;

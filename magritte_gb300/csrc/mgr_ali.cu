@@ -834,6 +834,7 @@ extern "C" {
 
 int mgr_model_set_species(MgrModel* model, uint32_t nlspecs, const MgrSpeciesDesc* species, uint32_t nspecs,
                           const double* abundance, const double* const* populations) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !species || nlspecs == 0 || !abundance || !populations || nspecs == 0) {
         set_error("mgr_model_set_species: null argument");
         return MGR_ERR_ARGUMENT;
@@ -957,6 +958,7 @@ int mgr_model_set_species(MgrModel* model, uint32_t nlspecs, const MgrSpeciesDes
 }
 
 int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, double* Jdif) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !model->ali || l >= model->ali->species.size()) {
         set_error("mgr_compute_jeff: no species attached (mgr_model_set_species) or species index out of range");
         return MGR_ERR_ARGUMENT;
@@ -979,6 +981,7 @@ int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, do
 int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, long max_iterations,
                                   const MgrAliParams* params, int* iterations, double* error_mean,
                                   double* error_max, uint32_t err_capacity) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !params || !model->ali) {
         set_error("mgr_compute_level_populations: null argument or no species attached (mgr_model_set_species)");
         return MGR_ERR_ARGUMENT;
@@ -1136,6 +1139,7 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
 int mgr_compute_level_populations_sparse(MgrModel* model, int precision, int use_ng, long max_iterations,
                                          const MgrAliParams* params, int* iterations, double* error_mean,
                                          double* error_max, uint32_t err_capacity) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !model->ali) {
         set_error("mgr_compute_level_populations_sparse: null argument or no species attached (mgr_model_set_species)");
         return MGR_ERR_ARGUMENT;
@@ -1148,6 +1152,7 @@ int mgr_compute_level_populations_sparse(MgrModel* model, int precision, int use
 }
 
 int mgr_compute_jeff_sparse(MgrModel* model, uint32_t l, double* Jlin, double* Jeff) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !model->ali || l >= model->ali->species.size()) {
         set_error("mgr_compute_jeff_sparse: no species attached (mgr_model_set_species) or species index out of range");
         return MGR_ERR_ARGUMENT;
@@ -1167,6 +1172,7 @@ int mgr_compute_jeff_sparse(MgrModel* model, uint32_t l, double* Jlin, double* J
 }
 
 int mgr_get_populations(MgrModel* model, uint32_t l, double* populations) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !model->ali || l >= model->ali->species.size() || !populations) {
         set_error("mgr_get_populations: invalid argument");
         return MGR_ERR_ARGUMENT;
@@ -1180,6 +1186,7 @@ int mgr_get_populations(MgrModel* model, uint32_t l, double* populations) {
 }
 
 int mgr_get_line_data(MgrModel* model, double* emissivity, double* opacity) {
+    MGR_MODEL_DEVICE(model);
     if (!model) {
         set_error("mgr_get_line_data: null model");
         return MGR_ERR_ARGUMENT;

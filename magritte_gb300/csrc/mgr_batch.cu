@@ -204,6 +204,7 @@ static cudaError_t launch_batch_approx(MgrBatch* b) {
 
 static void batch_release(MgrBatch* b) {
     if (!b) return;
+    DeviceScope on_device(b->device);
     cudaFree(b->d_models);
     cudaFree(b->d_offsets);
     cudaFree(b->d_J);
@@ -286,7 +287,8 @@ int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out)
         offsets[i + 1] = offsets[i] + m->dm.P;
     }
     b->n_items = offsets[n_models];
-    cudaError_t e = cudaSetDevice(b->device);
+    DeviceScope on_device(b->device);
+    cudaError_t e = on_device.error();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_models, n_models * sizeof(DevModel));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_offsets, (n_models + 1) * sizeof(uint64_t));
@@ -319,6 +321,7 @@ int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out)
 void mgr_batch_free(MgrBatch* batch) { batch_release(batch); }
 
 int mgr_batch_set_tuning(MgrBatch* batch, int min_blocks_per_sm, int warps_per_block) {
+    MGR_MODEL_DEVICE(batch);
     if (!batch) {
         set_error("mgr_batch_set_tuning: null batch");
         return MGR_ERR_ARGUMENT;
@@ -346,6 +349,7 @@ int mgr_batch_set_tuning(MgrBatch* batch, int min_blocks_per_sm, int warps_per_b
 
 int mgr_batch_formal_solve_fo2_device(MgrBatch* batch, int precision, double* const* J_dev,
                                       double* const* lambda_diag_dev) {
+    MGR_MODEL_DEVICE(batch);
     if (!batch || !J_dev) {
         set_error("mgr_batch_formal_solve_fo2_device: null argument");
         return MGR_ERR_ARGUMENT;
@@ -381,6 +385,7 @@ int mgr_batch_formal_solve_fo2_device(MgrBatch* batch, int precision, double* co
 }
 
 int mgr_batch_formal_solve_fo2(MgrBatch* batch, int precision, double* const* J, double* const* lambda_diag) {
+    MGR_MODEL_DEVICE(batch);
     if (!batch || !J) {
         set_error("mgr_batch_formal_solve_fo2: null argument");
         return MGR_ERR_ARGUMENT;
@@ -427,6 +432,7 @@ int mgr_batch_formal_solve_fo2(MgrBatch* batch, int precision, double* const* J,
 }
 
 int mgr_batch_timings(MgrBatch* batch, double* start_ms, double* finish_ms) {
+    MGR_MODEL_DEVICE(batch);
     if (!batch || !start_ms || !finish_ms) {
         set_error("mgr_batch_timings: null argument");
         return MGR_ERR_ARGUMENT;

@@ -536,29 +536,35 @@ using namespace mgr;
 extern "C" {
 
 int mgr_image(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY) {
+    MGR_MODEL_DEVICE(model);
     return image_old_impl(model, precision, ray_nr, I, ImX, ImY, false, "mgr_image");
 }
 
 int mgr_image_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny, double* I,
                   double* ImX, double* ImY) {
+    MGR_MODEL_DEVICE(model);
     return image_new_impl(model, precision, raydir, nx, ny, I, ImX, ImY, false, "mgr_image_new");
 }
 
 int mgr_image_optical_depth(MgrModel* model, int precision, uint32_t ray_nr, double* I, double* ImX, double* ImY) {
+    MGR_MODEL_DEVICE(model);
     return image_old_impl(model, precision, ray_nr, I, ImX, ImY, true, "mgr_image_optical_depth");
 }
 
 int mgr_image_optical_depth_new(MgrModel* model, int precision, const double* raydir, uint32_t nx, uint32_t ny,
                                 double* I, double* ImX, double* ImY) {
+    MGR_MODEL_DEVICE(model);
     return image_new_impl(model, precision, raydir, nx, ny, I, ImX, ImY, true, "mgr_image_optical_depth_new");
 }
 
 int mgr_image_for_point(MgrModel* model, int precision, uint32_t ray_nr, uint32_t p, uint32_t* n_tot, double* S_ray,
                         double* dtau_ray, double* u_ray, uint32_t capacity) {
+    MGR_MODEL_DEVICE(model);
     return image_for_point_impl(model, precision, ray_nr, p, n_tot, S_ray, dtau_ray, u_ray, capacity);
 }
 
 int mgr_set_column(MgrModel* model, const double* density, double* column) {
+    MGR_MODEL_DEVICE(model);
     return set_column_impl(model, density, column);
 }
 

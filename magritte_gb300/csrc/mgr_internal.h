@@ -76,6 +76,45 @@ namespace mgr {
 
 void set_error(const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
+
+// Makes `device` the calling thread's current CUDA device for the lifetime of the
+// object and restores the caller's device afterwards.  Every entry point that works
+// on a model enters its device first: a process may drive several GPUs, and the
+// model's stream, allocations and the staging array's address all belong to the
+// device the model was created on.  device < 0 leaves the current device alone.
+class DeviceScope {
+  public:
+    explicit DeviceScope(int device) {
+        if (device < 0) return;
+        if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+        if (prev_ != device) {
+            err_ = cudaSetDevice(device);
+            restore_ = (err_ == cudaSuccess && prev_ >= 0);
+        }
+    }
+    ~DeviceScope() {
+        if (restore_) cudaSetDevice(prev_);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+    cudaError_t error() const { return err_; }
+
+  private:
+    int prev_ = -1;
+    bool restore_ = false;
+    cudaError_t err_ = cudaSuccess;
+};
+
+}  // namespace mgr
+
+// First statement of an int-returning entry point taking a model (which may be null:
+// the entry point's own argument check follows).
+#define MGR_MODEL_DEVICE(mdl)                                                       \
+    ::mgr::DeviceScope mgr_device_scope_((mdl) ? (mdl)->device : -1);              \
+    if (mgr_device_scope_.error() != cudaSuccess)                                   \
+    return ::mgr::cuda_fail(mgr_device_scope_.error(), "entering the model's device")
+
+namespace mgr {
 // Device status word (ST_* bits) -> MGR_* code with the error message set.
 int decode_status(int st);
 // FP32 line-table scales of split precision (powers of two) and the derived DevModel fields.

@@ -48,6 +48,9 @@ using namespace mgr;
 
 extern "C" int mgr_formal_solve_fo2_device_noalloc(MgrModel* model, int precision, double* J_dev, double* u_dev,
                                                    double* lambda_diag_dev) {
+    // The model's device is current from here on, so the staging array's address
+    // looked up below is the one on that device.
+    MGR_MODEL_DEVICE(model);
     if (!model || !J_dev) {
         set_error("mgr_formal_solve_fo2_device_noalloc: null argument");
         return MGR_ERR_ARGUMENT;
@@ -55,6 +58,13 @@ extern "C" int mgr_formal_solve_fo2_device_noalloc(MgrModel* model, int precisio
     if (precision != MGR_PRECISION_FP64 && precision != MGR_PRECISION_SPLIT) {
         set_error("mgr_formal_solve_fo2_device_noalloc: unknown precision mode");
         return MGR_ERR_ARGUMENT;
+    }
+    if (!model->line_disc) {
+        // frequencies of an imaging discretisation have no (line, quadrature point)
+        // map, which the ALO and the per-line tables of the solve index
+        set_error("mgr_formal_solve_fo2_device_noalloc: the formal solve needs a line spectral discretisation "
+                  "(nfreqs = nlines*nquads with every frequency mapped to its line)");
+        return MGR_ERR_UNSUPPORTED;
     }
     const int k = (u_dev ? 0 : 1) + (lambda_diag_dev ? 1 : 0);
     const size_t per_origin = (size_t)model->dm.hnrays * model->dm.F * sizeof(double) * k;
@@ -69,5 +79,9 @@ extern "C" int mgr_formal_solve_fo2_device_noalloc(MgrModel* model, int precisio
     if (e != cudaSuccess) return cuda_fail(e, "staging area address");
     e = launch_fo2_range(model, precision, 0, model->dm.P, J_dev, u_dev, lambda_diag_dev, stage, kStageBytes);
     if (e != cudaSuccess) return cuda_fail(e, "formal solve launch");
+    // the caller's J and ALO buffers are this model's latest formal-solve results,
+    // which mgr_compute_jeff reads
+    model->last_J = J_dev;
+    model->last_lam = lambda_diag_dev;
     return MGR_OK;
 }

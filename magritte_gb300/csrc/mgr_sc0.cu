@@ -232,6 +232,7 @@ extern "C" {
 
 int mgr_formal_solve_sc0_device(MgrModel* model, int precision, double* J_dev, double* I_dev, double* u_dev,
                                 double* v_dev, double* lambda_diag_dev) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !J_dev) {
         set_error("mgr_formal_solve_sc0_device: null argument");
         return MGR_ERR_ARGUMENT;
@@ -265,6 +266,7 @@ int mgr_formal_solve_sc0_device(MgrModel* model, int precision, double* J_dev, d
 
 int mgr_formal_solve_sc0(MgrModel* model, int precision, double* J, double* I, double* u, double* v,
                          double* lambda_diag) {
+    MGR_MODEL_DEVICE(model);
     if (!model || !J) {
         set_error("mgr_formal_solve_sc0: null argument");
         return MGR_ERR_ARGUMENT;
