@@ -53,6 +53,7 @@ def parse():
     p.add_argument("--precision", default="split", choices=["split", "fp64"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-parity", action="store_true", help="skip the oracle parity sample")
     p.add_argument("--no-ali", action="store_true", help="skip the ALI wall-time leg")
     p.add_argument("--ali-points", type=int, default=50_000)
     p.add_argument("--ali-nside", type=int, default=2)
@@ -152,20 +153,87 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(raw, nthreads, rr_count=2, n_origins=40000):
-    """The oracle port of the reference CPU algorithm on a bounded sample."""
+# The CPU legs (this arm's cpu_baseline and the --impl reference arm) time the same
+# bounded sample of the workload: every SAMPLE_STRIDE-th origin with every ray pair and
+# frequency, the reference's arithmetic (the oracle port with glibc's erff), all host
+# threads.  The sizing pass (Solver::get_ray_lengths_max) runs over the sampled origins.
+SAMPLE_STRIDE = 32
+
+
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
+    return oracle
+
+
+def cpu_sample(raw):
+    """(oracle module, Oracle, sampled origins, solves per sample) of the CPU legs."""
+    import numpy as np
+    oracle = _oracle()
     arrays = oracle.reference_setup(raw)
     orc = oracle.Oracle(arrays)
-    n_o = min(n_origins, arrays["npoints"])
+    origins = np.arange(0, arrays["npoints"], SAMPLE_STRIDE, dtype=np.uint32)
+    solves = len(origins) * arrays["hnrays"] * arrays["nfreqs"]
+    return oracle, orc, origins, solves
+
+
+def _sample_desc(origins, solves):
+    return (f"every {SAMPLE_STRIDE}th origin ({len(origins)}) x all ray pairs x all frequencies "
+            f"({solves} solves per step)")
+
+
+def cpu_baseline(raw, nthreads):
+    """The oracle port of the reference CPU algorithm on the bounded sample."""
+    oracle, orc, origins, solves = cpu_sample(raw)
+    oracle.set_erf_mode(0)
     t0 = time.perf_counter()
-    orc.formal_solve_fo2_range(0, rr_count, 0, n_o, nthreads=nthreads)
+    orc.formal_solve_fo2_origins(origins, nthreads=nthreads)
     dt = time.perf_counter() - t0
-    solves = n_o * rr_count * arrays["nfreqs"]
     return {"value": solves / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"ray pairs 0-{rr_count - 1} x origins 0-{n_o - 1} ({solves} solves, {dt:.2f} s)"}
+            "sample": _sample_desc(origins, solves) + f", {dt:.2f} s"}
+
+
+def parity_sample(raw, gpu_rows, stride=50):
+    """Max relative error of the GPU's J and ALO diagonal (FP64 and split) against the
+    oracle on every ``stride``-th origin, in both oracle arithmetics: erf mode 1 (the
+    correctly rounded erff of the GPU's FP64 mode) and erf mode 0 (glibc's erff, the
+    reference's own arithmetic).  ``gpu_rows[prec] = (J [P][F], lam [P][L])``."""
+    import numpy as np
+    oracle = _oracle()
+    arrays = oracle.reference_setup(raw)
+    orc = oracle.Oracle(arrays)
+    origins = np.arange(0, arrays["npoints"], stride, dtype=np.uint32)
+    ref = {}
+    t0 = time.perf_counter()
+    try:
+        for mode in (0, 1):
+            oracle.set_erf_mode(mode)
+            ref[mode] = orc.formal_solve_fo2_origins(origins)
+    finally:
+        oracle.set_erf_mode(0)
+    rel = lambda a, b: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+    out = {"sample": f"every {stride}th origin ({len(origins)}) x all ray pairs x all frequencies",
+           "oracle_s": time.perf_counter() - t0, "bar": 1e-5}
+    for prec, (J, lam) in gpu_rows.items():
+        for mode, name in ((1, "erf_cr"), (0, "erf_glibc")):
+            out[f"{prec}_J_vs_oracle_{name}"] = rel(J[origins], ref[mode]["J"])
+            out[f"{prec}_alo_vs_oracle_{name}"] = rel(lam[origins], ref[mode]["lambda_diag"])
+    out["oracle_erf_glibc_vs_erf_cr_J"] = rel(ref[0]["J"], ref[1]["J"])
+    out["note"] = ("erf_cr: the oracle with the correctly rounded erff of the GPU's FP64 mode; erf_glibc: the "
+                   "reference's own arithmetic (glibc erff)")
+    return out
+
+
+def pipe_rates():
+    """Measured issue rates of the FP64-pipe instruction kinds (mgr_measure_pipe_rate)."""
+    from magritte_gb300 import _abi
+    out = {}
+    for kind in ("dfma", "dadd", "dmul", "dsetp", "f2f", "mufu_rcp64"):
+        r = _abi.pipe_rate(kind, iterations=4096 if kind != "mufu_rcp64" else 16384)
+        out[kind] = {"thread_ops_per_s": r["thread_ops_per_s"],
+                     "per_clk_per_sm": r["thread_ops_per_clk_per_sm"], "ms": r["ms"]}
+    return out
 
 
 def run_ali(args):
@@ -423,23 +491,18 @@ def run_reference(args, rank, ws):
         return
     raw, desc = workload(args)
     nthreads = os.cpu_count() or 1
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    oracle.build()
-    arrays = oracle.reference_setup(raw)
-    orc = oracle.Oracle(arrays)
-    rr_count, n_o = 1, min(40000, arrays["npoints"])
-    solves = n_o * rr_count * arrays["nfreqs"]
+    oracle, orc, origins, solves = cpu_sample(raw)
+    oracle.set_erf_mode(0)  # the reference's glibc erff
     for _ in range(args.warmup):
-        orc.formal_solve_fo2_range(0, rr_count, 0, n_o, nthreads=nthreads)
+        orc.formal_solve_fo2_origins(origins, nthreads=nthreads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        orc.formal_solve_fo2_range(0, rr_count, 0, n_o, nthreads=nthreads)
+        orc.formal_solve_fo2_origins(origins, nthreads=nthreads)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = solves * args.steps / total
-    sample = f"ray pair 0 x origins 0-{n_o - 1} per step ({solves} solves)"
+    sample = _sample_desc(origins, solves)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -541,13 +604,20 @@ def run_ours(args, rank, ws):
 
     # accuracy of this precision against the FP64 path on the full workload
     J_ref = torch.empty_like(J)
+    lam_ref = torch.empty_like(lam)
     with torch.cuda.stream(stream):
-        rc = lib.mgr_formal_solve_fo2_device(handle, _abi.PRECISION["fp64"], C.c_void_p(J_ref.data_ptr()), None, None)
+        rc = lib.mgr_formal_solve_fo2_device(handle, _abi.PRECISION["fp64"], C.c_void_p(J_ref.data_ptr()), None,
+                                             C.c_void_p(lam_ref.data_ptr()))
         if rc != 0:
             raise RuntimeError(lib.mgr_last_error().decode())
         step()
         stream.synchronize()
     max_rel = float(((J - J_ref).abs() / J_ref.abs()).max().item())
+    gpu_rows = None
+    if ws == 1 and not args.no_parity:
+        gpu_rows = {"fp64": (J_ref.cpu().numpy(), lam_ref.cpu().numpy())}
+        if args.precision != "fp64":
+            gpu_rows[args.precision] = (J.cpu().numpy(), lam.cpu().numpy())
     # plain FP64 GPU throughput on the same workload (the comparison path)
     fp64_ms = None
     if args.precision != "fp64":
@@ -585,25 +655,49 @@ def run_ours(args, rank, ws):
                        "allreduce) + J/ALO read-back"}
     elif not args.no_e2e:
         prm.store_u = False
-        model.release_device()
-        model.compute_radiation_field_feautrier_order_2()  # warm the host paths
-        e2e_times = []
-        for _ in range(max(1, min(args.steps, 3))):
-            model.release_device()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            model.compute_radiation_field_feautrier_order_2()
-            e2e_times.append(time.perf_counter() - t0)
         h2d = (P * 3 * 8 * 2 + len(raw.neighbors) * 4 + P * 4 * 3 + P * F * 8 + 4 * P * L * 8 + P * 8 * 3
                + F * 4 * 4 + F)
         d2h = P * F * 8 + P * L * 8
-        e2e_s = max_over_ranks(sum(e2e_times) / len(e2e_times), ws)
-        e2e = {"value": solves / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "s_per_step": e2e_s,
-               "path": "core.Model.compute_radiation_field_feautrier_order_2 (upload + solve + J/ALO read-back)"}
+
+        def e2e_leg(prec):
+            """compute_radiation_field_feautrier_order_2 with a fresh upload each step, and
+            its parts: the upload alone, then the call on the resident model."""
+            prm.precision = prec
+            model.release_device()
+            model.compute_radiation_field_feautrier_order_2()  # warm the host paths
+            times = []
+            for _ in range(max(1, min(args.steps, 3))):
+                model.release_device()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                model.compute_radiation_field_feautrier_order_2()
+                times.append(time.perf_counter() - t0)
+            model.release_device()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            model.upload()
+            torch.cuda.synchronize()
+            t_up = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            model.compute_radiation_field_feautrier_order_2()
+            t_call = time.perf_counter() - t0
+            e_s = max_over_ranks(sum(times) / len(times), ws)
+            return {"value": solves / e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "s_per_step": e_s, "precision": prec,
+                    "breakdown_s": {"upload (host set-up, copies, tables, ray sizing)": t_up,
+                                    "call on the resident model (line-data refresh, solve, read-back)": t_call},
+                    "path": "core.Model.compute_radiation_field_feautrier_order_2 (upload + solve + J/ALO "
+                            "read-back)"}
+
+        e2e = e2e_leg(args.precision)
+        if args.precision != "fp64":
+            e2e["fp64"] = e2e_leg("fp64")
+        prm.precision = args.precision
 
     if rank != 0:
         return
+    parity = parity_sample(raw, gpu_rows) if gpu_rows is not None else None
+    rates = pipe_rates()
     ali = None if args.no_ali else run_ali(args)
     batch = None if args.no_batch else run_batch(args)
     adj = None if args.no_adjoint else run_adjoint(args)
@@ -635,6 +729,10 @@ def run_ours(args, rank, ws):
         "wall_s_timed": wall,
         "step_ms": step_ms,
         "max_rel_err_J_vs_fp64_gpu": max_rel,
+        "max_rel_err_J_vs_oracle": (max(parity[f"{args.precision}_J_vs_oracle_erf_cr"],
+                                        parity[f"{args.precision}_J_vs_oracle_erf_glibc"]) if parity else None),
+        "parity": parity,
+        "pipe_rates": rates,
         "fp64_gpu_solves_per_s": (solves / (fp64_ms / 1000.0)) if fp64_ms else None,
         "speedup_vs_fp64_gpu": (fp64_ms / (1000.0 * kernel_s / args.steps)) if fp64_ms else None,
         "work": {"trace_steps": st_steps.value, "neighbour_reads": st_nbr.value, "elements": st_elem.value},

@@ -483,6 +483,17 @@ void* mgr_model_stream(MgrModel* model);
 /* Number of this library's kernel launches so far (all models, all streams). */
 uint64_t mgr_launch_count(void);
 
+/* Measured issue rate of one instruction kind on the current device, for the
+ * benchmark's FP64-pipe roofline (no reference counterpart: the reference has no GPU
+ * path).  kind: 0 DFMA, 1 DADD, 2 DMUL, 3 DSETP (FP64 compare), 4 F2F (FP64 <-> FP32
+ * conversion), 5 MUFU.RCP64H (rcp.approx.ftz.f64).  Eight independent chains per
+ * thread, `iterations` steps each, over SMs x 8 CTAs of 256 threads; the best of three
+ * timed launches.  Outputs (any may be NULL): thread operations per second for the
+ * whole device, thread operations per SM clock cycle per SM (from the kernel's own
+ * clock64 counts), and the launch time in ms.  Blocks. */
+int mgr_measure_pipe_rate(int kind, uint32_t iterations, double* thread_ops_per_s,
+                          double* thread_ops_per_clk_per_sm, float* ms);
+
 #ifdef __cplusplus
 }
 #endif

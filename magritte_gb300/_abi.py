@@ -14,6 +14,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libmgr_gpu.so")
 
 MGR_OK = 0
+# MgrStatus codes (include/magritte_gb300.h)
+MGR_ERR_ARGUMENT, MGR_ERR_CUDA, MGR_ERR_NO_DEVICE = -1, -2, -3
+MGR_ERR_TRACE, MGR_ERR_CAPACITY, MGR_ERR_NONFINITE, MGR_ERR_UNSUPPORTED = -4, -5, -6, -7
 PRECISION = {"fp64": 0, "split": 1}
 APPROX = {"None": 0, "OneLine": 1, "CloseLines": 2}
 
@@ -146,6 +149,8 @@ SIGNATURES = {
     "mgr_sync": (C.c_int, [C.c_void_p]),
     "mgr_model_stream": (C.c_void_p, [C.c_void_p]),
     "mgr_launch_count": (C.c_uint64, []),
+    "mgr_measure_pipe_rate": (C.c_int, [C.c_int, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_float)]),
 }
 
 _lib = None
@@ -531,6 +536,17 @@ def autotune(handle, precision="split", sample_points=0):
     _check(load().mgr_autotune_fo2(handle, PRECISION[precision], sample_points, C.byref(mb), C.byref(w),
                                    C.byref(ms)))
     return {"min_blocks_per_sm": mb.value, "warps_per_block": w.value, "sample_ms": ms.value}
+
+
+PIPE_KINDS = {"dfma": 0, "dadd": 1, "dmul": 2, "dsetp": 3, "f2f": 4, "mufu_rcp64": 5}
+
+
+def pipe_rate(kind, iterations=4096):
+    """Measured rate of one instruction kind (mgr_measure_pipe_rate): thread operations
+    per second, per SM clock per SM, and the probe's launch time in ms."""
+    ops, per_clk, ms = C.c_double(), C.c_double(), C.c_float()
+    _check(load().mgr_measure_pipe_rate(PIPE_KINDS[kind], iterations, C.byref(ops), C.byref(per_clk), C.byref(ms)))
+    return dict(thread_ops_per_s=ops.value, thread_ops_per_clk_per_sm=per_clk.value, ms=ms.value)
 
 
 def launch_count():

@@ -19,6 +19,10 @@ using namespace mgr;
 
 namespace {
 
+// Failure returns of trace_half_host, as the kernel's status bits ST_TRACE / ST_CAPACITY.
+constexpr int kTraceLeftGrid = -1;
+constexpr int kTraceOverCapacity = -2;
+
 // Sequential restatement of trace_half (same arithmetic, neighbour order, strict <).
 int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int frame = 0) {
     const double* d = frame ? m.raydir + 3 * r : ray_dir(m, o, r);
@@ -35,8 +39,8 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
         while (true) {
             uint32_t nxt;
             double dZl;
-            if (!next_point_sph(m, Rcos, Rsin2, crt, Z, nxt, dZl)) return count > 0 ? -1 : 0;
-            if ((uint32_t)count >= cap) return -1;
+            if (!next_point_sph(m, Rcos, Rsin2, crt, Z, nxt, dZl)) return count > 0 ? kTraceLeftGrid : 0;
+            if ((uint32_t)count >= cap) return kTraceOverCapacity;
             Z = dadd_rn(Z, dZl);
             h.ids[count] = nxt;
             h.eid[count] = sph_eid(crt, nxt);
@@ -70,8 +74,8 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
                 }
             }
         }
-        if (besti == 0xffffffffu) return count > 0 ? -1 : 0;
-        if ((uint32_t)count >= cap) return -1;
+        if (besti == 0xffffffffu) return count > 0 ? kTraceLeftGrid : 0;
+        if ((uint32_t)count >= cap) return kTraceOverCapacity;
         long long bits;
         std::memcpy(&bits, &m.edge[cum + besti].w, 8);
         const uint32_t nxt = (uint32_t)bits;
@@ -253,6 +257,11 @@ LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {
 
 constexpr uint32_t kCap = 1u << 16;
 
+// Half-ray capacity the emulated formal solve traces with (the kernel's shared-memory
+// ray buffers hold the longest half ray found by the sizing pass); tests lower it to
+// reach the capacity-overflow status without a GPU.
+uint32_t g_half_cap = kCap;
+
 template <int MODE, bool UV = false>
 LaneResult solve_any(const DevModel& m, const LaneCtx& c, const HalfSmem& bk, int nb, const HalfSmem& fw, int nf) {
     switch (m.approx) {
@@ -289,7 +298,8 @@ static int emu_fo2(const MgrModelDesc* d, int precision, uint32_t rr0, uint32_t 
     const uint32_t P = m.P, L = m.L, F = m.F, R = m.hnrays, Q = m.Q;
     if (rr1 > R) rr1 = R;
     if (rr0 >= rr1) return MGR_ERR_ARGUMENT;
-    int err = 0;
+    int err = 0;  // status bits, as the kernel's status word
+    const uint32_t cap = g_half_cap;
 #pragma omp parallel
     {
         HalfBuf b(kCap), fbuf(kCap);
@@ -300,9 +310,12 @@ static int emu_fo2(const MgrModelDesc* d, int precision, uint32_t rr0, uint32_t 
             const uint32_t o = (uint32_t)oo;
             bool ok = true;
             for (uint32_t rr = rr0; rr < rr1 && ok; rr++) {
-                const int nb = trace_half_host(m, o, rr, kCap, bk);
-                const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
+                const int nb = trace_half_host(m, o, rr, cap, bk);
+                const int nf = trace_half_host(m, o, m.antipod[rr], cap, fw);
                 if (nb < 0 || nf < 0) {
+                    const int bit = (nb == kTraceOverCapacity || nf == kTraceOverCapacity) ? ST_CAPACITY : ST_TRACE;
+#pragma omp atomic
+                    err |= bit;
                     ok = false;
                     break;
                 }
@@ -312,11 +325,7 @@ static int emu_fo2(const MgrModelDesc* d, int precision, uint32_t rr0, uint32_t 
                     LD[(size_t)rr * F + f] = r.solved ? r.Ldiag : 0.0;
                 }
             }
-            if (!ok) {
-#pragma omp atomic write
-                err = 1;
-                continue;
-            }
+            if (!ok) continue;
             for (uint32_t f = 0; f < F; f++) {
                 double s = 0.0;
                 for (uint32_t rr = rr0; rr < rr1; rr++) s += U[(size_t)rr * F + f] * 2.0 * ray_w(m, o, rr);
@@ -342,8 +351,12 @@ static int emu_fo2(const MgrModelDesc* d, int precision, uint32_t rr0, uint32_t 
             }
         }
     }
-    return err ? MGR_ERR_TRACE : MGR_OK;
+    // the host's decoding of the kernel's status word: a trace failure first
+    return (err & ST_TRACE) ? MGR_ERR_TRACE : (err & ST_CAPACITY) ? MGR_ERR_CAPACITY : MGR_OK;
 }
+
+// Half-ray capacity of the emulated formal solve; 0 restores the default.
+extern "C" void mgr_emu_set_half_capacity(uint32_t cap) { g_half_cap = (cap == 0 || cap > kCap) ? kCap : cap; }
 
 extern "C" int mgr_emu_formal_solve_fo2(const MgrModelDesc* d, int precision, double* J, double* lam) {
     return emu_fo2(d, precision, 0, 0xffffffffu, J, lam);

@@ -357,20 +357,29 @@ static uint32_t image_ray_lengths_max(const OrcModel* m, int nthreads) {
     return a > b ? a : b;
 }
 
-static uint32_t ray_lengths_max_impl(const OrcModel* m, int nthreads, int adaptive) {
+/* olist != NULL: over the origins olist[0 .. n-1] only (the sizing pass's share of a
+ * sample of origins), else over every point. */
+static uint32_t ray_lengths_max_of(const OrcModel* m, int nthreads, int adaptive, const uint32_t* olist,
+                                   uint32_t n) {
     uint32_t mx = 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
+    const int64_t no = olist ? (int64_t)n : (int64_t)m->npoints;
     for (uint32_t rr = 0; rr < m->hnrays; rr++) {
         const uint32_t ar = m->antipod[rr];
 #pragma omp parallel for reduction(max : mx) schedule(dynamic, 64)
-        for (int64_t o = 0; o < (int64_t)m->npoints; o++) {
-            const uint32_t len = get_ray_length(m, (uint32_t)o, rr, adaptive) + get_ray_length(m, (uint32_t)o, ar, adaptive);
+        for (int64_t i = 0; i < no; i++) {
+            const uint32_t o = olist ? olist[i] : (uint32_t)i;
+            const uint32_t len = get_ray_length(m, o, rr, adaptive) + get_ray_length(m, o, ar, adaptive);
             if (len > mx) mx = len;
         }
     }
     return mx;
+}
+
+static uint32_t ray_lengths_max_impl(const OrcModel* m, int nthreads, int adaptive) {
+    return ray_lengths_max_of(m, nthreads, adaptive, NULL, 0);
 }
 
 /* ------------------------------------------------------------------ */
@@ -886,7 +895,8 @@ int orc_trace_ray_pair_for_line(const OrcModel* m, uint32_t o, uint32_t rr, uint
 /* Formal solve driver (solver.tpp:458-540)                             */
 /* ------------------------------------------------------------------ */
 static int fo2_range_v(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0, uint32_t o1,
-                       double* J, double* u, double* v, double* lambda_diag, uint8_t* lambda_has, int nthreads);
+                       const uint32_t* olist, double* J, double* u, double* v, double* lambda_diag,
+                       uint8_t* lambda_has, int nthreads);
 
 /* The v part of Solver::solve_feautrier_order_2_uv(model, o, f) (solver.tpp:2767-2921)
  * after solve_feautrier_order_2 with full back substitution (Su[centre .. last] hold u):
@@ -926,7 +936,7 @@ static double feautrier_v(const OrcModel* m, Buf* b, uint32_t o, uint32_t f) {
 
 static int fo2_range(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0, uint32_t o1,
                      double* J, double* u, double* lambda_diag, uint8_t* lambda_has, int nthreads) {
-    return fo2_range_v(m, rr0, rr1, o0, o1, J, u, NULL, lambda_diag, lambda_has, nthreads);
+    return fo2_range_v(m, rr0, rr1, o0, o1, NULL, J, u, NULL, lambda_diag, lambda_has, nthreads);
 }
 
 /* Model::compute_radiation_field_feautrier_order_2_uv (model.cpp:395-433 ->
@@ -935,14 +945,18 @@ int orc_formal_solve_fo2_uv(const OrcModel* m, double* u, double* v, int nthread
     const size_t PF = (size_t)m->npoints * m->nfreqs;
     double* J = (double*)calloc(PF ? PF : 1, sizeof(double));
     if (!J) return -3;
-    const int rc = fo2_range_v(m, 0, m->hnrays, 0, m->npoints, J, u, v, NULL, NULL, nthreads);
+    const int rc = fo2_range_v(m, 0, m->hnrays, 0, m->npoints, NULL, J, u, v, NULL, NULL, nthreads);
     free(J);
     return rc;
 }
 
+/* olist != NULL: the origins olist[o0 .. o1-1] instead of o0 .. o1-1. */
 static int fo2_range_v(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o0, uint32_t o1,
-                       double* J, double* u, double* v, double* lambda_diag, uint8_t* lambda_has, int nthreads) {
-    const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
+                       const uint32_t* olist, double* J, double* u, double* v, double* lambda_diag,
+                       uint8_t* lambda_has, int nthreads) {
+    const uint32_t length =
+        2 * (olist ? ray_lengths_max_of(m, nthreads, m->use_adaptive_directions, olist + o0, o1 - o0)
+                   : orc_ray_lengths_max(m, nthreads)) + 1;
     const uint32_t P = m->npoints, F = m->nfreqs, Q = m->nquads;
     int err_any = 0;
 #ifdef _OPENMP
@@ -958,7 +972,7 @@ static int fo2_range_v(const OrcModel* m, uint32_t rr0, uint32_t rr1, uint32_t o
 #pragma omp for schedule(dynamic, 16)
                 for (int64_t oo = o0; oo < (int64_t)o1; oo++) {
                     if (bad) continue;
-                    const uint32_t o = (uint32_t)oo;
+                    const uint32_t o = olist ? olist[oo] : (uint32_t)oo;
                     const uint32_t c = b.centre;
                     b.nr[c]          = o;
                     b.shift[c]       = 1.0;
@@ -1013,6 +1027,17 @@ int orc_formal_solve_fo2(const OrcModel* m, double* J, double* u, double* lambda
 int orc_formal_solve_fo2_range(const OrcModel* m, uint32_t rr_begin, uint32_t rr_end, uint32_t o_begin,
                                uint32_t o_end, double* J, int nthreads) {
     return fo2_range(m, rr_begin, rr_end, o_begin, o_end, J, NULL, NULL, NULL, nthreads);
+}
+
+/* The whole formal solve (every ray pair) at the listed origins only: their rows of
+ * J [P][F] and of the ALO diagonal [P][L] (may be NULL) are accumulated, the others are
+ * left alone.  Used to check a sample of origins of models too large to solve whole on
+ * the host. */
+int orc_formal_solve_fo2_origins(const OrcModel* m, const uint32_t* origins, uint32_t n, double* J,
+                                 double* lambda_diag, uint8_t* lambda_has, int nthreads) {
+    for (uint32_t i = 0; i < n; i++)
+        if (origins[i] >= m->npoints) return -1;
+    return fo2_range_v(m, 0, m->hnrays, 0, n, origins, J, NULL, NULL, lambda_diag, lambda_has, nthreads);
 }
 
 /* ------------------------------------------------------------------ */

@@ -126,6 +126,10 @@ int orc_formal_solve_fo2_uv(const OrcModel* m, double* u, double* v, int nthread
  * used to time a bounded sample.  Accumulates into J (not cleared). */
 int orc_formal_solve_fo2_range(const OrcModel* m, uint32_t rr_begin, uint32_t rr_end,
                                uint32_t o_begin, uint32_t o_end, double* J, int nthreads);
+/* Every ray pair at the listed origins only (J [P][F], ALO diagonal [P][L] rows of
+ * those origins accumulated; lambda_diag / lambda_has may be NULL). */
+int orc_formal_solve_fo2_origins(const OrcModel* m, const uint32_t* origins, uint32_t n, double* J,
+                                 double* lambda_diag, uint8_t* lambda_has, int nthreads);
 
 /* Model::compute_radiation_field_shortchar_order_0 -> Solver::solve_shortchar_order_0
  * (model.cpp:313-349, solver.tpp:150-235, :1564-1757).

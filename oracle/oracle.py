@@ -253,6 +253,9 @@ def _declare(l):
     l.orc_formal_solve_fo2_range.restype = C.c_int
     l.orc_formal_solve_fo2_range.argtypes = [C.POINTER(OrcModel), C.c_uint32, C.c_uint32, C.c_uint32,
                                              C.c_uint32, _f64p, C.c_int]
+    l.orc_formal_solve_fo2_origins.restype = C.c_int
+    l.orc_formal_solve_fo2_origins.argtypes = [C.POINTER(OrcModel), _u32p, C.c_uint32, _f64p, _f64p, _u8p,
+                                               C.c_int]
     l.orc_formal_solve_sc0.restype = C.c_int
     l.orc_formal_solve_sc0.argtypes = [C.POINTER(OrcModel), _f64p, _f64p, _f64p, _f64p, _f64p, _u8p, C.c_int]
     l.orc_image_fo2.restype = C.c_int
@@ -361,6 +364,19 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle formal solve failed ({rc})")
         return J
+
+    def formal_solve_fo2_origins(self, origins, nthreads=0):
+        """J [n][F] and the ALO diagonal [n][L] at the given origins (every ray pair)."""
+        P, F, L = self.a["npoints"], self.a["nfreqs"], self.a["nlines"]
+        orig = np.ascontiguousarray(origins, np.uint32)
+        J = np.zeros((P, F))
+        lam = np.zeros((P, L))
+        has = np.zeros((P, L), np.uint8)
+        rc = lib().orc_formal_solve_fo2_origins(C.byref(self.m), _ptr(orig, _u32p), len(orig), _ptr(J, _f64p),
+                                                _ptr(lam, _f64p), _ptr(has, _u8p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle formal solve failed ({rc})")
+        return dict(J=J[orig], lambda_diag=lam[orig])
 
     def formal_solve_sc0(self, nthreads=0):
         P, F, L, R = self.a["npoints"], self.a["nfreqs"], self.a["nlines"], self.a["hnrays"]
