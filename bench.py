@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--adjoint-points", type=int, default=100_000)
     p.add_argument("--adjoint-pixels", type=int, default=256)
     p.add_argument("--adjoint-fd-points", type=int, default=64)
+    p.add_argument("--no-adjoint-j", action="store_true", help="skip the differentiable formal-solve leg")
+    p.add_argument("--adjoint-j-n", type=int, default=58, help="grid points per side of the J-adjoint model")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the library's default launch shape (for profiling one production launch)")
     return p.parse_args()
@@ -481,6 +483,107 @@ def run_adjoint(args):
             "setup_s": setup_s, "loss": float(loss.detach())}
 
 
+def run_adjoint_j(args):
+    """Differentiable formal solve: the benchmarked grid-sphere family reduced to about
+    100k points (n = 58), J of every origin as a smooth function of the per-point
+    velocity, temperature, turbulence and abundance (LTE level populations, frequencies
+    following the line widths); loss = sum of squared differences of J to the J of
+    perturbed fields (velocity x (1 + 0.05 N), temperature x 1.1).  Forward and
+    forward + backward are timed over every origin.  The gradients are checked against
+    FP64 central differences (Richardson-extrapolated) at 64 random interior points,
+    each on a loss localised to the point and its neighbours (a random weighting of
+    their J rows), along a random direction of the point's six parameters."""
+    import numpy as np
+    import torch
+    from magritte_gb300 import adjoint, loader, synthetic
+
+    t_setup = time.perf_counter()
+    raw = synthetic.grid_sphere(n=args.adjoint_j_n)
+    model = loader.to_core(raw, precision="fp64")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    solver = adjoint.FormalSolver(model)
+    setup_s = time.perf_counter() - t_setup
+    dev = dict(dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(0)
+    v0 = torch.tensor(raw.velocity, **dev)
+    T0 = torch.tensor(raw.temperature, **dev)
+    vt0 = torch.tensor(raw.vturb2, **dev)
+    ab0 = torch.tensor(raw.abundance, **dev)
+    with torch.no_grad():
+        vt = v0 * (1.0 + 0.05 * torch.tensor(rng.normal(size=(raw.npoints, 1)), **dev))
+        target = solver(vt, T0 * 1.10, vt0, ab0)
+
+    def loss_of(v, T, vtu, ab):
+        return ((solver(v, T, vtu, ab) - target) ** 2).sum()
+
+    params = [t.clone().requires_grad_(True) for t in (v0, T0, vt0, ab0)]
+    loss_of(*params).backward()  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.no_grad():
+        loss_of(v0, T0, vt0, ab0)
+    torch.cuda.synchronize()
+    fwd_s = time.perf_counter() - t0
+    params = [t.clone().requires_grad_(True) for t in (v0, T0, vt0, ab0)]
+    t0 = time.perf_counter()
+    loss = loss_of(*params)
+    loss.backward()
+    torch.cuda.synchronize()
+    fb_s = time.perf_counter() - t0
+    # finite-difference check on localised losses
+    interior = np.setdiff1d(np.arange(raw.npoints), raw.boundary2point)
+    pts = rng.choice(interior, size=min(args.adjoint_fd_points, len(interior)), replace=False)
+    cum = np.concatenate([[0], np.cumsum(raw.n_neighbors)])
+    errs, flips, t_fd = [], 0, time.perf_counter()
+    for p in pts:
+        S = np.unique(np.concatenate([[p], raw.neighbors[cum[p]:cum[p + 1]]])).astype(np.int32)
+        orig = torch.tensor(S, dtype=torch.int32, device="cuda")
+        w = torch.tensor(rng.normal(size=(len(S), solver.F)), **dev)
+        rows = torch.tensor(S, dtype=torch.long, device="cuda")
+
+        def local(v, T, vtu, ab):
+            return (solver(v, T, vtu, ab, origins=orig)[rows] * w).sum()
+
+        prm = [t.clone().requires_grad_(True) for t in (v0, T0, vt0, ab0)]
+        local(*prm).backward()
+        grads = [q.grad.detach() for q in prm]
+        dirv = [torch.zeros_like(t) for t in (v0, T0, vt0, ab0)]
+        u = rng.normal(size=6)
+        dirv[0][p] = torch.tensor(u[:3], **dev) * 1e-4 * v0.abs().max()
+        dirv[1][p] = u[3] * 1e-4 * T0[p]
+        dirv[2][p] = u[4] * 1e-4 * vt0[p]
+        dirv[3][p, 0] = u[5] * 1e-4 * ab0[p, 0]
+        an = sum(float((g * dv).sum()) for g, dv in zip(grads, dirv))
+
+        def central(eps):
+            with torch.no_grad():
+                lp = local(*[t + eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
+                lm = local(*[t - eps * dv for t, dv in zip((v0, T0, vt0, ab0), dirv)])
+            return float(lp - lm) / (2 * eps)
+
+        c1, c2 = central(1.0), central(0.5)
+        if abs(c1 - c2) > 1e-3 * abs(c2):
+            flips += 1  # the step crossed a held branch (large-shift test, line bracket)
+        elif (4.0 * c2 - c1) / 3.0 != 0.0:
+            fd = (4.0 * c2 - c1) / 3.0
+            errs.append(abs(an - fd) / abs(fd))
+    fd_s = time.perf_counter() - t_fd
+    solves = float(raw.npoints) * (raw.nrays // 2) * solver.F
+    return {"workload": f"grid_sphere {args.adjoint_j_n}^3 cutout ({raw.npoints} points), {raw.nrays} rays, "
+                        f"5-level rotor (4 lines) x nquads {raw.nquads}, LTE",
+            "forward_s": fwd_s, "forward_backward_s": fb_s,
+            "forward_solves_per_s": solves / fwd_s, "forward_backward_solves_per_s": solves / fb_s,
+            "fd_check": {"points": len(errs), "branch_crossings_skipped": flips,
+                         "max_rel_err": max(errs) if errs else None,
+                         "median_rel_err": float(np.median(errs)) if errs else None, "bar": 1e-4,
+                         "method": "Richardson-extrapolated central differences of a random weighting of the J "
+                                   "rows of the point and its neighbours, along a random direction of the point's "
+                                   "(v_x, v_y, v_z, T, vturb2, abundance)", "s": fd_s},
+            "setup_s": setup_s, "loss": float(loss.detach())}
+
+
 def C_void(x):
     import ctypes as C
     return C.c_void_p(x)
@@ -701,6 +804,7 @@ def run_ours(args, rank, ws):
     ali = None if args.no_ali else run_ali(args)
     batch = None if args.no_batch else run_batch(args)
     adj = None if args.no_adjoint else run_adjoint(args)
+    adj_j = None if args.no_adjoint_j else run_adjoint_j(args)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(raw, os.cpu_count() or 1)
@@ -740,6 +844,7 @@ def run_ours(args, rank, ws):
         "ali": ali,
         "batch": batch,
         "adjoint": adj,
+        "adjoint_j": adj_j,
     }
     print(json.dumps(line), flush=True)
 

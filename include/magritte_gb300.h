@@ -327,6 +327,34 @@ int mgr_image_new_adjoint_device(MgrModel* model, const double* raydir, uint32_t
                                  const double* gI_dev, double* g_em_dev, double* g_op_dev, double* g_iw_dev,
                                  double* g_Sp_dev, double* g_vel_dev);
 
+/* ---- Differentiable formal solve ---------------------------------------------------
+ * No reference counterpart (the reference has no derivatives): a smooth FP64 form of
+ * Model::compute_radiation_field_feautrier_order_2 (model.cpp:353-390 ->
+ * Solver::solve_feautrier_order_2, solver.tpp:458-540, :2193-2318) and its adjoint, for
+ * gradients of J.  As for the imager, the reference's single-precision powf / expf /
+ * expm1f / erff become pow / exp / expm1 / erf, and the ray traces, interpolation
+ * points, CloseLines brackets, the large-shift branch and the dtau clamp are held at
+ * the model's state.  None and CloseLines approximations, general geometry (shared or
+ * adaptive rays).  Device pointers; the calls block until done.
+ * origins_dev: NULL for every origin, else n_origins origin indices (device array);
+ * only those rows of J are written / only those rows of gJ are read. */
+
+/* Replaces the model's frequencies nu [P][F] (device pointer), e.g. after the line
+ * widths changed (Model::compute_spectral_discretisation, model.cpp:70-161). */
+int mgr_model_set_frequencies_device(MgrModel* model, const double* nu_dev);
+
+/* Smooth J_dev [P][F]: J(o, f) = sum_rr 2 w_rr u(rr, o, f) in ray-pair order. */
+int mgr_formal_solve_fo2_smooth_device(MgrModel* model, const uint32_t* origins_dev, uint32_t n_origins,
+                                       double* J_dev);
+
+/* Adjoint of mgr_formal_solve_fo2_smooth_device for d(loss)/d(J) = gJ_dev [P][F]: adds
+ * d(loss)/d(emissivity, opacity, inverse width, source emissivity/opacity) [P][L],
+ * d(loss)/d(velocity) [P][3] and d(loss)/d(nu) [P][F] into the given device arrays
+ * (not zeroed). */
+int mgr_formal_solve_fo2_adjoint_device(MgrModel* model, const uint32_t* origins_dev, uint32_t n_origins,
+                                        const double* gJ_dev, double* g_em_dev, double* g_op_dev, double* g_iw_dev,
+                                        double* g_Sp_dev, double* g_vel_dev, double* g_nu_dev);
+
 /* ---- Many-model batch ------------------------------------------------------------
  * No single reference counterpart: the reference solves one Model per call
  * (Model::compute_radiation_field_feautrier_order_2, src/model/model.cpp:353-390);

@@ -1,5 +1,6 @@
-"""Differentiable new imager: gradients of compute_image_new images with respect to
-the per-point velocity, temperature, turbulence and abundance of a model.
+"""Differentiable new imager and formal solve: gradients of compute_image_new images
+and of the mean intensity J of compute_radiation_field_feautrier_order_2 with respect
+to the per-point velocity, temperature, turbulence and abundance of a model.
 
 The reference has no derivatives.  Its imager (Model::compute_image_new,
 src/model/model.cpp:977-1013 -> Solver::image_feautrier_order_2_new_imager,
@@ -20,7 +21,21 @@ src/solver/solver.tpp:576-627) becomes a differentiable function in two layers:
   and Lines::set_inverse_width (lines.tpp:45-59), written as torch operations so
   autograd chains them into the kernel's derivatives.
 
-PyTorch is the autograd plumbing here; every image and adjoint is computed by the
+The formal solve (Model::compute_radiation_field_feautrier_order_2, model.cpp:353-390
+-> Solver::solve_feautrier_order_2, solver.tpp:458-540, :2193-2318) is differentiated the
+same way:
+
+* ``FormalSolveFunction``: J [P][F] as a function of the velocity, the line data and
+  the frequencies nu [P][F] (which move with the line widths: Model::
+  compute_spectral_discretisation, model.cpp:70-161).  Forward and backward are
+  mgr_formal_solve_fo2_smooth_device / mgr_formal_solve_fo2_adjoint_device: the smooth
+  FP64 two-sided Feautrier solve and its adjoint, which recomputes every ray pair's
+  elimination factors in the backward pass.  An optional list of origins restricts
+  both to those rows of J.
+* ``FormalSolver``: line data and frequencies from temperature, turbulence and
+  abundance as torch operations.
+
+PyTorch is the autograd plumbing here; every image, J and adjoint is computed by the
 library's kernels, and the calls fail if the CUDA library is missing."""
 import ctypes as C
 
@@ -88,6 +103,139 @@ class ImageNewFunction(torch.autograd.Function):
         return None, None, None, None, None, g_vel, g_em, g_op, g_iw
 
 
+def _species(model, device):
+    """Per-species line data of a core.Model as torch tensors."""
+    dev = dict(dtype=torch.float64, device=device)
+    out = []
+    for ls in model.lines.lineProducingSpecies:
+        ld = ls.linedata
+        out.append(dict(
+            num=int(ld.num), nlev=int(ld.nlev), nrad=int(ld.nrad), inverse_mass=float(ld.inverse_mass),
+            energy=torch.tensor(np.array(ld.energy), **dev), weight=torch.tensor(np.array(ld.weight), **dev),
+            frequency=torch.tensor(np.array(ld.frequency), **dev), A=torch.tensor(np.array(ld.A), **dev),
+            Ba=torch.tensor(np.array(ld.Ba), **dev), Bs=torch.tensor(np.array(ld.Bs), **dev),
+            irad=torch.tensor(np.array(ld.irad), dtype=torch.long, device=device),
+            jrad=torch.tensor(np.array(ld.jrad), dtype=torch.long, device=device),
+            roots=torch.tensor(np.array(ls.quadrature.roots), **dev)))
+    return out
+
+
+def line_data(species, min_em, min_op, temperature, vturb2, abundance):
+    """Emissivity, opacity and inverse width [P][L] from temperature [P], vturb2 [P]
+    ((v_turb/c)^2) and abundance [P][nspecs] (number densities): LTE populations
+    (LineProducingSpecies::update_using_LTE, lineProducingSpecies.tpp:52-75),
+    Lines::set_emissivity_and_opacity with the reference's floors (lines.tpp:29-40),
+    Lines::set_inverse_width (lines.tpp:45-59), as torch operations."""
+    em_cols, op_cols, iw_cols = [], [], []
+    T = temperature[:, None]
+    for s in species:
+        pop = s["weight"][None, :] * torch.exp(-s["energy"][None, :] / (KB * T))
+        pop = pop * (abundance[:, s["num"]][:, None] / pop.sum(dim=1, keepdim=True))
+        up, lo = pop[:, s["irad"]], pop[:, s["jrad"]]
+        nu = s["frequency"][None, :]
+        em = nu * HH_OVER_FOUR_PI * s["A"][None, :] * up
+        op = nu * HH_OVER_FOUR_PI * (lo * s["Ba"][None, :] - up * s["Bs"][None, :])
+        em_cols.append(torch.clamp(em, min=min_em))
+        op_cols.append(torch.clamp(op, min=min_op))
+        width = nu * torch.sqrt(TWO_KB_OVER_AMU_CC_SQUARED * s["inverse_mass"] * T + vturb2[:, None])
+        iw_cols.append(1.0 / width)
+    return (torch.cat(em_cols, dim=1).contiguous(), torch.cat(op_cols, dim=1).contiguous(),
+            torch.cat(iw_cols, dim=1).contiguous())
+
+
+def line_frequencies(species, temperature, vturb2):
+    """nu [P][F] of the line spectral discretisation (Model::compute_spectral_discretisation,
+    model.cpp:70-161): nu(p, f) = line + width(p) root_z for f = line * nquads + z, with the
+    line's Doppler width from temperature and turbulence."""
+    cols = []
+    T = temperature[:, None]
+    for s in species:
+        pw = torch.sqrt(TWO_KB_OVER_AMU_CC_SQUARED * s["inverse_mass"] * T + vturb2[:, None])  # [P][1]
+        for k in range(s["nrad"]):
+            line = s["frequency"][k]
+            cols.append(line + (line * pw) * s["roots"][None, :])
+    return torch.cat(cols, dim=1).contiguous()
+
+
+class FormalSolveFunction(torch.autograd.Function):
+    """J = formal_solve(velocity, emissivity, opacity, inverse_width, nu) [P][F]; with
+    ``origins`` (an int32 CUDA tensor) only those rows are computed (others are 0)."""
+
+    @staticmethod
+    def forward(ctx, handle, origins, P, F, velocity, emissivity, opacity, inverse_width, nu):
+        lib = _abi.load()
+        for t, n in ((velocity, "velocity"), (emissivity, "emissivity"), (opacity, "opacity"),
+                     (inverse_width, "inverse_width"), (nu, "nu")):
+            _check_f64_cuda(t, n)
+        torch.cuda.current_stream().synchronize()
+        _set_inputs(lib, handle, velocity, emissivity, opacity, inverse_width, nu)
+        J = torch.zeros((P, F), dtype=torch.float64, device=velocity.device)
+        optr, n_o = (None, 0) if origins is None else (_ptr(origins), int(origins.numel()))
+        _abi._check(lib.mgr_formal_solve_fo2_smooth_device(handle, optr, n_o, _ptr(J)))
+        ctx.handle, ctx.origins = handle, origins
+        ctx.save_for_backward(velocity, emissivity, opacity, inverse_width, nu)
+        return J
+
+    @staticmethod
+    def backward(ctx, gJ):
+        lib = _abi.load()
+        velocity, em, op, iw, nu = ctx.saved_tensors
+        gJ = gJ.contiguous().to(torch.float64)
+        torch.cuda.current_stream().synchronize()
+        _set_inputs(lib, ctx.handle, velocity, em, op, iw, nu)
+        g_em, g_op, g_iw, g_Sp = (torch.zeros_like(em) for _ in range(4))
+        g_vel = torch.zeros_like(velocity)
+        g_nu = torch.zeros_like(nu)
+        optr, n_o = (None, 0) if ctx.origins is None else (_ptr(ctx.origins), int(ctx.origins.numel()))
+        _abi._check(lib.mgr_formal_solve_fo2_adjoint_device(ctx.handle, optr, n_o, _ptr(gJ), _ptr(g_em), _ptr(g_op),
+                                                            _ptr(g_iw), _ptr(g_Sp), _ptr(g_vel), _ptr(g_nu)))
+        g_em = g_em + g_Sp / op
+        g_op = g_op - g_Sp * em / (op * op)
+        return None, None, None, None, g_vel, g_em, g_op, g_iw, g_nu
+
+
+def _set_inputs(lib, handle, velocity, em, op, iw, nu):
+    _abi._check(lib.mgr_model_set_velocity_device(handle, _ptr(velocity)))
+    _abi._check(lib.mgr_model_set_line_data_device(handle, _ptr(em), _ptr(op), _ptr(iw)))
+    _abi._check(lib.mgr_model_set_frequencies_device(handle, _ptr(nu)))
+
+
+class FormalSolver:
+    """Differentiable Model::compute_radiation_field_feautrier_order_2 of a core.Model:
+    J [P][F] from velocity [P][3] (v/c), temperature [P], vturb2 [P] and abundance
+    [P][nspecs] (number densities), with the line data and the line frequencies
+    recomputed in torch.  The model needs its line spectral discretisation, line widths
+    and level populations set up; its device copy (core.Model.upload) is used, and its
+    velocities, line data and frequencies are replaced by each call.  The trace-fixed
+    structure (interpolation points, line brackets, large-shift branches) follows the
+    model's host state at construction or ``refresh()``."""
+
+    def __init__(self, model, device=None):
+        self.model = model
+        prm = model.parameters
+        self.P, self.F, self.L = prm.npoints(), prm.nfreqs(), prm.nlines()
+        self.device = torch.device(device if device is not None else "cuda")
+        self.min_em = float(prm.min_line_emissivity)
+        self.min_op = float(prm.min_line_opacity)
+        self.species = _species(model, self.device)
+        self.handle = None
+        self.refresh()
+
+    def refresh(self):
+        self.model.release_device()
+        self.handle = C.c_void_p(self.model.upload())
+
+    def solve(self, velocity, emissivity, opacity, inverse_width, nu, origins=None):
+        """J [P][F] from the kernel's direct inputs (differentiable)."""
+        return FormalSolveFunction.apply(self.handle, origins, self.P, self.F, velocity.contiguous(), emissivity,
+                                         opacity, inverse_width, nu)
+
+    def __call__(self, velocity, temperature, vturb2, abundance, origins=None):
+        em, op, iw = line_data(self.species, self.min_em, self.min_op, temperature, vturb2, abundance)
+        nu = line_frequencies(self.species, temperature, vturb2)
+        return self.solve(velocity, em, op, iw, nu, origins)
+
+
 class NewImager:
     """Differentiable Model::compute_image_new(raydir, nx, ny) of a core.Model.
 
@@ -106,17 +254,7 @@ class NewImager:
         self.device = torch.device(device if device is not None else "cuda")
         self.min_em = float(prm.min_line_emissivity)
         self.min_op = float(prm.min_line_opacity)
-        dev = dict(dtype=torch.float64, device=self.device)
-        self.species = []
-        for ls in model.lines.lineProducingSpecies:
-            ld = ls.linedata
-            self.species.append(dict(
-                num=int(ld.num), nlev=int(ld.nlev), nrad=int(ld.nrad), inverse_mass=float(ld.inverse_mass),
-                energy=torch.tensor(np.array(ld.energy), **dev), weight=torch.tensor(np.array(ld.weight), **dev),
-                frequency=torch.tensor(np.array(ld.frequency), **dev), A=torch.tensor(np.array(ld.A), **dev),
-                Ba=torch.tensor(np.array(ld.Ba), **dev), Bs=torch.tensor(np.array(ld.Bs), **dev),
-                irad=torch.tensor(np.array(ld.irad), dtype=torch.long, device=self.device),
-                jrad=torch.tensor(np.array(ld.jrad), dtype=torch.long, device=self.device)))
+        self.species = _species(model, self.device)
         self.handle = None
         self.refresh()
 
@@ -130,21 +268,7 @@ class NewImager:
         """Emissivity, opacity and inverse width [P][L] (torch, differentiable) from
         temperature [P], vturb2 [P] ((v_turb/c)^2) and abundance [P][nspecs]
         (number densities)."""
-        em_cols, op_cols, iw_cols = [], [], []
-        T = temperature[:, None]
-        for s in self.species:
-            pop = s["weight"][None, :] * torch.exp(-s["energy"][None, :] / (KB * T))
-            pop = pop * (abundance[:, s["num"]][:, None] / pop.sum(dim=1, keepdim=True))
-            up, lo = pop[:, s["irad"]], pop[:, s["jrad"]]
-            nu = s["frequency"][None, :]
-            em = nu * HH_OVER_FOUR_PI * s["A"][None, :] * up
-            op = nu * HH_OVER_FOUR_PI * (lo * s["Ba"][None, :] - up * s["Bs"][None, :])
-            em_cols.append(torch.clamp(em, min=self.min_em))
-            op_cols.append(torch.clamp(op, min=self.min_op))
-            width = nu * torch.sqrt(TWO_KB_OVER_AMU_CC_SQUARED * s["inverse_mass"] * T + vturb2[:, None])
-            iw_cols.append(1.0 / width)
-        return (torch.cat(em_cols, dim=1).contiguous(), torch.cat(op_cols, dim=1).contiguous(),
-                torch.cat(iw_cols, dim=1).contiguous())
+        return line_data(self.species, self.min_em, self.min_op, temperature, vturb2, abundance)
 
     def render(self, raydir, velocity, emissivity, opacity, inverse_width):
         """Image [nx*ny][F] along raydir from velocity / line data (differentiable)."""

@@ -23,7 +23,7 @@ BUILD = os.path.join(PKG, "_build")
 GPU_LIB = os.path.join(BUILD, "libmgr_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["mgr_abi.cu", "mgr_fo2.cu", "mgr_noalloc.cu", "mgr_ali.cu", "mgr_sc0.cu", "mgr_image.cu", "mgr_batch.cu", "mgr_adjoint.cu", "mgr_peaks.cu"]
+CU_SOURCES = ["mgr_abi.cu", "mgr_fo2.cu", "mgr_noalloc.cu", "mgr_ali.cu", "mgr_sc0.cu", "mgr_image.cu", "mgr_batch.cu", "mgr_adjoint.cu", "mgr_adjoint_fo2.cu", "mgr_peaks.cu"]
 
 
 def _nvcc():

@@ -11,6 +11,7 @@
 
 #include "../../../include/magritte_gb300.h"
 #include "../mgr_adjoint.cuh"
+#include "../mgr_adjoint_fo2.cuh"
 #include "../mgr_image.cuh"
 #include "../mgr_scale.h"
 #include "../mgr_solve.cuh"
@@ -768,6 +769,93 @@ extern "C" int mgr_emu_image_new_adjoint(const MgrModelDesc* d, const double* ra
                                 : image_lane_adj<APPROX_CLOSELINES>(m, m.sorted_line, start, nu, bk, nb, g, scr, acc);
             if (!ok) fail = 1;
         }
+    });
+    if (rc == MGR_OK && fail) rc = MGR_ERR_CAPACITY;
+    return rc;
+}
+
+// ---- differentiable formal solve (fo2_s_kernel / fo2_adj_kernel lane code) ----
+
+namespace {
+
+// Runs fn(o, rr, bk, nb, fw, nf) for every origin and ray pair (host traces).
+template <typename Fn>
+int for_each_ray_pair(const DevModel& m, Fn fn) {
+    HalfBuf b(kCap), fbuf(kCap);
+    HalfSmem bk = b.view(), fw = fbuf.view();
+    for (uint32_t o = 0; o < m.P; o++)
+        for (uint32_t rr = 0; rr < m.hnrays; rr++) {
+            const int nb = trace_half_host(m, o, rr, kCap, bk);
+            const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw);
+            if (nb < 0 || nf < 0) return (nb == kTraceOverCapacity || nf == kTraceOverCapacity) ? MGR_ERR_CAPACITY
+                                                                                              : MGR_ERR_TRACE;
+            fn(o, rr, bk, nb, fw, nf);
+        }
+    return MGR_OK;
+}
+
+}  // namespace
+
+// Smooth J [P][F] (every origin), summed over ray pairs in order.
+extern "C" int mgr_emu_fo2_smooth(const MgrModelDesc* d, double* J) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    std::fill(J, J + (size_t)m.P * m.F, 0.0);
+    return for_each_ray_pair(m, [&](uint32_t o, uint32_t rr, const HalfSmem& bk, int nb, const HalfSmem& fw, int nf) {
+        const double wt = 2.0 * ray_w(m, o, rr);
+        for (uint32_t l = 0; l < m.L; l++)
+            for (uint32_t q = 0; q < m.Q; q++) {
+                const uint32_t f = m.lq2f[(size_t)l * m.Q + q];
+                const double nu = m.nu[(size_t)o * m.F + f];
+                const LaneS r = m.approx == APPROX_NONE
+                                    ? solve_lane_s<APPROX_NONE>(m, m.sorted_line, o, nu, l, bk, nb, fw, nf, nullptr)
+                                    : solve_lane_s<APPROX_CLOSELINES>(m, m.sorted_line, o, nu, l, bk, nb, fw, nf,
+                                                                      nullptr);
+                J[(size_t)o * m.F + f] += r.u * wt;
+            }
+    });
+}
+
+// Adjoint of mgr_emu_fo2_smooth for d(loss)/d(J) = gJ: adds into g_em, g_op, g_iw, g_Sp
+// [P][L], g_vel [P][3] and g_nu [P][F].
+extern "C" int mgr_emu_fo2_adjoint(const MgrModelDesc* d, const double* gJ, double* g_em, double* g_op, double* g_iw,
+                                   double* g_Sp, double* g_vel, double* g_nu) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    std::vector<double> scratch;
+    int fail = 0;
+    int rc = for_each_ray_pair(m, [&](uint32_t o, uint32_t rr, const HalfSmem& bk, int nb, const HalfSmem& fw,
+                                      int nf) {
+        const uint32_t ar = m.antipod[rr];
+        size_t pairs = 2;
+        for (int s = 0; s < nb; s++) pairs += m.nint_all[bk.eid[s]];
+        for (int s = 0; s < nf; s++) pairs += m.nint_all[fw.eid[s]];
+        if (scratch.size() < 4 * pairs) scratch.resize(4 * pairs);
+        const Fo2Scratch scr{scratch.data(), 1, (uint32_t)pairs};
+        const double* db = ray_dir(m, o, rr);
+        const double* df = ray_dir(m, o, ar);
+        const AdjAcc acc_b{AdjGrads{g_em, g_op, g_iw, g_Sp, g_vel, {db[0], db[1], db[2]}}, m.L};
+        const AdjAcc acc_f{AdjGrads{g_em, g_op, g_iw, g_Sp, g_vel, {df[0], df[1], df[2]}}, m.L};
+        const double wt = 2.0 * ray_w(m, o, rr);
+        for (uint32_t l = 0; l < m.L; l++)
+            for (uint32_t q = 0; q < m.Q; q++) {
+                const uint32_t f = m.lq2f[(size_t)l * m.Q + q];
+                const double gu = gJ[(size_t)o * m.F + f] * wt;
+                if (gu == 0.0) continue;
+                const double nu = m.nu[(size_t)o * m.F + f];
+                double gvb = 0.0, gvf = 0.0, gn = 0.0;
+                const bool ok =
+                    m.approx == APPROX_NONE
+                        ? solve_lane_s_adj<APPROX_NONE>(m, m.sorted_line, o, nu, l, bk, nb, fw, nf, gu, scr, acc_b,
+                                                        acc_f, gvb, gvf, gn)
+                        : solve_lane_s_adj<APPROX_CLOSELINES>(m, m.sorted_line, o, nu, l, bk, nb, fw, nf, gu, scr,
+                                                              acc_b, acc_f, gvb, gvf, gn);
+                if (!ok) fail = 1;
+                for (int k = 0; k < 3; k++) g_vel[3 * (size_t)o + k] += gvb * db[k] + gvf * df[k];
+                g_nu[(size_t)o * m.F + f] += gn;
+            }
     });
     if (rc == MGR_OK && fail) rc = MGR_ERR_CAPACITY;
     return rc;
