@@ -517,8 +517,9 @@ uint64_t mgr_launch_count(void);
  * conversion), 5 MUFU.RCP64H (rcp.approx.ftz.f64).  Eight independent chains per
  * thread, `iterations` steps each, over SMs x 8 CTAs of 256 threads; the best of three
  * timed launches.  Outputs (any may be NULL): thread operations per second for the
- * whole device, thread operations per SM clock cycle per SM (from the kernel's own
- * clock64 counts), and the launch time in ms.  Blocks. */
+ * whole device, thread operations per SM clock cycle per SM (each SM's span from its
+ * first CTA's start to its last CTA's end on its own clock64), and the launch time in
+ * ms.  Blocks. */
 int mgr_measure_pipe_rate(int kind, uint32_t iterations, double* thread_ops_per_s,
                           double* thread_ops_per_clk_per_sm, float* ms);
 

@@ -36,7 +36,7 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
         const double Rcos = dot3_rn(po.x, po.y, po.z, d[0], d[1], d[2]);
         const double Rsin2 = dsub_rn(sqnorm_rn(po), dmul_rn(Rcos, Rcos));
         h.shift0 = origin_shift(m, frame, o, r);
-        h.dsh0 = (float)dsub_rn(h.shift0, 1.0);
+        set_dsh0(h, h.shift0);
         while (true) {
             uint32_t nxt;
             double dZl;
@@ -48,7 +48,7 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
             h.dZ[count] = dZl;
             const double s = shift_sph(m, frame, o, r, nxt, Z, d);
             h.shift[count] = s;
-            h.dsh[count] = (float)dsub_rn(s, 1.0);
+            store_dsh(h, count, s);
             h.dzs[count] = (float)dZl * m.dz_scale;
             count++;
             if (m.p2b[nxt] != m.P) break;
@@ -87,7 +87,7 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
         h.dZ[count] = dZl;
         const double s = frame ? shift_rest(m, r, nxt, d) : shift_comoving(m, o, nxt, d);
         h.shift[count] = s;
-        h.dsh[count] = (float)dsub_rn(s, 1.0);
+        store_dsh(h, count, s);
         h.dzs[count] = (float)dZl * m.dz_scale;
         count++;
         if (m.p2b[nxt] != m.P) break;
@@ -105,7 +105,7 @@ float to_f32_floor_host(double x) {
 struct EmuModel {
     std::vector<double4_32a> pos, vel, edge;
     std::vector<double> ub, Sp;
-    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f;
+    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f, iw_lo, line_df;
     std::vector<uint16_t> nint, nint_all;
     std::vector<uint32_t> lq2f, corr_line;
     DevModel m{};
@@ -135,6 +135,7 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     x.em_f.resize(PL);
     x.op_f.resize(PL);
     x.iw_f.resize(PL);
+    x.iw_lo.resize(PL);
     x.Sp_f.resize(PL);
     x.dsm_f.resize(P);
     x.ub_f.resize(P);
@@ -150,6 +151,7 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
         x.em_f[i] = to_f32_floor_host(d->emissivity[i] * Ke);
         x.op_f[i] = to_f32_floor_host(d->opacity[i] * Ko);
         x.iw_f[i] = (float)d->inverse_width[i];
+        x.iw_lo[i] = (float)(d->inverse_width[i] - (double)x.iw_f[i]);
         x.Sp_f[i] = to_f32_floor_host(x.Sp[i] * (Ke / Ko));
     }
     DevModel& m = x.m;
@@ -178,6 +180,13 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     line_offset_tables(d->line, d->sorted_line, L, x.dls, x.dll);
     m.dls = x.dls.data();
     m.dll = x.dll.data();
+    x.line_df.resize(2 * (size_t)L);
+    for (uint32_t l = 0; l < L; l++) {
+        x.line_df[2 * l] = (float)d->line[l];
+        x.line_df[2 * l + 1] = (float)(d->line[l] - (double)x.line_df[2 * l]);
+    }
+    m.line_df = x.line_df.data();
+    m.iw_lo = x.iw_lo.data();
     // the maps of an imaging spectral discretisation are unset: keep only valid
     // (line, quadrature point) entries, and measure each frequency from its nearest
     // line, as mgr_model_create does
@@ -240,21 +249,15 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
 struct HalfBuf {
     std::vector<double> sh, dz;
     std::vector<uint32_t> id, ei;
-    std::vector<float> ds, dzs;
-    explicit HalfBuf(uint32_t cap) : sh(cap), dz(cap), id(cap), ei(cap), ds(cap), dzs(cap) {}
-    HalfSmem view() { return HalfSmem{id.data(), sh.data(), dz.data(), ds.data(), dzs.data(), ei.data()}; }
+    std::vector<float> ds, dzs, dl;
+    explicit HalfBuf(uint32_t cap) : sh(cap), dz(cap), id(cap), ei(cap), ds(cap), dzs(cap), dl(cap) {}
+    HalfSmem view() {
+        HalfSmem h{id.data(), sh.data(), dz.data(), ds.data(), dzs.data(), ei.data()};
+        h.dsl = dl.data();
+        return h;
+    }
 };
 
-LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {
-    LaneCtx c;
-    c.o = o;
-    c.f = f;
-    c.l0 = m.corr_line[f];
-    c.freq = m.nu[(size_t)o * m.F + f];
-    c.fq = (float)c.freq;
-    c.a0 = (float)(c.freq - m.line[c.l0]);
-    return c;
-}
 
 constexpr uint32_t kCap = 1u << 16;
 
@@ -492,8 +495,8 @@ extern "C" int mgr_emu_image(const MgrModelDesc* d, int precision, uint32_t rr, 
             const double shf = origin_shift(m, 1, o, ar);
             bk.shift0 = shb;
             fw.shift0 = shf;
-            bk.dsh0 = (float)(shb - 1.0);
-            fw.dsh0 = (float)(shf - 1.0);
+            set_dsh0(bk, shb);
+            set_dsh0(fw, shf);
             bk.cshift = fw.cshift = shb;
             const int nb = trace_half_host(m, o, rr, kCap, bk, 1);
             const int nf = trace_half_host(m, o, m.antipod[rr], kCap, fw, 1);
@@ -531,8 +534,8 @@ extern "C" int mgr_emu_image_for_point(const MgrModelDesc* d, int precision, uin
     const double shf = origin_shift(m, 1, p, ar);
     bk.shift0 = shb;
     fw.shift0 = shf;
-    bk.dsh0 = (float)(shb - 1.0);
-    fw.dsh0 = (float)(shf - 1.0);
+    set_dsh0(bk, shb);
+    set_dsh0(fw, shf);
     bk.cshift = fw.cshift = shb;
     const int nb = trace_half_host(m, p, rr, kCap, bk, 1);
     const int nf = trace_half_host(m, p, ar, kCap, fw, 1);
@@ -682,7 +685,7 @@ int trace_image_host(const DevModel& m, const double* org, const ImagePlane& ip,
         const double4_32a v = m.vel[h.ids[s]];
         const double sh = 1.0 + dot3_rn(v.x, v.y, v.z, dx, dy, dz);
         h.shift[s] = sh;
-        h.dsh[s] = (float)(sh - 1.0);
+        store_dsh(h, s, sh);
         h.dzs[s] = (float)h.dZ[s] * m.dz_scale;
     }
     return count;

@@ -1,5 +1,6 @@
 // C ABI of libmgr_gpu.so: model upload, formal-solve entry points, status handling.
 #include <atomic>
+#include <mutex>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -98,6 +99,37 @@ void set_line_scales(MgrModel* m, double Ke, double Ko) {
     m->dm.min_op_s = (float)(m->dm.min_opacity * m->scales.Ko);
     m->dm.dz_scale = (float)(1.0 / m->scales.Ko);
     m->dm.s_scale = (float)(m->scales.Ko / m->scales.Ke);
+}
+
+// One correctly rounded erff table per device (51 MB), shared by every model on it.
+static std::mutex g_erf_mutex;
+static const float* g_erf_band[64] = {};
+
+cudaError_t erf_band_table(const float** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_erf_mutex);
+    if (!g_erf_band[dev]) {
+        int nsm = 1;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        void* p = nullptr;
+        e = cudaMalloc(&p, (size_t)kErfBandCount * sizeof(float));
+        if (e != cudaSuccess) return e;
+        cudaStream_t s = nullptr;
+        e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = fill_erf_band(static_cast<float*>(p), s, nsm);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (s) cudaStreamDestroy(s);
+        if (e != cudaSuccess) {
+            cudaFree(p);
+            return e;
+        }
+        g_erf_band[dev] = static_cast<const float*>(p);
+    }
+    *out = g_erf_band[dev];
+    return cudaSuccess;
 }
 
 static int size_model(MgrModel* model) {
@@ -290,6 +322,11 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     }
     std::vector<float> dls, dll;
     line_offset_tables(d->line, d->sorted_line, L, dls, dll);
+    std::vector<float> line_df(2 * (size_t)L);  // double-float line centres (hi, lo)
+    for (uint32_t l = 0; l < L; l++) {
+        line_df[2 * l] = (float)d->line[l];
+        line_df[2 * l + 1] = (float)(d->line[l] - (double)line_df[2 * l]);
+    }
     std::vector<uint32_t> lq2f((size_t)L * d->nquads, 0xffffffffu);
     for (uint32_t f = 0; f < F; f++) {
         const size_t i = (size_t)d->corr_line[f] * d->nquads + d->corr_z[f];
@@ -315,6 +352,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.dls, dls.data(), (size_t)L * L)) != cudaSuccess) break;
         if ((e = upload(m, &dm.lq2f, lq2f.data(), lq2f.size())) != cudaSuccess) break;
         if ((e = upload(m, &dm.dll, dll.data(), (size_t)L * L)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.line_df, line_df.data(), line_df.size())) != cudaSuccess) break;
         if ((e = dalloc(m, &m->em, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->op, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->iw, PL)) != cudaSuccess) break;
@@ -324,6 +362,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = dalloc(m, &m->op_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->iw_f, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->Sp_f, PL)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->iw_lo, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->nint, (ET ? ET : 1) * (size_t)L)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->nint_all, ET ? ET : 1)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->em, d->emissivity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
@@ -363,6 +402,12 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.op_f = m->op_f;
     dm.iw_f = m->iw_f;
     dm.Sp_f = m->Sp_f;
+    dm.iw_lo = m->iw_lo;
+    if ((e = erf_band_table(&dm.erf_band)) != cudaSuccess) {
+        int rc = cuda_fail(e, "erff table");
+        mgr_model_free(m);
+        return rc;
+    }
     dm.nint = m->nint;
     dm.nint_all = m->nint_all;
     apply_scales(m, d->emissivity, d->opacity);

@@ -110,13 +110,7 @@ __global__ void __launch_bounds__(256, MINB)
             for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
                 const uint32_t f = f0 + lane;
                 if (f < m.F) {
-                    LaneCtx c;
-                    c.o = o;
-                    c.f = f;
-                    c.l0 = m.corr_line[f];
-                    c.freq = m.nu[(size_t)o * m.F + f];
-                    c.fq = (float)c.freq;
-                    c.a0 = (float)(c.freq - m.line[c.l0]);
+                    const LaneCtx c = lane_ctx(m, o, f);
                     const LaneResult r = solve_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
                     Jacc[f] += r.u * 2.0 * w2;
                     LDr[f] = r.solved ? r.Ldiag : 0.0;

@@ -96,6 +96,14 @@ struct DevModel {
     const uint32_t* lq2f;        // [L][Q] frequency of (line, quadrature point), ~0u if none
     // Split precision keeps FP32 line data in scaled units (exact powers of two):
     // em_f = em * Ke, op_f = op * Ko, Sp_f = Sp * Ke / Ko.
+    // Low parts of double-float copies (value = hi + lo, about 48 significant bits) for
+    // split precision's same-wing erf arguments: the line centres [L][2] (hi, lo) and
+    // the inverse widths iw - (double)iw_f [P][L].
+    const float* line_df;
+    const float* iw_lo;
+    // (float)erf((double)x) for every float x in [kErfBandLo, 3.919206), indexed by the
+    // bit pattern of x minus that of kErfBandLo (one table per device, owned by the library)
+    const float* erf_band;
     const float* dls;            // [L][L] (float)(sorted_line[s] - line[l0]) at l0*L + s
     const float* dll;            // [L][L] (float)(line[l] - line[l0]) at l0*L + l
     float max_dist_f;            // (float)max_dist
@@ -288,6 +296,11 @@ MGR_HD uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt
     const uint32_t n = (c == c && c > 0.0) ? (c < 4294967295.0 ? (uint32_t)c : 0xffffffffu) : 0u;
     return n > 1 ? n : 1;
 }
+
+// Range of the correctly rounded erff table of split precision: every float in
+// [kErfBandLo, 3.919206) (12.8 M entries, 51 MB).
+constexpr float kErfBandLo = 1.4375f;
+constexpr uint32_t kErfBandCount = 0x407ad445u - 0x3fb80000u;  // bits(3.919206f) - bits(1.4375f)
 
 // Correctly rounded single-precision erf (double erf rounded once to float).
 // For |x| >= 3.919206f (the smallest float whose erf rounds to 1.0f) the value is

@@ -18,7 +18,7 @@ __device__ __forceinline__ float to_f32_floor(double x) {
 __global__ void line_tables_kernel(const double* __restrict__ em, const double* __restrict__ op,
                                    const double* __restrict__ iw, double* __restrict__ Sp, float* __restrict__ em_f,
                                    float* __restrict__ op_f, float* __restrict__ iw_f, float* __restrict__ Sp_f,
-                                   size_t n, double Ke, double Ko) {
+                                   float* __restrict__ iw_lo, size_t n, double Ke, double Ko) {
     const double KeKo = Ke / Ko;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const double e = em[i], o = op[i];
@@ -26,9 +26,27 @@ __global__ void line_tables_kernel(const double* __restrict__ em, const double* 
         Sp[i] = s;
         em_f[i] = to_f32_floor(e * Ke);
         op_f[i] = to_f32_floor(o * Ko);
-        iw_f[i] = (float)iw[i];
+        const float w = (float)iw[i];
+        iw_f[i] = w;
+        iw_lo[i] = (float)(iw[i] - (double)w);
         Sp_f[i] = to_f32_floor(s * KeKo);
     }
+}
+
+// ---------------------------------------------------------------------------------
+// Correctly rounded erff table of split precision's same-wing erf differences:
+// (float)erf((double)x) for every float x in [kErfBandLo, 3.919206).
+// ---------------------------------------------------------------------------------
+__global__ void erf_band_kernel(float* __restrict__ t) {
+    const uint32_t base = __float_as_uint(kErfBandLo);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < kErfBandCount; i += gridDim.x * blockDim.x)
+        t[i] = (float)erf((double)__uint_as_float(base + i));
+}
+
+cudaError_t fill_erf_band(float* table, cudaStream_t stream, int sm_count) {
+    count_launch();
+    erf_band_kernel<<<sm_count * 8, 256, 0, stream>>>(table);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------------
@@ -193,13 +211,7 @@ __global__ void __launch_bounds__(256, MINB)
         for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
             const uint32_t f = f0 + lane;
             if (f < m.F) {
-                LaneCtx c;
-                c.o = o;
-                c.f = f;
-                c.l0 = m.corr_line[f];
-                c.freq = m.nu[(size_t)o * m.F + f];
-                c.fq = (float)c.freq;
-                c.a0 = (float)(c.freq - m.line[c.l0]);
+                const LaneCtx c = lane_ctx(m, o, f);
                 const LaneResult r = solve_lane<MODE, AP, UV>(m, sl, c, bk, nb, fw, nf);
                 Ui[f] = r.u;
                 if constexpr (UV) V[(size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F + f] = r.v;
@@ -411,8 +423,8 @@ cudaError_t launch_line_tables(MgrModel* model) {
     const int blocks = (int)((n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads : 152 * 16);
     count_launch();
     line_tables_kernel<<<blocks > 0 ? blocks : 1, threads, 0, model->stream>>>(
-        model->em, model->op, model->iw, model->Sp, model->em_f, model->op_f, model->iw_f, model->Sp_f, n,
-        model->scales.Ke, model->scales.Ko);
+        model->em, model->op, model->iw, model->Sp, model->em_f, model->op_f, model->iw_f, model->Sp_f, model->iw_lo,
+        n, model->scales.Ke, model->scales.Ko);
     return cudaGetLastError();
 }
 

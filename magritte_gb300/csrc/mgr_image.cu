@@ -39,8 +39,8 @@ __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, ui
         const double shf = origin_shift(m, 1, o, ar);
         bk.shift0 = shb;
         fw.shift0 = shf;
-        bk.dsh0 = (float)dsub_rn(shb, 1.0);
-        fw.dsh0 = (float)dsub_rn(shf, 1.0);
+        set_dsh0(bk, shb);
+        set_dsh0(fw, shf);
         bk.cshift = fw.cshift = shb;
         const int nb = trace_half<true, 1>(m, o, rr, cap, bk, lane, status);
         const int nf = trace_half<true, 1>(m, o, ar, cap, fw, lane, status);
@@ -48,13 +48,7 @@ __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, ui
         for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
             const uint32_t f = f0 + lane;
             if (f < m.F) {
-                LaneCtx c;
-                c.o = o;
-                c.f = f;
-                c.l0 = m.corr_line[f];
-                c.freq = m.nu[(size_t)o * m.F + f];
-                c.fq = (float)c.freq;
-                c.a0 = (float)(c.freq - m.line[c.l0]);
+                const LaneCtx c = lane_ctx(m, o, f);
                 const double v = image_lane<MODE, AP, TAU>(m, sl, c, bk, nb, fw, nf);
                 I[(size_t)o * m.F + f] = v;
                 if (!isfinite(v)) atomicOr(status, ST_NONFINITE);
@@ -83,19 +77,14 @@ __global__ void __launch_bounds__(256) image_new_kernel(DevModel m, ImagePlane i
         const uint32_t start = pixel_start(m, org, ip, lane, Z);
         const double sh0 = image_shift(m, org, ip, start, Z);
         bk.shift0 = fw.shift0 = bk.cshift = fw.cshift = sh0;
-        bk.dsh0 = fw.dsh0 = (float)dsub_rn(sh0, 1.0);
+        set_dsh0(bk, sh0);
+        set_dsh0(fw, sh0);
         const int nb = trace_image<true>(m, org, ip, start, Z, cap, bk, lane, status);
         if (nb < 0) continue;
         for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
             const uint32_t f = f0 + lane;
             if (f < m.F) {
-                LaneCtx c;
-                c.o = start;
-                c.f = f;
-                c.l0 = m.corr_line[f];
-                c.freq = m.nu[(size_t)start * m.F + f];
-                c.fq = (float)c.freq;
-                c.a0 = (float)(c.freq - m.line[c.l0]);
+                const LaneCtx c = lane_ctx(m, start, f);
                 const double v = image_lane<MODE, AP, TAU>(m, sl, c, bk, nb, fw, 0);
                 I[(size_t)px * m.F + f] = v;
                 if (!isfinite(v)) atomicOr(status, ST_NONFINITE);
@@ -352,21 +341,15 @@ __global__ void __launch_bounds__(32) image_point_kernel(DevModel m, uint32_t ca
     const double shf = origin_shift(m, 1, p, ar);
     bk.shift0 = shb;
     fw.shift0 = shf;
-    bk.dsh0 = (float)dsub_rn(shb, 1.0);
-    fw.dsh0 = (float)dsub_rn(shf, 1.0);
+    set_dsh0(bk, shb);
+    set_dsh0(fw, shf);
     bk.cshift = fw.cshift = shb;
     const int nb = trace_half<true, 1>(m, p, rr, cap, bk, lane, status);
     const int nf = trace_half<true, 1>(m, p, ar, cap, fw, lane, status);
     if (nb < 0 || nf < 0) return;
     const uint32_t f = blockIdx.x * 32 + lane;
     if (f >= m.F) return;
-    LaneCtx c;
-    c.o = p;
-    c.f = f;
-    c.l0 = m.corr_line[f];
-    c.freq = m.nu[(size_t)p * m.F + f];
-    c.fq = (float)c.freq;
-    c.a0 = (float)(c.freq - m.line[c.l0]);
+    const LaneCtx c = lane_ctx(m, p, f);
     image_lane<MODE, AP, false, true>(m, sl, c, bk, nb, fw, nf, &ro);
     if (!isfinite(ro.u[f])) atomicOr(status, ST_NONFINITE);
 }

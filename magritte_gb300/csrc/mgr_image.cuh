@@ -125,7 +125,7 @@ static __device__ int trace_image(const DevModel& m, const double* org, const Im
                 h.dZ[count] = dZl;
                 const double sh = image_shift(m, org, ip, nxt, Z);
                 h.shift[count] = sh;
-                h.dsh[count] = (float)dsub_rn(sh, 1.0);
+                store_dsh(h, count, sh);
                 h.dzs[count] = (float)dZl * m.dz_scale;
             }
             count++;
@@ -206,7 +206,7 @@ static __device__ int trace_image(const DevModel& m, const double* org, const Im
             const double4_32a v = m.vel[h.ids[s]];
             const double sh = dadd_rn(1.0, dot3_rn(v.x, v.y, v.z, dx, dy, dz));
             h.shift[s] = sh;
-            h.dsh[s] = (float)dsub_rn(sh, 1.0);
+            store_dsh(h, s, sh);
             h.dzs[s] = (float)h.dZ[s] * m.dz_scale;
         }
         __syncwarp();

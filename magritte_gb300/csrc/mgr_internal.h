@@ -28,6 +28,7 @@ struct MgrModel {
     float* op_f = nullptr;
     float* iw_f = nullptr;
     float* Sp_f = nullptr;
+    float* iw_lo = nullptr;          // [P][L] low part of the double-float inverse widths
     uint16_t* nint = nullptr;        // [E][L] interpolation counts
     uint16_t* nint_all = nullptr;    // [E] interpolation counts over all lines (imagers)
     int fo2_warps = 8;               // warps (ray pairs in flight) per CTA of the formal solve
@@ -144,5 +145,10 @@ cudaError_t launch_line_tables(MgrModel* model);
 cudaError_t launch_ray_lengths(MgrModel* model, uint32_t* d_max_len);
 cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats);
 cudaError_t launch_nint_table(MgrModel* model);
+// Fills the correctly rounded erff table (kErfBandCount floats) on `stream`.
+cudaError_t fill_erf_band(float* table, cudaStream_t stream, int sm_count);
+// The current device's erff table, created (cudaMalloc, one fill launch, synchronised)
+// by the first call on each device and kept until the process exits.
+cudaError_t erf_band_table(const float** out);
 
 }  // namespace mgr

@@ -9,6 +9,9 @@
 //
 // Kinds: 0 DFMA, 1 DADD, 2 DMUL, 3 DSETP (FP64 compare), 4 F2F (FP64 <-> FP32
 // conversions, two per step), 5 MUFU.RCP64H (rcp.approx.ftz.f64).
+#include <algorithm>
+#include <vector>
+
 #include "mgr_internal.h"
 
 namespace mgr {
@@ -16,6 +19,7 @@ namespace mgr {
 constexpr int kProbeChains = 8;
 constexpr int kProbeThreads = 256;
 
+// cycles[3 * block] = {SM id, clock64 at the start, clock64 at the end} of each CTA.
 template <int KIND>
 __global__ void __launch_bounds__(kProbeThreads) pipe_probe_kernel(double* __restrict__ out,
                                                                    unsigned long long* __restrict__ cycles,
@@ -39,7 +43,11 @@ __global__ void __launch_bounds__(kProbeThreads) pipe_probe_kernel(double* __res
                 cnt += (x[i] < b) ? 1u : 0u;
                 x[i] = __longlong_as_double(__double_as_longlong(x[i]) + 1);  // integer pipe
             } else if constexpr (KIND == 4) {
-                x[i] = (double)((float)x[i] + 1.0f);
+                // FP64 -> FP32 -> FP64 through explicit conversion instructions (a C++
+                // cast chain would be folded to FP32 arithmetic)
+                float f;
+                asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(f) : "d"(x[i]));
+                asm volatile("cvt.f64.f32 %0, %1;" : "=d"(x[i]) : "f"(f));
             } else {
                 asm volatile("rcp.approx.ftz.f64 %0, %1;" : "=d"(x[i]) : "d"(x[i]));
             }
@@ -51,7 +59,13 @@ __global__ void __launch_bounds__(kProbeThreads) pipe_probe_kernel(double* __res
 #pragma unroll
     for (int i = 0; i < kProbeChains; i++) s += x[i];
     out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
-    if (threadIdx.x == 0) cycles[blockIdx.x] = t1 - t0;
+    if (threadIdx.x == 0) {
+        uint32_t smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        cycles[3 * blockIdx.x] = smid;
+        cycles[3 * blockIdx.x + 1] = t0;
+        cycles[3 * blockIdx.x + 2] = t1;
+    }
 }
 
 template <int KIND>
@@ -93,7 +107,7 @@ extern "C" int mgr_measure_pipe_rate(int kind, uint32_t iterations, double* thre
     cudaStream_t s = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     e = cudaMalloc(&out, (size_t)grid * kProbeThreads * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&cyc, (size_t)grid * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&cyc, (size_t)grid * 3 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
@@ -106,14 +120,27 @@ extern "C" int mgr_measure_pipe_rate(int kind, uint32_t iterations, double* thre
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         float t = 0.0f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
-        std::vector<unsigned long long> c(grid);
+        std::vector<unsigned long long> c((size_t)grid * 3);
         if (e == cudaSuccess)
-            e = cudaMemcpy(c.data(), cyc, grid * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+            e = cudaMemcpy(c.data(), cyc, c.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
         if (e == cudaSuccess && rep > 0 && (best == 0.0f || t < best)) {
             best = t;
-            double mean = 0.0;
-            for (unsigned long long v : c) mean += (double)v;
-            best_cyc = mean / grid;
+            // per SM: first CTA start to last CTA end on that SM's own clock
+            std::vector<unsigned long long> lo(nsm, ~0ull), hi(nsm, 0ull);
+            for (int b = 0; b < grid; b++) {
+                const unsigned long long sm = c[3 * b];
+                if (sm >= (unsigned long long)nsm) continue;
+                lo[sm] = std::min(lo[sm], c[3 * b + 1]);
+                hi[sm] = std::max(hi[sm], c[3 * b + 2]);
+            }
+            double span = 0.0;
+            int used = 0;
+            for (int k = 0; k < nsm; k++)
+                if (hi[k] > lo[k]) {
+                    span += (double)(hi[k] - lo[k]);
+                    used++;
+                }
+            best_cyc = used ? span / used : 0.0;
         }
     }
     if (out) cudaFree(out);
@@ -125,9 +152,7 @@ extern "C" int mgr_measure_pipe_rate(int kind, uint32_t iterations, double* thre
     const double per_step = (kind == 4) ? 2.0 : 1.0;
     const double ops = (double)grid * kProbeThreads * kProbeChains * (double)iterations * per_step;
     if (thread_ops_per_s) *thread_ops_per_s = ops / (best * 1e-3);
-    // the 8 CTAs of an SM run side by side: an SM executes 8 CTAs' operations in the
-    // mean CTA's cycle count
-    if (thread_ops_per_clk_per_sm) *thread_ops_per_clk_per_sm = (ops / nsm) / best_cyc;
+    if (thread_ops_per_clk_per_sm) *thread_ops_per_clk_per_sm = best_cyc > 0.0 ? (ops / nsm) / best_cyc : 0.0;
     if (ms) *ms = best;
     return MGR_OK;
 }

@@ -43,13 +43,7 @@ __global__ void __launch_bounds__(256, MINB)
         for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
             const uint32_t f = f0 + lane;
             if (f < m.F) {
-                LaneCtx c;
-                c.o = o;
-                c.f = f;
-                c.l0 = m.corr_line[f];
-                c.freq = m.nu[(size_t)o * m.F + f];
-                c.fq = (float)c.freq;
-                c.a0 = (float)(c.freq - m.line[c.l0]);
+                const LaneCtx c = lane_ctx(m, o, f);
                 const LaneResultSC r = solve_lane_sc0<MODE, AP>(m, sl, c, bk, nb, fw, nf);
                 const double u = r.solved ? 0.5 * (r.If + r.Ib) : r.If;
                 Ui[f] = u;

@@ -37,7 +37,23 @@ struct HalfSmem {
     double shift0 = 1.0;  // shift of the origin as this half's trace starts from it (1 comoving)
     float dsh0 = 0.0f;    // shift0 - 1
     double cshift = 1.0;  // shift of the origin element itself (the backward half's shift0)
+    float* dsl = nullptr;  // (shift - 1) - dsh, the low part of a double-float shift - 1
+    float dsl0 = 0.0f;     // the same for shift0
 };
+
+// shift - 1 of step s as a float and its low part (exact: shift - 1 is an FP64 value
+// near 0; hi + lo carries about 48 of its bits).
+MGR_HD void store_dsh(const HalfSmem& h, int s, double shift) {
+    const double d = dsub_rn(shift, 1.0);
+    const float hi = (float)d;
+    h.dsh[s] = hi;
+    h.dsl[s] = (float)dsub_rn(d, (double)hi);
+}
+MGR_HD void set_dsh0(HalfSmem& h, double shift0) {
+    const double d = dsub_rn(shift0, 1.0);
+    h.dsh0 = (float)d;
+    h.dsl0 = (float)dsub_rn(d, (double)h.dsh0);
+}
 
 // Interpolation over all lines (Solver::set_data, solver.tpp:1003-1043) instead of
 // one line's criterion, as the imagers trace.
@@ -60,9 +76,11 @@ __device__ __forceinline__ void carve_halves(unsigned char* base, uint32_t cap, 
     fw.dsh = f + cap;
     bk.dzs = f + 2 * cap;
     fw.dzs = f + 3 * cap;
+    bk.dsl = f + 4 * cap;
+    fw.dsl = f + 5 * cap;
 }
 
-__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 4 * 4 + 4 * 4); }
+__host__ __device__ constexpr size_t half_bytes_per_warp(uint32_t cap) { return (size_t)cap * (4 * 8 + 4 * 4 + 6 * 4); }
 
 // Order-preserving 64-bit key of a finite double (total order, -0 below +0; the
 // squared distances compared here are never -0).  Lets the warp's argmin run on the
@@ -134,7 +152,7 @@ __device__ int trace_half_sph(const DevModel& m, uint32_t o, uint32_t r, uint32_
     const double Rsin2 = dsub_rn(sqnorm_rn(po), dmul_rn(Rcos, Rcos));
     if (STORE) {
         h.shift0 = origin_shift(m, FRAME, o, r);
-        h.dsh0 = (float)dsub_rn(h.shift0, 1.0);
+        set_dsh0(h, h.shift0);
     }
     double Z = 0.0;
     uint32_t crt = o;
@@ -159,7 +177,7 @@ __device__ int trace_half_sph(const DevModel& m, uint32_t o, uint32_t r, uint32_
             h.dZ[count] = dZl;
             const double sh = shift_sph(m, FRAME, o, r, nxt, Z, d);
             h.shift[count] = sh;
-            h.dsh[count] = (float)dsub_rn(sh, 1.0);
+            store_dsh(h, count, sh);
             h.dzs[count] = (float)dZl * m.dz_scale;
         }
         count++;
@@ -225,7 +243,7 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
         for (int s = lane; s < count; s += 32) {
             const double sh = FRAME ? shift_rest(m, r, h.ids[s], d) : shift_comoving(m, o, h.ids[s], d);
             h.shift[s] = sh;
-            h.dsh[s] = (float)dsub_rn(sh, 1.0);
+            store_dsh(h, s, sh);
             h.dzs[s] = (float)h.dZ[s] * m.dz_scale;
         }
         __syncwarp();
@@ -415,7 +433,21 @@ struct LaneCtx {
     double freq;   // nu(o, f)
     float fq;      // (float)freq
     float a0;      // (float)(freq - line[l0])
+    float fql;     // freq - fq, the low part of a double-float freq
 };
+
+// The lane context of frequency f at origin o.
+MGR_HD LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {
+    LaneCtx c;
+    c.o = o;
+    c.f = f;
+    c.l0 = m.corr_line[f];
+    c.freq = m.nu[(size_t)o * m.F + f];
+    c.fq = (float)c.freq;
+    c.a0 = (float)(c.freq - m.line[c.l0]);
+    c.fql = (float)(c.freq - (double)c.fq);
+    return c;
+}
 
 // FP64 (reference arithmetic) -------------------------------------------------------
 
@@ -598,28 +630,106 @@ MGR_HD void eta_chi_f32(const DevModel& m, const LaneCtx& c, const Elem& e, floa
 // Out-of-line paths of split precision.  They run for a small fraction of pairs and
 // are kept out of the hot loop so that its code stays small.
 
+// ---- double-float arithmetic: a value carried as the unevaluated sum hi + lo of two
+// floats (about 48 significant bits), with Knuth's TwoSum and an FMA-based exact
+// product (Dekker 1971).  Split precision uses it for the same-wing erf arguments.
+struct F2 {
+    float hi, lo;
+};
+MGR_HD F2 f2_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return F2{s, (a - (s - bb)) + (b - bb)};
+}
+MGR_HD F2 f2_quick(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = a + b;
+    return F2{s, b - (s - a)};
+}
+MGR_HD F2 f2_add(F2 a, F2 b) {
+    F2 s = f2_two_sum(a.hi, b.hi);
+    const F2 t = f2_two_sum(a.lo, b.lo);
+    s = f2_quick(s.hi, s.lo + t.hi);
+    return f2_quick(s.hi, s.lo + t.lo);
+}
+MGR_HD F2 f2_sub(F2 a, F2 b) { return f2_add(a, F2{-b.hi, -b.lo}); }
+MGR_HD F2 f2_mul(F2 a, F2 b) {
+    const float p = a.hi * b.hi;
+    const float e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+    return f2_quick(p, e);
+}
+
+// i / n as a double-float: q = fl(i / n) and the exact remainder i - q n over n.
+MGR_HD F2 f2_ratio(uint32_t i, uint32_t n) {
+    const float fi = (float)i, fn = (float)n;
+#ifdef __CUDA_ARCH__
+    const float q = __fdiv_rn(fi, fn);
+#else
+    const float q = fi / fn;
+#endif
+    return f2_quick(q, fmaf(-q, fn, fi) / fn);
+}
+
+// shift - 1 of a split-precision element as a double-float: the step's stored value
+// (n = 1), the FP64 iterator's shc + i (shn - shc) / n (n > 1), or the origin's.
+MGR_HD F2 elem_dsh_f2(const HalfSmem& h, const Elem& e) {
+    if (e.n == 0) {
+        const double d = h.cshift - 1.0;
+        const float hi = (float)d;
+        return F2{hi, (float)(d - (double)hi)};
+    }
+    const F2 dn{h.dsh[e.s], h.dsl[e.s]};
+    if (e.n == 1) return dn;
+    const F2 dc = e.s ? F2{h.dsh[e.s - 1], h.dsl[e.s - 1]} : F2{h.dsh0, h.dsl0};
+    return f2_add(dc, f2_mul(f2_sub(dn, dc), f2_ratio(e.i, e.n)));
+}
+
+// The element's inverse width of line l as a double-float (interpolate_linear with the
+// factor 1 - i / n between its two points).
+MGR_HD F2 elem_iw_f2(const DevModel& m, const Elem& e, uint32_t l) {
+    const size_t a = (size_t)e.nr * m.L + l;
+    const F2 w1{m.iw_f[a], m.iw_lo[a]};
+    if (e.n <= 1) return w1;
+    const size_t b = (size_t)e.ni * m.L + l;
+    const F2 w2{m.iw_f[b], m.iw_lo[b]};
+    const F2 fac = f2_sub(F2{1.0f, 0.0f}, f2_ratio(e.i, e.n));
+    return f2_add(w1, f2_mul(f2_sub(w2, w1), fac));
+}
+
+// Correctly rounded erff(x) (the FP64 mode's erff_cr) without FP64 arithmetic: +-1 for
+// |x| >= 3.919206, the device's table of (float)erf((double)x) over every float in
+// [kErfBandLo, 3.919206) (erf_band_table), and FP64 below (the same-wing arguments
+// start at 1.5: the float positions that select them are within 1e-5 of the exact ones).
+MGR_HD float erff_band(const DevModel& m, float x) {
+#ifdef __CUDA_ARCH__
+    const float ax = fabsf(x);
+    if (ax >= 3.919206f) return copysignf(1.0f, x);
+    if (ax < kErfBandLo) return erff_cr(x);
+    return copysignf(m.erf_band[__float_as_uint(ax) - __float_as_uint(kErfBandLo)], x);
+#else
+    (void)m;  // the host emulation evaluates the table's entries directly
+    return erff_cr(x);
+#endif
+}
+
 // Same-wing erf difference on the FP64 mode's arguments (linefreq - nu shift) * avg_iw,
-// computed with the expressions of dtau_single_line_fp64 and the correctly rounded
-// erff.  Returns {erff(next) - erff(curr), next - curr}.
-static __host__ __device__ __noinline__ float2 band_erf(const double* iw, uint32_t L, double linefreq, double freq,
-                                                 const double* hshift, double shift0, double cshift, Elem lo, Elem hi,
-                                                 uint32_t l) {
-    double lo_shift, lo_fac, hi_shift, hi_fac;
-    const HalfSmem h{nullptr, const_cast<double*>(hshift), nullptr, nullptr, nullptr, nullptr, shift0, 0.0f, cshift};
-    elem_shift_fac(h, lo, lo_shift, lo_fac);
-    elem_shift_fac(h, hi, hi_shift, hi_fac);
-    const double cf = freq * lo_shift;
-    const double nf = freq * hi_shift;
-    const size_t c1 = (size_t)lo.nr * L, c2 = (size_t)lo.ni * L;
-    const size_t n1 = (size_t)hi.nr * L, n2 = (size_t)hi.ni * L;
-    const double iwc = interpolate_linear(iw[c1 + l], iw[c2 + l], lo_fac);
-    const double iwn = interpolate_linear(iw[n1 + l], iw[n2 + l], hi_fac);
-    const double avg_iw = (iwc + iwn) / 2.0;
-    const double np = (linefreq - nf) * avg_iw;
-    const double cp = (linefreq - cf) * avg_iw;
+// without FP64 arithmetic: the arguments are evaluated in double-float, written as
+// (linefreq - nu) - nu (shift - 1), so that the float they round to is the one the FP64
+// expressions of dtau_single_line_fp64 round to (except for values within about 1e-10
+// relative of a rounding midpoint), and the correctly rounded erff of each comes from
+// the table.  Returns {erff(next) - erff(curr), next - curr}; both arguments are in
+// the table's range.
+MGR_HD float2 band_erf(const DevModel& m, const LaneCtx& c, const HalfSmem& h, const Elem& lo, const Elem& hi,
+                       uint32_t l) {
+    const F2 freq{c.fq, c.fql};
+    const F2 a = f2_sub(F2{m.line_df[2 * l], m.line_df[2 * l + 1]}, freq);
+    F2 avg = f2_add(elem_iw_f2(m, lo, l), elem_iw_f2(m, hi, l));
+    avg.hi *= 0.5f;
+    avg.lo *= 0.5f;
+    const F2 np = f2_mul(f2_sub(a, f2_mul(freq, elem_dsh_f2(h, hi))), avg);
+    const F2 cp = f2_mul(f2_sub(a, f2_mul(freq, elem_dsh_f2(h, lo))), avg);
     float2 r;
-    r.x = erff_cr_fast((float)np) - erff_cr_fast((float)cp);
-    r.y = (float)(np - cp);
+    r.x = erff_band(m, np.hi) - erff_band(m, cp.hi);
+    r.y = f2_sub(np, cp).hi;
     return r;
 }
 
@@ -670,7 +780,7 @@ MGR_HD float dtau_single_line_f32(const DevModel& m, const LaneCtx& c, const Hal
         // cancels and its single-ulp roundings decide the result, so take it on the
         // FP64 mode's arguments with the correctly rounded erff (split precision then
         // stays within 1e-5 of the FP64 path in J).
-        const float2 r = band_erf(m.iw, m.L, m.line[l], c.freq, h.shift, h.shift0, h.cshift, lo, hi, l);
+        const float2 r = band_erf(m, c, h, lo, hi, l);
         erfdiff = r.x;
         diff_pos = r.y;
     } else {
@@ -899,6 +1009,52 @@ MGR_HD void elim_row(typename Real_<MODE>::T dt_out, typename Real_<MODE>::T dt_
     }
 }
 
+// Split precision, the elimination in projective form.  A sweep keeps (NG, D, NS)
+// with G = F / (1 + F) = NG / D and Su = NS / D, and D_prev = D - NG (so that
+// 1 / (1 + F) = D_prev / D).  A row
+//     F' = q G + iC,  Su' = (q Su + S iC) / (1 + F')
+// becomes, multiplied through by D' = D (1 + F'),
+//     NG' = q NG + iC D,   D' = NG' + D,   NS' = q NS + S iC D:
+// five FP64 operations and no reciprocal per element, all of them sums of positive
+// terms as in the (1+B)/C form.  D never decreases; the state is scaled by 2^-600
+// (exact) once D passes 2^600, well before it could leave the FP64 range (one row
+// multiplies D by 1 + F' < 2^122).
+struct Proj {
+    double NG, D, NS, Dp;
+};
+
+MGR_HD void proj_rescale(Proj& s) {
+#ifdef __CUDA_ARCH__
+    const bool big = __double2hiint(s.D) > 0x65700000;  // D > 2^600
+#else
+    const bool big = s.D > 0x1p600;
+#endif
+    if (big) {
+        s.NG *= 0x1p-600;
+        s.D *= 0x1p-600;
+        s.NS *= 0x1p-600;
+        s.Dp *= 0x1p-600;
+    }
+}
+
+MGR_HD void elim_row_proj(float dt_out, float dt_in, float S, Proj& s) {
+    double q, iC;
+    if (dt_out > 1.0e-18f && dt_out < 1.0e18f && dt_in > 1.0e-18f && dt_in < 1.0e18f) {
+        q = f2d(fast_div(dt_in, dt_out));
+        iC = f2d(0.5f * (dt_out + dt_in) * dt_in);
+    } else {
+        const double2 k = elim_coeffs_fp64(dt_out, dt_in);
+        q = k.x;
+        iC = k.y;
+    }
+    const double iCD = iC * s.D;
+    s.Dp = s.D;
+    s.NG = fma(q, s.NG, iCD);
+    s.NS = fma(q, s.NS, f2d(S) * iCD);
+    s.D = s.NG + s.D;
+    proj_rescale(s);
+}
+
 // Result of one lane's ray-pair solve.
 struct LaneResult {
     double u;       // Su[centre]
@@ -931,6 +1087,9 @@ template <int MODE, int AP, bool UV = false>
 __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
                                           int nb, const HalfSmem& fw, int nf) {
     using T = typename Real_<MODE>::T;
+    // split precision eliminates in projective form (the uv solve keeps the (F, FI, Su)
+    // state its origin rows need)
+    constexpr bool PROJ = (MODE == MODE_SPLIT) && !UV;
     LaneResult res;
     res.solved = (nb > 0) || (nf > 0);
     res.v = 0.0;
@@ -944,12 +1103,14 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     const uint32_t l = c.l0;
     EC<MODE> ec_cen{T(0), T(0), false};
     Sweep top{0.0, 0.0, 0.0, 0.0, 0.0, false, false, 0.0, 0.0}, bot = top;
+    Proj ptop{0.0, 1.0, 0.0, 1.0}, pbot = ptop;
 
 #pragma unroll 1
     for (int side = 0; side < 2; side++) {
         const HalfSmem& h = side ? fw : bk;
         const int n = side ? nf : nb;
         Sweep st{0.0, 0.0, 0.0, 0.0, 0.0, false, false, 0.0, 0.0};
+        Proj ps{0.0, 1.0, 0.0, 1.0};
         if (n > 0) {
             ElemIter it;
             iter_begin<MODE>(m, h, c.o, l, n, it);
@@ -978,7 +1139,19 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                     st.dz_last = (MODE == MODE_FP64) ? outer.dzin : (double)outer.dzf;
                 }
                 const T rowS = (side == 0 || first) ? po.Slo : S_carry;
-                if (first) {
+                if (PROJ && first) {
+                    // boundary row multiplied through by dtau^2/2: F = h = dtau (dtau/2 + 1),
+                    // Su = (S dtau^2/2 + I_bdy dtau) / (1 + h)
+                    const double dt = po.dtau;
+                    const double hb = dt * fma(0.5, dt, 1.0);
+                    ps.NG = hb;
+                    ps.D = 1.0 + hb;
+                    ps.NS = fma((double)rowS * 0.5 * dt, dt, Ibdy * dt);
+                    ps.Dp = 1.0;
+                    first = false;
+                } else if (PROJ) {
+                    elim_row_proj((float)dt_prev, (float)po.dtau, (float)rowS, ps);
+                } else if (first) {
                     // boundary row (solver.tpp:2239-2252 first, :2284-2293 last)
                     const double dt = po.dtau;
                     const double inverse_dtau = drcp<MODE>(dt);
@@ -1003,8 +1176,29 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             st.S_in = S_carry;
             st.rows = true;
         }
-        if (side) bot = st;
-        else top = st;
+        if (side) {
+            bot = st;
+            pbot = ps;
+        } else {
+            top = st;
+            ptop = ps;
+        }
+    }
+
+    if constexpr (PROJ) {
+        // back to (F / (1 + F), 1 / (1 + F), Su) at the origin: two reciprocals per lane
+        if (top.rows) {
+            const double r = drcp<MODE>(ptop.D);
+            top.F = ptop.NG * r;  // G
+            top.FI = ptop.Dp * r;
+            top.Su = ptop.NS * r;
+        }
+        if (bot.rows) {
+            const double r = drcp<MODE>(pbot.D);
+            bot.F = pbot.NG * r;
+            bot.FI = pbot.Dp * r;
+            bot.Su = pbot.NS * r;
+        }
     }
 
     // ---- combine at the origin ----
@@ -1013,9 +1207,9 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         const double iA = dtau_avg * top.dt;
         const double iC = dtau_avg * bot.dt;
         const double A = drcp<MODE>(iA);
-        const double FFc = (A * top.F * top.FI + 1.0) * iC;
+        const double FFc = (A * (PROJ ? top.F : top.F * top.FI) + 1.0) * iC;
         const double Su_pre = (A * top.Su + bot.S_in) * iC;
-        const double GP = bot.F * bot.FI;
+        const double GP = PROJ ? bot.F : bot.F * bot.FI;
         const double D = drcp<MODE>(FFc + GP);
         res.u = (Su_pre + bot.Su) * D;
         res.Ldiag = iC * D;
@@ -1050,7 +1244,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         if constexpr (MODE == MODE_FP64) Suf = (bot.S_in + 2.0 * Ibdy * inverse_dtau_f) / Bf;
         else Suf = (bot.S_in + 2.0 * Ibdy * inverse_dtau_f) * drcp<MODE>(Bf);
         const double FFf = 0.5 * Bf_min_Cf * bot.dt * bot.dt;
-        const double GP = bot.F * bot.FI;
+        const double GP = PROJ ? bot.F : bot.F * bot.FI;
         const double D = drcp<MODE>(FFf + GP);
         res.u = (Suf * (1.0 + FFf) + bot.Su) * D;
         res.Ldiag = drcp<MODE>(Cf) * D;
@@ -1061,12 +1255,19 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
         const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
         const double Bl = Bl_min_Al + Al;
-        const double denominator = drcp<MODE>(Bl * top.F + Bl_min_Al);
         const double Sl = top.S_in + 2.0 * Ibdy * inverse_dtau_l;
-        res.u = (Al * top.Su + Sl) * (1.0 + top.F) * denominator;
-        if constexpr (UV) res.v = res.u - Ibdy;  // Sv[last] = Su[last] - I_bdy_l
-        if constexpr (MODE == MODE_FP64) res.Ldiag = (1.0 + top.F) / (Bl_min_Al + Bl * top.F);
-        else res.Ldiag = (1.0 + top.F) * denominator;
+        if constexpr (PROJ) {
+            // with G = F / (1 + F) and FI = 1 / (1 + F): (1 + F) / (Bl F + Bl - Al) = 1 / (Bl G + (Bl - Al) FI)
+            const double den = drcp<MODE>(Bl * top.F + Bl_min_Al * top.FI);
+            res.u = (Al * top.Su + Sl) * den;
+            res.Ldiag = den;
+        } else {
+            const double denominator = drcp<MODE>(Bl * top.F + Bl_min_Al);
+            res.u = (Al * top.Su + Sl) * (1.0 + top.F) * denominator;
+            if constexpr (UV) res.v = res.u - Ibdy;  // Sv[last] = Su[last] - I_bdy_l
+            if constexpr (MODE == MODE_FP64) res.Ldiag = (1.0 + top.F) / (Bl_min_Al + Bl * top.F);
+            else res.Ldiag = (1.0 + top.F) * denominator;
+        }
     }
     return res;
 }
