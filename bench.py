@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--ali-points", type=int, default=50_000)
     p.add_argument("--ali-nside", type=int, default=2)
     p.add_argument("--ali-iterations", type=int, default=20)
+    p.add_argument("--ali-full", action="store_true",
+                   help="the ALI leg at the stated size: 500k points, nside 4 (192 rays)")
     p.add_argument("--no-batch", action="store_true", help="skip the many-model batch leg")
     p.add_argument("--batch-models", type=int, default=512)
     p.add_argument("--batch-steps", type=int, default=1)
@@ -238,21 +240,62 @@ def pipe_rates():
     return out
 
 
+def ali_parity(args):
+    """Level populations of the ALI loop against the oracle's on the non-LTE workload
+    reduced to 1,000 interior points (nside-8 outer shell, nside-4 rays, the 10-level
+    rotor x 21): 8 iterations with Default Ng every 4 and no early stop, in both
+    precisions; the oracle in the GPU FP64 mode's arithmetic (correctly rounded erff)."""
+    import numpy as np
+    from magritte_gb300 import _abi, synthetic
+    oracle = _oracle()
+    raw = synthetic.nlte_sphere(npoints=1000, nside=4, nside_out=8)
+    params = dict(use_adaptive_Ng_acceleration=0, Ng_acceleration_mem_limit=4, pop_prec=0.0)
+    oracle.set_erf_mode(1)
+    t0 = time.perf_counter()
+    try:
+        ref = oracle.AliOracle(raw, oracle.reference_setup(raw)).run(use_ng=True, max_it=8, **params)
+    finally:
+        oracle.set_erf_mode(0)
+    oracle_s = time.perf_counter() - t0
+    tot = raw.abundance[:, raw.linedata[0].num][:, None]
+    out = {"workload": f"nlte_sphere 1000 interior points ({raw.npoints} with the boundary shells), "
+                       f"{raw.nrays} rays, 8 iterations, Ng every 4", "oracle_s": oracle_s, "bar": {"fp64": 1e-6,
+                                                                                                "split": 1e-5}}
+    for prec in ("fp64", "split"):
+        a = oracle.reference_setup(raw)
+        dev = _abi.DeviceModel(a)
+        try:
+            dev.set_species(raw.linedata, raw.abundance, a["populations"])
+            dev.compute_level_populations(prec, use_ng=True, max_it=8, **params)
+            pop = dev.populations(0)
+        finally:
+            dev.close()
+        out[f"{prec}_max_rel_err_populations"] = float(np.max(np.abs(pop - ref["populations"][0]) /
+                                                              np.maximum(np.abs(ref["populations"][0]), 1e-10 * tot)))
+    return out
+
+
 def run_ali(args):
     """ALI wall time: compute_level_populations(use_Ng=True, N) through core.Model on
     the non-LTE sphere workload (Delaunay points ~ r^-2, 10-level rotor, nquads 21),
     Default Ng every 4 iterations, exactly N normal iterations (pop_prec = 0 keeps
-    the loop from stopping early), split-precision formal solves, graph-captured
-    iterations.  The timed call includes the model upload."""
+    the loop from stopping early), formal solves in the bench's precision,
+    graph-captured iterations.  The timed call includes the model upload.  The device
+    time of each phase comes from events inside the captured iteration
+    (mgr_ali_phase_times); the populations are checked against the oracle on a reduced
+    model (ali_parity)."""
+    import ctypes as C
     import time as _t
 
-    from magritte_gb300 import loader, synthetic
+    from magritte_gb300 import _abi, loader, synthetic
 
+    t_setup = _t.perf_counter()
     raw = synthetic.nlte_sphere(npoints=args.ali_points, nside=args.ali_nside)
     model = loader.to_core(raw, precision=args.precision)
     model.compute_spectral_discretisation()
     model.compute_inverse_line_widths()
     model.compute_LTE_level_populations()
+    setup_s = _t.perf_counter() - t_setup
     prm = model.parameters
     prm.store_u = False
     prm.use_adaptive_Ng_acceleration = False
@@ -261,12 +304,22 @@ def run_ali(args):
     t0 = _t.perf_counter()
     it = model.compute_level_populations(True, args.ali_iterations)
     wall = _t.perf_counter() - t0
+    ms = (C.c_double * 4)()
+    phases = None
+    if _abi.load().mgr_ali_phase_times(C.c_void_p(model.upload()), ms) == 0:
+        phases = {"formal_solve_ms": ms[0], "jeff_ms": ms[1], "stateq_corrections_refresh_ms": ms[2],
+                  "ng_ms": ms[3], "per_iteration_formal_solve_ms": ms[0] / max(it, 1)}
     P, F, R = prm.npoints(), prm.nfreqs(), prm.hnrays()
-    return {"workload": f"nlte_sphere {raw.npoints} points (Delaunay, density ~ r^-2), {raw.nrays} rays, "
-                        f"10-level rotor (9 lines) x nquads {raw.nquads}",
-            "iterations": it, "ng": "Default, every 4", "precision": args.precision, "wall_s": wall,
-            "s_per_iteration": wall / max(it, 1), "solves_per_iteration": float(P) * R * F,
-            "note": "config-2 family reduced to fit the bench time; no CPU leg (one oracle iteration takes minutes)"}
+    solves = float(P) * R * F
+    out = {"workload": f"nlte_sphere {raw.npoints} points (Delaunay, density ~ r^-2), {raw.nrays} rays, "
+                       f"10-level rotor (9 lines) x nquads {raw.nquads}",
+           "iterations": it, "ng": "Default, every 4", "precision": args.precision, "wall_s": wall,
+           "s_per_iteration": wall / max(it, 1), "solves_per_iteration": solves,
+           "formal_solve_solves_per_s": (solves * it / (ms[0] / 1000.0)) if phases and ms[0] > 0 else None,
+           "phases": phases, "setup_s": setup_s}
+    if not args.no_parity:
+        out["parity"] = ali_parity(args)
+    return out
 
 
 class _Handle:
@@ -535,7 +588,7 @@ def run_adjoint_j(args):
     # finite-difference check on localised losses
     interior = np.setdiff1d(np.arange(raw.npoints), raw.boundary2point)
     pts = rng.choice(interior, size=min(args.adjoint_fd_points, len(interior)), replace=False)
-    cum = np.concatenate([[0], np.cumsum(raw.n_neighbors)])
+    cum = np.concatenate([np.zeros(1, np.int64), np.cumsum(raw.n_neighbors, dtype=np.int64)])
     errs, flips, t_fd = [], 0, time.perf_counter()
     for p in pts:
         S = np.unique(np.concatenate([[p], raw.neighbors[cum[p]:cum[p + 1]]])).astype(np.int32)
@@ -851,6 +904,8 @@ def run_ours(args, rank, ws):
 
 def main():
     args = parse()
+    if args.ali_full:
+        args.ali_points, args.ali_nside = 500_000, 4
     rank, ws = dist_init()
     if args.impl == "reference":
         run_reference(args, rank, ws)

@@ -495,6 +495,14 @@ int mgr_compute_level_populations_sparse(MgrModel* model, int precision, int use
  * mgr_formal_solve_fo2_sparse: Jlin, Jeff [P][nrad] (host, may be NULL). */
 int mgr_compute_jeff_sparse(MgrModel* model, uint32_t l, double* Jlin, double* Jeff);
 
+/* Device time of the phases of the last mgr_compute_level_populations(_sparse) call on
+ * this model (no reference counterpart), ms[4] summed over its iterations: the formal
+ * solves (with the ray-shard reduce), compute_Jeff, the statistical equilibrium with the
+ * population corrections, convergence statistics and line-data refresh, and the Ng
+ * acceleration steps.  The iterations' events are recorded inside the captured graph.
+ * MGR_ERR_UNSUPPORTED when the timing was not available. */
+int mgr_ali_phase_times(MgrModel* model, double* ms);
+
 /* Copy species l's level populations [P][nlev] to the host. */
 int mgr_get_populations(MgrModel* model, uint32_t l, double* populations);
 

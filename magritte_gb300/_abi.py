@@ -154,6 +154,7 @@ SIGNATURES = {
     "mgr_formal_solve_fo2_adjoint_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                       C.c_void_p]),
+    "mgr_ali_phase_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "mgr_measure_pipe_rate": (C.c_int, [C.c_int, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_float)]),
 }

@@ -82,35 +82,33 @@ __device__ __forceinline__ double emissivity_of(const SpeciesView& s, const doub
     return v > min_line_emissivity ? v : min_line_emissivity;
 }
 
-// The rate block of point p into M (row-major, rows = equations) in the order the
-// reference emits its triplets; lane 0 only.
+// The rate block of point p into M (row-major, rows = equations), warp-cooperative.
+// Stage 1: the lanes compute the transitions' rates into R (per radiative line k:
+// A + Bs Jeff, Ba Jeff and the ALO term -L opacity / nu; per collisional transition:
+// Cd abn, Ce abn interpolated in temperature).  Stage 2: lane r owns row r and adds the
+// rates that land in it while scanning the transitions in the order the reference
+// emits its triplets (radiative, ALO, collisional; then the normalisation row), so
+// every entry receives its additions in the reference's order.
+// R holds 3 nrad + 2 ncol_total doubles.
 __device__ void rate_block(const DevModel& m, const SpeciesView& s, uint32_t p, const double* lam,
-                           const double* abundance, uint32_t nspecs, double min_line_opacity, double* M) {
-    const uint32_t n = s.nlev, last = n - 1;
+                           const double* abundance, uint32_t nspecs, double min_line_opacity, double* M, double* R,
+                           int lane) {
+    const uint32_t n = s.nlev, last = n - 1, nr = s.nrad;
     const double* pp = s.pop + (size_t)p * n;  // populations before this solve
-    const double* Jeff = s.Jeff + (size_t)p * s.nrad;
-#define ADD(r, c, v) M[(size_t)(r) * n + (c)] = __dadd_rn(M[(size_t)(r) * n + (c)], (v))
-    for (uint32_t k = 0; k < s.nrad; k++) {
-        const double v_IJ = __dadd_rn(s.A[k], __dmul_rn(s.Bs[k], Jeff[k]));
-        const double v_JI = __dmul_rn(s.Ba[k], Jeff[k]);
-        const uint32_t I = s.irad[k], J = s.jrad[k];
-        if (J != last) {
-            ADD(J, I, v_IJ);
-            ADD(J, J, -v_JI);
-        }
-        if (I != last) {
-            ADD(I, J, v_JI);
-            ADD(I, I, -v_IJ);
-        }
-    }
-    for (uint32_t k = 0; k < s.nrad; k++) {
+    const double* Jeff = s.Jeff + (size_t)p * nr;
+    double* rIJ = R;            // [nr]
+    double* rJI = R + nr;       // [nr]
+    double* rA = R + 2 * nr;    // [nr]
+    double* cIJ = R + 3 * nr;   // [ncol_total]
+    double* cJI = cIJ + s.ncol_total;
+    for (uint32_t k = lane; k < nr; k += 32) {
+        rIJ[k] = __dadd_rn(s.A[k], __dmul_rn(s.Bs[k], Jeff[k]));
+        rJI[k] = __dmul_rn(s.Ba[k], Jeff[k]);
         const double Ls = lam[(size_t)p * m.L + s.line_offset + k];
-        const double v_IJ = -__ddiv_rn(__dmul_rn(Ls, opacity_of(s, pp, k, min_line_opacity)), s.freq[k]);
-        const uint32_t I = s.irad[k], J = s.jrad[k];
-        if (J != last) ADD(J, I, v_IJ);
-        if (I != last) ADD(I, I, -v_IJ);
+        rA[k] = -__ddiv_rn(__dmul_rn(Ls, opacity_of(s, pp, k, min_line_opacity)), s.freq[k]);
     }
     const double T = m.T[p];
+    uint32_t off = 0;
     for (uint32_t c = 0; c < s.ncolpar; c++) {
         const ColParView& cp = s.cp[c];
         double abn = abundance[(size_t)p * nspecs + cp.num];
@@ -122,7 +120,7 @@ __device__ void rate_block(const DevModel& m, const SpeciesView& s, uint32_t p, 
         const uint32_t t = search_table(cp.tmp, cp.ntmp, T);
         const bool edge = (t == 0 || t == cp.ntmp - 1);
         const double step = edge ? 0.0 : __ddiv_rn(T - cp.tmp[t - 1], cp.tmp[t] - cp.tmp[t - 1]);
-        for (uint32_t k = 0; k < cp.ncol; k++) {
+        for (uint32_t k = lane; k < cp.ncol; k += 32) {
             double Cd, Ce;
             if (edge) {
                 Cd = cp.Cd[(size_t)t * cp.ncol + k];
@@ -133,39 +131,76 @@ __device__ void rate_block(const DevModel& m, const SpeciesView& s, uint32_t p, 
                 Ce = __dadd_rn(ce0, __dmul_rn(__dsub_rn(ce1, ce0), step));
                 Cd = __dadd_rn(cd0, __dmul_rn(__dsub_rn(cd1, cd0), step));
             }
-            const double v_IJ = __dmul_rn(Cd, abn);
-            const double v_JI = __dmul_rn(Ce, abn);
-            const uint32_t I = cp.icol[k], J = cp.jcol[k];
-            if (J != last) {
-                ADD(J, I, v_IJ);
-                ADD(J, J, -v_JI);
-            }
-            if (I != last) {
-                ADD(I, J, v_JI);
-                ADD(I, I, -v_IJ);
-            }
+            cIJ[off + k] = __dmul_rn(Cd, abn);
+            cJI[off + k] = __dmul_rn(Ce, abn);
         }
+        off += cp.ncol;
     }
-    for (uint32_t i = 0; i < n; i++) ADD(last, i, 1.0);
+    __syncwarp();
+    for (uint32_t r = lane; r < n; r += 32) {
+        double* row = M + (size_t)r * n;
+#define ADD(c, v) row[c] = __dadd_rn(row[c], (v))
+        if (r != last) {
+            for (uint32_t k = 0; k < nr; k++) {
+                const uint32_t I = s.irad[k], J = s.jrad[k];
+                if (J == r) {
+                    ADD(I, rIJ[k]);
+                    ADD(J, -rJI[k]);
+                }
+                if (I == r) {
+                    ADD(J, rJI[k]);
+                    ADD(I, -rIJ[k]);
+                }
+            }
+            for (uint32_t k = 0; k < nr; k++) {
+                const uint32_t I = s.irad[k], J = s.jrad[k];
+                if (J == r) ADD(I, rA[k]);
+                if (I == r) ADD(I, -rA[k]);
+            }
+            uint32_t o = 0;
+            for (uint32_t c = 0; c < s.ncolpar; c++) {
+                const ColParView& cp = s.cp[c];
+                for (uint32_t k = 0; k < cp.ncol; k++) {
+                    const uint32_t I = cp.icol[k], J = cp.jcol[k];
+                    if (J == r) {
+                        ADD(I, cIJ[o + k]);
+                        ADD(J, -cJI[o + k]);
+                    }
+                    if (I == r) {
+                        ADD(J, cJI[o + k]);
+                        ADD(I, -cIJ[o + k]);
+                    }
+                }
+                o += cp.ncol;
+            }
+        } else {
+            for (uint32_t i = 0; i < n; i++) ADD(i, 1.0);
+        }
 #undef ADD
+    }
 }
 
-// Warp per point; the block's warps each own nlev*(nlev+1) doubles of shared memory.
+// Doubles of shared memory per warp of stateq_kernel: the block, the right-hand side and
+// the transitions' rates.
+__host__ __device__ inline size_t stateq_warp_doubles(const SpeciesView& s) {
+    return (size_t)s.nlev * (s.nlev + 1) + 3 * (size_t)s.nrad + 2 * (size_t)s.ncol_total;
+}
+
+// Warp per point; the block's warps each own stateq_warp_doubles of shared memory.
 __global__ void stateq_kernel(DevModel m, SpeciesView s, const double* __restrict__ lam,
                               const double* __restrict__ abundance, uint32_t nspecs, double min_line_opacity,
                               double* pop_out, int* status) {
     extern __shared__ __align__(16) double smem_ali[];
     const uint32_t n = s.nlev;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double* M = smem_ali + (size_t)w * n * (n + 1);
+    double* M = smem_ali + (size_t)w * stateq_warp_doubles(s);
     double* y = M + (size_t)n * n;
+    double* R = y + n;
     for (uint32_t p = blockIdx.x * nw + w; p < m.P; p += gridDim.x * nw) {
         for (uint32_t i = lane; i < n * (n + 1); i += 32) M[i] = 0.0;
         __syncwarp();
-        if (lane == 0) {
-            rate_block(m, s, p, lam, abundance, nspecs, min_line_opacity, M);
-            y[n - 1] = s.tot[p];
-        }
+        rate_block(m, s, p, lam, abundance, nspecs, min_line_opacity, M, R, lane);
+        if (lane == 0) y[n - 1] = s.tot[p];
         __syncwarp();
         bool singular = false;
         for (uint32_t c = 0; c < n; c++) {
@@ -527,7 +562,8 @@ cudaError_t ali_launch_stateq_and_refresh(MgrModel* model, const double* lam) {
         AliSpecies& sp = st.species[l];
         const uint32_t n = sp.view.nlev;
         const int wpb = 4;
-        const size_t smem = (size_t)wpb * n * (n + 1) * sizeof(double);
+        const size_t smem = (size_t)wpb * stateq_warp_doubles(sp.view) * sizeof(double);
+        (void)n;
         cudaError_t e = cudaFuncSetAttribute(stateq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         count_launch();
@@ -697,6 +733,8 @@ void ali_free(MgrModel* model) {
     if (!model || !model->ali) return;
     AliState* st = model->ali;
     if (st->graph) cudaGraphExecDestroy(st->graph);
+    for (cudaEvent_t& ev : st->ev)
+        if (ev) cudaEventDestroy(ev);
     for (void* p : st->pool_allocs) cudaFree(p);
     for (void* p : st->allocs) cudaFree(p);
     if (st->stats_host) cudaFreeHost(st->stats_host);
@@ -762,11 +800,35 @@ static int read_stats(MgrModel* model) {
 // function sums J and the ALO diagonal over the shards before Jeff.
 // The memory-lean variant (compute_level_populations_sparse) sums the line-integrated
 // J in the formal solve instead of J per frequency.
+// Phase events (AliState::ev): recorded on the model's stream, i.e. as event nodes of
+// the captured iteration.
+static void mark(MgrModel* model, int i) {
+    AliState& st = *model->ali;
+    if (st.timing && cudaEventRecord(st.ev[i], model->stream) != cudaSuccess) {
+        (void)cudaGetLastError();
+        st.timing = false;
+    }
+}
+
+// Adds the elapsed time between events a and b to phase_ms[k] (after the stream has
+// been synchronised).
+static void accumulate(AliState& st, int a, int b, int k) {
+    if (!st.timing) return;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, st.ev[a], st.ev[b]) != cudaSuccess) {
+        (void)cudaGetLastError();
+        st.timing = false;
+        return;
+    }
+    st.phase_ms[k] += ms;
+}
+
 static cudaError_t normal_iteration_launches(MgrModel* model, int precision) {
     AliState& st = *model->ali;
     const DevModel& m = model->dm;
     double* J = st.sparse ? nullptr : model->J_scratch;
     double* Jlin = st.sparse ? st.Jlin_buf : nullptr;
+    mark(model, 0);
     cudaError_t e = launch_fo2_range(model, precision, 0, m.P, J, nullptr, model->lam_scratch, model->work,
                                      model->work_bytes, model->shard_begin, model->shard_end, Jlin);
     if (e == cudaSuccess && model->shard_reduce) {
@@ -778,8 +840,11 @@ static cudaError_t normal_iteration_launches(MgrModel* model, int precision) {
             e = cudaErrorUnknown;
         }
     }
+    mark(model, 1);
     if (e == cudaSuccess) e = ali_launch_jeff(model, J, model->lam_scratch, Jlin);
+    mark(model, 2);
     if (e == cudaSuccess) e = ali_launch_stateq_and_refresh(model, model->lam_scratch);
+    mark(model, 3);
     return e;
 }
 
@@ -892,6 +957,8 @@ int mgr_model_set_species(MgrModel* model, uint32_t nlspecs, const MgrSpeciesDes
         v.nrad = d.nrad;
         v.line_offset = offset;
         v.ncolpar = d.ncolpar;
+        v.ncol_total = 0;
+        for (uint32_t c = 0; c < d.ncolpar; c++) v.ncol_total += d.colpar[c].ncol;
         offset += d.nrad;
         const double *en, *wt, *A, *Bs, *Ba, *fr;
         const uint32_t *ir, *jr;
@@ -1048,6 +1115,13 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
         }
     }
     if ((e = ali_launch_line_refresh(model)) != cudaSuccess) return cuda_fail(e, "line data");
+    for (double& t : st.phase_ms) t = 0.0;
+    st.timing = true;
+    for (cudaEvent_t& ev : st.ev)
+        if (!ev && cudaEventCreate(&ev) != cudaSuccess) {
+            (void)cudaGetLastError();
+            st.timing = false;
+        }
 
     const uint32_t nls = (uint32_t)st.species.size();
     const uint32_t skip = prm.Ng_acceleration_remove_N_its;
@@ -1088,8 +1162,11 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
             }
         }
         if (use_step) {
+            mark(model, 4);
             if ((e = ali_ng_step(model, order)) != cudaSuccess) return cuda_fail(e, "Ng acceleration");
+            mark(model, 5);
             if ((rc = read_stats(model)) != MGR_OK) return rc;
+            accumulate(st, 4, 5, 3);
             take_stats();
             iteration_normal = 0;
             continue;
@@ -1106,6 +1183,9 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
             return cuda_fail(e, "ALI iteration");
         }
         if ((rc = read_stats(model)) != MGR_OK) return rc;
+        accumulate(st, 0, 1, 0);
+        accumulate(st, 1, 2, 1);
+        accumulate(st, 2, 3, 2);
         take_stats();
         iteration_normal++;
         for (uint32_t l = 0; l < nls; l++) {
@@ -1134,6 +1214,21 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
         }
     }
     return st_rc;
+}
+
+int mgr_ali_phase_times(MgrModel* model, double* ms) {
+    MGR_MODEL_DEVICE(model);
+    if (!model || !ms || !model->ali) {
+        set_error("mgr_ali_phase_times: null argument or no species attached");
+        return MGR_ERR_ARGUMENT;
+    }
+    const AliState& st = *model->ali;
+    if (!st.timing) {
+        set_error("mgr_ali_phase_times: no timed ALI loop on this model");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    for (int k = 0; k < 4; k++) ms[k] = st.phase_ms[k];
+    return MGR_OK;
 }
 
 int mgr_compute_level_populations_sparse(MgrModel* model, int precision, int use_ng, long max_iterations,

@@ -26,6 +26,7 @@ struct ColParView {
 // One line-producing species, passed by value to the kernels.
 struct SpeciesView {
     uint32_t num, nlev, nrad, line_offset, ncolpar;
+    uint32_t ncol_total;   // collisional transitions summed over the partners
     const double* energy;
     const double* weight;
     const uint32_t* irad;  // upper level
@@ -85,6 +86,13 @@ struct AliState {
     int graph_sparse = -1;
     double* Jlin_buf = nullptr;  // [P][L]
     size_t Jlin_bytes = 0;
+    // Per-phase device time of the last compute_level_populations: events between the
+    // phases of a normal iteration (recorded inside the captured graph) and around the
+    // Ng steps; ms of [formal solve (and shard reduce), Jeff, statistical equilibrium
+    // with corrections / convergence / line-data refresh, Ng steps].
+    cudaEvent_t ev[6] = {};
+    bool timing = false;
+    double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
 };
 
 // Jlin: the memory-lean solve's line-integrated J [P][L] (compute_Jeff_sparse), or NULL.

