@@ -322,6 +322,9 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     }
     std::vector<float> dls, dll;
     line_offset_tables(d->line, d->sorted_line, L, dls, dll);
+    std::vector<float> bt_f(d->nboundary);  // boundary temperatures of the FP32 Planck function
+    for (uint32_t b = 0; b < d->nboundary; b++)
+        bt_f[b] = (float)(d->boundary_condition[b] == BC_THERMAL ? d->boundary_temperature[b] : T_CMB);
     std::vector<float> line_df(2 * (size_t)L);  // double-float line centres (hi, lo)
     for (uint32_t l = 0; l < L; l++) {
         line_df[2 * l] = (float)d->line[l];
@@ -343,6 +346,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.p2b, d->point2boundary, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bc, d->boundary_condition, d->nboundary)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bt, d->boundary_temperature, d->nboundary)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.bt_f, bt_f.data(), d->nboundary)) != cudaSuccess) break;
         if ((e = upload(m, &dm.raydir, d->ray_direction, 3 * NR)) != cudaSuccess) break;
         if ((e = upload(m, &dm.rayw, d->ray_weight, NR)) != cudaSuccess) break;
         if ((e = upload(m, &dm.antipod, d->antipod, d->nrays)) != cudaSuccess) break;

@@ -956,6 +956,21 @@ MGR_HD double f2d(float x) {
 #endif
 }
 
+// Split precision's boundary intensity (Solver::boundary_intensity / planck,
+// solver.tpp:1119-1142) in FP32 at the FP32 frequency nu: (2h/c^2 10^33) (nu 10^-11)^3 /
+// expm1f(h nu / (k T)), the reference's own single-precision expm1f, the constant scaled
+// so that every intermediate stays a normal float while h nu / (k T) < 40 (B > 1e-35);
+// beyond that, the FP64 expression.
+MGR_HD float boundary_intensity_f32(const DevModel& m, uint32_t p, float nu) {
+    const uint32_t b = m.p2b[p];
+    if (b >= m.B) return 0.0f;
+    if (m.bc[b] == BC_ZERO) return 0.0f;
+    const float x = (float)HH_OVER_KB * nu / m.bt_f[b];
+    if (!(x < 40.0f)) return (float)boundary_intensity(m, p, (double)nu);
+    const float n = nu * 1.0e-11f;
+    return (float)(TWO_HH_OVER_CC_SQUARED * 1.0e33) * (n * n * n) / expm1f(x);
+}
+
 // Split-precision Planck function / boundary intensity: the reference's expressions
 // with the two divisions as reciprocals.
 template <int MODE>
@@ -1073,6 +1088,7 @@ struct Sweep {
     // uv solve only: the last pair's branch, its outer element's opacity, its distance
     bool last_large;
     double chi_out, dz_last;
+    float dtf = 0.0f, S_inf = 0.0f;  // dt and S_in as the split sweep's floats
 };
 
 // Two-sided Feautrier solve of frequency c.f on the ray pair staged in `bk`
@@ -1095,7 +1111,8 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     res.v = 0.0;
     res.dtm = res.dtp = 0.0;
     if (!res.solved) {
-        res.u = boundary_intensity_m<MODE>(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
+        if constexpr (MODE == MODE_SPLIT) res.u = f2d(boundary_intensity_f32(m, c.o, c.fq));
+        else res.u = boundary_intensity_m<MODE>(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
         res.Ldiag = 0.0;
         return res;
     }
@@ -1117,12 +1134,13 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             Elem outer;
             iter_next<MODE>(m, h, c.o, l, it, outer);
             EC<MODE> ec_out{T(0), T(0), false};
-            double bshift = outer.shift;
+            double Ibdy;
             if constexpr (MODE == MODE_SPLIT) {
-                double fac;
-                elem_shift_fac(h, outer, bshift, fac);
+                // at the outer element's frequency nu shift = nu + nu (shift - 1), in FP32
+                Ibdy = f2d(boundary_intensity_f32(m, outer.nr, fmaf(c.fq, outer.dsh, c.fq)));
+            } else {
+                Ibdy = boundary_intensity_m<MODE>(m, outer.nr, c.freq * outer.shift);
             }
-            const double Ibdy = boundary_intensity_m<MODE>(m, outer.nr, c.freq * bshift);
             T dt_prev = T(0), S_carry = T(0);
             bool first = true;
             while (true) {
@@ -1141,12 +1159,14 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 const T rowS = (side == 0 || first) ? po.Slo : S_carry;
                 if (PROJ && first) {
                     // boundary row multiplied through by dtau^2/2: F = h = dtau (dtau/2 + 1),
-                    // Su = (S dtau^2/2 + I_bdy dtau) / (1 + h)
-                    const double dt = po.dtau;
-                    const double hb = dt * fma(0.5, dt, 1.0);
+                    // Su = (S dtau^2/2 + I_bdy dtau) / (1 + h); h from the FP32 dtau in FP32,
+                    // as the interior rows form their coefficients
+                    const float dtf = (float)po.dtau;
+                    const double dt = f2d(dtf);
+                    const double hb = f2d(dtf * fmaf(0.5f, dtf, 1.0f));
                     ps.NG = hb;
                     ps.D = 1.0 + hb;
-                    ps.NS = fma((double)rowS * 0.5 * dt, dt, Ibdy * dt);
+                    ps.NS = fma(f2d((float)rowS * 0.5f) * dt, dt, Ibdy * dt);
                     ps.Dp = 1.0;
                     first = false;
                 } else if (PROJ) {
@@ -1174,6 +1194,8 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             }
             st.dt = dt_prev;
             st.S_in = S_carry;
+            st.dtf = (float)dt_prev;
+            st.S_inf = (float)S_carry;
             st.rows = true;
         }
         if (side) {
@@ -1186,7 +1208,30 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     }
 
     if constexpr (PROJ) {
-        // back to (F / (1 + F), 1 / (1 + F), Su) at the origin: two reciprocals per lane
+        if (top.rows && bot.rows) {
+            // the origin's row in projective form with elim_row_proj's FP32 coefficients
+            // q = dtau_b / dtau_t, iC = (dtau_t + dtau_b) dtau_b / 2:
+            //   u = (q Su_t + S_in iC + Su_b) / (q G_t + iC + G_b),  L_diag = iC / (same)
+            // (the reference's u[c] and L_diag[c], with G = NG / D, Su = NS / D per side)
+            const float dto = top.dtf, dti = bot.dtf;
+            double q, iC;
+            if (dto > 1.0e-18f && dto < 1.0e18f && dti > 1.0e-18f && dti < 1.0e18f) {
+                q = f2d(fast_div(dti, dto));
+                iC = f2d(0.5f * (dto + dti) * dti);
+            } else {
+                const double2 k = elim_coeffs_fp64(dto, dti);
+                q = k.x;
+                iC = k.y;
+            }
+            const double qrt = q * drcp<MODE>(ptop.D);
+            const double rb = drcp<MODE>(pbot.D);
+            const double num = fma(qrt, ptop.NS, fma(rb, pbot.NS, f2d(bot.S_inf) * iC));
+            const double rd = drcp<MODE>(fma(qrt, ptop.NG, fma(rb, pbot.NG, iC)));
+            res.u = num * rd;
+            res.Ldiag = iC * rd;
+            return res;
+        }
+        // one-sided rays: back to (F / (1 + F), 1 / (1 + F), Su) at the origin
         if (top.rows) {
             const double r = drcp<MODE>(ptop.D);
             top.F = ptop.NG * r;  // G
@@ -1235,7 +1280,8 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             res.v = -(coeffmin * u_min + coeffplus * u_plus + coeffzero * res.u);
         }
     } else if (bot.rows) {  // origin is the first element
-        const double Ibdy = boundary_intensity_m<MODE>(m, c.o, c.freq);
+        const double Ibdy = (MODE == MODE_SPLIT) ? f2d(boundary_intensity_f32(m, c.o, c.fq))
+                                                 : boundary_intensity_m<MODE>(m, c.o, c.freq);
         const double inverse_dtau_f = drcp<MODE>(bot.dt);
         const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
         const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
@@ -1250,7 +1296,8 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         res.Ldiag = drcp<MODE>(Cf) * D;
         if constexpr (UV) res.v = Ibdy - res.u;  // Sv[first] = I_bdy_f - Su[first]
     } else {  // origin is the last element
-        const double Ibdy = boundary_intensity_m<MODE>(m, c.o, c.freq);
+        const double Ibdy = (MODE == MODE_SPLIT) ? f2d(boundary_intensity_f32(m, c.o, c.fq))
+                                                 : boundary_intensity_m<MODE>(m, c.o, c.freq);
         const double inverse_dtau_l = drcp<MODE>(top.dt);
         const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
         const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
