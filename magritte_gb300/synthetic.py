@@ -69,6 +69,11 @@ class Linedata:
     jrad: np.ndarray
     A: np.ndarray
     colpar: List[CollisionPartner] = field(default_factory=list)
+    # line frequencies and Einstein B coefficients as given (a model read from files
+    # carries its own); None derives them from the levels as the reference's setup does
+    frequency_given: Optional[np.ndarray] = None
+    Bs_given: Optional[np.ndarray] = None
+    Ba_given: Optional[np.ndarray] = None
 
     @property
     def nlev(self):
@@ -80,15 +85,21 @@ class Linedata:
 
     @property
     def frequency(self):
+        if self.frequency_given is not None:
+            return self.frequency_given
         return (self.energy[self.irad] - self.energy[self.jrad]) / HH
 
     @property
     def Bs(self):
+        if self.Bs_given is not None:
+            return self.Bs_given
         f = self.frequency
         return self.A * CC**2 / (2.0 * HH * f**3)
 
     @property
     def Ba(self):
+        if self.Ba_given is not None:
+            return self.Ba_given
         return self.weight[self.irad] / self.weight[self.jrad] * self.Bs
 
 
