@@ -105,7 +105,7 @@ float to_f32_floor_host(double x) {
 struct EmuModel {
     std::vector<double4_32a> pos, vel, edge;
     std::vector<double> ub, Sp;
-    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f, iw_lo, line_df, bt_f;
+    std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f, iw_lo, line_df, bkt;
     std::vector<uint16_t> nint, nint_all;
     std::vector<uint32_t> lq2f, corr_line;
     DevModel m{};
@@ -186,10 +186,13 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
         x.line_df[2 * l + 1] = (float)(d->line[l] - (double)x.line_df[2 * l]);
     }
     m.line_df = x.line_df.data();
-    x.bt_f.resize(d->nboundary ? d->nboundary : 1);
-    for (uint32_t b = 0; b < d->nboundary; b++)
-        x.bt_f[b] = (float)(d->boundary_condition[b] == BC_THERMAL ? d->boundary_temperature[b] : T_CMB);
-    m.bt_f = x.bt_f.data();
+    x.bkt.resize(d->nboundary ? 2 * (size_t)d->nboundary : 2);
+    for (uint32_t b = 0; b < d->nboundary; b++) {
+        const double k = HH_OVER_KB / (d->boundary_condition[b] == BC_THERMAL ? d->boundary_temperature[b] : T_CMB);
+        x.bkt[2 * b] = (float)k;
+        x.bkt[2 * b + 1] = (float)(k - (double)x.bkt[2 * b]);
+    }
+    m.bkt = x.bkt.data();
     m.iw_lo = x.iw_lo.data();
     // the maps of an imaging spectral discretisation are unset: keep only valid
     // (line, quadrature point) entries, and measure each frequency from its nearest

@@ -315,5 +315,8 @@ PYBIND11_MODULE(core, m) {
         .def("release_device", &Model::release_device)
         .def("upload", [](Model& m) { return (uintptr_t)m.upload(); },
              "Upload (or refresh) the device model; returns the MgrModel* handle as an integer")
-        .def("gpu_launches", &Model::launches);
+        .def("gpu_launches", &Model::launches)
+        .def("ali_phase_times", &Model::ali_phase_times,
+             "Device ms of the latest ALI loop's phases: formal solve, Jeff, rate equations + corrections + "
+             "line refresh, Ng steps (empty list without a timed loop)");
 }

@@ -26,6 +26,12 @@ void Model::release_device() {
 
 uint64_t Model::launches() const { return mgr_launch_count(); }
 
+std::vector<double> Model::ali_phase_times() const {
+    double ms[4];
+    if (!dev_ || mgr_ali_phase_times(dev_, ms) != MGR_OK) return {};
+    return std::vector<double>(ms, ms + 4);
+}
+
 // ---------------------------------------------------------------------------------
 // prepare(): derived data that the reference computes in its read() methods.
 // ---------------------------------------------------------------------------------

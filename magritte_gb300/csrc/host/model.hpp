@@ -296,6 +296,10 @@ class Model {
     void release_device();
     MgrModel* device_model();
     uint64_t launches() const;
+    // Device time of each ALI phase in the latest compute_level_populations call
+    // (formal solve, Jeff, rate equations + corrections + line refresh, Ng), in ms;
+    // empty without a timed loop on the current device model.
+    std::vector<double> ali_phase_times() const;
 
    private:
     MgrModel* dev_ = nullptr;

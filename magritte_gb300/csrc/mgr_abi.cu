@@ -322,9 +322,12 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     }
     std::vector<float> dls, dll;
     line_offset_tables(d->line, d->sorted_line, L, dls, dll);
-    std::vector<float> bt_f(d->nboundary);  // boundary temperatures of the FP32 Planck function
-    for (uint32_t b = 0; b < d->nboundary; b++)
-        bt_f[b] = (float)(d->boundary_condition[b] == BC_THERMAL ? d->boundary_temperature[b] : T_CMB);
+    std::vector<float> bkt(2 * (size_t)d->nboundary);  // h / (k T) per boundary, double-float
+    for (uint32_t b = 0; b < d->nboundary; b++) {
+        const double k = HH_OVER_KB / (d->boundary_condition[b] == BC_THERMAL ? d->boundary_temperature[b] : T_CMB);
+        bkt[2 * b] = (float)k;
+        bkt[2 * b + 1] = (float)(k - (double)bkt[2 * b]);
+    }
     std::vector<float> line_df(2 * (size_t)L);  // double-float line centres (hi, lo)
     for (uint32_t l = 0; l < L; l++) {
         line_df[2 * l] = (float)d->line[l];
@@ -346,7 +349,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.p2b, d->point2boundary, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bc, d->boundary_condition, d->nboundary)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bt, d->boundary_temperature, d->nboundary)) != cudaSuccess) break;
-        if ((e = upload(m, &dm.bt_f, bt_f.data(), d->nboundary)) != cudaSuccess) break;
+        if ((e = upload(m, &dm.bkt, bkt.data(), 2 * (size_t)d->nboundary)) != cudaSuccess) break;
         if ((e = upload(m, &dm.raydir, d->ray_direction, 3 * NR)) != cudaSuccess) break;
         if ((e = upload(m, &dm.rayw, d->ray_weight, NR)) != cudaSuccess) break;
         if ((e = upload(m, &dm.antipod, d->antipod, d->nrays)) != cudaSuccess) break;

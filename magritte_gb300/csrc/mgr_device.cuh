@@ -54,7 +54,7 @@ struct DevModel {
     const uint32_t* p2b;     // [P]
     const int32_t* bc;       // [B]
     const double* bt;        // [B]
-    const float* bt_f;       // [B] boundary temperatures as floats (Thermal) or T_CMB (CMB)
+    const float* bkt;        // [B][2] h / (k T) of each boundary (T_CMB for CMB) as a double-float (hi, lo)
     const double* raydir;    // [nrays][3]
     const double* rayw;      // [nrays]
     const uint32_t* antipod; // [nrays]

@@ -956,19 +956,34 @@ MGR_HD double f2d(float x) {
 #endif
 }
 
+// 2h/c^2 2^108 as a double-float: with nu scaled by 2^-36, nu^3 and the product stay
+// normal floats for every nu between 1e8 and 1e16 Hz.
+constexpr double kPlanckScaled = TWO_HH_OVER_CC_SQUARED * 0x1p108;
+constexpr float kPlanckHi = (float)kPlanckScaled;
+constexpr float kPlanckLo = (float)(kPlanckScaled - (double)kPlanckHi);
+
 // Split precision's boundary intensity (Solver::boundary_intensity / planck,
-// solver.tpp:1119-1142) in FP32 at the FP32 frequency nu: (2h/c^2 10^33) (nu 10^-11)^3 /
-// expm1f(h nu / (k T)), the reference's own single-precision expm1f, the constant scaled
-// so that every intermediate stays a normal float while h nu / (k T) < 40 (B > 1e-35);
-// beyond that, the FP64 expression.
-MGR_HD float boundary_intensity_f32(const DevModel& m, uint32_t p, float nu) {
+// solver.tpp:1119-1142) without FP64 arithmetic, at the double-float frequency nu:
+//   x = h nu / (k T)  as a double-float product, rounded once to the float the
+//       reference passes to expm1f (the reference rounds its FP64 quotient; the two
+//       agree except within ~1e-14 of a rounding boundary),
+//   B = (2h/c^2 2^108) (nu 2^-36)^3 / expm1f(x)  as double-float products and a
+//       double-float quotient (q = fl(N / e), then the exact remainder N - q e over e),
+// so B carries ~1e-14 relative error against the FP64 expression instead of the FP32
+// roundings of nu, T and nu^3.  Beyond x = 40 (B below 1e-17 of its peak), the FP64
+// expression.
+MGR_HD double boundary_intensity_f2(const DevModel& m, uint32_t p, F2 nu) {
     const uint32_t b = m.p2b[p];
-    if (b >= m.B) return 0.0f;
-    if (m.bc[b] == BC_ZERO) return 0.0f;
-    const float x = (float)HH_OVER_KB * nu / m.bt_f[b];
-    if (!(x < 40.0f)) return (float)boundary_intensity(m, p, (double)nu);
-    const float n = nu * 1.0e-11f;
-    return (float)(TWO_HH_OVER_CC_SQUARED * 1.0e33) * (n * n * n) / expm1f(x);
+    if (b >= m.B) return 0.0;
+    if (m.bc[b] == BC_ZERO) return 0.0;
+    const F2 x = f2_mul(nu, F2{m.bkt[2 * b], m.bkt[2 * b + 1]});
+    if (!(x.hi < 40.0f)) return boundary_intensity(m, p, (double)nu.hi + (double)nu.lo);
+    const F2 n{nu.hi * 0x1p-36f, nu.lo * 0x1p-36f};
+    const F2 num = f2_mul(f2_mul(f2_mul(n, n), n), F2{kPlanckHi, kPlanckLo});
+    const float e = expm1f(x.hi);
+    const float q = num.hi / e;
+    const float q2 = (fmaf(-q, e, num.hi) + num.lo) / e;
+    return (double)q + (double)q2;
 }
 
 // Split-precision Planck function / boundary intensity: the reference's expressions
@@ -1111,7 +1126,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     res.v = 0.0;
     res.dtm = res.dtp = 0.0;
     if (!res.solved) {
-        if constexpr (MODE == MODE_SPLIT) res.u = f2d(boundary_intensity_f32(m, c.o, c.fq));
+        if constexpr (MODE == MODE_SPLIT) res.u = boundary_intensity_f2(m, c.o, F2{c.fq, c.fql});
         else res.u = boundary_intensity_m<MODE>(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
         res.Ldiag = 0.0;
         return res;
@@ -1136,8 +1151,9 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             EC<MODE> ec_out{T(0), T(0), false};
             double Ibdy;
             if constexpr (MODE == MODE_SPLIT) {
-                // at the outer element's frequency nu shift = nu + nu (shift - 1), in FP32
-                Ibdy = f2d(boundary_intensity_f32(m, outer.nr, fmaf(c.fq, outer.dsh, c.fq)));
+                // at the outer element's frequency nu shift = nu + nu (shift - 1), double-float
+                const F2 nu{c.fq, c.fql};
+                Ibdy = boundary_intensity_f2(m, outer.nr, f2_add(nu, f2_mul(nu, elem_dsh_f2(h, outer))));
             } else {
                 Ibdy = boundary_intensity_m<MODE>(m, outer.nr, c.freq * outer.shift);
             }
@@ -1159,11 +1175,13 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 const T rowS = (side == 0 || first) ? po.Slo : S_carry;
                 if (PROJ && first) {
                     // boundary row multiplied through by dtau^2/2: F = h = dtau (dtau/2 + 1),
-                    // Su = (S dtau^2/2 + I_bdy dtau) / (1 + h); h from the FP32 dtau in FP32,
-                    // as the interior rows form their coefficients
+                    // Su = (S dtau^2/2 + I_bdy dtau) / (1 + h); from the FP32 dtau, as the
+                    // interior rows form their coefficients, but h with one FP64 FMA: in
+                    // FP32 the factor 1 + dtau/2 rounds away dtau/2 below ~1e-7, and
+                    // NS / NG, the boundary intensity the sweep carries, with it
                     const float dtf = (float)po.dtau;
                     const double dt = f2d(dtf);
-                    const double hb = f2d(dtf * fmaf(0.5f, dtf, 1.0f));
+                    const double hb = fma(f2d(0.5f * dtf), dt, dt);
                     ps.NG = hb;
                     ps.D = 1.0 + hb;
                     ps.NS = fma(f2d((float)rowS * 0.5f) * dt, dt, Ibdy * dt);
@@ -1280,7 +1298,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             res.v = -(coeffmin * u_min + coeffplus * u_plus + coeffzero * res.u);
         }
     } else if (bot.rows) {  // origin is the first element
-        const double Ibdy = (MODE == MODE_SPLIT) ? f2d(boundary_intensity_f32(m, c.o, c.fq))
+        const double Ibdy = (MODE == MODE_SPLIT) ? boundary_intensity_f2(m, c.o, F2{c.fq, c.fql})
                                                  : boundary_intensity_m<MODE>(m, c.o, c.freq);
         const double inverse_dtau_f = drcp<MODE>(bot.dt);
         const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
@@ -1296,7 +1314,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         res.Ldiag = drcp<MODE>(Cf) * D;
         if constexpr (UV) res.v = Ibdy - res.u;  // Sv[first] = I_bdy_f - Su[first]
     } else {  // origin is the last element
-        const double Ibdy = (MODE == MODE_SPLIT) ? f2d(boundary_intensity_f32(m, c.o, c.fq))
+        const double Ibdy = (MODE == MODE_SPLIT) ? boundary_intensity_f2(m, c.o, F2{c.fq, c.fql})
                                                  : boundary_intensity_m<MODE>(m, c.o, c.freq);
         const double inverse_dtau_l = drcp<MODE>(top.dt);
         const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;

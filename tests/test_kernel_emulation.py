@@ -197,3 +197,26 @@ def test_emulated_image_for_point_matches_oracle(emu, name, approx):
                 floor = 1e-300 if precision == "fp64" else 1e-10 * np.abs(ref[k]).max()
                 kt = tol if (precision == "fp64" or k == "u_ray") else 1e-4
                 assert H.max_rel(got[k], ref[k], floor=floor) < kt, (rr, p, precision, k)
+
+
+@pytest.mark.parametrize("bc", ["cmb", "thermal"])
+def test_split_boundary_intensity_equals_fp64(emu, bc):
+    """Without opacity J is the Doppler-shifted boundary intensity alone.  Split
+    precision evaluates it in double-float arithmetic (h nu / k T rounded once to the
+    float expm1f takes, as the reference rounds it; nu^3 / expm1f as double-float
+    products and quotient) and forms the boundary row's h = dtau (1 + dtau/2) in FP64,
+    so it equals the FP64 mode's to ~1e-14 and meets the reference's analytic bar
+    (all_zero_single_ray.py: 6.41e-6) as the FP64 mode does.  Both ends carry the same
+    temperature: with two different boundary intensities the FP32 optical depths of
+    the two boundary pairs weigh them (a ~1e-8 effect, inside the split bar)."""
+    raw = H.all_zero_model()
+    if bc == "thermal":
+        raw.boundary_condition[:] = S.BC_THERMAL
+        raw.boundary_temperature[:] = 211.0
+    a = H.setup(raw)
+    J64, _ = run(emu, a, "fp64")
+    J32, _ = run(emu, a, "split")
+    assert H.max_rel(J32, J64) < 1e-12
+    if bc == "cmb":
+        err = np.abs(H.relative_error(H.all_zero_solution(raw), J32[:, 0]))
+        assert np.max(err) < 6.41e-6
