@@ -37,8 +37,8 @@ __global__ void __launch_bounds__(256) fo2_s_kernel(DevModel m, uint32_t cap, co
         __syncwarp();
         bool ok = true;
         for (uint32_t rr = 0; rr < m.hnrays; rr++) {
-            const int nb = trace_half<true, 0, 1>(m, o, rr, cap, bk, lane, status);
-            const int nf = trace_half<true, 0, 1>(m, o, m.antipod[rr], cap, fw, lane, status);
+            int nb = 0, nf = 0;
+            trace_pair<true, 0, 1>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
             if (nb < 0 || nf < 0) {
                 ok = false;  // status recorded by the trace
                 break;
@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(256) fo2_adj_kernel(DevModel m, uint32_t cap, 
         double vo[3] = {0.0, 0.0, 0.0};
         for (uint32_t rr = 0; rr < m.hnrays; rr++) {
             const uint32_t ar = m.antipod[rr];
-            const int nb = trace_half<true, 0, 1>(m, o, rr, cap, bk, lane, status);
-            const int nf = trace_half<true, 0, 1>(m, o, ar, cap, fw, lane, status);
+            int nb = 0, nf = 0;
+            trace_pair<true, 0, 1>(m, o, rr, ar, cap, bk, fw, lane, status, nb, nf);
             if (nb < 0 || nf < 0) break;
             const double* db = ray_dir(m, o, rr);
             const double* df = ray_dir(m, o, ar);

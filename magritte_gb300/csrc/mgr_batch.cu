@@ -100,8 +100,8 @@ __global__ void __launch_bounds__(256, MINB)
         __syncwarp();
         for (uint32_t rr = 0; rr < m.hnrays && ok; rr++) {
             // general geometry with shared rays (mgr_batch_create refuses the other kinds)
-            const int nb = trace_half<true, 0, 0>(m, o, rr, cap, bk, lane, status);
-            const int nf = trace_half<true, 0, 0>(m, o, m.antipod[rr], cap, fw, lane, status);
+            int nb = 0, nf = 0;
+            trace_pair<true, 0, 0>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
             if (nb < 0 || nf < 0) {  // status recorded by the trace
                 ok = false;
                 break;

@@ -161,8 +161,8 @@ __global__ void ray_lengths_kernel(DevModel m, uint32_t cap, uint32_t* d_max, in
     carve_halves(smem + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
     const uint32_t o = (uint32_t)(gw / m.hnrays);
     const uint32_t rr = (uint32_t)(gw % m.hnrays);
-    const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-    const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+    int nb = 0, nf = 0;
+    trace_pair<true>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
     if (nb < 0 || nf < 0) return;
     uint32_t len = 0;
     for (int s = lane; s < nb; s += 32) len += n_interp_all_lines(m, s ? bk.ids[s - 1] : o, bk.ids[s]);
@@ -203,8 +203,8 @@ __global__ void __launch_bounds__(256, MINB)
     for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
         const uint32_t o = o_begin + (uint32_t)(item / nR);
         const uint32_t rr = rr0 + (uint32_t)(item % nR);
-        const int nb = trace_half<true, 0, GEO>(m, o, rr, cap, bk, lane, status);
-        const int nf = trace_half<true, 0, GEO>(m, o, m.antipod[rr], cap, fw, lane, status);
+        int nb = 0, nf = 0;
+        trace_pair<true, 0, GEO>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
         if (nb < 0 || nf < 0) continue;  // status recorded by the trace
         double* Ui = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
         double* Li = LD ? LD + (size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F : nullptr;
@@ -356,8 +356,8 @@ __global__ void trace_export_kernel(DevModel m, uint32_t o, uint32_t rr, uint32_
     const int lane = threadIdx.x & 31;
     HalfSmem bk, fw;
     carve_halves(smem, cap, bk, fw);
-    const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-    const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+    int nb = 0, nf = 0;
+    trace_pair<true>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
     if (lane != 0) return;
     if (nb < 0 || nf < 0) {
         meta[0] = 0;
@@ -464,8 +464,8 @@ __global__ void ray_stats_kernel(DevModel m, uint32_t cap, unsigned long long* s
     carve_halves(smem + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
     const uint32_t o = (uint32_t)(gw / m.hnrays);
     const uint32_t rr = (uint32_t)(gw % m.hnrays);
-    const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-    const int nf = trace_half<true>(m, o, m.antipod[rr], cap, fw, lane, status);
+    int nb = 0, nf = 0;
+    trace_pair<true>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
     if (nb < 0 || nf < 0) return;
     unsigned long long nbr = 0, elems = 0;
     for (int s = lane; s < nb; s += 32) {

@@ -42,8 +42,8 @@ __global__ void __launch_bounds__(256) image_kernel(DevModel m, uint32_t cap, ui
         set_dsh0(bk, shb);
         set_dsh0(fw, shf);
         bk.cshift = fw.cshift = shb;
-        const int nb = trace_half<true, 1>(m, o, rr, cap, bk, lane, status);
-        const int nf = trace_half<true, 1>(m, o, ar, cap, fw, lane, status);
+        int nb = 0, nf = 0;
+        trace_pair<true, 1>(m, o, rr, ar, cap, bk, fw, lane, status, nb, nf);
         if (nb < 0 || nf < 0) continue;
         for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
             const uint32_t f = f0 + lane;
@@ -309,8 +309,8 @@ __global__ void __launch_bounds__(32) image_point_count_kernel(DevModel m, uint3
     HalfSmem bk, fw;
     carve_halves(smem, cap, bk, fw);
     const uint32_t ar = m.antipod[rr];
-    const int nb = trace_half<true, 1>(m, p, rr, cap, bk, lane, status);
-    const int nf = trace_half<true, 1>(m, p, ar, cap, fw, lane, status);
+    int nb = 0, nf = 0;
+    trace_pair<true, 1>(m, p, rr, ar, cap, bk, fw, lane, status, nb, nf);
     uint32_t n = 0;
     if (nb >= 0 && nf >= 0) {
         for (int s = lane; s < nb; s += 32) n += m.nint_all[bk.eid[s]];
@@ -344,8 +344,8 @@ __global__ void __launch_bounds__(32) image_point_kernel(DevModel m, uint32_t ca
     set_dsh0(bk, shb);
     set_dsh0(fw, shf);
     bk.cshift = fw.cshift = shb;
-    const int nb = trace_half<true, 1>(m, p, rr, cap, bk, lane, status);
-    const int nf = trace_half<true, 1>(m, p, ar, cap, fw, lane, status);
+    int nb = 0, nf = 0;
+    trace_pair<true, 1>(m, p, rr, ar, cap, bk, fw, lane, status, nb, nf);
     if (nb < 0 || nf < 0) return;
     const uint32_t f = blockIdx.x * 32 + lane;
     if (f >= m.F) return;

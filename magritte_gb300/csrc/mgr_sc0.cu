@@ -35,8 +35,8 @@ __global__ void __launch_bounds__(256, MINB)
         const uint32_t o = o_begin + (uint32_t)(item / R);
         const uint32_t rr = (uint32_t)(item % R);
         const uint32_t ar = m.antipod[rr];
-        const int nb = trace_half<true>(m, o, rr, cap, bk, lane, status);
-        const int nf = trace_half<true>(m, o, ar, cap, fw, lane, status);
+        int nb = 0, nf = 0;
+        trace_pair<true>(m, o, rr, ar, cap, bk, fw, lane, status, nb, nf);
         if (nb < 0 || nf < 0) continue;
         double* Ui = U + (size_t)rr * u_stride + (size_t)(o - u_o0) * m.F;
         const size_t xo = (size_t)rr * x_stride + (size_t)(o - x_o0) * m.F;

@@ -105,6 +105,7 @@ __device__ __forceinline__ bool warp_next_point(const DevModel& m, const double4
     unsigned long long best = ~0ull;
     uint32_t besti = 0xffffffffu;
     double bestZ = 0.0;
+#pragma unroll 1
     for (uint32_t i = lane; i < nnb; i += 32) {
         const double4_32a e = m.edge[cum + i];
         const double Rx = dsub_rn(e.x, po.x);
@@ -249,6 +250,19 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
         __syncwarp();
     }
     return count;
+}
+
+// Both halves of a ray pair: r into `bk`, its antipode ar into `fw`.  One loop over
+// the two halves, so that a kernel holds a single copy of the trace's code.
+template <bool STORE, int FRAME = 0, int GEO = 1>
+__device__ __forceinline__ void trace_pair(const DevModel& m, uint32_t o, uint32_t r, uint32_t ar, uint32_t cap,
+                                           HalfSmem& bk, HalfSmem& fw, int lane, int* status, int& nb, int& nf) {
+#pragma unroll 1
+    for (int side = 0; side < 2; side++) {
+        const int n = trace_half<STORE, FRAME, GEO>(m, o, side ? ar : r, cap, side ? fw : bk, lane, status);
+        if (side) nf = n;
+        else nb = n;
+    }
 }
 
 // An element of the ray pair as the reference's per-thread buffers hold it
@@ -699,11 +713,15 @@ MGR_HD F2 elem_iw_f2(const DevModel& m, const Elem& e, uint32_t l) {
 // |x| >= 3.919206, the device's table of (float)erf((double)x) over every float in
 // [kErfBandLo, 3.919206) (erf_band_table), and FP64 below (the same-wing arguments
 // start at 1.5: the float positions that select them are within 1e-5 of the exact ones).
+// erff_cr out of line, for the band's lower edge: the same-wing arguments start at
+// 1.5, so the kernels reach it only through FP32 rounding, and their code stays small.
+static __host__ __device__ __noinline__ float erff_cr_cold(float x) { return erff_cr(x); }
+
 MGR_HD float erff_band(const DevModel& m, float x) {
 #ifdef __CUDA_ARCH__
     const float ax = fabsf(x);
     if (ax >= 3.919206f) return copysignf(1.0f, x);
-    if (ax < kErfBandLo) return erff_cr(x);
+    if (ax < kErfBandLo) return erff_cr_cold(x);
     return copysignf(m.erf_band[__float_as_uint(ax) - __float_as_uint(kErfBandLo)], x);
 #else
     (void)m;  // the host emulation evaluates the table's entries directly
@@ -915,8 +933,17 @@ MGR_HD void eval_pair(const DevModel& m, const double* sl, const LaneCtx& c, con
             pair_li_f32<AP>(m, c, h, outer, inner, dzf, out.dtau, out.Slo, out.Shi);
         }
     } else {
-        elem_fresh<MODE, AP>(m, sl, c, outer, eco);
-        elem_fresh<MODE, AP>(m, sl, c, inner, eci);
+        // one call site for both caches (the outer element's is usually the previous
+        // pair's inner one): a second inlined copy of the line sum would only grow the
+        // loop's code
+#pragma unroll 1
+        for (int k = 0; k < 2; k++) {
+            if (k ? eci.ok : eco.ok) continue;
+            EC<MODE> r{};
+            elem_fresh<MODE, AP>(m, sl, c, k ? inner : outer, r);
+            if (k) eci = r;
+            else eco = r;
+        }
         out.Slo = eco.S;
         out.Shi = eci.S;
         if constexpr (MODE == MODE_FP64) {
@@ -956,6 +983,10 @@ MGR_HD double f2d(float x) {
 #endif
 }
 
+// The FP64 Planck function out of line (split precision's boundary intensities
+// beyond h nu / k T = 40).
+static __host__ __device__ __noinline__ double planck_cold(double temp, double freq) { return planck(temp, freq); }
+
 // 2h/c^2 2^108 as a double-float: with nu scaled by 2^-36, nu^3 and the product stay
 // normal floats for every nu between 1e8 and 1e16 Hz.
 constexpr double kPlanckScaled = TWO_HH_OVER_CC_SQUARED * 0x1p108;
@@ -977,7 +1008,7 @@ MGR_HD double boundary_intensity_f2(const DevModel& m, uint32_t p, F2 nu) {
     if (b >= m.B) return 0.0;
     if (m.bc[b] == BC_ZERO) return 0.0;
     const F2 x = f2_mul(nu, F2{m.bkt[2 * b], m.bkt[2 * b + 1]});
-    if (!(x.hi < 40.0f)) return boundary_intensity(m, p, (double)nu.hi + (double)nu.lo);
+    if (!(x.hi < 40.0f)) return planck_cold(m.bc[b] == BC_THERMAL ? m.bt[b] : T_CMB, (double)nu.hi + (double)nu.lo);
     const F2 n{nu.hi * 0x1p-36f, nu.lo * 0x1p-36f};
     const F2 num = f2_mul(f2_mul(f2_mul(n, n), n), F2{kPlanckHi, kPlanckLo});
     const float e = expm1f(x.hi);
@@ -1125,9 +1156,13 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     res.solved = (nb > 0) || (nf > 0);
     res.v = 0.0;
     res.dtm = res.dtp = 0.0;
+    // the origin's own boundary intensity (no ray pair, or a one-sided one: boundary
+    // origins only; 0 at once for interior points), evaluated at one site
+    double Io;
+    if constexpr (MODE == MODE_SPLIT) Io = boundary_intensity_f2(m, c.o, F2{c.fq, c.fql});
+    else Io = boundary_intensity_m<MODE>(m, c.o, c.freq);
     if (!res.solved) {
-        if constexpr (MODE == MODE_SPLIT) res.u = boundary_intensity_f2(m, c.o, F2{c.fq, c.fql});
-        else res.u = boundary_intensity_m<MODE>(m, c.o, m.nu[(size_t)c.o * m.F + c.f]);
+        res.u = Io;
         res.Ldiag = 0.0;
         return res;
     }
@@ -1147,22 +1182,27 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             ElemIter it;
             iter_begin<MODE>(m, h, c.o, l, n, it);
             Elem outer;
-            iter_next<MODE>(m, h, c.o, l, it, outer);
             EC<MODE> ec_out{T(0), T(0), false};
-            double Ibdy;
-            if constexpr (MODE == MODE_SPLIT) {
-                // at the outer element's frequency nu shift = nu + nu (shift - 1), double-float
-                const F2 nu{c.fq, c.fql};
-                Ibdy = boundary_intensity_f2(m, outer.nr, f2_add(nu, f2_mul(nu, elem_dsh_f2(h, outer))));
-            } else {
-                Ibdy = boundary_intensity_m<MODE>(m, outer.nr, c.freq * outer.shift);
-            }
+            double Ibdy = 0.0;
             T dt_prev = T(0), S_carry = T(0);
-            bool first = true;
+            bool first = true, have_outer = false;
             while (true) {
+                // one iter_next site: the first element taken is the half's outer end
                 Elem inner;
                 const bool more = iter_next<MODE>(m, h, c.o, l, it, inner);
                 if (!more) inner = cen;
+                if (!have_outer) {
+                    outer = inner;
+                    have_outer = true;
+                    if constexpr (MODE == MODE_SPLIT) {
+                        // at the outer element's frequency nu shift = nu + nu (shift - 1), double-float
+                        const F2 nu{c.fq, c.fql};
+                        Ibdy = boundary_intensity_f2(m, outer.nr, f2_add(nu, f2_mul(nu, elem_dsh_f2(h, outer))));
+                    } else {
+                        Ibdy = boundary_intensity_m<MODE>(m, outer.nr, c.freq * outer.shift);
+                    }
+                    continue;
+                }
                 EC<MODE> ec_inn{T(0), T(0), false};
                 EC<MODE>& eci = more ? ec_inn : ec_cen;
                 PairOut<MODE> po;
@@ -1298,8 +1338,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             res.v = -(coeffmin * u_min + coeffplus * u_plus + coeffzero * res.u);
         }
     } else if (bot.rows) {  // origin is the first element
-        const double Ibdy = (MODE == MODE_SPLIT) ? boundary_intensity_f2(m, c.o, F2{c.fq, c.fql})
-                                                 : boundary_intensity_m<MODE>(m, c.o, c.freq);
+        const double Ibdy = Io;
         const double inverse_dtau_f = drcp<MODE>(bot.dt);
         const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
         const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
@@ -1314,8 +1353,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
         res.Ldiag = drcp<MODE>(Cf) * D;
         if constexpr (UV) res.v = Ibdy - res.u;  // Sv[first] = I_bdy_f - Su[first]
     } else {  // origin is the last element
-        const double Ibdy = (MODE == MODE_SPLIT) ? boundary_intensity_f2(m, c.o, F2{c.fq, c.fql})
-                                                 : boundary_intensity_m<MODE>(m, c.o, c.freq);
+        const double Ibdy = Io;
         const double inverse_dtau_l = drcp<MODE>(top.dt);
         const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
         const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
