@@ -495,7 +495,7 @@ def run_adjoint(args):
     # finite-difference check on random interior points
     interior = np.setdiff1d(np.arange(raw.npoints), raw.boundary2point)
     pts = rng.choice(interior, size=min(args.adjoint_fd_points, len(interior)), replace=False)
-    errs, flips, t_fd = [], 0, time.perf_counter()
+    errs, flips, worst, t_fd = [], 0, [], time.perf_counter()
     for p in pts:
         dirv = [torch.zeros_like(t) for t in (v0, T0, vt0, ab0)]
         u = rng.normal(size=6)
@@ -520,6 +520,7 @@ def run_adjoint(args):
             flips += 1
         elif fd != 0.0:
             errs.append(abs(an - fd) / abs(fd))
+            worst.append((errs[-1], int(p), an, fd, c1))
     fd_s = time.perf_counter() - t_fd
     solves = float(npx * npx * 41 * len(dirs))
     return {"workload": f"nlte_sphere {raw.npoints} points (LTE), {npx}x{npx} pixels x 41 frequencies "

@@ -184,6 +184,35 @@ int mgr_formal_solve_fo2_uv(MgrModel* model, int precision, double* u, double* v
 int mgr_formal_solve_fo2_anis(MgrModel* model, int precision, double* J, double* J2_0, double* J2_1_Re,
                               double* J2_1_Im, double* J2_2_Re, double* J2_2_Im);
 
+/* Parameters::n_off_diag (src/model/parameters/parameters.hpp:66): the number of band
+ * elements on each side of the origin that the formal solve adds to the ALO
+ * (0, the default: the diagonal only; at most 4).  With n_off_diag > 0 the formal
+ * solves of mgr_compute_level_populations run the banded FP64 solve and the global
+ * rate system (below).  Replaces the reference's parameters->n_off_diag, read by
+ * Solver::setup (src/solver/solver.tpp:6-36). */
+int mgr_model_set_n_off_diag(MgrModel* model, uint32_t n_off_diag);
+
+/* The formal solve with the non-local ALO (n_off_diag > 0, FP64): J_dev [P][F], the ALO
+ * diagonal lambda_diag_dev [P][L] as mgr_formal_solve_fo2_device writes it, and the
+ * band elements alo_off_dev / alo_nr_dev [P][L][hnrays][2 n_off_diag]: for origin p,
+ * line l and ray pair rr, slot m < n_off_diag the update_Lambda term (summed over the
+ * line's quadrature points) of the element centre - m - 1 of the ray and slot
+ * n_off_diag + m that of centre + m + 1, with the element's point (a slot whose element
+ * lies beyond the ray's end holds 0 and point 0).  The reference keeps these in
+ * Lambda lists per (p, k) merged by point (Lambda::add_element,
+ * src/model/lines/lineProducingSpecies/lambda/lambda.tpp:74-86), filled by
+ * Solver::update_Lambda (src/solver/solver.tpp:1760-1850) from the banded inverse of
+ * solve_feautrier_order_2 (solver.tpp:2319-2355).  Device pointers, model's stream. */
+int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* lambda_diag_dev, double* alo_off_dev,
+                                    uint32_t* alo_nr_dev);
+
+/* Host-buffer form of mgr_formal_solve_fo2_alo_device: J [P][F]; lambda_diag [P][L],
+ * alo_off and alo_nr (same layouts) may be NULL.  The band elements stay on the device
+ * (model scratch) for a following mgr_compute_jeff, as the reference's Lambda lists
+ * do for compute_Jeff.  Replaces Model::compute_radiation_field_feautrier_order_2
+ * (src/model/model.cpp:353-390) with parameters->n_off_diag > 0. */
+int mgr_formal_solve_fo2_alo(MgrModel* model, double* J, double* lambda_diag, double* alo_off, uint32_t* alo_nr);
+
 /* Partial formal solve over the ray pairs [rr_begin, rr_end) only: J_dev [P][F] and
  * lambda_diag_dev [P][L] (may be NULL) receive the sums over those ray pairs, so that
  * the sum over disjoint ranges covering [0, hnrays) is the full solve's J and ALO
@@ -468,7 +497,8 @@ int mgr_model_set_species(MgrModel* model, uint32_t nlspecs, const MgrSpeciesDes
                           const double* abundance, const double* const* populations);
 
 /* Model::compute_Jeff (model.cpp:514-545) from the J and ALO of the last formal solve
- * on this model (its buffers must still be valid for the device entry points).
+ * on this model (its buffers must still be valid for the device entry points), with
+ * the band elements when that solve was a banded one (mgr_formal_solve_fo2_alo*).
  * Outputs of species l, [P][nrad] each; any may be NULL.  Blocks. */
 int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, double* Jdif);
 
@@ -478,7 +508,14 @@ int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, do
  * number of normal iterations; error_mean / error_max (may be NULL, room for
  * err_capacity values) receive relative_change_mean / _max per normal iteration and
  * species, as Model::error_mean / error_max.  Populations stay on the device
- * (mgr_get_populations); the line emissivities and opacities are updated. */
+ * (mgr_get_populations); the line emissivities and opacities are updated.
+ * With n_off_diag > 0 (mgr_model_set_n_off_diag) every iteration runs the banded FP64
+ * formal solve (precision must be MGR_PRECISION_FP64; no ray-pair shard), Jeff with the
+ * band elements, and the global rate system of each species
+ * (lineProducingSpecies.tpp:377-581, the reference's Eigen SparseLU): here
+ * BiCGSTAB preconditioned by the per-point blocks' LU factors, on unknowns scaled by
+ * each point's population_tot, to a max-norm residual of 1e-13 of the right-hand
+ * side (MGR_ERR_NONFINITE above 1e-9 after 200 iterations). */
 int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, long max_iterations,
                                   const MgrAliParams* params, int* iterations, double* error_mean,
                                   double* error_max, uint32_t err_capacity);
@@ -486,7 +523,9 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
 /* Model::compute_level_populations_sparse (model.cpp:756-850): the same ALI loop with
  * the memory-lean formal solve and compute_Jeff_sparse (model.cpp:549-570; Jlin taken
  * from the solve, Jdif left unchanged) and the per-point rate solve of
- * update_using_statistical_equilibrium_sparse (lineProducingSpecies.tpp:589-705). */
+ * update_using_statistical_equilibrium_sparse (lineProducingSpecies.tpp:589-705).
+ * MGR_ERR_UNSUPPORTED with n_off_diag > 0, as the reference throws
+ * (lineProducingSpecies.tpp:592-593). */
 int mgr_compute_level_populations_sparse(MgrModel* model, int precision, int use_ng, long max_iterations,
                                          const MgrAliParams* params, int* iterations, double* error_mean,
                                          double* error_max, uint32_t err_capacity);

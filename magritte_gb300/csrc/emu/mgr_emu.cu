@@ -870,3 +870,47 @@ extern "C" int mgr_emu_fo2_adjoint(const MgrModelDesc* d, const double* gJ, doub
     if (rc == MGR_OK && fail) rc = MGR_ERR_CAPACITY;
     return rc;
 }
+
+// The band elements of the non-local ALO (fo2_alo_kernel's layout): alo_off / alo_nr
+// [P][L][hnrays][2 n_off_diag], summed over each line's quadrature points in order.
+extern "C" int mgr_emu_fo2_alo(const MgrModelDesc* d, uint32_t n_off_diag, double* alo_off, uint32_t* alo_nr) {
+    if (n_off_diag == 0 || n_off_diag > kMaxOffDiag) return MGR_ERR_ARGUMENT;
+    EmuModel x;
+    build_emu_model(d, x);
+    DevModel& m = x.m;
+    m.n_off_diag = n_off_diag;
+    const uint32_t K = n_off_diag;
+    const size_t n = (size_t)m.P * m.L * m.hnrays * 2 * K;
+    std::fill(alo_off, alo_off + n, 0.0);
+    const size_t per_o = (size_t)m.L * m.hnrays * 2 * K;
+    for (size_t t = 0; t < n; t++) alo_nr[t] = (uint32_t)(t / per_o);  // absent elements: the origin itself
+    return for_each_ray_pair(m, [&](uint32_t o, uint32_t rr, const HalfSmem& bk, int nb, const HalfSmem& fw, int nf) {
+        for (uint32_t f = 0; f < m.F; f++) {
+            const LaneCtx c = lane_ctx(m, o, f);
+            BandOut<kMaxOffDiag> bo;
+            bo.K = K;
+            bo.w_rr = ray_w(m, o, rr);
+            LaneResult r;
+            switch (m.approx) {
+                case APPROX_ONELINE:
+                    r = solve_lane<MODE_FP64, APPROX_ONELINE, false, kMaxOffDiag>(m, m.sorted_line, c, bk, nb, fw, nf,
+                                                                                  &bo);
+                    break;
+                case APPROX_CLOSELINES:
+                    r = solve_lane<MODE_FP64, APPROX_CLOSELINES, false, kMaxOffDiag>(m, m.sorted_line, c, bk, nb, fw,
+                                                                                     nf, &bo);
+                    break;
+                default:
+                    r = solve_lane<MODE_FP64, APPROX_NONE, false, kMaxOffDiag>(m, m.sorted_line, c, bk, nb, fw, nf,
+                                                                               &bo);
+            }
+            if (!r.solved || !m.in_line[f]) continue;
+            const uint32_t lid = m.corr_line[f];
+            for (uint32_t s = 0; s < 2 * K; s++) {
+                const size_t a = (((size_t)o * m.L + lid) * m.hnrays + rr) * 2 * K + s;
+                alo_off[a] += bo.val[s];
+                alo_nr[a] = bo.nr[s];
+            }
+        }
+    });
+}

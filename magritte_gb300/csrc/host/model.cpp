@@ -378,17 +378,20 @@ int Model::compute_LTE_level_populations() {
 // Model::set_dshift_max (model.cpp:1158-1178)
 int Model::set_dshift_max() {
     const Size P = parameters.npoints_.v;
-    dshift_max.resize({P});
+    std::vector<double> d(P);
     const auto& T = thermodynamics.temperature.gas;
     const auto& vt2 = thermodynamics.turbulence.vturb2;
     for (Size o = 0; o < P; o++) {
-        dshift_max[o] = std::numeric_limits<Real>::max();
+        d[o] = std::numeric_limits<Real>::max();
         for (const auto& ls : lines.lineProducingSpecies) {
             const double nd = parameters.max_width_fraction *
                               std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * ls.linedata.inverse_mass * T[o] + vt2[o]);
-            if (dshift_max[o] > nd) dshift_max[o] = nd;
+            if (d[o] > nd) d[o] = nd;
         }
     }
+    // unchanged values keep the array's version, so the resident device model is reused
+    if (dshift_max.size() != P || std::memcmp(dshift_max.data(), d.data(), sizeof(double) * P) != 0)
+        dshift_max.assign({P}, d.data());
     return 0;
 }
 
@@ -532,10 +535,10 @@ MgrModel* Model::upload() {
     prepare();
     if (radiation.frequencies.nu.size() == 0)
         throw std::runtime_error("compute_spectral_discretisation must be called before the formal solve");
-    if (parameters.n_off_diag != 0)
-        throw std::runtime_error("n_off_diag > 0 (non-local ALO) is not supported by the GPU formal solve");
     set_dshift_max();
-    return device_model();
+    MgrModel* dev = device_model();
+    check(mgr_model_set_n_off_diag(dev, (uint32_t)parameters.n_off_diag));
+    return dev;
 }
 
 int Model::compute_radiation_field_feautrier_order_2() {
@@ -545,8 +548,16 @@ int Model::compute_radiation_field_feautrier_order_2() {
     radiation.J.resize({P, F});
     if (parameters.store_u) radiation.u.resize({R, P, F});
     std::vector<double> lam((size_t)P * L);
-    check(mgr_formal_solve_fo2(dev, parameters.precision, radiation.J.data(),
-                               parameters.store_u ? radiation.u.data() : nullptr, lam.data()));
+    if (parameters.n_off_diag > 0) {
+        // the banded solve (FP64): J, the diagonal, and the band elements kept on the
+        // device for compute_Jeff (solver.tpp:2319-2355, :1760-1850)
+        if (parameters.store_u)
+            throw std::runtime_error("store_u with n_off_diag > 0: the banded solve does not return u");
+        check(mgr_formal_solve_fo2_alo(dev, radiation.J.data(), lam.data(), nullptr, nullptr));
+    } else {
+        check(mgr_formal_solve_fo2(dev, parameters.precision, radiation.J.data(),
+                                   parameters.store_u ? radiation.u.data() : nullptr, lam.data()));
+    }
     store_lambda(lam);
     return 0;
 }

@@ -183,6 +183,8 @@ void mgr_model_free(MgrModel* model) {
     if (model->work) cudaFree(model->work);
     if (model->adj_scratch) cudaFree(model->adj_scratch);
     if (model->v_scratch) cudaFree(model->v_scratch);
+    if (model->alo_scratch) cudaFree(model->alo_scratch);
+    if (model->alo_nr_scratch) cudaFree(model->alo_nr_scratch);
     ali_free(model);
     if (model->stream) cudaStreamDestroy(model->stream);
     delete model;
@@ -555,7 +557,82 @@ int mgr_formal_solve_fo2_device(MgrModel* model, int precision, double* J_dev, d
     if (e != cudaSuccess) return cuda_fail(e, "formal solve launch");
     model->last_J = J_dev;
     model->last_lam = lambda_diag_dev;
+    model->last_alo_off = nullptr;
+    model->last_alo_nr = nullptr;
     return MGR_OK;
+}
+
+int mgr_model_set_n_off_diag(MgrModel* model, uint32_t n_off_diag) {
+    MGR_MODEL_DEVICE(model);
+    if (!model) {
+        set_error("mgr_model_set_n_off_diag: null model");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (n_off_diag > kMaxOffDiag) {
+        set_error("mgr_model_set_n_off_diag: n_off_diag = " + std::to_string(n_off_diag) + " above the supported " +
+                  std::to_string(kMaxOffDiag));
+        return MGR_ERR_UNSUPPORTED;
+    }
+    model->dm.n_off_diag = n_off_diag;
+    if (model->ali) ali_shard_changed(model);  // drop a captured ALI iteration
+    return MGR_OK;
+}
+
+int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* lambda_diag_dev, double* alo_off_dev,
+                                    uint32_t* alo_nr_dev) {
+    MGR_MODEL_DEVICE(model);
+    if (!model || !J_dev || !lambda_diag_dev || !alo_off_dev || !alo_nr_dev) {
+        set_error("mgr_formal_solve_fo2_alo_device: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (model->dm.n_off_diag == 0) {
+        set_error("mgr_formal_solve_fo2_alo_device: n_off_diag is 0 (mgr_model_set_n_off_diag)");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!model->line_disc) {
+        set_error("mgr_formal_solve_fo2_alo_device: the formal solve needs a line spectral discretisation");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    const size_t wb = fo2_work_bytes(model, model->dm.P, true, true);
+    int rc = ensure_scratch(model, &model->work, &model->work_bytes, wb);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = launch_fo2_range(model, MGR_PRECISION_FP64, 0, model->dm.P, J_dev, nullptr, lambda_diag_dev,
+                                     model->work, model->work_bytes, 0, 0xffffffffu, nullptr, nullptr, nullptr,
+                                     alo_off_dev, alo_nr_dev);
+    if (e != cudaSuccess) return cuda_fail(e, "banded formal solve launch");
+    model->last_J = J_dev;
+    model->last_lam = lambda_diag_dev;
+    model->last_alo_off = alo_off_dev;
+    model->last_alo_nr = alo_nr_dev;
+    return MGR_OK;
+}
+
+int mgr_formal_solve_fo2_alo(MgrModel* model, double* J, double* lambda_diag, double* alo_off, uint32_t* alo_nr) {
+    MGR_MODEL_DEVICE(model);
+    if (!model || !J) {
+        set_error("mgr_formal_solve_fo2_alo: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    const DevModel& dm = model->dm;
+    const size_t PF = (size_t)dm.P * dm.F, PL = (size_t)dm.P * dm.L;
+    const size_t nalo = PL * dm.hnrays * 2 * (dm.n_off_diag ? dm.n_off_diag : 1);
+    int rc = ensure_scratch(model, &model->J_scratch, &model->J_scratch_bytes, PF * 8);
+    if (rc == MGR_OK) rc = ensure_scratch(model, &model->lam_scratch, &model->lam_scratch_bytes, PL * 8);
+    if (rc == MGR_OK) rc = ensure_scratch(model, &model->alo_scratch, &model->alo_scratch_bytes, nalo * 8);
+    if (rc == MGR_OK) rc = ensure_scratch(model, &model->alo_nr_scratch, &model->alo_nr_scratch_bytes, nalo * 4);
+    if (rc != MGR_OK) return rc;
+    uint32_t* nr_dev = reinterpret_cast<uint32_t*>(model->alo_nr_scratch);
+    rc = mgr_formal_solve_fo2_alo_device(model, model->J_scratch, model->lam_scratch, model->alo_scratch, nr_dev);
+    if (rc != MGR_OK) return rc;
+    cudaError_t e = cudaMemcpyAsync(J, model->J_scratch, PF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && lambda_diag)
+        e = cudaMemcpyAsync(lambda_diag, model->lam_scratch, PL * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && alo_off)
+        e = cudaMemcpyAsync(alo_off, model->alo_scratch, nalo * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && alo_nr)
+        e = cudaMemcpyAsync(alo_nr, nr_dev, nalo * 4, cudaMemcpyDeviceToHost, model->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "result copy");
+    return read_status(model);
 }
 
 int mgr_formal_solve_fo2_rays_device(MgrModel* model, int precision, uint32_t rr_begin, uint32_t rr_end,
@@ -660,6 +737,8 @@ int mgr_formal_solve_fo2_sparse_device(MgrModel* model, int precision, double* J
     model->last_J = nullptr;
     model->last_Jlin = Jlin_dev;
     model->last_lam = lambda_diag_dev;
+    model->last_alo_off = nullptr;
+    model->last_alo_nr = nullptr;
     return MGR_OK;
 }
 

@@ -31,8 +31,11 @@ constexpr double HH_OVER_FOUR_PI = HH / (4.0 * 3.14159265358979323846);  // cons
 // ---------------------------------------------------------------------------------
 // With Jlin_in (the memory-lean solve's line-integrated J, [P][L]): compute_Jeff_sparse
 // (model.cpp:549-570), Jlin taken as it is and Jdif left unchanged.
+// alo_off / alo_nr (n_off_diag > 0): the band elements of the non-local ALO, whose
+// terms Ls * population(nr, upper) join the diagonal's in diff.
 __global__ void jeff_kernel(DevModel m, SpeciesView s, const double* __restrict__ J, const double* __restrict__ lam,
-                            const double* __restrict__ Jlin_in) {
+                            const double* __restrict__ Jlin_in, const double* __restrict__ alo_off,
+                            const uint32_t* __restrict__ alo_nr) {
     const size_t n = (size_t)m.P * s.nrad;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
         const uint32_t p = (uint32_t)(t / s.nrad), k = (uint32_t)(t % s.nrad);
@@ -46,7 +49,15 @@ __global__ void jeff_kernel(DevModel m, SpeciesView s, const double* __restrict_
                 jl = __dadd_rn(jl, __dmul_rn(m.quad_w[(size_t)m.corr_lspec[f] * m.Q + z], J[(size_t)p * m.F + f]));
             }
         }
-        const double diff = __dmul_rn(lam[(size_t)p * m.L + lid], s.pop[(size_t)p * s.nlev + s.irad[k]]);
+        double diff = __dmul_rn(lam[(size_t)p * m.L + lid], s.pop[(size_t)p * s.nlev + s.irad[k]]);
+        if (alo_off) {
+            const size_t nb = (size_t)m.hnrays * 2 * m.n_off_diag;
+            const size_t b0 = ((size_t)p * m.L + lid) * nb;
+            for (size_t e = 0; e < nb; e++) {
+                const double v = alo_off[b0 + e];
+                if (v != 0.0) diff = __dadd_rn(diff, __dmul_rn(v, s.pop[(size_t)alo_nr[b0 + e] * s.nlev + s.irad[k]]));
+            }
+        }
         s.Jlin[t] = jl;
         s.Jeff[t] = __dsub_rn(jl, __dmul_rn(HH_OVER_FOUR_PI, diff));
         if (!Jlin_in) s.Jdif[t] = __dmul_rn(HH_OVER_FOUR_PI, diff);
@@ -265,6 +276,335 @@ __global__ void stateq_kernel(DevModel m, SpeciesView s, const double* __restric
         __syncwarp();
         for (uint32_t i = lane; i < n; i += 32) pop_out[(size_t)p * n + i] = y[i];
         __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// The global rate system with the non-local ALO (n_off_diag > 0;
+// lineProducingSpecies.tpp:377-581 with the band elements of Lambda, :440-462): the
+// element (nr, Ls) of point p's list for line k adds
+//     v = -Ls opacity(p, k) / frequency(k)
+// at row (p, lower k), column (nr, upper k) and -v at row (nr, upper k), column
+// (nr, upper k) (rows of the last level are the normalisation).  Elements with nr = p
+// stay inside p's block; the others couple blocks.  Unknowns are scaled by
+// population_tot (xi = population / tot), and with B the block diagonal and E the
+// coupling, the preconditioned system
+//     xi + S^-1 B^-1 E S xi = S^-1 B^-1 b
+// is solved by BiCGSTAB.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double tot_scale(const SpeciesView& s, uint32_t p) {
+    const double t = s.tot[p];
+    return t > 0.0 ? t : 1.0;
+}
+
+// v of every band element of the species (thread per element): coef[(p nrad + k) nb + e].
+__global__ void band_coef_kernel(DevModel m, SpeciesView s, const double* __restrict__ alo_off,
+                                 double min_line_opacity, double* __restrict__ coef) {
+    const size_t nb = (size_t)m.hnrays * 2 * m.n_off_diag;
+    const size_t n = (size_t)m.P * s.nrad * nb;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t pk = t / nb, e = t % nb;
+        const uint32_t p = (uint32_t)(pk / s.nrad), k = (uint32_t)(pk % s.nrad);
+        const double Ls = alo_off[((size_t)p * m.L + s.line_offset + k) * nb + e];
+        coef[t] = (Ls == 0.0) ? 0.0
+                              : -__ddiv_rn(__dmul_rn(Ls, opacity_of(s, s.pop + (size_t)p * s.nlev, k, min_line_opacity)),
+                                           s.freq[k]);
+    }
+}
+
+// Warp per point: the block (rate_block, the point's own band elements, the -v of
+// other points' elements emitted by this point, gathered through the CSR), its LU
+// factorisation with partial pivoting, and S^-1 B^-1 b as the right-hand side and the
+// first iterate.  Shared memory per warp: stateq_warp_doubles.
+__global__ void global_block_kernel(DevModel m, SpeciesView s, const double* __restrict__ lam,
+                                    const double* __restrict__ abundance, uint32_t nspecs, double min_line_opacity,
+                                    const double* __restrict__ coef, const uint32_t* __restrict__ alo_nr,
+                                    const uint32_t* __restrict__ csr_off, const uint32_t* __restrict__ csr_ent,
+                                    double* __restrict__ lu, uint32_t* __restrict__ piv, double* __restrict__ rhs,
+                                    double* __restrict__ x, int* status) {
+    extern __shared__ __align__(16) double smem_ali[];
+    const uint32_t n = s.nlev, last = n - 1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double* M = smem_ali + (size_t)w * stateq_warp_doubles(s);
+    double* y = M + (size_t)n * n;
+    double* R = y + n;
+    const size_t nb = (size_t)m.hnrays * 2 * m.n_off_diag;
+    for (uint32_t p = blockIdx.x * nw + w; p < m.P; p += gridDim.x * nw) {
+        for (uint32_t i = lane; i < n * (n + 1); i += 32) M[i] = 0.0;
+        __syncwarp();
+        rate_block(m, s, p, lam, abundance, nspecs, min_line_opacity, M, R, lane);
+        __syncwarp();
+        if (lane == 0) {
+            // the point's own elements with nr = p (an interpolated element of its own rays)
+            for (uint32_t k = 0; k < s.nrad; k++) {
+                const uint32_t I = s.irad[k], J = s.jrad[k];
+                const size_t b0 = ((size_t)p * m.L + s.line_offset + k) * nb;
+                for (size_t e = 0; e < nb; e++) {
+                    const double v = coef[((size_t)p * s.nrad + k) * nb + e];
+                    if (v == 0.0 || alo_nr[b0 + e] != p) continue;
+                    if (J != last) M[(size_t)J * n + I] += v;
+                    if (I != last) M[(size_t)I * n + I] -= v;
+                }
+            }
+            // other points' elements emitted by p: -v on (p, upper)
+            for (uint32_t lv = 0; lv < last; lv++) {
+                const uint32_t row = p * n + lv;
+                for (uint32_t j = csr_off[row]; j < csr_off[row + 1]; j++) M[(size_t)lv * n + lv] -= coef[csr_ent[j]];
+            }
+            for (uint32_t i = 0; i < n; i++) y[i] = 0.0;
+            y[last] = s.tot[p];
+        }
+        __syncwarp();
+        bool singular = false;
+        uint32_t* pv = piv + (size_t)p * n;
+        for (uint32_t c = 0; c < n; c++) {
+            double best = -1.0;
+            uint32_t pr = c;
+            for (uint32_t r = c + lane; r < n; r += 32) {
+                const double v = fabs(M[(size_t)r * n + c]);
+                if (v > best) {
+                    best = v;
+                    pr = r;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const uint32_t op = __shfl_xor_sync(0xffffffffu, pr, off);
+                if (ob > best || (ob == best && op < pr)) {
+                    best = ob;
+                    pr = op;
+                }
+            }
+            if (!(best > 0.0)) {
+                singular = true;
+                break;
+            }
+            if (lane == 0) pv[c] = pr;
+            if (pr != c) {
+                for (uint32_t j = lane; j < n; j += 32) {
+                    const double t = M[(size_t)c * n + j];
+                    M[(size_t)c * n + j] = M[(size_t)pr * n + j];
+                    M[(size_t)pr * n + j] = t;
+                }
+                __syncwarp();
+            }
+            const double d = M[(size_t)c * n + c];
+            for (uint32_t r = c + 1; r < n; r++) {
+                const double f = M[(size_t)r * n + c] / d;
+                for (uint32_t j = c + 1 + lane; j < n; j += 32) M[(size_t)r * n + j] -= f * M[(size_t)c * n + j];
+                __syncwarp();
+                if (lane == 0) M[(size_t)r * n + c] = f;  // the multiplier, kept for the solves
+                __syncwarp();
+            }
+        }
+        if (singular) {
+            if (lane == 0) atomicOr(status, ST_NONFINITE);
+            continue;
+        }
+        for (uint32_t i = lane; i < n * n; i += 32) lu[(size_t)p * n * n + i] = M[i];
+        if (lane == 0) {
+            // B^-1 b with the factors just stored (b = tot e_last): the row interchanges in
+            // order (they moved whole rows, multipliers included), then L and U
+            for (uint32_t c = 0; c < n; c++) {
+                const uint32_t pr = pv[c];
+                if (pr != c) {
+                    const double t = y[c];
+                    y[c] = y[pr];
+                    y[pr] = t;
+                }
+            }
+            for (uint32_t c = 0; c < n; c++)
+                for (uint32_t r = c + 1; r < n; r++) y[r] -= M[(size_t)r * n + c] * y[c];
+            for (uint32_t c = n; c-- > 0;) {
+                double acc = y[c];
+                for (uint32_t j = c + 1; j < n; j++) acc -= M[(size_t)c * n + j] * y[j];
+                y[c] = acc / M[(size_t)c * n + c];
+            }
+            const double sc = tot_scale(s, p);
+            for (uint32_t i = 0; i < n; i++) {
+                rhs[(size_t)p * n + i] = y[i] / sc;
+                x[(size_t)p * n + i] = y[i] / sc;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// out = xi + S^-1 B^-1 E S xi, warp per point: lanes gather the coupling of the
+// point's elements with nr != p (rows of the lower levels) into per-lane partial rows,
+// summed in lane order; lane 0 applies the stored LU factors.  Shared memory per warp:
+// 33 nlev doubles.
+__global__ void global_op_kernel(DevModel m, SpeciesView s, const double* __restrict__ coef,
+                                 const uint32_t* __restrict__ alo_nr, const double* __restrict__ lu,
+                                 const uint32_t* __restrict__ piv, const double* __restrict__ xi,
+                                 double* __restrict__ out) {
+    extern __shared__ __align__(16) double smem_ali[];
+    const uint32_t n = s.nlev, last = n - 1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double* part = smem_ali + (size_t)w * 33 * n;  // [32][n] partial rows, then [n] the sum
+    double* c = part + (size_t)32 * n;
+    const size_t nb = (size_t)m.hnrays * 2 * m.n_off_diag;
+    const size_t ne = (size_t)s.nrad * nb;
+    for (uint32_t p = blockIdx.x * nw + w; p < m.P; p += gridDim.x * nw) {
+        for (uint32_t i = 0; i < n; i++) part[(size_t)lane * n + i] = 0.0;
+        for (size_t t = lane; t < ne; t += 32) {
+            const uint32_t k = (uint32_t)(t / nb);
+            const size_t e = t % nb;
+            const double v = coef[(size_t)p * ne + t];
+            const uint32_t nr = alo_nr[((size_t)p * m.L + s.line_offset + k) * nb + e];
+            if (v == 0.0 || nr == p || s.jrad[k] == last) continue;
+            part[(size_t)lane * n + s.jrad[k]] += v * (tot_scale(s, nr) * xi[(size_t)nr * n + s.irad[k]]);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            for (uint32_t i = 0; i < n; i++) {
+                double acc = 0.0;
+                for (int l = 0; l < 32; l++) acc += part[(size_t)l * n + i];
+                c[i] = acc;
+            }
+            const double* M = lu + (size_t)p * n * n;
+            const uint32_t* pv = piv + (size_t)p * n;
+            for (uint32_t cc = 0; cc < n; cc++) {
+                const uint32_t pr = pv[cc];
+                if (pr != cc) {
+                    const double t = c[cc];
+                    c[cc] = c[pr];
+                    c[pr] = t;
+                }
+            }
+            for (uint32_t cc = 0; cc < n; cc++)
+                for (uint32_t r = cc + 1; r < n; r++) c[r] -= M[(size_t)r * n + cc] * c[cc];
+            for (uint32_t cc = n; cc-- > 0;) {
+                double acc = c[cc];
+                for (uint32_t j = cc + 1; j < n; j++) acc -= M[(size_t)cc * n + j] * c[j];
+                c[cc] = acc / M[(size_t)cc * n + cc];
+            }
+            const double sc = tot_scale(s, p);
+            for (uint32_t i = 0; i < n; i++) out[(size_t)p * n + i] = xi[(size_t)p * n + i] + c[i] / sc;
+        }
+        __syncwarp();
+    }
+}
+
+// Partial sums of a.b (mode 0) or partial maxima of |a| (mode 1) over blocks; then
+// reduce_finalize sums / maximises them in block order.
+__global__ void dot_kernel(const double* __restrict__ a, const double* __restrict__ b, size_t n, int mode,
+                           double* __restrict__ partial) {
+    __shared__ double acc[256];
+    double v = 0.0;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        v = mode ? fmax(v, fabs(a[t])) : v + a[t] * b[t];
+    acc[threadIdx.x] = v;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            acc[threadIdx.x] = mode ? fmax(acc[threadIdx.x], acc[threadIdx.x + h]) : acc[threadIdx.x] + acc[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc[0];
+}
+
+__global__ void reduce_finalize(const double* __restrict__ partial, int nblocks, int mode, double* __restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double v = 0.0;
+    for (int b = 0; b < nblocks; b++) v = mode ? fmax(v, partial[b]) : v + partial[b];
+    *out = v;
+}
+
+// out = a + alpha b + beta c (any of b, c may be null).
+__global__ void axpby_kernel(double* __restrict__ out, const double* __restrict__ a, double alpha,
+                             const double* __restrict__ b, double beta, const double* __restrict__ c, size_t n) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        double v = a[t];
+        if (b) v += alpha * b[t];
+        if (c) v += beta * c[t];
+        out[t] = v;
+    }
+}
+
+// population = tot xi
+__global__ void unscale_kernel(SpeciesView s, uint32_t P, const double* __restrict__ xi) {
+    const size_t n = (size_t)P * s.nlev;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        s.pop[t] = xi[t] * tot_scale(s, (uint32_t)(t / s.nlev));
+}
+
+// CSR of the band elements by the row whose diagonal their -v reaches: (element point
+// nr, upper level), for nr != p and upper levels below the last.  Element index t is
+// the coef index ((p nrad + k) hnrays 2K + e).
+__device__ __forceinline__ bool csr_row_of(const DevModel& m, const SpeciesView& s, const uint32_t* alo_nr, size_t t,
+                                           size_t nb, size_t* row) {
+    const size_t pk = t / nb, e = t % nb;
+    const uint32_t p = (uint32_t)(pk / s.nrad), k = (uint32_t)(pk % s.nrad);
+    const uint32_t nr = alo_nr[((size_t)p * m.L + s.line_offset + k) * nb + e];
+    if (nr == p || s.irad[k] == s.nlev - 1) return false;
+    *row = (size_t)nr * s.nlev + s.irad[k];
+    return true;
+}
+
+__global__ void csr_count_kernel(DevModel m, SpeciesView s, const uint32_t* __restrict__ alo_nr,
+                                 uint32_t* __restrict__ cnt) {
+    const size_t nb = (size_t)m.hnrays * 2 * m.n_off_diag;
+    const size_t n = (size_t)m.P * s.nrad * nb;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        size_t row;
+        if (csr_row_of(m, s, alo_nr, t, nb, &row)) atomicAdd(&cnt[row], 1u);
+    }
+}
+
+// Exclusive scan of cnt [rows] into off [rows + 1], one block of 1024 threads (each a
+// contiguous range); off[rows] is the total.
+__global__ void csr_scan_kernel(const uint32_t* __restrict__ cnt, size_t rows, uint32_t* __restrict__ off) {
+    __shared__ unsigned long long part[1024];
+    const size_t per = (rows + blockDim.x - 1) / blockDim.x;
+    const size_t b = (size_t)threadIdx.x * per;
+    const size_t e = b + per < rows ? b + per : rows;
+    unsigned long long sum = 0;
+    for (size_t i = b; i < e; i++) sum += cnt[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long acc = 0;
+        for (unsigned i = 0; i < blockDim.x; i++) {
+            const unsigned long long v = part[i];
+            part[i] = acc;
+            acc += v;
+        }
+        off[rows] = (uint32_t)acc;
+    }
+    __syncthreads();
+    unsigned long long acc = part[threadIdx.x];
+    for (size_t i = b; i < e; i++) {
+        off[i] = (uint32_t)acc;
+        acc += cnt[i];
+    }
+}
+
+__global__ void csr_fill_kernel(DevModel m, SpeciesView s, const uint32_t* __restrict__ alo_nr,
+                                uint32_t* __restrict__ cursor, uint32_t* __restrict__ ent) {
+    const size_t nb = (size_t)m.hnrays * 2 * m.n_off_diag;
+    const size_t n = (size_t)m.P * s.nrad * nb;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        size_t row;
+        if (csr_row_of(m, s, alo_nr, t, nb, &row)) ent[atomicAdd(&cursor[row], 1u)] = (uint32_t)t;
+    }
+}
+
+// Thread per row: the row's entries in ascending element order, so that the sums over
+// them do not depend on the order of the atomic fill.
+__global__ void csr_sort_kernel(const uint32_t* __restrict__ off, size_t rows, uint32_t* __restrict__ ent) {
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t b = off[r], e = off[r + 1];
+        for (uint32_t i = b + 1; i < e; i++) {
+            const uint32_t v = ent[i];
+            uint32_t j = i;
+            while (j > b && ent[j - 1] > v) {
+                ent[j] = ent[j - 1];
+                j--;
+            }
+            ent[j] = v;
+        }
     }
 }
 
@@ -526,12 +866,14 @@ static unsigned grid_for(size_t n, int threads, int cap) {
     return (unsigned)(b ? b : 1);
 }
 
-cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam, const double* Jlin) {
+cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam, const double* Jlin,
+                            const double* alo_off, const uint32_t* alo_nr) {
+    const bool bands = alo_off && alo_nr && !Jlin && model->dm.n_off_diag > 0;
     for (auto& sp : model->ali->species) {
         const size_t n = (size_t)model->dm.P * sp.view.nrad;
         count_launch();
-        jeff_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, model->stream>>>(model->dm, sp.view, J, lam,
-                                                                                      Jlin);
+        jeff_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, model->stream>>>(
+            model->dm, sp.view, J, lam, Jlin, bands ? alo_off : nullptr, bands ? alo_nr : nullptr);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -729,6 +1071,8 @@ void AliSpecies::pop_back_history() {
 // ---------------------------------------------------------------------------------
 namespace mgr {
 
+static void grs_free(GlobalRate& g);
+
 void ali_free(MgrModel* model) {
     if (!model || !model->ali) return;
     AliState* st = model->ali;
@@ -737,6 +1081,7 @@ void ali_free(MgrModel* model) {
         if (ev) cudaEventDestroy(ev);
     for (void* p : st->pool_allocs) cudaFree(p);
     for (void* p : st->allocs) cudaFree(p);
+    grs_free(st->grs);
     if (st->stats_host) cudaFreeHost(st->stats_host);
     if (st->Jlin_buf) cudaFree(st->Jlin_buf);
     delete st;
@@ -804,7 +1149,9 @@ static int read_stats(MgrModel* model) {
 // the captured iteration.
 static void mark(MgrModel* model, int i) {
     AliState& st = *model->ali;
-    if (st.timing && cudaEventRecord(st.ev[i], model->stream) != cudaSuccess) {
+    // External: inside a stream capture a plain record only orders the graph's nodes;
+    // an external record node takes the timestamp on every replay
+    if (st.timing && cudaEventRecordWithFlags(st.ev[i], model->stream, cudaEventRecordExternal) != cudaSuccess) {
         (void)cudaGetLastError();
         st.timing = false;
     }
@@ -881,6 +1228,277 @@ static cudaError_t normal_iteration(MgrModel* model, int precision) {
         return cudaGraphLaunch(st.graph, model->stream);
     }
     return normal_iteration_launches(model, precision);
+}
+
+// ---------------------------------------------------------------------------------
+// The global rate system with the non-local ALO (n_off_diag > 0)
+// ---------------------------------------------------------------------------------
+template <typename T>
+static cudaError_t grs_alloc(GlobalRate& g, T** dst, size_t n) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, (n ? n : 1) * sizeof(T));
+    if (e == cudaSuccess) {
+        g.allocs.push_back(p);
+        *dst = static_cast<T*>(p);
+    }
+    return e;
+}
+
+static void grs_free(GlobalRate& g) {
+    for (void* p : g.allocs) cudaFree(p);
+    if (g.red_host) cudaFreeHost(g.red_host);
+    g = GlobalRate();
+}
+
+static size_t band_slots(const DevModel& m) { return (size_t)m.hnrays * 2 * m.n_off_diag; }
+
+// Device state of the global solve and of the band elements, sized for the model.
+static cudaError_t ensure_global(MgrModel* model) {
+    AliState& st = *model->ali;
+    GlobalRate& g = st.grs;
+    const DevModel& m = model->dm;
+    const size_t nb = band_slots(m);
+    const size_t alo = (size_t)m.P * m.L * nb;
+    cudaError_t e = cudaSuccess;
+    auto grow = [](double** p, size_t* have, size_t bytes) -> cudaError_t {
+        if (*have >= bytes) return cudaSuccess;
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        *have = 0;
+        const cudaError_t r = cudaMalloc(p, bytes);
+        if (r == cudaSuccess) *have = bytes;
+        return r;
+    };
+    if ((e = grow(&model->alo_scratch, &model->alo_scratch_bytes, alo * 8)) != cudaSuccess) return e;
+    if ((e = grow(&model->alo_nr_scratch, &model->alo_nr_scratch_bytes, alo * 4)) != cudaSuccess) return e;
+    st.alo_off = model->alo_scratch;
+    st.alo_nr = reinterpret_cast<uint32_t*>(model->alo_nr_scratch);
+    uint32_t nmax = 0, rmax = 0;
+    for (auto& sp : st.species) {
+        nmax = std::max(nmax, sp.view.nlev);
+        rmax = std::max(rmax, sp.view.nrad);
+    }
+    const size_t n = (size_t)m.P * nmax, ncoef = (size_t)m.P * rmax * nb;
+    if (g.cap_n >= n && g.cap_coef >= ncoef && g.csr_off.size() == st.species.size()) return cudaSuccess;
+    grs_free(g);
+    if ((e = grs_alloc(g, &g.lu, (size_t)m.P * nmax * nmax)) != cudaSuccess) return e;
+    if ((e = grs_alloc(g, &g.piv, n)) != cudaSuccess) return e;
+    if ((e = grs_alloc(g, &g.coef, ncoef)) != cudaSuccess) return e;
+    if ((e = grs_alloc(g, &g.vec, 9 * n)) != cudaSuccess) return e;
+    if ((e = grs_alloc(g, &g.red, (size_t)kConvBlocks + 8)) != cudaSuccess) return e;
+    if ((e = grs_alloc(g, &g.cursor, n + 1)) != cudaSuccess) return e;
+    if ((e = cudaMallocHost(&g.red_host, 8 * sizeof(double))) != cudaSuccess) return e;
+    g.csr_off.assign(st.species.size(), nullptr);
+    g.csr_ent.assign(st.species.size(), nullptr);
+    g.csr_cap.assign(st.species.size(), 0);
+    for (size_t l = 0; l < st.species.size(); l++)
+        if ((e = grs_alloc(g, &g.csr_off[l], (size_t)m.P * st.species[l].view.nlev + 1)) != cudaSuccess) return e;
+    g.cap_n = n;
+    g.cap_coef = ncoef;
+    g.built = false;
+    return cudaSuccess;
+}
+
+// The CSR of every species from the band elements' points of the latest banded solve.
+static cudaError_t build_csr(MgrModel* model) {
+    AliState& st = *model->ali;
+    GlobalRate& g = st.grs;
+    const DevModel& m = model->dm;
+    cudaStream_t s = model->stream;
+    for (size_t l = 0; l < st.species.size(); l++) {
+        const SpeciesView& v = st.species[l].view;
+        const size_t rows = (size_t)m.P * v.nlev;
+        const size_t n = (size_t)m.P * v.nrad * band_slots(m);
+        cudaError_t e = cudaMemsetAsync(g.cursor, 0, (rows + 1) * 4, s);
+        if (e != cudaSuccess) return e;
+        count_launch();
+        csr_count_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, s>>>(m, v, st.alo_nr, g.cursor);
+        count_launch();
+        csr_scan_kernel<<<1, 1024, 0, s>>>(g.cursor, rows, g.csr_off[l]);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        uint32_t total = 0;
+        if ((e = cudaMemcpyAsync(&total, g.csr_off[l] + rows, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        if (g.csr_cap[l] < total) {
+            if ((e = grs_alloc(g, &g.csr_ent[l], total)) != cudaSuccess) return e;
+            g.csr_cap[l] = total;
+        }
+        if ((e = cudaMemcpyAsync(g.cursor, g.csr_off[l], rows * 4, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+            return e;
+        count_launch();
+        csr_fill_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, s>>>(m, v, st.alo_nr, g.cursor,
+                                                                              g.csr_ent[l]);
+        count_launch();
+        csr_sort_kernel<<<grid_for(rows, 128, model->sm_count * 8), 128, 0, s>>>(g.csr_off[l], rows, g.csr_ent[l]);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    g.built = true;
+    return cudaSuccess;
+}
+
+// Dot product (mode 0) or max-norm (mode 1, b unused) into result slot `slot`.
+static cudaError_t grs_reduce(MgrModel* model, const double* a, const double* b, size_t n, int mode, int slot) {
+    GlobalRate& g = model->ali->grs;
+    const int blocks = (int)grid_for(n, 256, kConvBlocks);
+    count_launch();
+    dot_kernel<<<blocks, 256, 0, model->stream>>>(a, b ? b : a, n, mode, g.red);
+    count_launch();
+    reduce_finalize<<<1, 32, 0, model->stream>>>(g.red, blocks, mode, g.red + kConvBlocks + slot);
+    return cudaGetLastError();
+}
+
+static cudaError_t grs_read(MgrModel* model, int nslots) {
+    GlobalRate& g = model->ali->grs;
+    cudaError_t e = cudaMemcpyAsync(g.red_host, g.red + kConvBlocks, nslots * sizeof(double),
+                                    cudaMemcpyDeviceToHost, model->stream);
+    return e == cudaSuccess ? cudaStreamSynchronize(model->stream) : e;
+}
+
+static cudaError_t grs_axpby(MgrModel* model, double* out, const double* a, double alpha, const double* b,
+                             double beta, const double* c, size_t n) {
+    count_launch();
+    axpby_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, model->stream>>>(out, a, alpha, b, beta, c, n);
+    return cudaGetLastError();
+}
+
+static cudaError_t grs_op(MgrModel* model, const SpeciesView& v, const double* xi, double* out) {
+    GlobalRate& g = model->ali->grs;
+    const int wpb = 4;
+    const size_t smem = (size_t)wpb * 33 * v.nlev * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(global_op_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    global_op_kernel<<<grid_for(model->dm.P, wpb, model->sm_count * 8), wpb * 32, smem, model->stream>>>(
+        model->dm, v, g.coef, model->ali->alo_nr, g.lu, g.piv, xi, out);
+    return cudaGetLastError();
+}
+
+constexpr double kRateTol = 1.0e-13;   // BiCGSTAB: max-norm residual relative to the right-hand side
+constexpr double kRateAccept = 1.0e-9;  // larger final residuals fail the solve
+constexpr int kRateMaxIt = 200;
+
+// The rate system of species l with the band elements of the latest banded solve:
+// populations(new) = tot xi, xi from BiCGSTAB on xi + S^-1 B^-1 E S xi = S^-1 B^-1 b
+// started at the block-Jacobi solution.
+static int global_stateq(MgrModel* model, size_t l) {
+    AliState& st = *model->ali;
+    GlobalRate& g = st.grs;
+    AliSpecies& sp = st.species[l];
+    const SpeciesView& v = sp.view;
+    const DevModel& m = model->dm;
+    cudaStream_t s = model->stream;
+    const size_t n = (size_t)m.P * v.nlev;
+    const size_t ncoef = (size_t)m.P * v.nrad * band_slots(m);
+    double *x = g.vec, *r = x + n, *rh = r + n, *pp = rh + n, *vv = pp + n, *ss = vv + n, *tt = ss + n,
+           *rhs = tt + n;
+    count_launch();
+    band_coef_kernel<<<grid_for(ncoef, 256, model->sm_count * 16), 256, 0, s>>>(m, v, st.alo_off,
+                                                                               st.prm.min_line_opacity, g.coef);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "band coefficients");
+    const int wpb = 4;
+    const size_t smem = (size_t)wpb * stateq_warp_doubles(v) * sizeof(double);
+    if ((e = cudaFuncSetAttribute(global_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return cuda_fail(e, "rate blocks");
+    count_launch();
+    global_block_kernel<<<grid_for(m.P, wpb, model->sm_count * 8), wpb * 32, smem, s>>>(
+        m, v, model->lam_scratch, st.abundance, st.nspecs, st.prm.min_line_opacity, g.coef, st.alo_nr,
+        g.csr_off[l], g.csr_ent[l], g.lu, g.piv, rhs, x, model->status);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "rate blocks");
+    // r = rhs - A x, rhat = r
+    if ((e = grs_op(model, v, x, tt)) != cudaSuccess) return cuda_fail(e, "rate operator");
+    if ((e = grs_axpby(model, r, rhs, -1.0, tt, 0.0, nullptr, n)) != cudaSuccess) return cuda_fail(e, "BiCGSTAB");
+    if ((e = cudaMemcpyAsync(rh, r, n * 8, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return cuda_fail(e, "BiCGSTAB");
+    if ((e = grs_reduce(model, rhs, nullptr, n, 1, 0)) != cudaSuccess) return cuda_fail(e, "BiCGSTAB");
+    if ((e = grs_read(model, 1)) != cudaSuccess) return cuda_fail(e, "BiCGSTAB");
+    const double bn = g.red_host[0] > 0.0 ? g.red_host[0] : 1.0;
+    double rho = 1.0, alpha = 1.0, omega = 1.0, rn = 0.0;
+    bool first = true;
+    int it = 0;
+    for (;; it++) {
+        if ((e = grs_reduce(model, r, nullptr, n, 1, 0)) != cudaSuccess) break;
+        if ((e = grs_reduce(model, rh, r, n, 0, 1)) != cudaSuccess) break;
+        if ((e = grs_read(model, 2)) != cudaSuccess) break;
+        rn = g.red_host[0] / bn;
+        const double rho_new = g.red_host[1];
+        if (!(rn > kRateTol) || it >= kRateMaxIt || rho_new == 0.0) break;
+        // p = r + beta (p - omega v)
+        if (first) {
+            if ((e = cudaMemcpyAsync(pp, r, n * 8, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) break;
+            first = false;
+        } else {
+            const double beta = (rho_new / rho) * (alpha / omega);
+            if ((e = grs_axpby(model, pp, r, beta, pp, -beta * omega, vv, n)) != cudaSuccess) break;
+        }
+        rho = rho_new;
+        if ((e = grs_op(model, v, pp, vv)) != cudaSuccess) break;
+        if ((e = grs_reduce(model, rh, vv, n, 0, 0)) != cudaSuccess) break;
+        if ((e = grs_read(model, 1)) != cudaSuccess) break;
+        if (g.red_host[0] == 0.0) break;
+        alpha = rho / g.red_host[0];
+        // s = r - alpha v; t = A s; omega = (t, s) / (t, t)
+        if ((e = grs_axpby(model, ss, r, -alpha, vv, 0.0, nullptr, n)) != cudaSuccess) break;
+        if ((e = grs_op(model, v, ss, tt)) != cudaSuccess) break;
+        if ((e = grs_reduce(model, tt, ss, n, 0, 0)) != cudaSuccess) break;
+        if ((e = grs_reduce(model, tt, tt, n, 0, 1)) != cudaSuccess) break;
+        if ((e = grs_read(model, 2)) != cudaSuccess) break;
+        omega = g.red_host[1] > 0.0 ? g.red_host[0] / g.red_host[1] : 0.0;
+        // x += alpha p + omega s; r = s - omega t
+        if ((e = grs_axpby(model, x, x, alpha, pp, omega, ss, n)) != cudaSuccess) break;
+        if ((e = grs_axpby(model, r, ss, -omega, tt, 0.0, nullptr, n)) != cudaSuccess) break;
+        if (omega == 0.0) {
+            it++;
+            if ((e = grs_reduce(model, r, nullptr, n, 1, 0)) != cudaSuccess) break;
+            if ((e = grs_read(model, 1)) != cudaSuccess) break;
+            rn = g.red_host[0] / bn;
+            break;
+        }
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "BiCGSTAB");
+    g.last_iterations = it;
+    g.last_residual = rn;
+    if (!(rn <= kRateAccept)) {
+        set_error("mgr_compute_level_populations: the global rate system (n_off_diag > 0) did not converge: "
+                  "relative residual " + std::to_string(rn) + " after " + std::to_string(it) + " iterations");
+        return MGR_ERR_NONFINITE;
+    }
+    count_launch();
+    unscale_kernel<<<grid_for(n, 256, model->sm_count * 16), 256, 0, s>>>(v, m.P, x);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "populations");
+    return MGR_OK;
+}
+
+// One normal iteration with the non-local ALO: the banded FP64 formal solve, Jeff with
+// the band elements, the global rate system per species, corrections, convergence and
+// the line data.  Launched directly (the rate solve reads its scalars on the host).
+static int banded_iteration(MgrModel* model) {
+    AliState& st = *model->ali;
+    const DevModel& m = model->dm;
+    mark(model, 0);
+    cudaError_t e = launch_fo2_range(model, MGR_PRECISION_FP64, 0, m.P, model->J_scratch, nullptr,
+                                     model->lam_scratch, model->work, model->work_bytes, 0, 0xffffffffu, nullptr,
+                                     nullptr, nullptr, st.alo_off, st.alo_nr);
+    mark(model, 1);
+    if (e == cudaSuccess)
+        e = ali_launch_jeff(model, model->J_scratch, model->lam_scratch, nullptr, st.alo_off, st.alo_nr);
+    mark(model, 2);
+    if (e == cudaSuccess && !st.grs.built) e = build_csr(model);
+    if (e != cudaSuccess) return cuda_fail(e, "banded ALI iteration");
+    for (size_t l = 0; l < st.species.size(); l++) {
+        AliSpecies& sp = st.species[l];
+        const int rc = global_stateq(model, l);
+        if (rc != MGR_OK) return rc;
+        count_launch();
+        negcorr_kernel<<<grid_for(m.P, 128, model->sm_count * 8), 128, 0, model->stream>>>(
+            m, sp.view, st.prm.population_inversion_fraction);
+        if ((e = cudaGetLastError()) == cudaSuccess)
+            e = launch_convergence(model, sp.view.pop, sp.prev1, sp.view.tot, sp.view.nlev, true, st.stats_dev + 3 * l);
+        if (e != cudaSuccess) return cuda_fail(e, "banded ALI iteration");
+    }
+    e = ali_launch_line_refresh(model);
+    mark(model, 3);
+    return e == cudaSuccess ? MGR_OK : cuda_fail(e, "line data");
 }
 
 void ali_shard_changed(MgrModel* model) {
@@ -1034,7 +1652,8 @@ int mgr_compute_jeff(MgrModel* model, uint32_t l, double* Jlin, double* Jeff, do
         set_error("mgr_compute_jeff: needs a formal solve with the ALO diagonal first");
         return MGR_ERR_ARGUMENT;
     }
-    cudaError_t e = ali_launch_jeff(model, model->last_J, model->last_lam, nullptr);
+    cudaError_t e = ali_launch_jeff(model, model->last_J, model->last_lam, nullptr, model->last_alo_off,
+                                    model->last_alo_nr);
     const SpeciesView& v = model->ali->species[l].view;
     const size_t bytes = (size_t)model->dm.P * v.nrad * sizeof(double);
     if (e == cudaSuccess && Jlin) e = cudaMemcpyAsync(Jlin, v.Jlin, bytes, cudaMemcpyDeviceToHost, model->stream);
@@ -1068,9 +1687,30 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
         return MGR_ERR_UNSUPPORTED;
     }
     AliState& st = *model->ali;
+    const DevModel& dm = model->dm;
+    const bool bands = dm.n_off_diag > 0;
+    if (bands) {
+        if (st.sparse) {  // lineProducingSpecies.tpp:592-593
+            set_error("mgr_compute_level_populations_sparse: n_off_diag != 0, so the sparse update cannot be used");
+            return MGR_ERR_UNSUPPORTED;
+        }
+        if (precision != MGR_PRECISION_FP64) {
+            set_error("mgr_compute_level_populations: n_off_diag > 0 runs the banded FP64 formal solve "
+                      "(precision must be FP64)");
+            return MGR_ERR_UNSUPPORTED;
+        }
+        if (model->shard_reduce || model->shard_begin != 0 || model->shard_end < dm.hnrays) {
+            set_error("mgr_compute_level_populations: n_off_diag > 0 needs every ray pair on this model "
+                      "(no ray-pair shard)");
+            return MGR_ERR_UNSUPPORTED;
+        }
+        if ((size_t)dm.P * dm.L * band_slots(dm) >= ((size_t)1 << 32)) {
+            set_error("mgr_compute_level_populations: more than 2^32 band elements");
+            return MGR_ERR_UNSUPPORTED;
+        }
+    }
     st.prm = prm;
     st.keep_history = use_ng != 0;
-    const DevModel& dm = model->dm;
     const size_t PF = (size_t)dm.P * dm.F, PL = (size_t)dm.P * dm.L;
     int rc = MGR_OK;
     auto scratch = [&](double** p, size_t* have, size_t bytes) -> int {
@@ -1093,6 +1733,11 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
     if ((rc = scratch(&model->lam_scratch, &model->lam_scratch_bytes, PL * 8)) != MGR_OK) return rc;
     if (st.sparse && (rc = scratch(&st.Jlin_buf, &st.Jlin_bytes, PL * 8)) != MGR_OK) return rc;
     if ((rc = scratch(&model->work, &model->work_bytes, fo2_work_bytes(model, dm.P, true, true))) != MGR_OK) return rc;
+    if (bands) {
+        cudaError_t eg = ensure_global(model);
+        if (eg != cudaSuccess) return cuda_fail(eg, "global rate system allocation");
+        st.grs.built = false;  // the CSR follows the first banded solve of this call
+    }
     // Between two Ng steps the history grows by one residual and one population per
     // normal iteration (at most mem_limit + remove_N_its of them), plus the initial
     // population and one trial residual/population pair.
@@ -1174,7 +1819,9 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
         iteration++;
         some_not_converged = false;
         if ((e = ali_history_push_all(model)) != cudaSuccess) return cuda_fail(e, "population history");
-        if ((e = normal_iteration(model, precision)) != cudaSuccess) {
+        if (bands) {
+            if ((rc = banded_iteration(model)) != MGR_OK) return rc;
+        } else if ((e = normal_iteration(model, precision)) != cudaSuccess) {
             if (st.reduce_failed) {
                 st.reduce_failed = false;
                 set_error("mgr_compute_level_populations: the ray-shard reduce function failed");
@@ -1200,6 +1847,8 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
     model->last_J = st.sparse ? nullptr : model->J_scratch;
     model->last_Jlin = st.sparse ? st.Jlin_buf : nullptr;
     model->last_lam = model->lam_scratch;
+    model->last_alo_off = bands ? st.alo_off : nullptr;
+    model->last_alo_nr = bands ? st.alo_nr : nullptr;
     if (iterations) *iterations = iteration;
     int st_rc = MGR_OK;
     {

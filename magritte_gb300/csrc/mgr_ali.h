@@ -62,6 +62,30 @@ struct AliSpecies {
     void pop_back_history();
 };
 
+// The global rate system (n_off_diag > 0): per point block an LU factorisation (the
+// block-Jacobi preconditioner), and over all points BiCGSTAB on the preconditioned,
+// population-scaled operator.  The band elements couple point p's lower level to the
+// upper level of the element's point nr; the diagonal term they add to nr's own block
+// is gathered through a CSR of the elements by (nr, upper level), built once per ALI
+// call (the rays, hence the elements' points, do not change between iterations).
+struct GlobalRate {
+    bool built = false;                 // CSR of the current ALI call
+    std::vector<uint32_t*> csr_off;     // per species: [P nlev + 1] row starts
+    std::vector<uint32_t*> csr_ent;     // per species: element indices (into coef), ascending per row
+    std::vector<size_t> csr_cap;        // entries allocated per species
+    uint32_t* cursor = nullptr;         // [P max_nlev + 1] counts, then fill cursors
+    double* lu = nullptr;               // [P][nlev^2] LU factors of the point blocks
+    uint32_t* piv = nullptr;            // [P][nlev] row interchanges
+    double* coef = nullptr;             // [P][nrad][hnrays 2K] v of each band element
+    double* vec = nullptr;              // 9 vectors of P nlev (x, r, rhat, p, v, s, t, rhs, spare)
+    double* red = nullptr;              // reduction partials [kConvBlocks] and results [8]
+    double* red_host = nullptr;         // pinned copy of the results
+    size_t cap_n = 0, cap_lu = 0, cap_coef = 0;
+    int last_iterations = 0;            // BiCGSTAB iterations of the latest solve
+    double last_residual = 0.0;         // its final max-norm residual relative to the right-hand side
+    std::vector<void*> allocs;
+};
+
 struct AliState {
     std::vector<AliSpecies> species;
     std::vector<void*> allocs;       // every device allocation of this state
@@ -93,10 +117,18 @@ struct AliState {
     cudaEvent_t ev[6] = {};
     bool timing = false;
     double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
+    // Non-local ALO (n_off_diag > 0): the band elements of the latest formal solve
+    // [P][L][hnrays][2 n_off_diag] (the model's alo_scratch / alo_nr_scratch, which
+    // outlive this state for mgr_compute_jeff) and the global rate system.
+    double* alo_off = nullptr;
+    uint32_t* alo_nr = nullptr;
+    GlobalRate grs;
 };
 
 // Jlin: the memory-lean solve's line-integrated J [P][L] (compute_Jeff_sparse), or NULL.
-cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam, const double* Jlin = nullptr);
+// alo_off / alo_nr: the band elements of the same formal solve (n_off_diag > 0), or NULL.
+cudaError_t ali_launch_jeff(MgrModel* model, const double* J, const double* lam, const double* Jlin = nullptr,
+                            const double* alo_off = nullptr, const uint32_t* alo_nr = nullptr);
 // Drops the captured iteration after the ray-pair shard or its reduce function changed.
 void ali_shard_changed(MgrModel* model);
 cudaError_t ali_launch_stateq_and_refresh(MgrModel* model, const double* lam);

@@ -112,6 +112,7 @@ struct DevModel {
     float dz_scale;              // 1 / Ko  (true optical depth = chi_f * dz * dz_scale)
     float s_scale;               // Ko / Ke (true source = scaled source * s_scale)
     int approx;
+    uint32_t n_off_diag;  // Parameters::n_off_diag: band elements of the non-local ALO (0: diagonal only)
     uint32_t sph;                // 1D spherical symmetry (Parameters::spherical_symmetry)
     uint32_t adaptive;           // Rays::use_adaptive_directions: raydir [P][nrays][3], rayw [P][nrays]
 };
@@ -300,6 +301,8 @@ MGR_HD uint32_t n_interp_all_lines(const DevModel& m, uint32_t crt, uint32_t nxt
 
 // Range of the correctly rounded erff table of split precision: every float in
 // [kErfBandLo, 3.919206) (12.8 M entries, 51 MB).
+constexpr uint32_t kMaxOffDiag = 4;  // largest n_off_diag of the banded (non-local ALO) solve
+
 constexpr float kErfBandLo = 1.4375f;
 constexpr uint32_t kErfBandCount = 0x407ad445u - 0x3fb80000u;  // bits(3.919206f) - bits(1.4375f)
 

@@ -224,6 +224,91 @@ __global__ void __launch_bounds__(256, MINB)
 }
 
 // ---------------------------------------------------------------------------------
+// Formal solve with the non-local ALO (n_off_diag > 0, FP64 mode): fo2_kernel's work
+// plus, per lane of a frequency in a line integral, the update_Lambda terms of the
+// K = m.n_off_diag band elements on each side of the origin (solve_lane<..., NB>).
+// They are summed over the line's quadrature points by a segmented shuffle scan (the
+// lanes of one line are adjacent) and added to
+//   alo_off[((o * L + l) * hnrays + rr) * 2K + slot],  alo_nr[...] the element's point
+// (slot m: centre - m - 1, slot K + m: centre + m + 1).  One warp owns an (o, rr) item
+// and adds its frequency chunks in order, so the sums are deterministic.
+// ---------------------------------------------------------------------------------
+constexpr int kMaxBand = (int)kMaxOffDiag;
+
+template <int AP>
+__global__ void __launch_bounds__(256, 2)
+    fo2_alo_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
+                   double* __restrict__ U, size_t u_stride, uint32_t u_o0, double* __restrict__ LD, size_t ld_stride,
+                   uint32_t ld_o0, double* __restrict__ alo_off, uint32_t* __restrict__ alo_nr, int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nw = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    double* sl = reinterpret_cast<double*>(smem);
+    const uint32_t Lpad = (m.L + 1) & ~1u;
+    HalfSmem bk, fw;
+    carve_halves(smem + (size_t)Lpad * 8 + (size_t)w * half_bytes_per_warp(cap), cap, bk, fw);
+    for (uint32_t i = threadIdx.x; i < m.L; i += blockDim.x) sl[i] = m.sorted_line[i];
+    __syncthreads();
+    const uint32_t K = m.n_off_diag;
+    const uint64_t n_items = (uint64_t)(o_end - o_begin) * nR;
+    const uint64_t stride = (uint64_t)gridDim.x * nw;
+    for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
+        const uint32_t o = o_begin + (uint32_t)(item / nR);
+        const uint32_t rr = rr0 + (uint32_t)(item % nR);
+        int nb = 0, nf = 0;
+        trace_pair<true, 0, 1>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
+        if (nb < 0 || nf < 0) continue;  // status recorded by the trace
+        double* Ui = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
+        double* Li = LD ? LD + (size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F : nullptr;
+        for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
+            const uint32_t f = f0 + lane;
+            BandOut<kMaxBand> bo;
+            bo.K = K;
+            bo.w_rr = 0.0;
+            uint32_t lid = 0xffffffffu;
+            bool bands = false;
+            if (f < m.F) {
+                const LaneCtx c = lane_ctx(m, o, f);
+                bo.w_rr = ray_w(m, o, rr);
+                const LaneResult r = solve_lane<MODE_FP64, AP, false, kMaxBand>(m, sl, c, bk, nb, fw, nf, &bo);
+                Ui[f] = r.u;
+                if (Li) Li[f] = r.solved ? r.Ldiag : 0.0;
+                if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
+                lid = m.corr_line[f];
+                bands = r.solved && m.in_line[f];
+            }
+            // lanes of one line are adjacent: a segment starts where the line changes
+            const uint32_t prev = __shfl_up_sync(FULL_MASK, lid, 1);
+            const uint32_t heads = __ballot_sync(FULL_MASK, lane == 0 || prev != lid);
+            const int seg0 = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+            const uint32_t next = __shfl_down_sync(FULL_MASK, lid, 1);
+            const bool tail = (lane == 31) || next != lid;
+            // the segment's first lane with band terms supplies the elements' points
+            const uint32_t with = __ballot_sync(FULL_MASK, bands) & (0xffffffffu << seg0);
+            const int src = with ? __ffs(with) - 1 : lane;
+            const bool write = tail && with != 0 && src <= lane;
+            for (uint32_t s = 0; s < 2 * K; s++) {
+                double v = bands ? bo.val[s] : 0.0;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const double up = __shfl_up_sync(FULL_MASK, v, off);
+                    if (lane - off >= seg0) v += up;
+                }
+                const uint32_t seg_nr = __shfl_sync(FULL_MASK, bands ? bo.nr[s] : o, src);
+                if (write) {
+                    const size_t a = (((size_t)o * m.L + lid) * m.hnrays + rr) * 2 * K + s;
+                    alo_off[a] += v;
+                    alo_nr[a] = seg_nr;
+                }
+            }
+            __syncwarp();  // a line split over two chunks: the next chunk's tail lane adds to these sums
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------
 // Formal solve, stage 2: J and the ALO diagonal per origin, summed over ray pairs in
 // the reference's order (ray pair outer, quadrature point inner):
 //   J(o, f)   = sum_rr u(rr, o, f) 2 w_rr                               (solver.tpp:497-504)
@@ -587,15 +672,71 @@ static cudaError_t launch_fo2_approx(MgrModel* model, uint32_t o_begin, uint32_t
     }
 }
 
+// Band elements of origins [o_begin, o_end) cleared: value 0 and the origin's own
+// point, which an element keeps where no frequency of its line has a band term (a
+// ray of one point, or an element beyond the ray's end), so that every slot names a
+// point whatever the values.
+__global__ void alo_init_kernel(uint32_t o_begin, uint32_t o_end, size_t per_o, double* __restrict__ alo_off,
+                                uint32_t* __restrict__ alo_nr) {
+    const size_t n = (size_t)(o_end - o_begin) * per_o;
+    const size_t base = (size_t)o_begin * per_o;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        alo_off[base + t] = 0.0;
+        alo_nr[base + t] = o_begin + (uint32_t)(t / per_o);
+    }
+}
+
+// The banded solve (non-local ALO): FP64 mode, the run-time geometry variant.
+static cudaError_t launch_fo2_alo(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
+                                  double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo,
+                                  double* alo_off, uint32_t* alo_nr) {
+    const DevModel& m = model->dm;
+    const uint32_t cap = model->half_cap;
+    const int nw = 4;
+    const uint32_t Lpad = (m.L + 1) & ~1u;
+    const size_t smem = (size_t)Lpad * 8 + (size_t)nw * half_bytes_per_warp(cap);
+    auto kern = (m.approx == APPROX_ONELINE)      ? fo2_alo_kernel<APPROX_ONELINE>
+                : (m.approx == APPROX_CLOSELINES) ? fo2_alo_kernel<APPROX_CLOSELINES>
+                                                  : fo2_alo_kernel<APPROX_NONE>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nw * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const uint64_t items = (uint64_t)(o_end - o_begin) * nR;
+    uint64_t grid = (uint64_t)model->sm_count * per_sm;
+    const uint64_t need = (items + nw - 1) / nw;
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
+    count_launch();
+    kern<<<(unsigned)grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo,
+                                                          alo_off, alo_nr, model->status);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
                              double* lam, double* work, size_t work_bytes, uint32_t rr_begin, uint32_t rr_end,
-                             double* Jlin, double* anis, double* v) {
+                             double* Jlin, double* anis, double* v, double* alo_off, uint32_t* alo_nr) {
     const DevModel& m = model->dm;
     if (o_end <= o_begin) return cudaSuccess;
     if (rr_end > m.hnrays) rr_end = m.hnrays;
     if (rr_begin >= rr_end) return cudaErrorInvalidValue;
     const uint32_t nR = rr_end - rr_begin;
     if (u && nR != m.hnrays) return cudaErrorInvalidValue;  // u is written for full solves only
+    if (alo_off) {
+        // every ray pair of the origins' lists, cleared first
+        if (m.n_off_diag == 0 || m.n_off_diag > (uint32_t)kMaxBand || nR != m.hnrays || v || !alo_nr)
+            return cudaErrorInvalidValue;
+        const size_t per_o = (size_t)m.L * m.hnrays * 2 * m.n_off_diag;
+        const size_t n0 = (size_t)(o_end - o_begin) * per_o;
+        size_t g0 = (n0 + 255) / 256;
+        if (g0 > (size_t)model->sm_count * 16) g0 = (size_t)model->sm_count * 16;
+        count_launch();
+        alo_init_kernel<<<(unsigned)(g0 ? g0 : 1), 256, 0, model->stream>>>(o_begin, o_end, per_o, alo_off, alo_nr);
+        const cudaError_t e0 = cudaGetLastError();
+        if (e0 != cudaSuccess) return e0;
+    }
     const int k = (u ? 0 : 1) + (lam ? 1 : 0);
     const size_t per = fo2_bytes_per_origin(model);
     uint32_t chunk = o_end - o_begin;
@@ -625,7 +766,9 @@ cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, u
         double* LD = lam ? next : nullptr;
         const size_t ls = (size_t)n * m.F;
         cudaError_t e;
-        if (v)  // v has u's layout: u is given (no chunked staging of U)
+        if (alo_off)
+            e = launch_fo2_alo(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, alo_off, alo_nr);
+        else if (v)  // v has u's layout: u is given (no chunked staging of U)
             e = (precision == MGR_PRECISION_SPLIT)
                     ? launch_fo2_uv<MODE_SPLIT>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, v)
                     : launch_fo2_uv<MODE_FP64>(model, c0, c1, rr_begin, nR, U, us, uo, LD, ls, c0, v);

@@ -49,6 +49,10 @@ struct MgrModel {
     size_t lam_scratch_bytes = 0;
     double* v_scratch = nullptr;  // v of the uv solve
     size_t v_scratch_bytes = 0;
+    double* alo_scratch = nullptr;     // band elements of the host-buffer banded solve [P][L][hnrays][2K]
+    size_t alo_scratch_bytes = 0;
+    double* alo_nr_scratch = nullptr;  // their points (uint32 data in a double-sized allocation)
+    size_t alo_nr_scratch_bytes = 0;
     // staging of u(rr, o, f) / L_diag(rr, o, f) between the two formal-solve stages
     double* work = nullptr;
     size_t work_bytes = 0;
@@ -56,6 +60,9 @@ struct MgrModel {
     const double* last_J = nullptr;
     const double* last_lam = nullptr;
     const double* last_Jlin = nullptr;  // line-integrated J [P][L] of the last memory-lean solve
+    // band elements of the non-local ALO of the last formal solve (null when it had none)
+    const double* last_alo_off = nullptr;
+    const uint32_t* last_alo_nr = nullptr;
     // line-producing species and the ALI loop (mgr_ali.cu)
     mgr::AliState* ali = nullptr;
     // ray-pair shard of the ALI loop's formal solves and the sum over shards
@@ -137,7 +144,7 @@ size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, b
 cudaError_t launch_fo2_range(MgrModel* model, int precision, uint32_t o_begin, uint32_t o_end, double* J, double* u,
                              double* lam, double* work, size_t work_bytes, uint32_t rr_begin = 0,
                              uint32_t rr_end = 0xffffffffu, double* Jlin = nullptr, double* anis = nullptr,
-                             double* v = nullptr);
+                             double* v = nullptr, double* alo_off = nullptr, uint32_t* alo_nr = nullptr);
 cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32_t l, uint32_t capacity,
                                 uint32_t* d_meta, uint32_t* d_nr, uint32_t* d_ni, double* d_fac, double* d_shift,
                                 double* d_dZ);

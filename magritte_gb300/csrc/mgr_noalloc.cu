@@ -83,5 +83,7 @@ extern "C" int mgr_formal_solve_fo2_device_noalloc(MgrModel* model, int precisio
     // which mgr_compute_jeff reads
     model->last_J = J_dev;
     model->last_lam = lambda_diag_dev;
+    model->last_alo_off = nullptr;
+    model->last_alo_nr = nullptr;
     return MGR_OK;
 }

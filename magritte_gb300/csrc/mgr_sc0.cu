@@ -255,6 +255,8 @@ int mgr_formal_solve_sc0_device(MgrModel* model, int precision, double* J_dev, d
     if (e != cudaSuccess) return cuda_fail(e, "short-characteristics launch");
     model->last_J = J_dev;
     model->last_lam = lambda_diag_dev;
+    model->last_alo_off = nullptr;
+    model->last_alo_nr = nullptr;
     return MGR_OK;
 }
 

@@ -1137,6 +1137,33 @@ struct Sweep {
     float dtf = 0.0f, S_inf = 0.0f;  // dt and S_in as the split sweep's floats
 };
 
+// Non-local ALO (n_off_diag > 0, FP64 mode): the last NB + 1 rows of one sweep as it
+// reaches the origin, so that the band entries of the inverse Feautrier matrix next
+// to the origin can be formed once both sweeps are done (band_tail).
+template <int NB>
+struct BandRing {
+    double F[NB + 1];    // FF (backward half) or GG (forward half) of the row
+    double dt[NB + 1];   // optical depth of the row's pair toward the origin
+    double sh[NB + 1];   // the row element's shift
+    uint32_t nr[NB + 1]; // the row element's point
+    int rows = 0;        // rows eliminated so far (the ring holds the last NB + 1)
+};
+
+// In: K (the model's n_off_diag, at most NB) and w_rr (the ray pair's weight).  Out:
+// the update_Lambda terms of the elements centre - m - 1 (slot m) and centre + m + 1
+// (slot K + m), m < K, and their points; 0 and the origin where the ray ends first.
+template <int NB>
+struct BandOut {
+    uint32_t K;
+    double w_rr;
+    double val[2 * NB + 1];
+    uint32_t nr[2 * NB + 1];
+};
+
+template <int NB>
+MGR_HD void band_tail(const DevModel& m, const double* sl, const LaneCtx& c, const BandRing<NB>& tp,
+                      const BandRing<NB>& bt, BandOut<NB>& out);
+
 // Two-sided Feautrier solve of frequency c.f on the ray pair staged in `bk`
 // (backward half, direction rr) and `fw` (forward half, antipode).  Both halves run
 // through the same sweep code (outer end first):
@@ -1145,9 +1172,12 @@ struct Sweep {
 //   forward half:  elements last .. centre+1, row `last` with the source of its own
 //                  pair, rows i < last with S[i] from pair (i, i+1) = the previous
 //                  pair's inner element.
-template <int MODE, int AP, bool UV = false>
+// NB > 0 (FP64 mode): also the non-local ALO terms of the K = bo->K band elements on
+// each side of the origin (solver.tpp:2319-2355, :1800-1846).
+template <int MODE, int AP, bool UV = false, int NB = 0>
 __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, const LaneCtx& c, const HalfSmem& bk,
-                                          int nb, const HalfSmem& fw, int nf) {
+                                          int nb, const HalfSmem& fw, int nf, BandOut<NB>* bo = nullptr) {
+    static_assert(NB == 0 || (MODE == MODE_FP64 && !UV), "band elements: FP64 mode, J / ALO solve");
     using T = typename Real_<MODE>::T;
     // split precision eliminates in projective form (the uv solve keeps the (F, FI, Su)
     // state its origin rows need)
@@ -1171,6 +1201,7 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
     EC<MODE> ec_cen{T(0), T(0), false};
     Sweep top{0.0, 0.0, 0.0, 0.0, 0.0, false, false, 0.0, 0.0}, bot = top;
     Proj ptop{0.0, 1.0, 0.0, 1.0}, pbot = ptop;
+    BandRing<NB> rtop{}, rbot{};
 
 #pragma unroll 1
     for (int side = 0; side < 2; side++) {
@@ -1244,6 +1275,15 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
                 } else {
                     elim_row<MODE>(dt_prev, po.dtau, rowS, st.F, st.FI, st.Su);
                 }
+                if constexpr (NB > 0) {
+                    BandRing<NB>& rg = side ? rbot : rtop;
+                    const int r = rg.rows % (NB + 1);
+                    rg.F[r] = st.F;
+                    rg.dt[r] = (double)po.dtau;
+                    rg.nr[r] = outer.nr;
+                    rg.sh[r] = outer.shift;
+                    rg.rows++;
+                }
                 dt_prev = po.dtau;
                 S_carry = po.Shi;
                 if (!more) break;
@@ -1264,6 +1304,8 @@ __host__ __device__ LaneResult solve_lane(const DevModel& m, const double* sl, c
             ptop = ps;
         }
     }
+
+    if constexpr (NB > 0) band_tail<NB>(m, sl, c, rtop, rbot, *bo);
 
     if constexpr (PROJ) {
         if (top.rows && bot.rows) {
@@ -1635,6 +1677,136 @@ MGR_HD LambdaFactors lambda_factors(const DevModel& m, const double* sl, uint32_
 MGR_HD double lambda_element(const LambdaFactors& k, double w_rr, double Ldiag) {
     const double constante = k.Aqw * (2.0 * w_rr);
     return constante * k.frq * k.phi * Ldiag * k.inverse_chi;
+}
+
+// The update_Lambda factors of element n of the ray (point p, shift sh) for
+// frequency f (solver.tpp:1811-1846): chi at p for line k, nu(p, f) sh and the profile
+// of p there.
+MGR_HD LambdaFactors lambda_factors_at(const DevModel& m, const double* sl, uint32_t p, uint32_t f, double sh) {
+    const uint32_t ls = m.corr_lspec[f];
+    const uint32_t k = m.corr_k[f];
+    const uint32_t z = m.corr_z[f];
+    const uint32_t lid = m.nrad_cum[ls] + k;
+    const double freq_line = m.line[lid];
+    const double invr_mass = m.lspec_inv_mass[ls];
+    LambdaFactors r;
+    r.Aqw = m.line_A[lid] * m.quad_w[(size_t)ls * m.Q + z];
+    double eta, chi;
+    get_eta_and_chi(m, sl, p, k, freq_line, eta, chi);
+    r.inverse_chi = 1.0 / chi;
+    r.frq = m.nu[(size_t)p * m.F + f] * sh;
+    r.phi = thermo_profile(m, invr_mass, p, freq_line, r.frq);
+    return r;
+}
+
+// The band entries next to the origin from the two sweeps' last rows, in the
+// reference's banded form (solver.tpp:2319-2355) with elements indexed by i = n - centre:
+//   FF(i), i >= 0: the forward recurrence continued over the forward half's pairs
+//                  (FF(0) the boundary row when the origin is the first element);
+//   GG(i), i <= 0: the backward recurrence continued over the backward half's pairs
+//                  (GG(0) the boundary row when the origin is the last element);
+//   L_diag(i) = iC(i) / (FF(i) + GP(i + 1)), with the boundary rows' own forms at the
+//                  ray's two ends;
+//   L_lower(m) = L_diag(-m-1) GI(-m) ... GI(0),  L_upper(m) = L_diag(m+1) FI(m) ... FI(0),
+// then the update_Lambda term of each (solver.tpp:1800-1846).
+template <int NB>
+MGR_HD void band_tail(const DevModel& m, const double* sl, const LaneCtx& c, const BandRing<NB>& tp,
+                      const BandRing<NB>& bt, BandOut<NB>& out) {
+    constexpr int O = NB + 1;  // index offset of element i in the local arrays
+    const int K = (int)out.K;
+    const int Rt = tp.rows, Rb = bt.rows;  // rows of each sweep: centre - first, last - centre
+    double dtv[2 * NB + 3], FF[2 * NB + 3], GG[2 * NB + 3], LD[2 * NB + 3];
+    uint32_t nrv[2 * NB + 3];
+    double shv[2 * NB + 3];
+    for (int j = 1; j <= NB + 1 && j <= Rt; j++) {  // backward half: element -j, pair (-j, -j+1)
+        const int r = (Rt - j) % (NB + 1);
+        dtv[O - j] = tp.dt[r];
+        FF[O - j] = tp.F[r];
+        nrv[O - j] = tp.nr[r];
+        shv[O - j] = tp.sh[r];
+    }
+    for (int j = 1; j <= NB + 1 && j <= Rb; j++) {  // forward half: element j, pair (j-1, j)
+        const int r = (Rb - j) % (NB + 1);
+        dtv[O + j - 1] = bt.dt[r];
+        GG[O + j] = bt.F[r];
+        nrv[O + j] = bt.nr[r];
+        shv[O + j] = bt.sh[r];
+    }
+    // FF(i), 0 <= i <= K, element i not the last
+    for (int i = 0; i <= K && i <= Rb - 1; i++) {
+        if (i == 0 && Rt == 0) {
+            const double dt = dtv[O];
+            const double Bf_min_Cf = 1.0 + 2.0 * (1.0 / dt);
+            FF[O] = 0.5 * Bf_min_Cf * dt * dt;
+        } else {
+            const double dc = dtv[O + i - 1], dn = dtv[O + i];
+            const double dtau_avg = 0.5 * (dc + dn);
+            const double A = 1.0 / (dtau_avg * dc);
+            const double FIp = 1.0 / (1.0 + FF[O + i - 1]);
+            FF[O + i] = (A * FF[O + i - 1] * FIp + 1.0) * (dtau_avg * dn);
+        }
+    }
+    // GG(i), -K + 1 <= i <= 0, element i not the first
+    for (int i = 0; i >= -K + 1 && i >= -Rt + 1; i--) {
+        if (i == 0 && Rb == 0) {
+            const double dt = dtv[O - 1];
+            const double Bl_min_Al = 1.0 + 2.0 * (1.0 / dt);
+            GG[O] = 0.5 * Bl_min_Al * dt * dt;
+        } else {
+            const double dc = dtv[O + i - 1], dn = dtv[O + i];
+            const double dtau_avg = 0.5 * (dc + dn);
+            const double C = 1.0 / (dtau_avg * dn);
+            const double GP = GG[O + i + 1] * (1.0 / (1.0 + GG[O + i + 1]));
+            GG[O + i] = (C * GP + 1.0) * (dtau_avg * dc);
+        }
+    }
+    // L_diag(i), -K <= i <= K on the ray
+    for (int i = -K; i <= K; i++) {
+        if (i < -Rt || i > Rb || i == 0) continue;
+        if (i == Rb) {  // the last element
+            const double inverse_dtau_l = 1.0 / dtv[O + i - 1];
+            const double Al = 2.0 * inverse_dtau_l * inverse_dtau_l;
+            const double Bl_min_Al = 1.0 + 2.0 * inverse_dtau_l;
+            const double Bl = Bl_min_Al + Al;
+            LD[O + i] = (1.0 + FF[O + i - 1]) / (Bl_min_Al + Bl * FF[O + i - 1]);
+        } else if (i == -Rt) {  // the first element
+            const double inverse_dtau_f = 1.0 / dtv[O + i];
+            const double Cf = 2.0 * inverse_dtau_f * inverse_dtau_f;
+            const double Bf_min_Cf = 1.0 + 2.0 * inverse_dtau_f;
+            const double Bf = Bf_min_Cf + Cf;
+            LD[O + i] = (1.0 + GG[O + i + 1]) / (Bf_min_Cf + Bf * GG[O + i + 1]);
+        } else {
+            const double dc = dtv[O + i - 1], dn = dtv[O + i];
+            const double dtau_avg = 0.5 * (dc + dn);
+            const double GP = GG[O + i + 1] * (1.0 / (1.0 + GG[O + i + 1]));
+            LD[O + i] = (dtau_avg * dn) / (FF[O + i] + GP);
+        }
+    }
+    const double w2 = 2.0 * out.w_rr;
+    for (int mm = 0; mm < K; mm++) {
+        // lower: element -(mm + 1), L_diag GI(-mm) ... GI(0) in the reference's order
+        out.val[mm] = 0.0;
+        out.nr[mm] = c.o;
+        if (mm + 1 <= Rt) {
+            const int i = -(mm + 1);
+            double L = LD[O + i];
+            for (int j = i + 1; j <= 0; j++) L *= 1.0 / (1.0 + GG[O + j]);
+            const LambdaFactors f = lambda_factors_at(m, sl, nrv[O + i], c.f, shv[O + i]);
+            out.val[mm] = f.Aqw * w2 * f.frq * f.phi * L * f.inverse_chi;
+            out.nr[mm] = nrv[O + i];
+        }
+        // upper: element mm + 1, L_diag FI(mm) ... FI(0)
+        out.val[K + mm] = 0.0;
+        out.nr[K + mm] = c.o;
+        if (mm + 1 <= Rb) {
+            const int i = mm + 1;
+            double L = LD[O + i];
+            for (int j = i - 1; j >= 0; j--) L *= 1.0 / (1.0 + FF[O + j]);
+            const LambdaFactors f = lambda_factors_at(m, sl, nrv[O + i], c.f, shv[O + i]);
+            out.val[K + mm] = f.Aqw * w2 * f.frq * f.phi * L * f.inverse_chi;
+            out.nr[K + mm] = nrv[O + i];
+        }
+    }
 }
 
 // Short characteristics: one direction's element (solver.tpp:1624-1638),

@@ -867,6 +867,157 @@ int orc_feautrier_bands(const OrcModel* m, uint32_t o, uint32_t rr, uint32_t f, 
 }
 
 /* ------------------------------------------------------------------ */
+/* Non-local ALO (n_off_diag > 0)                                      */
+/* ------------------------------------------------------------------ */
+/* Lambda::add_element (lambda.tpp:74-86) on lists per (p, line): an element whose
+ * emitting point nr is already listed accumulates, else it is appended. */
+typedef struct {
+    uint32_t cap;
+    uint32_t* n;  /* [P][L] */
+    uint32_t* nr; /* [P][L][cap] */
+    double* ls;   /* [P][L][cap] */
+    int overflow;
+} AloLists;
+
+static void alo_add(AloLists* a, uint32_t L, uint32_t p, uint32_t lid, uint32_t nr, double v) {
+    const size_t key = (size_t)p * L + lid;
+    uint32_t* nrs    = a->nr + key * a->cap;
+    double* ls       = a->ls + key * a->cap;
+    for (uint32_t i = 0; i < a->n[key]; i++)
+        if (nrs[i] == nr) {
+            ls[i] += v;
+            return;
+        }
+    if (a->n[key] == a->cap) {
+        a->overflow = 1;
+        return;
+    }
+    nrs[a->n[key]] = nr;
+    ls[a->n[key]]  = v;
+    a->n[key]++;
+}
+
+/* The update_Lambda term of element n (solver.tpp:1787-1799, :1811-1846):
+ * A_k w_z 2 w_rr nu(nr[n], f) shift[n] phi(nr[n]) L / chi(nr[n], line k). */
+static double lambda_term(const OrcModel* m, const Buf* b, uint32_t rr, uint32_t f, uint32_t n, double L) {
+    const uint32_t c        = b->centre;
+    const double w_ang      = 2.0 * ray_wt(m, b->nr[c], rr);
+    const uint32_t ls       = m->corr_lspec[f];
+    const uint32_t k        = m->corr_k[f];
+    const uint32_t z        = m->corr_z[f];
+    const uint32_t lid      = m->nrad_cum[ls] + k;
+    const double freq_line  = m->line[lid];
+    const double invr_mass  = m->lspec_inverse_mass[ls];
+    const double constante  = m->line_A[lid] * m->quad_weights[(size_t)ls * m->nquads + z] * w_ang;
+    const uint32_t p        = b->nr[n];
+    double eta, chi;
+    get_eta_and_chi(m, p, k, freq_line, &eta, &chi);
+    const double inverse_chi = 1.0 / chi;
+    const double frq         = m->nu[(size_t)p * m->nfreqs + f] * b->shift[n];
+    const double phi         = thermo_profile(m, invr_mass, p, freq_line, frq);
+    return constante * frq * phi * L * inverse_chi;
+}
+
+/* Solver::update_Lambda with n_off_diag > 0 (solver.tpp:1760-1850): the diagonal
+ * element, then for m < n_off_diag the lower (centre - m - 1) and upper (centre + m + 1)
+ * elements that lie on the ray.  Ld [n_tot], Lu / Ll [n_off_diag][n_tot] as
+ * feautrier_bands writes them (index n - first). */
+static void update_lambda_bands(const OrcModel* m, const Buf* b, uint32_t rr, uint32_t f, uint32_t K,
+                                const double* Ld, const double* Lu, const double* Ll, AloLists* a) {
+    if (!m->in_line_integral[f]) return;
+    const uint32_t c = b->centre, first = b->first, last = b->last, N = b->n_tot;
+    const uint32_t p   = b->nr[c];
+    const uint32_t lid = m->nrad_cum[m->corr_lspec[f]] + m->corr_k[f];
+    alo_add(a, m->nlines, p, lid, p, lambda_term(m, b, rr, f, c, Ld[c - first]));
+    for (uint32_t mm = 0; mm < K && mm + 1 < N; mm++) {
+        if (c >= first + mm + 1) {
+            const uint32_t n = c - mm - 1;
+            alo_add(a, m->nlines, p, lid, b->nr[n], lambda_term(m, b, rr, f, n, Ll[(size_t)mm * N + (n - first)]));
+        }
+        if (c + mm + 1 <= last) {
+            const uint32_t n = c + mm + 1;
+            alo_add(a, m->nlines, p, lid, b->nr[n], lambda_term(m, b, rr, f, n, Lu[(size_t)mm * N + (n - first)]));
+        }
+    }
+}
+
+int orc_formal_solve_fo2_alo(const OrcModel* m, uint32_t n_off_diag, double* J, uint32_t cap, uint32_t* alo_n,
+                             uint32_t* alo_nr, double* alo_ls, int nthreads) {
+    const uint32_t length = 2 * orc_ray_lengths_max(m, nthreads) + 1;
+    const uint32_t P = m->npoints, F = m->nfreqs, Q = m->nquads, L = m->nlines;
+    const uint32_t K = n_off_diag;
+    AloLists a = {cap, alo_n, alo_nr, alo_ls, 0};
+    memset(J, 0, sizeof(double) * (size_t)P * F);
+    memset(alo_n, 0, sizeof(uint32_t) * (size_t)P * L);
+    int err_any = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+    {
+        Buf b;
+        int bad = buf_init(&b, length);
+        double* Aw = (double*)calloc(length, sizeof(double));
+        double* Cw = (double*)calloc(length, sizeof(double));
+        double* Ld = (double*)calloc(length, sizeof(double));
+        double* Lu = (double*)calloc((size_t)(K ? K : 1) * length, sizeof(double));
+        double* Ll = (double*)calloc((size_t)(K ? K : 1) * length, sizeof(double));
+        if (!Aw || !Cw || !Ld || !Lu || !Ll) bad = 1;
+        for (uint32_t rr = 0; rr < m->hnrays; rr++) {
+            const uint32_t ar = m->antipod[rr];
+            for (uint32_t ls = 0; ls < m->nlspecs; ls++) {
+#pragma omp for schedule(dynamic, 16)
+                for (int64_t oo = 0; oo < (int64_t)P; oo++) {
+                    if (bad) continue;
+                    const uint32_t o = (uint32_t)oo;
+                    const uint32_t c = b.centre;
+                    b.nr[c]          = o;
+                    b.shift[c]       = 1.0;
+                    for (uint32_t k = 0; k < m->nrad[ls]; k++) {
+                        const uint32_t l = m->nrad_cum[ls] + k;
+                        int err          = 0;
+                        const int64_t first = trace(m, &b, 0, l, o, rr, -1, (int64_t)c - 1, (int64_t)c - 1, &err) + 1;
+                        const int64_t last  = trace(m, &b, 0, l, o, ar, +1, (int64_t)c + 1, (int64_t)c, &err) - 1;
+                        if (err) {
+#pragma omp atomic write
+                            err_any = 1;
+                            continue;
+                        }
+                        b.first = (uint32_t)first;
+                        b.last  = (uint32_t)last;
+                        b.n_tot = (uint32_t)(last + 1 - first);
+                        for (uint32_t q = 0; q < Q; q++) {
+                            const uint32_t f = l * Q + q;
+                            if (b.n_tot > 1) {
+                                solve_feautrier_order_2(m, &b, o, f, 1);
+                                J[(size_t)o * F + f] += b.Su[c] * 2.0 * ray_wt(m, o, rr);
+                                if (m->in_line_integral[f]) {
+                                    memset(Lu, 0, sizeof(double) * (size_t)(K ? K : 1) * b.n_tot);
+                                    memset(Ll, 0, sizeof(double) * (size_t)(K ? K : 1) * b.n_tot);
+                                    feautrier_bands(m, &b, o, f, K, Aw, Cw, Ld, Lu, Ll);
+                                    update_lambda_bands(m, &b, rr, f, K, Ld, Lu, Ll, &a);
+                                }
+                            } else {
+                                J[(size_t)o * F + f] +=
+                                    2.0 * ray_wt(m, o, rr) * boundary_intensity(m, o, m->nu[(size_t)o * F + f]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        buf_free(&b);
+        free(Aw);
+        free(Cw);
+        free(Ld);
+        free(Lu);
+        free(Ll);
+    }
+    if (err_any) return -2;
+    return a.overflow ? -4 : 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* Public traces                                                       */
 /* ------------------------------------------------------------------ */
 int orc_trace_ray_pair_for_line(const OrcModel* m, uint32_t o, uint32_t rr, uint32_t l, OrcRay* ray) {

@@ -198,12 +198,22 @@ typedef struct {
     const OrcColPar* colpar;
 } OrcSpecies;
 
+/* The formal solve with n_off_diag > 0 (solver.tpp:2319-2355) and the non-local ALO it
+ * builds (update_Lambda, solver.tpp:1760-1850; Lambda::add_element, lambda.tpp:74-86):
+ * J [P][F] and, per (point, line), alo_n[p][lid] elements (alo_nr, alo_ls)[p][lid][cap]
+ * in the reference's insertion order (the first is the point itself).  Returns -4 when
+ * a list would exceed cap (2 n_off_diag hnrays + 1 always suffices). */
+int orc_formal_solve_fo2_alo(const OrcModel* m, uint32_t n_off_diag, double* J, uint32_t cap, uint32_t* alo_n,
+                             uint32_t* alo_nr, double* alo_ls, int nthreads);
+
 /* Parameters of compute_level_populations (parameters.hpp:76-104). */
 typedef struct {
     double   pop_prec, min_rel_pop_for_convergence, convergence_fraction, population_inversion_fraction;
     double   min_line_opacity, min_line_emissivity;
     uint32_t Ng_acceleration_mem_limit, adaptive_Ng_acceleration_min_order, Ng_acceleration_remove_N_its;
     int32_t  use_adaptive_Ng_acceleration, adaptive_Ng_acceleration_use_max_criterion;
+    uint32_t n_off_diag;      /* parameters.hpp:66; > 0: non-local ALO, global rate system */
+    int32_t  global_stateq;   /* solve the global rate system also when n_off_diag = 0 */
 } OrcAliParams;
 
 /* Model::compute_Jeff (model.cpp:514-545) from J [P][F], the ALO diagonal lam [P][L]

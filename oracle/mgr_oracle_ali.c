@@ -59,6 +59,38 @@ static void jeff_species(const OrcModel* m, const OrcSpecies* s, const double* J
     free(nr_line);
 }
 
+/* Jeff with the non-local ALO (model.cpp:514-545): diff sums Ls * population of the
+ * emitting point's upper level over the (p, line) list, in list order. */
+static void jeff_species_alo(const OrcModel* m, const OrcSpecies* s, const double* J, uint32_t cap,
+                             const uint32_t* alo_n, const uint32_t* alo_nr, const double* alo_ls, const ld* pop,
+                             double* Jlin, double* Jeff, double* Jdif) {
+    const uint32_t P = m->npoints, L = m->nlines, Q = m->nquads, F = m->nfreqs;
+    uint32_t* nr_line = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)s->nrad * Q);
+    for (uint32_t g = 0; g < F; g++) {
+        const uint32_t lid = m->corr_line[g];
+        if (lid >= s->line_offset && lid < s->line_offset + s->nrad)
+            nr_line[(size_t)(lid - s->line_offset) * Q + m->corr_z[g]] = g;
+    }
+    for (uint32_t p = 0; p < P; p++)
+        for (uint32_t k = 0; k < s->nrad; k++) {
+            const uint32_t lid = s->line_offset + k;
+            const size_t key   = (size_t)p * L + lid;
+            double jl          = 0.0;
+            for (uint32_t z = 0; z < Q; z++) {
+                const uint32_t f = nr_line[(size_t)k * Q + z];
+                jl += m->quad_weights[(size_t)m->corr_lspec[f] * Q + z] * J[(size_t)p * F + f];
+            }
+            double diff = 0.0;
+            for (uint32_t i = 0; i < alo_n[key]; i++)
+                diff = (double)((ld)diff + (ld)alo_ls[key * cap + i] *
+                                               pop[(size_t)alo_nr[key * cap + i] * s->nlev + s->irad[k]]);
+            Jlin[(size_t)p * s->nrad + k] = jl;
+            Jeff[(size_t)p * s->nrad + k] = jl - HH_OVER_FOUR_PI_ALI * diff;
+            Jdif[(size_t)p * s->nrad + k] = HH_OVER_FOUR_PI_ALI * diff;
+        }
+    free(nr_line);
+}
+
 int orc_compute_jeff(const OrcModel* m, uint32_t nlspecs, const OrcSpecies* sp, const double* J, const double* lam,
                      double* const* pops, double* const* Jlin, double* const* Jeff, double* const* Jdif) {
     for (uint32_t l = 0; l < nlspecs; l++) {
@@ -221,6 +253,86 @@ static void rate_block(const OrcSpecies* s, const ld* pp, const double* Jeff, co
     }
     for (uint32_t i = 0; i < n; i++) ADD(last, i, 1.0L);
 #undef ADD
+}
+
+/* The global rate system of update_using_statistical_equilibrium
+ * (lineProducingSpecies.tpp:377-581) for every point at once: per point p its
+ * radiative triplets, the ALO triplets of each element (nr, Ls) of its (p, line) lists
+ * (row (p, lower) gains v at column (nr, upper); row (nr, upper) loses v on its
+ * diagonal, v = -Ls opacity(p, k) / frequency), the collisional triplets and the
+ * normalisation row, in that order, into a dense long-double matrix of order P nlev
+ * solved by Gaussian elimination with partial pivoting (the reference: Eigen
+ * SparseLU).  pp: populations before the solve; out: the solution. */
+static int stateq_global(const OrcSpecies* s, uint32_t P, uint32_t L, const ld* pp, const double* Jeff, uint32_t cap,
+                         const uint32_t* alo_n, const uint32_t* alo_nr, const double* alo_ls, const double* T,
+                         const double* abundance, uint32_t nspecs, const ld* tot, double min_line_opacity, ld* out) {
+    const uint32_t n = s->nlev, last = n - 1;
+    const size_t N = (size_t)P * n;
+    ld* M = (ld*)calloc(N * N, sizeof(ld));
+    ld* y = (ld*)calloc(N, sizeof(ld));
+    if (!M || !y) {
+        free(M);
+        free(y);
+        return -1;
+    }
+#define GADD(r, c, v) M[(size_t)(r) * N + (c)] += (v)
+    for (uint32_t p = 0; p < P; p++) {
+        const size_t o = (size_t)p * n;
+        for (uint32_t k = 0; k < s->nrad; k++) {
+            const ld Je = (ld)Jeff[(size_t)p * s->nrad + k];
+            const ld v_IJ = (ld)s->A[k] + (ld)s->Bs[k] * Je;
+            const ld v_JI = (ld)s->Ba[k] * Je;
+            const size_t I = o + s->irad[k], J = o + s->jrad[k];
+            if (s->jrad[k] != last) {
+                GADD(J, I, +v_IJ);
+                GADD(J, J, -v_JI);
+            }
+            if (s->irad[k] != last) {
+                GADD(I, J, +v_JI);
+                GADD(I, I, -v_IJ);
+            }
+        }
+        for (uint32_t k = 0; k < s->nrad; k++) {
+            const size_t key = (size_t)p * L + s->line_offset + k;
+            const double opac = opacity_of(s, pp + o, k, min_line_opacity);
+            for (uint32_t i = 0; i < alo_n[key]; i++) {
+                const ld v_IJ = -(ld)alo_ls[key * cap + i] * (ld)opac / (ld)s->frequency[k];
+                const size_t I = (size_t)alo_nr[key * cap + i] * n + s->irad[k], J = o + s->jrad[k];
+                if (s->jrad[k] != last) GADD(J, I, +v_IJ);
+                if (s->irad[k] != last) GADD(I, I, -v_IJ);
+            }
+        }
+        for (uint32_t c = 0; c < s->ncolpar; c++) {
+            const OrcColPar* cp = &s->colpar[c];
+            const double abn = partner_abundance(cp, T[p], abundance[(size_t)p * nspecs + cp->num_col_partner]);
+            double* cd = (double*)malloc(sizeof(double) * cp->ncol);
+            double* ce = (double*)malloc(sizeof(double) * cp->ncol);
+            collision_rates(cp, T[p], cd, ce);
+            for (uint32_t k = 0; k < cp->ncol; k++) {
+                const ld v_IJ = (ld)cd[k] * (ld)abn;
+                const ld v_JI = (ld)ce[k] * (ld)abn;
+                const size_t I = o + cp->icol[k], J = o + cp->jcol[k];
+                if (cp->jcol[k] != last) {
+                    GADD(J, I, +v_IJ);
+                    GADD(J, J, -v_JI);
+                }
+                if (cp->icol[k] != last) {
+                    GADD(I, J, +v_JI);
+                    GADD(I, I, -v_IJ);
+                }
+            }
+            free(cd);
+            free(ce);
+        }
+        for (uint32_t i = 0; i < n; i++) GADD(o + last, o + i, 1.0L);
+        y[o + last] = tot[p];
+    }
+#undef GADD
+    const int rc = solve_dense(M, y, (uint32_t)N);
+    for (size_t i = 0; i < N; i++) out[i] = y[i];
+    free(M);
+    free(y);
+    return rc;
 }
 
 int orc_stateq(const OrcSpecies* s, uint32_t P, const double* abundance, uint32_t nspecs, const double* temperature,
@@ -570,6 +682,18 @@ int orc_ali_run(OrcModel* m, double* em, double* op, double* crit, uint32_t nlsp
     }
     Ls = (double*)malloc(sizeof(double) * (ls_cap ? ls_cap : 1));
     set_line_data(m, em, op, crit, xs, nlspecs, prm);
+    /* n_off_diag > 0 (or global_stateq): ALO lists and the global rate system */
+    const int global = prm->n_off_diag > 0 || prm->global_stateq;
+    const uint32_t cap = 2 * prm->n_off_diag * m->hnrays + 1;
+    uint32_t* alo_n = NULL;
+    uint32_t* alo_nr = NULL;
+    double* alo_ls = NULL;
+    if (global) {
+        alo_n = (uint32_t*)calloc((size_t)P * L, sizeof(uint32_t));
+        alo_nr = (uint32_t*)calloc((size_t)P * L * cap, sizeof(uint32_t));
+        alo_ls = (double*)calloc((size_t)P * L * cap, sizeof(double));
+        if (!alo_n || !alo_nr || !alo_ls) rc = -1;
+    }
 
     int iteration = 0, iteration_normal = 0, some_not_converged = 1;
     long nerr = 0;
@@ -609,6 +733,32 @@ int orc_ali_run(OrcModel* m, double* em, double* op, double* crit, uint32_t nlsp
         }
         iteration++;
         some_not_converged = 0;
+        if (global) {
+            const int frc = orc_formal_solve_fo2_alo(m, prm->n_off_diag, J, cap, alo_n, alo_nr, alo_ls, nthreads);
+            if (frc != 0) rc = frc;
+            for (uint32_t l = 0; l < nlspecs; l++)
+                jeff_species_alo(m, xs[l].s, J, cap, alo_n, alo_nr, alo_ls, xs[l].pop, xs[l].Jlin, xs[l].Jeff,
+                                 xs[l].Jdif);
+            for (uint32_t l = 0; l < nlspecs && rc == 0; l++) {
+                Lsp* x = &xs[l];
+                memcpy(x->prev1, x->pop, sizeof(ld) * x->n);
+                residual_push(x);
+                if (stateq_global(x->s, P, L, x->prev1, x->Jeff, cap, alo_n, alo_nr, alo_ls, T, abundance, nspecs,
+                                  x->tot, prm->min_line_opacity, x->pop) != 0)
+                    rc = -3;
+                correct_negative(x, P, T, prm);
+                check_convergence(x, P, prm);
+            }
+            set_line_data(m, em, op, crit, xs, nlspecs, prm);
+            iteration_normal++;
+            for (uint32_t l = 0; l < nlspecs; l++) {
+                if (err_mean) err_mean[nerr] = xs[l].rcm;
+                if (err_max) err_max[nerr] = xs[l].rcmax;
+                nerr++;
+                if (xs[l].fnc > 1.0 - prm->convergence_fraction) some_not_converged = 1;
+            }
+            continue;
+        }
         if (orc_formal_solve_fo2(m, J, NULL, lam, NULL, nthreads) != 0) rc = -2;
         for (uint32_t l = 0; l < nlspecs; l++) jeff_species(m, xs[l].s, J, lam, xs[l].pop, xs[l].Jlin, xs[l].Jeff, xs[l].Jdif);
         for (uint32_t l = 0; l < nlspecs && rc == 0; l++) {
@@ -666,5 +816,8 @@ int orc_ali_run(OrcModel* m, double* em, double* op, double* crit, uint32_t nlsp
     free(J);
     free(lam);
     free(Ls);
+    free(alo_n);
+    free(alo_nr);
+    free(alo_ls);
     return rc == 0 ? iteration : rc;
 }

@@ -453,6 +453,27 @@ class Oracle:
             raise RuntimeError(f"oracle image_for_point failed ({rc})")
         return out
 
+    def formal_solve_fo2_alo(self, n_off_diag, nthreads=0):
+        """The formal solve with n_off_diag > 0 (solver.tpp:2319-2355) and its non-local
+        ALO (update_Lambda, solver.tpp:1760-1850): J [P][F] and the Lambda lists per
+        (point, line): n [P][L], nr / Ls [P][L][cap], in the reference's insertion order."""
+        l = lib()
+        l.orc_formal_solve_fo2_alo.restype = C.c_int
+        l.orc_formal_solve_fo2_alo.argtypes = [C.POINTER(OrcModel), C.c_uint32, _f64p, C.c_uint32,
+                                               C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), _f64p, C.c_int]
+        P, F, L = self.a["npoints"], self.a["nfreqs"], self.a["nlines"]
+        cap = 2 * n_off_diag * self.a["hnrays"] + 1
+        J = np.zeros((P, F))
+        n = np.zeros((P, L), np.uint32)
+        nr = np.zeros((P, L, cap), np.uint32)
+        ls = np.zeros((P, L, cap))
+        rc = l.orc_formal_solve_fo2_alo(C.byref(self.m), n_off_diag, _ptr(J, _f64p), cap,
+                                        n.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                        nr.ctypes.data_as(C.POINTER(C.c_uint32)), _ptr(ls, _f64p), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle formal_solve_fo2_alo failed ({rc})")
+        return dict(J=J, alo_n=n, alo_nr=nr, alo_ls=ls)
+
     def feautrier_bands(self, o, rr, f, n_off_diag):
         """Solver::solve_feautrier_order_2 with n_off_diag > 0 (solver.tpp:2319-2355) for one
         ray pair and frequency: A, C, L_diag [n_tot] and L_upper, L_lower [n_off_diag][n_tot]
@@ -523,7 +544,8 @@ class OrcAliParams(C.Structure):
                 ("min_line_opacity", C.c_double), ("min_line_emissivity", C.c_double),
                 ("Ng_acceleration_mem_limit", C.c_uint32), ("adaptive_Ng_acceleration_min_order", C.c_uint32),
                 ("Ng_acceleration_remove_N_its", C.c_uint32), ("use_adaptive_Ng_acceleration", C.c_int32),
-                ("adaptive_Ng_acceleration_use_max_criterion", C.c_int32)]
+                ("adaptive_Ng_acceleration_use_max_criterion", C.c_int32), ("n_off_diag", C.c_uint32),
+                ("global_stateq", C.c_int32)]
 
 
 # Defaults of src/model/parameters/parameters.hpp:76-103.
@@ -531,7 +553,9 @@ ALI_DEFAULTS = dict(pop_prec=1.0e-6, min_rel_pop_for_convergence=1.0e-10, conver
                     population_inversion_fraction=-1.0, min_line_opacity=1.0e-13, min_line_emissivity=1.0e-50,
                     Ng_acceleration_mem_limit=9, adaptive_Ng_acceleration_min_order=2,
                     Ng_acceleration_remove_N_its=0, use_adaptive_Ng_acceleration=1,
-                    adaptive_Ng_acceleration_use_max_criterion=1)
+                    adaptive_Ng_acceleration_use_max_criterion=1, n_off_diag=0,
+                    # the oracle's own switch: the global rate system also for n_off_diag = 0
+                    global_stateq=0)
 
 _ORTHO_PARA = {"n": 0, "o": 1, "p": 2}
 

@@ -218,3 +218,26 @@ def velocity_gradient_1d_image_solution(raw, nu, imx, imy):
 
     rs = np.sqrt(imx**2 + imy**2)
     return np.array([[I_im(f, r) for f in nu] for r in rs])
+
+
+def band_alo_error(alo_off, alo_nr, lam, ref):
+    """Largest difference between the non-local ALO of a banded solve in the library's
+    layout (alo_off / alo_nr [P][L][hnrays][2K] and the diagonal lam [P][L]) and the
+    oracle's Lambda lists (``Oracle.formal_solve_fo2_alo``: per (point, line) the
+    elements merged by point, Lambda::add_element), relative to the largest element of
+    each list.  Elements are compared per (point, line, element point) after summing
+    the library's slots that name the same point."""
+    P, L = lam.shape
+    worst = 0.0
+    for p in range(P):
+        for l in range(L):
+            mine = {p: lam[p, l]}
+            for v, q in zip(alo_off[p, l].ravel(), alo_nr[p, l].ravel()):
+                if v != 0.0:
+                    mine[int(q)] = mine.get(int(q), 0.0) + v
+            n = int(ref["alo_n"][p, l])
+            theirs = {int(ref["alo_nr"][p, l, i]): ref["alo_ls"][p, l, i] for i in range(n)}
+            scale = max([abs(v) for v in theirs.values()] + [1e-300])
+            for q in set(mine) | set(theirs):
+                worst = max(worst, abs(mine.get(q, 0.0) - theirs.get(q, 0.0)) / scale)
+    return worst

@@ -113,6 +113,10 @@ def test_core_model_compute_level_populations(gpu_lib):
     tot = raw.abundance[:, raw.linedata[0].num][:, None]
     assert _rel(pop, ref["populations"][0], 1e-10 * tot) < 1e-6
     assert len(model.error_max) == it
+    # device time of the phases of the captured iterations (formal solve, Jeff, rate
+    # equations and line data, Ng)
+    ph = list(model.ali_phase_times())
+    assert len(ph) == 4 and ph[0] > 0.0 and ph[1] > 0.0 and ph[2] > 0.0
     model.compute_radiation_field_feautrier_order_2()
     model.compute_Jeff()
     assert np.isfinite(np.array(model.lines.lineProducingSpecies[0].Jeff)).all()

@@ -85,3 +85,33 @@ def test_jeff_is_weighted_line_integral_minus_alo_part():
     HH_OVER_FOUR_PI = 6.62607004e-34 / (4.0 * np.pi)
     diff = res["lambda_diag"] * pops[0][:, ld.irad]
     np.testing.assert_allclose(out["Jeff"][0], Jlin - HH_OVER_FOUR_PI * diff, rtol=1e-12)
+
+
+def test_global_rate_system_with_diagonal_alo_is_the_block_solve():
+    """With n_off_diag = 0 the reference's global rate system (one sparse system over all
+    points, lineProducingSpecies.tpp:377-581) is block diagonal: the oracle's global
+    assembly and dense solve give the per-point block solve's populations."""
+    raw = S.grid_cube(n=6, nquads=5)
+    import helpers as H
+
+    block = O.AliOracle(raw, H.setup(raw)).run(use_ng=True, max_it=6, Ng_acceleration_mem_limit=4)
+    glob = O.AliOracle(raw, H.setup(raw)).run(use_ng=True, max_it=6, Ng_acceleration_mem_limit=4, global_stateq=1)
+    assert glob["iterations"] == block["iterations"]
+    np.testing.assert_allclose(glob["populations"][0], block["populations"][0], rtol=1e-12)
+
+
+@pytest.mark.parametrize("n_off_diag", [1, 2])
+def test_non_local_alo_changes_the_path_not_the_fixed_point(n_off_diag):
+    """The band elements of the ALO (n_off_diag > 0) change the first iterations'
+    populations (by ~1e-4 here) but not the converged ones (the ALO terms cancel at the
+    fixed point of the iteration)."""
+    raw = S.grid_cube(n=6, nquads=5)
+    import helpers as H
+
+    one_b = O.AliOracle(raw, H.setup(raw)).run(use_ng=False, max_it=1)
+    one_k = O.AliOracle(raw, H.setup(raw)).run(use_ng=False, max_it=1, n_off_diag=n_off_diag)
+    d1 = np.max(np.abs(one_k["populations"][0] / one_b["populations"][0] - 1.0))
+    assert d1 > 1e-5
+    conv_b = O.AliOracle(raw, H.setup(raw)).run(use_ng=False, max_it=30, pop_prec=1e-10)
+    conv_k = O.AliOracle(raw, H.setup(raw)).run(use_ng=False, max_it=30, pop_prec=1e-10, n_off_diag=n_off_diag)
+    np.testing.assert_allclose(conv_k["populations"][0], conv_b["populations"][0], rtol=1e-9)
