@@ -192,8 +192,9 @@ int mgr_formal_solve_fo2_anis(MgrModel* model, int precision, double* J, double*
  * Solver::setup (src/solver/solver.tpp:6-36). */
 int mgr_model_set_n_off_diag(MgrModel* model, uint32_t n_off_diag);
 
-/* The formal solve with the non-local ALO (n_off_diag > 0, FP64): J_dev [P][F], the ALO
- * diagonal lambda_diag_dev [P][L] as mgr_formal_solve_fo2_device writes it, and the
+/* The formal solve with the non-local ALO (n_off_diag > 0, FP64): J_dev [P][F], u_dev
+ * [hnrays][P][F] (may be NULL), the ALO diagonal lambda_diag_dev [P][L] as
+ * mgr_formal_solve_fo2_device writes them, and the
  * band elements alo_off_dev / alo_nr_dev [P][L][hnrays][2 n_off_diag]: for origin p,
  * line l and ray pair rr, slot m < n_off_diag the update_Lambda term (summed over the
  * line's quadrature points) of the element centre - m - 1 of the ray and slot
@@ -203,15 +204,16 @@ int mgr_model_set_n_off_diag(MgrModel* model, uint32_t n_off_diag);
  * src/model/lines/lineProducingSpecies/lambda/lambda.tpp:74-86), filled by
  * Solver::update_Lambda (src/solver/solver.tpp:1760-1850) from the banded inverse of
  * solve_feautrier_order_2 (solver.tpp:2319-2355).  Device pointers, model's stream. */
-int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* lambda_diag_dev, double* alo_off_dev,
-                                    uint32_t* alo_nr_dev);
+int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* u_dev, double* lambda_diag_dev,
+                                    double* alo_off_dev, uint32_t* alo_nr_dev);
 
-/* Host-buffer form of mgr_formal_solve_fo2_alo_device: J [P][F]; lambda_diag [P][L],
- * alo_off and alo_nr (same layouts) may be NULL.  The band elements stay on the device
+/* Host-buffer form of mgr_formal_solve_fo2_alo_device: J [P][F]; u [hnrays][P][F],
+ * lambda_diag [P][L], alo_off and alo_nr (same layouts) may be NULL.  The band elements stay on the device
  * (model scratch) for a following mgr_compute_jeff, as the reference's Lambda lists
  * do for compute_Jeff.  Replaces Model::compute_radiation_field_feautrier_order_2
  * (src/model/model.cpp:353-390) with parameters->n_off_diag > 0. */
-int mgr_formal_solve_fo2_alo(MgrModel* model, double* J, double* lambda_diag, double* alo_off, uint32_t* alo_nr);
+int mgr_formal_solve_fo2_alo(MgrModel* model, double* J, double* u, double* lambda_diag, double* alo_off,
+                             uint32_t* alo_nr);
 
 /* Partial formal solve over the ray pairs [rr_begin, rr_end) only: J_dev [P][F] and
  * lambda_diag_dev [P][L] (may be NULL) receive the sums over those ray pairs, so that

@@ -98,8 +98,9 @@ SIGNATURES = {
     "mgr_formal_solve_fo2_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_formal_solve_fo2_rays": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, _f64p, _f64p]),
     "mgr_model_set_n_off_diag": (C.c_int, [C.c_void_p, C.c_uint32]),
-    "mgr_formal_solve_fo2_alo_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
-    "mgr_formal_solve_fo2_alo": (C.c_int, [C.c_void_p, _f64p, _f64p, _f64p, _u32p]),
+    "mgr_formal_solve_fo2_alo_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p]),
+    "mgr_formal_solve_fo2_alo": (C.c_int, [C.c_void_p, _f64p, _f64p, _f64p, _f64p, _u32p]),
     "mgr_formal_solve_fo2_rays_device": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p,
                                                    C.c_void_p]),
     "mgr_set_ray_shard": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, REDUCE_FN, C.c_void_p, C.c_int]),
@@ -372,8 +373,8 @@ class DeviceModel:
         self.n_off_diag = int(n_off_diag)
 
     def formal_solve_fo2_alo(self):
-        """The banded FP64 formal solve (n_off_diag > 0): J [P][F], the ALO diagonal
-        [P][L] and the band elements alo_off / alo_nr [P][L][hnrays][2 n_off_diag]."""
+        """The banded FP64 formal solve (n_off_diag > 0): J [P][F], u [hnrays][P][F], the
+        ALO diagonal [P][L] and the band elements alo_off / alo_nr [P][L][hnrays][2 n_off_diag]."""
         import torch
 
         K = getattr(self, "n_off_diag", 0)
@@ -382,11 +383,13 @@ class DeviceModel:
         lam = torch.empty((self.P, self.L), dtype=torch.float64, device=dev)
         off = torch.empty((self.P, self.L, self.R, 2 * max(K, 1)), dtype=torch.float64, device=dev)
         nr = torch.empty((self.P, self.L, self.R, 2 * max(K, 1)), dtype=torch.int32, device=dev)
+        u = torch.empty((self.R, self.P, self.F), dtype=torch.float64, device=dev)
         torch.cuda.synchronize(dev)
-        _check(load().mgr_formal_solve_fo2_alo_device(self.h, C.c_void_p(J.data_ptr()), C.c_void_p(lam.data_ptr()),
-                                                      C.c_void_p(off.data_ptr()), C.c_void_p(nr.data_ptr())))
+        _check(load().mgr_formal_solve_fo2_alo_device(self.h, C.c_void_p(J.data_ptr()), C.c_void_p(u.data_ptr()),
+                                                      C.c_void_p(lam.data_ptr()), C.c_void_p(off.data_ptr()),
+                                                      C.c_void_p(nr.data_ptr())))
         self.sync()
-        return dict(J=J.cpu().numpy(), lambda_diag=lam.cpu().numpy(), alo_off=off.cpu().numpy(),
+        return dict(J=J.cpu().numpy(), u=u.cpu().numpy(), lambda_diag=lam.cpu().numpy(), alo_off=off.cpu().numpy(),
                     alo_nr=nr.cpu().numpy().view(np.uint32))
 
     def ray_statistics(self):

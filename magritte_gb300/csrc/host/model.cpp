@@ -549,11 +549,10 @@ int Model::compute_radiation_field_feautrier_order_2() {
     if (parameters.store_u) radiation.u.resize({R, P, F});
     std::vector<double> lam((size_t)P * L);
     if (parameters.n_off_diag > 0) {
-        // the banded solve (FP64): J, the diagonal, and the band elements kept on the
+        // the banded solve (FP64): J, u, the diagonal, and the band elements kept on the
         // device for compute_Jeff (solver.tpp:2319-2355, :1760-1850)
-        if (parameters.store_u)
-            throw std::runtime_error("store_u with n_off_diag > 0: the banded solve does not return u");
-        check(mgr_formal_solve_fo2_alo(dev, radiation.J.data(), lam.data(), nullptr, nullptr));
+        check(mgr_formal_solve_fo2_alo(dev, radiation.J.data(), parameters.store_u ? radiation.u.data() : nullptr,
+                                       lam.data(), nullptr, nullptr));
     } else {
         check(mgr_formal_solve_fo2(dev, parameters.precision, radiation.J.data(),
                                    parameters.store_u ? radiation.u.data() : nullptr, lam.data()));

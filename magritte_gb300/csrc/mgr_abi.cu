@@ -578,8 +578,8 @@ int mgr_model_set_n_off_diag(MgrModel* model, uint32_t n_off_diag) {
     return MGR_OK;
 }
 
-int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* lambda_diag_dev, double* alo_off_dev,
-                                    uint32_t* alo_nr_dev) {
+int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* u_dev, double* lambda_diag_dev,
+                                    double* alo_off_dev, uint32_t* alo_nr_dev) {
     MGR_MODEL_DEVICE(model);
     if (!model || !J_dev || !lambda_diag_dev || !alo_off_dev || !alo_nr_dev) {
         set_error("mgr_formal_solve_fo2_alo_device: null argument");
@@ -596,7 +596,7 @@ int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* lamb
     const size_t wb = fo2_work_bytes(model, model->dm.P, true, true);
     int rc = ensure_scratch(model, &model->work, &model->work_bytes, wb);
     if (rc != MGR_OK) return rc;
-    cudaError_t e = launch_fo2_range(model, MGR_PRECISION_FP64, 0, model->dm.P, J_dev, nullptr, lambda_diag_dev,
+    cudaError_t e = launch_fo2_range(model, MGR_PRECISION_FP64, 0, model->dm.P, J_dev, u_dev, lambda_diag_dev,
                                      model->work, model->work_bytes, 0, 0xffffffffu, nullptr, nullptr, nullptr,
                                      alo_off_dev, alo_nr_dev);
     if (e != cudaSuccess) return cuda_fail(e, "banded formal solve launch");
@@ -607,7 +607,8 @@ int mgr_formal_solve_fo2_alo_device(MgrModel* model, double* J_dev, double* lamb
     return MGR_OK;
 }
 
-int mgr_formal_solve_fo2_alo(MgrModel* model, double* J, double* lambda_diag, double* alo_off, uint32_t* alo_nr) {
+int mgr_formal_solve_fo2_alo(MgrModel* model, double* J, double* u, double* lambda_diag, double* alo_off,
+                             uint32_t* alo_nr) {
     MGR_MODEL_DEVICE(model);
     if (!model || !J) {
         set_error("mgr_formal_solve_fo2_alo: null argument");
@@ -620,11 +621,15 @@ int mgr_formal_solve_fo2_alo(MgrModel* model, double* J, double* lambda_diag, do
     if (rc == MGR_OK) rc = ensure_scratch(model, &model->lam_scratch, &model->lam_scratch_bytes, PL * 8);
     if (rc == MGR_OK) rc = ensure_scratch(model, &model->alo_scratch, &model->alo_scratch_bytes, nalo * 8);
     if (rc == MGR_OK) rc = ensure_scratch(model, &model->alo_nr_scratch, &model->alo_nr_scratch_bytes, nalo * 4);
+    if (rc == MGR_OK && u) rc = ensure_scratch(model, &model->u_scratch, &model->u_scratch_bytes, PF * dm.hnrays * 8);
     if (rc != MGR_OK) return rc;
     uint32_t* nr_dev = reinterpret_cast<uint32_t*>(model->alo_nr_scratch);
-    rc = mgr_formal_solve_fo2_alo_device(model, model->J_scratch, model->lam_scratch, model->alo_scratch, nr_dev);
+    rc = mgr_formal_solve_fo2_alo_device(model, model->J_scratch, u ? model->u_scratch : nullptr, model->lam_scratch,
+                                         model->alo_scratch, nr_dev);
     if (rc != MGR_OK) return rc;
     cudaError_t e = cudaMemcpyAsync(J, model->J_scratch, PF * 8, cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess && u)
+        e = cudaMemcpyAsync(u, model->u_scratch, PF * dm.hnrays * 8, cudaMemcpyDeviceToHost, model->stream);
     if (e == cudaSuccess && lambda_diag)
         e = cudaMemcpyAsync(lambda_diag, model->lam_scratch, PL * 8, cudaMemcpyDeviceToHost, model->stream);
     if (e == cudaSuccess && alo_off)

@@ -4,12 +4,13 @@
 // descriptions into one device array and solves all of them with one kernel launch.
 // The unit of work is one (model, origin) item handled by one warp: the warp traces
 // and solves every ray pair of its origin in turn (lanes over frequencies, the same
-// solve_lane code as the single-model kernel) and keeps J and the ALO diagonal of the
-// origin in shared memory, summed in the reference's order (ray pair outer,
-// quadrature point inner; Solver::solve_feautrier_order_2, solver.tpp:476-540, and
-// Lambda via update_Lambda, solver.tpp:1760-1850).  Every model's J and ALO diagonal
-// are therefore the values its own mgr_formal_solve_fo2 returns, bit for bit, with no
-// staging of per-ray results in HBM.
+// solve_lane code as the single-model kernel) and keeps J and the ALO elements of the
+// origin in shared memory per frequency, summed over the ray pairs in order
+// (Solver::solve_feautrier_order_2, solver.tpp:476-540, and update_Lambda,
+// solver.tpp:1760-1850); each line's ALO diagonal is then the sum of its quadrature
+// points' sums across the lanes, the association fo2_reduce_kernel uses.  Every
+// model's J and ALO diagonal are therefore the values its own mgr_formal_solve_fo2
+// returns, bit for bit, with no staging of per-ray results in HBM.
 //
 // Items are ordered model by model; warps take them in a grid-stride loop over a
 // persistent grid, so models finish roughly in submission order.  Per model the
@@ -49,8 +50,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Per-warp shared memory: sorted line centres [L_max], J accumulators [F_max], the
-// current ray pair's L_diag values [F_max], the origin's ray-independent ALO factors
+// Per-warp shared memory: sorted line centres [L_max], J accumulators [F_max], ALO
+// accumulators per frequency [F_max], the origin's ray-independent ALO factors
 // [F_max] (LambdaFactors), then the two trace halves.
 __host__ __device__ inline size_t batch_head_bytes(uint32_t F_max, uint32_t L_max) {
     const size_t head = ((size_t)L_max + 2 * (size_t)F_max) * 8 + (size_t)F_max * sizeof(LambdaFactors);
@@ -73,8 +74,8 @@ __global__ void __launch_bounds__(256, MINB)
     unsigned char* base = smem + (size_t)w * batch_warp_bytes(cap, F_max, L_max);
     double* sl = reinterpret_cast<double*>(base);
     double* Jacc = sl + L_max;
-    double* LDr = Jacc + F_max;
-    LambdaFactors* LF = reinterpret_cast<LambdaFactors*>(LDr + F_max);
+    double* Lacc = Jacc + F_max;
+    LambdaFactors* LF = reinterpret_cast<LambdaFactors*>(Lacc + F_max);
     HalfSmem bk, fw;
     carve_halves(base + batch_head_bytes(F_max, L_max), cap, bk, fw);
     if (threadIdx.x == 0) atomicMin(&tstamp[2 * n_models], global_ns());
@@ -89,8 +90,10 @@ __global__ void __launch_bounds__(256, MINB)
         const uint32_t o = (uint32_t)(item - offsets[mi]);
         if (lane == 0 && o == 0) tstamp[2 * mi] = global_ns();  // origins start in order
         for (uint32_t i = lane; i < m.L; i += 32) sl[i] = m.sorted_line[i];
-        for (uint32_t f = lane; f < m.F; f += 32) Jacc[f] = 0.0;
-        double lam_acc = 0.0;  // lane l: ALO diagonal of line l (l < 32), lines >= 32 in the loop below
+        for (uint32_t f = lane; f < m.F; f += 32) {
+            Jacc[f] = 0.0;
+            Lacc[f] = 0.0;
+        }
         bool ok = true;
         const bool want_lam = Lout[mi] != nullptr;
         __syncwarp();
@@ -113,39 +116,32 @@ __global__ void __launch_bounds__(256, MINB)
                     const LaneCtx c = lane_ctx(m, o, f);
                     const LaneResult r = solve_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
                     Jacc[f] += r.u * 2.0 * w2;
-                    LDr[f] = r.solved ? r.Ldiag : 0.0;
+                    // the frequency's ALO elements over the ray pairs in order
+                    if (want_lam && r.solved && m.in_line[f]) Lacc[f] += lambda_element(LF[f], w2, r.Ldiag);
                     if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
                 }
             }
             __syncwarp();
-            if (want_lam) {
-                // line l: lane q holds the element of quadrature point q, added in q order
-                for (uint32_t l = 0; l < m.L; l++) {
-                    const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
-                    double s = __shfl_sync(FULL_MASK, lam_acc, l & 31);
-                    if (l >= 32) s = rr ? Lout[mi][(size_t)o * m.L + l] : 0.0;  // running sum kept in the output
-                    for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
-                        const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
-                        const bool valid = f != 0xffffffffu && m.in_line[f];
-                        double e = 0.0;
-                        if (valid) e = lambda_element(LF[f], w2, LDr[f]);
-                        const uint32_t nq = min(32u, m.Q - q0);
-                        for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
-                    }
-                    if (l < 32) {
-                        if (lane == (int)l) lam_acc = s;
-                    } else {
-                        __syncwarp();
-                        if (lane == 0) Lout[mi][(size_t)o * m.L + l] = s;
-                    }
-                    __syncwarp();
-                }
-            }
         }
         if (ok) {
             double* J = Jout[mi] + (size_t)o * m.F;
             for (uint32_t f = lane; f < m.F; f += 32) J[f] = Jacc[f];
-            if (want_lam && lane < m.L) Lout[mi][(size_t)o * m.L + lane] = lam_acc;
+            if (want_lam)
+                // line l: its quadrature points' sums, lane by lane, then across the lanes
+                // (fo2_reduce_kernel's association)
+                for (uint32_t l = 0; l < m.L; l++) {
+                    const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
+                    double s = 0.0;
+                    for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
+                        const uint32_t q = q0 + lane;
+                        const uint32_t f = q < m.Q ? l2f[q] : 0xffffffffu;
+                        if (f == 0xffffffffu || !m.in_line[f]) continue;
+                        s += Lacc[f];
+                    }
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(FULL_MASK, s, off);
+                    if (lane == 0) Lout[mi][(size_t)o * m.L + l] = s;
+                }
         }
         __syncwarp();
         if (lane == 0) {

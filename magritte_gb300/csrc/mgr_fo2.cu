@@ -309,13 +309,22 @@ __global__ void __launch_bounds__(256, 2)
 }
 
 // ---------------------------------------------------------------------------------
-// Formal solve, stage 2: J and the ALO diagonal per origin, summed over ray pairs in
-// the reference's order (ray pair outer, quadrature point inner):
-//   J(o, f)   = sum_rr u(rr, o, f) 2 w_rr                               (solver.tpp:497-504)
-//   Lambda(o, l) = sum_rr sum_q lambda_element(o, rr, f(l, q))          (update_Lambda)
-// One CTA per origin (grid-stride); J by threads over f, the ALO by warps over lines
-// with lanes over quadrature points.  lq2f[l * Q + q] is the frequency of (l, q).
+// Formal solve, stage 2: J and the ALO diagonal per origin.
+//   J(o, f)      = sum_rr u(rr, o, f) 2 w_rr, in ray-pair order       (solver.tpp:497-504)
+//   Lambda(o, l) = sum_q sum_rr lambda_element(o, rr, f(l, q))         (update_Lambda)
+// One CTA per origin (grid-stride); J by threads over f; the line integrals (ALO,
+// memory-lean J, anisotropic sums) by warps over lines, lane q summing its quadrature
+// point over the ray pairs in order and the warp then summing its lanes by a butterfly
+// (so every FP64 instruction does the work of all lanes; the reference's own order
+// is rr outer, q inner, a different association of the same terms).
+// lq2f[l * Q + q] is the frequency of (l, q).
 // ---------------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL_MASK, v, off);
+    return v;
+}
+
 __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_begin, uint32_t o_end,
                                                          uint32_t rr0, uint32_t nR,
                                                          const double* __restrict__ U, size_t u_stride, uint32_t u_o0,
@@ -337,58 +346,64 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
         }
         if (Jlin) {
             // line-integrated J of the memory-lean solve (solve_feautrier_order_2_sparse,
-            // solver.tpp:297-363): J(o, l) += w_z (2 w_rr) u in (rr, z) order
+            // solver.tpp:297-363): J(o, l) = sum of w_z (2 w_rr) u over (rr, z)
             for (uint32_t l = w; l < m.L; l += nw) {
                 const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
                 double s = 0.0;
-                for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
-                    const double* Ur = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
-                    const double wt = ray_w(m, o, rr) * 2.0;
-                    for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
-                        const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
-                        const double e =
-                            f != 0xffffffffu ? (m.quad_w[(size_t)m.corr_lspec[f] * m.Q + q0 + lane] * wt) * Ur[f] : 0.0;
-                        const uint32_t nq = min(32u, m.Q - q0);
-                        for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
-                    }
+                for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    if (q >= m.Q) continue;
+                    const uint32_t f = l2f[q];
+                    const double wz = m.quad_w[(size_t)m.corr_lspec[f] * m.Q + q];
+                    double part = 0.0;
+                    for (uint32_t rr = rr0; rr < rr0 + nR; rr++)
+                        part += (wz * (ray_w(m, o, rr) * 2.0)) *
+                                U[(size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F + f];
+                    s += part;
                 }
+                s = warp_sum(s);
                 if (lane == 0) Jlin[(size_t)o * m.L + l] = s;
             }
         }
         if (anis) {
             // line-integrated J and anisotropy tensor elements (solve_feautrier_order_2_anis,
-            // solver.tpp:366-456): du = w_z w_rr u, J += 2 du, J2_x += wt_x(n) du, in (rr, z) order
+            // solver.tpp:366-456): du = w_z w_rr u, J += 2 du, J2_x += wt_x(n) du over (rr, z)
             const double sqrt3 = sqrt(3.0), inv_sqrt2 = 1.0 / sqrt(2.0);
             const size_t PL = (size_t)m.P * m.L;
             for (uint32_t l = w; l < m.L; l += nw) {
                 const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
                 double sJ = 0.0, s0 = 0.0, s1r = 0.0, s1i = 0.0, s2r = 0.0, s2i = 0.0;
-                for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
-                    const double* Ur = U + (size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F;
-                    const double wt = ray_w(m, o, rr);
-                    const double* dn = ray_dir(m, o, rr);
-                    const double nx = dn[0], ny = dn[1], nz = dn[2];
-                    const double wt_0 = inv_sqrt2 * (3.0 * nz * nz - 1.0);
-                    const double wt_1_Re = -sqrt3 * nx * nz;
-                    const double wt_1_Im = -sqrt3 * ny * nz;
-                    const double wt_2_Re = 0.5 * sqrt3 * (nx * nx - ny * ny);
-                    const double wt_2_Im = sqrt3 * nx * ny;
-                    for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
-                        const uint32_t f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
-                        const double du =
-                            f != 0xffffffffu ? (m.quad_w[(size_t)m.corr_lspec[f] * m.Q + q0 + lane] * wt) * Ur[f] : 0.0;
-                        const uint32_t nq = min(32u, m.Q - q0);
-                        for (uint32_t j = 0; j < nq; j++) {
-                            const double d = __shfl_sync(FULL_MASK, du, j);
-                            sJ += 2.0 * d;
-                            s0 += wt_0 * d;
-                            s1r += wt_1_Re * d;
-                            s1i += wt_1_Im * d;
-                            s2r += wt_2_Re * d;
-                            s2i += wt_2_Im * d;
-                        }
+                for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    if (q >= m.Q) continue;
+                    const uint32_t f = l2f[q];
+                    const double wz = m.quad_w[(size_t)m.corr_lspec[f] * m.Q + q];
+                    double pJ = 0.0, p0 = 0.0, p1r = 0.0, p1i = 0.0, p2r = 0.0, p2i = 0.0;
+                    for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
+                        const double* dn = ray_dir(m, o, rr);
+                        const double nx = dn[0], ny = dn[1], nz = dn[2];
+                        const double d =
+                            (wz * ray_w(m, o, rr)) * U[(size_t)(rr - rr0) * u_stride + (size_t)(o - u_o0) * m.F + f];
+                        pJ += 2.0 * d;
+                        p0 += (inv_sqrt2 * (3.0 * nz * nz - 1.0)) * d;
+                        p1r += (-sqrt3 * nx * nz) * d;
+                        p1i += (-sqrt3 * ny * nz) * d;
+                        p2r += (0.5 * sqrt3 * (nx * nx - ny * ny)) * d;
+                        p2i += (sqrt3 * nx * ny) * d;
                     }
+                    sJ += pJ;
+                    s0 += p0;
+                    s1r += p1r;
+                    s1i += p1i;
+                    s2r += p2r;
+                    s2i += p2i;
                 }
+                sJ = warp_sum(sJ);
+                s0 = warp_sum(s0);
+                s1r = warp_sum(s1r);
+                s1i = warp_sum(s1i);
+                s2r = warp_sum(s2r);
+                s2i = warp_sum(s2i);
                 if (lane == 0) {
                     const size_t i = (size_t)o * m.L + l;
                     anis[i] = sJ;
@@ -402,29 +417,22 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
         }
         if (!lam) continue;
         for (uint32_t l = w; l < m.L; l += nw) {
-            // Lane q holds the ray-independent factors of quadrature point q (computed
-            // once when Q <= 32, per ray pair otherwise); each ray pair's elements are
-            // added lane by lane, i.e. in (rr, q) order.
+            // lane q: the ray-independent factors of quadrature point q, then its elements
+            // over the ray pairs in order
             const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
-            const bool once = m.Q <= 32;
-            LambdaFactors k{0.0, 0.0, 0.0, 0.0};
-            uint32_t f = lane < m.Q ? l2f[lane] : 0xffffffffu;
-            bool valid = f != 0xffffffffu && m.in_line[f];
-            if (once && valid) k = lambda_factors(m, m.sorted_line, o, f);
             double s = 0.0;
-            for (uint32_t rr = rr0; rr < rr0 + nR; rr++) {
-                const double* Lr = LD + (size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F;
-                for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
-                    if (!once) {
-                        f = q0 + lane < m.Q ? l2f[q0 + lane] : 0xffffffffu;
-                        valid = f != 0xffffffffu && m.in_line[f];
-                        if (valid) k = lambda_factors(m, m.sorted_line, o, f);
-                    }
-                    const double e = valid ? lambda_element(k, ray_w(m, o, rr), Lr[f]) : 0.0;
-                    const uint32_t nq = min(32u, m.Q - q0);
-                    for (uint32_t j = 0; j < nq; j++) s += __shfl_sync(FULL_MASK, e, j);
-                }
+            for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
+                const uint32_t q = q0 + lane;
+                const uint32_t f = q < m.Q ? l2f[q] : 0xffffffffu;
+                if (f == 0xffffffffu || !m.in_line[f]) continue;
+                const LambdaFactors k = lambda_factors(m, m.sorted_line, o, f);
+                double part = 0.0;
+                for (uint32_t rr = rr0; rr < rr0 + nR; rr++)
+                    part += lambda_element(k, ray_w(m, o, rr),
+                                           LD[(size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F + f]);
+                s += part;
             }
+            s = warp_sum(s);
             if (lane == 0) lam[(size_t)o * m.L + l] = s;
         }
     }

@@ -561,8 +561,8 @@ def nlte_sphere(npoints: int = 500_000, nside: int = 4, nlev: int = 10, nquads: 
                 v_out: float = 15.0e3, v_turb: float = 150.0, nside_in: int = 4, nside_out: int = 16) -> RawModel:
     """The non-LTE ALI workload: ``npoints`` interior points with number density
     ~ r^-2 (uniform in r) between r_in and r_out, HEALPix boundary shells (CMB) at
-    r_in (nside_in) and r_out (nside_out), Delaunay neighbours, 12 nside^2 rays,
-    a 10-level linear rotor (B = 57.6 GHz, A_10 = 7.2e-8 /s, 28 amu) with one seeded
+    r_in (nside_in) and r_out (nside_out), interior points on the convex hull also
+    boundary points, Delaunay neighbours, 12 nside^2 rays, a 10-level linear rotor (B = 57.6 GHz, A_10 = 7.2e-8 /s, 28 amu) with one seeded
     collision partner (H2), n_H2 = nH2_in (r_in/r)^2, X_mol = 1e-6, outward wind
     ``v_out``, v_turb 150 m/s.  The workload does not fix the temperature; it is
     T = 100 K (r/r_in)^-0.4, at least 10 K."""
@@ -575,6 +575,13 @@ def nlte_sphere(npoints: int = 500_000, nside: int = 4, nlev: int = 10, nquads: 
     position = np.concatenate([inner, r[:, None] * d, outer])
     P = position.shape[0]
     b2p = np.concatenate([np.arange(len(inner)), np.arange(P - len(outer), P)]).astype(np.uint32)
+    # interior points just below r_out can stick out of the outer shell's flat faces and
+    # so lie on the convex hull, where a ray leaves the Delaunay mesh: they are boundary
+    # points too (appended after the shells)
+    from scipy.spatial import ConvexHull
+
+    hull = np.setdiff1d(ConvexHull(position).vertices, b2p)
+    b2p = np.concatenate([b2p, np.sort(hull)]).astype(np.uint32)
     rs = np.linalg.norm(position, axis=1)
     nH2 = nH2_in * (r_in / rs) ** 2
     velocity = (v_out / CC) * position / rs[:, None]

@@ -59,9 +59,10 @@ def test_banded_solve_matches_oracle(gpu_lib, name, n_off_diag):
                 mine = set(out["alo_nr"][p, l][out["alo_off"][p, l] != 0.0].tolist()) | {p}
                 theirs = set(ref["alo_nr"][p, l, :ref["alo_n"][p, l]].tolist())
                 assert mine <= theirs | {p}, (p, l)
-        # the ordinary FP64 solve: the same J and diagonal
-        plain = dev.formal_solve_fo2("fp64")
+        # the ordinary FP64 solve: the same J, u and diagonal
+        plain = dev.formal_solve_fo2("fp64", want_u=True)
         assert H.max_rel(plain["J"], out["J"]) < 1e-13
+        assert H.max_rel(plain["u"], out["u"]) < 1e-13
         has = plain["lambda_diag"] != 0.0
         assert H.max_rel(out["lambda_diag"][has], plain["lambda_diag"][has]) < 1e-13
     finally:

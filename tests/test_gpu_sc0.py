@@ -43,6 +43,10 @@ def test_shortchar_matches_oracle(gpu_lib, model, approx):
     try:
         g = dev.formal_solve_sc0("fp64", want_I=True, want_uv=True)
         assert _wing_rel(g["J"], ref["J"]) < 1e-5
+        # the plain relative error, wings included, stated beside the floored one
+        plain = H.max_rel(g["J"], ref["J"])
+        print(f"sc0 {model} {approx}: max rel err J plain {plain:.3e}, line-peak floored {_wing_rel(g['J'], ref['J']):.3e}")
+        assert plain < 1e-2
         for k in ("I", "u"):  # single rays: the amplified libm noise is not averaged over directions
             assert _wing_rel(g[k], ref[k]) < 1e-4, k
         # v = (I(rr) - I(ar))/2 cancels: compare on the scale of the intensities
