@@ -374,6 +374,14 @@ int mgr_image_new_adjoint_device(MgrModel* model, const double* raydir, uint32_t
  * widths changed (Model::compute_spectral_discretisation, model.cpp:70-161). */
 int mgr_model_set_frequencies_device(MgrModel* model, const double* nu_dev);
 
+/* Puts the host's velocities (v/c, [P][3]) and frequencies nu [P][F] back on the
+ * device if mgr_model_set_velocity_device or mgr_model_set_frequencies_device replaced
+ * them since the model was created or last restored; otherwise does nothing.  A host
+ * model that keeps its device copy between calls (the reference's Model methods run on
+ * the model's own fields, model.cpp:353-390) calls it before a solve, so that a
+ * differentiable solve run on the same device copy in between leaves no trace. */
+int mgr_model_restore_inputs(MgrModel* model, const double* velocity, const double* nu);
+
 /* Smooth J_dev [P][F]: J(o, f) = sum_rr 2 w_rr u(rr, o, f) in ray-pair order. */
 int mgr_formal_solve_fo2_smooth_device(MgrModel* model, const uint32_t* origins_dev, uint32_t n_origins,
                                        double* J_dev);
@@ -432,13 +440,17 @@ int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_read
 
 /* Launch shape of the formal-solve kernel for one precision mode: the register budget
  * (min_blocks_per_sm = 2, 3 or 4 CTAs of 256 threads per SM; 0 keeps the current value)
- * and warps per CTA (1..8; 0 keeps it).  Results do not depend on either; they are
+ * and warps per CTA for that precision (1..8; 0 keeps it).  Results do not depend on either; they are
  * picked by magritte_gb300.autotune for a given model. */
 int mgr_set_tuning(MgrModel* model, int precision, int min_blocks_per_sm, int warps_per_block);
 
 /* Time every launch shape of the formal-solve kernel for `precision` on a sample of
- * `sample_points` origins of this model (0 = 16384) and keep the fastest.  Outputs
- * may be NULL.  Blocks until done. */
+ * `sample_points` origins of this model (0 = 16384) and keep the fastest.  The shape
+ * is also remembered for the model's device and that precision: models created later
+ * in the process start from it (a fresh upload of the same model reuses the tuning).
+ * Without a tuning a model starts from the shapes measured fastest on GB300 for the
+ * 64^3 benchmark model (split: 4 CTAs x 8 warps, FP64: 2 CTAs x 4 warps).  Outputs may
+ * be NULL.  Blocks until done. */
 int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int* best_min_blocks,
                      int* best_warps, float* best_ms);
 

@@ -154,6 +154,7 @@ SIGNATURES = {
     "mgr_model_stream": (C.c_void_p, [C.c_void_p]),
     "mgr_launch_count": (C.c_uint64, []),
     "mgr_model_set_frequencies_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mgr_model_restore_inputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_formal_solve_fo2_smooth_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "mgr_formal_solve_fo2_adjoint_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

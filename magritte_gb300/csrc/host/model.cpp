@@ -498,6 +498,9 @@ MgrModel* Model::device_model() {
     }
     const uint64_t sig = signature();
     if (dev_ && sig == dev_signature_) {
+        // a differentiable solve or imager (velocities, frequencies and line data set
+        // from device tensors) may have run on this device copy since the last call
+        check(mgr_model_restore_inputs(dev_, geometry.points.velocity.data(), radiation.frequencies.nu.data()));
         check(mgr_model_set_line_data(dev_, lines.emissivity.data(), lines.opacity.data(), lines.inverse_width.data(),
                                       crit_.data()));
         return dev_;

@@ -132,6 +132,33 @@ cudaError_t erf_band_table(const float** out) {
     return cudaSuccess;
 }
 
+// Formal-solve launch shapes last picked by mgr_autotune_fo2, per device and precision
+// (0: none yet): models created later in the process start from them.
+static std::mutex g_tuned_mutex;
+static int g_tuned[64][2][2] = {};
+
+static void remember_tuned_shape(int dev, int precision, int minb, int warps) {
+    if (dev < 0 || dev >= 64) return;
+    std::lock_guard<std::mutex> lock(g_tuned_mutex);
+    const int k = precision == MGR_PRECISION_SPLIT ? 1 : 0;
+    g_tuned[dev][k][0] = minb;
+    g_tuned[dev][k][1] = warps;
+}
+
+static void apply_tuned_shapes(MgrModel* m) {
+    if (m->device < 0 || m->device >= 64) return;
+    std::lock_guard<std::mutex> lock(g_tuned_mutex);
+    const int(*t)[2] = g_tuned[m->device];
+    if (t[0][0]) {
+        m->fo2_minb_fp64 = t[0][0];
+        m->fo2_warps_fp64 = t[0][1];
+    }
+    if (t[1][0]) {
+        m->fo2_minb_split = t[1][0];
+        m->fo2_warps_split = t[1][1];
+    }
+}
+
 static int size_model(MgrModel* model) {
     uint32_t* d_max = nullptr;
     cudaError_t e = cudaMalloc(&d_max, sizeof(uint32_t));
@@ -271,6 +298,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     cudaGetDevice(&m->device);
     cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, m->device);
     if (m->sm_count < 1) m->sm_count = 1;
+    apply_tuned_shapes(m);
     cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete m;
@@ -452,6 +480,28 @@ int mgr_model_set_line_data(MgrModel* model, const double* emissivity, const dou
     if (e == cudaSuccess && interp_criterion) e = launch_nint_table(model);
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     if (e != cudaSuccess) return cuda_fail(e, "line data update");
+    return MGR_OK;
+}
+
+int mgr_model_restore_inputs(MgrModel* model, const double* velocity, const double* nu) {
+    MGR_MODEL_DEVICE(model);
+    if (!model || !velocity || !nu) {
+        set_error("mgr_model_restore_inputs: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (!model->inputs_replaced) return MGR_OK;
+    const uint32_t P = model->dm.P;
+    std::vector<double4_32a> vel4(P);
+    for (uint32_t p = 0; p < P; p++)
+        vel4[p] = make_double4_32a(velocity[3 * p], velocity[3 * p + 1], velocity[3 * p + 2], 0.0);
+    cudaError_t e = cudaMemcpyAsync(const_cast<double4_32a*>(model->dm.vel), vel4.data(), P * sizeof(double4_32a),
+                                    cudaMemcpyHostToDevice, model->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(const_cast<double*>(model->dm.nu), nu, (size_t)P * model->dm.F * 8, cudaMemcpyHostToDevice,
+                            model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);  // vel4 is read by the copy
+    if (e != cudaSuccess) return cuda_fail(e, "input restore");
+    model->inputs_replaced = false;
     return MGR_OK;
 }
 
@@ -887,11 +937,9 @@ int mgr_set_tuning(MgrModel* model, int precision, int min_blocks_per_sm, int wa
         set_error("mgr_set_tuning: min_blocks_per_sm must be 2..4 (0 keeps it), warps_per_block 1..8 (0 keeps it)");
         return MGR_ERR_ARGUMENT;
     }
-    if (min_blocks_per_sm) {
-        if (precision == MGR_PRECISION_SPLIT) model->fo2_minb_split = min_blocks_per_sm;
-        else model->fo2_minb_fp64 = min_blocks_per_sm;
-    }
-    if (warps_per_block) model->fo2_warps = warps_per_block;
+    const bool split = precision == MGR_PRECISION_SPLIT;
+    if (min_blocks_per_sm) (split ? model->fo2_minb_split : model->fo2_minb_fp64) = min_blocks_per_sm;
+    if (warps_per_block) (split ? model->fo2_warps_split : model->fo2_warps_fp64) = warps_per_block;
     return MGR_OK;
 }
 
@@ -912,7 +960,8 @@ int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int
     rc = ensure_scratch(model, &model->work, &model->work_bytes, fo2_work_bytes(model, n, true, false));
     if (rc != MGR_OK) return rc;
     int& minb = precision == MGR_PRECISION_SPLIT ? model->fo2_minb_split : model->fo2_minb_fp64;
-    const int keep_minb = minb, keep_warps = model->fo2_warps;
+    int& nwarps = precision == MGR_PRECISION_SPLIT ? model->fo2_warps_split : model->fo2_warps_fp64;
+    const int keep_minb = minb, keep_warps = nwarps;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -924,7 +973,7 @@ int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int
     for (int mi = 0; mi < 3 && e == cudaSuccess; mi++) {
         for (int wi = 0; wi < 2 && e == cudaSuccess; wi++) {
             minb = minbs[mi];
-            model->fo2_warps = warps[wi];
+            nwarps = warps[wi];
             e = launch_fo2_range(model, precision, o0, o1, model->J_scratch, nullptr, nullptr, model->work,
                                  model->work_bytes);  // warm
             if (e == cudaSuccess) e = cudaEventRecord(e0, model->stream);
@@ -946,11 +995,12 @@ int mgr_autotune_fo2(MgrModel* model, int precision, uint32_t sample_points, int
     cudaEventDestroy(e1);
     if (e != cudaSuccess) {
         minb = keep_minb;
-        model->fo2_warps = keep_warps;
+        nwarps = keep_warps;
         return cuda_fail(e, "autotune");
     }
     minb = bm;
-    model->fo2_warps = bw;
+    nwarps = bw;
+    remember_tuned_shape(model->device, precision, bm, bw);
     if (best_min_blocks) *best_min_blocks = bm;
     if (best_warps) *best_warps = bw;
     if (best_ms) *best_ms = best;

@@ -218,6 +218,7 @@ int mgr_model_set_velocity_device(MgrModel* model, const double* velocity_dev) {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     if (e != cudaSuccess) return cuda_fail(e, "velocity update");
+    model->inputs_replaced = true;
     return MGR_OK;
 }
 

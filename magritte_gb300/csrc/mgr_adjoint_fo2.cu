@@ -202,6 +202,7 @@ int mgr_model_set_frequencies_device(MgrModel* model, const double* nu_dev) {
                                     cudaMemcpyDeviceToDevice, model->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     if (e != cudaSuccess) return cuda_fail(e, "frequency update");
+    model->inputs_replaced = true;
     return MGR_OK;
 }
 

@@ -1151,9 +1151,17 @@ static void mark(MgrModel* model, int i) {
     AliState& st = *model->ali;
     // External: inside a stream capture a plain record only orders the graph's nodes;
     // an external record node takes the timestamp on every replay
-    if (st.timing && cudaEventRecordWithFlags(st.ev[i], model->stream, cudaEventRecordExternal) != cudaSuccess) {
+    if (!st.timing) return;
+    // the external flag is for captures only: outside one the record is a plain one
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(model->stream, &cs);
+    if (e == cudaSuccess)
+        e = cudaEventRecordWithFlags(st.ev[i], model->stream,
+                                     cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault);
+    if (e != cudaSuccess) {
         (void)cudaGetLastError();
         st.timing = false;
+        st.timing_error = std::string("event record ") + std::to_string(i) + ": " + cudaGetErrorString(e);
     }
 }
 
@@ -1162,9 +1170,12 @@ static void mark(MgrModel* model, int i) {
 static void accumulate(AliState& st, int a, int b, int k) {
     if (!st.timing) return;
     float ms = 0.0f;
-    if (cudaEventElapsedTime(&ms, st.ev[a], st.ev[b]) != cudaSuccess) {
+    const cudaError_t e = cudaEventElapsedTime(&ms, st.ev[a], st.ev[b]);
+    if (e != cudaSuccess) {
         (void)cudaGetLastError();
         st.timing = false;
+        st.timing_error = std::string("elapsed time ") + std::to_string(a) + "-" + std::to_string(b) + ": " +
+                          cudaGetErrorString(e);
         return;
     }
     st.phase_ms[k] += ms;
@@ -1762,10 +1773,15 @@ int mgr_compute_level_populations(MgrModel* model, int precision, int use_ng, lo
     if ((e = ali_launch_line_refresh(model)) != cudaSuccess) return cuda_fail(e, "line data");
     for (double& t : st.phase_ms) t = 0.0;
     st.timing = true;
+    st.timing_error.clear();
     for (cudaEvent_t& ev : st.ev)
-        if (!ev && cudaEventCreate(&ev) != cudaSuccess) {
-            (void)cudaGetLastError();
-            st.timing = false;
+        if (!ev) {
+            const cudaError_t ec = cudaEventCreate(&ev);
+            if (ec != cudaSuccess) {
+                (void)cudaGetLastError();
+                st.timing = false;
+                st.timing_error = std::string("event create: ") + cudaGetErrorString(ec);
+            }
         }
 
     const uint32_t nls = (uint32_t)st.species.size();
@@ -1873,7 +1889,8 @@ int mgr_ali_phase_times(MgrModel* model, double* ms) {
     }
     const AliState& st = *model->ali;
     if (!st.timing) {
-        set_error("mgr_ali_phase_times: no timed ALI loop on this model");
+        set_error("mgr_ali_phase_times: no timed ALI loop on this model" +
+                  (st.timing_error.empty() ? std::string() : " (" + st.timing_error + ")"));
         return MGR_ERR_UNSUPPORTED;
     }
     for (int k = 0; k < 4; k++) ms[k] = st.phase_ms[k];

@@ -1,5 +1,6 @@
 // Device state of the ALI level-population loop (mgr_ali.cu).
 #pragma once
+#include <string>
 #include <vector>
 
 #include "mgr_internal.h"
@@ -116,6 +117,7 @@ struct AliState {
     // with corrections / convergence / line-data refresh, Ng steps].
     cudaEvent_t ev[6] = {};
     bool timing = false;
+    std::string timing_error;  // why the phase timing stopped, when it did
     double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
     // Non-local ALO (n_off_diag > 0): the band elements of the latest formal solve
     // [P][L][hnrays][2 n_off_diag] (the model's alo_scratch / alo_nr_scratch, which

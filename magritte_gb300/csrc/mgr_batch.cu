@@ -50,11 +50,19 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Per-warp shared memory: sorted line centres [L_max], J accumulators [F_max], ALO
-// accumulators per frequency [F_max], the origin's ray-independent ALO factors
-// [F_max] (LambdaFactors), then the two trace halves.
+// Per-warp shared memory: the current model's DevModel, sorted line centres [L_max],
+// J accumulators [F_max], ALO accumulators per frequency [F_max], the origin's
+// ray-independent ALO factors [F_max] (LambdaFactors), then the two trace halves.
+// The single-model kernels take their DevModel as a kernel parameter, whose fields the
+// instructions read from the constant bank; a batch kernel indexes its models at run
+// time, and reading each field from the descriptor array in global memory put a
+// dependent global load in front of every table access and kept the loaded pointers
+// live in registers (spills).  The warp copies its model's descriptor into shared
+// memory when the model changes.
+constexpr size_t kDescBytes = (sizeof(DevModel) + 15) & ~size_t(15);
 __host__ __device__ inline size_t batch_head_bytes(uint32_t F_max, uint32_t L_max) {
-    const size_t head = ((size_t)L_max + 2 * (size_t)F_max) * 8 + (size_t)F_max * sizeof(LambdaFactors);
+    const size_t head =
+        kDescBytes + ((size_t)L_max + 2 * (size_t)F_max) * 8 + (size_t)F_max * sizeof(LambdaFactors);
     return (head + 15) & ~size_t(15);
 }
 __host__ __device__ inline size_t batch_warp_bytes(uint32_t cap, uint32_t F_max, uint32_t L_max) {
@@ -72,7 +80,8 @@ __global__ void __launch_bounds__(256, MINB)
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     unsigned char* base = smem + (size_t)w * batch_warp_bytes(cap, F_max, L_max);
-    double* sl = reinterpret_cast<double*>(base);
+    DevModel* desc = reinterpret_cast<DevModel*>(base);
+    double* sl = reinterpret_cast<double*>(base + kDescBytes);
     double* Jacc = sl + L_max;
     double* Lacc = Jacc + F_max;
     LambdaFactors* LF = reinterpret_cast<LambdaFactors*>(Lacc + F_max);
@@ -82,11 +91,19 @@ __global__ void __launch_bounds__(256, MINB)
 
     const uint64_t n_items = offsets[n_models];
     const uint64_t stride = (uint64_t)gridDim.x * nw;
-    uint32_t mi = 0;
+    uint32_t mi = 0, desc_mi = 0xffffffffu;
     for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
         // model of this item: offsets is ascending and items only grow within a warp
         while (offsets[mi + 1] <= item) mi++;
-        const DevModel& m = models[mi];
+        if (mi != desc_mi) {
+            static_assert(sizeof(DevModel) % 8 == 0, "DevModel copied in 8-byte words");
+            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(models + mi);
+            unsigned long long* dst = reinterpret_cast<unsigned long long*>(desc);
+            for (uint32_t i = lane; i < sizeof(DevModel) / 8; i += 32) dst[i] = src[i];
+            desc_mi = mi;
+            __syncwarp();
+        }
+        const DevModel& m = *desc;
         const uint32_t o = (uint32_t)(item - offsets[mi]);
         if (lane == 0 && o == 0) tstamp[2 * mi] = global_ns();  // origins start in order
         for (uint32_t i = lane; i < m.L; i += 32) sl[i] = m.sorted_line[i];

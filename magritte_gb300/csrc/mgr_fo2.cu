@@ -617,8 +617,8 @@ static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_
                                       uint32_t ld_o0, double* V = nullptr) {
     const DevModel& m = model->dm;
     const uint32_t cap = model->half_cap;
-    int nw = model->fo2_warps > 0 ? model->fo2_warps : 8;
-    if (nw > 8) nw = 8;
+    int nw = (MODE == MODE_SPLIT) ? model->fo2_warps_split : model->fo2_warps_fp64;
+    if (nw < 1 || nw > 8) nw = 8;
     const uint32_t Lpad = (m.L + 1) & ~1u;
     const size_t smem = (size_t)Lpad * 8 + (size_t)nw * half_bytes_per_warp(cap);
     auto kern = fo2_kernel<MODE, AP, MINB, UV, GEO>;

@@ -31,11 +31,16 @@ struct MgrModel {
     float* iw_lo = nullptr;          // [P][L] low part of the double-float inverse widths
     uint16_t* nint = nullptr;        // [E][L] interpolation counts
     uint16_t* nint_all = nullptr;    // [E] interpolation counts over all lines (imagers)
-    int fo2_warps = 8;               // warps (ray pairs in flight) per CTA of the formal solve
-    int fo2_minb_split = 3;          // register budget variant: CTAs per SM (2, 3 or 4)
-    int fo2_minb_fp64 = 3;
+    // launch shape of the formal solve per precision: register budget variant (CTAs per
+    // SM: 2, 3 or 4) and warps (ray pairs in flight) per CTA; a new model starts from the
+    // shape last tuned on its device in this process (tuned_shape), else these defaults
+    int fo2_minb_split = 4;
+    int fo2_warps_split = 8;
+    int fo2_minb_fp64 = 2;
+    int fo2_warps_fp64 = 4;
     int sm_count = 1;                // multiprocessors of the model's device
     bool line_disc = true;           // frequencies form a line spectral discretisation
+    bool inputs_replaced = false;    // velocities or frequencies replaced through a *_device setter
     int* status = nullptr;           // device status word
     mgr::LineScales scales;          // FP32 line-table scales (split precision)
     uint32_t half_cap = 0;           // longest half ray in base steps (0 = not sized yet)

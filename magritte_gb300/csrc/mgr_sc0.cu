@@ -131,8 +131,8 @@ static cudaError_t launch_sc0_variant(MgrModel* model, uint32_t c0, uint32_t c1,
                                       double* XF, double* XB, size_t xs, uint32_t xo, double* I, double* V) {
     const DevModel& m = model->dm;
     const uint32_t cap = model->half_cap;
-    int nw = model->fo2_warps > 0 ? model->fo2_warps : 8;
-    if (nw > 8) nw = 8;
+    int nw = (MODE == MODE_SPLIT) ? model->fo2_warps_split : model->fo2_warps_fp64;
+    if (nw < 1 || nw > 8) nw = 8;
     const uint32_t Lpad = (m.L + 1) & ~1u;
     const size_t smem = (size_t)Lpad * 8 + (size_t)nw * half_bytes_per_warp(cap);
     auto kern = sc0_kernel<MODE, AP, MINB>;

@@ -175,3 +175,23 @@ def test_autograd_gradients_match_finite_differences(gpu_lib):
         assert abs(an - fd) <= 1e-4 * abs(fd) + 1e-9 * abs(loss.item()), (p, an, fd)
         checked += 1
     assert checked >= 6
+
+
+def test_drop_in_solve_after_differentiable_solve_sees_host_state(gpu_lib):
+    """FormalSolver runs on the core.Model's own device copy and replaces its
+    velocities, frequencies and line data; the next drop-in solve of that model must
+    still solve the host state (bit for bit the J of a solve before)."""
+    import torch
+    from magritte_gb300 import adjoint
+
+    raw = S.grid_sphere(n=10, nside=1, nquads=5)
+    model = _core(raw)
+    solver = adjoint.FormalSolver(model)
+    model.compute_radiation_field_feautrier_order_2()
+    J0 = np.array(model.radiation.J).copy()
+    dev = dict(dtype=torch.float64, device="cuda")
+    with torch.no_grad():
+        solver(torch.tensor(raw.velocity, **dev) * 1.05, torch.tensor(raw.temperature, **dev) * 1.1,
+               torch.tensor(raw.vturb2, **dev), torch.tensor(raw.abundance, **dev))
+    model.compute_radiation_field_feautrier_order_2()
+    assert np.array_equal(np.array(model.radiation.J), J0)

@@ -122,6 +122,25 @@ def test_core_model_compute_level_populations(gpu_lib):
     assert np.isfinite(np.array(model.lines.lineProducingSpecies[0].Jeff)).all()
 
 
+def test_core_model_phase_times_with_ng_steps(gpu_lib):
+    """ali_phase_times after a loop that takes Ng steps (Default Ng every 4 normal
+    iterations, no early stop): every phase, Ng included, has a device time."""
+    from magritte_gb300 import loader
+
+    raw = S.grid_cube(n=8, nquads=7)
+    model = loader.to_core(raw, precision="split")
+    model.compute_spectral_discretisation()
+    model.compute_inverse_line_widths()
+    model.compute_LTE_level_populations()
+    prm = model.parameters
+    prm.use_adaptive_Ng_acceleration = False
+    prm.Ng_acceleration_mem_limit = 4
+    prm.pop_prec = 0.0
+    assert model.compute_level_populations(True, 12) == 12
+    ph = list(model.ali_phase_times())
+    assert len(ph) == 4 and all(t > 0.0 for t in ph), ph
+
+
 def test_memory_lean_solve_and_jeff(gpu_lib):
     """compute_radiation_field_feautrier_order_2_sparse / compute_Jeff_sparse: the
     line-integrated J summed in the solve equals the quadrature of J per frequency
