@@ -438,6 +438,17 @@ void* mgr_batch_stream(MgrBatch* batch);
  * (the n_tot of solver.tpp:492-496 per line).  Used for algorithmic-byte counts. */
 int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_reads, uint64_t* elements);
 
+/* Self-check of the ray trace (no reference counterpart; the reference's trace is
+ * Geometry::get_next_general_geometry, src/model/geometry/geometry.tpp:13-44).  The
+ * kernels pick each next point with an FP32 filter whose error bounds decide the
+ * reference's FP64 argmin, falling back to the FP64 argmin on near ties.  This walks
+ * every half ray (every origin, every ray) both ways and counts the rays, the steps and
+ * the rays whose point sequence, edges or distance increments differ in any bit
+ * (*mismatches, 0 when the filter is exact on this model).  Blocks until done.
+ * Spherically symmetric models, and models whose ray directions are not unit vectors,
+ * trace with the FP64 argmin alone: MGR_ERR_UNSUPPORTED. */
+int mgr_trace_self_check(MgrModel* model, uint64_t* rays, uint64_t* steps, uint64_t* mismatches);
+
 /* Launch shape of the formal-solve kernel for one precision mode: the register budget
  * (min_blocks_per_sm = 2, 3 or 4 CTAs of 256 threads per SM; 0 keeps the current value)
  * and warps per CTA for that precision (1..8; 0 keeps it).  Results do not depend on either; they are

@@ -118,6 +118,8 @@ SIGNATURES = {
     "mgr_formal_solve_fo2_device_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgr_ray_statistics": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                      C.POINTER(C.c_uint64)]),
+    "mgr_trace_self_check": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                        C.POINTER(C.c_uint64)]),
     "mgr_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "mgr_autotune_fo2": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_float)]),

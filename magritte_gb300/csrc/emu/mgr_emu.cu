@@ -96,6 +96,116 @@ int trace_half_host(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, Hal
     return count;
 }
 
+// Sequential restatement of trace_half's FP32-filtered walk (the same float
+// arithmetic as the device: filt_cand / filt_ahead, explicit fmaf): the filter's
+// decision where the device's would decide, the exact argmin elsewhere, exact Zn and dZ
+// of the filter's steps chained afterwards in step order.  Writes ids / eid / dZ and
+// counts the steps the exact argmin took.
+int trace_half_host_f32(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, uint32_t* ids, uint32_t* eids,
+                        double* dZs, uint64_t& exact_steps) {
+    const double* d = ray_dir(m, o, r);
+    const double4_32a po = m.pos[o];
+    TraceF32 t;
+    t.poh = m.pos_hl[2 * (size_t)o];
+    t.pol = m.pos_hl[2 * (size_t)o + 1];
+    t.dx = (float)d[0];
+    t.dy = (float)d[1];
+    t.dz = (float)d[2];
+    t.Zc = 0.0f;
+    t.eZc = 0.0f;
+    double Z = 0.0;
+    int count = 0, np = 0;
+    auto flush = [&]() {
+        for (int j = count - np; j < count; j++) {
+            const double4_32a q = m.pos[ids[j]];
+            const double Zn = dot3_rn(dsub_rn(q.x, po.x), dsub_rn(q.y, po.y), dsub_rn(q.z, po.z), d[0], d[1], d[2]);
+            const double dZl = dsub_rn(Zn, Z);
+            Z = dadd_rn(Z, dZl);
+            dZs[j] = dZl;
+        }
+        np = 0;
+    };
+    uint32_t crt = o;
+    while (true) {
+        const uint32_t nnb = m.n_nb[crt], cum = m.cum_nb[crt];
+        int found = -1;
+        uint32_t nxt = 0, eid = 0;
+        float Zw = 0.0f, EZw = 0.0f;
+        if (nnb <= 32) {
+            FiltCand c[32];
+            int ah[32];
+            float best = INFINITY;
+            for (uint32_t i = 0; i < nnb; i++) {
+                c[i] = filt_cand(m.edge_hl[2 * (size_t)(cum + i)], m.edge_hl[2 * (size_t)(cum + i) + 1], t);
+                ah[i] = filt_ahead(c[i], t);
+                if (ah[i] > 0) best = std::fmin(best, c[i].hi);
+            }
+            int ncont = 0, w = -1;
+            for (uint32_t i = 0; i < nnb; i++)
+                if (ah[i] >= 0 && c[i].lo <= best) {
+                    ncont++;
+                    if (w < 0) w = (int)i;
+                }
+            if (ncont == 0) {
+                found = 0;
+            } else if (ncont == 1 && ah[w] == 1) {
+                found = 1;
+                nxt = f32_bits(m.edge_hl[2 * (size_t)(cum + w)].w);
+                eid = cum + (uint32_t)w;
+                Zw = c[w].Zf;
+                EZw = c[w].EZ;
+            }
+        }
+        bool exact = false;
+        double dZl = 0.0;
+        if (found < 0) {
+            flush();
+            exact_steps++;
+            double best = DBL_MAX, bestZ = 0.0;
+            uint32_t besti = 0xffffffffu;
+            for (uint32_t i = 0; i < nnb; i++) {
+                const double4_32a e = m.edge[cum + i];
+                const double Rx = dsub_rn(e.x, po.x), Ry = dsub_rn(e.y, po.y), Rz = dsub_rn(e.z, po.z);
+                const double Zn = dot3_rn(Rx, Ry, Rz, d[0], d[1], d[2]);
+                if (Zn > Z) {
+                    const double d2 = dsub_rn(dot3_rn(Rx, Ry, Rz, Rx, Ry, Rz), dmul_rn(Zn, Zn));
+                    if (d2 < best) {
+                        best = d2;
+                        besti = i;
+                        bestZ = Zn;
+                    }
+                }
+            }
+            found = besti != 0xffffffffu ? 1 : 0;
+            if (found) {
+                exact = true;
+                long long bits;
+                std::memcpy(&bits, &m.edge[cum + besti].w, 8);
+                nxt = (uint32_t)bits;
+                eid = cum + besti;
+                dZl = dsub_rn(bestZ, Z);
+                Z = dadd_rn(Z, dZl);
+                Zw = (float)dmul_rn(Z, m.pos_scale);
+                EZw = fmaf(2.0f * kU32, fabsf(Zw), 32.0f * kU32Sq);
+            }
+        }
+        if (!found) return count > 0 ? kTraceLeftGrid : 0;
+        if ((uint32_t)count >= cap) return kTraceOverCapacity;
+        ids[count] = nxt;
+        eids[count] = eid;
+        if (exact) dZs[count] = dZl;
+        else np++;
+        count++;
+        t.Zc = Zw;
+        t.eZc = EZw;
+        if (np == 32) flush();
+        if (m.p2b[nxt] != m.P) break;
+        crt = nxt;
+    }
+    flush();
+    return count;
+}
+
 float to_f32_floor_host(double x) {
     const float f = (float)x;
     return (x > 0.0 && f < FLT_MIN) ? FLT_MIN : f;
@@ -108,6 +218,7 @@ struct EmuModel {
     std::vector<float> em_f, op_f, iw_f, Sp_f, dsm_f, dls, dll, ub_f, iw_lo, line_df, bkt;
     std::vector<uint16_t> nint, nint_all;
     std::vector<uint32_t> lq2f, corr_line;
+    std::vector<float4> edge_hl, pos_hl;
     DevModel m{};
 };
 
@@ -129,6 +240,23 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
         std::memcpy(&w, &bits, 8);
         x.edge[i] = make_double4_32a(d->position[3 * n], d->position[3 * n + 1], d->position[3 * n + 2], w);
     }
+    // trace filter tables, as hl_tables_kernel builds them
+    double maxabs = 0.0;
+    for (size_t i = 0; i < 3 * (size_t)P; i++) maxabs = std::max(maxabs, std::fabs(d->position[i]));
+    int pexp = 0;
+    if (maxabs > 0.0 && std::isfinite(maxabs)) std::frexp(maxabs, &pexp);
+    const double pscale = std::ldexp(1.0, -pexp);
+    x.edge_hl.resize(2 * (E ? E : 1));
+    x.pos_hl.resize(2 * (size_t)P);
+    auto hl = [&](const double4_32a& q, float w, float4* out) {
+        split_hl(q.x * pscale, out[0].x, out[1].x);
+        split_hl(q.y * pscale, out[0].y, out[1].y);
+        split_hl(q.z * pscale, out[0].z, out[1].z);
+        out[0].w = w;
+        out[1].w = 0.0f;
+    };
+    for (size_t i = 0; i < E; i++) hl(x.edge[i], bits_f32(d->neighbors[i]), &x.edge_hl[2 * i]);
+    for (uint32_t p = 0; p < P; p++) hl(x.pos[p], 0.0f, &x.pos_hl[2 * (size_t)p]);
     const size_t PL = (size_t)P * L;
     x.ub.resize(P);
     x.Sp.resize(PL);
@@ -159,6 +287,14 @@ void build_emu_model(const MgrModelDesc* d, EmuModel& x) {
     m.nlspecs = d->nlspecs; m.B = d->nboundary;
     m.pos = x.pos.data(); m.vel = x.vel.data(); m.n_nb = d->n_neighbors; m.cum_nb = d->cum_n_neighbors;
     m.edge = x.edge.data(); m.p2b = d->point2boundary; m.bc = d->boundary_condition;
+    m.edge_hl = x.edge_hl.data(); m.pos_hl = x.pos_hl.data(); m.pos_scale = pscale;
+    {
+        const size_t NR = (size_t)d->nrays * (d->use_adaptive_directions ? P : 1);
+        for (size_t i = 0; i < NR; i++) {
+            const double* v = d->ray_direction + 3 * i;
+            if (std::fabs(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] - 1.0) > 2.0e-15) m.edge_hl = nullptr;
+        }
+    }
     m.bt = d->boundary_temperature; m.raydir = d->ray_direction; m.rayw = d->ray_weight; m.antipod = d->antipod;
     m.line = d->line; m.sorted_line = d->sorted_line; m.sorted_map = d->sorted_line_map;
     m.max_inv_mass = d->max_inverse_mass; m.em = d->emissivity; m.op = d->opacity; m.iw = d->inverse_width;
@@ -573,6 +709,38 @@ extern "C" int mgr_emu_image_for_point(const MgrModelDesc* d, int precision, uin
 }
 
 // One lane's solve for (o, rr, f): out = {u, L_diag, solved}.
+// The FP32-filtered walk against the exact one over every origin and every ray of a
+// general-geometry model: counts rays, steps, steps the exact argmin took, and rays
+// whose point sequence, edges or dZ bits differ.
+extern "C" int mgr_emu_trace_filter_check(const MgrModelDesc* d, uint64_t* rays, uint64_t* steps,
+                                          uint64_t* exact_steps, uint64_t* mismatches) {
+    EmuModel x;
+    build_emu_model(d, x);
+    const DevModel& m = x.m;
+    if (m.sph || !m.edge_hl) return MGR_ERR_UNSUPPORTED;
+    HalfBuf b(kCap);
+    std::vector<uint32_t> ids(kCap), eids(kCap);
+    std::vector<double> dz(kCap);
+    uint64_t nr = 0, ns = 0, ne = 0, bad = 0;
+    for (uint32_t o = 0; o < m.P; o++)
+        for (uint32_t r = 0; r < m.nrays; r++) {
+            HalfSmem h = b.view();
+            const int n0 = trace_half_host(m, o, r, kCap, h);
+            const int n1 = trace_half_host_f32(m, o, r, kCap, ids.data(), eids.data(), dz.data(), ne);
+            nr++;
+            bool same = n0 == n1;
+            for (int k = 0; same && k < n0; k++)
+                same = ids[k] == b.id[k] && eids[k] == b.ei[k] && std::memcmp(&dz[k], &b.dz[k], 8) == 0;
+            if (!same) bad++;
+            if (n0 > 0) ns += (uint64_t)n0;
+        }
+    *rays = nr;
+    *steps = ns;
+    *exact_steps = ne;
+    *mismatches = bad;
+    return MGR_OK;
+}
+
 extern "C" int mgr_emu_lane(const MgrModelDesc* d, int precision, uint32_t o, uint32_t rr, uint32_t f,
                             double* out) {
     EmuModel x;

@@ -161,18 +161,20 @@ static void apply_tuned_shapes(MgrModel* m) {
 
 static int size_model(MgrModel* model) {
     uint32_t* d_max = nullptr;
-    cudaError_t e = cudaMalloc(&d_max, sizeof(uint32_t));
+    constexpr size_t nmax = 1 + kLenClasses;
+    cudaError_t e = cudaMalloc(&d_max, nmax * sizeof(uint32_t));
     if (e != cudaSuccess) return cuda_fail(e, "sizing allocation");
-    cudaMemsetAsync(d_max, 0, sizeof(uint32_t), model->stream);
+    cudaMemsetAsync(d_max, 0, nmax * sizeof(uint32_t), model->stream);
     e = launch_size_rays(model, d_max);
-    uint32_t mx = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, d_max, sizeof(uint32_t), cudaMemcpyDeviceToHost, model->stream);
+    uint32_t mx[nmax] = {};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mx, d_max, sizeof(mx), cudaMemcpyDeviceToHost, model->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
     cudaFree(d_max);
     if (e != cudaSuccess) return cuda_fail(e, "ray sizing");
     int st = read_status(model);
     if (st != MGR_OK) return st;
-    model->half_cap = mx > 0 ? mx : 1;
+    model->half_cap = mx[0] > 0 ? mx[0] : 1;
+    for (int c = 0; c < kLenClasses; c++) model->class_cap[c] = mx[1 + c];
     return MGR_OK;
 }
 
@@ -331,9 +333,22 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
 
     // host-side derived tables
     std::vector<double4_32a> pos4(P), vel4(P), edge(E ? E : 1);
+    double maxabs = 0.0;
     for (uint32_t p = 0; p < P; p++) {
         pos4[p] = make_double4_32a(d->position[3 * p], d->position[3 * p + 1], d->position[3 * p + 2], 0.0);
         vel4[p] = make_double4_32a(d->velocity[3 * p], d->velocity[3 * p + 1], d->velocity[3 * p + 2], 0.0);
+        for (int k = 0; k < 3; k++) maxabs = std::max(maxabs, std::fabs(d->position[3 * p + k]));
+    }
+    // power of two that brings every coordinate into [-1, 1] (trace filter tables)
+    int pexp = 0;
+    if (maxabs > 0.0 && std::isfinite(maxabs)) std::frexp(maxabs, &pexp);
+    dm.pos_scale = std::ldexp(1.0, -pexp);
+    // the trace filter's bounds take unit ray directions (|d|^2 = 1 within 2e-15, as
+    // HEALPix and rotated directions are); other models trace with the exact argmin only
+    bool unit_rays = true;
+    for (size_t i = 0; i < NR && unit_rays; i++) {
+        const double* v = d->ray_direction + 3 * i;
+        unit_rays = std::fabs(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] - 1.0) <= 2.0e-15;
     }
     for (size_t i = 0; i < E; i++) {
         const uint32_t n = d->neighbors[i];
@@ -402,6 +417,15 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = dalloc(m, &m->iw_lo, PL)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->nint, (ET ? ET : 1) * (size_t)L)) != cudaSuccess) break;
         if ((e = dalloc(m, &m->nint_all, ET ? ET : 1)) != cudaSuccess) break;
+        if ((e = dalloc(m, &m->pair_class, (size_t)P * d->hnrays)) != cudaSuccess) break;
+        {
+            float4* ehl = nullptr;
+            float4* phl = nullptr;
+            if ((e = dalloc(m, &ehl, 2 * (E ? E : 1))) != cudaSuccess) break;
+            if ((e = dalloc(m, &phl, 2 * (size_t)P)) != cudaSuccess) break;
+            dm.edge_hl = unit_rays ? ehl : nullptr;
+            dm.pos_hl = phl;
+        }
         if ((e = cudaMemcpyAsync(m->em, d->emissivity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->op, d->opacity, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(m->iw, d->inverse_width, PL * 8, cudaMemcpyHostToDevice, m->stream)) != cudaSuccess) break;
@@ -448,7 +472,8 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     dm.nint = m->nint;
     dm.nint_all = m->nint_all;
     apply_scales(m, d->emissivity, d->opacity);
-    if ((e = launch_line_tables(m)) != cudaSuccess || (e = launch_nint_table(m)) != cudaSuccess) {
+    if ((e = launch_line_tables(m)) != cudaSuccess || (e = launch_nint_table(m)) != cudaSuccess ||
+        (e = launch_hl_tables(m)) != cudaSuccess) {
         int rc = cuda_fail(e, "line tables");
         mgr_model_free(m);
         return rc;
@@ -926,6 +951,35 @@ int mgr_ray_statistics(MgrModel* model, uint64_t* steps, uint64_t* neighbor_read
     *steps = h[0];
     *neighbor_reads = h[1];
     *elements = h[2];
+    return MGR_OK;
+}
+
+int mgr_trace_self_check(MgrModel* model, uint64_t* rays, uint64_t* steps, uint64_t* mismatches) {
+    MGR_MODEL_DEVICE(model);
+    if (!model || !rays || !steps || !mismatches) {
+        set_error("mgr_trace_self_check: null argument");
+        return MGR_ERR_ARGUMENT;
+    }
+    if (model->dm.sph || !model->dm.edge_hl) {
+        set_error("mgr_trace_self_check: this model traces with the exact argmin only (spherical symmetry, or ray "
+                  "directions that are not unit vectors)");
+        return MGR_ERR_UNSUPPORTED;
+    }
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 3 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(e, "allocation");
+    unsigned long long h[3] = {0, 0, 0};
+    e = cudaMemsetAsync(d, 0, sizeof(h), model->stream);
+    if (e == cudaSuccess) e = launch_trace_check(model, d);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, model->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(model->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "trace self-check");
+    int st = read_status(model);
+    if (st != MGR_OK) return st;
+    *rays = h[0];
+    *steps = h[1];
+    *mismatches = h[2];
     return MGR_OK;
 }
 

@@ -51,6 +51,13 @@ struct DevModel {
     const uint32_t* n_nb;    // [P]
     const uint32_t* cum_nb;  // [P]
     const double4_32a* edge;     // [E] neighbour position x, y, z and its index (bits of w)
+    // FP32 copies for the trace's next-point filter: edge_hl[2i] = neighbour position
+    // times pos_scale as floats (hi) with its index in the bits of w, edge_hl[2i + 1] the
+    // rounding remainders (lo); pos_hl the same per point.  pos_scale is the power of
+    // two that brings every coordinate into [-1, 1].
+    const float4* edge_hl;       // [E][2]
+    const float4* pos_hl;        // [P][2]
+    double pos_scale;
     const uint32_t* p2b;     // [P]
     const int32_t* bc;       // [B]
     const double* bt;        // [B]
@@ -345,6 +352,17 @@ MGR_HD R interpolate_linear(R f_start, R f_end, R factor) {
     if (factor == R(0)) return f_start;
     if (factor == R(1)) return f_end;
     return (f_end - f_start) * factor + f_start;
+}
+// FP64: the product and the sum rounded separately, as the reference's build computes
+// them.  A contracted multiply-add rounds once; which one the compiler contracts can
+// differ between kernels that inline the same code, and the inverse widths interpolated
+// here feed the single-precision erff arguments of the line-integrated optical depth,
+// whose same-wing differences amplify an ulp of an argument to ~1e-8 of J.
+template <>
+MGR_HD double interpolate_linear<double>(double f_start, double f_end, double factor) {
+    if (factor == 0.0) return f_start;
+    if (factor == 1.0) return f_end;
+    return dadd_rn(dmul_rn(dsub_rn(f_end, f_start), factor), f_start);
 }
 
 MGR_HD double interpolate_log(double f_start, double f_end, double factor) {

@@ -50,21 +50,61 @@ cudaError_t fill_erf_band(float* table, cudaStream_t stream, int sm_count) {
 }
 
 // ---------------------------------------------------------------------------------
-// Longest half ray (base steps) over all points and rays: sizes the shared-memory
-// ray buffers.  One warp per (point, ray).
+// Hi/lo float copies of the neighbour records and points for the trace's FP32
+// next-point filter (DevModel::edge_hl, pos_hl), positions scaled by pos_scale.
 // ---------------------------------------------------------------------------------
-__global__ void size_rays_kernel(DevModel m, uint32_t* d_max, int* status) {
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    const uint64_t total = (uint64_t)m.P * m.nrays;
-    if (gw >= total) return;
-    const uint32_t o = (uint32_t)(gw / m.nrays);
-    const uint32_t r = (uint32_t)(gw % m.nrays);
-    HalfSmem h{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    const int n = trace_half<false>(m, o, r, 0xffffffffu, h, lane, status);
-    if (lane == 0 && n > 0) atomicMax(d_max, (uint32_t)n);
+__global__ void hl_tables_kernel(const double4_32a* __restrict__ edge, uint64_t E, const double4_32a* __restrict__ pos,
+                                 uint32_t P, double scale, float4* __restrict__ edge_hl, float4* __restrict__ pos_hl) {
+    const uint64_t n = E + P;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const bool is_edge = i < E;
+        const double4_32a q = is_edge ? edge[i] : pos[i - E];
+        float4 hi, lo;
+        split_hl(dmul_rn(q.x, scale), hi.x, lo.x);
+        split_hl(dmul_rn(q.y, scale), hi.y, lo.y);
+        split_hl(dmul_rn(q.z, scale), hi.z, lo.z);
+        hi.w = is_edge ? bits_f32((uint32_t)__double_as_longlong(q.w)) : 0.0f;
+        lo.w = 0.0f;
+        if (is_edge && !edge_hl) continue;
+        float4* out = is_edge ? edge_hl + 2 * i : pos_hl + 2 * (i - E);
+        out[0] = hi;
+        out[1] = lo;
+    }
 }
 
+cudaError_t launch_hl_tables(MgrModel* model) {
+    const uint64_t n = (uint64_t)model->n_edges + model->dm.P;
+    uint64_t blocks = (n + 255) / 256;
+    if (blocks > (uint64_t)model->sm_count * 16) blocks = (uint64_t)model->sm_count * 16;
+    count_launch();
+    hl_tables_kernel<<<(unsigned)(blocks ? blocks : 1), 256, 0, model->stream>>>(
+        model->dm.edge, model->n_edges, model->dm.pos, model->dm.P, model->dm.pos_scale,
+        const_cast<float4*>(model->dm.edge_hl), const_cast<float4*>(model->dm.pos_hl));
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// Ray sizing: one warp per (point, ray pair) walks both halves; the longer half's step
+// count gives the pair's length class (pair_class) and feeds the maxima of the class
+// and of all rays (d_max[1 + c], d_max[0]), which size the shared-memory ray buffers.
+// ---------------------------------------------------------------------------------
+__global__ void size_rays_kernel(DevModel m, uint8_t* __restrict__ pair_class, uint32_t* d_max, int* status) {
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint64_t total = (uint64_t)m.P * m.hnrays;
+    if (gw >= total) return;
+    const uint32_t o = (uint32_t)(gw / m.hnrays);
+    const uint32_t rr = (uint32_t)(gw % m.hnrays);
+    HalfSmem h{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const int nb = trace_half<false>(m, o, rr, 0xffffffffu, h, lane, status);
+    const int nf = trace_half<false>(m, o, m.antipod[rr], 0xffffffffu, h, lane, status);
+    if (lane != 0 || nb < 0 || nf < 0) return;
+    const uint32_t n = (uint32_t)(nb > nf ? nb : nf);
+    const int c = len_class(n);
+    pair_class[gw] = (uint8_t)c;
+    if (n > 0) atomicMax(d_max, n);
+    atomicMax(d_max + 1 + c, n > 0 ? n : 1u);  // a class with pairs is never empty
+}
 
 // ---------------------------------------------------------------------------------
 // Interpolation count of every CSR edge (crt -> nxt) and line:
@@ -186,7 +226,8 @@ template <int MODE, int AP, int MINB, bool UV = false, int GEO = 0>
 __global__ void __launch_bounds__(256, MINB)
     fo2_kernel(DevModel m, uint32_t cap, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                double* __restrict__ U, size_t u_stride, uint32_t u_o0, double* __restrict__ LD, size_t ld_stride,
-               uint32_t ld_o0, double* __restrict__ V, int* status) {
+               uint32_t ld_o0, double* __restrict__ V, const uint8_t* __restrict__ cls, uint32_t cls_id,
+               int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
@@ -203,6 +244,7 @@ __global__ void __launch_bounds__(256, MINB)
     for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
         const uint32_t o = o_begin + (uint32_t)(item / nR);
         const uint32_t rr = rr0 + (uint32_t)(item % nR);
+        if (cls && cls[(size_t)o * m.hnrays + rr] != cls_id) continue;  // another length class's launch
         int nb = 0, nf = 0;
         trace_pair<true, 0, GEO>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
         if (nb < 0 || nf < 0) continue;  // status recorded by the trace
@@ -522,11 +564,12 @@ cudaError_t launch_line_tables(MgrModel* model) {
 }
 
 cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps) {
-    const uint64_t warps = (uint64_t)model->dm.P * model->dm.nrays;
+    const uint64_t warps = (uint64_t)model->dm.P * model->dm.hnrays;
     const int threads = 256;
     const uint64_t blocks = (warps * 32 + threads - 1) / threads;
     count_launch();
-    size_rays_kernel<<<(unsigned)blocks, threads, 0, model->stream>>>(model->dm, d_max_steps, model->status);
+    size_rays_kernel<<<(unsigned)blocks, threads, 0, model->stream>>>(model->dm, model->pair_class, d_max_steps,
+                                                                     model->status);
     return cudaGetLastError();
 }
 
@@ -596,6 +639,47 @@ cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats) {
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------------
+// Self-check of the trace's FP32 next-point filter: one warp per (origin, ray) walks
+// the half ray with the exact FP64 argmin into one buffer and with the filter into the
+// other; stats = {rays, steps, rays whose point sequence, edges or dZ bits differ}.
+// ---------------------------------------------------------------------------------
+__global__ void trace_check_kernel(DevModel m, uint32_t cap, unsigned long long* stats, int* status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + w;
+    if (gw >= (uint64_t)m.P * m.nrays) return;
+    HalfSmem ex, fl;
+    carve_halves(smem + (size_t)w * half_bytes_per_warp(cap), cap, ex, fl);
+    const uint32_t o = (uint32_t)(gw / m.nrays);
+    const uint32_t r = (uint32_t)(gw % m.nrays);
+    const int n0 = trace_half<true, 0, 1, false>(m, o, r, cap, ex, lane, status);
+    const int n1 = trace_half<true, 0, 1, true>(m, o, r, cap, fl, lane, status);
+    bool same = n0 == n1;
+    for (int k = lane; same && k < n0; k += 32)
+        same = ex.ids[k] == fl.ids[k] && ex.eid[k] == fl.eid[k] &&
+               __double_as_longlong(ex.dZ[k]) == __double_as_longlong(fl.dZ[k]);
+    same = __all_sync(FULL_MASK, same);
+    if (lane == 0) {
+        atomicAdd(&stats[0], 1ull);
+        if (n0 > 0) atomicAdd(&stats[1], (unsigned long long)n0);
+        if (!same) atomicAdd(&stats[2], 1ull);
+    }
+}
+
+cudaError_t launch_trace_check(MgrModel* model, unsigned long long* d_stats) {
+    const uint32_t cap = model->half_cap;
+    const int wpb = 4;
+    const size_t smem = wpb * half_bytes_per_warp(cap);
+    const uint64_t warps = (uint64_t)model->dm.P * model->dm.nrays;
+    const uint64_t blocks = (warps + wpb - 1) / wpb;
+    cudaError_t e = cudaFuncSetAttribute(trace_check_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    count_launch();
+    trace_check_kernel<<<(unsigned)blocks, wpb * 32, smem, model->stream>>>(model->dm, cap, d_stats, model->status);
+    return cudaGetLastError();
+}
+
 // Bytes of U / L_diag staging per origin and the origins one chunk may hold.
 static size_t fo2_bytes_per_origin(const MgrModel* model) {
     return (size_t)model->dm.hnrays * model->dm.F * sizeof(double);
@@ -611,12 +695,16 @@ size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, b
     return chunk * per;
 }
 
+// One launch of fo2_kernel over origins [o_begin, o_end) x ray pairs [rr0, rr0 + nR):
+// every pair (cls null, buffers sized for the model's longest half ray) or the pairs of
+// length class cls_id (buffers sized for that class's longest half ray).
 template <int MODE, int AP, int MINB, bool UV = false, int GEO = 0>
 static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                                       double* U, size_t u_stride, uint32_t u_o0, double* LD, size_t ld_stride,
-                                      uint32_t ld_o0, double* V = nullptr) {
+                                      uint32_t ld_o0, double* V = nullptr, const uint8_t* cls = nullptr,
+                                      uint32_t cls_id = 0) {
     const DevModel& m = model->dm;
-    const uint32_t cap = model->half_cap;
+    const uint32_t cap = cls ? model->class_cap[cls_id] : model->half_cap;
     int nw = (MODE == MODE_SPLIT) ? model->fo2_warps_split : model->fo2_warps_fp64;
     if (nw < 1 || nw > 8) nw = 8;
     const uint32_t Lpad = (m.L + 1) & ~1u;
@@ -635,20 +723,34 @@ static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_
     if (grid < 1) grid = 1;
     count_launch();
     kern<<<(unsigned)grid, nw * 32, smem, model->stream>>>(m, cap, o_begin, o_end, rr0, nR, U, u_stride, u_o0, LD,
-                                                          ld_stride, ld_o0, V, model->status);
+                                                          ld_stride, ld_o0, V, cls, cls_id, model->status);
     return cudaGetLastError();
 }
 
+// The formal solve's launches: one per non-empty ray-length class, each with shared
+// memory for its own rays, so that short rays are not solved at the occupancy the
+// longest ray of the model allows.
 template <int MODE, int AP>
 static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                                    double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo) {
-    // spherical symmetry and adaptive rays: the run-time geometry variant, one tile
-    if (model->dm.sph || model->dm.adaptive)
-        return launch_fo2_variant<MODE, AP, 3, false, 1>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
     const int minb = (MODE == MODE_SPLIT) ? model->fo2_minb_split : model->fo2_minb_fp64;
-    if (minb == 2) return launch_fo2_variant<MODE, AP, 2>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
-    if (minb == 4) return launch_fo2_variant<MODE, AP, 4>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
-    return launch_fo2_variant<MODE, AP, 3>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo);
+    const bool any_geo = model->dm.sph || model->dm.adaptive;
+    const uint8_t* cls = model->pair_class;
+    for (int c = 0; c < (cls ? kLenClasses : 1); c++) {
+        if (cls && model->class_cap[c] == 0) continue;
+        cudaError_t e;
+        // spherical symmetry and adaptive rays: the run-time geometry variant, one tile
+        if (any_geo) e = launch_fo2_variant<MODE, AP, 3, false, 1>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo,
+                                                                  nullptr, cls, c);
+        else if (minb == 2)
+            e = launch_fo2_variant<MODE, AP, 2>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo, nullptr, cls, c);
+        else if (minb == 4)
+            e = launch_fo2_variant<MODE, AP, 4>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo, nullptr, cls, c);
+        else
+            e = launch_fo2_variant<MODE, AP, 3>(model, o_begin, o_end, rr0, nR, U, us, uo, LD, ls, lo, nullptr, cls, c);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // The uv solve: one register budget (MINB 3), no tuning.

@@ -14,6 +14,15 @@ namespace mgr {
 struct AliState;
 }
 
+namespace mgr {
+// Ray-length classes of the formal solve (half-ray steps at most; the last is open).
+constexpr int kLenClasses = 5;
+constexpr uint32_t kLenClassBound[kLenClasses] = {32, 64, 128, 256, 0xffffffffu};
+MGR_HD int len_class(uint32_t steps) {
+    return steps <= 32 ? 0 : steps <= 64 ? 1 : steps <= 128 ? 2 : steps <= 256 ? 3 : 4;
+}
+}  // namespace mgr
+
 struct MgrModel {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -44,6 +53,12 @@ struct MgrModel {
     int* status = nullptr;           // device status word
     mgr::LineScales scales;          // FP32 line-table scales (split precision)
     uint32_t half_cap = 0;           // longest half ray in base steps (0 = not sized yet)
+    // ray-length classes of the formal solve: pair_class[o * hnrays + rr] is the class of
+    // ray pair (o, rr) by its longer half (kLenClassBound), class_cap[c] the longest half
+    // ray in class c (0: empty); each class is solved by its own launch, whose shared
+    // memory holds that class's rays only
+    uint8_t* pair_class = nullptr;
+    uint32_t class_cap[mgr::kLenClasses] = {};
     size_t n_edges = 0;
     // scratch outputs for the host-buffer entry points
     double* J_scratch = nullptr;
@@ -135,11 +150,13 @@ void set_line_scales(MgrModel* m, double Ke, double Ko);
 void count_launch();
 
 // Kernel launchers (mgr_fo2.cu).  All enqueue on model->stream.
+// d_max_steps[0]: longest half ray; d_max_steps[1 + c]: longest half ray of class c
 cudaError_t launch_size_rays(MgrModel* model, uint32_t* d_max_steps);
 // Formal solve of origins [o_begin, o_end): J [P][F] and lam [P][L] rows of those
 // origins, u [hnrays][P][F] (may be NULL).  Per-ray results are staged in `work`
 // (sized by fo2_work_bytes for the same u / lam choice), in chunks of origins that fit.
-constexpr size_t kFo2WorkBudget = size_t(2) << 30;
+// 6.5 GiB: the 64^3 benchmark model (6.2 GB of u and L_diag) in one chunk.
+constexpr size_t kFo2WorkBudget = size_t(13) << 29;
 size_t fo2_work_bytes(const MgrModel* model, uint32_t n_origins, bool stage_u, bool stage_ld);
 // Ray pairs [rr_begin, rr_end) only (partial J / ALO sums, u must then be NULL).
 // J may be NULL; Jlin [P][L] (may be NULL) receives the line-integrated J in the order
@@ -156,7 +173,9 @@ cudaError_t launch_trace_export(MgrModel* model, uint32_t o, uint32_t rr, uint32
 cudaError_t launch_line_tables(MgrModel* model);
 cudaError_t launch_ray_lengths(MgrModel* model, uint32_t* d_max_len);
 cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats);
+cudaError_t launch_trace_check(MgrModel* model, unsigned long long* d_stats);
 cudaError_t launch_nint_table(MgrModel* model);
+cudaError_t launch_hl_tables(MgrModel* model);  // trace filter tables (edge_hl, pos_hl)
 // Fills the correctly rounded erff table (kErfBandCount floats) on `stream`.
 cudaError_t fill_erf_band(float* table, cudaStream_t stream, int sm_count);
 // The current device's erff table, created (cudaMalloc, one fill launch, synchronised)

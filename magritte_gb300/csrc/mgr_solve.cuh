@@ -20,6 +20,8 @@
 // once.  Pair quantities (optical depth, row source) are pure functions of the two
 // elements, so they can be evaluated in either sweep direction.
 #pragma once
+#include <cstring>
+
 #include "mgr_device.cuh"
 
 namespace mgr {
@@ -140,6 +142,140 @@ __device__ __forceinline__ bool warp_next_point(const DevModel& m, const double4
     return true;
 }
 
+// ---------------------------------------------------------------------------------
+// FP32 filter of the next-point argmin.  On GB300 the FP64 pipe issues one warp
+// instruction per 16 cycles whatever the number of active lanes, and the exact argmin
+// above costs 15 FP64 instructions per step.  The filter evaluates every neighbour's
+// distance along the ray and squared distance to the ray in FP32, from hi/lo float
+// copies of the positions (the origin-relative vector is then accurate to about
+// 3 u |R|, u = 2^-24, with no cancellation against the absolute coordinates), with
+// rigorous bounds on how far each FP32 value can lie from the FP64 value the reference
+// computes:
+//   |Zf  - Zn_ref|  <= EZ  = 10 u s1 + 32 u^2,             s1 = sum |r_i d_i|
+//   |d2f - d2_ref|  <= Ed2 = 2 ec |c|_1 + 3 ec^2 + 6 u d2f + 1e-14 |r|_1^2,
+//                           ec = 8 u |r|_1 + 32 u^2,  c = r x d
+// (positions scaled into [-1, 1] by a power of two; d2 through the cross product, which
+// equals |R|^2 - (R.d)^2 up to |R|^2 (1 - |d|^2) and the FP64 roundings, both covered by
+// the last term for unit directions: models whose directions are not unit to 2e-15 get
+// no filter tables (edge_hl null) and trace with the exact argmin).  A neighbour is
+// certainly ahead (Zn > Z) when Zf - Zc exceeds EZ plus the bound of the current Z's
+// estimate Zc, certainly behind when it is below minus that, else undecided.  When
+// exactly one neighbour that is certainly ahead or undecided has a lower bound of d2 at
+// or below the smallest upper bound among the certainly-ahead ones, and it is certainly
+// ahead, it is the reference's choice: every other candidate's d2 is strictly larger.
+// Otherwise (near ties, undecided ahead/behind, more than 32 neighbours) the step is
+// taken by the exact FP64 argmin.  The exact Z of the chosen points (and dZ) are
+// computed afterwards, one step per lane, and chained in the reference's order
+// (Z += Zn - Z).
+// ---------------------------------------------------------------------------------
+constexpr float kU32 = 5.9604644775390625e-8f;     // 2^-24
+constexpr float kU32Sq = 3.552713678800501e-15f;   // 2^-48
+
+// Float bits (host and device).
+MGR_HD uint32_t f32_bits(float x) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(x);
+#else
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    return b;
+#endif
+}
+MGR_HD float bits_f32(uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float x;
+    std::memcpy(&x, &b, 4);
+    return x;
+#endif
+}
+
+// A double as the unevaluated sum hi + lo of two floats (round to nearest each).
+MGR_HD void split_hl(double x, float& hi, float& lo) {
+    hi = (float)x;
+    lo = (float)dsub_rn(x, (double)hi);
+}
+
+// Per-trace state of the filter: the origin's hi/lo position, the direction as floats,
+// and the estimate Zc of the current Z with its bound eZc (all in scaled units).
+struct TraceF32 {
+    float4 poh, pol;
+    float dx, dy, dz;
+    float Zc, eZc;
+};
+
+// One neighbour's filter values: Zf and its bound EZ, and the bounds lo <= d2 <= hi.
+struct FiltCand {
+    float Zf, EZ, lo, hi;
+};
+
+// Explicit fmaf everywhere, so that the host emulation and the device compute the same
+// floats (nothing is left for the compiler to contract).
+MGR_HD FiltCand filt_cand(const float4& a, const float4& b, const TraceF32& t) {
+    const float rx = (a.x - t.poh.x) + (b.x - t.pol.x);
+    const float ry = (a.y - t.poh.y) + (b.y - t.pol.y);
+    const float rz = (a.z - t.poh.z) + (b.z - t.pol.z);
+    FiltCand c;
+    c.Zf = fmaf(rz, t.dz, fmaf(ry, t.dy, rx * t.dx));
+    const float s1 = fabsf(rx * t.dx) + fabsf(ry * t.dy) + fabsf(rz * t.dz);
+    const float rn1 = fabsf(rx) + fabsf(ry) + fabsf(rz);
+    const float cx = fmaf(ry, t.dz, -(rz * t.dy));
+    const float cy = fmaf(rz, t.dx, -(rx * t.dz));
+    const float cz = fmaf(rx, t.dy, -(ry * t.dx));
+    const float d2 = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+    const float cn1 = fabsf(cx) + fabsf(cy) + fabsf(cz);
+    const float ec = fmaf(8.0f * kU32, rn1, 32.0f * kU32Sq);
+    const float rr = rn1 * rn1;
+    const float e = fmaf(2.0f * ec, cn1, fmaf(3.0f * ec, ec, fmaf(6.0f * kU32, d2, 1.0e-14f * rr)));
+    const float Ed2 = e * 1.001f;
+    c.EZ = fmaf(10.0f * kU32, s1, 32.0f * kU32Sq);
+    c.lo = d2 - Ed2;
+    c.hi = d2 + Ed2;
+    return c;
+}
+
+// Ahead / behind decision of a candidate against the current Z estimate: 1 certainly
+// ahead (Zn > Z), -1 certainly not, 0 undecided.
+MGR_HD int filt_ahead(const FiltCand& c, const TraceF32& t) {
+    const float diff = c.Zf - t.Zc;
+    const float tol = (c.EZ + t.eZc) * 1.0001f;
+    return diff > tol ? 1 : (diff < -tol ? -1 : 0);
+}
+
+// The filter's step, warp-cooperative (lane i holds neighbour i).  Returns 1 with the
+// next point, its neighbour-record index and its Zf / EZ when the filter decides; 0
+// when no neighbour can lie further along the ray; -1 when the exact argmin must decide.
+__device__ __forceinline__ int warp_next_point_f32(const DevModel& m, const TraceF32& t, uint32_t crt, int lane,
+                                                   uint32_t& nxt, uint32_t& eid, float& Zw, float& EZw) {
+    const uint32_t nnb = m.n_nb[crt];
+    if (nnb > 32) return -1;
+    const uint32_t cum = m.cum_nb[crt];
+    int ah = -1;
+    FiltCand c{0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t idx = 0;
+    if ((uint32_t)lane < nnb) {
+        const float4 a = m.edge_hl[2 * (size_t)(cum + lane)];
+        const float4 b = m.edge_hl[2 * (size_t)(cum + lane) + 1];
+        c = filt_cand(a, b, t);
+        ah = filt_ahead(c, t);
+        idx = f32_bits(a.w);
+    }
+    float best = ah > 0 ? c.hi : INFINITY;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) best = fminf(best, __shfl_xor_sync(FULL_MASK, best, off));
+    const unsigned cont = __ballot_sync(FULL_MASK, ah >= 0 && c.lo <= best);
+    if (cont == 0) return 0;
+    if (__popc(cont) != 1) return -1;
+    const int w = __ffs(cont) - 1;
+    if (__shfl_sync(FULL_MASK, ah, w) != 1) return -1;
+    nxt = __shfl_sync(FULL_MASK, idx, w);
+    eid = cum + (uint32_t)w;
+    Zw = __shfl_sync(FULL_MASK, c.Zf, w);
+    EZw = __shfl_sync(FULL_MASK, c.EZ, w);
+    return 1;
+}
+
 // The walk of trace_half in 1D spherical symmetry (Geometry::get_next_spherical_symmetry,
 // geometry.tpp:118-159): every lane steps the same shells; lane 0 stores the steps, with
 // each step's shift at its distance along the ray (get_shift_spherical_symmetry) and the
@@ -199,7 +335,7 @@ __device__ int trace_half_sph(const DevModel& m, uint32_t o, uint32_t r, uint32_
 // r >= hnrays, geometry.tpp:428-465).
 // GEO 0 compiles the general geometry with shared rays only (the caller has checked the
 // model); GEO 1 handles every geometry at run time.
-template <bool STORE, int FRAME = 0, int GEO = 1>
+template <bool STORE, int FRAME = 0, int GEO = 1, bool FILTER = true>
 __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t cap, HalfSmem& h, int lane,
                           int* status) {
     if (GEO && m.sph) return trace_half_sph<STORE, FRAME>(m, o, r, cap, h, lane, status);
@@ -208,13 +344,60 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
     const double* d = (FRAME || !GEO) ? m.raydir + 3 * r : ray_dir(m, o, r);
     const double dx = d[0], dy = d[1], dz = d[2];
     const double4_32a po = m.pos[o];
-    double Z = 0.0;
+    TraceF32 t;
+    if (FILTER) {
+        t.poh = m.pos_hl[2 * (size_t)o];
+        t.pol = m.pos_hl[2 * (size_t)o + 1];
+        t.dx = (float)dx;
+        t.dy = (float)dy;
+        t.dz = (float)dz;
+        t.Zc = 0.0f;
+        t.eZc = 0.0f;
+    }
+    double Z = 0.0;  // exact Z after the last step whose Zn is known in FP64
+    // Steps chosen by the filter whose exact Zn and dZ are not computed yet: the last
+    // np steps; lane j holds the point of the j-th of them.
+    uint32_t pend = 0;
+    int np = 0;
     uint32_t crt = o;
     int count = 0;
+    // Exact Zn of the pending steps, one step per lane, then Z += Zn - Z in step order.
+    auto flush = [&]() {
+        if (np == 0) return;
+        double Zn = 0.0;
+        if (lane < np) {
+            const double4_32a q = m.pos[pend];
+            Zn = dot3_rn(dsub_rn(q.x, po.x), dsub_rn(q.y, po.y), dsub_rn(q.z, po.z), dx, dy, dz);
+        }
+        const int base = count - np;
+        for (int j = 0; j < np; j++) {
+            const double dZl = dsub_rn(__shfl_sync(FULL_MASK, Zn, j), Z);
+            Z = dadd_rn(Z, dZl);
+            if (STORE && lane == 0) h.dZ[base + j] = dZl;
+        }
+        np = 0;
+    };
     while (true) {
-        uint32_t nxt, eid;
-        double bestZ;
-        if (!warp_next_point(m, po, dx, dy, dz, crt, Z, lane, nxt, bestZ, eid)) {
+        uint32_t nxt = 0, eid = 0;
+        float Zw = 0.0f, EZw = 0.0f;
+        int found = (FILTER && m.edge_hl) ? warp_next_point_f32(m, t, crt, lane, nxt, eid, Zw, EZw) : -1;
+        bool exact = false;
+        double dZl = 0.0;
+        if (found < 0) {
+            flush();
+            double bestZ;
+            found = warp_next_point(m, po, dx, dy, dz, crt, Z, lane, nxt, bestZ, eid) ? 1 : 0;
+            if (found) {
+                exact = true;
+                dZl = dsub_rn(bestZ, Z);
+                Z = dadd_rn(Z, dZl);
+                if (FILTER) {
+                    Zw = (float)dmul_rn(Z, m.pos_scale);
+                    EZw = fmaf(2.0f * kU32, fabsf(Zw), 32.0f * kU32Sq);
+                }
+            }
+        }
+        if (!found) {
             // No point further along the ray.  From the origin this is an empty half;
             // after a step it means the walk left the grid on an interior point, where
             // the reference would index point2boundary out of range.
@@ -227,17 +410,25 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
             count = -1;
             break;
         }
-        const double dZl = dsub_rn(bestZ, Z);
-        Z = dadd_rn(Z, dZl);
         if (STORE && lane == 0) {
             h.ids[count] = nxt;
             h.eid[count] = eid;
-            h.dZ[count] = dZl;
+            if (exact) h.dZ[count] = dZl;
+        }
+        if (!exact) {
+            if (lane == np) pend = nxt;
+            np++;
         }
         count++;
+        if (FILTER) {
+            t.Zc = Zw;
+            t.eZc = EZw;
+        }
+        if (np == 32) flush();
         if (m.p2b[nxt] != m.P) break;
         crt = nxt;
     }
+    if (count > 0) flush();
     __syncwarp();
     if (STORE && count > 0) {
         // Per-step Doppler shifts and FP32 copies, one step per lane.
@@ -254,12 +445,12 @@ __device__ int trace_half(const DevModel& m, uint32_t o, uint32_t r, uint32_t ca
 
 // Both halves of a ray pair: r into `bk`, its antipode ar into `fw`.  One loop over
 // the two halves, so that a kernel holds a single copy of the trace's code.
-template <bool STORE, int FRAME = 0, int GEO = 1>
+template <bool STORE, int FRAME = 0, int GEO = 1, bool FILTER = true>
 __device__ __forceinline__ void trace_pair(const DevModel& m, uint32_t o, uint32_t r, uint32_t ar, uint32_t cap,
                                            HalfSmem& bk, HalfSmem& fw, int lane, int* status, int& nb, int& nf) {
 #pragma unroll 1
     for (int side = 0; side < 2; side++) {
-        const int n = trace_half<STORE, FRAME, GEO>(m, o, side ? ar : r, cap, side ? fw : bk, lane, status);
+        const int n = trace_half<STORE, FRAME, GEO, FILTER>(m, o, side ? ar : r, cap, side ? fw : bk, lane, status);
         if (side) nf = n;
         else nb = n;
     }

@@ -127,7 +127,7 @@ def test_core_model_phase_times_with_ng_steps(gpu_lib):
     iterations, no early stop): every phase, Ng included, has a device time."""
     from magritte_gb300 import loader
 
-    raw = S.grid_cube(n=8, nquads=7)
+    raw = S.nlte_sphere(npoints=1000, nside=1, nside_out=8)
     model = loader.to_core(raw, precision="split")
     model.compute_spectral_discretisation()
     model.compute_inverse_line_widths()
@@ -136,7 +136,7 @@ def test_core_model_phase_times_with_ng_steps(gpu_lib):
     prm.use_adaptive_Ng_acceleration = False
     prm.Ng_acceleration_mem_limit = 4
     prm.pop_prec = 0.0
-    assert model.compute_level_populations(True, 12) == 12
+    assert model.compute_level_populations(True, 10) == 10
     ph = list(model.ali_phase_times())
     assert len(ph) == 4 and all(t > 0.0 for t in ph), ph
 

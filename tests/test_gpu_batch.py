@@ -40,12 +40,13 @@ def test_batch_matches_single_model_solves(gpu_lib, approx):
     try:
         for prec in ("fp64", "split"):
             got = batch.formal_solve_fo2(prec)
-            # Same lane code and order of the sums: 1e-13.  Exception: the FP64 mode under
-            # the None approximation, where the two kernels' lane code may round one FP64
-            # multiply-add differently (the compiler's contraction of each instantiation)
-            # and the far-wing erf differences summed over every line amplify that ulp
-            # (measured 1.3e-8); 1e-6 there, far inside the 1e-5 parity bar.
-            bar = 1e-6 if (prec == "fp64" and approx == "None") else 1e-13
+            # Split precision: the same lane code and order of the sums, 1e-13.  FP64 mode:
+            # the two kernels' lane code may round an FP64 multiply-add differently (the
+            # compiler's contraction of each instantiation), which can move a
+            # single-precision erff argument by an ulp; the same-wing erf differences
+            # amplify that (measured 8.5e-9 under CloseLines, 1.3e-8 under None): 1e-6,
+            # far inside the 1e-5 parity bar.
+            bar = 1e-6 if prec == "fp64" else 1e-13
             for d, g in zip(devs, got):
                 ref = d.formal_solve_fo2(prec)
                 assert _rel(g["J"], ref["J"]) < bar
