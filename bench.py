@@ -760,6 +760,13 @@ def run_ours(args, rank, ws):
     solves = float(P) * R * F
     value = solves * args.steps / kernel_s  # the whole job solves one model per step
 
+    # the trace's FP32 filter against the exact FP64 walk on every half ray of the model
+    tr_rays, tr_steps, tr_bad = C.c_uint64(), C.c_uint64(), C.c_uint64()
+    _abi._check(lib.mgr_trace_self_check(handle, C.byref(tr_rays), C.byref(tr_steps), C.byref(tr_bad)))
+    trace_check = {"half_rays": tr_rays.value, "steps": tr_steps.value, "mismatched_half_rays": tr_bad.value,
+                   "method": "mgr_trace_self_check: every (origin, ray) walked with the FP32 filter and with the "
+                             "exact FP64 argmin; point sequences, edges and dZ compared bit for bit"}
+
     # work statistics for the algorithmic-bytes roofline
     st_steps, st_nbr, st_elem = C.c_uint64(), C.c_uint64(), C.c_uint64()
     _abi._check(lib.mgr_ray_statistics(handle, C.byref(st_steps), C.byref(st_nbr), C.byref(st_elem)))
@@ -871,17 +878,18 @@ def run_ours(args, rank, ws):
     parity = parity_sample(raw, gpu_rows) if gpu_rows is not None else None
     rates = pipe_rates()
     # FP64-pipe roofline: the FP64 thread operations the algorithm needs per launch (the
-    # elimination's five per element and frequency, the trace's 14 per neighbour record
-    # scanned and 11 per step for Z and the Doppler shift) over the launch time, against
-    # the measured FP64 pipe rate
-    fp64_ops = (5.0 * st_elem.value * prm.nquads() + 14.0 * st_nbr.value + 11.0 * st_steps.value) * (rr1 - rr0) / R
+    # elimination's five per element and frequency; per trace step the exact Zn of the
+    # chosen point and Z += Zn - Z (10) and the Doppler shift (11): the FP32 filter picks
+    # the points, the exact argmin's 14 per neighbour record runs on the few steps it
+    # leaves) over the launch time, against the measured FP64 pipe rate
+    fp64_ops = (5.0 * st_elem.value * prm.nquads() + 21.0 * st_steps.value) * (rr1 - rr0) / R
     fp64_peak = rates["dfma"]["thread_ops_per_s"]
     roofline_fp64 = {"bound": "fp64", "achieved": fp64_ops / mean_launch_s, "peak": fp64_peak,
                      "unit": "FP64 thread-ops/s", "frac": fp64_ops / mean_launch_s / fp64_peak,
                      "algorithmic_ops_per_launch": fp64_ops, "peak_source": "measured (mgr_measure_pipe_rate, DFMA)",
-                     "note": "algorithmic FP64 ops = 5 per element-frequency (projective elimination row) + 14 per "
-                             "neighbour record + 11 per trace step; the pipe is busy 16 cycles per warp instruction "
-                             "whatever the active lanes"}
+                     "note": "algorithmic FP64 ops = 5 per element-frequency (projective elimination row) + 21 per "
+                             "trace step (exact Zn and Z of the point the FP32 filter chose, Doppler shift); the pipe "
+                             "is busy 16 cycles per warp instruction whatever the active lanes"}
     ali = None if args.no_ali else run_ali(args)
     batch = None if args.no_batch else run_batch(args)
     adj = None if args.no_adjoint else run_adjoint(args)
@@ -918,6 +926,7 @@ def run_ours(args, rank, ws):
         "max_rel_err_J_vs_oracle": (max(parity[f"{args.precision}_J_vs_oracle_erf_cr"],
                                         parity[f"{args.precision}_J_vs_oracle_erf_glibc"]) if parity else None),
         "parity": parity,
+        "trace_self_check": trace_check,
         "pipe_rates": rates,
         "fp64_gpu_solves_per_s": (solves / (fp64_ms / 1000.0)) if fp64_ms else None,
         "speedup_vs_fp64_gpu": (fp64_ms / (1000.0 * kernel_s / args.steps)) if fp64_ms else None,

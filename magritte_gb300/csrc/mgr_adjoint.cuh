@@ -115,9 +115,9 @@ MGR_HD void elem_bracket(const DevModel& m, const double* sl, double freq, uint3
     lo = 0;
     hi = m.L;
     if (AP == APPROX_CLOSELINES) {
-        const double ub = m.max_dist * (freq * m.ub[nr]);
-        lo = lower_bound(sl, m.L, freq - ub);
-        hi = upper_bound(sl, m.L, freq + ub);
+        const double ub = dmul_rn(m.max_dist, dmul_rn(freq, m.ub[nr]));
+        lo = lower_bound(sl, m.L, dsub_rn(freq, ub));
+        hi = upper_bound(sl, m.L, dadd_rn(freq, ub));
     }
 }
 
@@ -200,11 +200,11 @@ MGR_HD void pair_bracket(const DevModel& m, const double* sl, double cf, double 
     b = m.L;
     if (AP == APPROX_CLOSELINES) {
         const double left = cf < nf ? cf : nf, right = cf < nf ? nf : cf;
-        const double cb = m.max_dist * (right * m.ub[lo_nr]);
-        const double nb = m.max_dist * (right * m.ub[hi_nr]);
+        const double cb = dmul_rn(m.max_dist, dmul_rn(right, m.ub[lo_nr]));
+        const double nb = dmul_rn(m.max_dist, dmul_rn(right, m.ub[hi_nr]));
         const double ubw = cb > nb ? cb : nb;
-        a = lower_bound(sl, m.L, left - ubw);
-        b = upper_bound(sl, m.L, right + ubw);
+        a = lower_bound(sl, m.L, dsub_rn(left, ubw));
+        b = upper_bound(sl, m.L, dadd_rn(right, ubw));
     }
 }
 

@@ -450,9 +450,9 @@ MGR_HD void get_eta_and_chi(const DevModel& m, const double* sl, uint32_t p, uin
         }
         return;
     }
-    const double ub = m.max_dist * (freq * m.ub[p]);
-    const uint32_t lo = lower_bound(sl, m.L, freq - ub);
-    const uint32_t hi = upper_bound(sl, m.L, freq + ub);
+    const double ub = dmul_rn(m.max_dist, dmul_rn(freq, m.ub[p]));
+    const uint32_t lo = lower_bound(sl, m.L, dsub_rn(freq, ub));
+    const uint32_t hi = upper_bound(sl, m.L, dadd_rn(freq, ub));
     for (uint32_t s = lo; s < hi; s++) {
         const uint32_t l = m.sorted_map[s];
         const double prof = gaussian(m.iw[base + l], freq - sl[s]);

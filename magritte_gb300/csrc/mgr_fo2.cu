@@ -727,15 +727,18 @@ static cudaError_t launch_fo2_variant(MgrModel* model, uint32_t o_begin, uint32_
     return cudaGetLastError();
 }
 
-// The formal solve's launches: one per non-empty ray-length class, each with shared
-// memory for its own rays, so that short rays are not solved at the occupancy the
-// longest ray of the model allows.
+// The formal solve's launches.  Models whose longest half ray is over 128 steps (9 KB
+// of shared memory per warp, fewer than 24 warps per SM) get one launch per non-empty
+// ray-length class, each with shared memory for its own rays, so that short rays are
+// not solved at the occupancy the longest ray allows; shorter models get one launch
+// (measured on the 64^3 sphere cutout, longest half ray ~110 steps, the split launches
+// were 4 % slower).
 template <int MODE, int AP>
 static cudaError_t launch_fo2_minb(MgrModel* model, uint32_t o_begin, uint32_t o_end, uint32_t rr0, uint32_t nR,
                                    double* U, size_t us, uint32_t uo, double* LD, size_t ls, uint32_t lo) {
     const int minb = (MODE == MODE_SPLIT) ? model->fo2_minb_split : model->fo2_minb_fp64;
     const bool any_geo = model->dm.sph || model->dm.adaptive;
-    const uint8_t* cls = model->pair_class;
+    const uint8_t* cls = model->half_cap > kLenClassBound[2] ? model->pair_class : nullptr;
     for (int c = 0; c < (cls ? kLenClasses : 1); c++) {
         if (cls && model->class_cap[c] == 0) continue;
         cudaError_t e;

@@ -674,9 +674,11 @@ MGR_HD void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
     chi = m.min_opacity;
     uint32_t lo = 0, hi = m.L;
     if (AP == APPROX_CLOSELINES) {
-        const double ub = m.max_dist * (freq * m.ub[e.nr]);
-        lo = lower_bound(sl, m.L, freq - ub);
-        hi = upper_bound(sl, m.L, freq + ub);
+        // explicitly rounded: a contracted freq - max_dist * (...) moves the bracket's
+        // edge by an ulp and can add or drop a far line (the reference rounds twice)
+        const double ub = dmul_rn(m.max_dist, dmul_rn(freq, m.ub[e.nr]));
+        lo = lower_bound(sl, m.L, dsub_rn(freq, ub));
+        hi = upper_bound(sl, m.L, dadd_rn(freq, ub));
     }
     for (uint32_t s = lo; s < hi; s++) {
         uint32_t l;
@@ -746,11 +748,11 @@ MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
         double left_freq, right_freq;
         if (cf < nf) { left_freq = cf; right_freq = nf; }
         else { right_freq = cf; left_freq = nf; }
-        const double cb = m.max_dist * (right_freq * m.ub[lo.nr]);
-        const double nb = m.max_dist * (right_freq * m.ub[hi.nr]);
+        const double cb = dmul_rn(m.max_dist, dmul_rn(right_freq, m.ub[lo.nr]));
+        const double nb = dmul_rn(m.max_dist, dmul_rn(right_freq, m.ub[hi.nr]));
         const double ubw = cb > nb ? cb : nb;
-        a = lower_bound(sl, m.L, left_freq - ubw);
-        b = upper_bound(sl, m.L, right_freq + ubw);
+        a = lower_bound(sl, m.L, dsub_rn(left_freq, ubw));
+        b = upper_bound(sl, m.L, dadd_rn(right_freq, ubw));
     }
     for (uint32_t s = a; s < b; s++) {
         const uint32_t l = (AP == APPROX_CLOSELINES) ? m.sorted_map[s] : s;
