@@ -36,8 +36,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "point.ray.freq solves/s"
 # DRAM bytes per solve of the split formal-solve kernel, ncu on the 32^3 sphere cutout:
-# (67.8 MB read + 784.2 MB written) / 45.9 M solves
-TRAFFIC_BYTES_PER_SOLVE = (67.764736e6 + 784.199936e6) / 45_854_208.0
+# (1004.8 MB read + 1575.3 MB written) / 45.9 M solves
+TRAFFIC_BYTES_PER_SOLVE = (1004.780e6 + 1575.276e6) / 45_854_208.0
 UNIT = "solves/s"
 
 
@@ -909,8 +909,9 @@ def run_ours(args, rank, ws):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": TRAFFIC_BYTES_PER_SOLVE * solves * (rr1 - rr0) / R,
                      "traffic_note": "DRAM read + write bytes per launch from an ncu capture of the 32^3 case "
-                                     "(67.8 MB read + 784.2 MB written for 45.9 M solves), scaled by the solves "
-                                     "of this launch; the writes are the u / L_diag staging, proportional to solves",
+                                     "(1004.8 MB read + 1575.3 MB written for 45.9 M solves; ncu flushes the caches "
+                                     "between its passes), scaled by the solves of this launch; the writes are the "
+                                     "u / L_diag staging, proportional to solves",
                      "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "note": "algorithmic bytes = 28 per trace step and per neighbour record + 52 per ray-pair "

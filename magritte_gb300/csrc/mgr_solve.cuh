@@ -660,12 +660,17 @@ MGR_HD LaneCtx lane_ctx(const DevModel& m, uint32_t o, uint32_t f) {
 template <int AP>
 MGR_HD void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& e,
                                              double& eta, double& chi) {
-    const double freq = c.freq * e.shift;
+    // The FP64 mode's frequency products and differences are explicitly rounded: a
+    // product contracted into the difference that follows it rounds once where the
+    // reference rounds twice, and which ones the compiler contracts differs between
+    // kernels; an ulp of a profile's or an erff's argument can flip its rounding to
+    // float and move J by ~1e-8.
+    const double freq = dmul_rn(c.freq, e.shift);
     const size_t b1 = (size_t)e.nr * m.L, b2 = (size_t)e.ni * m.L;
     if (AP == APPROX_ONELINE) {
         const uint32_t l = c.l0;
         const double iw = interpolate_linear(m.iw[b1 + l], m.iw[b2 + l], e.fac);
-        const double prof = gaussian(iw, freq - m.line[l]);
+        const double prof = gaussian(iw, dsub_rn(freq, m.line[l]));
         eta = prof * interpolate_log(m.em[b1 + l], m.em[b2 + l], e.fac);
         chi = prof * interpolate_log(m.op[b1 + l], m.op[b2 + l], e.fac) + m.min_opacity;
         return;
@@ -685,10 +690,10 @@ MGR_HD void eta_chi_fp64(const DevModel& m, const double* sl, const LaneCtx& c, 
         double diff;
         if (AP == APPROX_CLOSELINES) {
             l = m.sorted_map[s];
-            diff = freq - sl[s];
+            diff = dsub_rn(freq, sl[s]);
         } else {
             l = s;
-            diff = freq - m.line[l];
+            diff = dsub_rn(freq, m.line[l]);
         }
         const double iw = interpolate_linear(m.iw[b1 + l], m.iw[b2 + l], e.fac);
         const double prof = gaussian(iw, diff);
@@ -709,11 +714,11 @@ MGR_HD double dtau_single_line_fp64(const DevModel& m, const Elem& lo, const Ele
     const double cop = interpolate_log(m.op[c1 + l], m.op[c2 + l], lo.fac);
     const double nop = interpolate_log(m.op[n1 + l], m.op[n2 + l], hi.fac);
     if (cf == nf) {
-        const double prof = gaussian(avg_iw, cf - m.line[l]);
+        const double prof = gaussian(avg_iw, dsub_rn(cf, m.line[l]));
         return dz * (prof * ((cop + nop) / 2.0) + m.min_opacity);
     }
-    const double next_pos = (linefreq - nf) * avg_iw;
-    const double curr_pos = (linefreq - cf) * avg_iw;
+    const double next_pos = dmul_rn(dsub_rn(linefreq, nf), avg_iw);
+    const double curr_pos = dmul_rn(dsub_rn(linefreq, cf), avg_iw);
     const double diff_pos = next_pos - curr_pos;
     const double average_opacity = (nop + cop) / 2.0;
     // The reference subtracts two single-precision erff values (solver.tpp:2450).
@@ -731,8 +736,8 @@ template <int AP>
 MGR_HD void pair_li_fp64(const DevModel& m, const double* sl, const LaneCtx& c, const Elem& lo,
                                              const Elem& hi, double dz, double& out_dtau, double& out_Slo,
                                              double& out_Shi) {
-    const double cf = c.freq * lo.shift;
-    const double nf = c.freq * hi.shift;
+    const double cf = dmul_rn(c.freq, lo.shift);
+    const double nf = dmul_rn(c.freq, hi.shift);
     const size_t c1 = (size_t)lo.nr * m.L, c2 = (size_t)lo.ni * m.L;
     const size_t n1 = (size_t)hi.nr * m.L, n2 = (size_t)hi.ni * m.L;
     if (AP == APPROX_ONELINE) {
