@@ -321,7 +321,32 @@ def run_ali(args):
            "phases": phases, "setup_s": setup_s}
     if not args.no_parity:
         out["parity"] = ali_parity(args)
+    if not args.no_cpu_baseline:
+        out["cpu_formal_solve"] = ali_cpu_formal_solve(raw)
     return out
+
+
+def ali_cpu_formal_solve(raw, target_solves=6.0e6):
+    """The formal solve that dominates each ALI iteration, timed on the host cores: the
+    oracle port of the reference's formal solve (glibc erff, all threads) on every
+    k-th origin of the same non-LTE model (LTE line data, every ray pair and frequency),
+    k chosen for about ``target_solves`` solves."""
+    import numpy as np
+    oracle = _oracle()
+    a = oracle.reference_setup(raw)
+    orc = oracle.Oracle(a)
+    per_origin = a["hnrays"] * a["nfreqs"]
+    stride = max(1, int(a["npoints"] * per_origin / target_solves))
+    origins = np.arange(0, a["npoints"], stride, dtype=np.uint32)
+    nthreads = os.cpu_count() or 1
+    oracle.set_erf_mode(0)
+    t0 = time.perf_counter()
+    orc.formal_solve_fo2_origins(origins, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    solves = len(origins) * per_origin
+    return {"solves_per_s": solves / dt, "cores": nthreads, "kind": "port",
+            "sample": f"every {stride}th origin ({len(origins)}) x all ray pairs x all frequencies ({solves} "
+                      f"solves), {dt:.2f} s"}
 
 
 class _Handle:

@@ -332,7 +332,7 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
     const size_t ET = dm.sph ? 3 * (size_t)P : E;
 
     // host-side derived tables
-    std::vector<double4_32a> pos4(P), vel4(P), edge(E ? E : 1);
+    std::vector<double4_32a> pos4(P), vel4(P);
     double maxabs = 0.0;
     for (uint32_t p = 0; p < P; p++) {
         pos4[p] = make_double4_32a(d->position[3 * p], d->position[3 * p + 1], d->position[3 * p + 2], 0.0);
@@ -350,13 +350,14 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         const double* v = d->ray_direction + 3 * i;
         unit_rays = std::fabs(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] - 1.0) <= 2.0e-15;
     }
-    for (size_t i = 0; i < E; i++) {
-        const uint32_t n = d->neighbors[i];
-        long long bits = (long long)n;
-        double w;
-        std::memcpy(&w, &bits, sizeof(w));
-        edge[i] = make_double4_32a(d->position[3 * n], d->position[3 * n + 1], d->position[3 * n + 2], w);
-    }
+    // the neighbour records (position + index) are packed on the device from the points
+    // and the CSR lists: check the indices here
+    for (size_t i = 0; i < E; i++)
+        if (d->neighbors[i] >= P) {
+            mgr_model_free(m);
+            set_error("mgr_model_create: neighbour index out of range");
+            return MGR_ERR_ARGUMENT;
+        }
     std::vector<double> ub(P);
     for (uint32_t p = 0; p < P; p++)
         ub[p] = std::sqrt(TWO_KB_OVER_AMU_CC_SQUARED * d->max_inverse_mass * d->temperature[p] + d->vturb2[p]);
@@ -390,7 +391,14 @@ int mgr_model_create(const MgrModelDesc* d, MgrModel** out) {
         if ((e = upload(m, &dm.vel, vel4.data(), P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.n_nb, d->n_neighbors, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.cum_nb, d->cum_n_neighbors, P)) != cudaSuccess) break;
-        if ((e = upload(m, &dm.edge, edge.data(), E ? E : 1)) != cudaSuccess) break;
+        {
+            const uint32_t* nbr = nullptr;
+            double4_32a* edge = nullptr;
+            if ((e = upload(m, &nbr, d->neighbors, E)) != cudaSuccess) break;
+            if ((e = dalloc(m, &edge, E ? E : 1)) != cudaSuccess) break;
+            if ((e = launch_edge_pack(m, dm.pos, nbr, E, edge)) != cudaSuccess) break;
+            dm.edge = edge;
+        }
         if ((e = upload(m, &dm.p2b, d->point2boundary, P)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bc, d->boundary_condition, d->nboundary)) != cudaSuccess) break;
         if ((e = upload(m, &dm.bt, d->boundary_temperature, d->nboundary)) != cudaSuccess) break;

@@ -50,6 +50,30 @@ cudaError_t fill_erf_band(float* table, cudaStream_t stream, int sm_count) {
 }
 
 // ---------------------------------------------------------------------------------
+// Neighbour records: edge[i] = position of neighbour nbr[i] with its index in the bits
+// of w (one 32-byte load per neighbour in the trace), packed from the uploaded points.
+// ---------------------------------------------------------------------------------
+__global__ void edge_pack_kernel(const double4_32a* __restrict__ pos, const uint32_t* __restrict__ nbr, uint64_t E,
+                                 double4_32a* __restrict__ edge) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < E; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t n = nbr[i];
+        double4_32a e = pos[n];
+        e.w = __longlong_as_double((long long)n);
+        edge[i] = e;
+    }
+}
+
+cudaError_t launch_edge_pack(MgrModel* model, const double4_32a* pos, const uint32_t* nbr, uint64_t E,
+                             double4_32a* edge) {
+    if (E == 0) return cudaSuccess;
+    uint64_t blocks = (E + 255) / 256;
+    if (blocks > (uint64_t)model->sm_count * 16) blocks = (uint64_t)model->sm_count * 16;
+    count_launch();
+    edge_pack_kernel<<<(unsigned)blocks, 256, 0, model->stream>>>(pos, nbr, E, edge);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
 // Hi/lo float copies of the neighbour records and points for the trace's FP32
 // next-point filter (DevModel::edge_hl, pos_hl), positions scaled by pos_scale.
 // ---------------------------------------------------------------------------------

@@ -176,6 +176,8 @@ cudaError_t launch_ray_stats(MgrModel* model, unsigned long long* d_stats);
 cudaError_t launch_trace_check(MgrModel* model, unsigned long long* d_stats);
 cudaError_t launch_nint_table(MgrModel* model);
 cudaError_t launch_hl_tables(MgrModel* model);  // trace filter tables (edge_hl, pos_hl)
+cudaError_t launch_edge_pack(MgrModel* model, const double4_32a* pos, const uint32_t* nbr, uint64_t E,
+                             double4_32a* edge);
 // Fills the correctly rounded erff table (kErfBandCount floats) on `stream`.
 cudaError_t fill_erf_band(float* table, cudaStream_t stream, int sm_count);
 // The current device's erff table, created (cudaMalloc, one fill launch, synchronised)
