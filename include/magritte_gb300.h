@@ -397,10 +397,12 @@ int mgr_formal_solve_fo2_adjoint_device(MgrModel* model, const uint32_t* origins
 /* ---- Many-model batch ------------------------------------------------------------
  * No single reference counterpart: the reference solves one Model per call
  * (Model::compute_radiation_field_feautrier_order_2, src/model/model.cpp:353-390);
- * a batch runs that call for many independent models in one persistent kernel
- * launch.  Each model's J and ALO diagonal equal those of its own
- * mgr_formal_solve_fo2 (same lane code, same order of the sums; in FP64 mode up to a
- * differently contracted multiply-add, a few ulp). */
+ * a batch runs that call for many independent models with one persistent solve launch
+ * and one reduction launch per wave of models (consecutive models whose staged per-ray
+ * results fit the batch's staging area of up to 2 x 4 GiB; one wave for most batches).
+ * Each model's J and ALO diagonal equal those of its own mgr_formal_solve_fo2 (same
+ * lane code, same order of the sums; in FP64 mode up to a differently contracted
+ * multiply-add). */
 typedef struct MgrBatch MgrBatch;
 
 /* Collects n_models models (same device, same line approximation, line spectral
@@ -425,8 +427,8 @@ int mgr_batch_formal_solve_fo2_device(MgrBatch* batch, int precision, double* co
 int mgr_batch_formal_solve_fo2(MgrBatch* batch, int precision, double* const* J, double* const* lambda_diag);
 
 /* Per-model timing of the last batch solve from the GPU's global timer, in ms since
- * the first CTA of the launch started: when the model's first origin started and
- * when its last origin finished.  Blocks until the solve is done. */
+ * the first CTA of the solve started: when the model's first ray pair started and
+ * when its last origin was reduced.  Blocks until the solve is done. */
 int mgr_batch_timings(MgrBatch* batch, double* start_ms, double* finish_ms);
 
 /* The batch's CUDA stream (cudaStream_t). */

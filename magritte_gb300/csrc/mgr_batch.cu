@@ -1,25 +1,26 @@
-// Many-model batch of second-order Feautrier formal solves in one persistent launch.
+// Many-model batch of second-order Feautrier formal solves.
 //
 // Each model is an ordinary MgrModel (mgr_model_create); a batch collects their device
-// descriptions into one device array and solves all of them with one kernel launch.
-// The unit of work is one (model, origin) item handled by one warp: the warp traces
-// and solves every ray pair of its origin in turn (lanes over frequencies, the same
-// solve_lane code as the single-model kernel) and keeps J and the ALO elements of the
-// origin in shared memory per frequency, summed over the ray pairs in order
-// (Solver::solve_feautrier_order_2, solver.tpp:476-540, and update_Lambda,
-// solver.tpp:1760-1850); each line's ALO diagonal is then the sum of its quadrature
-// points' sums across the lanes, the association fo2_reduce_kernel uses.  Every
-// model's J and ALO diagonal are therefore the values its own mgr_formal_solve_fo2
-// returns, bit for bit, with no staging of per-ray results in HBM.
-//
-// Items are ordered model by model; warps take them in a grid-stride loop over a
-// persistent grid, so models finish roughly in submission order.  Per model the
-// kernel records, from the GPU's global timer, when its origin 0 started (origins
-// start in order) and when its last origin finished (the per-model latency).
+// descriptions into one device array.  The models are solved in waves: consecutive
+// models whose staged per-ray results fit the batch's staging area (a few GiB; one
+// wave for most batches) are solved by one persistent launch of fo2_multi_kernel and
+// one launch of fo2_multi_reduce_kernel.
+//   * fo2_multi_kernel: one warp per (model, origin, ray pair) item, lanes over
+//     frequencies, the same trace and solve_lane code as the single-model fo2_kernel;
+//     u and L_diag go to the model's slice of the staging area.  Items are ordered
+//     model by model, origin by origin, and taken in a grid-stride loop, so short and
+//     long rays and small and large models mix on every SM.
+//   * fo2_multi_reduce_kernel: one CTA per (model, origin), the single-model
+//     reduction's per-origin code (mgr_reduce.cuh): J and the ALO diagonal in the same
+//     order as the model's own mgr_formal_solve_fo2, so every model's results are its
+//     own solve's (bit for bit in split precision).
+// Per model the kernels record, from the GPU's global timer, when its first item
+// started and when its last origin was reduced (the per-model latency).
 #include <algorithm>
 #include <vector>
 
 #include "mgr_internal.h"
+#include "mgr_reduce.cuh"
 #include "mgr_solve.cuh"
 
 struct MgrBatch {
@@ -31,18 +32,28 @@ struct MgrBatch {
     uint32_t F_max = 1, L_max = 1;
     uint64_t n_items = 0;   // total origins
     mgr::DevModel* d_models = nullptr;     // [n]
-    uint64_t* d_offsets = nullptr;         // [n + 1] first item of each model
+    uint64_t* d_offsets = nullptr;         // [n + 1] first origin of each model (cumulative P)
+    uint64_t* d_item_off = nullptr;        // [n + 1] first (origin, ray pair) item of each model
+    uint64_t* d_stage_off = nullptr;       // [n + 1] first staging entry of each model (cumulative P R F)
+    std::vector<uint64_t> item_off, stage_off, origin_off;  // host copies
+    double* stage_u = nullptr;             // staging of u for one wave
+    double* stage_ld = nullptr;            // staging of L_diag for one wave
+    uint64_t stage_entries = 0;            // entries of each staging area
     double** d_J = nullptr;                // [n] output pointers
     double** d_lam = nullptr;              // [n]
     unsigned long long* d_t = nullptr;     // [n][2] first-start / last-finish ns, [2n] batch start
-    uint32_t* d_done = nullptr;            // [n] finished items per model
+    uint32_t* d_done = nullptr;            // [n] reduced origins per model
     int* status = nullptr;
     mgr::DevModel* h_models = nullptr;     // pinned staging of the device descriptions
     int warps = 8;
-    int minb = 2;
+    int minb = 4;
 };
 
 namespace mgr {
+
+// Staged u (and L_diag) entries of one wave at most: 512 Mi doubles (4 GiB each) or,
+// when larger, the biggest single model.
+constexpr uint64_t kBatchStageEntries = uint64_t(1) << 29;
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -50,130 +61,143 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Per-warp shared memory: the current model's DevModel, sorted line centres [L_max],
-// J accumulators [F_max], ALO accumulators per frequency [F_max], the origin's
-// ray-independent ALO factors [F_max] (LambdaFactors), then the two trace halves.
-// The single-model kernels take their DevModel as a kernel parameter, whose fields the
-// instructions read from the constant bank; a batch kernel indexes its models at run
-// time, and reading each field from the descriptor array in global memory put a
-// dependent global load in front of every table access and kept the loaded pointers
-// live in registers (spills).  The warp copies its model's descriptor into shared
-// memory when the model changes.
-constexpr size_t kDescBytes = (sizeof(DevModel) + 15) & ~size_t(15);
-__host__ __device__ inline size_t batch_head_bytes(uint32_t F_max, uint32_t L_max) {
-    const size_t head =
-        kDescBytes + ((size_t)L_max + 2 * (size_t)F_max) * 8 + (size_t)F_max * sizeof(LambdaFactors);
-    return (head + 15) & ~size_t(15);
-}
-__host__ __device__ inline size_t batch_warp_bytes(uint32_t cap, uint32_t F_max, uint32_t L_max) {
-    return batch_head_bytes(F_max, L_max) + half_bytes_per_warp(cap);
+// The model of index i (an item or an origin) among models [m0, m1): offsets ascending.
+__device__ __forceinline__ uint32_t model_of(const uint64_t* __restrict__ off, uint32_t m0, uint32_t m1, uint64_t i) {
+    uint32_t lo = m0, hi = m1;  // off[lo] <= i < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
+// Per-warp shared memory of fo2_multi_kernel: the current model's DevModel and sorted
+// line centres, then the two trace halves.  The single-model kernels take their
+// DevModel as a kernel parameter, whose fields the instructions read from the constant
+// bank; a batch kernel indexes its models at run time.  Read from the descriptor array
+// in global memory, every table access waited on a dependent global load and the loaded
+// pointers stayed live in registers; the warp copies its model's descriptor into shared
+// memory when the model changes (measured faster than passing the wave's descriptors
+// as a kernel parameter indexed by the model: 160 against 153 M solves/s).
+constexpr size_t kDescBytes = (sizeof(DevModel) + 15) & ~size_t(15);
+__host__ __device__ inline size_t batch_head_bytes(uint32_t L_max) {
+    return (kDescBytes + (size_t)L_max * 8 + 15) & ~size_t(15);
+}
+__host__ __device__ inline size_t batch_warp_bytes(uint32_t cap, uint32_t L_max) {
+    return batch_head_bytes(L_max) + half_bytes_per_warp(cap);
+}
+
+__device__ __forceinline__ void copy_desc(const DevModel* __restrict__ src, DevModel* dst, int t, int nt) {
+    static_assert(sizeof(DevModel) % 8 == 0, "DevModel copied in 8-byte words");
+    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(dst);
+    for (uint32_t i = (uint32_t)t; i < sizeof(DevModel) / 8; i += (uint32_t)nt) d[i] = s[i];
+}
+
+// Stage 1 of models [m0, m1): u (and L_diag) of every (model, origin, ray pair) item.
 template <int MODE, int AP, int MINB>
 __global__ void __launch_bounds__(256, MINB)
-    fo2_batch_kernel(const DevModel* __restrict__ models, const uint64_t* __restrict__ offsets, uint32_t n_models,
-                     uint32_t cap, uint32_t F_max, uint32_t L_max, double* const* __restrict__ Jout,
-                     double* const* __restrict__ Lout, unsigned long long* __restrict__ tstamp,
-                     uint32_t* __restrict__ done, int* status) {
+    fo2_multi_kernel(const DevModel* __restrict__ models, uint32_t m0, uint32_t m1,
+                     const uint64_t* __restrict__ item_off, const uint64_t* __restrict__ stage_off, uint32_t cap,
+                     uint32_t L_max, double* __restrict__ U, double* __restrict__ LD,
+                     unsigned long long* __restrict__ tstamp, uint32_t n_models, int* status) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nw = blockDim.x >> 5;
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    unsigned char* base = smem + (size_t)w * batch_warp_bytes(cap, F_max, L_max);
+    unsigned char* base = smem + (size_t)w * batch_warp_bytes(cap, L_max);
     DevModel* desc = reinterpret_cast<DevModel*>(base);
     double* sl = reinterpret_cast<double*>(base + kDescBytes);
-    double* Jacc = sl + L_max;
-    double* Lacc = Jacc + F_max;
-    LambdaFactors* LF = reinterpret_cast<LambdaFactors*>(Lacc + F_max);
     HalfSmem bk, fw;
-    carve_halves(base + batch_head_bytes(F_max, L_max), cap, bk, fw);
+    carve_halves(base + batch_head_bytes(L_max), cap, bk, fw);
     if (threadIdx.x == 0) atomicMin(&tstamp[2 * n_models], global_ns());
 
-    const uint64_t n_items = offsets[n_models];
+    const uint64_t i0 = item_off[m0], i1 = item_off[m1];
+    const uint64_t s0 = stage_off[m0];
     const uint64_t stride = (uint64_t)gridDim.x * nw;
-    uint32_t mi = 0, desc_mi = 0xffffffffu;
-    for (uint64_t item = (uint64_t)blockIdx.x * nw + w; item < n_items; item += stride) {
-        // model of this item: offsets is ascending and items only grow within a warp
-        while (offsets[mi + 1] <= item) mi++;
+    uint32_t mi = m0, desc_mi = 0xffffffffu;
+    for (uint64_t item = i0 + (uint64_t)blockIdx.x * nw + w; item < i1; item += stride) {
+        // the item's model: items only grow within a warp
+        while (item_off[mi + 1] <= item) mi++;
         if (mi != desc_mi) {
-            static_assert(sizeof(DevModel) % 8 == 0, "DevModel copied in 8-byte words");
-            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(models + mi);
-            unsigned long long* dst = reinterpret_cast<unsigned long long*>(desc);
-            for (uint32_t i = lane; i < sizeof(DevModel) / 8; i += 32) dst[i] = src[i];
+            copy_desc(models + mi, desc, lane, 32);
+            __syncwarp();
+            for (uint32_t i = lane; i < desc->L; i += 32) sl[i] = desc->sorted_line[i];
             desc_mi = mi;
             __syncwarp();
         }
         const DevModel& m = *desc;
-        const uint32_t o = (uint32_t)(item - offsets[mi]);
-        if (lane == 0 && o == 0) tstamp[2 * mi] = global_ns();  // origins start in order
-        for (uint32_t i = lane; i < m.L; i += 32) sl[i] = m.sorted_line[i];
-        for (uint32_t f = lane; f < m.F; f += 32) {
-            Jacc[f] = 0.0;
-            Lacc[f] = 0.0;
-        }
-        bool ok = true;
-        const bool want_lam = Lout[mi] != nullptr;
-        __syncwarp();
-        if (want_lam)  // ray-independent factors of the origin's ALO elements, once per origin
-            for (uint32_t f = lane; f < m.F; f += 32)
-                if (m.in_line[f]) LF[f] = lambda_factors(m, sl, o, f);
-        __syncwarp();
-        for (uint32_t rr = 0; rr < m.hnrays && ok; rr++) {
-            // general geometry with shared rays (mgr_batch_create refuses the other kinds)
-            int nb = 0, nf = 0;
-            trace_pair<true, 0, 0>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
-            if (nb < 0 || nf < 0) {  // status recorded by the trace
-                ok = false;
-                break;
+        const uint64_t k = item - item_off[mi];
+        const uint32_t o = (uint32_t)(k / m.hnrays);
+        const uint32_t rr = (uint32_t)(k % m.hnrays);
+        if (k == 0 && lane == 0) tstamp[2 * mi] = global_ns();
+        // general geometry with shared rays (mgr_batch_create refuses the other kinds)
+        int nb = 0, nf = 0;
+        trace_pair<true, 0, 0>(m, o, rr, m.antipod[rr], cap, bk, fw, lane, status, nb, nf);
+        if (nb < 0 || nf < 0) continue;  // status recorded by the trace
+        const size_t at = (size_t)(stage_off[mi] - s0) + ((size_t)rr * m.P + o) * m.F;
+        double* Ui = U + at;
+        double* Li = LD ? LD + at : nullptr;
+        for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
+            const uint32_t f = f0 + lane;
+            if (f < m.F) {
+                const LaneCtx c = lane_ctx(m, o, f);
+                const LaneResult r = solve_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
+                Ui[f] = r.u;
+                if (Li) Li[f] = r.solved ? r.Ldiag : 0.0;
+                if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
             }
-            const double w2 = ray_w(m, o, rr);
-            for (uint32_t f0 = 0; f0 < m.F; f0 += 32) {
-                const uint32_t f = f0 + lane;
-                if (f < m.F) {
-                    const LaneCtx c = lane_ctx(m, o, f);
-                    const LaneResult r = solve_lane<MODE, AP>(m, sl, c, bk, nb, fw, nf);
-                    Jacc[f] += r.u * 2.0 * w2;
-                    // the frequency's ALO elements over the ray pairs in order
-                    if (want_lam && r.solved && m.in_line[f]) Lacc[f] += lambda_element(LF[f], w2, r.Ldiag);
-                    if (!isfinite(r.u)) atomicOr(status, ST_NONFINITE);
-                }
-            }
-            __syncwarp();
-        }
-        if (ok) {
-            double* J = Jout[mi] + (size_t)o * m.F;
-            for (uint32_t f = lane; f < m.F; f += 32) J[f] = Jacc[f];
-            if (want_lam)
-                // line l: its quadrature points' sums, lane by lane, then across the lanes
-                // (fo2_reduce_kernel's association)
-                for (uint32_t l = 0; l < m.L; l++) {
-                    const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
-                    double s = 0.0;
-                    for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
-                        const uint32_t q = q0 + lane;
-                        const uint32_t f = q < m.Q ? l2f[q] : 0xffffffffu;
-                        if (f == 0xffffffffu || !m.in_line[f]) continue;
-                        s += Lacc[f];
-                    }
-#pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(FULL_MASK, s, off);
-                    if (lane == 0) Lout[mi][(size_t)o * m.L + l] = s;
-                }
         }
         __syncwarp();
-        if (lane == 0) {
+    }
+}
+
+// Stage 2 of models [m0, m1): J and the ALO diagonal of every (model, origin), one CTA
+// per origin, in the single-model reduction's order.  The CTA copies its model's
+// descriptor into shared memory when the model changes.
+__global__ void __launch_bounds__(128)
+    fo2_multi_reduce_kernel(const DevModel* __restrict__ models, uint32_t m0, uint32_t m1,
+                            const uint64_t* __restrict__ origin_off, const uint64_t* __restrict__ stage_off,
+                            const double* __restrict__ U, const double* __restrict__ LD,
+                            double* const* __restrict__ Jout, double* const* __restrict__ Lout,
+                            unsigned long long* __restrict__ tstamp, uint32_t* __restrict__ done) {
+    __shared__ __align__(16) unsigned char dbuf[kDescBytes];
+    DevModel* desc = reinterpret_cast<DevModel*>(dbuf);
+    const int nw = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint64_t g0 = origin_off[m0], g1 = origin_off[m1];
+    const uint64_t s0 = stage_off[m0];
+    uint32_t desc_mi = 0xffffffffu;
+    for (uint64_t g = g0 + blockIdx.x; g < g1; g += gridDim.x) {
+        const uint32_t mi = model_of(origin_off, m0, m1, g);
+        if (mi != desc_mi) {
+            __syncthreads();  // every thread is done with the previous model's descriptor
+            copy_desc(models + mi, desc, threadIdx.x, blockDim.x);
+            desc_mi = mi;
+            __syncthreads();
+        }
+        const DevModel& m = *desc;
+        const uint32_t o = (uint32_t)(g - origin_off[mi]);
+        const double* Um = U + (stage_off[mi] - s0);
+        const size_t stride = (size_t)m.P * m.F;
+        reduce_J_origin(m, o, 0, m.hnrays, Um, stride, 0, Jout[mi], threadIdx.x, blockDim.x);
+        if (LD && Lout[mi])
+            reduce_lam_origin(m, o, 0, m.hnrays, LD + (stage_off[mi] - s0), stride, 0, Lout[mi], w, nw, lane);
+        __syncthreads();
+        if (threadIdx.x == 0) {
             __threadfence();
-            const uint32_t P = m.P;
-            if (atomicAdd(&done[mi], 1u) + 1 == P) tstamp[2 * mi + 1] = global_ns();
+            if (atomicAdd(&done[mi], 1u) + 1 == m.P) tstamp[2 * mi + 1] = global_ns();
         }
     }
 }
 
 template <int MODE, int AP, int MINB>
-static cudaError_t launch_batch_variant(MgrBatch* b) {
+static cudaError_t launch_multi_variant(MgrBatch* b, uint32_t m0, uint32_t m1, bool want_lam) {
     const int nw = b->warps;
-    const size_t smem = (size_t)nw * batch_warp_bytes(b->cap, b->F_max, b->L_max);
-    auto kern = fo2_batch_kernel<MODE, AP, MINB>;
+    const size_t smem = (size_t)nw * batch_warp_bytes(b->cap, b->L_max);
+    auto kern = fo2_multi_kernel<MODE, AP, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -182,30 +206,58 @@ static cudaError_t launch_batch_variant(MgrBatch* b) {
     if (per_sm < 1) return cudaErrorInvalidConfiguration;  // the per-warp buffers do not fit
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    const uint64_t items = b->item_off[m1] - b->item_off[m0];
     uint64_t grid = (uint64_t)sms * per_sm;
-    const uint64_t need = (b->n_items + nw - 1) / nw;
+    const uint64_t need = (items + nw - 1) / nw;
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
+    const uint32_t n = (uint32_t)b->models.size();
     count_launch();
-    kern<<<(unsigned)grid, nw * 32, smem, b->stream>>>(b->d_models, b->d_offsets, (uint32_t)b->models.size(), b->cap,
-                                                       b->F_max, b->L_max, b->d_J, b->d_lam, b->d_t, b->d_done,
-                                                       b->status);
+    kern<<<(unsigned)grid, nw * 32, smem, b->stream>>>(b->d_models, m0, m1, b->d_item_off, b->d_stage_off, b->cap,
+                                                       b->L_max, b->stage_u, want_lam ? b->stage_ld : nullptr,
+                                                       b->d_t, n, b->status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const uint64_t origins = b->origin_off[m1] - b->origin_off[m0];
+    uint64_t rgrid = (uint64_t)sms * 16;
+    if (rgrid > origins) rgrid = origins;
+    if (rgrid < 1) rgrid = 1;
+    count_launch();
+    fo2_multi_reduce_kernel<<<(unsigned)rgrid, 128, 0, b->stream>>>(b->d_models, m0, m1, b->d_offsets,
+                                                                    b->d_stage_off, b->stage_u,
+                                                                    want_lam ? b->stage_ld : nullptr, b->d_J,
+                                                                    b->d_lam, b->d_t, b->d_done);
     return cudaGetLastError();
 }
 
+// Every wave of the batch: consecutive models whose staging fits the staging area.
+template <int MODE, int AP, int MINB>
+static cudaError_t launch_batch_variant(MgrBatch* b, bool want_lam) {
+    const uint32_t n = (uint32_t)b->models.size();
+    uint32_t m0 = 0;
+    while (m0 < n) {
+        uint32_t m1 = m0 + 1;
+        while (m1 < n && b->stage_off[m1 + 1] - b->stage_off[m0] <= b->stage_entries) m1++;
+        cudaError_t e = launch_multi_variant<MODE, AP, MINB>(b, m0, m1, want_lam);
+        if (e != cudaSuccess) return e;
+        m0 = m1;
+    }
+    return cudaSuccess;
+}
+
 template <int MODE, int AP>
-static cudaError_t launch_batch_minb(MgrBatch* b) {
-    if (b->minb == 3) return launch_batch_variant<MODE, AP, 3>(b);
-    if (b->minb == 4) return launch_batch_variant<MODE, AP, 4>(b);
-    return launch_batch_variant<MODE, AP, 2>(b);
+static cudaError_t launch_batch_minb(MgrBatch* b, bool want_lam) {
+    if (b->minb == 3) return launch_batch_variant<MODE, AP, 3>(b, want_lam);
+    if (b->minb == 2) return launch_batch_variant<MODE, AP, 2>(b, want_lam);
+    return launch_batch_variant<MODE, AP, 4>(b, want_lam);
 }
 
 template <int MODE>
-static cudaError_t launch_batch_approx(MgrBatch* b) {
+static cudaError_t launch_batch_approx(MgrBatch* b, bool want_lam) {
     switch (b->approx) {
-        case APPROX_ONELINE: return launch_batch_minb<MODE, APPROX_ONELINE>(b);
-        case APPROX_CLOSELINES: return launch_batch_minb<MODE, APPROX_CLOSELINES>(b);
-        default: return launch_batch_minb<MODE, APPROX_NONE>(b);
+        case APPROX_ONELINE: return launch_batch_minb<MODE, APPROX_ONELINE>(b, want_lam);
+        case APPROX_CLOSELINES: return launch_batch_minb<MODE, APPROX_CLOSELINES>(b, want_lam);
+        default: return launch_batch_minb<MODE, APPROX_NONE>(b, want_lam);
     }
 }
 
@@ -214,6 +266,10 @@ static void batch_release(MgrBatch* b) {
     DeviceScope on_device(b->device);
     cudaFree(b->d_models);
     cudaFree(b->d_offsets);
+    cudaFree(b->d_item_off);
+    cudaFree(b->d_stage_off);
+    cudaFree(b->stage_u);
+    cudaFree(b->stage_ld);
     cudaFree(b->d_J);
     cudaFree(b->d_lam);
     cudaFree(b->d_t);
@@ -259,7 +315,8 @@ int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out)
     *out = nullptr;
     auto* b = new MgrBatch();
     b->models.assign(models, models + n_models);
-    std::vector<uint64_t> offsets(n_models + 1, 0);
+    std::vector<uint64_t> offsets(n_models + 1, 0), item_off(n_models + 1, 0), stage_off(n_models + 1, 0);
+    uint64_t largest = 1;
     for (uint32_t i = 0; i < n_models; i++) {
         MgrModel* m = models[i];
         if (!m) {
@@ -292,13 +349,25 @@ int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out)
         b->F_max = std::max(b->F_max, m->dm.F);
         b->L_max = std::max(b->L_max, m->dm.L);
         offsets[i + 1] = offsets[i] + m->dm.P;
+        item_off[i + 1] = item_off[i] + (uint64_t)m->dm.P * m->dm.hnrays;
+        const uint64_t entries = (uint64_t)m->dm.P * m->dm.hnrays * m->dm.F;
+        stage_off[i + 1] = stage_off[i] + entries;
+        largest = std::max(largest, entries);
     }
     b->n_items = offsets[n_models];
+    b->origin_off = offsets;
+    b->item_off = item_off;
+    b->stage_off = stage_off;
+    b->stage_entries = std::min(stage_off[n_models], std::max(kBatchStageEntries, largest));
     DeviceScope on_device(b->device);
     cudaError_t e = on_device.error();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_models, n_models * sizeof(DevModel));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_offsets, (n_models + 1) * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_item_off, (n_models + 1) * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_stage_off, (n_models + 1) * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->stage_u, b->stage_entries * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&b->stage_ld, b->stage_entries * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_J, n_models * sizeof(double*));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_lam, n_models * sizeof(double*));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_t, (2 * n_models + 1) * sizeof(unsigned long long));
@@ -307,12 +376,16 @@ int mgr_batch_create(MgrModel* const* models, uint32_t n_models, MgrBatch** out)
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_models, n_models * sizeof(DevModel));
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_offsets, offsets.data(), (n_models + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_item_off, item_off.data(), (n_models + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_stage_off, stage_off.data(), (n_models + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->status, 0, sizeof(int));
     if (e != cudaSuccess) {
         batch_release(b);
         return cuda_fail(e, "batch set-up");
     }
-    const size_t per_warp = batch_warp_bytes(b->cap, b->F_max, b->L_max);
+    const size_t per_warp = batch_warp_bytes(b->cap, b->L_max);
     int max_smem = 0;
     cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
     while (b->warps > 1 && (size_t)b->warps * per_warp > (size_t)max_smem) b->warps /= 2;
@@ -344,7 +417,7 @@ int mgr_batch_set_tuning(MgrBatch* batch, int min_blocks_per_sm, int warps_per_b
     if (warps_per_block) {
         int max_smem = 0;
         cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, batch->device);
-        if ((size_t)warps_per_block * batch_warp_bytes(batch->cap, batch->F_max, batch->L_max) > (size_t)max_smem) {
+        if ((size_t)warps_per_block * batch_warp_bytes(batch->cap, batch->L_max) > (size_t)max_smem) {
             set_error("mgr_batch_set_tuning: that many warps do not fit in shared memory");
             return MGR_ERR_CAPACITY;
         }
@@ -367,12 +440,14 @@ int mgr_batch_formal_solve_fo2_device(MgrBatch* batch, int precision, double* co
     }
     const size_t n = batch->models.size();
     std::vector<double*> lam(n, nullptr);
+    bool want_lam = false;
     for (size_t i = 0; i < n; i++) {
         if (!J_dev[i]) {
             set_error("mgr_batch_formal_solve_fo2_device: null J pointer for model " + std::to_string(i));
             return MGR_ERR_ARGUMENT;
         }
         if (lambda_diag_dev) lam[i] = lambda_diag_dev[i];
+        want_lam = want_lam || lam[i] != nullptr;
     }
     cudaError_t e = batch_sync_models(batch);
     if (e == cudaSuccess)
@@ -385,8 +460,8 @@ int mgr_batch_formal_solve_fo2_device(MgrBatch* batch, int precision, double* co
     // the host vectors above are read by the copies: wait for them before returning
     if (e == cudaSuccess) e = cudaStreamSynchronize(batch->stream);
     if (e == cudaSuccess)
-        e = (precision == MGR_PRECISION_SPLIT) ? launch_batch_approx<MODE_SPLIT>(batch)
-                                               : launch_batch_approx<MODE_FP64>(batch);
+        e = (precision == MGR_PRECISION_SPLIT) ? launch_batch_approx<MODE_SPLIT>(batch, want_lam)
+                                               : launch_batch_approx<MODE_FP64>(batch, want_lam);
     if (e != cudaSuccess) return cuda_fail(e, "batch formal solve launch");
     return MGR_OK;
 }

@@ -1,5 +1,6 @@
 // Kernels of the formal-solve path and their launchers.
 #include "mgr_internal.h"
+#include "mgr_reduce.cuh"
 #include "mgr_solve.cuh"
 
 namespace mgr {
@@ -385,12 +386,6 @@ __global__ void __launch_bounds__(256, 2)
 // is rr outer, q inner, a different association of the same terms).
 // lq2f[l * Q + q] is the frequency of (l, q).
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL_MASK, v, off);
-    return v;
-}
-
 __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_begin, uint32_t o_end,
                                                          uint32_t rr0, uint32_t nR,
                                                          const double* __restrict__ U, size_t u_stride, uint32_t u_o0,
@@ -402,14 +397,7 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     for (uint32_t o = o_begin + blockIdx.x; o < o_end; o += gridDim.x) {
-        if (J) {
-            for (uint32_t f = threadIdx.x; f < m.F; f += blockDim.x) {
-                const double* Uo = U + (size_t)(o - u_o0) * m.F + f;
-                double s = 0.0;
-                for (uint32_t k = 0; k < nR; k++) s += Uo[(size_t)k * u_stride] * 2.0 * ray_w(m, o, rr0 + k);
-                J[(size_t)o * m.F + f] = s;
-            }
-        }
+        if (J) reduce_J_origin(m, o, rr0, nR, U, u_stride, u_o0, J, threadIdx.x, blockDim.x);
         if (Jlin) {
             // line-integrated J of the memory-lean solve (solve_feautrier_order_2_sparse,
             // solver.tpp:297-363): J(o, l) = sum of w_z (2 w_rr) u over (rr, z)
@@ -481,26 +469,7 @@ __global__ void __launch_bounds__(128) fo2_reduce_kernel(DevModel m, uint32_t o_
                 }
             }
         }
-        if (!lam) continue;
-        for (uint32_t l = w; l < m.L; l += nw) {
-            // lane q: the ray-independent factors of quadrature point q, then its elements
-            // over the ray pairs in order
-            const uint32_t* l2f = m.lq2f + (size_t)l * m.Q;
-            double s = 0.0;
-            for (uint32_t q0 = 0; q0 < m.Q; q0 += 32) {
-                const uint32_t q = q0 + lane;
-                const uint32_t f = q < m.Q ? l2f[q] : 0xffffffffu;
-                if (f == 0xffffffffu || !m.in_line[f]) continue;
-                const LambdaFactors k = lambda_factors(m, m.sorted_line, o, f);
-                double part = 0.0;
-                for (uint32_t rr = rr0; rr < rr0 + nR; rr++)
-                    part += lambda_element(k, ray_w(m, o, rr),
-                                           LD[(size_t)(rr - rr0) * ld_stride + (size_t)(o - ld_o0) * m.F + f]);
-                s += part;
-            }
-            s = warp_sum(s);
-            if (lane == 0) lam[(size_t)o * m.L + l] = s;
-        }
+        if (lam) reduce_lam_origin(m, o, rr0, nR, LD, ld_stride, ld_o0, lam, w, nw, lane);
     }
 }
 
