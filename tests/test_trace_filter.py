@@ -27,8 +27,27 @@ def emu():
     return lib
 
 
+def _lattice_rays(raw):
+    """The 13 lattice directions of the 26-neighbour grid and their antipodes as rays:
+    every step has neighbours placed symmetrically about the ray, so the reference's
+    argmin is decided by FP64 rounding between exact ties, which the filter must leave
+    to the exact argmin."""
+    import dataclasses
+    dirs = []
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                v = (dx, dy, dz)
+                if v != (0, 0, 0) and v > (0, 0, 0):
+                    dirs.append(np.array(v, float) / np.linalg.norm(v))
+    d = np.array(dirs + [-x for x in dirs])
+    return dataclasses.replace(raw, ray_direction=d, ray_weight=np.full(len(d), 1.0 / len(d)))
+
+
 MODELS = {
     "cube12": lambda: S.grid_cube(n=12, nquads=3),
+    "cube10_lattice_rays": lambda: _lattice_rays(S.grid_cube(n=10, nquads=3)),
+    "delaunay_nside4": lambda: S.nlte_sphere(npoints=2000, nside=4, nlev=2, nquads=3),
     "cube10_nside2": lambda: S.grid_cube(n=10, nside=2, nquads=3, seed=3),
     "sphere20_nside2": lambda: S.grid_sphere(n=20, nside=2, nquads=3, nlev=2),
     "delaunay_sphere": lambda: S.nlte_sphere(npoints=3000, nside=2, nlev=2, nquads=3),
